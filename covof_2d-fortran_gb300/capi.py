@@ -1,0 +1,145 @@
+"""ctypes mirror of include/covof_gpu.h.
+
+Loads the in-tree libcovof_gpu.so.  There is no CPU fallback: if the library
+is missing or cannot be loaded, importing the package raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_build" / "libcovof_gpu.so"
+
+# status codes (include/covof_gpu.h)
+OK, MAXITER, BREAKDOWN, NAN, TIMEOUT, UNSUPPORTED, CUDA_ERROR, INVALID = range(8)
+STATUS_NAMES = {0: "OK", 1: "MAXITER", 2: "BREAKDOWN", 3: "NAN", 4: "TIMEOUT",
+                5: "UNSUPPORTED", 6: "CUDA_ERROR", 7: "INVALID"}
+# codes shared with src/module_constants.f90
+BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC, BC_FREESLIP = 1, 2, 3, 4
+LINEAR_BICGSTAB2, LINEAR_BICGSTAB, LINEAR_CG = 1, 2, 3
+PRECOND_NONE, PRECOND_JACOBI, PRECOND_SSOR, PRECOND_ILU0 = 0, 1, 2, 3
+CONV_UPWIND, CONV_CENTERED = 1, 2
+RECON_PLIC, RECON_ELVIRA = 0, 1
+GAUGE_REFERENCE, GAUGE_PINNED = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+
+class Params(C.Structure):
+    """covof_params (include/covof_gpu.h)."""
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("dx", C.c_double), ("dy", C.c_double),
+        ("bc_type", C.c_int * 4), ("bc_u", C.c_double * 4), ("bc_v", C.c_double * 4),
+        ("linear_solver", C.c_int), ("precond", C.c_int), ("use_precond", C.c_int),
+        ("max_iter", C.c_int), ("tol", C.c_double),
+        ("enable_convection", C.c_int), ("convective_scheme", C.c_int),
+        ("p_precond", C.c_int), ("p_max_iter", C.c_int), ("p_gauge", C.c_int),
+        ("p_precision", C.c_int), ("p_tol", C.c_double), ("p_inner_tol", C.c_double),
+        ("p_inner_max_iter", C.c_int), ("p_max_refine", C.c_int),
+        ("enable_two_phase", C.c_int), ("enable_surface_tension", C.c_int),
+        ("rho1", C.c_double), ("rho2", C.c_double), ("mu1", C.c_double), ("mu2", C.c_double),
+        ("sigma", C.c_double), ("gx", C.c_double), ("gy", C.c_double),
+        ("recon", C.c_int),
+    ]
+
+    def copy(self) -> "Params":
+        p = Params()
+        C.memmove(C.byref(p), C.byref(self), C.sizeof(Params))
+        return p
+
+    def as_dict(self) -> dict:
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+
+class CovofError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)} ({describe(status)})")
+
+
+_lib = None
+_DP = C.POINTER(C.c_double)
+_VP = C.c_void_p
+_IP = C.POINTER(C.c_int)
+
+# name -> argument types; every function returns int except where noted
+_SIGS = {
+    "covof_create": [C.POINTER(Params), C.POINTER(C.c_void_p)],
+    "covof_destroy": [_VP],
+    "covof_abi_version": [],
+    "covof_device_info": [_VP, _IP, _IP],
+    "covof_get_stream": [_VP, C.POINTER(C.c_void_p)],
+    "covof_last_solve_ms": [_VP, _DP],
+    "covof_last_refine_steps": [_VP, _IP],
+    "covof_get_vof_step_count": [_VP, _IP],
+    "covof_set_vof_step_count": [_VP, C.c_int],
+    "covof_sp_step": [_VP, C.c_double] + [_VP] * 11 + [_IP, _DP],
+    "covof_sp_step_dev": [_VP, C.c_double] + [_VP] * 11 + [_IP, _DP],
+    "covof_predictor": [_VP, C.c_double] + [_VP] * 10 + [_IP],
+    "covof_predictor_dev": [_VP, C.c_double] + [_VP] * 10 + [_IP],
+    "covof_momentum_apply": [_VP, C.c_double] + [_VP] * 10,
+    "covof_poisson_solve": [_VP, C.c_double] + [_VP] * 5 + [_IP, _DP],
+    "covof_poisson_solve_dev": [_VP, C.c_double] + [_VP] * 5 + [_IP, _DP],
+    "covof_poisson_solve_rhs": [_VP, C.c_double] + [_VP] * 4 + [_IP, _DP],
+    "covof_poisson_solve_rhs_dev": [_VP, C.c_double] + [_VP] * 4 + [_IP, _DP],
+    "covof_poisson_apply": [_VP, C.c_double] + [_VP] * 4,
+    "covof_project_correct": [_VP, C.c_double] + [_VP] * 5,
+    "covof_vof_reconstruct": [_VP, _VP, _VP],
+    "covof_vof_reconstruct_dev": [_VP, _VP, _VP],
+    "covof_vof_wy_step": [_VP, C.c_double, C.c_int, _VP, _VP, _VP],
+    "covof_vof_wy_step_dev": [_VP, C.c_double, C.c_int, _VP, _VP, _VP],
+    "covof_vof_advect": [_VP, C.c_double] + [_VP] * 11,
+    "covof_vof_advect_dev": [_VP, C.c_double] + [_VP] * 11,
+    "covof_update_physical_properties": [_VP] + [_VP] * 6,
+    "covof_compute_curvature_and_csf": [_VP] + [_VP] * 4,
+}
+
+
+def load_library(path: Path | str | None = None):
+    """Load libcovof_gpu.so once; raise if it is absent (no fallback path)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(
+            f"GB300 library not built ({p} missing): run __graft_entry__.build(); "
+            "this package has no CPU fallback")
+    lib = C.CDLL(str(p), mode=C.RTLD_GLOBAL)
+    for name, args in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    lib.covof_strerror.argtypes = [C.c_int]
+    lib.covof_strerror.restype = C.c_char_p
+    lib.covof_params_default.argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.c_double, C.c_double]
+    lib.covof_params_default.restype = None
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    """Every entry point the header declares (for the export test)."""
+    return sorted(list(_SIGS) + ["covof_strerror", "covof_params_default"])
+
+
+def describe(status: int) -> str:
+    try:
+        return load_library().covof_strerror(status).decode()
+    except Exception:  # library not loadable: fall back to the name only
+        return STATUS_NAMES.get(status, str(status))
+
+
+def default_params(nx: int, ny: int, lx: float, ly: float) -> Params:
+    p = Params()
+    load_library().covof_params_default(C.byref(p), nx, ny, lx, ly)
+    return p
+
+
+def library_path() -> str:
+    return os.fspath(LIB_PATH)

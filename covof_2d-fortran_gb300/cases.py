@@ -1,0 +1,190 @@
+"""Seeded synthetic inputs for the hot-path workloads.
+
+No dataset or case file ships with the reference, so every workload is a
+seeded synthetic stand-in with the shapes, sizes and value ranges of the
+configurations it represents.  Seeds: base 20261203, workload k uses
+base + k with numpy's PCG64.  Arrays use the reference layout (ny+2, nx+2).
+
+* ``bubble_case``      -- rising bubble, 128x256 on [0,1]x[0,2] (the small
+  STANDARD_PROJECTION + ELVIRA + Weymouth-Yue case).
+* ``poisson_inclusions`` -- standalone variable-density Poisson on 1024^2
+  with 200 heavy circular inclusions (rho 1000 in, 1 out), zero-mean
+  Gaussian RHS, homogeneous Neumann walls.
+* ``vortex_case``      -- Rider-Kothe single-vortex VOF transport
+  (src/module_simulation.f90:2175-2416).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import capi
+from .capi import Params
+
+SEED = 20261203
+
+
+def make_params(nx: int, ny: int, lx: float, ly: float) -> Params:
+    """Pure-Python twin of covof_params_default (checked against it in tests)."""
+    p = Params()
+    p.nx, p.ny = nx, ny
+    p.dx, p.dy = lx / nx, ly / ny
+    for s in range(4):
+        p.bc_type[s] = capi.BC_DIRICHLET
+        p.bc_u[s] = 0.0
+        p.bc_v[s] = 0.0
+    p.linear_solver = capi.LINEAR_BICGSTAB2
+    p.precond = capi.PRECOND_JACOBI
+    p.use_precond = 1
+    p.max_iter = 300
+    p.tol = 1.0e-5
+    p.enable_convection = 1
+    p.convective_scheme = capi.CONV_UPWIND
+    p.p_precond = capi.PRECOND_JACOBI
+    p.p_max_iter = 1000
+    p.p_gauge = capi.GAUGE_REFERENCE
+    p.p_precision = capi.PREC_FP64
+    p.p_tol = 1.0e-7
+    p.p_inner_tol = 1.0e-4
+    p.p_inner_max_iter = 100000
+    p.p_max_refine = 20
+    p.enable_two_phase = 0
+    p.enable_surface_tension = 0
+    p.rho1, p.rho2, p.mu1, p.mu2 = 1.0, 1.0, 1.0e-3, 1.0e-3
+    p.sigma, p.gx, p.gy = 0.0, 0.0, 0.0
+    p.recon = capi.RECON_PLIC
+    return p
+
+
+def field(p: Params, value: float = 0.0) -> np.ndarray:
+    return np.full((p.ny + 2, p.nx + 2), value, dtype=np.float64)
+
+
+def subsample_fraction(nx, ny, dx, dy, inside, nsub: int) -> np.ndarray:
+    """Fraction of nsub x nsub cell sub-samples where inside(x, y) holds, for
+    every cell of (0:nx+1, 0:ny+1) (sample points as in
+    src/module_interface_vof.f90:128-152)."""
+    i = np.arange(0, nx + 2)
+    j = np.arange(0, ny + 2)
+    s = (np.arange(nsub) + 0.5) / nsub
+    xs = ((i[:, None] - 1) + s[None, :]).reshape(-1) * dx   # (nx+2)*nsub
+    ys = ((j[:, None] - 1) + s[None, :]).reshape(-1) * dy
+    X, Y = np.meshgrid(xs, ys)                              # (ny+2)*nsub, (nx+2)*nsub
+    ins = inside(X, Y)
+    frac = ins.reshape(ny + 2, nsub, nx + 2, nsub).mean(axis=(1, 3))
+    return np.ascontiguousarray(frac, dtype=np.float64)
+
+
+# ---------------------------------------------------------------------------
+def bubble_case(nx: int = 128, ny: int = 256, seed: int = SEED + 0, nsub: int = 16):
+    """Rising gas bubble in liquid: params + initial C (liquid = fluid 1,
+    C = fraction of sub-samples outside the bubble)."""
+    lx, ly = 1.0, 2.0
+    p = make_params(nx, ny, lx, ly)
+    rng = np.random.default_rng(seed)
+    phases = rng.uniform(0.0, 2.0 * math.pi, size=7)
+    ks = np.arange(2, 9)
+
+    def outside(X, Y):
+        dxp, dyp = X - 0.5, Y - 0.5
+        th = np.arctan2(dyp, dxp)
+        r = 0.25 * (1.0 + 1.0e-3 * np.cos(ks[None, None, :] * th[..., None] + phases).sum(-1))
+        return np.hypot(dxp, dyp) > r
+
+    C = subsample_fraction(nx, ny, p.dx, p.dy, outside, nsub)
+    p.enable_two_phase = 1
+    p.enable_surface_tension = 1
+    p.rho1, p.mu1, p.rho2, p.mu2 = 1000.0, 10.0, 1.0, 0.1
+    p.sigma, p.gx, p.gy = 24.5, 0.0, -0.98
+    p.linear_solver = capi.LINEAR_BICGSTAB
+    p.tol = 1.0e-10
+    p.p_tol = 1.0e-10
+    p.p_max_iter = 100000
+    p.recon = capi.RECON_ELVIRA
+    dt = 1.0e-4
+    return p, C, dt
+
+
+def poisson_inclusions(n: int = 1024, n_incl: int = 200, seed: int = SEED + 1, nsub: int = 4):
+    """Standalone variable-density Poisson: returns (params, b, rho_u, rho_v, dt).
+    rho = 1000 C + (1 - C) with C the sub-sampled inclusion fraction; face
+    densities arithmetic (src/module_interface_vof.f90:576-591); RHS N(0,1)
+    per cell minus its mean; walls => homogeneous Neumann for p."""
+    p = make_params(n, n, 1.0, 1.0)
+    rng = np.random.default_rng(seed)
+    cx = rng.uniform(0.0, 1.0, n_incl)
+    cy = rng.uniform(0.0, 1.0, n_incl)
+    rr = rng.uniform(0.01, 0.05, n_incl)
+    # sub-sample mask, built inclusion by inclusion on its bounding box
+    ns = nsub
+    h = 1.0 / (n * ns)
+    ins = np.zeros((n * ns, n * ns), dtype=bool)
+    for x0, y0, r in zip(cx, cy, rr):
+        i0 = max(0, int((x0 - r) / h) - 1); i1 = min(n * ns, int((x0 + r) / h) + 2)
+        j0 = max(0, int((y0 - r) / h) - 1); j1 = min(n * ns, int((y0 + r) / h) + 2)
+        xs = (np.arange(i0, i1) + 0.5) * h
+        ys = (np.arange(j0, j1) + 0.5) * h
+        ins[j0:j1, i0:i1] |= ((xs[None, :] - x0) ** 2 + (ys[:, None] - y0) ** 2) <= r * r
+    Cin = ins.reshape(n, ns, n, ns).mean(axis=(1, 3))
+    C = np.zeros((n + 2, n + 2))
+    C[1:-1, 1:-1] = Cin
+    C[0, :] = C[1, :]; C[-1, :] = C[-2, :]; C[:, 0] = C[:, 1]; C[:, -1] = C[:, -2]
+    rho = 1000.0 * C + 1.0 * (1.0 - C)
+    rho_u = np.ones_like(rho)
+    rho_v = np.ones_like(rho)
+    rho_u[1:-1, 1:] = 0.5 * (rho[1:-1, :-1] + rho[1:-1, 1:])
+    rho_v[1:, 1:-1] = 0.5 * (rho[:-1, 1:-1] + rho[1:, 1:-1])
+    b = np.zeros_like(rho)
+    g = rng.standard_normal((n, n))
+    b[1:-1, 1:-1] = g - g.mean()
+    p.p_tol = 1.0e-10
+    p.p_max_iter = 200000
+    p.p_gauge = capi.GAUGE_PINNED
+    dt = 1.0
+    return p, b, rho_u, rho_v, dt
+
+
+def vortex_case(n: int = 64, recon: int = capi.RECON_PLIC, nsub: int = 16):
+    """Single-vortex VOF case (Rider & Kothe): disk R=0.125 at (0.5, 0.75), T=6."""
+    p = make_params(n, n, 1.0, 1.0)
+    p.enable_two_phase = 1
+    p.rho1, p.mu1, p.rho2, p.mu2 = 1000.0, 1.0e-3, 1.0, 1.0e-5
+    p.recon = recon
+    C = subsample_fraction(n, n, p.dx, p.dy,
+                           lambda X, Y: (X - 0.5) ** 2 + (Y - 0.75) ** 2 <= 0.125 ** 2, nsub)
+    dt = {64: 0.005, 128: 0.0025, 256: 0.00125, 512: 0.0005}.get(n, 0.32 / n)
+    return p, C, dt, 6.0
+
+
+def vortex_velocity(p: Params, t: float, dt: float, T: float):
+    """Analytic faces velocity at t + dt/2 (src/module_simulation.f90:2254-2288)."""
+    nx, ny = p.nx, p.ny
+    cf = math.cos(math.pi * (t + 0.5 * dt) / T)
+    u = field(p)
+    v = field(p)
+    xf = (np.arange(1, nx + 2) - 1) * p.dx            # faces i = 1..nx+1
+    yc = ((np.arange(1, ny + 1) - 1) + 0.5) * p.dy     # centres j = 1..ny
+    sx = np.sin(math.pi * xf)
+    sy = np.sin(2.0 * math.pi * yc)
+    u[1:ny + 1, 1:nx + 2] = -(sx[None, :] * sx[None, :]) * sy[:, None] * cf
+    xc = ((np.arange(1, nx + 1) - 1) + 0.5) * p.dx
+    yf = (np.arange(1, ny + 2) - 1) * p.dy
+    sx2 = np.sin(2.0 * math.pi * xc)
+    sy2 = np.sin(math.pi * yf)
+    v[1:ny + 2, 1:nx + 1] = sx2[None, :] * (sy2[:, None] * sy2[:, None]) * cf
+    return u, v
+
+
+def random_velocity(p: Params, scale: float, seed: int):
+    """Seeded random MAC velocity with zero normal velocity on the walls."""
+    rng = np.random.default_rng(seed)
+    u = field(p)
+    v = field(p)
+    u[1:p.ny + 1, 1:p.nx + 2] = scale * rng.standard_normal((p.ny, p.nx + 1))
+    v[1:p.ny + 2, 1:p.nx + 1] = scale * rng.standard_normal((p.ny + 1, p.nx))
+    u[1:p.ny + 1, 1] = 0.0
+    u[1:p.ny + 1, p.nx + 1] = 0.0
+    v[1, 1:p.nx + 1] = 0.0
+    v[p.ny + 1, 1:p.nx + 1] = 0.0
+    return u, v

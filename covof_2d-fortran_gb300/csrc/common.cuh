@@ -1,0 +1,192 @@
+// common.cuh -- shared device helpers for the COVOF GB300 kernels.
+//
+// Field layout: the reference's (0:nx+1, 0:ny+1) Fortran arrays, i fastest,
+// pitch nx+2 (src/module_fields.f90:129-169).  Device mirrors keep exactly
+// that layout so host<->device copies are single contiguous memcpys.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "../../include/covof_gpu.h"
+
+#define COVOF_WARP 32
+
+namespace covof {
+
+// Error word written by device code.  A bounded wait that gives up stores
+// COVOF_TIMEOUT; the first writer wins.
+__device__ __forceinline__ void set_error(int* err, int code) { atomicCAS(err, 0, code); }
+
+struct Dims {
+  int nx, ny, P;  // P = nx + 2
+  __host__ __device__ __forceinline__ int id(int i, int j) const { return j * P + i; }
+};
+
+// ---------------------------------------------------------------------------
+// Grid-wide barrier for kernels launched with cudaLaunchCooperativeKernel
+// (co-residency of all blocks is guaranteed by that launch, so the wait ends
+// in a few microseconds).  Every spin is still bounded: after kSpinLimit
+// polls the waiting block records COVOF_TIMEOUT and returns false; every
+// caller then leaves its loop, so no block can wait forever.
+//   bar[0] = arrival count, bar[1] = generation.
+constexpr long long kSpinLimit = 1LL << 25;  // ~1-2 s with the 32 ns back-off
+
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, unsigned int nblocks, int* err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned int* gen = bar + 1;
+    unsigned int g = *gen;
+    __threadfence();
+    unsigned int arrived = atomicAdd(bar, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      long long spins = 0;
+      while (*gen == g) {
+        if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    if (*(volatile int*)err != 0) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic reductions.  Block partials are combined by every block in
+// the same fixed order, so all blocks obtain bit-identical totals and take
+// identical convergence decisions.
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum NV values per thread across the block; result valid in thread 0.
+template <typename T, int NV>
+__device__ __forceinline__ void block_sum(T (&v)[NV]) {
+  __shared__ T sh[NV][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[k][wid] = v[k];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      T t = lane < nw ? sh[k][lane] : T(0);
+      v[k] = warp_sum(t);
+    }
+  }
+  __syncthreads();
+}
+
+// Combine the per-block FP64 partials part[b*NV + k], b < nblocks, into
+// tot[k] in every block (identical order everywhere).  Reads bypass L1.
+template <int NV>
+__device__ __forceinline__ void grid_combine(const double* part, int nblocks, double (&tot)[NV]) {
+  __shared__ double sh[NV];
+  if (threadIdx.x < 32) {
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += 32) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) acc[k] += __ldcg(part + b * NV + k);
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = warp_sum(acc[k]);
+      if (threadIdx.x == 0) sh[k] = t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) tot[k] = sh[k];
+  __syncthreads();
+}
+
+// Fused hypot: sqrt(x^2+y^2) with an FMA-based residual correction (after
+// C. F. Borges, "An improved algorithm for hypot(a,b)", ACM TOMS 2021).  Each
+// operation is an explicit IEEE round-to-nearest intrinsic so the result is
+// identical to the host implementation bit for bit.
+__device__ __forceinline__ double fhypot(double x, double y) {
+  double ax = fabs(x), ay = fabs(y);
+  if (isinf(ax) || isinf(ay)) return __longlong_as_double(0x7ff0000000000000LL);
+  if (isnan(ax) || isnan(ay)) return __dadd_rn(ax, ay);
+  if (ax < ay) { double t = ax; ax = ay; ay = t; }
+  if (ay == 0.0) return ax;
+  if (ay < __dmul_rn(ax, 0x1p-30)) return ax;
+  double scale = 1.0;
+  if (ax > 0x1p+500) { ax = __dmul_rn(ax, 0x1p-600); ay = __dmul_rn(ay, 0x1p-600); scale = 0x1p+600; }
+  else if (ax < 0x1p-450) { ax = __dmul_rn(ax, 0x1p+600); ay = __dmul_rn(ay, 0x1p+600); scale = 0x1p-600; }
+  double h = __dsqrt_rn(__fma_rn(ax, ax, __dmul_rn(ay, ay)));
+  double h_sq = __dmul_rn(h, h), h_lo = __fma_rn(h, h, -h_sq);
+  double x_sq = __dmul_rn(ax, ax), x_lo = __fma_rn(ax, ax, -x_sq);
+  double y_sq = __dmul_rn(ay, ay), y_lo = __fma_rn(ay, ay, -y_sq);
+  double r = __dadd_rn(__dadd_rn(__dsub_rn(x_sq, h_sq), y_sq), __dadd_rn(__dsub_rn(x_lo, h_lo), y_lo));
+  h = __dadd_rn(h, __ddiv_rn(r, __dmul_rn(2.0, h)));
+  return __dmul_rn(h, scale);
+}
+
+}  // namespace covof
+
+namespace covof {
+
+// Grid-wide sum of up to 8 FP64 values per thread.  Consecutive reductions
+// alternate between two partial regions, so a region is rewritten only after
+// every block has passed the barrier that follows its last read.
+// part must hold 2 * 8 * nblocks doubles.
+struct GridReducer {
+  double* part;
+  unsigned int* bar;
+  int* err;
+  unsigned int nblocks;
+  int region;
+  template <int NV>
+  __device__ bool sum(double (&v)[NV]) {
+    static_assert(NV <= 8, "at most 8 values");
+    block_sum<double, NV>(v);
+    double* base = part + (size_t)region * nblocks * 8;
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) base[blockIdx.x * 8 + q] = v[q];
+    }
+    bool ok = grid_barrier(bar, nblocks, err);
+    __shared__ double sh[8];
+    if (threadIdx.x < 32) {
+      double acc[NV];
+#pragma unroll
+      for (int q = 0; q < NV; ++q) acc[q] = 0.0;
+      for (int b = threadIdx.x; b < (int)nblocks; b += 32) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) acc[q] += __ldcg(base + b * 8 + q);
+      }
+#pragma unroll
+      for (int q = 0; q < NV; ++q) {
+        double t = warp_sum(acc[q]);
+        if (threadIdx.x == 0) sh[q] = t;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = sh[q];
+    __syncthreads();
+    region ^= 1;
+    return ok;
+  }
+};
+
+}  // namespace covof

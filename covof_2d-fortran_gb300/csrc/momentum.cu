@@ -1,0 +1,724 @@
+// momentum.cu -- momentum predictor of the STANDARD_PROJECTION step on one
+// GB300: matrix-free MAC momentum operator (unsteady + upwind/centred
+// convection with Picard linearisation + 2 mu normal stress + mu_node shear),
+// its Jacobi diagonal and right-hand side, and persistent cooperative
+// BiCGSTAB / BiCGSTAB(2) / CG kernels that run a whole Krylov solve in one
+// launch with device-side convergence tests.
+//
+// Krylov vectors hold the u DOFs (i=1..nx+1, j=1..ny) in the first
+// (nx+2)*(ny+2) block and the v DOFs (i=1..nx, j=1..ny+1) in the second, in
+// the field layout itself; ghost entries are never read: the operator
+// evaluates the homogeneous ghost conditions of
+// src/module_mpi_comm.f90:290-537 on the fly from the DOF values, as the
+// reference does when ns_unpack_vector applies them before every product
+// (src/module_navier_stokes.f90:397-458).  Expressions follow the reference
+// term order and the unit is built with -fmad=false, so one operator
+// application is bit-identical to a serial FP64 evaluation.
+#include "common.cuh"
+#include "momentum.cuh"
+
+namespace covof {
+
+enum { SL = 0, SR = 1, SB = 2, ST = 3 };
+
+__device__ __forceinline__ bool is_wall(const MomArgs& a, int s) {
+  return a.bc[s] == COVOF_BC_DIRICHLET || a.bc[s] == COVOF_BC_FREESLIP;
+}
+
+// Operand u with homogeneous ghosts.  Reads bypass L1: other blocks of the
+// persistent kernel wrote the vector.
+__device__ __forceinline__ double tu(const MomArgs& a, const double* xu, int i, int j) {
+  const Dims& D = a.D;
+  const int nx = D.nx, ny = D.ny;
+  if (j >= 1 && j <= ny) {
+    if (i >= 1) return __ldcg(xu + D.id(i, j));  // i <= nx+1 for every read made
+    return 0.0;                                   // west wall: u(0,j) = u_l = 0
+  }
+  if (j == 0) {
+    const double u1 = __ldcg(xu + D.id(i, 1));
+    if (a.bc[SB] == COVOF_BC_DIRICHLET) {
+      if (ny >= 2) return (8.0 * 0.0 - 6.0 * u1 + __ldcg(xu + D.id(i, 2))) / 3.0;
+      return 2.0 * 0.0 - u1;
+    }
+    return u1;  // FREESLIP
+  }
+  // j == ny + 1
+  const double un = __ldcg(xu + D.id(i, ny));
+  if (a.bc[ST] == COVOF_BC_DIRICHLET) {
+    if (ny >= 2) return (8.0 * 0.0 - 6.0 * un + __ldcg(xu + D.id(i, ny - 1))) / 3.0;
+    return 2.0 * 0.0 - un;
+  }
+  return un;
+}
+
+// Operand v with homogeneous ghosts.
+__device__ __forceinline__ double tv(const MomArgs& a, const double* xv, int i, int j) {
+  const Dims& D = a.D;
+  const int nx = D.nx;
+  if (j == 0) return 0.0;  // south wall: v(i,0) = v_b = 0
+  if (i == 0) {
+    const double v1 = __ldcg(xv + D.id(1, j));
+    return a.bc[SL] == COVOF_BC_DIRICHLET ? 2.0 * 0.0 - v1 : v1;
+  }
+  if (i == nx + 1) {
+    const double vn = __ldcg(xv + D.id(nx, j));
+    return a.bc[SR] == COVOF_BC_DIRICHLET ? 2.0 * 0.0 - vn : vn;
+  }
+  return __ldcg(xv + D.id(i, j));
+}
+
+// src/module_navier_stokes.f90:2388-2416 (UPWIND / CENTERED)
+__device__ __forceinline__ double conv_face_flux(int scheme, double flux, double pl, double pr) {
+  if (scheme == COVOF_CONV_CENTERED) return 0.5 * flux * (pl + pr);
+  return (flux >= 0.0) ? flux * pl : flux * pr;
+}
+
+// src/module_navier_stokes.f90:2418-2457 compute_u_conv_fluxes (PICARD)
+__device__ __forceinline__ void u_fluxes(const MomArgs& a, int i, int j, double& FE, double& FW,
+                                         double& FN, double& FS) {
+  const Dims& D = a.D;
+  const double un = a.u_n[D.id(i, j)], unE = a.u_n[D.id(i + 1, j)], unW = a.u_n[D.id(i - 1, j)];
+  const double vnN = 0.5 * (a.v_n[D.id(i - 1, j + 1)] + a.v_n[D.id(i, j + 1)]);
+  const double vnS = 0.5 * (a.v_n[D.id(i - 1, j)] + a.v_n[D.id(i, j)]);
+  FE = 0.5 * (un + unE) * a.dy;
+  FW = 0.5 * (unW + un) * a.dy;
+  FN = vnN * a.dx;
+  FS = vnS * a.dx;
+}
+// src/module_navier_stokes.f90:2459-2498 compute_v_conv_fluxes (PICARD)
+__device__ __forceinline__ void v_fluxes(const MomArgs& a, int i, int j, double& FE, double& FW,
+                                         double& FN, double& FS) {
+  const Dims& D = a.D;
+  const double vn = a.v_n[D.id(i, j)], vnN = a.v_n[D.id(i, j + 1)], vnS = a.v_n[D.id(i, j - 1)];
+  const double unE = 0.5 * (a.u_n[D.id(i + 1, j - 1)] + a.u_n[D.id(i + 1, j)]);
+  const double unW = 0.5 * (a.u_n[D.id(i, j - 1)] + a.u_n[D.id(i, j)]);
+  FE = unE * a.dy;
+  FW = unW * a.dy;
+  FN = 0.5 * (vn + vnN) * a.dx;
+  FS = 0.5 * (vnS + vn) * a.dx;
+}
+
+// (A x) at one DOF (src/module_navier_stokes.f90:474-617 for u, :624-750 for v).
+__device__ double mom_apply_dof(const MomArgs& a, int part, int i, int j, const double* xu,
+                                const double* xv) {
+  const Dims& D = a.D;
+  const int nx = D.nx, ny = D.ny;
+  const double dx = a.dx, dy = a.dy, dvol = dx * dy, dt = a.dt;
+  const int k = D.id(i, j);
+  if (part == 0) {
+    const double rho = a.rho_u[k];
+    const double diag_bc = ((1.0 * rho) / dt) * dvol;
+    if (i == 1) return diag_bc * tu(a, xu, 1, j);        // DIRICHLET / FREESLIP west
+    if (i == nx + 1) return diag_bc * tu(a, xu, nx + 1, j);
+    const double uc = tu(a, xu, i, j);
+    double val = (((1.0 * rho) / dt) * uc) * dvol;
+    const double uE = tu(a, xu, i + 1, j), uW = tu(a, xu, i - 1, j);
+    const double uN = tu(a, xu, i, j + 1), uS = tu(a, xu, i, j - 1);
+    if (a.conv) {
+      double FE, FW, FN, FS;
+      u_fluxes(a, i, j, FE, FW, FN, FS);
+      const double pE = conv_face_flux(a.scheme, FE, uc, uE);
+      const double pW = conv_face_flux(a.scheme, FW, uW, uc);
+      const double pN = conv_face_flux(a.scheme, FN, uc, uN);
+      const double pS = conv_face_flux(a.scheme, FS, uS, uc);
+      val = val + rho * (pE - pW + pN - pS);
+    }
+    const double muE = a.mu[k], muW = a.mu[k - 1];
+    const double dE = 2.0 * muE * (uE - uc) / dx * dy;
+    const double dW = 2.0 * muW * (uc - uW) / dx * dy;
+    val = val - (dE - dW);
+    const double mN = a.mu_node[k + D.P], mS = a.mu_node[k];
+    const double sN = mN * ((uN - uc) / dy + (tv(a, xv, i, j + 1) - tv(a, xv, i - 1, j + 1)) / dx) * dx;
+    const double sS = mS * ((uc - uS) / dy + (tv(a, xv, i, j) - tv(a, xv, i - 1, j)) / dx) * dx;
+    val = val - (sN - sS);
+    return val;
+  }
+  const double rho = a.rho_v[k];
+  const double diag_bc = ((1.0 * rho) / dt) * dvol;
+  if ((j == 1 && is_wall(a, SB)) || (j == ny + 1 && is_wall(a, ST))) return diag_bc * tv(a, xv, i, j);
+  const double vc = tv(a, xv, i, j);
+  double val = (((1.0 * rho) / dt) * vc) * dvol;
+  const double vE = tv(a, xv, i + 1, j), vW = tv(a, xv, i - 1, j);
+  const double vN = tv(a, xv, i, j + 1), vS = tv(a, xv, i, j - 1);
+  if (a.conv) {
+    double FE, FW, FN, FS;
+    v_fluxes(a, i, j, FE, FW, FN, FS);
+    const double pE = conv_face_flux(a.scheme, FE, vc, vE);
+    const double pW = conv_face_flux(a.scheme, FW, vW, vc);
+    const double pN = conv_face_flux(a.scheme, FN, vc, vN);
+    const double pS = conv_face_flux(a.scheme, FS, vS, vc);
+    val = val + rho * (pE - pW + pN - pS);
+  }
+  const double muN = a.mu[k], muS = a.mu[k - D.P];
+  const double dN = 2.0 * muN * (vN - vc) / dy * dx;
+  const double dS = 2.0 * muS * (vc - vS) / dy * dx;
+  val = val - (dN - dS);
+  const double mE = a.mu_node[k + 1], mW = a.mu_node[k];
+  const double sE = mE * ((vE - vc) / dx + (tu(a, xu, i + 1, j) - tu(a, xu, i + 1, j - 1)) / dy) * dy;
+  const double sW = mW * ((vc - vW) / dx + (tu(a, xu, i, j) - tu(a, xu, i, j - 1)) / dy) * dy;
+  val = val - (sE - sW);
+  return val;
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi diagonal, src/module_navier_stokes.f90:1313-1539 (diag_u / diag_v).
+__global__ void k_mom_diag(MomArgs a) {
+  const Dims& D = a.D;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int nx = D.nx, ny = D.ny;
+  const double dx = a.dx, dy = a.dy, dvol = dx * dy;
+  const double dt_safe = a.dt > 1.0e-30 ? a.dt : 1.0;
+  const int g = D.P * (ny + 2);
+  if (i <= nx + 1 && j <= ny) {
+    const int k = D.id(i, j);
+    const double rho = a.rho_u[k];
+    double Du = ((1.0 * rho) / dt_safe) * dvol;
+    if (Du <= 1.0e-30) Du = 1.0;
+    double out;
+    if (i == 1 || i == nx + 1) {
+      out = Du;
+    } else {
+      const double mue = a.mu[k], muw = a.mu[k - 1];
+      const double cE = 2.0 * mue * (dy / dx), cW = 2.0 * muw * (dy / dx);
+      const double cNr = a.mu_node[k + D.P] * (dx / dy);
+      const double cSr = a.mu_node[k] * (dx / dy);
+      double cNv = cNr, cSv = cSr, dwy = 0.0;
+      if (j == 1) {
+        if (a.bc[SB] == COVOF_BC_DIRICHLET) dwy = dwy + (ny >= 2 ? 3.0 * cSr : 2.0 * cSr);
+        cSv = 0.0;
+      }
+      if (j == ny) {
+        if (a.bc[ST] == COVOF_BC_DIRICHLET) dwy = dwy + (ny >= 2 ? 3.0 * cNr : 2.0 * cNr);
+        cNv = 0.0;
+      }
+      double conv_diag = 0.0;
+      if (a.conv) {
+        double FE, FW, FN, FS;
+        u_fluxes(a, i, j, FE, FW, FN, FS);
+        conv_diag = rho * (fmax(FE, 0.0) + fmax(-FW, 0.0) + fmax(FN, 0.0) + fmax(-FS, 0.0));
+      }
+      double aP = Du + dwy + conv_diag + 0.0 + 0.0 + cW + cE + cSv + cNv + 0.0 + 0.0;
+      if (aP <= 1.0e-15) aP = 1.0;
+      out = aP;
+    }
+    a.diag[k] = out;
+  }
+  if (i <= nx && j <= ny + 1) {
+    const int k = D.id(i, j);
+    const double rho = a.rho_v[k];
+    double Dv = ((1.0 * rho) / dt_safe) * dvol;
+    if (Dv <= 1.0e-30) Dv = 1.0;
+    double out;
+    if ((j == 1 && is_wall(a, SB)) || (j == ny + 1 && is_wall(a, ST))) {
+      out = Dv;
+    } else {
+      const double mun = a.mu[k], mus = a.mu[k - D.P];
+      const double cN = 2.0 * mun * (dx / dy), cS = 2.0 * mus * (dx / dy);
+      const double cEr = a.mu_node[k + 1] * (dy / dx);
+      const double cWr = a.mu_node[k] * (dy / dx);
+      double cEv = cEr, cWv = cWr, dwx = 0.0;
+      if (i == 1) {
+        if (a.bc[SL] == COVOF_BC_DIRICHLET) dwx = dwx + 2.0 * cWr;
+        cWv = 0.0;
+      }
+      if (i == nx) {
+        if (a.bc[SR] == COVOF_BC_DIRICHLET) dwx = dwx + 2.0 * cEr;
+        cEv = 0.0;
+      }
+      double conv_diag = 0.0;
+      if (a.conv) {
+        double FE, FW, FN, FS;
+        v_fluxes(a, i, j, FE, FW, FN, FS);
+        conv_diag = rho * (fmax(FE, 0.0) + fmax(-FW, 0.0) + fmax(FN, 0.0) + fmax(-FS, 0.0));
+      }
+      double aP = Dv + dwx + conv_diag + 0.0 + 0.0 + cWv + cEv + cS + cN + 0.0 + 0.0;
+      if (aP <= 1.0e-15) aP = 1.0;
+      out = aP;
+    }
+    a.diag[g + k] = out;
+  }
+}
+
+// Right-hand side, src/module_navier_stokes.f90:817-1088 (SP, Euler, constant walls).
+__global__ void k_mom_rhs(MomArgs a) {
+  const Dims& D = a.D;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int nx = D.nx, ny = D.ny;
+  const double dx = a.dx, dy = a.dy, dvol = dx * dy, dt = a.dt;
+  const int g = D.P * (ny + 2);
+  if (i <= nx + 1 && j <= ny) {
+    const int k = D.id(i, j);
+    const double rho = a.rho_u[k];
+    const double diag_bc = ((1.0 * rho) / dt) * dvol;
+    double out;
+    if (i == 1) {
+      out = diag_bc * (a.bc[SL] == COVOF_BC_DIRICHLET ? a.bcu[SL] : 0.0);
+    } else if (i == nx + 1) {
+      out = diag_bc * (a.bc[SR] == COVOF_BC_DIRICHLET ? a.bcu[SR] : 0.0);
+    } else {
+      double val = (rho / dt) * a.u_old[k] * dvol;
+      val = val + rho * a.gx * dvol;
+      val = val + a.fx[k] * dvol;
+      if (j == ny && a.bc[ST] == COVOF_BC_DIRICHLET) {
+        const double mN = a.mu_node[k + D.P];
+        if (ny >= 2) val = val + mN * ((8.0 / 3.0) * a.bcu[ST] / dy) * dx;
+        else val = val + mN * (2.0 * a.bcu[ST] / dy) * dx;
+      }
+      if (j == 1 && a.bc[SB] == COVOF_BC_DIRICHLET) {
+        const double mS = a.mu_node[k];
+        if (ny >= 2) val = val + mS * ((8.0 / 3.0) * a.bcu[SB] / dy) * dx;
+        else val = val + mS * (2.0 * a.bcu[SB] / dy) * dx;
+      }
+      out = val;
+    }
+    a.rhs[k] = out;
+  }
+  if (i <= nx && j <= ny + 1) {
+    const int k = D.id(i, j);
+    const double rho = a.rho_v[k];
+    const double diag_bc = ((1.0 * rho) / dt) * dvol;
+    double out;
+    if (j == 1 && is_wall(a, SB)) {
+      out = diag_bc * (a.bc[SB] == COVOF_BC_DIRICHLET ? a.bcv[SB] : 0.0);
+    } else if (j == ny + 1 && is_wall(a, ST)) {
+      out = diag_bc * (a.bc[ST] == COVOF_BC_DIRICHLET ? a.bcv[ST] : 0.0);
+    } else {
+      double val = (rho / dt) * a.v_old[k] * dvol;
+      val = val + rho * a.gy * dvol;
+      val = val + a.fy[k] * dvol;
+      if (i == 1 && a.bc[SL] == COVOF_BC_DIRICHLET) {
+        const double mW = a.mu_node[k];
+        val = val + mW * (2.0 * a.bcv[SL] / dx) * dy;
+      }
+      if (i == nx && a.bc[SR] == COVOF_BC_DIRICHLET) {
+        const double mE = a.mu_node[k + 1];
+        val = val + mE * (2.0 * a.bcv[SR] / dx) * dy;
+      }
+      out = val;
+    }
+    a.rhs[g + k] = out;
+  }
+}
+
+// One operator application over all DOFs (tests; also the reference's
+// ns_apply_system_matrix on unpacked vectors).
+__global__ void k_mom_apply(MomArgs a, const double* xu, const double* xv, double* yu, double* yv) {
+  const Dims& D = a.D;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i <= D.nx + 1 && j <= D.ny) yu[D.id(i, j)] = mom_apply_dof(a, 0, i, j, xu, xv);
+  if (i <= D.nx && j <= D.ny + 1) yv[D.id(i, j)] = mom_apply_dof(a, 1, i, j, xu, xv);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent Krylov solvers.  DOF ownership: warp w walks 32-wide row
+// segments of the u block, then of the v block.
+struct DofWalker {
+  int nsu, nsv, su, stot, gw, nw, lane, g;
+  __device__ explicit DofWalker(const Dims& D) {
+    nsu = (D.nx + 1 + 31) >> 5;
+    nsv = (D.nx + 31) >> 5;
+    su = nsu * D.ny;
+    stot = su + nsv * (D.ny + 1);
+    lane = threadIdx.x & 31;
+    gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    nw = (gridDim.x * blockDim.x) >> 5;
+    g = D.P * (D.ny + 2);
+  }
+  // Decode segment s; returns false when this lane has no DOF there.
+  __device__ __forceinline__ bool at(const Dims& D, int s, int& part, int& i, int& j, int& k) const {
+    if (s < su) {
+      part = 0; j = s / nsu + 1; i = (s - (j - 1) * nsu) * 32 + lane + 1;
+      if (i > D.nx + 1) return false;
+      k = D.id(i, j);
+    } else {
+      const int t = s - su;
+      part = 1; j = t / nsv + 1; i = (t - (j - 1) * nsv) * 32 + lane + 1;
+      if (i > D.nx) return false;
+      k = g + D.id(i, j);
+    }
+    return true;
+  }
+};
+#define FOR_DOFS(A, W, part, i, j, k)                                 \
+  for (int s_ = (W).gw; s_ < (W).stot; s_ += (W).nw)                 \
+    for (int part = 0, i = 0, j = 0, k = 0, once_ = (W).at((A).D, s_, part, i, j, k); once_; once_ = 0)
+
+__device__ __forceinline__ double prec(const MomArgs& a, int k, double src) {
+  const double d = a.diag[k];
+  return (a.precond_on && fabs(d) > 1.0e-15) ? src / d : src;
+}
+
+// y = M^-1 A x (or A x when with_prec = false) at own DOFs.
+__device__ __forceinline__ double pa_at(const MomArgs& a, const DofWalker& W, int part, int i,
+                                        int j, int k, const double* x, bool with_prec) {
+  const double y = mom_apply_dof(a, part, i, j, x, x + W.g);
+  return with_prec ? prec(a, k, y) : y;
+}
+
+struct KCtx {
+  GridReducer R;
+  bool ok;
+};
+
+__device__ void krylov_finish(const MomArgs& a, int iters, int status, bool ok) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.res->iters = iters;
+    a.res->status = ok ? status : COVOF_TIMEOUT;
+  }
+}
+
+// src/module_linear_solvers.f90:584-730 solve_bicgstab (left Jacobi).
+__global__ void __launch_bounds__(256) k_bicgstab(MomArgs a) {
+  DofWalker W(a.D);
+  GridReducer R{a.part, a.bar, a.err, gridDim.x, 0};
+  double *x = a.x, *bh = a.v0, *r = a.v1, *rt = a.v2, *p = a.v3, *v = a.v4, *s = a.v5, *t = a.v6;
+  const double tol = a.tol;
+  const int max_iter = a.max_iter;
+  // b_hat = M^-1 b ; r = b_hat - M^-1 A x ; ||r||
+  double acc[1] = {0.0};
+  FOR_DOFS(a, W, part, i, j, k) {
+    const double bb = prec(a, k, a.rhs[k]);
+    bh[k] = bb;
+    const double rr = bb - pa_at(a, W, part, i, j, k, x, true);
+    r[k] = rr; rt[k] = rr;
+    acc[0] += rr * rr;
+  }
+  bool ok = R.sum(acc);
+  const double rsq0 = acc[0];
+  const double r0 = sqrt(rsq0);
+  if (!ok || r0 < 1.0e-12) { krylov_finish(a, 0, COVOF_OK, ok); return; }
+  double rho_old = 1.0, alpha = 1.0, omega = 1.0, rho = rsq0;
+  int iters = max_iter, status = COVOF_MAXITER;
+  for (int it = 1; it <= max_iter && ok; ++it) {
+    if (fabs(rho) < 1.0e-30) { status = COVOF_BREAKDOWN; break; }
+    const double beta = (rho / rho_old) * (alpha / omega);
+    FOR_DOFS(a, W, part, i, j, k) {
+      p[k] = (it == 1) ? r[k] : r[k] + beta * (p[k] - omega * v[k]);
+    }
+    ok = grid_barrier(a.bar, gridDim.x, a.err);
+    if (!ok) break;
+    double a1[1] = {0.0};
+    FOR_DOFS(a, W, part, i, j, k) {
+      const double vv = pa_at(a, W, part, i, j, k, p, true);
+      v[k] = vv;
+      a1[0] += rt[k] * vv;
+    }
+    ok = R.sum(a1);
+    if (!ok) break;
+    if (fabs(a1[0]) < 1.0e-30) { status = COVOF_BREAKDOWN; break; }
+    alpha = rho / a1[0];
+    double a2[1] = {0.0};
+    FOR_DOFS(a, W, part, i, j, k) {
+      const double sv = r[k] - alpha * v[k];
+      s[k] = sv;
+      a2[0] += sv * sv;
+    }
+    ok = R.sum(a2);
+    if (!ok) break;
+    const double sn = sqrt(a2[0]);
+    if (sn != sn || sn > 1.0e30) { status = COVOF_NAN; break; }
+    if (sn / r0 < tol || sn < 1.0e-12) {
+      FOR_DOFS(a, W, part, i, j, k) x[k] = x[k] + alpha * p[k];
+      iters = it; status = COVOF_OK;
+      break;
+    }
+    double a3[2] = {0.0, 0.0};
+    FOR_DOFS(a, W, part, i, j, k) {
+      const double tt = pa_at(a, W, part, i, j, k, s, true);
+      t[k] = tt;
+      a3[0] += tt * tt;
+      a3[1] += tt * s[k];
+    }
+    ok = R.sum(a3);
+    if (!ok) break;
+    omega = a3[0] > 1.0e-30 ? a3[1] / a3[0] : 0.0;
+    double a4[2] = {0.0, 0.0};
+    FOR_DOFS(a, W, part, i, j, k) {
+      x[k] = x[k] + alpha * p[k] + omega * s[k];
+      const double rr = s[k] - omega * t[k];
+      r[k] = rr;
+      a4[0] += rr * rr;
+      a4[1] += rt[k] * rr;  // next iteration's rho = <r~, r>
+    }
+    ok = R.sum(a4);
+    if (!ok) break;
+    rho_old = rho;
+    rho = a4[1];
+    const double rn = sqrt(a4[0]);
+    if (rn != rn || rn > 1.0e30) { status = COVOF_NAN; break; }
+    if (rn / r0 < tol || rn < 1.0e-12) { iters = it; status = COVOF_OK; break; }
+    if (fabs(omega) < 1.0e-30) { status = COVOF_BREAKDOWN; break; }
+  }
+  krylov_finish(a, iters, status, ok);
+}
+
+// src/module_linear_solvers.f90:735-838 solve_cg (unpreconditioned operator,
+// separate Jacobi application).
+__global__ void __launch_bounds__(256) k_cg(MomArgs a) {
+  DofWalker W(a.D);
+  GridReducer R{a.part, a.bar, a.err, gridDim.x, 0};
+  double *x = a.x, *r = a.v1, *p = a.v3, *Ap = a.v4;
+  const double tol = a.tol;
+  const int max_iter = a.max_iter;
+  double acc[2] = {0.0, 0.0};
+  FOR_DOFS(a, W, part, i, j, k) {
+    const double rr = a.rhs[k] - pa_at(a, W, part, i, j, k, x, false);
+    r[k] = rr;
+    const double z = prec(a, k, rr);
+    p[k] = z;
+    acc[0] += rr * rr;
+    acc[1] += rr * z;
+  }
+  bool ok = R.sum(acc);
+  const double r0 = sqrt(acc[0]);
+  if (!ok || r0 < 1.0e-12) { krylov_finish(a, 0, COVOF_OK, ok); return; }
+  double rz_old = acc[1];
+  int iters = max_iter, status = COVOF_MAXITER;
+  for (int it = 1; it <= max_iter && ok; ++it) {
+    double a1[1] = {0.0};
+    FOR_DOFS(a, W, part, i, j, k) {
+      const double y = pa_at(a, W, part, i, j, k, p, false);
+      Ap[k] = y;
+      a1[0] += p[k] * y;
+    }
+    ok = R.sum(a1);
+    if (!ok) break;
+    if (fabs(a1[0]) < 1.0e-30) { status = COVOF_BREAKDOWN; break; }
+    const double alpha = rz_old / a1[0];
+    double a2[2] = {0.0, 0.0};
+    FOR_DOFS(a, W, part, i, j, k) {
+      x[k] = x[k] + alpha * p[k];
+      const double rr = r[k] - alpha * Ap[k];
+      r[k] = rr;
+      a2[0] += rr * rr;
+      a2[1] += rr * prec(a, k, rr);
+    }
+    ok = R.sum(a2);
+    if (!ok) break;
+    const double rn = sqrt(a2[0]);
+    if (rn / r0 < tol || rn < 1.0e-13) { iters = it; status = COVOF_OK; break; }
+    const double beta = a2[1] / rz_old;
+    rz_old = a2[1];
+    FOR_DOFS(a, W, part, i, j, k) p[k] = prec(a, k, r[k]) + beta * p[k];
+    ok = grid_barrier(a.bar, gridDim.x, a.err);
+  }
+  krylov_finish(a, iters, status, ok);
+}
+
+// src/module_linear_solvers.f90:361-579 solve_bicgstab2 (left Jacobi).
+__global__ void __launch_bounds__(256) k_bicgstab2(MomArgs a) {
+  DofWalker W(a.D);
+  GridReducer R{a.part, a.bar, a.err, gridDim.x, 0};
+  double *x = a.x, *rt = a.v0, *r0 = a.v1, *r1 = a.v2, *r2 = a.v3, *u0 = a.v4, *u1 = a.v5, *u2 = a.v6;
+  const double tol = a.tol;
+  const int max_iter = a.max_iter;
+  double acc[1] = {0.0};
+  FOR_DOFS(a, W, part, i, j, k) {
+    const double bb = prec(a, k, a.rhs[k]);
+    const double rr = bb - pa_at(a, W, part, i, j, k, x, true);
+    r0[k] = rr; rt[k] = rr;
+    u0[k] = 0.0; u1[k] = 0.0; u2[k] = 0.0; r1[k] = 0.0; r2[k] = 0.0;
+    acc[0] += rr * rr;
+  }
+  bool ok = R.sum(acc);
+  const double r0n = sqrt(acc[0]);
+  if (!ok || r0n < 1.0e-12) { krylov_finish(a, 0, COVOF_OK, ok); return; }
+  double rho0 = 1.0, alpha = 0.0, omega = 1.0;
+  int iter = 0, status = COVOF_MAXITER;
+  bool have_rho1 = true;
+  double rho1_next = acc[0];  // <r~, r0> with r~ = r0
+  while (iter < max_iter && ok) {
+    iter += 2;
+    rho0 = -omega * rho0;
+    double rho1 = rho1_next;
+    (void)have_rho1;
+    if (fabs(rho0) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
+    double beta = alpha * (rho1 / rho0);
+    rho0 = rho1;
+    FOR_DOFS(a, W, part, i, j, k) u0[k] = r0[k] - beta * u0[k];
+    ok = grid_barrier(a.bar, gridDim.x, a.err);
+    if (!ok) break;
+    double g1[1] = {0.0};
+    FOR_DOFS(a, W, part, i, j, k) {
+      const double y = pa_at(a, W, part, i, j, k, u0, true);
+      u1[k] = y;
+      g1[0] += rt[k] * y;
+    }
+    ok = R.sum(g1);
+    if (!ok) break;
+    if (fabs(g1[0]) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
+    alpha = rho0 / g1[0];
+    FOR_DOFS(a, W, part, i, j, k) {
+      r0[k] = r0[k] - alpha * u1[k];
+      x[k] = x[k] + alpha * u0[k];
+    }
+    ok = grid_barrier(a.bar, gridDim.x, a.err);
+    if (!ok) break;
+    double g2[1] = {0.0};
+    FOR_DOFS(a, W, part, i, j, k) {
+      const double y = pa_at(a, W, part, i, j, k, r0, true);
+      r1[k] = y;
+      g2[0] += rt[k] * y;
+    }
+    ok = R.sum(g2);
+    if (!ok) break;
+    rho1 = g2[0];
+    if (fabs(rho0) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
+    beta = alpha * (rho1 / rho0);
+    rho0 = rho1;
+    FOR_DOFS(a, W, part, i, j, k) {
+      u0[k] = r0[k] - beta * u0[k];
+      u1[k] = r1[k] - beta * u1[k];
+    }
+    ok = grid_barrier(a.bar, gridDim.x, a.err);
+    if (!ok) break;
+    double g3[1] = {0.0};
+    FOR_DOFS(a, W, part, i, j, k) {
+      const double y = pa_at(a, W, part, i, j, k, u1, true);
+      u2[k] = y;
+      g3[0] += rt[k] * y;
+    }
+    ok = R.sum(g3);
+    if (!ok) break;
+    if (fabs(g3[0]) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
+    alpha = rho0 / g3[0];
+    FOR_DOFS(a, W, part, i, j, k) {
+      x[k] = x[k] + alpha * u0[k];
+      r0[k] = r0[k] - alpha * u1[k];
+      r1[k] = r1[k] - alpha * u2[k];
+    }
+    ok = grid_barrier(a.bar, gridDim.x, a.err);
+    if (!ok) break;
+    double sg[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    FOR_DOFS(a, W, part, i, j, k) {
+      const double y = pa_at(a, W, part, i, j, k, r1, true);
+      r2[k] = y;
+      sg[0] += r1[k] * r1[k];
+      sg[1] += y * r1[k];
+      sg[2] += y * y;
+      sg[3] += r0[k] * r1[k];
+      sg[4] += r0[k] * y;
+    }
+    ok = R.sum(sg);
+    if (!ok) break;
+    const double s11 = sg[0], s12 = sg[1], s22 = sg[2], rhs1 = sg[3], rhs2 = sg[4];
+    const double rn1 = sqrt(s11), rn2 = sqrt(s22);
+    double gm1, gm2;
+    if (rn1 < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
+    else if (rn2 < 1.0e-300) { gm2 = 0.0; gm1 = rhs1 / s11; }
+    else {
+      const double i1 = 1.0 / rn1, i2 = 1.0 / rn2;
+      const double c12 = s12 * i1 * i2;
+      const double b1 = rhs1 * i1, b2 = rhs2 * i2;
+      const double det = 1.0 - c12 * c12;
+      if (fabs(det) < 1.0e-14) { gm2 = 0.0; gm1 = b1 * i1; }
+      else { gm1 = (b1 - c12 * b2) / (det * rn1); gm2 = (b2 - c12 * b1) / (det * rn2); }
+    }
+    double fin[2] = {0.0, 0.0};
+    FOR_DOFS(a, W, part, i, j, k) {
+      x[k] = x[k] + gm1 * r0[k] + gm2 * r1[k];
+      const double rr = r0[k] - (gm1 * r1[k] + gm2 * r2[k]);
+      r0[k] = rr;
+      u0[k] = u0[k] - (gm1 * u1[k] + gm2 * u2[k]);
+      fin[0] += rr * rr;
+      fin[1] += rt[k] * rr;  // rho1 of the next sweep
+    }
+    ok = R.sum(fin);
+    if (!ok) break;
+    rho1_next = fin[1];
+    if (gm2 != 0.0) omega = gm2;
+    else if (fabs(gm1) > 1.0e-300) omega = gm1;
+    else omega = 1.0;
+    const double rn = sqrt(fin[0]);
+    if (rn != rn || rn > 1.0e30) { status = COVOF_NAN; break; }
+    if (rn / r0n < tol || rn < 1.0e-12) { status = COVOF_OK; break; }
+  }
+  krylov_finish(a, iter, status, ok);
+}
+
+// ---------------------------------------------------------------------------
+// Copy the solution DOFs back into (u, v); ghosts come from k_vbc_*.
+__global__ void k_mom_unpack(MomArgs a, double* u, double* v) {
+  const Dims& D = a.D;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int g = D.P * (D.ny + 2);
+  if (i <= D.nx + 1 && j <= D.ny) u[D.id(i, j)] = a.x[D.id(i, j)];
+  if (i <= D.nx && j <= D.ny + 1) v[D.id(i, j)] = a.x[g + D.id(i, j)];
+}
+// Pack (u, v) DOFs into the Krylov start vector.
+__global__ void k_mom_pack(MomArgs a, const double* u, const double* v) {
+  const Dims& D = a.D;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int g = D.P * (D.ny + 2);
+  if (i <= D.nx + 1 && j <= D.ny) a.x[D.id(i, j)] = u[D.id(i, j)];
+  if (i <= D.nx && j <= D.ny + 1) a.x[g + D.id(i, j)] = v[D.id(i, j)];
+}
+
+// Non-homogeneous velocity ghost conditions, src/module_mpi_comm.f90:290-537,
+// in the reference's order: west/east columns, then south/north rows, then
+// the physical corners.
+__global__ void k_vbc_we(BcArgs b, double* u, double* v) {
+  const Dims& D = b.D;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int nx = D.nx;
+  if (j > D.ny) return;
+  // west
+  if (b.bc[SL] == COVOF_BC_DIRICHLET) {
+    u[D.id(1, j)] = b.bcu[SL];
+    u[D.id(0, j)] = b.bcu[SL];
+    v[D.id(0, j)] = 2.0 * b.bcv[SL] - v[D.id(1, j)];
+  } else if (b.bc[SL] == COVOF_BC_FREESLIP) {
+    u[D.id(1, j)] = 0.0;
+    u[D.id(0, j)] = 0.0;
+    v[D.id(0, j)] = v[D.id(1, j)];
+  }
+  // east
+  if (b.bc[SR] == COVOF_BC_DIRICHLET) {
+    u[D.id(nx + 1, j)] = b.bcu[SR];
+    v[D.id(nx + 1, j)] = 2.0 * b.bcv[SR] - v[D.id(nx, j)];
+  } else if (b.bc[SR] == COVOF_BC_FREESLIP) {
+    u[D.id(nx + 1, j)] = 0.0;
+    v[D.id(nx + 1, j)] = v[D.id(nx, j)];
+  }
+}
+__global__ void k_vbc_sn(BcArgs b, double* u, double* v) {
+  const Dims& D = b.D;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int ny = D.ny;
+  if (i > D.nx) return;
+  if (b.bc[SB] == COVOF_BC_DIRICHLET) {
+    v[D.id(i, 1)] = b.bcv[SB];
+    v[D.id(i, 0)] = b.bcv[SB];
+    if (ny >= 2) u[D.id(i, 0)] = (8.0 * b.bcu[SB] - 6.0 * u[D.id(i, 1)] + u[D.id(i, 2)]) / 3.0;
+    else u[D.id(i, 0)] = 2.0 * b.bcu[SB] - u[D.id(i, 1)];
+  } else if (b.bc[SB] == COVOF_BC_FREESLIP) {
+    v[D.id(i, 1)] = 0.0;
+    v[D.id(i, 0)] = 0.0;
+    u[D.id(i, 0)] = u[D.id(i, 1)];
+  }
+  if (b.bc[ST] == COVOF_BC_DIRICHLET) {
+    v[D.id(i, ny + 1)] = b.bcv[ST];
+    if (ny >= 2) u[D.id(i, ny + 1)] = (8.0 * b.bcu[ST] - 6.0 * u[D.id(i, ny)] + u[D.id(i, ny - 1)]) / 3.0;
+    else u[D.id(i, ny + 1)] = 2.0 * b.bcu[ST] - u[D.id(i, ny)];
+  } else if (b.bc[ST] == COVOF_BC_FREESLIP) {
+    v[D.id(i, ny + 1)] = 0.0;
+    u[D.id(i, ny + 1)] = u[D.id(i, ny)];
+  }
+}
+__global__ void k_vbc_corners(BcArgs b, double* u, double* v) {
+  const Dims& D = b.D;
+  const int nx = D.nx, ny = D.ny;
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  u[D.id(nx + 1, 0)] = u[D.id(nx + 1, 1)];
+  v[D.id(nx + 1, 0)] = v[D.id(nx, 0)];
+  u[D.id(nx + 1, ny + 1)] = u[D.id(nx + 1, ny)];
+  v[D.id(nx + 1, ny + 1)] = v[D.id(nx, ny + 1)];
+  v[D.id(0, ny + 1)] = v[D.id(1, ny + 1)];
+}
+
+}  // namespace covof

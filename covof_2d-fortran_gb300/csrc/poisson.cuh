@@ -1,0 +1,51 @@
+// poisson.cuh -- argument blocks shared by poisson.cu and the C ABI layer.
+#pragma once
+#include "common.cuh"
+
+namespace covof {
+
+struct PcgResult {
+  int iters;      // PCG iterations (mixed: total FP32 inner iterations)
+  int status;     // COVOF_*
+  int outer;      // mixed: FP64 refinement steps
+  int pad;
+  double relres;  // ||r||/||b|| at exit (mixed: true FP64 residual)
+};
+
+struct PoissonArgs {
+  Dims D;
+  // FP64 system
+  double* x; const double* b; double* r; double* d; double* Ad;
+  const double* ax; const double* ay; const double* aP;
+  // FP32 inner system (mixed)
+  float* e32; float* r32b; float* r32; float* d32; float* Ad32;
+  const float* ax32; const float* ay32; const float* aP32;
+  // control
+  unsigned int* bar; int* err; double* part;  // part: 5 * nblocks doubles
+  PcgResult* res;
+  double tol, inner_tol;
+  int max_iter, inner_max_iter, max_refine, pinned;
+};
+
+__global__ void k_poisson_assemble(Dims D, double dt, double dx, double dy, int4 wall,
+                                   const double* __restrict__ rho_u,
+                                   const double* __restrict__ rho_v,
+                                   const double* __restrict__ u, const double* __restrict__ v,
+                                   const double* __restrict__ b_in, int pinned,
+                                   double* __restrict__ ax, double* __restrict__ ay,
+                                   double* __restrict__ aP, double* __restrict__ b,
+                                   float* __restrict__ ax32, float* __restrict__ ay32,
+                                   float* __restrict__ aP32);
+__global__ void k_copy_interior(Dims D, const double* __restrict__ src, double* __restrict__ dst,
+                                int zero_pin);
+__global__ void k_pcg_fp64(PoissonArgs a);
+__global__ void k_pcg_mixed(PoissonArgs a);
+__global__ void k_project_correct(Dims D, double dt, double dx, double dy, int4 wall,
+                                  double* __restrict__ u, double* __restrict__ v,
+                                  const double* __restrict__ p, const double* __restrict__ rho_u,
+                                  const double* __restrict__ rho_v);
+__global__ void k_poisson_apply(Dims D, const double* __restrict__ x, double* __restrict__ y,
+                                const double* __restrict__ ax, const double* __restrict__ ay,
+                                const double* __restrict__ aP);
+
+}  // namespace covof

@@ -1,0 +1,44 @@
+// vof.cuh -- argument blocks for the VOF kernels (vof.cu).
+#pragma once
+#include "common.cuh"
+
+namespace covof {
+
+struct VofArgs {
+  Dims D;
+  double dx, dy, dt;
+  int method;              // COVOF_RECON_*
+  const double* C;         // field reconstructed by k_vof_reconstruct / k_vof_ring
+  double* seg;             // 3 * (nx+2)*(ny+2), AoS {nx, ny, alpha}
+  const double* Cn;        // C at time n (dilatation indicator source)
+  const double* u;
+  const double* v;
+};
+
+struct PropsArgs {
+  Dims D;
+  int two_phase;
+  double rho1, rho2, mu1, mu2;
+  double* C; double* rho; double* rho_u; double* rho_v; double* mu; double* mu_node;
+};
+
+struct CsfArgs {
+  Dims D;
+  double dx, dy, sigma;
+  const double* C;
+  double* nxv; double* nyv; double* kappa;   // scratch, zero ghost ring
+  double* fx; double* fy; double* curv;
+};
+
+__global__ void k_vof_reconstruct(VofArgs a);
+__global__ void k_vof_ring(VofArgs a);
+__global__ void k_vof_pass(VofArgs a, int dir, int clamp, const double* __restrict__ Cin,
+                           double* __restrict__ Cout);
+__global__ void k_vof_bc(Dims D, double* __restrict__ C);
+__global__ void k_props_cells(PropsArgs a);
+__global__ void k_props_faces(PropsArgs a);
+__global__ void k_csf_normals(CsfArgs a);
+__global__ void k_csf_kappa(CsfArgs a);
+__global__ void k_csf_force(CsfArgs a);
+
+}  // namespace covof

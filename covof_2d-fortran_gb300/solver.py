@@ -1,0 +1,245 @@
+"""Host-side mirror of the reference's hot-path subroutines over the C ABI.
+
+Arrays follow the reference layout: a Fortran (0:nx+1, 0:ny+1) array is a
+C-contiguous numpy array of shape (ny+2, nx+2) with a[j, i] == f(i, j); the
+two are the same bytes.  Method names follow the reference:
+
+* ``sim_solve_standard_projection`` -- src/module_simulation.f90:2424-2666
+* ``advect_vof``                    -- src/module_interface_vof.f90:792-825
+* ``advect_vof_weymouth_yue``       -- src/module_interface_vof.f90:1162-1377
+* ``reconstruct_interface``         -- src/module_interface_reconstruction.f90:580-683
+* ``update_physical_properties``    -- src/module_interface_vof.f90:479-616
+* ``compute_curvature_and_csf``     -- src/module_interface_vof.f90:627-789
+
+Error behaviour mirrors the reference: a Krylov loop that stops on its
+iteration cap or on a breakdown guard still returns its iterate (the status
+is returned, not raised); invalid arguments, unsupported options, CUDA errors
+and device-side wait timeouts raise CovofError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+from .capi import CovofError, Params
+
+_RAISE = {capi.INVALID, capi.UNSUPPORTED, capi.CUDA_ERROR, capi.TIMEOUT}
+
+
+def _ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+        raise TypeError("fields must be C-contiguous float64 numpy arrays of shape (ny+2, nx+2)")
+    return a.ctypes.data
+
+
+def _dptr(t):
+    """Device pointer of a torch CUDA tensor (float64, contiguous) or an int."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    if not t.is_cuda or not t.is_contiguous():
+        raise TypeError("device arguments must be contiguous CUDA tensors")
+    return t.data_ptr()
+
+
+def new_field(p: Params, value: float = 0.0) -> np.ndarray:
+    return np.full((p.ny + 2, p.nx + 2), value, dtype=np.float64)
+
+
+@dataclass
+class Fields:
+    """The subset of flow_fields_t (src/module_fields.f90:27-92) on the hot path,
+    with reset_fields defaults (:232-278)."""
+    u: np.ndarray
+    v: np.ndarray
+    p: np.ndarray
+    C: np.ndarray
+    rho: np.ndarray
+    rho_u: np.ndarray
+    rho_v: np.ndarray
+    mu: np.ndarray
+    mu_node: np.ndarray
+    fx_sigma: np.ndarray
+    fy_sigma: np.ndarray
+    curvature: np.ndarray
+    u_old: np.ndarray
+    v_old: np.ndarray
+
+    @classmethod
+    def allocate(cls, p: Params) -> "Fields":
+        z = lambda val=0.0: new_field(p, val)  # noqa: E731
+        return cls(u=z(), v=z(), p=z(), C=z(1.0), rho=z(1.0), rho_u=z(1.0), rho_v=z(1.0),
+                   mu=z(1.0e-3), mu_node=z(1.0e-3), fx_sigma=z(), fy_sigma=z(), curvature=z(),
+                   u_old=z(), v_old=z())
+
+    def copy(self) -> "Fields":
+        return Fields(**{k: getattr(self, k).copy() for k in self.__dataclass_fields__})
+
+
+class Solver:
+    """One handle (device buffers + stream) for one mesh and parameter set."""
+
+    def __init__(self, params: Params):
+        self.lib = capi.load_library()
+        self.params = params.copy()
+        h = C.c_void_p()
+        st = self.lib.covof_create(C.byref(self.params), C.byref(h))
+        if st != capi.OK:
+            raise CovofError(st, "covof_create")
+        self.h = h
+
+    # -- life cycle -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.covof_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int, where: str) -> int:
+        if st in _RAISE:
+            raise CovofError(st, where)
+        return st
+
+    @property
+    def stream_ptr(self) -> int:
+        s = C.c_void_p()
+        self.lib.covof_get_stream(self.h, C.byref(s))
+        return s.value or 0
+
+    def last_solve_ms(self) -> float:
+        ms = C.c_double()
+        self.lib.covof_last_solve_ms(self.h, C.byref(ms))
+        return ms.value
+
+    def last_refine_steps(self) -> int:
+        n = C.c_int()
+        self.lib.covof_last_refine_steps(self.h, C.byref(n))
+        return n.value
+
+    @property
+    def vof_step_count(self) -> int:
+        n = C.c_int()
+        self.lib.covof_get_vof_step_count(self.h, C.byref(n))
+        return n.value
+
+    @vof_step_count.setter
+    def vof_step_count(self, n: int):
+        self._check(self.lib.covof_set_vof_step_count(self.h, int(n)), "set_vof_step_count")
+
+    # -- STANDARD_PROJECTION --------------------------------------------------
+    def sim_solve_standard_projection(self, dt: float, f: Fields):
+        """One SP step on host fields; returns (total_iters, poisson_relres, status)."""
+        it, rr = C.c_int(), C.c_double()
+        st = self.lib.covof_sp_step(self.h, dt, _ptr(f.u), _ptr(f.v), _ptr(f.p), _ptr(f.rho_u),
+                                    _ptr(f.rho_v), _ptr(f.mu), _ptr(f.mu_node), _ptr(f.fx_sigma),
+                                    _ptr(f.fy_sigma), _ptr(f.u_old), _ptr(f.v_old),
+                                    C.byref(it), C.byref(rr))
+        return it.value, rr.value, self._check(st, "covof_sp_step")
+
+    def predictor(self, dt: float, f: Fields):
+        it = C.c_int()
+        st = self.lib.covof_predictor(self.h, dt, _ptr(f.u), _ptr(f.v), _ptr(f.rho_u), _ptr(f.rho_v),
+                                      _ptr(f.mu), _ptr(f.mu_node), _ptr(f.fx_sigma), _ptr(f.fy_sigma),
+                                      _ptr(f.u_old), _ptr(f.v_old), C.byref(it))
+        return it.value, self._check(st, "covof_predictor")
+
+    def momentum_apply(self, dt, xu, xv, u_n, v_n, rho_u, rho_v, mu, mu_node):
+        yu = np.zeros_like(xu)
+        yv = np.zeros_like(xv)
+        st = self.lib.covof_momentum_apply(self.h, dt, _ptr(xu), _ptr(xv), _ptr(yu), _ptr(yv),
+                                           _ptr(u_n), _ptr(v_n), _ptr(rho_u), _ptr(rho_v),
+                                           _ptr(mu), _ptr(mu_node))
+        self._check(st, "covof_momentum_apply")
+        return yu, yv
+
+    def poisson_solve(self, dt, u_star, v_star, rho_u, rho_v, p):
+        it, rr = C.c_int(), C.c_double()
+        st = self.lib.covof_poisson_solve(self.h, dt, _ptr(u_star), _ptr(v_star), _ptr(rho_u),
+                                          _ptr(rho_v), _ptr(p), C.byref(it), C.byref(rr))
+        return it.value, rr.value, self._check(st, "covof_poisson_solve")
+
+    def poisson_solve_rhs(self, dt, b, rho_u, rho_v, p):
+        it, rr = C.c_int(), C.c_double()
+        st = self.lib.covof_poisson_solve_rhs(self.h, dt, _ptr(b), _ptr(rho_u), _ptr(rho_v), _ptr(p),
+                                              C.byref(it), C.byref(rr))
+        return it.value, rr.value, self._check(st, "covof_poisson_solve_rhs")
+
+    def poisson_apply(self, dt, rho_u, rho_v, x):
+        y = np.zeros_like(x)
+        st = self.lib.covof_poisson_apply(self.h, dt, _ptr(rho_u), _ptr(rho_v), _ptr(x), _ptr(y))
+        self._check(st, "covof_poisson_apply")
+        return y
+
+    def project_correct(self, dt, u, v, p, rho_u, rho_v):
+        st = self.lib.covof_project_correct(self.h, dt, _ptr(u), _ptr(v), _ptr(p), _ptr(rho_u), _ptr(rho_v))
+        self._check(st, "covof_project_correct")
+
+    # device-resident variants (torch CUDA tensors or raw device pointers)
+    def poisson_solve_rhs_dev(self, dt, b, rho_u, rho_v, p):
+        it, rr = C.c_int(), C.c_double()
+        st = self.lib.covof_poisson_solve_rhs_dev(self.h, dt, _dptr(b), _dptr(rho_u), _dptr(rho_v),
+                                                  _dptr(p), C.byref(it), C.byref(rr))
+        return it.value, rr.value, self._check(st, "covof_poisson_solve_rhs_dev")
+
+    def poisson_solve_dev(self, dt, u_star, v_star, rho_u, rho_v, p):
+        it, rr = C.c_int(), C.c_double()
+        st = self.lib.covof_poisson_solve_dev(self.h, dt, _dptr(u_star), _dptr(v_star), _dptr(rho_u),
+                                              _dptr(rho_v), _dptr(p), C.byref(it), C.byref(rr))
+        return it.value, rr.value, self._check(st, "covof_poisson_solve_dev")
+
+    def sp_step_dev(self, dt, u, v, p, rho_u, rho_v, mu, mu_node, fx, fy, u_old, v_old):
+        it, rr = C.c_int(), C.c_double()
+        st = self.lib.covof_sp_step_dev(self.h, dt, _dptr(u), _dptr(v), _dptr(p), _dptr(rho_u),
+                                        _dptr(rho_v), _dptr(mu), _dptr(mu_node), _dptr(fx), _dptr(fy),
+                                        _dptr(u_old), _dptr(v_old), C.byref(it), C.byref(rr))
+        return it.value, rr.value, self._check(st, "covof_sp_step_dev")
+
+    def vof_advect_dev(self, dt, u, v, Cf, rho, rho_u, rho_v, mu, mu_node, fx, fy, curv):
+        st = self.lib.covof_vof_advect_dev(self.h, dt, _dptr(u), _dptr(v), _dptr(Cf), _dptr(rho),
+                                           _dptr(rho_u), _dptr(rho_v), _dptr(mu), _dptr(mu_node),
+                                           _dptr(fx), _dptr(fy), _dptr(curv))
+        return self._check(st, "covof_vof_advect_dev")
+
+    # -- geometric VOF ----------------------------------------------------------
+    def reconstruct_interface(self, Cf: np.ndarray) -> np.ndarray:
+        seg = np.zeros(Cf.shape + (3,), dtype=np.float64)
+        st = self.lib.covof_vof_reconstruct(self.h, _ptr(Cf), seg.ctypes.data)
+        self._check(st, "covof_vof_reconstruct")
+        return seg
+
+    def advect_vof_weymouth_yue(self, dt: float, u, v, Cf, x_first: bool):
+        st = self.lib.covof_vof_wy_step(self.h, dt, int(bool(x_first)), _ptr(u), _ptr(v), _ptr(Cf))
+        self._check(st, "covof_vof_wy_step")
+
+    def advect_vof(self, dt: float, f: Fields):
+        st = self.lib.covof_vof_advect(self.h, dt, _ptr(f.u), _ptr(f.v), _ptr(f.C), _ptr(f.rho),
+                                       _ptr(f.rho_u), _ptr(f.rho_v), _ptr(f.mu), _ptr(f.mu_node),
+                                       _ptr(f.fx_sigma), _ptr(f.fy_sigma), _ptr(f.curvature))
+        self._check(st, "covof_vof_advect")
+
+    def update_physical_properties(self, f: Fields):
+        st = self.lib.covof_update_physical_properties(self.h, _ptr(f.C), _ptr(f.rho), _ptr(f.rho_u),
+                                                       _ptr(f.rho_v), _ptr(f.mu), _ptr(f.mu_node))
+        self._check(st, "covof_update_physical_properties")
+
+    def compute_curvature_and_csf(self, f: Fields):
+        st = self.lib.covof_compute_curvature_and_csf(self.h, _ptr(f.C), _ptr(f.fx_sigma),
+                                                      _ptr(f.fy_sigma), _ptr(f.curvature))
+        self._check(st, "covof_compute_curvature_and_csf")

@@ -1,0 +1,218 @@
+/*
+ * covof_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the COVOF 2D
+ * per-timestep hot path: the STANDARD_PROJECTION step (momentum predictor,
+ * variable-density pressure Poisson solve, velocity correction) and the
+ * geometric VOF step (PLIC / ELVIRA reconstruction + Weymouth-Yue fluxes).
+ *
+ * Layout contract (identical to the reference's flow_fields_t,
+ * src/module_fields.f90:129-169): every field argument is a Fortran array
+ * dimensioned (0:nx+1, 0:ny+1), column-major, i fastest, one ghost layer,
+ * i.e. (nx+2)*(ny+2) contiguous doubles with element (i,j) at i + (nx+2)*j.
+ * u(i,j) is the normal velocity on the west face of cell i (x = (i-1)*dx),
+ * v(i,j) on the south face of cell j (y = (j-1)*dy); p, C, rho, mu at cell
+ * centres; mu_node(i,j) at the south-west node of cell (i,j).
+ *
+ * Host-pointer entry points copy in, compute on the device and copy out;
+ * the caller owns every host array and nothing is retained past the call.
+ * The *_dev entry points take device pointers with the same layout and run on
+ * the handle's stream; all calls are synchronous on return.  A handle is not
+ * thread-safe.  No entry point throws; every one returns a COVOF_* status.
+ */
+#ifndef COVOF_GPU_H
+#define COVOF_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define COVOF_ABI_VERSION 1
+
+/* Status codes.  MAXITER and BREAKDOWN mirror the reference's silent Krylov
+ * exits (src/module_linear_solvers.f90:565,576,715; src/module_simulation.f90:2558):
+ * the result is still written, the code tells the caller why the loop ended. */
+enum {
+  COVOF_OK = 0,
+  COVOF_MAXITER = 1,
+  COVOF_BREAKDOWN = 2,
+  COVOF_NAN = 3,
+  COVOF_TIMEOUT = 4,      /* a bounded device-side wait gave up */
+  COVOF_UNSUPPORTED = 5,  /* option outside the implemented path */
+  COVOF_CUDA_ERROR = 6,
+  COVOF_INVALID = 7       /* bad argument (null pointer, size, code) */
+};
+
+/* Boundary codes: same values as BC_* in src/module_constants.f90:41-44. */
+enum { COVOF_BC_DIRICHLET = 1, COVOF_BC_NEUMANN = 2, COVOF_BC_PERIODIC = 3, COVOF_BC_FREESLIP = 4 };
+/* Linear solvers: LINEAR_* in src/module_constants.f90:53-58. */
+enum { COVOF_LINEAR_BICGSTAB2 = 1, COVOF_LINEAR_BICGSTAB = 2, COVOF_LINEAR_CG = 3 };
+/* Preconditioners: PRECOND_* in src/module_constants.f90:67-72.
+ * ILU0 is the same diagonal scaling as JACOBI in the reference
+ * (src/module_linear_solvers.f90:280-304).  SSOR is accepted for the pressure
+ * Poisson only, where it names the reference's symmetric Gauss-Seidel sweep
+ * pair (src/module_simulation.f90:2709-2758). */
+enum { COVOF_PRECOND_NONE = 0, COVOF_PRECOND_JACOBI = 1, COVOF_PRECOND_SSOR = 2, COVOF_PRECOND_ILU0 = 3 };
+/* Convective schemes: CONV_* in src/module_constants.f90:76-78. */
+enum { COVOF_CONV_UPWIND = 1, COVOF_CONV_CENTERED = 2 };
+/* Interface reconstruction (cfg%reconstruction_method). */
+enum { COVOF_RECON_PLIC = 0, COVOF_RECON_ELVIRA = 1 };
+/* Pressure gauge.  REFERENCE: 1e-12*dvol diagonal shift + mean removal
+ * (src/module_simulation.f90:2531,2579-2582).  PINNED: same operator with
+ * cell (1,1) held at p = 0 (no mean removal). */
+enum { COVOF_GAUGE_REFERENCE = 0, COVOF_GAUGE_PINNED = 1 };
+/* Poisson arithmetic.  FP64: plain FP64 PCG.  MIXED: FP32 PCG inner solves
+ * inside FP64 iterative refinement (FP64 residual, FP64 solution). */
+enum { COVOF_PREC_FP64 = 0, COVOF_PREC_MIXED = 1 };
+
+/* Plain-old-data parameter block (the subset of config_t,
+ * src/module_config.f90:31-184, that the hot path reads). */
+typedef struct covof_params {
+  int nx, ny;            /* cells */
+  double dx, dy;         /* mesh%dx, mesh%dy */
+  int bc_type[4];        /* left, right, bottom, top: COVOF_BC_* */
+  double bc_u[4];        /* wall velocity (cfg%bc_*%u) */
+  double bc_v[4];        /* wall velocity (cfg%bc_*%v) */
+  /* momentum predictor (cfg%linear_solver, precond_type, tol, max_iter) */
+  int linear_solver;
+  int precond;
+  int use_precond;
+  int max_iter;
+  double tol;
+  int enable_convection;
+  int convective_scheme;
+  /* pressure Poisson */
+  int p_precond;         /* JACOBI (GPU and oracle) or SSOR (oracle only) */
+  int p_max_iter;
+  int p_gauge;
+  int p_precision;
+  double p_tol;          /* ||r||/||b|| target */
+  double p_inner_tol;    /* MIXED: relative reduction asked of each FP32 inner solve */
+  int p_inner_max_iter;  /* MIXED: cap per inner solve */
+  int p_max_refine;      /* MIXED: cap on outer refinement steps */
+  /* two-phase properties */
+  int enable_two_phase;
+  int enable_surface_tension;
+  double rho1, rho2, mu1, mu2, sigma, gx, gy;
+  int recon;             /* COVOF_RECON_* */
+} covof_params;
+
+typedef struct covof_handle covof_handle;
+
+/* Reference-default parameters for an nx*ny mesh of lx*ly: no-slip walls,
+ * BiCGSTAB(2)+Jacobi tol 1e-5 / 300 its (src/module_config.f90:576-636),
+ * UPWIND, Poisson Jacobi-PCG tol 1e-7 / 1000 its, reference gauge, FP64. */
+void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly);
+
+int covof_create(const covof_params* params, covof_handle** out);
+int covof_destroy(covof_handle* h);
+const char* covof_strerror(int status);
+int covof_abi_version(void);
+/* Device the handle was created on and the number of SMs it uses. */
+int covof_device_info(const covof_handle* h, int* device, int* sm_count);
+
+/* ---- STANDARD_PROJECTION --------------------------------------------- */
+
+/* Whole SP step: replaces sim_solve_standard_projection
+ * (src/module_simulation.f90:2424-2666).  u, v hold u^n on entry and u^{n+1}
+ * on exit (ghosts set by the non-homogeneous velocity BC, as
+ * src/module_mpi_comm.f90:290-537); p is the warm start on entry and the
+ * projected pressure on exit.  total_iters = predictor + Poisson iterations. */
+int covof_sp_step(covof_handle* h, double dt, double* u, double* v, double* p,
+                  const double* rho_u, const double* rho_v, const double* mu,
+                  const double* mu_node, const double* fx_sigma, const double* fy_sigma,
+                  const double* u_old, const double* v_old,
+                  int* total_iters, double* final_relres);
+int covof_sp_step_dev(covof_handle* h, double dt, double* u, double* v, double* p,
+                      const double* rho_u, const double* rho_v, const double* mu,
+                      const double* mu_node, const double* fx_sigma, const double* fy_sigma,
+                      const double* u_old, const double* v_old,
+                      int* total_iters, double* final_relres);
+
+/* Momentum predictor only (src/module_simulation.f90:2454-2470): u, v in/out. */
+int covof_predictor(covof_handle* h, double dt, double* u, double* v,
+                    const double* rho_u, const double* rho_v, const double* mu,
+                    const double* mu_node, const double* fx_sigma, const double* fy_sigma,
+                    const double* u_old, const double* v_old, int* iters);
+int covof_predictor_dev(covof_handle* h, double dt, double* u, double* v,
+                        const double* rho_u, const double* rho_v, const double* mu,
+                        const double* mu_node, const double* fx_sigma, const double* fy_sigma,
+                        const double* u_old, const double* v_old, int* iters);
+
+/* Momentum operator y = A x on one (u,v) pair (ns_apply_system_matrix,
+ * src/module_navier_stokes.f90:380-780), fields_old = (u_n, v_n, rho_u, rho_v,
+ * mu, mu_node); x and y are ghosted (u,v) arrays, only DOF entries of y are
+ * written.  Exposed for parity tests of the operator itself. */
+int covof_momentum_apply(covof_handle* h, double dt, const double* xu, const double* xv,
+                         double* yu, double* yv, const double* u_n, const double* v_n,
+                         const double* rho_u, const double* rho_v, const double* mu,
+                         const double* mu_node);
+
+/* Pressure Poisson from a predicted velocity (src/module_simulation.f90:2476-2584):
+ * assembly, PCG, gauge.  p: warm start in, solution out (interior). */
+int covof_poisson_solve(covof_handle* h, double dt, const double* u_star, const double* v_star,
+                        const double* rho_u, const double* rho_v, double* p,
+                        int* iters, double* relres);
+int covof_poisson_solve_dev(covof_handle* h, double dt, const double* u_star, const double* v_star,
+                            const double* rho_u, const double* rho_v, double* p,
+                            int* iters, double* relres);
+/* Same operator with an explicit right-hand side b (ghosted layout, interior
+ * read) in place of -div(u*): the standalone variable-density Poisson. */
+int covof_poisson_solve_rhs(covof_handle* h, double dt, const double* b,
+                            const double* rho_u, const double* rho_v, double* p,
+                            int* iters, double* relres);
+int covof_poisson_solve_rhs_dev(covof_handle* h, double dt, const double* b,
+                                const double* rho_u, const double* rho_v, double* p,
+                                int* iters, double* relres);
+/* Velocity correction u -= dt/rho_u dp/dx, v -= dt/rho_v dp/dy
+ * (src/module_simulation.f90:2586-2660). */
+int covof_project_correct(covof_handle* h, double dt, double* u, double* v, const double* p,
+                          const double* rho_u, const double* rho_v);
+
+/* Poisson operator y = A x (interior of y written), assembled from rho_u,
+ * rho_v and dt as in covof_poisson_solve.  Exposed for parity tests of the
+ * operator (src/module_simulation.f90:2668-2707). */
+int covof_poisson_apply(covof_handle* h, double dt, const double* rho_u, const double* rho_v,
+                        const double* x, double* y);
+
+/* The handle's CUDA stream (a blocking stream: it orders after work on the
+ * legacy default stream) and the device time of the last Poisson solve
+ * kernel, measured with CUDA events on that stream. */
+int covof_get_stream(const covof_handle* h, void** stream);
+int covof_last_solve_ms(const covof_handle* h, double* ms);
+/* Outer FP64 refinement steps of the last MIXED Poisson solve. */
+int covof_last_refine_steps(const covof_handle* h, int* steps);
+
+/* ---- geometric VOF ---------------------------------------------------- */
+
+/* reconstruct_interface (src/module_interface_reconstruction.f90:580-683):
+ * seg = 3*(nx+2)*(ny+2) doubles, AoS {nx, ny, alpha} per cell. */
+int covof_vof_reconstruct(covof_handle* h, const double* C, double* seg);
+int covof_vof_reconstruct_dev(covof_handle* h, const double* C, double* seg);
+/* advect_vof_weymouth_yue (src/module_interface_vof.f90:1162-1377) with the
+ * pass order given explicitly (x_first = mod(vof_step_count,2)==0). */
+int covof_vof_wy_step(covof_handle* h, double dt, int x_first, const double* u, const double* v,
+                      double* C);
+int covof_vof_wy_step_dev(covof_handle* h, double dt, int x_first, const double* u,
+                          const double* v, double* C);
+/* advect_vof (src/module_interface_vof.f90:792-825) for WEYMOUTH_YUE: the WY
+ * step with the handle's vof_step_count, the count increment, the VOF BC,
+ * update_physical_properties and compute_curvature_and_csf. */
+int covof_vof_advect(covof_handle* h, double dt, const double* u, const double* v, double* C,
+                     double* rho, double* rho_u, double* rho_v, double* mu, double* mu_node,
+                     double* fx_sigma, double* fy_sigma, double* curvature);
+int covof_vof_advect_dev(covof_handle* h, double dt, const double* u, const double* v, double* C,
+                         double* rho, double* rho_u, double* rho_v, double* mu, double* mu_node,
+                         double* fx_sigma, double* fy_sigma, double* curvature);
+int covof_get_vof_step_count(const covof_handle* h, int* count);
+int covof_set_vof_step_count(covof_handle* h, int count);
+/* update_physical_properties (src/module_interface_vof.f90:479-616); C's
+ * physical corners are rewritten as in the reference. */
+int covof_update_physical_properties(covof_handle* h, double* C, double* rho, double* rho_u,
+                                     double* rho_v, double* mu, double* mu_node);
+/* compute_curvature_and_csf (src/module_interface_vof.f90:627-789). */
+int covof_compute_curvature_and_csf(covof_handle* h, const double* C, double* fx_sigma,
+                                    double* fy_sigma, double* curvature);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* COVOF_GPU_H */

@@ -1,0 +1,1484 @@
+// covof_oracle.cpp -- TEST INFRASTRUCTURE ONLY (see covof_oracle.h).
+//
+// Serial FP64 CPU restatement of the COVOF 2D hot path, following the
+// reference subroutines line by line (cited per function).  Built with
+// -O2 -ffp-contract=off so that no multiply-add is fused behind our back; the
+// evaluation order of every expression follows the Fortran source (left to
+// right, parentheses respected).  np = 1 semantics throughout: the MPI halo
+// exchanges of the reference are no-ops on a single non-periodic domain
+// (src/module_mpi_comm.f90:46-56) and are omitted.
+#include "covof_oracle.h"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+enum { L = 0, R = 1, B = 2, T = 3 };
+
+struct Mesh {
+  int nx, ny;
+  double dx, dy;
+  int P;  // pitch = nx + 2
+  inline size_t id(int i, int j) const { return (size_t)j * (size_t)P + (size_t)i; }
+  // src/module_mesh.f90:177-206, single domain: i_start_global = 1
+  inline double x_face(int i) const { return (double)(i - 1) * dx; }
+  inline double y_face(int j) const { return (double)(j - 1) * dy; }
+  inline double x_center(int i) const { return ((double)(i - 1) + 0.5) * dx; }
+  inline double y_center(int j) const { return ((double)(j - 1) + 0.5) * dy; }
+};
+
+inline Mesh mesh_of(const covof_params* p) {
+  Mesh m;
+  m.nx = p->nx; m.ny = p->ny; m.dx = p->dx; m.dy = p->dy; m.P = p->nx + 2;
+  return m;
+}
+
+inline bool is_wall(const covof_params* p, int side) {
+  return p->bc_type[side] == COVOF_BC_DIRICHLET || p->bc_type[side] == COVOF_BC_FREESLIP;
+}
+
+int check_params(const covof_params* p, bool allow_neumann) {
+  if (!p || p->nx < 2 || p->ny < 2 || !(p->dx > 0) || !(p->dy > 0)) return COVOF_INVALID;
+  for (int s = 0; s < 4; ++s) {
+    int t = p->bc_type[s];
+    if (t == COVOF_BC_PERIODIC) return COVOF_UNSUPPORTED;
+    if (t == COVOF_BC_NEUMANN && !allow_neumann) return COVOF_UNSUPPORTED;
+    if (t != COVOF_BC_DIRICHLET && t != COVOF_BC_FREESLIP && t != COVOF_BC_NEUMANN)
+      return COVOF_INVALID;
+  }
+  return COVOF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Fused hypot: sqrt(x^2+y^2) with an FMA-based residual correction (after
+// C. F. Borges, "An improved algorithm for hypot(a,b)", ACM TOMS 2021).
+// Stands in for the Fortran intrinsic; bit-identical to the GPU's version.
+double fhypot(double x, double y) {
+  double ax = std::fabs(x), ay = std::fabs(y);
+  if (std::isinf(ax) || std::isinf(ay)) return INFINITY;
+  if (std::isnan(ax) || std::isnan(ay)) return ax + ay;
+  if (ax < ay) std::swap(ax, ay);
+  if (ay == 0.0) return ax;
+  if (ay < ax * 0x1p-30) return ax;  // ay^2 below half an ulp of ax^2
+  double scale = 1.0;
+  if (ax > 0x1p+500) { ax *= 0x1p-600; ay *= 0x1p-600; scale = 0x1p+600; }
+  else if (ax < 0x1p-450) { ax *= 0x1p+600; ay *= 0x1p+600; scale = 0x1p-600; }
+  double h = std::sqrt(std::fma(ax, ax, ay * ay));
+  double h_sq = h * h, h_lo = std::fma(h, h, -h_sq);
+  double x_sq = ax * ax, x_lo = std::fma(ax, ax, -x_sq);
+  double y_sq = ay * ay, y_lo = std::fma(ay, ay, -y_sq);
+  double r = ((x_sq - h_sq) + y_sq) + ((x_lo - h_lo) + y_lo);
+  h = h + r / (2.0 * h);
+  return h * scale;
+}
+
+// ---------------------------------------------------------------------------
+// src/module_interface_reconstruction.f90:33-101  cut_box_area
+double cut_box_area(double xmin, double xmax, double ymin, double ymax, double nx, double ny,
+                    double alpha) {
+  if ((xmax - xmin) <= 1.0e-14 || (ymax - ymin) <= 1.0e-14) return 0.0;
+  double bx[4] = {xmin, xmax, xmax, xmin};
+  double by[4] = {ymin, ymin, ymax, ymax};
+  double d[4];
+  for (int i = 0; i < 4; ++i) d[i] = nx * bx[i] + ny * by[i] + alpha;
+  double cx[8], cy[8];
+  int n = 0;
+  for (int i = 0; i < 4; ++i) {
+    int ni = (i + 1) % 4;
+    double d1 = d[i], d2 = d[ni];
+    if (d1 <= 0.0) {
+      if (d2 <= 0.0) {
+        cx[n] = bx[ni]; cy[n] = by[ni]; ++n;
+      } else {
+        double t = -d1 / (d2 - d1);
+        cx[n] = bx[i] + t * (bx[ni] - bx[i]);
+        cy[n] = by[i] + t * (by[ni] - by[i]);
+        ++n;
+      }
+    } else {
+      if (d2 <= 0.0) {
+        double t = -d1 / (d2 - d1);
+        cx[n] = bx[i] + t * (bx[ni] - bx[i]);
+        cy[n] = by[i] + t * (by[ni] - by[i]);
+        ++n;
+        cx[n] = bx[ni]; cy[n] = by[ni]; ++n;
+      }
+    }
+  }
+  if (n < 3) return 0.0;
+  double s = 0.0;
+  for (int q = 0; q < n; ++q) {
+    int nq = (q + 1) % n;
+    s = s + (cx[q] * cy[nq] - cx[nq] * cy[q]);
+  }
+  return 0.5 * std::fabs(s);
+}
+
+// src/module_interface_reconstruction.f90:105-147  compute_alpha (45-step bisection)
+double compute_alpha(double xmin, double xmax, double ymin, double ymax, double nx, double ny,
+                     double c_target) {
+  double total_area = (xmax - xmin) * (ymax - ymin);
+  if (c_target <= 1.0e-7) return 1.0e9;
+  if (c_target >= 1.0 - 1.0e-7) return -1.0e9;
+  double target_area = std::max(0.0, std::min(1.0, c_target)) * total_area;
+  double v1 = nx * xmin + ny * ymin;
+  double v2 = nx * xmax + ny * ymin;
+  double v3 = nx * xmax + ny * ymax;
+  double v4 = nx * xmin + ny * ymax;
+  double min_val = std::min(v1, std::min(v2, std::min(v3, v4)));
+  double max_val = std::max(v1, std::max(v2, std::max(v3, v4)));
+  double lo = -max_val - 1.0e-12;
+  double hi = -min_val + 1.0e-12;
+  for (int it = 0; it < 45; ++it) {
+    double mid = 0.5 * (lo + hi);
+    double a = cut_box_area(xmin, xmax, ymin, ymax, nx, ny, mid);
+    if (a < target_area) hi = mid; else lo = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+// ---------------------------------------------------------------------------
+// src/module_mpi_comm.f90:290-537 apply_velocity_bc (np=1, constant walls,
+// no PARABOLIC / JET_INLET / obstacle profiles).
+void velocity_bc(const covof_params* prm, const Mesh& m, double* u, double* v, bool homog) {
+  const int nx = m.nx, ny = m.ny;
+  double ul = homog ? 0.0 : prm->bc_u[L], vl = homog ? 0.0 : prm->bc_v[L];
+  double ur = homog ? 0.0 : prm->bc_u[R], vr = homog ? 0.0 : prm->bc_v[R];
+  double ub = homog ? 0.0 : prm->bc_u[B], vb = homog ? 0.0 : prm->bc_v[B];
+  double ut = homog ? 0.0 : prm->bc_u[T], vt = homog ? 0.0 : prm->bc_v[T];
+  // west (:339-373)
+  for (int j = 1; j <= ny; ++j) {
+    int t = prm->bc_type[L];
+    if (t == COVOF_BC_DIRICHLET) {
+      if (!homog) u[m.id(1, j)] = ul;
+      u[m.id(0, j)] = ul;
+      v[m.id(0, j)] = 2.0 * vl - v[m.id(1, j)];
+    } else if (t == COVOF_BC_FREESLIP) {
+      if (!homog) u[m.id(1, j)] = 0.0;
+      u[m.id(0, j)] = 0.0;
+      v[m.id(0, j)] = v[m.id(1, j)];
+    } else if (t == COVOF_BC_NEUMANN) {
+      u[m.id(0, j)] = u[m.id(1, j)];
+      v[m.id(0, j)] = v[m.id(1, j)];
+    }
+  }
+  // east (:377-394)
+  for (int j = 1; j <= ny; ++j) {
+    int t = prm->bc_type[R];
+    if (t == COVOF_BC_DIRICHLET) {
+      if (!homog) u[m.id(nx + 1, j)] = ur;
+      v[m.id(nx + 1, j)] = 2.0 * vr - v[m.id(nx, j)];
+    } else if (t == COVOF_BC_FREESLIP) {
+      if (!homog) u[m.id(nx + 1, j)] = 0.0;
+      v[m.id(nx + 1, j)] = v[m.id(nx, j)];
+    } else if (t == COVOF_BC_NEUMANN) {
+      if (!homog) u[m.id(nx + 1, j)] = u[m.id(nx, j)];
+      v[m.id(nx + 1, j)] = v[m.id(nx, j)];
+    }
+  }
+  // south (:397-425)
+  for (int i = 1; i <= nx; ++i) {
+    int t = prm->bc_type[B];
+    if (t == COVOF_BC_DIRICHLET) {
+      if (!homog) v[m.id(i, 1)] = vb;
+      v[m.id(i, 0)] = vb;
+      if (ny >= 2)
+        u[m.id(i, 0)] = (8.0 * ub - 6.0 * u[m.id(i, 1)] + u[m.id(i, 2)]) / 3.0;
+      else
+        u[m.id(i, 0)] = 2.0 * ub - u[m.id(i, 1)];
+    } else if (t == COVOF_BC_FREESLIP) {
+      if (!homog) v[m.id(i, 1)] = 0.0;
+      v[m.id(i, 0)] = 0.0;
+      u[m.id(i, 0)] = u[m.id(i, 1)];
+    } else if (t == COVOF_BC_NEUMANN) {
+      u[m.id(i, 0)] = u[m.id(i, 1)];
+      v[m.id(i, 0)] = v[m.id(i, 1)];
+    }
+  }
+  // north (:456-479)
+  for (int i = 1; i <= nx; ++i) {
+    int t = prm->bc_type[T];
+    if (t == COVOF_BC_DIRICHLET) {
+      if (!homog) v[m.id(i, ny + 1)] = vt;
+      if (ny >= 2)
+        u[m.id(i, ny + 1)] = (8.0 * ut - 6.0 * u[m.id(i, ny)] + u[m.id(i, ny - 1)]) / 3.0;
+      else
+        u[m.id(i, ny + 1)] = 2.0 * ut - u[m.id(i, ny)];
+    } else if (t == COVOF_BC_FREESLIP) {
+      if (!homog) v[m.id(i, ny + 1)] = 0.0;
+      u[m.id(i, ny + 1)] = u[m.id(i, ny)];
+    } else if (t == COVOF_BC_NEUMANN) {
+      u[m.id(i, ny + 1)] = u[m.id(i, ny)];
+      if (!homog) v[m.id(i, ny + 1)] = v[m.id(i, ny)];
+    }
+  }
+  // physical corners, non-homogeneous only (:484-500)
+  if (!homog) {
+    u[m.id(nx + 1, 0)] = u[m.id(nx + 1, 1)];
+    v[m.id(nx + 1, 0)] = v[m.id(nx, 0)];
+    u[m.id(nx + 1, ny + 1)] = u[m.id(nx + 1, ny)];
+    v[m.id(nx + 1, ny + 1)] = v[m.id(nx, ny + 1)];
+    v[m.id(0, ny + 1)] = v[m.id(1, ny + 1)];
+  }
+}
+
+// src/module_mpi_comm.f90:636-683 apply_vof_bc (np=1, no JET_INLET)
+void vof_bc(const Mesh& m, double* C) {
+  const int nx = m.nx, ny = m.ny;
+  for (int j = 1; j <= ny; ++j) {
+    C[m.id(0, j)] = C[m.id(1, j)];
+    C[m.id(nx + 1, j)] = C[m.id(nx, j)];
+  }
+  for (int i = 1; i <= nx; ++i) C[m.id(i, 0)] = C[m.id(i, 1)];
+  for (int i = 1; i <= nx; ++i) C[m.id(i, ny + 1)] = C[m.id(i, ny)];
+}
+
+// ---------------------------------------------------------------------------
+// Pressure Poisson.  Coefficient arrays are (nx, ny), index (i-1)+nx*(j-1).
+struct Poisson {
+  int nx, ny;
+  std::vector<double> aW, aE, aS, aN, aP, b;
+  inline size_t k(int i, int j) const { return (size_t)(i - 1) + (size_t)nx * (size_t)(j - 1); }
+};
+
+// src/module_simulation.f90:2483-2533 (obstacles disabled)
+void poisson_assemble(const covof_params* prm, const Mesh& m, double dt, const double* rho_u,
+                      const double* rho_v, Poisson& P) {
+  const int nx = m.nx, ny = m.ny;
+  const double dx = m.dx, dy = m.dy, dvol = dx * dy;
+  P.nx = nx; P.ny = ny;
+  size_t n = (size_t)nx * ny;
+  P.aW.assign(n, 0.0); P.aE.assign(n, 0.0); P.aS.assign(n, 0.0); P.aN.assign(n, 0.0);
+  P.aP.assign(n, 0.0); P.b.assign(n, 0.0);
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t q = P.k(i, j);
+      bool wW = (i == 1 && is_wall(prm, L));
+      if (!wW) {
+        double r = rho_u[m.id(i, j)];
+        if (r < 1.0e-12) r = 1.0;
+        P.aW[q] = (dt * dy) / (r * dx);
+      }
+      bool wE = (i == nx && is_wall(prm, R));
+      if (!wE) {
+        double r = rho_u[m.id(i + 1, j)];
+        if (r < 1.0e-12) r = 1.0;
+        P.aE[q] = (dt * dy) / (r * dx);
+      }
+      bool wS = (j == 1 && is_wall(prm, B));
+      if (!wS) {
+        double r = rho_v[m.id(i, j)];
+        if (r < 1.0e-12) r = 1.0;
+        P.aS[q] = (dt * dx) / (r * dy);
+      }
+      bool wN = (j == ny && is_wall(prm, T));
+      if (!wN) {
+        double r = rho_v[m.id(i, j + 1)];
+        if (r < 1.0e-12) r = 1.0;
+        P.aN[q] = (dt * dx) / (r * dy);
+      }
+      P.aP[q] = P.aW[q] + P.aE[q] + P.aS[q] + P.aN[q] + 1.0e-12 * dvol;
+    }
+}
+
+// src/module_simulation.f90:2484-2487 b = -div(u*)
+void poisson_rhs_from_velocity(const Mesh& m, const double* u, const double* v, Poisson& P) {
+  for (int j = 1; j <= m.ny; ++j)
+    for (int i = 1; i <= m.nx; ++i) {
+      double div = (u[m.id(i + 1, j)] - u[m.id(i, j)]) * m.dy + (v[m.id(i, j + 1)] - v[m.id(i, j)]) * m.dx;
+      P.b[P.k(i, j)] = -div;
+    }
+}
+
+// src/module_simulation.f90:2668-2707 poisson_matvec (non-periodic)
+void poisson_matvec(const Poisson& P, const double* x, double* y) {
+  const int nx = P.nx, ny = P.ny;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t q = P.k(i, j);
+      double val = P.aP[q] * x[q];
+      if (i > 1) val = val - P.aW[q] * x[q - 1];
+      if (i < nx) val = val - P.aE[q] * x[q + 1];
+      if (j > 1) val = val - P.aS[q] * x[q - nx];
+      if (j < ny) val = val - P.aN[q] * x[q + nx];
+      y[q] = val;
+    }
+}
+
+void poisson_matvec_omp(const Poisson& P, const double* x, double* y) {
+  const int nx = P.nx, ny = P.ny;
+#pragma omp parallel for schedule(static)
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t q = P.k(i, j);
+      double val = P.aP[q] * x[q];
+      if (i > 1) val = val - P.aW[q] * x[q - 1];
+      if (i < nx) val = val - P.aE[q] * x[q + 1];
+      if (j > 1) val = val - P.aS[q] * x[q - nx];
+      if (j < ny) val = val - P.aN[q] * x[q + nx];
+      y[q] = val;
+    }
+}
+
+// src/module_simulation.f90:2709-2758 poisson_ssor (SGS, omega = 1).
+// pinned: cell (1,1) is held at zero in both sweeps.
+void poisson_sgs(const Poisson& P, const double* r, double* z, bool pinned) {
+  const int nx = P.nx, ny = P.ny;
+  std::fill(z, z + (size_t)nx * ny, 0.0);
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t q = P.k(i, j);
+      double val = r[q];
+      if (i > 1) val = val + P.aW[q] * z[q - 1];
+      if (j > 1) val = val + P.aS[q] * z[q - nx];
+      z[q] = val / P.aP[q];
+      if (pinned && i == 1 && j == 1) z[q] = 0.0;
+    }
+  for (int j = ny; j >= 1; --j)
+    for (int i = nx; i >= 1; --i) {
+      size_t q = P.k(i, j);
+      double val = P.aP[q] * z[q];
+      if (i < nx) val = val + P.aE[q] * z[q + 1];
+      if (j < ny) val = val + P.aN[q] * z[q + nx];
+      z[q] = val / P.aP[q];
+      if (pinned && i == 1 && j == 1) z[q] = 0.0;
+    }
+}
+
+// Jacobi alternative (diagonal scaling by a_P), an option of this build.
+void poisson_jacobi(const Poisson& P, const double* r, double* z, bool pinned) {
+  size_t n = (size_t)P.nx * P.ny;
+  for (size_t q = 0; q < n; ++q) z[q] = r[q] / P.aP[q];
+  if (pinned) z[0] = 0.0;
+}
+
+// src/module_simulation.f90:2760-2774 dot / norm (sequential, column-major order)
+double dot(const double* x, const double* y, size_t n) {
+  double s = 0.0;
+  for (size_t q = 0; q < n; ++q) s = s + x[q] * y[q];
+  return s;
+}
+double dot_omp(const double* x, const double* y, size_t n) {
+  double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+  for (long q = 0; q < (long)n; ++q) s += x[q] * y[q];
+  return s;
+}
+
+// src/module_simulation.f90:2535-2584  PCG + gauge.  x: (nx,ny) warm start / result.
+int poisson_pcg(const covof_params* prm, Poisson& P, std::vector<double>& x, int* iters_out,
+                double* relres_out, int nthreads, int fixed_iters) {
+  const size_t n = (size_t)P.nx * P.ny;
+  const bool pinned = prm->p_gauge == COVOF_GAUGE_PINNED;
+  const bool sgs = prm->p_precond == COVOF_PRECOND_SSOR;
+  const bool par = nthreads > 1;
+  const double tol = prm->p_tol;
+  const int max_iter = fixed_iters > 0 ? fixed_iters : prm->p_max_iter;
+#ifdef _OPENMP
+  if (par) omp_set_num_threads(nthreads);
+#endif
+  auto DOT = [&](const double* a, const double* b) { return par ? dot_omp(a, b, n) : dot(a, b, n); };
+  auto MATVEC = [&](const double* a, double* y) {
+    if (par) poisson_matvec_omp(P, a, y); else poisson_matvec(P, a, y);
+    if (pinned) y[0] = 0.0;
+  };
+  auto PREC = [&](const double* r, double* z) {
+    if (sgs) poisson_sgs(P, r, z, pinned); else poisson_jacobi(P, r, z, pinned);
+  };
+  if (pinned) { P.b[0] = 0.0; x[0] = 0.0; }
+  std::vector<double> r(n), Ap(n), z(n), d(n), Ad(n);
+  MATVEC(x.data(), Ap.data());
+  for (size_t q = 0; q < n; ++q) r[q] = P.b[q] - Ap[q];
+  double b_norm = std::sqrt(DOT(P.b.data(), P.b.data()));
+  if (b_norm < 1.0e-30) b_norm = 1.0;
+  double r_norm = std::sqrt(DOT(r.data(), r.data()));
+  int iters = 0, status = COVOF_OK;
+  bool converged = false;
+  if (fixed_iters > 0 || r_norm / b_norm > tol) {
+    PREC(r.data(), z.data());
+    d = z;
+    double rz_old = DOT(r.data(), z.data());
+    for (int it = 1; it <= max_iter; ++it) {
+      iters = iters + 1;
+      MATVEC(d.data(), Ad.data());
+      double dAd = DOT(d.data(), Ad.data());
+      if (std::fabs(dAd) < 1.0e-35) { status = COVOF_BREAKDOWN; break; }
+      double alpha = rz_old / dAd;
+      for (size_t q = 0; q < n; ++q) x[q] = x[q] + alpha * d[q];
+      for (size_t q = 0; q < n; ++q) r[q] = r[q] - alpha * Ad[q];
+      r_norm = std::sqrt(DOT(r.data(), r.data()));
+      if (std::isnan(r_norm)) { status = COVOF_NAN; break; }
+      if (fixed_iters == 0 && r_norm / b_norm <= tol) { converged = true; break; }
+      PREC(r.data(), z.data());
+      double rz_new = DOT(r.data(), z.data());
+      if (std::fabs(rz_old) < 1.0e-35) { status = COVOF_BREAKDOWN; break; }
+      double beta = rz_new / rz_old;
+      rz_old = rz_new;
+      for (size_t q = 0; q < n; ++q) d[q] = z[q] + beta * d[q];
+    }
+    if (status == COVOF_OK && !converged && fixed_iters == 0) status = COVOF_MAXITER;
+  }
+  if (!pinned) {
+    // src/module_simulation.f90:2579-2582
+    double s = 0.0;
+    for (size_t q = 0; q < n; ++q) s = s + x[q];
+    double mean = s / (double)((long long)P.nx * P.ny);
+    for (size_t q = 0; q < n; ++q) x[q] = x[q] - mean;
+  }
+  if (iters_out) *iters_out = iters;
+  if (relres_out) *relres_out = r_norm / b_norm;
+  return status;
+}
+
+int poisson_driver(const covof_params* prm, double dt, const double* u_star, const double* v_star,
+                   const double* b_in, const double* rho_u, const double* rho_v, double* p,
+                   int* iters, double* relres, int nthreads, int fixed_iters) {
+  Mesh m = mesh_of(prm);
+  Poisson P;
+  poisson_assemble(prm, m, dt, rho_u, rho_v, P);
+  if (b_in) {
+    for (int j = 1; j <= m.ny; ++j)
+      for (int i = 1; i <= m.nx; ++i) P.b[P.k(i, j)] = b_in[m.id(i, j)];
+  } else {
+    poisson_rhs_from_velocity(m, u_star, v_star, P);
+  }
+  std::vector<double> x((size_t)m.nx * m.ny);
+  for (int j = 1; j <= m.ny; ++j)
+    for (int i = 1; i <= m.nx; ++i) x[P.k(i, j)] = p[m.id(i, j)];
+  int st = poisson_pcg(prm, P, x, iters, relres, nthreads, fixed_iters);
+  for (int j = 1; j <= m.ny; ++j)
+    for (int i = 1; i <= m.nx; ++i) p[m.id(i, j)] = x[P.k(i, j)];
+  return st;
+}
+
+// src/module_simulation.f90:2586-2654 projection correction (non-periodic)
+void project_correct(const covof_params* prm, const Mesh& m, double dt, double* u, double* v,
+                     const double* p, const double* rho_u, const double* rho_v) {
+  const int nx = m.nx, ny = m.ny;
+  const int u_nx = nx + 1, v_ny = ny + 1;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= u_nx; ++i) {
+      bool wall = (i == 1 && is_wall(prm, L)) || (i == u_nx && is_wall(prm, R));
+      if (wall) continue;
+      double r = rho_u[m.id(i, j)];
+      if (r < 1.0e-12) r = 1.0;
+      double pw = (i > 1) ? p[m.id(i - 1, j)] : p[m.id(1, j)];
+      double pe = (i <= nx) ? p[m.id(i, j)] : p[m.id(nx, j)];
+      double g = (pe - pw) / m.dx;
+      u[m.id(i, j)] = u[m.id(i, j)] - (dt / r) * g;
+    }
+  for (int j = 1; j <= v_ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      bool wall = (j == 1 && is_wall(prm, B)) || (j == v_ny && is_wall(prm, T));
+      if (wall) continue;
+      double r = rho_v[m.id(i, j)];
+      if (r < 1.0e-12) r = 1.0;
+      double ps = (j > 1) ? p[m.id(i, j - 1)] : p[m.id(i, 1)];
+      double pn = (j <= ny) ? p[m.id(i, j)] : p[m.id(i, ny)];
+      double g = (pn - ps) / m.dy;
+      v[m.id(i, j)] = v[m.id(i, j)] - (dt / r) * g;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Momentum predictor (SP: DOFs = u then v, src/module_navier_stokes.f90:164-169)
+struct MomCtx {
+  const covof_params* prm;
+  Mesh m;
+  double dt;
+  const double *u_n, *v_n, *rho_u, *rho_v, *mu, *mu_node;
+  int u_nx, v_ny;
+  size_t nu, nv;
+};
+
+// src/module_navier_stokes.f90:2388-2416 conv_face_flux (UPWIND / CENTERED)
+inline double conv_face_flux(int scheme, double flux, double phiL, double phiR) {
+  if (scheme == COVOF_CONV_CENTERED) return 0.5 * flux * (phiL + phiR);
+  return (flux >= 0.0) ? flux * phiL : flux * phiR;
+}
+
+// src/module_navier_stokes.f90:2418-2457 compute_u_conv_fluxes (PICARD)
+inline void u_conv_fluxes(const MomCtx& c, int i, int j, double& FE, double& FW, double& FN,
+                          double& FS) {
+  const Mesh& m = c.m;
+  double un = c.u_n[m.id(i, j)], unE = c.u_n[m.id(i + 1, j)], unW = c.u_n[m.id(i - 1, j)];
+  double vnN = 0.5 * (c.v_n[m.id(i - 1, j + 1)] + c.v_n[m.id(i, j + 1)]);
+  double vnS = 0.5 * (c.v_n[m.id(i - 1, j)] + c.v_n[m.id(i, j)]);
+  FE = 0.5 * (un + unE) * m.dy;
+  FW = 0.5 * (unW + un) * m.dy;
+  FN = vnN * m.dx;
+  FS = vnS * m.dx;
+}
+// src/module_navier_stokes.f90:2459-2498 compute_v_conv_fluxes (PICARD)
+inline void v_conv_fluxes(const MomCtx& c, int i, int j, double& FE, double& FW, double& FN,
+                          double& FS) {
+  const Mesh& m = c.m;
+  double vn = c.v_n[m.id(i, j)], vnN = c.v_n[m.id(i, j + 1)], vnS = c.v_n[m.id(i, j - 1)];
+  double unE = 0.5 * (c.u_n[m.id(i + 1, j - 1)] + c.u_n[m.id(i + 1, j)]);
+  double unW = 0.5 * (c.u_n[m.id(i, j - 1)] + c.u_n[m.id(i, j)]);
+  FE = unE * m.dy;
+  FW = unW * m.dy;
+  FN = 0.5 * (vn + vnN) * m.dx;
+  FS = 0.5 * (vnS + vn) * m.dx;
+}
+
+// src/module_navier_stokes.f90:380-780 ns_apply_system_matrix (SP, Euler,
+// PICARD, no AL/obstacle terms).  tu/tv: the unpacked operand with the
+// homogeneous ghost conditions applied (:458 -> src/module_mpi_comm.f90:290-537).
+void mom_apply(const MomCtx& c, const double* tu, const double* tv, double* yu, double* yv) {
+  const Mesh& m = c.m;
+  const covof_params* prm = c.prm;
+  const double dx = m.dx, dy = m.dy, dvol = dx * dy, dt = c.dt;
+  const int nx = m.nx, ny = m.ny, u_nx = c.u_nx, v_ny = c.v_ny;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= u_nx; ++i) {
+      size_t k = m.id(i, j);
+      double rho = c.rho_u[k];
+      double diag_bc = ((1.0 * rho) / dt) * dvol;
+      if (i == 1) {
+        if (prm->bc_type[L] == COVOF_BC_NEUMANN) yu[k] = diag_bc * (tu[m.id(1, j)] - tu[m.id(2, j)]);
+        else yu[k] = diag_bc * tu[m.id(1, j)];
+        continue;
+      }
+      if (i == u_nx) {
+        if (prm->bc_type[R] == COVOF_BC_NEUMANN)
+          yu[k] = diag_bc * (tu[m.id(u_nx, j)] - tu[m.id(u_nx - 1, j)]);
+        else yu[k] = diag_bc * tu[m.id(u_nx, j)];
+        continue;
+      }
+      double val = (((1.0 * rho) / dt) * tu[k]) * dvol;
+      if (prm->enable_convection) {
+        double FE, FW, FN, FS;
+        u_conv_fluxes(c, i, j, FE, FW, FN, FS);
+        int s = prm->convective_scheme;
+        double pE = conv_face_flux(s, FE, tu[k], tu[m.id(i + 1, j)]);
+        double pW = conv_face_flux(s, FW, tu[m.id(i - 1, j)], tu[k]);
+        double pN = conv_face_flux(s, FN, tu[k], tu[m.id(i, j + 1)]);
+        double pS = conv_face_flux(s, FS, tu[m.id(i, j - 1)], tu[k]);
+        val = val + rho * (pE - pW + pN - pS);
+      }
+      double muE = c.mu[m.id(i, j)], muW = c.mu[m.id(i - 1, j)];
+      double dE = 2.0 * muE * (tu[m.id(i + 1, j)] - tu[k]) / dx * dy;
+      double dW = 2.0 * muW * (tu[k] - tu[m.id(i - 1, j)]) / dx * dy;
+      val = val - (dE - dW);
+      double mN = c.mu_node[m.id(i, j + 1)], mS = c.mu_node[m.id(i, j)];
+      double sN = mN * ((tu[m.id(i, j + 1)] - tu[k]) / dy + (tv[m.id(i, j + 1)] - tv[m.id(i - 1, j + 1)]) / dx) * dx;
+      double sS = mS * ((tu[k] - tu[m.id(i, j - 1)]) / dy + (tv[m.id(i, j)] - tv[m.id(i - 1, j)]) / dx) * dx;
+      val = val - (sN - sS);
+      yu[k] = val;
+    }
+  for (int j = 1; j <= v_ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t k = m.id(i, j);
+      double rho = c.rho_v[k];
+      double diag_bc = ((1.0 * rho) / dt) * dvol;
+      bool wb = (j == 1 && is_wall(prm, B));
+      bool wt = (j == v_ny && is_wall(prm, T));
+      if (wb || wt) { yv[k] = diag_bc * tv[k]; continue; }
+      double val = (((1.0 * rho) / dt) * tv[k]) * dvol;
+      if (prm->enable_convection) {
+        double FE, FW, FN, FS;
+        v_conv_fluxes(c, i, j, FE, FW, FN, FS);
+        int s = prm->convective_scheme;
+        double pE = conv_face_flux(s, FE, tv[k], tv[m.id(i + 1, j)]);
+        double pW = conv_face_flux(s, FW, tv[m.id(i - 1, j)], tv[k]);
+        double pN = conv_face_flux(s, FN, tv[k], tv[m.id(i, j + 1)]);
+        double pS = conv_face_flux(s, FS, tv[m.id(i, j - 1)], tv[k]);
+        val = val + rho * (pE - pW + pN - pS);
+      }
+      double muN = c.mu[m.id(i, j)], muS = c.mu[m.id(i, j - 1)];
+      double dN = 2.0 * muN * (tv[m.id(i, j + 1)] - tv[k]) / dy * dx;
+      double dS = 2.0 * muS * (tv[k] - tv[m.id(i, j - 1)]) / dy * dx;
+      val = val - (dN - dS);
+      double mE = c.mu_node[m.id(i + 1, j)], mW = c.mu_node[m.id(i, j)];
+      double sE = mE * ((tv[m.id(i + 1, j)] - tv[k]) / dx + (tu[m.id(i + 1, j)] - tu[m.id(i + 1, j - 1)]) / dy) * dy;
+      double sW = mW * ((tv[k] - tv[m.id(i - 1, j)]) / dx + (tu[m.id(i, j)] - tu[m.id(i, j - 1)]) / dy) * dy;
+      val = val - (sE - sW);
+      yv[k] = val;
+    }
+}
+
+// src/module_navier_stokes.f90:1268-1539 ns_assemble_preconditioner_blocks
+// (diag_u / diag_v only; Euler, no AL / obstacle / Newton terms).
+void mom_diag(const MomCtx& c, double* du, double* dv) {
+  const Mesh& m = c.m;
+  const covof_params* prm = c.prm;
+  const double dx = m.dx, dy = m.dy, dvol = dx * dy;
+  const double dt_safe = c.dt > 1.0e-30 ? c.dt : 1.0;
+  const int nx = m.nx, ny = m.ny, u_nx = c.u_nx, v_ny = c.v_ny;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= u_nx; ++i) {
+      size_t k = m.id(i, j);
+      double rho = c.rho_u[k];
+      double Du = ((1.0 * rho) / dt_safe) * dvol;
+      if (Du <= 1.0e-30) Du = 1.0;
+      if (i == 1 || i == u_nx) { du[k] = Du; continue; }
+      double mue = c.mu[m.id(i, j)], muw = c.mu[m.id(i - 1, j)];
+      double cE = 2.0 * mue * (dy / dx), cW = 2.0 * muw * (dy / dx);
+      double cNr = c.mu_node[m.id(i, j + 1)] * (dx / dy);
+      double cSr = c.mu_node[m.id(i, j)] * (dx / dy);
+      double cNv = cNr, cSv = cSr, dwy = 0.0;
+      if (j == 1) {
+        if (prm->bc_type[B] == COVOF_BC_DIRICHLET) dwy = dwy + (ny >= 2 ? 3.0 * cSr : 2.0 * cSr);
+        cSv = 0.0;
+      }
+      if (j == ny) {
+        if (prm->bc_type[T] == COVOF_BC_DIRICHLET) dwy = dwy + (ny >= 2 ? 3.0 * cNr : 2.0 * cNr);
+        cNv = 0.0;
+      }
+      double conv_diag = 0.0;
+      if (prm->enable_convection) {
+        double FE, FW, FN, FS;
+        u_conv_fluxes(c, i, j, FE, FW, FN, FS);
+        conv_diag = rho * (std::max(FE, 0.0) + std::max(-FW, 0.0) + std::max(FN, 0.0) + std::max(-FS, 0.0));
+      }
+      double aP = Du + dwy + conv_diag + 0.0 + 0.0 + cW + cE + cSv + cNv + 0.0 + 0.0;
+      if (aP <= 1.0e-15) aP = 1.0;
+      du[k] = aP;
+    }
+  for (int j = 1; j <= v_ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t k = m.id(i, j);
+      double rho = c.rho_v[k];
+      double Dv = ((1.0 * rho) / dt_safe) * dvol;
+      if (Dv <= 1.0e-30) Dv = 1.0;
+      bool wall = (j == 1 && is_wall(prm, B)) || (j == v_ny && is_wall(prm, T));
+      if (wall) { dv[k] = Dv; continue; }
+      if ((j == 1 && prm->bc_type[B] == COVOF_BC_NEUMANN) ||
+          (j == v_ny && prm->bc_type[T] == COVOF_BC_NEUMANN)) { dv[k] = Dv; continue; }
+      double mun = c.mu[m.id(i, j)], mus = c.mu[m.id(i, j - 1)];
+      double cN = 2.0 * mun * (dx / dy), cS = 2.0 * mus * (dx / dy);
+      double cEr = c.mu_node[m.id(i + 1, j)] * (dy / dx);
+      double cWr = c.mu_node[m.id(i, j)] * (dy / dx);
+      double cEv = cEr, cWv = cWr, dwx = 0.0;
+      if (i == 1) {
+        if (prm->bc_type[L] == COVOF_BC_DIRICHLET) dwx = dwx + 2.0 * cWr;
+        cWv = 0.0;
+      }
+      if (i == nx) {
+        if (prm->bc_type[R] == COVOF_BC_DIRICHLET) dwx = dwx + 2.0 * cEr;
+        cEv = 0.0;
+      }
+      double conv_diag = 0.0;
+      if (prm->enable_convection) {
+        double FE, FW, FN, FS;
+        v_conv_fluxes(c, i, j, FE, FW, FN, FS);
+        conv_diag = rho * (std::max(FE, 0.0) + std::max(-FW, 0.0) + std::max(FN, 0.0) + std::max(-FS, 0.0));
+      }
+      double aP = Dv + dwx + conv_diag + 0.0 + 0.0 + cWv + cEv + cS + cN + 0.0 + 0.0;
+      if (aP <= 1.0e-15) aP = 1.0;
+      dv[k] = aP;
+    }
+}
+
+// src/module_navier_stokes.f90:785-1101 ns_assemble_rhs (SP, Euler, constant walls)
+void mom_rhs(const MomCtx& c, const double* mu_node, const double* fx, const double* fy,
+             const double* u_old, const double* v_old, double* ru, double* rv) {
+  const Mesh& m = c.m;
+  const covof_params* prm = c.prm;
+  const double dx = m.dx, dy = m.dy, dvol = dx * dy, dt = c.dt;
+  const int nx = m.nx, ny = m.ny, u_nx = c.u_nx, v_ny = c.v_ny;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= u_nx; ++i) {
+      size_t k = m.id(i, j);
+      double rho = c.rho_u[k];
+      double diag_bc = ((1.0 * rho) / dt) * dvol;
+      if (i == 1) {
+        double ubc = prm->bc_type[L] == COVOF_BC_DIRICHLET ? prm->bc_u[L] : 0.0;
+        ru[k] = diag_bc * ubc;
+        continue;
+      }
+      if (i == u_nx) {
+        double ubc = prm->bc_type[R] == COVOF_BC_DIRICHLET ? prm->bc_u[R] : 0.0;
+        ru[k] = diag_bc * ubc;
+        continue;
+      }
+      double val = (rho / dt) * u_old[k] * dvol;
+      val = val + rho * prm->gx * dvol;
+      val = val + fx[k] * dvol;
+      if (j == ny && prm->bc_type[T] == COVOF_BC_DIRICHLET) {
+        double mN = mu_node[m.id(i, j + 1)];
+        if (ny >= 2) val = val + mN * ((8.0 / 3.0) * prm->bc_u[T] / dy) * dx;
+        else val = val + mN * (2.0 * prm->bc_u[T] / dy) * dx;
+      }
+      if (j == 1 && prm->bc_type[B] == COVOF_BC_DIRICHLET) {
+        double mS = mu_node[m.id(i, j)];
+        if (ny >= 2) val = val + mS * ((8.0 / 3.0) * prm->bc_u[B] / dy) * dx;
+        else val = val + mS * (2.0 * prm->bc_u[B] / dy) * dx;
+      }
+      ru[k] = val;
+    }
+  for (int j = 1; j <= v_ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t k = m.id(i, j);
+      double rho = c.rho_v[k];
+      double diag_bc = ((1.0 * rho) / dt) * dvol;
+      if (j == 1 && is_wall(prm, B)) {
+        double vbc = prm->bc_type[B] == COVOF_BC_DIRICHLET ? prm->bc_v[B] : 0.0;
+        rv[k] = diag_bc * vbc;
+        continue;
+      }
+      if (j == v_ny && is_wall(prm, T)) {
+        double vbc = prm->bc_type[T] == COVOF_BC_DIRICHLET ? prm->bc_v[T] : 0.0;
+        rv[k] = diag_bc * vbc;
+        continue;
+      }
+      double val = (rho / dt) * v_old[k] * dvol;
+      val = val + rho * prm->gy * dvol;
+      val = val + fy[k] * dvol;
+      if (i == 1 && prm->bc_type[L] == COVOF_BC_DIRICHLET) {
+        double mW = mu_node[m.id(i, j)];
+        val = val + mW * (2.0 * prm->bc_v[L] / dx) * dy;
+      }
+      if (i == nx && prm->bc_type[R] == COVOF_BC_DIRICHLET) {
+        double mE = mu_node[m.id(i + 1, j)];
+        val = val + mE * (2.0 * prm->bc_v[R] / dx) * dy;
+      }
+      rv[k] = val;
+    }
+}
+
+// Packed Krylov vectors: u DOFs (i=1..u_nx, j=1..ny) then v DOFs
+// (i=1..nx, j=1..v_ny), src/module_navier_stokes.f90:231-296.
+struct Packer {
+  const MomCtx& c;
+  size_t n() const { return c.nu + c.nv; }
+  void pack(const double* u, const double* v, double* x) const {
+    const Mesh& m = c.m;
+    size_t d = 0;
+    for (int j = 1; j <= m.ny; ++j) for (int i = 1; i <= c.u_nx; ++i) x[d++] = u[m.id(i, j)];
+    for (int j = 1; j <= c.v_ny; ++j) for (int i = 1; i <= m.nx; ++i) x[d++] = v[m.id(i, j)];
+  }
+  void unpack(const double* x, double* u, double* v) const {
+    const Mesh& m = c.m;
+    size_t d = 0;
+    for (int j = 1; j <= m.ny; ++j) for (int i = 1; i <= c.u_nx; ++i) u[m.id(i, j)] = x[d++];
+    for (int j = 1; j <= c.v_ny; ++j) for (int i = 1; i <= m.nx; ++i) v[m.id(i, j)] = x[d++];
+  }
+};
+
+struct Krylov {
+  const MomCtx& c;
+  Packer pk;
+  std::vector<double> tu, tv, yu, yv, diag;  // tf (saved operand), diag packed
+  explicit Krylov(const MomCtx& cc) : c(cc), pk{cc} {
+    size_t g = (size_t)(c.m.nx + 2) * (c.m.ny + 2);
+    tu.assign(g, 0.0); tv.assign(g, 0.0); yu.assign(g, 0.0); yv.assign(g, 0.0);
+  }
+  // ns_apply_system_matrix with unpack + homogeneous BC (:397-458)
+  void A(const double* x, double* y) {
+    pk.unpack(x, tu.data(), tv.data());
+    velocity_bc(c.prm, c.m, tu.data(), tv.data(), true);
+    mom_apply(c, tu.data(), tv.data(), yu.data(), yv.data());
+    pk.pack(yu.data(), yv.data(), y);
+  }
+  // src/module_linear_solvers.f90:88-117 (JACOBI) / :280-304 (ILU0 = same)
+  void M(const double* src, double* dst) {
+    size_t n = pk.n();
+    bool on = c.prm->use_precond && (c.prm->precond == COVOF_PRECOND_JACOBI ||
+                                     c.prm->precond == COVOF_PRECOND_ILU0);
+    for (size_t q = 0; q < n; ++q) {
+      double d = diag[q];
+      dst[q] = (on && std::fabs(d) > 1.0e-15) ? src[q] / d : src[q];
+    }
+  }
+  void PA(const double* src, double* dst) {  // apply_PA (:323-356)
+    std::vector<double> tmp(pk.n());
+    A(src, tmp.data());
+    M(tmp.data(), dst);
+  }
+};
+
+// src/module_linear_solvers.f90:584-730 solve_bicgstab
+int solve_bicgstab(Krylov& K, const double* b, double* x, int* iters) {
+  const covof_params* prm = K.c.prm;
+  size_t n = K.pk.n();
+  double tol = prm->tol;
+  int max_iter = prm->max_iter;
+  *iters = max_iter;
+  std::vector<double> bh(n), r(n), rt(n), p(n), v(n), s(n), t(n);
+  K.M(b, bh.data());
+  K.PA(x, r.data());
+  for (size_t q = 0; q < n; ++q) r[q] = bh[q] - r[q];
+  double r0 = std::sqrt(dot(r.data(), r.data(), n));
+  if (r0 < 1.0e-12) { *iters = 0; return COVOF_OK; }
+  rt = r;
+  double rho_old = 1.0, alpha = 1.0, omega = 1.0;
+  for (int it = 1; it <= max_iter; ++it) {
+    double rho = dot(rt.data(), r.data(), n);
+    if (std::fabs(rho) < 1.0e-30) return COVOF_BREAKDOWN;
+    if (it == 1) p = r;
+    else {
+      double beta = (rho / rho_old) * (alpha / omega);
+      for (size_t q = 0; q < n; ++q) p[q] = r[q] + beta * (p[q] - omega * v[q]);
+    }
+    K.PA(p.data(), v.data());
+    double den = dot(rt.data(), v.data(), n);
+    if (std::fabs(den) < 1.0e-30) return COVOF_BREAKDOWN;
+    alpha = rho / den;
+    for (size_t q = 0; q < n; ++q) s[q] = r[q] - alpha * v[q];
+    double sn = std::sqrt(dot(s.data(), s.data(), n));
+    if (sn != sn || sn > 1.0e30) return COVOF_NAN;
+    if (sn / r0 < tol || sn < 1.0e-12) {
+      for (size_t q = 0; q < n; ++q) x[q] = x[q] + alpha * p[q];
+      *iters = it;
+      return COVOF_OK;
+    }
+    K.PA(s.data(), t.data());
+    double tt = dot(t.data(), t.data(), n);
+    omega = tt > 1.0e-30 ? dot(t.data(), s.data(), n) / tt : 0.0;
+    for (size_t q = 0; q < n; ++q) x[q] = x[q] + alpha * p[q] + omega * s[q];
+    for (size_t q = 0; q < n; ++q) r[q] = s[q] - omega * t[q];
+    rho_old = rho;
+    double rn = std::sqrt(dot(r.data(), r.data(), n));
+    if (rn != rn || rn > 1.0e30) return COVOF_NAN;
+    if (rn / r0 < tol || rn < 1.0e-12) { *iters = it; return COVOF_OK; }
+    if (std::fabs(omega) < 1.0e-30) return COVOF_BREAKDOWN;
+  }
+  return COVOF_MAXITER;
+}
+
+// src/module_linear_solvers.f90:361-579 solve_bicgstab2
+int solve_bicgstab2(Krylov& K, const double* b, double* x, int* iters) {
+  const covof_params* prm = K.c.prm;
+  size_t n = K.pk.n();
+  double tol = prm->tol;
+  int max_iter = prm->max_iter;
+  *iters = 0;
+  std::vector<double> bh(n), rt(n), r0(n), r1(n, 0.0), r2(n, 0.0), u0(n, 0.0), u1(n, 0.0), u2(n, 0.0);
+  K.M(b, bh.data());
+  K.PA(x, r0.data());
+  for (size_t q = 0; q < n; ++q) r0[q] = bh[q] - r0[q];
+  double r0n = std::sqrt(dot(r0.data(), r0.data(), n));
+  if (r0n < 1.0e-12) return COVOF_OK;
+  rt = r0;
+  double rho0 = 1.0, alpha = 0.0, omega = 1.0;
+  int iter = 0;
+  int status = COVOF_MAXITER;
+  while (iter < max_iter) {
+    iter = iter + 2;
+    rho0 = -omega * rho0;
+    double rho1 = dot(rt.data(), r0.data(), n);
+    if (std::fabs(rho0) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
+    double beta = alpha * (rho1 / rho0);
+    rho0 = rho1;
+    for (size_t q = 0; q < n; ++q) u0[q] = r0[q] - beta * u0[q];
+    K.PA(u0.data(), u1.data());
+    double gamma = dot(rt.data(), u1.data(), n);
+    if (std::fabs(gamma) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
+    alpha = rho0 / gamma;
+    for (size_t q = 0; q < n; ++q) r0[q] = r0[q] - alpha * u1[q];
+    for (size_t q = 0; q < n; ++q) x[q] = x[q] + alpha * u0[q];
+    K.PA(r0.data(), r1.data());
+    rho1 = dot(rt.data(), r1.data(), n);
+    if (std::fabs(rho0) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
+    beta = alpha * (rho1 / rho0);
+    rho0 = rho1;
+    for (size_t q = 0; q < n; ++q) u0[q] = r0[q] - beta * u0[q];
+    for (size_t q = 0; q < n; ++q) u1[q] = r1[q] - beta * u1[q];
+    K.PA(u1.data(), u2.data());
+    gamma = dot(rt.data(), u2.data(), n);
+    if (std::fabs(gamma) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
+    alpha = rho0 / gamma;
+    for (size_t q = 0; q < n; ++q) x[q] = x[q] + alpha * u0[q];
+    for (size_t q = 0; q < n; ++q) r0[q] = r0[q] - alpha * u1[q];
+    for (size_t q = 0; q < n; ++q) r1[q] = r1[q] - alpha * u2[q];
+    K.PA(r1.data(), r2.data());
+    double s11 = dot(r1.data(), r1.data(), n);
+    double s12 = dot(r2.data(), r1.data(), n);
+    double s22 = dot(r2.data(), r2.data(), n);
+    double rhs1 = dot(r0.data(), r1.data(), n);
+    double rhs2 = dot(r0.data(), r2.data(), n);
+    double rn1 = std::sqrt(s11), rn2 = std::sqrt(s22), g1, g2;
+    if (rn1 < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
+    else if (rn2 < 1.0e-300) { g2 = 0.0; g1 = rhs1 / s11; }
+    else {
+      double i1 = 1.0 / rn1, i2 = 1.0 / rn2;
+      double c12 = s12 * i1 * i2;
+      double b1 = rhs1 * i1, b2 = rhs2 * i2;
+      double det = 1.0 - c12 * c12;
+      if (std::fabs(det) < 1.0e-14) { g2 = 0.0; g1 = b1 * i1; }
+      else { g1 = (b1 - c12 * b2) / (det * rn1); g2 = (b2 - c12 * b1) / (det * rn2); }
+    }
+    for (size_t q = 0; q < n; ++q) x[q] = x[q] + g1 * r0[q] + g2 * r1[q];
+    for (size_t q = 0; q < n; ++q) r0[q] = r0[q] - (g1 * r1[q] + g2 * r2[q]);
+    for (size_t q = 0; q < n; ++q) u0[q] = u0[q] - (g1 * u1[q] + g2 * u2[q]);
+    if (g2 != 0.0) omega = g2;
+    else if (std::fabs(g1) > 1.0e-300) omega = g1;
+    else omega = 1.0;
+    double rn = std::sqrt(dot(r0.data(), r0.data(), n));
+    if (rn != rn || rn > 1.0e30) { status = COVOF_NAN; break; }
+    if (rn / r0n < tol || rn < 1.0e-12) { *iters = iter; return COVOF_OK; }
+  }
+  *iters = iter;
+  return status;
+}
+
+// src/module_linear_solvers.f90:735-838 solve_cg
+int solve_cg(Krylov& K, const double* b, double* x, int* iters) {
+  const covof_params* prm = K.c.prm;
+  size_t n = K.pk.n();
+  double tol = prm->tol;
+  int max_iter = prm->max_iter;
+  *iters = max_iter;
+  std::vector<double> Ax(n), r(n), z(n), p(n), Ap(n);
+  K.A(x, Ax.data());
+  for (size_t q = 0; q < n; ++q) r[q] = b[q] - Ax[q];
+  double r0 = std::sqrt(dot(r.data(), r.data(), n));
+  if (r0 < 1.0e-12) { *iters = 0; return COVOF_OK; }
+  K.M(r.data(), z.data());
+  p = z;
+  double rz_old = dot(r.data(), z.data(), n);
+  for (int it = 1; it <= max_iter; ++it) {
+    K.A(p.data(), Ap.data());
+    double pAp = dot(p.data(), Ap.data(), n);
+    if (std::fabs(pAp) < 1.0e-30) return COVOF_BREAKDOWN;
+    double alpha = rz_old / pAp;
+    for (size_t q = 0; q < n; ++q) x[q] = x[q] + alpha * p[q];
+    for (size_t q = 0; q < n; ++q) r[q] = r[q] - alpha * Ap[q];
+    double rn = std::sqrt(dot(r.data(), r.data(), n));
+    if (rn / r0 < tol || rn < 1.0e-13) { *iters = it; return COVOF_OK; }
+    K.M(r.data(), z.data());
+    double rz_new = dot(r.data(), z.data(), n);
+    double beta = rz_new / rz_old;
+    rz_old = rz_new;
+    for (size_t q = 0; q < n; ++q) p[q] = z[q] + beta * p[q];
+  }
+  return COVOF_MAXITER;
+}
+
+MomCtx make_ctx(const covof_params* prm, double dt, const double* u_n, const double* v_n,
+                const double* rho_u, const double* rho_v, const double* mu, const double* mu_node) {
+  MomCtx c;
+  c.prm = prm; c.m = mesh_of(prm); c.dt = dt;
+  c.u_n = u_n; c.v_n = v_n; c.rho_u = rho_u; c.rho_v = rho_v; c.mu = mu; c.mu_node = mu_node;
+  c.u_nx = prm->nx + 1; c.v_ny = prm->ny + 1;
+  c.nu = (size_t)c.u_nx * prm->ny; c.nv = (size_t)prm->nx * c.v_ny;
+  return c;
+}
+
+// src/module_simulation.f90:2454-2470: diag, rhs, pack, solve, unpack, BC
+int predictor(const covof_params* prm, double dt, double* u, double* v, const double* rho_u,
+              const double* rho_v, const double* mu, const double* mu_node, const double* fx,
+              const double* fy, const double* u_old, const double* v_old, int* iters) {
+  // fields_old for the operator is the current field (u^n) itself.
+  size_t g = (size_t)(prm->nx + 2) * (prm->ny + 2);
+  std::vector<double> un(u, u + g), vn(v, v + g);
+  MomCtx c = make_ctx(prm, dt, un.data(), vn.data(), rho_u, rho_v, mu, mu_node);
+  Krylov K(c);
+  std::vector<double> du(g, 1.0), dv(g, 1.0), ru(g, 0.0), rv(g, 0.0);
+  mom_diag(c, du.data(), dv.data());
+  K.diag.resize(K.pk.n());
+  K.pk.pack(du.data(), dv.data(), K.diag.data());
+  mom_rhs(c, mu_node, fx, fy, u_old, v_old, ru.data(), rv.data());
+  std::vector<double> rhs(K.pk.n()), x(K.pk.n());
+  K.pk.pack(ru.data(), rv.data(), rhs.data());
+  K.pk.pack(un.data(), vn.data(), x.data());
+  int st;
+  switch (prm->linear_solver) {
+    case COVOF_LINEAR_BICGSTAB: st = solve_bicgstab(K, rhs.data(), x.data(), iters); break;
+    case COVOF_LINEAR_CG: st = solve_cg(K, rhs.data(), x.data(), iters); break;
+    default: st = solve_bicgstab2(K, rhs.data(), x.data(), iters); break;
+  }
+  K.pk.unpack(x.data(), u, v);
+  velocity_bc(prm, c.m, u, v, false);
+  return st;
+}
+
+// ---------------------------------------------------------------------------
+// Geometric VOF
+struct Seg { double nx, ny, alpha; };
+
+// src/module_interface_reconstruction.f90:283-343 reconstruct_plic
+void reconstruct_plic(const Mesh& m, const double* C, Seg* s) {
+  const int nx = m.nx, ny = m.ny;
+  for (int j = 0; j <= ny + 1; ++j)
+    for (int i = 0; i <= nx + 1; ++i) {
+      size_t k = m.id(i, j);
+      double c = C[k];
+      if (c <= 1.0e-6) { s[k] = {1.0, 0.0, 1.0e9}; continue; }
+      if (c >= 1.0 - 1.0e-6) { s[k] = {1.0, 0.0, -1.0e9}; continue; }
+      double mx, my;
+      if (i >= 1 && i <= nx && j >= 1 && j <= ny) {
+        double cmm = C[m.id(i - 1, j - 1)], c0m = C[m.id(i, j - 1)], cpm = C[m.id(i + 1, j - 1)];
+        double cm0 = C[m.id(i - 1, j)], cp0 = C[m.id(i + 1, j)];
+        double cmp = C[m.id(i - 1, j + 1)], c0p = C[m.id(i, j + 1)], cpp = C[m.id(i + 1, j + 1)];
+        mx = -((cpp + 2.0 * cp0 + cpm) - (cmp + 2.0 * cm0 + cmm)) / (8.0 * m.dx);
+        my = -((cpp + 2.0 * c0p + cmp) - (cpm + 2.0 * c0m + cmm)) / (8.0 * m.dy);
+      } else {
+        mx = 1.0; my = 0.0;
+      }
+      double nrm = fhypot(mx, my), pnx, pny;
+      if (nrm > 1.0e-12) { pnx = mx / nrm; pny = my / nrm; }
+      else { pnx = 1.0; pny = 0.0; }
+      double a = compute_alpha(m.x_face(i), m.x_face(i + 1), m.y_face(j), m.y_face(j + 1), pnx, pny, c);
+      s[k] = {pnx, pny, a};
+    }
+}
+
+// src/module_interface_reconstruction.f90:346-457 reconstruct_elvira
+void reconstruct_elvira(const Mesh& m, const double* C, Seg* s) {
+  const int nx = m.nx, ny = m.ny;
+  const double dx = m.dx, dy = m.dy;
+  for (int j = 0; j <= ny + 1; ++j)
+    for (int i = 0; i <= nx + 1; ++i) {
+      size_t k = m.id(i, j);
+      double c = C[k];
+      if (c <= 1.0e-6) { s[k] = {1.0, 0.0, 1.0e9}; continue; }
+      if (c >= 1.0 - 1.0e-6) { s[k] = {1.0, 0.0, -1.0e9}; continue; }
+      double xmin = m.x_face(i), xmax = m.x_face(i + 1), ymin = m.y_face(j), ymax = m.y_face(j + 1);
+      if (!(i >= 1 && i <= nx && j >= 1 && j <= ny)) {
+        s[k] = {1.0, 0.0, compute_alpha(xmin, xmax, ymin, ymax, 1.0, 0.0, c)};
+        continue;
+      }
+      auto Cq = [&](int a, int b) { return C[m.id(a, b)]; };
+      double Hm1 = (Cq(i - 1, j - 1) + Cq(i - 1, j) + Cq(i - 1, j + 1)) * dy;
+      double H0 = (Cq(i, j - 1) + Cq(i, j) + Cq(i, j + 1)) * dy;
+      double Hp1 = (Cq(i + 1, j - 1) + Cq(i + 1, j) + Cq(i + 1, j + 1)) * dy;
+      double Wm1 = (Cq(i - 1, j - 1) + Cq(i, j - 1) + Cq(i + 1, j - 1)) * dx;
+      double W0 = (Cq(i - 1, j) + Cq(i, j) + Cq(i + 1, j)) * dx;
+      double Wp1 = (Cq(i - 1, j + 1) + Cq(i, j + 1) + Cq(i + 1, j + 1)) * dx;
+      double sgy = (Cq(i, j + 1) < Cq(i, j - 1)) ? 1.0 : -1.0;
+      double sgx = (Cq(i + 1, j) < Cq(i - 1, j)) ? 1.0 : -1.0;
+      double cnx[7], cny[7];
+      cnx[0] = -sgy * (Hp1 - Hm1) / (2.0 * dx); cny[0] = sgy * 1.0;
+      cnx[1] = -sgy * (Hp1 - H0) / (dx);        cny[1] = sgy * 1.0;
+      cnx[2] = -sgy * (H0 - Hm1) / (dx);        cny[2] = sgy * 1.0;
+      cnx[3] = sgx * 1.0; cny[3] = -sgx * (Wp1 - Wm1) / (2.0 * dy);
+      cnx[4] = sgx * 1.0; cny[4] = -sgx * (Wp1 - W0) / (dy);
+      cnx[5] = sgx * 1.0; cny[5] = -sgx * (W0 - Wm1) / (dy);
+      double mx = -((Cq(i + 1, j + 1) + 2.0 * Cq(i + 1, j) + Cq(i + 1, j - 1)) -
+                    (Cq(i - 1, j + 1) + 2.0 * Cq(i - 1, j) + Cq(i - 1, j - 1))) / (8.0 * dx);
+      double my = -((Cq(i + 1, j + 1) + 2.0 * Cq(i, j + 1) + Cq(i - 1, j + 1)) -
+                    (Cq(i + 1, j - 1) + 2.0 * Cq(i, j - 1) + Cq(i - 1, j - 1))) / (8.0 * dy);
+      cnx[6] = mx; cny[6] = my;
+      double best_err = 1.0e30, bnx = 1.0, bny = 0.0, ba = 0.0;
+      for (int q = 0; q < 7; ++q) {
+        double cn = fhypot(cnx[q], cny[q]);
+        if (cn < 1.0e-12) continue;
+        double ux = cnx[q] / cn, uy = cny[q] / cn;
+        double ca = compute_alpha(xmin, xmax, ymin, ymax, ux, uy, c);
+        double err = 0.0;
+        for (int dj = -1; dj <= 1; ++dj)
+          for (int di = -1; di <= 1; ++di) {
+            if (di == 0 && dj == 0) continue;
+            double vt = Cq(i + di, j + dj) * dx * dy;
+            double vr = cut_box_area(m.x_face(i + di), m.x_face(i + di + 1), m.y_face(j + dj),
+                                     m.y_face(j + dj + 1), ux, uy, ca);
+            double df = vr - vt;
+            err = err + df * df;
+          }
+        if (err < best_err) { best_err = err; bnx = ux; bny = uy; ba = ca; }
+      }
+      s[k] = {bnx, bny, ba};
+    }
+}
+
+// src/module_interface_reconstruction.f90:580-683 reconstruct_interface (np=1, walls)
+void reconstruct_interface(const covof_params* prm, const Mesh& m, const double* C, Seg* s) {
+  const int nx = m.nx, ny = m.ny;
+  if (prm->recon == COVOF_RECON_ELVIRA) reconstruct_elvira(m, C, s);
+  else reconstruct_plic(m, C, s);
+  size_t g = (size_t)(nx + 2) * (ny + 2);
+  std::vector<double> snx(g, 0.0), sny(g, 0.0);
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) { snx[m.id(i, j)] = s[m.id(i, j)].nx; sny[m.id(i, j)] = s[m.id(i, j)].ny; }
+  for (int j = 1; j <= ny; ++j) {
+    snx[m.id(0, j)] = snx[m.id(1, j)]; sny[m.id(0, j)] = sny[m.id(1, j)];
+    snx[m.id(nx + 1, j)] = snx[m.id(nx, j)]; sny[m.id(nx + 1, j)] = sny[m.id(nx, j)];
+  }
+  for (int i = 0; i <= nx + 1; ++i) {
+    snx[m.id(i, 0)] = snx[m.id(i, 1)]; sny[m.id(i, 0)] = sny[m.id(i, 1)];
+    snx[m.id(i, ny + 1)] = snx[m.id(i, ny)]; sny[m.id(i, ny + 1)] = sny[m.id(i, ny)];
+  }
+  auto ring = [&](int i, int j) {
+    size_t k = m.id(i, j);
+    double c = C[k];
+    if (c > 1.0e-6 && c < 1.0 - 1.0e-6) {
+      double a = snx[k], b = sny[k];
+      double nr = fhypot(a, b);
+      if (nr > 1.0e-12) {
+        a = a / nr; b = b / nr;
+        s[k].nx = a; s[k].ny = b;
+        s[k].alpha = compute_alpha(m.x_face(i), m.x_face(i + 1), m.y_face(j), m.y_face(j + 1), a, b, c);
+      }
+    }
+  };
+  for (int j = 1; j <= ny; ++j) { ring(0, j); ring(nx + 1, j); }
+  for (int i = 0; i <= nx + 1; ++i) { ring(i, 0); ring(i, ny + 1); }
+}
+
+// One direction pass of src/module_interface_vof.f90:1162-1377.
+// dir 0 = x (:1203-1243), dir 1 = y (:1246-1285).  Cin -> Cout (interior),
+// ghosts of Cout copied from Cin; clamp applied when requested (pass 2).
+void wy_pass(const covof_params* prm, const Mesh& m, double dt, int dir, const double* u,
+             const double* v, const double* cd, const double* Cin, double* Cout, bool clamp) {
+  const int nx = m.nx, ny = m.ny;
+  const double dx = m.dx, dy = m.dy, area = dx * dy;
+  size_t g = (size_t)(nx + 2) * (ny + 2);
+  std::vector<Seg> seg(g);
+  reconstruct_interface(prm, m, Cin, seg.data());
+  std::vector<double> flux(g, 0.0);
+  if (dir == 0) {
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx + 1; ++i) {
+        double uf = u[m.id(i, j)];
+        double d = std::fabs(uf) * dt;
+        if (d <= 1.0e-14) continue;
+        double xp = m.x_face(i);
+        if (uf > 0.0) {
+          const Seg& s = seg[m.id(i - 1, j)];
+          flux[m.id(i, j)] = cut_box_area(xp - d, xp, m.y_face(j), m.y_face(j + 1), s.nx, s.ny, s.alpha);
+        } else {
+          const Seg& s = seg[m.id(i, j)];
+          flux[m.id(i, j)] = -cut_box_area(xp, xp + d, m.y_face(j), m.y_face(j + 1), s.nx, s.ny, s.alpha);
+        }
+      }
+    std::memcpy(Cout, Cin, g * sizeof(double));
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        double c = Cin[m.id(i, j)] - (flux[m.id(i + 1, j)] - flux[m.id(i, j)]) / area +
+                   cd[m.id(i, j)] * (dt / dx) * (u[m.id(i + 1, j)] - u[m.id(i, j)]);
+        if (clamp) c = std::max(0.0, std::min(1.0, c));
+        Cout[m.id(i, j)] = c;
+      }
+  } else {
+    for (int j = 1; j <= ny + 1; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        double vf = v[m.id(i, j)];
+        double d = std::fabs(vf) * dt;
+        if (d <= 1.0e-14) continue;
+        double yp = m.y_face(j);
+        if (vf > 0.0) {
+          const Seg& s = seg[m.id(i, j - 1)];
+          flux[m.id(i, j)] = cut_box_area(m.x_face(i), m.x_face(i + 1), yp - d, yp, s.nx, s.ny, s.alpha);
+        } else {
+          const Seg& s = seg[m.id(i, j)];
+          flux[m.id(i, j)] = -cut_box_area(m.x_face(i), m.x_face(i + 1), yp, yp + d, s.nx, s.ny, s.alpha);
+        }
+      }
+    std::memcpy(Cout, Cin, g * sizeof(double));
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        double c = Cin[m.id(i, j)] - (flux[m.id(i, j + 1)] - flux[m.id(i, j)]) / area +
+                   cd[m.id(i, j)] * (dt / dy) * (v[m.id(i, j + 1)] - v[m.id(i, j)]);
+        if (clamp) c = std::max(0.0, std::min(1.0, c));
+        Cout[m.id(i, j)] = c;
+      }
+  }
+}
+
+// src/module_interface_vof.f90:1162-1377 advect_vof_weymouth_yue
+void wy_step(const covof_params* prm, const Mesh& m, double dt, bool x_first, const double* u,
+             const double* v, double* C) {
+  size_t g = (size_t)(m.nx + 2) * (m.ny + 2);
+  std::vector<double> cd(g), cs(g), cf(g);
+  for (size_t k = 0; k < g; ++k) cd[k] = C[k] >= 0.5 ? 1.0 : 0.0;  // :1189-1197
+  int d1 = x_first ? 0 : 1, d2 = x_first ? 1 : 0;
+  wy_pass(prm, m, dt, d1, u, v, cd.data(), C, cs.data(), false);
+  vof_bc(m, cs.data());  // :1240-1243
+  wy_pass(prm, m, dt, d2, u, v, cd.data(), cs.data(), cf.data(), true);
+  std::memcpy(C, cf.data(), g * sizeof(double));
+}
+
+// src/module_interface_vof.f90:479-616 (two-phase, incompressible, no SVOF)
+void update_props(const covof_params* prm, const Mesh& m, double* C, double* rho, double* rho_u,
+                  double* rho_v, double* mu, double* mu_node) {
+  const int nx = m.nx, ny = m.ny;
+  size_t g = (size_t)(nx + 2) * (ny + 2);
+  if (!prm->enable_two_phase) {
+    for (size_t k = 0; k < g; ++k) {
+      rho[k] = prm->rho1; rho_u[k] = prm->rho1; rho_v[k] = prm->rho1;
+      mu[k] = prm->mu1; mu_node[k] = prm->mu1;
+    }
+    return;
+  }
+  C[m.id(0, 0)] = C[m.id(1, 1)];
+  C[m.id(nx + 1, 0)] = C[m.id(nx, 1)];
+  C[m.id(0, ny + 1)] = C[m.id(1, ny)];
+  C[m.id(nx + 1, ny + 1)] = C[m.id(nx, ny)];
+  for (int j = 0; j <= ny + 1; ++j)
+    for (int i = 0; i <= nx + 1; ++i) {
+      size_t k = m.id(i, j);
+      double c = std::max(0.0, std::min(1.0, C[k]));
+      rho[k] = c * prm->rho1 + (1.0 - c) * prm->rho2;
+      mu[k] = c * prm->mu1 + (1.0 - c) * prm->mu2;
+    }
+  mu[m.id(0, 0)] = mu[m.id(1, 1)];
+  mu[m.id(nx + 1, 0)] = mu[m.id(nx, 1)];
+  mu[m.id(0, ny + 1)] = mu[m.id(1, ny)];
+  mu[m.id(nx + 1, ny + 1)] = mu[m.id(nx, ny)];
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx + 1; ++i)
+      rho_u[m.id(i, j)] = 0.5 * (rho[m.id(i - 1, j)] + rho[m.id(i, j)]);
+  for (int j = 1; j <= ny + 1; ++j)
+    for (int i = 1; i <= nx; ++i)
+      rho_v[m.id(i, j)] = 0.5 * (rho[m.id(i, j - 1)] + rho[m.id(i, j)]);
+  for (int j = 1; j <= ny + 1; ++j)
+    for (int i = 1; i <= nx + 1; ++i) {
+      double sw = mu[m.id(i - 1, j - 1)], se = mu[m.id(i, j - 1)];
+      double nw = mu[m.id(i - 1, j)], ne = mu[m.id(i, j)];
+      mu_node[m.id(i, j)] = 4.0 / (1.0 / sw + 1.0 / se + 1.0 / nw + 1.0 / ne);
+    }
+}
+
+// src/module_interface_vof.f90:627-789 (no markers, no smoothing)
+void csf(const covof_params* prm, const Mesh& m, const double* C, double* fx, double* fy,
+         double* curv) {
+  const int nx = m.nx, ny = m.ny;
+  const double dx = m.dx, dy = m.dy;
+  size_t g = (size_t)(nx + 2) * (ny + 2);
+  if (!prm->enable_surface_tension || prm->sigma <= 0.0) {
+    for (size_t k = 0; k < g; ++k) { fx[k] = 0.0; fy[k] = 0.0; curv[k] = 0.0; }
+    return;
+  }
+  std::vector<double> nxv(g, 0.0), nyv(g, 0.0), kap(g, 0.0);
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      double dcx = (C[m.id(i + 1, j)] - C[m.id(i - 1, j)]) / (2.0 * dx);
+      double dcy = (C[m.id(i, j + 1)] - C[m.id(i, j - 1)]) / (2.0 * dy);
+      double gm = std::sqrt(dcx * dcx + dcy * dcy);
+      if (gm > 1.0e-3 / dx) { nxv[m.id(i, j)] = dcx / gm; nyv[m.id(i, j)] = dcy / gm; }
+    }
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t k = m.id(i, j);
+      if (nxv[k] != 0.0 || nyv[k] != 0.0)
+        kap[k] = -((nxv[m.id(i + 1, j)] - nxv[m.id(i - 1, j)]) / (2.0 * dx) +
+                   (nyv[m.id(i, j + 1)] - nyv[m.id(i, j - 1)]) / (2.0 * dy));
+    }
+  for (size_t k = 0; k < g; ++k) curv[k] = kap[k];
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx + 1; ++i) {
+      double ka = 0.5 * (kap[m.id(i - 1, j)] + kap[m.id(i, j)]);
+      double gc = (C[m.id(i, j)] - C[m.id(i - 1, j)]) / dx;
+      fx[m.id(i, j)] = prm->sigma * ka * gc;
+    }
+  for (int j = 1; j <= ny + 1; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      double ka = 0.5 * (kap[m.id(i, j - 1)] + kap[m.id(i, j)]);
+      double gc = (C[m.id(i, j)] - C[m.id(i, j - 1)]) / dy;
+      fy[m.id(i, j)] = prm->sigma * ka * gc;
+    }
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+double orc_hypot(double x, double y) { return fhypot(x, y); }
+double orc_cut_box_area(double a, double b, double c, double d, double nx, double ny, double al) {
+  return cut_box_area(a, b, c, d, nx, ny, al);
+}
+double orc_compute_alpha(double a, double b, double c, double d, double nx, double ny, double ct) {
+  return compute_alpha(a, b, c, d, nx, ny, ct);
+}
+
+int orc_apply_velocity_bc(const covof_params* prm, double* u, double* v, int homogeneous) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  velocity_bc(prm, mesh_of(prm), u, v, homogeneous != 0);
+  return COVOF_OK;
+}
+int orc_apply_vof_bc(const covof_params* prm, double* C) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  vof_bc(mesh_of(prm), C);
+  return COVOF_OK;
+}
+
+int orc_poisson_assemble(const covof_params* prm, double dt, const double* u_star,
+                         const double* v_star, const double* rho_u, const double* rho_v,
+                         double* aW, double* aE, double* aS, double* aN, double* aP, double* b) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  Mesh m = mesh_of(prm);
+  Poisson P;
+  poisson_assemble(prm, m, dt, rho_u, rho_v, P);
+  poisson_rhs_from_velocity(m, u_star, v_star, P);
+  size_t n = (size_t)m.nx * m.ny;
+  std::memcpy(aW, P.aW.data(), n * 8); std::memcpy(aE, P.aE.data(), n * 8);
+  std::memcpy(aS, P.aS.data(), n * 8); std::memcpy(aN, P.aN.data(), n * 8);
+  std::memcpy(aP, P.aP.data(), n * 8); std::memcpy(b, P.b.data(), n * 8);
+  return COVOF_OK;
+}
+
+int orc_poisson_matvec(const covof_params* prm, double dt, const double* rho_u,
+                       const double* rho_v, const double* x, double* y) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  Mesh m = mesh_of(prm);
+  Poisson P;
+  poisson_assemble(prm, m, dt, rho_u, rho_v, P);
+  std::vector<double> xi((size_t)m.nx * m.ny), yi(xi.size());
+  for (int j = 1; j <= m.ny; ++j) for (int i = 1; i <= m.nx; ++i) xi[P.k(i, j)] = x[m.id(i, j)];
+  poisson_matvec(P, xi.data(), yi.data());
+  for (int j = 1; j <= m.ny; ++j) for (int i = 1; i <= m.nx; ++i) y[m.id(i, j)] = yi[P.k(i, j)];
+  return COVOF_OK;
+}
+
+int orc_poisson_solve(const covof_params* prm, double dt, const double* u_star,
+                      const double* v_star, const double* rho_u, const double* rho_v, double* p,
+                      int* iters, double* relres, int nthreads) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  return poisson_driver(prm, dt, u_star, v_star, nullptr, rho_u, rho_v, p, iters, relres, nthreads, 0);
+}
+
+int orc_poisson_solve_rhs(const covof_params* prm, double dt, const double* b,
+                          const double* rho_u, const double* rho_v, double* p, int* iters,
+                          double* relres, int nthreads) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  return poisson_driver(prm, dt, nullptr, nullptr, b, rho_u, rho_v, p, iters, relres, nthreads, 0);
+}
+
+int orc_poisson_fixed_iters(const covof_params* prm, double dt, const double* b,
+                            const double* rho_u, const double* rho_v, double* p, int n_iter,
+                            int nthreads, double* relres) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  if (n_iter < 1) return COVOF_INVALID;
+  int it = 0;
+  return poisson_driver(prm, dt, nullptr, nullptr, b, rho_u, rho_v, p, &it, relres, nthreads, n_iter);
+}
+
+int orc_project_correct(const covof_params* prm, double dt, double* u, double* v, const double* p,
+                        const double* rho_u, const double* rho_v) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  project_correct(prm, mesh_of(prm), dt, u, v, p, rho_u, rho_v);
+  return COVOF_OK;
+}
+
+int orc_momentum_apply(const covof_params* prm, double dt, const double* xu, const double* xv,
+                       double* yu, double* yv, const double* u_n, const double* v_n,
+                       const double* rho_u, const double* rho_v, const double* mu,
+                       const double* mu_node) {
+  int st = check_params(prm, false);
+  if (st) return st;
+  MomCtx c = make_ctx(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node);
+  size_t g = (size_t)(prm->nx + 2) * (prm->ny + 2);
+  // tf is a fresh field set: ghosts start at zero, then the DOFs are copied
+  // in and the homogeneous ghost conditions applied.
+  std::vector<double> tu(g, 0.0), tv(g, 0.0);
+  Packer pk{c};
+  std::vector<double> x(pk.n());
+  pk.pack(xu, xv, x.data());
+  pk.unpack(x.data(), tu.data(), tv.data());
+  velocity_bc(prm, c.m, tu.data(), tv.data(), true);
+  mom_apply(c, tu.data(), tv.data(), yu, yv);
+  return COVOF_OK;
+}
+
+int orc_momentum_diag(const covof_params* prm, double dt, const double* u_n, const double* v_n,
+                      const double* rho_u, const double* rho_v, const double* mu,
+                      const double* mu_node, double* diag_u, double* diag_v) {
+  int st = check_params(prm, false);
+  if (st) return st;
+  MomCtx c = make_ctx(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node);
+  mom_diag(c, diag_u, diag_v);
+  return COVOF_OK;
+}
+
+int orc_momentum_rhs(const covof_params* prm, double dt, const double* u_n, const double* v_n,
+                     const double* rho_u, const double* rho_v, const double* mu_node,
+                     const double* fx_sigma, const double* fy_sigma, const double* u_old,
+                     const double* v_old, double* rhs_u, double* rhs_v) {
+  int st = check_params(prm, false);
+  if (st) return st;
+  MomCtx c = make_ctx(prm, dt, u_n, v_n, rho_u, rho_v, nullptr, mu_node);
+  mom_rhs(c, mu_node, fx_sigma, fy_sigma, u_old, v_old, rhs_u, rhs_v);
+  return COVOF_OK;
+}
+
+int orc_predictor(const covof_params* prm, double dt, double* u, double* v, const double* rho_u,
+                  const double* rho_v, const double* mu, const double* mu_node,
+                  const double* fx_sigma, const double* fy_sigma, const double* u_old,
+                  const double* v_old, int* iters) {
+  int st = check_params(prm, false);
+  if (st) return st;
+  int it = 0;
+  st = predictor(prm, dt, u, v, rho_u, rho_v, mu, mu_node, fx_sigma, fy_sigma, u_old, v_old, &it);
+  if (iters) *iters = it;
+  return st;
+}
+
+// src/module_simulation.f90:2424-2666 sim_solve_standard_projection
+int orc_sp_step(const covof_params* prm, double dt, double* u, double* v, double* p,
+                const double* rho_u, const double* rho_v, const double* mu,
+                const double* mu_node, const double* fx_sigma, const double* fy_sigma,
+                const double* u_old, const double* v_old, int* iters_u, int* iters_p,
+                double* relres) {
+  int st = check_params(prm, false);
+  if (st) return st;
+  int iu = 0, ip = 0;
+  int s1 = predictor(prm, dt, u, v, rho_u, rho_v, mu, mu_node, fx_sigma, fy_sigma, u_old, v_old, &iu);
+  if (s1 == COVOF_NAN) return s1;
+  int s2 = poisson_driver(prm, dt, u, v, nullptr, rho_u, rho_v, p, &ip, relres, 1, 0);
+  Mesh m = mesh_of(prm);
+  project_correct(prm, m, dt, u, v, p, rho_u, rho_v);
+  velocity_bc(prm, m, u, v, false);
+  if (iters_u) *iters_u = iu;
+  if (iters_p) *iters_p = ip;
+  return s2 != COVOF_OK ? s2 : s1;
+}
+
+int orc_reconstruct(const covof_params* prm, const double* C, double* seg) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  Mesh m = mesh_of(prm);
+  size_t g = (size_t)(m.nx + 2) * (m.ny + 2);
+  std::vector<Seg> s(g);
+  reconstruct_interface(prm, m, C, s.data());
+  for (size_t k = 0; k < g; ++k) { seg[3 * k] = s[k].nx; seg[3 * k + 1] = s[k].ny; seg[3 * k + 2] = s[k].alpha; }
+  return COVOF_OK;
+}
+
+int orc_wy_step(const covof_params* prm, double dt, int x_first, const double* u, const double* v,
+                double* C) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  wy_step(prm, mesh_of(prm), dt, x_first != 0, u, v, C);
+  return COVOF_OK;
+}
+
+int orc_update_physical_properties(const covof_params* prm, double* C, double* rho,
+                                   double* rho_u, double* rho_v, double* mu, double* mu_node) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  update_props(prm, mesh_of(prm), C, rho, rho_u, rho_v, mu, mu_node);
+  return COVOF_OK;
+}
+
+int orc_compute_curvature_and_csf(const covof_params* prm, const double* C, double* fx_sigma,
+                                  double* fy_sigma, double* curvature) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  csf(prm, mesh_of(prm), C, fx_sigma, fy_sigma, curvature);
+  return COVOF_OK;
+}
+
+// src/module_interface_vof.f90:792-825 advect_vof (WEYMOUTH_YUE branch)
+int orc_vof_advect(const covof_params* prm, double dt, int step_count, const double* u,
+                   const double* v, double* C, double* rho, double* rho_u, double* rho_v,
+                   double* mu, double* mu_node, double* fx_sigma, double* fy_sigma,
+                   double* curvature) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  Mesh m = mesh_of(prm);
+  wy_step(prm, m, dt, (step_count % 2) == 0, u, v, C);
+  vof_bc(m, C);
+  update_props(prm, m, C, rho, rho_u, rho_v, mu, mu_node);
+  csf(prm, m, C, fx_sigma, fy_sigma, curvature);
+  return COVOF_OK;
+}
+
+}  // extern "C"

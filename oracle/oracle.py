@@ -1,0 +1,196 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes loader of the CPU oracle (covof_oracle.cpp).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs use this
+module, and only as the checker / the timed CPU restatement.  Arrays use the
+reference layout (ny+2, nx+2), float64, C-contiguous.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libcovof_oracle.so"
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    srcs = [HERE / "covof_oracle.cpp", HERE / "covof_oracle.h", HERE.parent / "include" / "covof_gpu.h"]
+    if force or not LIB.exists() or any(s.stat().st_mtime > LIB.stat().st_mtime for s in srcs):
+        subprocess.run(["make", "-s", "-C", str(HERE)] + (["-B"] if force else []), check=True)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        d, i, v = C.c_double, C.c_int, C.c_void_p
+        sig = {
+            "orc_hypot": (d, [d, d]),
+            "orc_cut_box_area": (d, [d] * 7),
+            "orc_compute_alpha": (d, [d] * 7),
+            "orc_apply_velocity_bc": (i, [v, v, v, i]),
+            "orc_apply_vof_bc": (i, [v, v]),
+            "orc_poisson_assemble": (i, [v, d] + [v] * 10),
+            "orc_poisson_matvec": (i, [v, d] + [v] * 4),
+            "orc_poisson_solve": (i, [v, d] + [v] * 5 + [v, v, i]),
+            "orc_poisson_solve_rhs": (i, [v, d] + [v] * 4 + [v, v, i]),
+            "orc_poisson_fixed_iters": (i, [v, d] + [v] * 4 + [i, i, v]),
+            "orc_project_correct": (i, [v, d] + [v] * 5),
+            "orc_momentum_apply": (i, [v, d] + [v] * 10),
+            "orc_momentum_diag": (i, [v, d] + [v] * 8),
+            "orc_momentum_rhs": (i, [v, d] + [v] * 11),
+            "orc_predictor": (i, [v, d] + [v] * 10 + [v]),
+            "orc_sp_step": (i, [v, d] + [v] * 11 + [v, v, v]),
+            "orc_reconstruct": (i, [v, v, v]),
+            "orc_wy_step": (i, [v, d, i, v, v, v]),
+            "orc_update_physical_properties": (i, [v] * 7),
+            "orc_compute_curvature_and_csf": (i, [v] * 5),
+            "orc_vof_advect": (i, [v, d, i] + [v] * 11),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data
+
+
+def _params(prm):
+    return C.byref(prm)
+
+
+def hypot(x, y): return lib().orc_hypot(x, y)
+def cut_box_area(*a): return lib().orc_cut_box_area(*[float(x) for x in a])
+def compute_alpha(*a): return lib().orc_compute_alpha(*[float(x) for x in a])
+
+
+def apply_velocity_bc(prm, u, v, homogeneous=False):
+    return lib().orc_apply_velocity_bc(_params(prm), _p(u), _p(v), int(homogeneous))
+
+
+def apply_vof_bc(prm, Cf):
+    return lib().orc_apply_vof_bc(_params(prm), _p(Cf))
+
+
+def poisson_assemble(prm, dt, u, v, rho_u, rho_v):
+    n = prm.nx * prm.ny
+    out = [np.zeros(n) for _ in range(6)]
+    st = lib().orc_poisson_assemble(_params(prm), dt, _p(u), _p(v), _p(rho_u), _p(rho_v), *[_p(o) for o in out])
+    assert st == 0, st
+    return [o.reshape(prm.ny, prm.nx) for o in out]
+
+
+def poisson_matvec(prm, dt, rho_u, rho_v, x):
+    y = np.zeros_like(x)
+    st = lib().orc_poisson_matvec(_params(prm), dt, _p(rho_u), _p(rho_v), _p(x), _p(y))
+    assert st == 0, st
+    return y
+
+
+def poisson_solve(prm, dt, u, v, rho_u, rho_v, p, nthreads=1):
+    it, rr = C.c_int(), C.c_double()
+    st = lib().orc_poisson_solve(_params(prm), dt, _p(u), _p(v), _p(rho_u), _p(rho_v), _p(p),
+                                 C.byref(it), C.byref(rr), nthreads)
+    return it.value, rr.value, st
+
+
+def poisson_solve_rhs(prm, dt, b, rho_u, rho_v, p, nthreads=1):
+    it, rr = C.c_int(), C.c_double()
+    st = lib().orc_poisson_solve_rhs(_params(prm), dt, _p(b), _p(rho_u), _p(rho_v), _p(p),
+                                     C.byref(it), C.byref(rr), nthreads)
+    return it.value, rr.value, st
+
+
+def poisson_fixed_iters(prm, dt, b, rho_u, rho_v, p, n_iter, nthreads=1):
+    rr = C.c_double()
+    st = lib().orc_poisson_fixed_iters(_params(prm), dt, _p(b), _p(rho_u), _p(rho_v), _p(p),
+                                       int(n_iter), int(nthreads), C.byref(rr))
+    return rr.value, st
+
+
+def project_correct(prm, dt, u, v, p, rho_u, rho_v):
+    return lib().orc_project_correct(_params(prm), dt, _p(u), _p(v), _p(p), _p(rho_u), _p(rho_v))
+
+
+def momentum_apply(prm, dt, xu, xv, u_n, v_n, rho_u, rho_v, mu, mu_node):
+    yu, yv = np.zeros_like(xu), np.zeros_like(xv)
+    st = lib().orc_momentum_apply(_params(prm), dt, _p(xu), _p(xv), _p(yu), _p(yv), _p(u_n), _p(v_n),
+                                  _p(rho_u), _p(rho_v), _p(mu), _p(mu_node))
+    assert st == 0, st
+    return yu, yv
+
+
+def momentum_diag(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node):
+    du, dv = np.zeros_like(u_n), np.zeros_like(v_n)
+    st = lib().orc_momentum_diag(_params(prm), dt, _p(u_n), _p(v_n), _p(rho_u), _p(rho_v), _p(mu),
+                                 _p(mu_node), _p(du), _p(dv))
+    assert st == 0, st
+    return du, dv
+
+
+def momentum_rhs(prm, dt, u_n, v_n, rho_u, rho_v, mu_node, fx, fy, u_old, v_old):
+    ru, rv = np.zeros_like(u_n), np.zeros_like(v_n)
+    st = lib().orc_momentum_rhs(_params(prm), dt, _p(u_n), _p(v_n), _p(rho_u), _p(rho_v), _p(mu_node),
+                                _p(fx), _p(fy), _p(u_old), _p(v_old), _p(ru), _p(rv))
+    assert st == 0, st
+    return ru, rv
+
+
+def predictor(prm, dt, f):
+    it = C.c_int()
+    st = lib().orc_predictor(_params(prm), dt, _p(f.u), _p(f.v), _p(f.rho_u), _p(f.rho_v), _p(f.mu),
+                             _p(f.mu_node), _p(f.fx_sigma), _p(f.fy_sigma), _p(f.u_old), _p(f.v_old),
+                             C.byref(it))
+    return it.value, st
+
+
+def sp_step(prm, dt, f):
+    iu, ip, rr = C.c_int(), C.c_int(), C.c_double()
+    st = lib().orc_sp_step(_params(prm), dt, _p(f.u), _p(f.v), _p(f.p), _p(f.rho_u), _p(f.rho_v),
+                           _p(f.mu), _p(f.mu_node), _p(f.fx_sigma), _p(f.fy_sigma), _p(f.u_old),
+                           _p(f.v_old), C.byref(iu), C.byref(ip), C.byref(rr))
+    return iu.value, ip.value, rr.value, st
+
+
+def reconstruct(prm, Cf):
+    seg = np.zeros(Cf.shape + (3,))
+    st = lib().orc_reconstruct(_params(prm), _p(Cf), seg.ctypes.data)
+    assert st == 0, st
+    return seg
+
+
+def wy_step(prm, dt, x_first, u, v, Cf):
+    st = lib().orc_wy_step(_params(prm), dt, int(bool(x_first)), _p(u), _p(v), _p(Cf))
+    assert st == 0, st
+
+
+def update_physical_properties(prm, f):
+    st = lib().orc_update_physical_properties(_params(prm), _p(f.C), _p(f.rho), _p(f.rho_u), _p(f.rho_v),
+                                              _p(f.mu), _p(f.mu_node))
+    assert st == 0, st
+
+
+def compute_curvature_and_csf(prm, f):
+    st = lib().orc_compute_curvature_and_csf(_params(prm), _p(f.C), _p(f.fx_sigma), _p(f.fy_sigma),
+                                             _p(f.curvature))
+    assert st == 0, st
+
+
+def vof_advect(prm, dt, step_count, f):
+    st = lib().orc_vof_advect(_params(prm), dt, int(step_count), _p(f.u), _p(f.v), _p(f.C), _p(f.rho),
+                              _p(f.rho_u), _p(f.rho_v), _p(f.mu), _p(f.mu_node), _p(f.fx_sigma),
+                              _p(f.fy_sigma), _p(f.curvature))
+    assert st == 0, st

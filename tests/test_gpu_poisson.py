@@ -1,0 +1,120 @@
+"""GPU Poisson parity (through the C ABI) against the oracle."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _inclusions(pkg, n, k):
+    return pkg.cases.poisson_inclusions(n=n, n_incl=k)
+
+
+def test_operator_is_bit_identical(gpu_pkg, orc):
+    pkg = gpu_pkg
+    p, b, ru, rv, dt = _inclusions(pkg, 96, 8)
+    x = np.random.default_rng(5).standard_normal(b.shape)
+    y_o = orc.poisson_matvec(p, dt, ru, rv, x)
+    with pkg.Solver(p) as s:
+        y_g = s.poisson_apply(dt, ru, rv, x)
+    assert np.array_equal(y_g[1:-1, 1:-1], y_o[1:-1, 1:-1])
+
+
+@pytest.mark.parametrize("gauge", ["pinned", "reference"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("n", [64, 128])
+def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
+    pkg = gpu_pkg
+    cap = pkg.capi
+    p, b, ru, rv, dt = _inclusions(pkg, n, 12)
+    p.p_gauge = cap.GAUGE_PINNED if gauge == "pinned" else cap.GAUGE_REFERENCE
+    p.p_tol = 1e-12
+    ref = np.zeros_like(b)
+    it_o, rr_o, st_o = orc.poisson_solve_rhs(p, dt, b, ru, rv, ref)
+    assert st_o == 0
+    q = p.copy()
+    q.p_precision = cap.PREC_MIXED if prec == "mixed" else cap.PREC_FP64
+    x = np.zeros_like(b)
+    with pkg.Solver(q) as s:
+        it, rr, st = s.poisson_solve_rhs(dt, b, ru, rv, x)
+    assert st == cap.OK
+    assert rr <= 1e-12
+    err = np.linalg.norm(x[1:-1, 1:-1] - ref[1:-1, 1:-1]) / np.linalg.norm(ref[1:-1, 1:-1])
+    # the spec bar for p is 1e-10 relative L2
+    assert err < 1e-10, err
+    if prec == "fp64":
+        assert abs(it - it_o) <= max(3, it_o // 50), (it, it_o)
+
+
+def test_reference_settings_from_velocity(gpu_pkg, orc):
+    """Reference-literal tolerance (1e-7, reference gauge) from a predicted
+    velocity: same iterations within a few, same pressure within the tolerance."""
+    pkg = gpu_pkg
+    p, C0, _ = pkg.cases.bubble_case(nx=48, ny=96, nsub=4)
+    f = pkg.Fields.allocate(p)
+    f.C[...] = C0
+    orc.apply_vof_bc(p, f.C)
+    orc.update_physical_properties(p, f)
+    u, v = pkg.cases.random_velocity(p, 1e-2, 3)
+    p.p_tol = 1e-7
+    p.p_max_iter = 1000
+    ref = np.zeros_like(u)
+    it_o, rr_o, st_o = orc.poisson_solve(p, 1e-4, u, v, f.rho_u, f.rho_v, ref)
+    x = np.zeros_like(u)
+    with pkg.Solver(p) as s:
+        it, rr, st = s.poisson_solve(1e-4, u, v, f.rho_u, f.rho_v, x)
+    assert st == st_o
+    assert abs(it - it_o) <= 3
+    d = np.linalg.norm(x - ref) / np.linalg.norm(ref)
+    assert d < 1e-5, d
+
+
+def test_maxiter_status_and_iterate_returned(gpu_pkg, orc):
+    pkg = gpu_pkg
+    p, b, ru, rv, dt = _inclusions(pkg, 64, 6)
+    p.p_tol = 1e-12
+    p.p_max_iter = 7
+    x = np.zeros_like(b)
+    ref = np.zeros_like(b)
+    _, _, st_o = orc.poisson_solve_rhs(p, dt, b, ru, rv, ref)
+    with pkg.Solver(p) as s:
+        it, rr, st = s.poisson_solve_rhs(dt, b, ru, rv, x)
+    assert st == pkg.capi.MAXITER == st_o and it == 7
+    assert np.linalg.norm(x - ref) / np.linalg.norm(ref) < 1e-8
+
+
+def test_zero_rhs_returns_immediately(gpu_pkg):
+    pkg = gpu_pkg
+    p, b, ru, rv, dt = _inclusions(pkg, 32, 2)
+    b[...] = 0.0
+    x = np.zeros_like(b)
+    with pkg.Solver(p) as s:
+        it, rr, st = s.poisson_solve_rhs(dt, b, ru, rv, x)
+    assert st == 0 and it == 0 and np.all(x == 0)
+
+
+def test_full_size_1024_converges_fp64_and_mixed(gpu_pkg, orc):
+    """Full 1024^2 workload: both arithmetics reach ||r||/||b|| <= 1e-10; the
+    true residual is re-checked with the oracle's operator; both solutions
+    agree to 1e-8 (size-independent properties at the benchmark size)."""
+    pkg = gpu_pkg
+    cap = pkg.capi
+    p, b, ru, rv, dt = _inclusions(pkg, 1024, 200)
+    sols = {}
+    for prec in (cap.PREC_FP64, cap.PREC_MIXED):
+        q = p.copy()
+        q.p_precision = prec
+        x = np.zeros_like(b)
+        with pkg.Solver(q) as s:
+            it, rr, st = s.poisson_solve_rhs(dt, b, ru, rv, x)
+        assert st == cap.OK, (prec, st, it, rr)
+        Ax = orc.poisson_matvec(q, dt, ru, rv, x)
+        r = (b - Ax)[1:-1, 1:-1].copy()
+        r[0, 0] = 0.0  # pinned cell
+        true_rel = np.linalg.norm(r) / np.linalg.norm(b[1:-1, 1:-1])
+        assert true_rel < 2e-10, (prec, true_rel)
+        assert x[1, 1] == 0.0
+        sols[prec] = x
+    d = np.linalg.norm(sols[0] - sols[1]) / np.linalg.norm(sols[0])
+    assert d < 1e-7, d

@@ -1,0 +1,123 @@
+"""GPU geometric VOF parity: bit-exact against the oracle (the VOF kernels
+evaluate every expression in reference order without FMA contraction)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _bubble(pkg, orc, nx=64, ny=128):
+    p, C0, dt = pkg.cases.bubble_case(nx=nx, ny=ny, nsub=8)
+    f = pkg.Fields.allocate(p)
+    f.C[...] = C0
+    orc.apply_vof_bc(p, f.C)
+    orc.update_physical_properties(p, f)
+    orc.compute_curvature_and_csf(p, f)
+    return p, f, dt
+
+
+def _random_C(n, seed):
+    rng = np.random.default_rng(seed)
+    C = rng.uniform(0, 1, (n + 2, n + 2))
+    C[C < 0.3] = 0.0
+    C[C > 0.7] = 1.0
+    return C
+
+
+@pytest.mark.parametrize("recon", ["PLIC", "ELVIRA"])
+def test_reconstruct_bit_exact(gpu_pkg, orc, recon):
+    pkg = gpu_pkg
+    p, f, _ = _bubble(pkg, orc)
+    p.recon = getattr(pkg.capi, "RECON_" + recon)
+    for Cf in (f.C, np.ascontiguousarray(_random_C(p.nx, 1)[:p.ny + 2, :] if p.nx == p.ny else f.C)):
+        s_o = orc.reconstruct(p, Cf)
+        with pkg.Solver(p) as s:
+            s_g = s.reconstruct_interface(Cf)
+        assert np.array_equal(s_g, s_o)
+    # ragged random field (many pure/mixed transitions, ghost-ring cases)
+    q = pkg.cases.make_params(37, 37, 1.0, 1.0)
+    q.recon = p.recon
+    Cr = _random_C(37, 2)
+    with pkg.Solver(q) as s:
+        assert np.array_equal(s.reconstruct_interface(Cr), orc.reconstruct(q, Cr))
+
+
+@pytest.mark.parametrize("recon", ["PLIC", "ELVIRA"])
+@pytest.mark.parametrize("x_first", [True, False])
+def test_wy_step_bit_exact(gpu_pkg, orc, recon, x_first):
+    pkg = gpu_pkg
+    p, f, _ = _bubble(pkg, orc)
+    p.recon = getattr(pkg.capi, "RECON_" + recon)
+    u, v = pkg.cases.random_velocity(p, 0.5, 7)
+    dt = 0.2 * p.dx
+    Co = f.C.copy()
+    orc.wy_step(p, dt, x_first, u, v, Co)
+    Cg = f.C.copy()
+    with pkg.Solver(p) as s:
+        s.advect_vof_weymouth_yue(dt, u, v, Cg, x_first)
+    assert np.array_equal(Cg, Co)
+
+
+def test_advect_with_properties_and_csf_bit_exact(gpu_pkg, orc):
+    pkg = gpu_pkg
+    p, f, dt = _bubble(pkg, orc)
+    u, v = pkg.cases.random_velocity(p, 0.5, 9)
+    f.u[...] = u
+    f.v[...] = v
+    g = f.copy()
+    with pkg.Solver(p) as s:
+        for k in range(4):
+            orc.vof_advect(p, 0.2 * p.dx, k, f)
+            s.advect_vof(0.2 * p.dx, g)
+        assert s.vof_step_count == 4
+    for name in ("C", "rho", "rho_u", "rho_v", "mu", "mu_node", "fx_sigma", "fy_sigma", "curvature"):
+        assert np.array_equal(getattr(g, name), getattr(f, name)), name
+
+
+def test_properties_single_phase_and_no_tension(gpu_pkg, orc):
+    pkg = gpu_pkg
+    p, f, _ = _bubble(pkg, orc, 32, 32)
+    p.enable_two_phase = 0
+    p.enable_surface_tension = 0
+    g = f.copy()
+    orc.update_physical_properties(p, f)
+    orc.compute_curvature_and_csf(p, f)
+    with pkg.Solver(p) as s:
+        s.update_physical_properties(g)
+        s.compute_curvature_and_csf(g)
+    for name in ("rho", "rho_u", "mu_node", "fx_sigma", "curvature"):
+        assert np.array_equal(getattr(g, name), getattr(f, name)), name
+
+
+def test_vortex_period_parity_and_conservation(gpu_pkg, orc):
+    """Whole reversal period of the single-vortex case on the GPU: bit-equal
+    to the oracle at every 100th step; volume conserved per step."""
+    pkg = gpu_pkg
+    cases = pkg.cases
+    p, C0, dt, T = cases.vortex_case(64, recon=pkg.capi.RECON_ELVIRA)
+    f = pkg.Fields.allocate(p)
+    f.C[...] = C0
+    orc.apply_vof_bc(p, f.C)
+    g = f.copy()
+    v0 = f.C[1:-1, 1:-1].sum()
+    t, k, worst, vprev = 0.0, 0, 0.0, v0
+    with pkg.Solver(p) as s:
+        while t < T - 1e-12:
+            u, v = cases.vortex_velocity(p, t, dt, T)
+            for F in (f, g):
+                F.u[...] = u
+                F.v[...] = v
+                orc.apply_velocity_bc(p, F.u, F.v, False)
+            orc.vof_advect(p, dt, k, f)
+            s.advect_vof(dt, g)
+            vk = g.C[1:-1, 1:-1].sum()
+            worst = max(worst, abs(vk - vprev) / v0)
+            vprev = vk
+            if k % 100 == 0:
+                assert np.array_equal(g.C, f.C), k
+            t += dt
+            k += 1
+    assert np.array_equal(g.C, f.C)
+    assert worst < 1e-12
