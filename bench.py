@@ -1,0 +1,359 @@
+#!/usr/bin/env python
+"""Benchmark: standalone variable-density pressure Poisson, 1024^2 cells,
+200 circular heavy inclusions (rho 1000 / 1), zero-mean Gaussian RHS,
+homogeneous Neumann walls with a pinned reference cell, Jacobi-PCG to
+||r||/||b|| <= 1e-10.  Headline = the mixed path (FP32 PCG inside FP64
+iterative refinement); the plain FP64 PCG path is timed beside it.
+
+One step = one Poisson solve from a zero initial guess.  Device time per step
+is measured with CUDA events on the library's own stream; a 512 MiB buffer is
+written between steps (outside the timed events) so every step starts with a
+cold L2.  e2e = the same solve through the host C ABI (pinned host arrays,
+H2D of the inputs and D2H of the pressure inside the timed region).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Poisson solves/s at rel-res 1e-10 (1024^2 variable-density, CG+Jacobi; mixed FP32/FP64-refine vs plain FP64)"
+UNIT = "solves/s"
+WORKLOAD = "variable-density pressure Poisson 1024x1024, 200 inclusions rho 1000/1, Neumann + pinned cell, Jacobi-PCG to rel-res 1e-10"
+# algorithmic bytes per cell (per-unit model): PCG iteration = SpMV (4w) + x,r
+# update with <r,z>,<r,r> (7w) + direction update (4w) = 15 words; FP64
+# refinement residual = read b, x, ax, ay, aP + write r = 6 words.
+W_ITER_FP64 = 15 * 8
+W_ITER_FP32 = 15 * 4
+W_RESID_FP64 = 6 * 8
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks + throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    import torch
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(pkg, orc, p, b, ru, rv, dt, iters_full, nthreads, budget_s):
+    """Time Jacobi-PCG iterations of the oracle on the full 1024^2 system for
+    about budget_s seconds and scale to one whole solve."""
+    x = np.zeros_like(b)
+    q = p.copy()
+    q.p_precision = 0
+    n = 20
+    t0 = time.perf_counter()
+    orc.poisson_fixed_iters(q, dt, b, ru, rv, x, n, nthreads)
+    t1 = time.perf_counter()
+    per_it = (t1 - t0) / n
+    n2 = max(20, min(int(budget_s / max(per_it, 1e-9)), 100000))
+    x[...] = 0.0
+    t0 = time.perf_counter()
+    orc.poisson_fixed_iters(q, dt, b, ru, rv, x, n2, nthreads)
+    t1 = time.perf_counter()
+    per_it = (t1 - t0) / n2
+    solve_s = per_it * iters_full
+    return {"value": 1.0 / solve_s, "unit": UNIT, "cores": nthreads,
+            "kind": "port",
+            "sample": f"{n2} Jacobi-PCG iterations of the FP64 C++ restatement on the full 1024^2 system "
+                      f"({t1 - t0:.1f} s, {per_it * 1e3:.2f} ms/iteration), scaled to the {iters_full} "
+                      f"iterations of one solve to 1e-10"}
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the reference path's CPU implementation (the FP64
+    C++ restatement; the Fortran reference cannot be built on these
+    machines), all host threads, bounded sample per step."""
+    if rank != 0:
+        return
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    orc = ge._load_oracle()
+    p, b, ru, rv, dt = pkg.cases.poisson_inclusions(n=1024, n_incl=200)
+    nth = os.cpu_count() or 1
+    # Iteration count of one full FP64 Jacobi-PCG solve of this system (the
+    # GPU FP64 path runs the same algorithm; measured count).
+    iters_full = int(os.environ.get("COVOF_BENCH_FP64_ITERS", "0")) or 4000
+    x = np.zeros_like(b)
+    for _ in range(args.warmup):
+        orc.poisson_fixed_iters(p, dt, b, ru, rv, x, 5, nth)
+    per = []
+    n_it = 50
+    for _ in range(args.steps):
+        x[...] = 0.0
+        t0 = time.perf_counter()
+        orc.poisson_fixed_iters(p, dt, b, ru, rv, x, n_it, nth)
+        per.append((time.perf_counter() - t0) / n_it)
+    per_it = statistics.median(per)
+    val = 1.0 / (per_it * iters_full)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_it * iters_full * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "n": 1024, "inclusions": 200},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": nth, "kind": "port",
+                         "sample": f"each step: {n_it} Jacobi-PCG iterations (OpenMP, {nth} threads) of the FP64 "
+                                   f"C++ restatement on the full system, scaled to {iters_full} iterations per solve"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import __graft_entry__ as ge
+    ge.build() if rank == 0 else None
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    pkg = ge.load_package()
+    cap = pkg.capi
+    n = args.size
+    p, b, ru, rv, dt = pkg.cases.poisson_inclusions(n=n, n_incl=200 if n >= 512 else 20)
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    tb = torch.from_numpy(b).to(dev)
+    tru = torch.from_numpy(ru).to(dev)
+    trv = torch.from_numpy(rv).to(dev)
+    tp = torch.zeros_like(tb)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    results = {}
+    for name, prec in (("fp64", cap.PREC_FP64), ("mixed", cap.PREC_MIXED)):
+        q = p.copy()
+        q.p_precision = prec
+        s = pkg.Solver(q)
+        stream = torch.cuda.ExternalStream(s.stream_ptr, device=dev)
+        for _ in range(args.warmup):
+            tp.zero_()
+            it, rr, st = s.poisson_solve_rhs_dev(dt, tb, tru, trv, tp)
+            assert st == cap.OK, (name, cap.STATUS_NAMES.get(st), it, rr, s.last_refine_steps())
+        barrier(world)
+        clocks = ClockSampler(local) if (name == "mixed" and rank == 0) else None
+        if clocks:
+            clocks.start()
+        step_ms, kern_ms, iters, outer = [], [], [], []
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1.0)          # cold L2 (512 MiB > 129 MB)
+            tp.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            it, rr, st = s.poisson_solve_rhs_dev(dt, tb, tru, trv, tp)
+            e1.record(stream)
+            e1.synchronize()
+            assert st == cap.OK and rr <= q.p_tol, (name, st, rr)
+            step_ms.append(e0.elapsed_time(e1))
+            kern_ms.append(s.last_solve_ms())
+            iters.append(it)
+            outer.append(s.last_refine_steps())
+        barrier(world)
+        wall = time.perf_counter() - t_wall0
+        clk = clocks.stop() if clocks else None
+        results[name] = {"ms_per_step": statistics.mean(step_ms), "kernel_ms": statistics.mean(kern_ms),
+                         "iters": int(statistics.median(iters)), "outer": int(statistics.median(outer)),
+                         "wall_s": wall, "clocks": clk, "solver": s}
+
+    # e2e through the host C ABI: pinned host arrays, copies inside the region
+    mixed = results["mixed"]
+    s = mixed["solver"]
+
+    def pinned(a):
+        t = torch.from_numpy(a).pin_memory()
+        return t, t.numpy()
+
+    _, hb = pinned(b)
+    _, hru = pinned(ru)
+    _, hrv = pinned(rv)
+    _, hp = pinned(np.zeros_like(b))
+    for _ in range(max(1, args.warmup)):
+        hp[...] = 0.0
+        s.poisson_solve_rhs(dt, hb, hru, hrv, hp)
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        hp[...] = 0.0
+        t0 = time.perf_counter()
+        it, rr, st = s.poisson_solve_rhs(dt, hb, hru, hrv, hp)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        assert st == cap.OK
+    e2e_step = max_over_ranks(statistics.mean(e2e_ms), world)
+    gbytes = 4 * b.nbytes
+
+    ms_mixed = max_over_ranks(mixed["ms_per_step"], world)
+    ms_fp64 = max_over_ranks(results["fp64"]["ms_per_step"], world)
+    value = world * 1000.0 / ms_mixed
+
+    # roofline of the dominant kernel (the persistent mixed PCG kernel)
+    cells = n * n
+    it_m, out_m = mixed["iters"], max(mixed["outer"], 1)
+    alg_bytes = it_m * cells * W_ITER_FP32 + (out_m + 1) * cells * W_RESID_FP64
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (mixed["kernel_ms"] * 1e-3) / 1e9
+    it_f = results["fp64"]["iters"]
+    achieved64 = it_f * cells * W_ITER_FP64 / (results["fp64"]["kernel_ms"] * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get("k_pcg_mixed_bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    line = None
+    if rank == 0:
+        orc = ge._load_oracle()
+        cpu = cpu_sample(pkg, orc, p, b, ru, rv, dt, it_f, 1, args.cpu_budget)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n": n, "inclusions": 200 if n >= 512 else 20, "tol": 1e-10,
+                       "gauge": "pinned cell (1,1)", "l2": "flushed between steps (512 MiB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "plain_fp64": {"ms_per_step": ms_fp64, "solves_per_s": world * 1000.0 / ms_fp64,
+                           "iters": it_f, "kernel_ms": results["fp64"]["kernel_ms"],
+                           "achieved_gbs": achieved64},
+            "mixed": {"iters_fp32": it_m, "refine_steps": mixed["outer"], "kernel_ms": mixed["kernel_ms"]},
+            "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_pcg_mixed", "peak_source": peak_kind,
+                         "note": "algorithmic bytes (15 words/cell/PCG iteration + FP64 residual passes) / event time"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * 1000.0 / e2e_step, "unit": UNIT, "h2d_bytes_per_step": gbytes,
+                    "d2h_bytes_per_step": b.nbytes},
+            "gpu_launches": 4 * args.steps,
+            "clocks": mixed["clocks"],
+        }
+    for r in results.values():
+        r["solver"].close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        rank = int(os.environ.get("RANK", "0"))
+        run_reference(args, world, rank)
+        return
+    world, rank, local = dist_setup()
+    run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

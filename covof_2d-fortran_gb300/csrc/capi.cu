@@ -16,7 +16,8 @@ using namespace covof;
 
 namespace {
 
-constexpr int kCoopThreads = 256;
+constexpr int kPoissonThreads = 1024;  // one cell per thread per 1024-cell tile
+constexpr int kKrylovThreads = 512;    // momentum Krylov kernels (80 registers)
 constexpr int kMaxPartRegions = 16;  // doubles per block in the partials array
 
 template <typename T>
@@ -60,8 +61,9 @@ struct covof_handle {
   // Poisson scratch
   bool have_poisson = false;
   double *px = nullptr, *pb = nullptr, *pr = nullptr, *pd = nullptr, *pAd = nullptr,
-         *pax = nullptr, *pay = nullptr, *paP = nullptr;
-  float *e32 = nullptr, *r32b = nullptr, *r32 = nullptr, *d32 = nullptr, *Ad32 = nullptr,
+         *pax = nullptr, *pay = nullptr, *paP = nullptr, *pisd = nullptr, *pinvD = nullptr,
+         *pd2 = nullptr;
+  float *e32 = nullptr, *r32b = nullptr, *r32 = nullptr, *d32 = nullptr, *d32b = nullptr, *Ad32 = nullptr,
         *ax32 = nullptr, *ay32 = nullptr, *aP32 = nullptr;
   // momentum scratch (each 2g)
   bool have_mom = false;
@@ -123,6 +125,7 @@ int ensure_poisson(covof_handle* h) {
   const size_t g = h->g;
   CS(dalloc(&h->px, g)); CS(dalloc(&h->pb, g)); CS(dalloc(&h->pr, g)); CS(dalloc(&h->pd, g));
   CS(dalloc(&h->pAd, g)); CS(dalloc(&h->pax, g)); CS(dalloc(&h->pay, g)); CS(dalloc(&h->paP, g));
+  CS(dalloc(&h->pisd, g)); CS(dalloc(&h->pinvD, g)); CS(dalloc(&h->pd2, g)); CS(dalloc(&h->d32b, g));
   CS(dalloc(&h->e32, g)); CS(dalloc(&h->r32b, g)); CS(dalloc(&h->r32, g)); CS(dalloc(&h->d32, g));
   CS(dalloc(&h->Ad32, g)); CS(dalloc(&h->ax32, g)); CS(dalloc(&h->ay32, g)); CS(dalloc(&h->aP32, g));
   h->have_poisson = true;
@@ -147,24 +150,25 @@ int ensure_vof(covof_handle* h) {
   return COVOF_OK;
 }
 
-// Co-resident block count for a cooperative kernel, capped by the work.
-int coop_blocks(covof_handle* h, const void* fn, long long warps_needed) {
+// Block count of a persistent cooperative kernel: at most one block per SM
+// (fewer arrivals per grid barrier; the 1024-thread Poisson blocks fill an
+// SM anyway), never more than the work units, never more than co-resident.
+int coop_blocks(covof_handle* h, const void* fn, int threads, long long units) {
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kCoopThreads, 0) != cudaSuccess || per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1)
     return -1;
-  long long maxb = (long long)per_sm * h->sm_count;
-  long long want = (warps_needed + (kCoopThreads / 32) - 1) / (kCoopThreads / 32);
-  if (want < 1) want = 1;
-  long long nb = want < maxb ? want : maxb;
+  long long nb = h->sm_count;
+  if (units < nb) nb = units < 1 ? 1 : units;
+  if (nb > (long long)per_sm * h->sm_count) nb = (long long)per_sm * h->sm_count;
   if (nb > h->part_blocks) nb = h->part_blocks;
   return (int)nb;
 }
 
-int launch_coop(covof_handle* h, const void* fn, int nblocks, void** args, bool timed) {
+int launch_coop(covof_handle* h, const void* fn, int nblocks, int threads, void** args, bool timed) {
   CK(cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned int), h->stream));
   CK(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
   if (timed) CK(cudaEventRecord(h->ev0, h->stream));
-  CK(cudaLaunchCooperativeKernel(fn, dim3(nblocks), dim3(kCoopThreads), args, 0, h->stream));
+  CK(cudaLaunchCooperativeKernel(fn, dim3(nblocks), dim3(threads), args, 0, h->stream));
   if (timed) CK(cudaEventRecord(h->ev1, h->stream));
   return COVOF_OK;
 }
@@ -198,25 +202,28 @@ int poisson_dev(covof_handle* h, double dt, const double* u, const double* v, co
   const dim3 blk(32, 8), grd = grid2(P.nx, P.ny, blk);
   k_poisson_assemble<<<grd, blk, 0, h->stream>>>(h->D, dt, P.dx, P.dy, wall_flags(P), rho_u, rho_v, u, v,
                                                   b, pinned, h->pax, h->pay, h->paP, h->pb,
-                                                  mixed ? h->ax32 : nullptr, h->ay32, h->aP32);
+                                                  mixed ? h->pisd : nullptr, mixed ? nullptr : h->pinvD);
+  if (mixed)
+    k_poisson_scale32<<<grid2(P.nx + 1, P.ny + 1, blk), blk, 0, h->stream>>>(h->D, h->pax, h->pay, h->pisd,
+                                                                           h->ax32, h->ay32, h->aP32);
   k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, p, h->px, pinned);
   CK(cudaGetLastError());
   PoissonArgs a;
   a.D = h->D;
-  a.x = h->px; a.b = h->pb; a.r = h->pr; a.d = h->pd; a.Ad = h->pAd;
-  a.ax = h->pax; a.ay = h->pay; a.aP = h->paP;
-  a.e32 = h->e32; a.r32b = h->r32b; a.r32 = h->r32; a.d32 = h->d32; a.Ad32 = h->Ad32;
+  a.x = h->px; a.b = h->pb; a.r = h->pr; a.d = h->pd; a.d2 = h->pd2; a.Ad = h->pAd;
+  a.ax = h->pax; a.ay = h->pay; a.aP = h->paP; a.invD = h->pinvD; a.isd = h->pisd;
+  a.e32 = h->e32; a.r32b = h->r32b; a.r32 = h->r32; a.d32 = h->d32; a.d32b = h->d32b; a.Ad32 = h->Ad32;
   a.ax32 = h->ax32; a.ay32 = h->ay32; a.aP32 = h->aP32;
   a.bar = h->bar; a.err = h->err; a.part = h->part; a.res = h->d_pres;
   a.tol = P.p_tol; a.inner_tol = P.p_inner_tol;
   a.max_iter = P.p_max_iter; a.inner_max_iter = P.p_inner_max_iter;
   a.max_refine = P.p_max_refine; a.pinned = pinned;
   const void* fn = mixed ? (const void*)k_pcg_mixed : (const void*)k_pcg_fp64;
-  const long long nseg = (long long)((P.nx + 31) / 32) * P.ny;
-  const int nb = coop_blocks(h, fn, nseg);
+  const long long ntiles = (long long)make_tiles(h->D).ntiles;
+  const int nb = coop_blocks(h, fn, kPoissonThreads, ntiles);
   if (nb < 1) return COVOF_CUDA_ERROR;
   void* args[] = {&a};
-  CS(launch_coop(h, fn, nb, args, true));
+  CS(launch_coop(h, fn, nb, kPoissonThreads, args, true));
   k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, h->px, p, 0);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(h->h_pres, h->d_pres, sizeof(PcgResult), cudaMemcpyDeviceToHost, h->stream));
@@ -304,10 +311,10 @@ int predictor_dev(covof_handle* h, double dt, double* u, double* v, const double
                  : P.linear_solver == COVOF_LINEAR_CG ? (const void*)k_cg
                  : (const void*)k_bicgstab2;
   const long long nseg = (long long)((P.nx + 1 + 31) / 32) * P.ny + (long long)((P.nx + 31) / 32) * (P.ny + 1);
-  const int nb = coop_blocks(h, fn, nseg);
+  const int nb = coop_blocks(h, fn, kKrylovThreads, (nseg + kKrylovThreads / 32 - 1) / (kKrylovThreads / 32));
   if (nb < 1) return COVOF_CUDA_ERROR;
   void* args[] = {&a};
-  CS(launch_coop(h, fn, nb, args, false));
+  CS(launch_coop(h, fn, nb, kKrylovThreads, args, false));
   k_mom_unpack<<<grd, blk, 0, h->stream>>>(a, u, v);
   CK(cudaGetLastError());
   CS(velocity_bc_dev(h, u, v));
@@ -478,7 +485,7 @@ int covof_create(const covof_params* params, covof_handle** out) {
   if (cudaStreamCreate(&h->stream) != cudaSuccess) return fail(COVOF_CUDA_ERROR);
   if (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
     return fail(COVOF_CUDA_ERROR);
-  h->part_blocks = 8 * h->sm_count;  // >= any co-resident count at 256 threads
+  h->part_blocks = h->sm_count;  // persistent kernels run at most one block per SM
   if (dalloc(&h->bar, 2) || dalloc(&h->err, 1) ||
       dalloc(&h->part, (size_t)kMaxPartRegions * h->part_blocks) ||
       dalloc(&h->d_pres, 1) || dalloc(&h->d_kres, 1))
@@ -496,11 +503,11 @@ int covof_destroy(covof_handle* h) {
   double** fl[] = {&h->f_u, &h->f_v, &h->f_p, &h->f_rho_u, &h->f_rho_v, &h->f_mu, &h->f_mu_node,
                    &h->f_fx, &h->f_fy, &h->f_u_old, &h->f_v_old, &h->f_C, &h->f_rho, &h->f_curv,
                    &h->f_b, &h->f_x2, &h->f_seg, &h->px, &h->pb, &h->pr, &h->pd, &h->pAd,
-                   &h->pax, &h->pay, &h->paP, &h->mx, &h->mrhs, &h->mdiag, &h->cs, &h->seg,
+                   &h->pax, &h->pay, &h->paP, &h->pisd, &h->pinvD, &h->pd2, &h->mx, &h->mrhs, &h->mdiag, &h->cs, &h->seg,
                    &h->cnx, &h->cny, &h->ckap, &h->part};
   for (double** q : fl) dfree(*q);
   for (int q = 0; q < 7; ++q) dfree(h->mv[q]);
-  float** ff[] = {&h->e32, &h->r32b, &h->r32, &h->d32, &h->Ad32, &h->ax32, &h->ay32, &h->aP32};
+  float** ff[] = {&h->e32, &h->r32b, &h->r32, &h->d32, &h->d32b, &h->Ad32, &h->ax32, &h->ay32, &h->aP32};
   for (float** q : ff) dfree(*q);
   dfree(h->bar); dfree(h->err); dfree(h->d_pres); dfree(h->d_kres);
   if (h->h_pres) cudaFreeHost(h->h_pres);
@@ -605,7 +612,7 @@ int covof_poisson_apply(covof_handle* h, double dt, const double* rho_u, const d
   // would do as well; only the coefficients are used).
   k_poisson_assemble<<<grd, blk, 0, h->stream>>>(h->D, dt, P.dx, P.dy, wall_flags(P), h->f_rho_u, h->f_rho_v,
                                                   nullptr, nullptr, h->f_b, 0, h->pax, h->pay, h->paP,
-                                                  h->pb, nullptr, nullptr, nullptr);
+                                                  h->pb, nullptr, nullptr);
   // operand with a zero ghost ring, as inside the solver
   CK(cudaMemsetAsync(h->px, 0, g * sizeof(double), h->stream));
   k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, h->f_p, h->px, 0);

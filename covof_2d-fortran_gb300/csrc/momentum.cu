@@ -371,7 +371,7 @@ __device__ void krylov_finish(const MomArgs& a, int iters, int status, bool ok) 
 }
 
 // src/module_linear_solvers.f90:584-730 solve_bicgstab (left Jacobi).
-__global__ void __launch_bounds__(256) k_bicgstab(MomArgs a) {
+__global__ void __launch_bounds__(512) k_bicgstab(MomArgs a) {
   DofWalker W(a.D);
   GridReducer R{a.part, a.bar, a.err, gridDim.x, 0};
   double *x = a.x, *bh = a.v0, *r = a.v1, *rt = a.v2, *p = a.v3, *v = a.v4, *s = a.v5, *t = a.v6;
@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(256) k_bicgstab(MomArgs a) {
 
 // src/module_linear_solvers.f90:735-838 solve_cg (unpreconditioned operator,
 // separate Jacobi application).
-__global__ void __launch_bounds__(256) k_cg(MomArgs a) {
+__global__ void __launch_bounds__(512) k_cg(MomArgs a) {
   DofWalker W(a.D);
   GridReducer R{a.part, a.bar, a.err, gridDim.x, 0};
   double *x = a.x, *r = a.v1, *p = a.v3, *Ap = a.v4;
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(256) k_cg(MomArgs a) {
 }
 
 // src/module_linear_solvers.f90:361-579 solve_bicgstab2 (left Jacobi).
-__global__ void __launch_bounds__(256) k_bicgstab2(MomArgs a) {
+__global__ void __launch_bounds__(512) k_bicgstab2(MomArgs a) {
   DofWalker W(a.D);
   GridReducer R{a.part, a.bar, a.err, gridDim.x, 0};
   double *x = a.x, *rt = a.v0, *r0 = a.v1, *r1 = a.v2, *r2 = a.v3, *u0 = a.v4, *u1 = a.v5, *u2 = a.v6;

@@ -32,8 +32,7 @@ __global__ void k_poisson_assemble(Dims D, double dt, double dx, double dy, int4
                                    const double* __restrict__ b_in, int pinned,
                                    double* __restrict__ ax, double* __restrict__ ay,
                                    double* __restrict__ aP, double* __restrict__ b,
-                                   float* __restrict__ ax32, float* __restrict__ ay32,
-                                   float* __restrict__ aP32) {
+                                   double* __restrict__ isd, double* __restrict__ invD) {
   int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (i > D.nx || j > D.ny) return;
@@ -72,11 +71,24 @@ __global__ void k_poisson_assemble(Dims D, double dt, double dx, double dy, int4
   }
   if (pinned && i == 1 && j == 1) bb = 0.0;
   b[k] = bb;
-  if (ax32) {
-    ax32[k] = (float)aW; ay32[k] = (float)aS; aP32[k] = (float)ap;
-    if (i == D.nx) ax32[k + 1] = (float)aE;
-    if (j == D.ny) ay32[k + D.P] = (float)aN;
-  }
+  if (isd) isd[k] = 1.0 / sqrt(ap);
+  if (invD) invD[k] = 1.0 / ap;
+}
+
+// FP32 copy of the symmetrically scaled operator D^-1/2 A D^-1/2 (unit
+// diagonal) for the mixed path: a face coefficient becomes
+// a_f / sqrt(aP_left aP_right).  Ghost entries of isd are zero, so an
+// outflow face (which only multiplies a zero ghost) gets a zero coefficient.
+__global__ void k_poisson_scale32(Dims D, const double* __restrict__ ax, const double* __restrict__ ay,
+                                  const double* __restrict__ isd, float* __restrict__ ax32,
+                                  float* __restrict__ ay32, float* __restrict__ aP32) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > D.nx + 1 || j > D.ny + 1) return;
+  const int k = D.id(i, j);
+  if (j <= D.ny) ax32[k] = (float)(ax[k] * isd[k - 1] * (i <= D.nx ? isd[k] : 0.0));
+  if (i <= D.nx) ay32[k] = (float)(ay[k] * isd[k - D.P] * (j <= D.ny ? isd[k] : 0.0));
+  if (i <= D.nx && j <= D.ny) aP32[k] = 1.0f;
 }
 
 // Interior copy between a caller field and a solver vector (ghosts of dst untouched).
@@ -90,344 +102,330 @@ __global__ void k_copy_interior(Dims D, const double* __restrict__ src, double* 
 }
 
 // ---------------------------------------------------------------------------
-// Arithmetic helpers with explicit rounding (no contraction), per type.
-template <typename T> struct Ar;
-template <> struct Ar<double> {
-  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
-  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-  static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
-};
-template <> struct Ar<float> {
-  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
-  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
-  static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
-  static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
-};
-
-// y = A x at (i,j), reference term order.  x is read through L2 (__ldcg):
-// other blocks wrote it earlier in this kernel.
-template <typename T>
-__device__ __forceinline__ T stencil(const Dims& D, int k, const T* __restrict__ x,
-                                     const T* __restrict__ ax, const T* __restrict__ ay,
-                                     const T* __restrict__ aP) {
-  using A = Ar<T>;
-  T val = A::mul(aP[k], __ldcg(x + k));
-  val = A::sub(val, A::mul(ax[k], __ldcg(x + k - 1)));
-  val = A::sub(val, A::mul(ax[k + 1], __ldcg(x + k + 1)));
-  val = A::sub(val, A::mul(ay[k], __ldcg(x + k - D.P)));
-  val = A::sub(val, A::mul(ay[k + D.P], __ldcg(x + k + D.P)));
+// Exact operator (reference term order, no contraction): used by the
+// operator-apply entry point, whose result is compared bit for bit.
+__device__ __forceinline__ double stencil_exact(const Dims& D, int k, const double* __restrict__ x,
+                                                const double* __restrict__ ax,
+                                                const double* __restrict__ ay,
+                                                const double* __restrict__ aP) {
+  double val = __dmul_rn(aP[k], x[k]);
+  val = __dsub_rn(val, __dmul_rn(ax[k], x[k - 1]));
+  val = __dsub_rn(val, __dmul_rn(ax[k + 1], x[k + 1]));
+  val = __dsub_rn(val, __dmul_rn(ay[k], x[k - D.P]));
+  val = __dsub_rn(val, __dmul_rn(ay[k + D.P], x[k + D.P]));
   return val;
 }
 
-// Static cell ownership: warp w of the grid walks 32-wide row segments
-// s = w, w + nwarps, ...; a thread owns the same cells in every phase.
-struct Walker {
-  int nsx, nseg, gw, nw, lane;
-  __device__ Walker(const Dims& D) {
-    nsx = (D.nx + 31) >> 5;
-    nseg = nsx * D.ny;
-    lane = threadIdx.x & 31;
-    gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    nw = (gridDim.x * blockDim.x) >> 5;
-  }
-};
-#define FOR_OWNED_CELLS(D, W, i, j, k)                                   \
-  for (int s_ = (W).gw; s_ < (W).nseg; s_ += (W).nw)                      \
-    for (int j = s_ / (W).nsx + 1, i = (s_ - (j - 1) * (W).nsx) * 32 + (W).lane + 1, k = (D).id(i, j); \
-         i <= (D).nx; i = (D).nx + 1)
-
-struct Ctl {
-  unsigned int* bar;
-  int* err;
-  double* part;  // nblocks * 4
-  unsigned int nblocks;
-};
+__device__ __forceinline__ double fmad_(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fmad_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
 // ---------------------------------------------------------------------------
-// One PCG solve on (x, b) in precision T (Jacobi preconditioner z = r / aP).
-// Returns the number of iterations; *rnorm_out / *bnorm_out are the final
-// recursive residual norm and ||b||; *st_out the loop status.  `rel` is the
-// stopping ratio on ||r||/||b||.  r, d, Ad are scratch vectors.
+// Tiled persistent PCG.  The interior is cut into TX x TY tiles (TX*TY =
+// 1024 = blockDim.x, one cell per thread); tile t belongs to block t % G for
+// the whole solve, so a cell is read and written by the same thread in every
+// phase.  Vectors written by other blocks (r, the old direction) are read
+// through L2 (__ldcg) after a grid barrier, into a shared-memory halo tile.
+//
+// One iteration = 2 grid barriers:
+//   phase S: d_new = z + beta d_old on the tile and its halo (from r, d_old),
+//            Ad = A d_new on the tile; write d_new, Ad; partial <d,Ad>
+//   phase U: alpha; x += alpha d; r -= alpha Ad; partials <r,r>, <r,z>
+// d is double-buffered (phase S of iteration k writes buffer k&1 and reads
+// buffer (k+1)&1), so no block overwrites a direction another block reads.
+__host__ __device__ Tiles make_tiles(const Dims& D) {
+  Tiles t;
+  t.TX = D.nx <= 32 ? 32 : (D.nx <= 64 ? 64 : 128);
+  t.TY = 1024 / t.TX;
+  t.ntx = (D.nx + t.TX - 1) / t.TX;
+  t.nty = (D.ny + t.TY - 1) / t.TY;
+  t.ntiles = t.ntx * t.nty;
+  return t;
+}
+
+constexpr int kHalo = 130 * 10;  // max (TX+2)*(TY+2) over TX in {32, 64, 128}
+
 template <typename T>
-__device__ int pcg_core(const Dims& D, const Ctl& C, const Walker& W, T* x, const T* b, T* r, T* d,
-                        T* Ad, const T* ax, const T* ay, const T* aP, int pinned, double rel,
-                        int max_iter, int* st_out, double* rnorm_out, double* bnorm_out,
-                        bool* ok_out) {
-  using A = Ar<T>;
-  const int bid = blockIdx.x;
-  bool ok = true;
-  // r = b - A x ; partials <b,b>, <r,r>
-  {
-    T acc[2] = {T(0), T(0)};
-    FOR_OWNED_CELLS(D, W, i, j, k) {
-      T y = stencil<T>(D, k, x, ax, ay, aP);
-      T rr = A::sub(b[k], y);
-      if (pinned && k == D.P + 1) rr = T(0);
-      r[k] = rr;
-      acc[0] = A::add(acc[0], A::mul(b[k], b[k]));
-      acc[1] = A::add(acc[1], A::mul(rr, rr));
-    }
-    block_sum<T, 2>(acc);
-    if (threadIdx.x == 0) { C.part[bid * 4 + 0] = (double)acc[0]; C.part[bid * 4 + 1] = (double)acc[1]; }
-  }
-  ok = grid_barrier(C.bar, C.nblocks, C.err);
-  double tot[4];
-  {
-    double t2[2];
-    // combine with stride 4 layout
-    __shared__ double sh2[2];
-    if (threadIdx.x < 32) {
-      double a0 = 0.0, a1 = 0.0;
-      for (int q = threadIdx.x; q < (int)C.nblocks; q += 32) {
-        a0 += __ldcg(C.part + q * 4 + 0);
-        a1 += __ldcg(C.part + q * 4 + 1);
+struct Sys {
+  T* x; const T* b; T* r; T* d0; T* d1; T* Ad;
+  const T* ax; const T* ay; const T* aP; const T* invD;  // aP, invD unused when unit diagonal
+};
+
+template <typename T, bool UNIT>
+__device__ __forceinline__ T precond(const Sys<T>& S, int k, T rv) {
+  return UNIT ? rv : rv * S.invD[k];
+}
+
+// Grid reduction of NV values: each thread accumulates its own cells in T
+// (FP32 on the mixed path), the block and grid combines run in FP64.
+template <typename T, int NV>
+__device__ __forceinline__ bool reduce(GridReducer& R, T (&acc)[NV], double (&out)[NV]) {
+  double v[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) v[q] = (double)acc[q];
+  bool ok = R.sum(v);
+#pragma unroll
+  for (int q = 0; q < NV; ++q) out[q] = v[q];
+  return ok;
+}
+
+// Phase S on one tile.  Returns this thread's <d,Ad> contribution.
+template <typename T, bool UNIT>
+__device__ __forceinline__ T phase_stencil(const Dims& D, const Tiles& tl, int tile, const Sys<T>& S,
+                                           const T* __restrict__ dold, T* __restrict__ dnew, T beta,
+                                           bool first, int pinned_k, T* sd) {
+  const int tx0 = (tile % tl.ntx) * tl.TX, ty0 = (tile / tl.ntx) * tl.TY;  // 0-based interior origin
+  const int HX = tl.TX + 2, HY = tl.TY + 2;
+  // d_new on tile + halo into shared memory (zero outside the ghost ring)
+  for (int e = threadIdx.x; e < HX * HY; e += blockDim.x) {
+    const int lx = e % HX, ly = e / HX;
+    const int i = tx0 + lx, j = ty0 + ly;  // global index incl. ghost (i = 0 .. nx+1)
+    T v = T(0);
+    if (i <= D.nx + 1 && j <= D.ny + 1) {
+      const int k = D.id(i, j);
+      const bool interior = i >= 1 && i <= D.nx && j >= 1 && j <= D.ny;
+      if (interior && k != pinned_k) {
+        const T z = precond<T, UNIT>(S, k, __ldcg(S.r + k));
+        v = first ? z : fmad_(beta, __ldcg(dold + k), z);
       }
-      a0 = warp_sum(a0); a1 = warp_sum(a1);
-      if (threadIdx.x == 0) { sh2[0] = a0; sh2[1] = a1; }
     }
-    __syncthreads();
-    t2[0] = sh2[0]; t2[1] = sh2[1];
-    __syncthreads();
-    tot[0] = t2[0]; tot[1] = t2[1];
+    sd[e] = v;
   }
-  double b_norm = sqrt(tot[0]);
-  if (b_norm < 1.0e-30) b_norm = 1.0;
-  double r_norm = sqrt(tot[1]);
-  int iters = 0, status = COVOF_OK;
-  if (ok && r_norm / b_norm > rel) {
-    // d = z = r / aP ; <r,z>
-    T acc[1] = {T(0)};
-    FOR_OWNED_CELLS(D, W, i, j, k) {
-      T z = A::div(r[k], aP[k]);
-      if (pinned && k == D.P + 1) z = T(0);
-      d[k] = z;
-      acc[0] = A::add(acc[0], A::mul(r[k], z));
-    }
-    block_sum<T, 1>(acc);
-    // reuse slot 2 so the previous slots stay readable until everyone passed
-    if (threadIdx.x == 0) C.part[bid * 4 + 2] = (double)acc[0];
-    ok = grid_barrier(C.bar, C.nblocks, C.err);
-    double rz_old;
-    {
-      __shared__ double sh1;
-      if (threadIdx.x < 32) {
-        double a0 = 0.0;
-        for (int q = threadIdx.x; q < (int)C.nblocks; q += 32) a0 += __ldcg(C.part + q * 4 + 2);
-        a0 = warp_sum(a0);
-        if (threadIdx.x == 0) sh1 = a0;
+  __syncthreads();
+  const int lx = threadIdx.x % tl.TX, ly = threadIdx.x / tl.TX;
+  const int i = tx0 + lx + 1, j = ty0 + ly + 1;
+  T contrib = T(0);
+  if (i <= D.nx && j <= D.ny) {
+    const int k = D.id(i, j);
+    const int c = (ly + 1) * HX + (lx + 1);
+    const T dc = sd[c];
+    T v = UNIT ? dc : S.aP[k] * dc;
+    v = fmad_(-S.ax[k], sd[c - 1], v);
+    v = fmad_(-S.ax[k + 1], sd[c + 1], v);
+    v = fmad_(-S.ay[k], sd[c - HX], v);
+    v = fmad_(-S.ay[k + D.P], sd[c + HX], v);
+    if (k == pinned_k) v = T(0);
+    dnew[k] = dc;
+    S.Ad[k] = v;
+    contrib = dc * v;
+  }
+  __syncthreads();
+  return contrib;
+}
+
+struct PcgOut {
+  int iters, status;
+  double r_norm, b_norm;
+  bool ok;
+};
+
+// Jacobi-PCG on S.x (in/out).  x_zero: S.x is known to be zero (skip A x).
+template <typename T, bool UNIT>
+__device__ PcgOut pcg_tiled(const Dims& D, const Tiles& tl, GridReducer& R, const Sys<T>& S,
+                            int pinned, double rel, int max_iter, bool x_zero, T* sd) {
+  const int pinned_k = pinned ? D.P + 1 : -1;
+  PcgOut o{0, COVOF_OK, 0.0, 1.0, true};
+  // r = b - A x ; <b,b>, <r,r>, <r,z>
+  {
+    T acc[3] = {T(0), T(0), T(0)};
+    for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+      const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
+      const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
+      if (i <= D.nx && j <= D.ny) {
+        const int k = D.id(i, j);
+        T rv = S.b[k];
+        if (!x_zero) {
+          const T xc = __ldcg(S.x + k);
+          T v = UNIT ? xc : S.aP[k] * xc;
+          v = fmad_(-S.ax[k], __ldcg(S.x + k - 1), v);
+          v = fmad_(-S.ax[k + 1], __ldcg(S.x + k + 1), v);
+          v = fmad_(-S.ay[k], __ldcg(S.x + k - D.P), v);
+          v = fmad_(-S.ay[k + D.P], __ldcg(S.x + k + D.P), v);
+          rv = rv - v;
+        }
+        if (k == pinned_k) rv = T(0);
+        S.r[k] = rv;
+        const T z = (k == pinned_k) ? T(0) : precond<T, UNIT>(S, k, rv);
+        acc[0] = fmad_(S.b[k], S.b[k], acc[0]);
+        acc[1] = fmad_(rv, rv, acc[1]);
+        acc[2] = fmad_(rv, z, acc[2]);
       }
-      __syncthreads();
-      rz_old = sh1;
-      __syncthreads();
     }
+    double tot[3];
+    o.ok = reduce<T, 3>(R, acc, tot);
+    o.b_norm = sqrt(tot[0]);
+    if (o.b_norm < 1.0e-30) o.b_norm = 1.0;
+    o.r_norm = sqrt(tot[1]);
+    if (!o.ok || !(o.r_norm / o.b_norm > rel)) {
+      if (!o.ok) o.status = COVOF_TIMEOUT;
+      return o;
+    }
+    double rz_old = tot[2];
+    double beta = 0.0;
     bool converged = false;
-    int slot = 0;  // alternate partial slots {0,1} / {2,3} between reductions
-    while (ok && iters < max_iter) {
-      iters++;
-      // Ad = A d ; <d,Ad>
-      {
-        T acc1[1] = {T(0)};
-        FOR_OWNED_CELLS(D, W, i, j, k) {
-          T y = stencil<T>(D, k, d, ax, ay, aP);
-          if (pinned && k == D.P + 1) y = T(0);
-          Ad[k] = y;
-          acc1[0] = A::add(acc1[0], A::mul(d[k], y));
-        }
-        block_sum<T, 1>(acc1);
-        if (threadIdx.x == 0) C.part[bid * 4 + slot] = (double)acc1[0];
-      }
-      ok = grid_barrier(C.bar, C.nblocks, C.err);
-      if (!ok) break;
-      double dAd;
-      {
-        __shared__ double sh1;
-        if (threadIdx.x < 32) {
-          double a0 = 0.0;
-          for (int q = threadIdx.x; q < (int)C.nblocks; q += 32) a0 += __ldcg(C.part + q * 4 + slot);
-          a0 = warp_sum(a0);
-          if (threadIdx.x == 0) sh1 = a0;
-        }
-        __syncthreads();
-        dAd = sh1;
-        __syncthreads();
-      }
-      slot ^= 2;
-      if (fabs(dAd) < 1.0e-35) { status = COVOF_BREAKDOWN; break; }
-      const double alpha = rz_old / dAd;
+    while (o.iters < max_iter) {
+      const int it = o.iters;
+      o.iters++;
+      T* dnew = (it & 1) ? S.d1 : S.d0;
+      const T* dold = (it & 1) ? S.d0 : S.d1;
+      // phase S
+      T a1[1] = {T(0)};
+      for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x)
+        a1[0] += phase_stencil<T, UNIT>(D, tl, tile, S, dold, dnew, (T)beta, it == 0, pinned_k, sd);
+      double dAd[1];
+      if (!reduce<T, 1>(R, a1, dAd)) { o.ok = false; break; }
+      if (fabs(dAd[0]) < 1.0e-35) { o.status = COVOF_BREAKDOWN; break; }
+      const double alpha = rz_old / dAd[0];
       const T al = (T)alpha;
-      // x += alpha d ; r -= alpha Ad ; <r,r>, <r,z>
-      {
-        T acc2[2] = {T(0), T(0)};
-        FOR_OWNED_CELLS(D, W, i, j, k) {
-          T xv = A::add(x[k], A::mul(al, d[k]));
-          T rv = A::sub(r[k], A::mul(al, Ad[k]));
-          x[k] = xv; r[k] = rv;
-          T z = A::div(rv, aP[k]);
-          if (pinned && k == D.P + 1) z = T(0);
-          acc2[0] = A::add(acc2[0], A::mul(rv, rv));
-          acc2[1] = A::add(acc2[1], A::mul(rv, z));
+      // phase U
+      T a2[2] = {T(0), T(0)};
+      for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+        const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
+        const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
+        if (i <= D.nx && j <= D.ny) {
+          const int k = D.id(i, j);
+          S.x[k] = fmad_(al, dnew[k], S.x[k]);
+          const T rv = fmad_(-al, S.Ad[k], S.r[k]);
+          S.r[k] = rv;
+          const T z = (k == pinned_k) ? T(0) : precond<T, UNIT>(S, k, rv);
+          a2[0] = fmad_(rv, rv, a2[0]);
+          a2[1] = fmad_(rv, z, a2[1]);
         }
-        block_sum<T, 2>(acc2);
-        if (threadIdx.x == 0) { C.part[bid * 4 + slot] = (double)acc2[0]; C.part[bid * 4 + slot + 1] = (double)acc2[1]; }
       }
-      ok = grid_barrier(C.bar, C.nblocks, C.err);
-      if (!ok) break;
-      double rr, rz_new;
-      {
-        __shared__ double sh2[2];
-        if (threadIdx.x < 32) {
-          double a0 = 0.0, a1 = 0.0;
-          for (int q = threadIdx.x; q < (int)C.nblocks; q += 32) {
-            a0 += __ldcg(C.part + q * 4 + slot);
-            a1 += __ldcg(C.part + q * 4 + slot + 1);
-          }
-          a0 = warp_sum(a0); a1 = warp_sum(a1);
-          if (threadIdx.x == 0) { sh2[0] = a0; sh2[1] = a1; }
-        }
-        __syncthreads();
-        rr = sh2[0]; rz_new = sh2[1];
-        __syncthreads();
-      }
-      slot ^= 2;
-      r_norm = sqrt(rr);
-      if (isnan(r_norm)) { status = COVOF_NAN; break; }
-      if (r_norm / b_norm <= rel) { converged = true; break; }
-      if (fabs(rz_old) < 1.0e-35) { status = COVOF_BREAKDOWN; break; }
-      const double beta = rz_new / rz_old;
-      rz_old = rz_new;
-      const T be = (T)beta;
-      // d = z + beta d
-      FOR_OWNED_CELLS(D, W, i, j, k) {
-        T z = A::div(r[k], aP[k]);
-        if (pinned && k == D.P + 1) z = T(0);
-        d[k] = A::add(z, A::mul(be, d[k]));
-      }
-      ok = grid_barrier(C.bar, C.nblocks, C.err);
+      double t2[2];
+      if (!reduce<T, 2>(R, a2, t2)) { o.ok = false; break; }
+      o.r_norm = sqrt(t2[0]);
+      if (isnan(o.r_norm)) { o.status = COVOF_NAN; break; }
+      if (o.r_norm / o.b_norm <= rel) { converged = true; break; }
+      if (fabs(rz_old) < 1.0e-35) { o.status = COVOF_BREAKDOWN; break; }
+      beta = t2[1] / rz_old;
+      rz_old = t2[1];
     }
-    if (ok && status == COVOF_OK && !converged) status = COVOF_MAXITER;
+    if (o.ok && o.status == COVOF_OK && !converged) o.status = COVOF_MAXITER;
+    if (!o.ok) o.status = COVOF_TIMEOUT;
   }
-  if (!ok) status = COVOF_TIMEOUT;
-  *st_out = status;
-  *rnorm_out = r_norm;
-  *bnorm_out = b_norm;
-  *ok_out = ok;
-  return iters;
+  return o;
 }
 
 // Mean removal (reference gauge, src/module_simulation.f90:2579-2582).
-__device__ bool remove_mean(const Dims& D, const Ctl& C, const Walker& W, double* x) {
+__device__ bool remove_mean(const Dims& D, const Tiles& tl, GridReducer& R, double* x) {
   double acc[1] = {0.0};
-  FOR_OWNED_CELLS(D, W, i, j, k) acc[0] += x[k];
-  block_sum<double, 1>(acc);
-  // A region of its own: the PCG loop may have exited right after a combine
-  // that other blocks are still reading.
-  double* mpart = C.part + 4 * C.nblocks;
-  if (threadIdx.x == 0) mpart[blockIdx.x] = acc[0];
-  bool ok = grid_barrier(C.bar, C.nblocks, C.err);
-  if (!ok) return false;
-  __shared__ double shm;
-  if (threadIdx.x < 32) {
-    double a0 = 0.0;
-    for (int q = threadIdx.x; q < (int)C.nblocks; q += 32) a0 += __ldcg(mpart + q);
-    a0 = warp_sum(a0);
-    if (threadIdx.x == 0) shm = a0;
+  for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+    const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
+    const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
+    if (i <= D.nx && j <= D.ny) acc[0] += x[D.id(i, j)];
   }
-  __syncthreads();
-  const double mean = shm / (double)((long long)D.nx * D.ny);
-  FOR_OWNED_CELLS(D, W, i, j, k) x[k] = x[k] - mean;
+  double tot[1];
+  if (!reduce<double, 1>(R, acc, tot)) return false;
+  const double mean = tot[0] / (double)((long long)D.nx * D.ny);
+  for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+    const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
+    const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
+    if (i <= D.nx && j <= D.ny) { const int k = D.id(i, j); x[k] = x[k] - mean; }
+  }
   return true;
 }
 
-// Plain FP64 PCG solve.
-__global__ void __launch_bounds__(256) k_pcg_fp64(PoissonArgs a) {
+// Plain FP64 Jacobi-PCG solve.
+__global__ void __launch_bounds__(1024, 1) k_pcg_fp64(PoissonArgs a) {
+  __shared__ double sd[kHalo];
   const Dims D = a.D;
-  Ctl C{a.bar, a.err, a.part, gridDim.x};
-  Walker W(D);
-  int st; double rn, bn; bool ok;
-  int it = pcg_core<double>(D, C, W, a.x, a.b, a.r, a.d, a.Ad, a.ax, a.ay, a.aP, a.pinned, a.tol,
-                            a.max_iter, &st, &rn, &bn, &ok);
-  if (ok && !a.pinned) ok = remove_mean(D, C, W, a.x);
+  const Tiles tl = make_tiles(D);
+  GridReducer R{a.part, a.bar, a.err, gridDim.x, 0};
+  Sys<double> S{a.x, a.b, a.r, a.d, a.d2, a.Ad, a.ax, a.ay, a.aP, a.invD};
+  PcgOut o = pcg_tiled<double, false>(D, tl, R, S, a.pinned, a.tol, a.max_iter, false, sd);
+  bool ok = o.ok;
+  if (ok && !a.pinned) ok = remove_mean(D, tl, R, a.x);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    a.res->iters = it;
-    a.res->relres = rn / bn;
-    a.res->status = ok ? st : COVOF_TIMEOUT;
+    a.res->iters = o.iters;
+    a.res->relres = o.r_norm / o.b_norm;
+    a.res->status = ok ? o.status : COVOF_TIMEOUT;
     a.res->outer = 0;
   }
 }
 
-// Mixed: FP32 PCG inner solves inside FP64 iterative refinement.
-__global__ void __launch_bounds__(256) k_pcg_mixed(PoissonArgs a) {
+// Mixed: FP32 PCG inner solves on S A S (unit diagonal) inside FP64
+// iterative refinement on the true FP64 residual.
+__global__ void __launch_bounds__(1024, 1) k_pcg_mixed(PoissonArgs a) {
+  __shared__ float sd[kHalo];
   const Dims D = a.D;
-  Ctl C{a.bar, a.err, a.part, gridDim.x};
-  Walker W(D);
-  const int bid = blockIdx.x;
+  const Tiles tl = make_tiles(D);
+  GridReducer R{a.part, a.bar, a.err, gridDim.x, 0};
+  const int pinned_k = a.pinned ? D.P + 1 : -1;
+  Sys<float> S{a.e32, a.r32b, a.r32, a.d32, a.d32b, a.Ad32, a.ax32, a.ay32, nullptr, nullptr};
   bool ok = true;
   int total_inner = 0, outer = 0, status = COVOF_OK;
   double b_norm = 1.0, r_norm = 0.0;
   for (;;) {
-    // FP64 residual r = b - A x, ||b||, ||r||
-    {
-      double acc[2] = {0.0, 0.0};
-      FOR_OWNED_CELLS(D, W, i, j, k) {
-        double y = stencil<double>(D, k, a.x, a.ax, a.ay, a.aP);
-        double rr = __dsub_rn(a.b[k], y);
-        if (a.pinned && k == D.P + 1) rr = 0.0;
+    // FP64 residual r = b - A x (FMA form), ||b||, ||r||, sum(r), sum(aP)
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+      const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
+      const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
+      if (i <= D.nx && j <= D.ny) {
+        const int k = D.id(i, j);
+        double v = a.aP[k] * __ldcg(a.x + k);
+        v = fma(-a.ax[k], __ldcg(a.x + k - 1), v);
+        v = fma(-a.ax[k + 1], __ldcg(a.x + k + 1), v);
+        v = fma(-a.ay[k], __ldcg(a.x + k - D.P), v);
+        v = fma(-a.ay[k + D.P], __ldcg(a.x + k + D.P), v);
+        double rr = a.b[k] - v;
+        if (k == pinned_k) rr = 0.0;
         a.r[k] = rr;
-        acc[0] += a.b[k] * a.b[k];
-        acc[1] += rr * rr;
+        acc[0] = fma(a.b[k], a.b[k], acc[0]);
+        acc[1] = fma(rr, rr, acc[1]);
+        acc[2] += rr;
+        acc[3] += a.aP[k];
       }
-      block_sum<double, 2>(acc);
-      if (threadIdx.x == 0) { a.part[bid * 4 + 0] = acc[0]; a.part[bid * 4 + 1] = acc[1]; }
     }
-    ok = grid_barrier(a.bar, gridDim.x, a.err);
-    if (!ok) break;
-    {
-      __shared__ double sh2[2];
-      if (threadIdx.x < 32) {
-        double a0 = 0.0, a1 = 0.0;
-        for (int q = threadIdx.x; q < (int)gridDim.x; q += 32) {
-          a0 += __ldcg(a.part + q * 4 + 0);
-          a1 += __ldcg(a.part + q * 4 + 1);
-        }
-        a0 = warp_sum(a0); a1 = warp_sum(a1);
-        if (threadIdx.x == 0) { sh2[0] = a0; sh2[1] = a1; }
-      }
-      __syncthreads();
-      b_norm = sqrt(sh2[0]);
-      r_norm = sqrt(sh2[1]);
-      __syncthreads();
-    }
+    double tot[4];
+    if (!reduce<double, 4>(R, acc, tot)) { ok = false; break; }
+    b_norm = sqrt(tot[0]);
     if (b_norm < 1.0e-30) b_norm = 1.0;
+    r_norm = sqrt(tot[1]);
     if (isnan(r_norm)) { status = COVOF_NAN; break; }
     if (r_norm / b_norm <= a.tol) break;
     if (outer >= a.max_refine || total_inner >= a.max_iter) { status = COVOF_MAXITER; break; }
-    // inner right-hand side r32 = r / ||r||, e = 0
+    // Inner problem on the scaled operator S A S, S = D^-1/2 (unit diagonal,
+    // O(1) entries, so FP32 rounding follows the Jacobi-scaled condition
+    // number, not the density contrast):
+    //   (S A S) y = S (r - c aP) / ||r||,   x += ||r|| S y.
+    // Reference gauge: A is a Neumann operator plus a 1e-12*dvol shift FP32
+    // cannot represent; c = sum(r)/sum(aP) removes the right-hand side's
+    // (rounding-level) component along the scaled null vector S^-1 1.  The
+    // outer test is always the true FP64 residual.
+    const double cdef = a.pinned ? 0.0 : tot[2] / tot[3];
     const double scale = 1.0 / r_norm;
-    FOR_OWNED_CELLS(D, W, i, j, k) {
-      a.r32b[k] = (float)(a.r[k] * scale);
-      a.e32[k] = 0.0f;
+    for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+      const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
+      const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
+      if (i <= D.nx && j <= D.ny) {
+        const int k = D.id(i, j);
+        a.r32b[k] = (k == pinned_k) ? 0.0f : (float)((a.r[k] - cdef * a.aP[k]) * a.isd[k] * scale);
+        a.e32[k] = 0.0f;
+      }
     }
-    // pcg_core starts with a residual pass that reads e through the stencil;
-    // every block must have cleared its cells first.
-    ok = grid_barrier(a.bar, gridDim.x, a.err);
-    if (!ok) break;
-    int st; double rn, bn; bool iok;
+    // (pcg_tiled's first pass reads only own cells when x_zero)
     int budget = a.max_iter - total_inner;
     if (budget > a.inner_max_iter) budget = a.inner_max_iter;
-    int it = pcg_core<float>(D, C, W, a.e32, a.r32b, a.r32, a.d32, a.Ad32, a.ax32, a.ay32, a.aP32,
-                             a.pinned, a.inner_tol, budget, &st, &rn, &bn, &iok);
-    total_inner += it;
+    PcgOut o = pcg_tiled<float, true>(D, tl, R, S, a.pinned, a.inner_tol, budget, true, sd);
+    total_inner += o.iters;
     outer++;
-    if (!iok) { ok = false; break; }
-    if (st == COVOF_NAN) { status = COVOF_NAN; break; }
-    // x += ||r|| e  (own cells; the next residual pass reads x after a barrier)
-    FOR_OWNED_CELLS(D, W, i, j, k) a.x[k] = __dadd_rn(a.x[k], __dmul_rn(r_norm, (double)a.e32[k]));
-    ok = grid_barrier(a.bar, gridDim.x, a.err);
-    if (!ok) break;
-    if (it == 0) { status = COVOF_BREAKDOWN; break; }
+    if (!o.ok) { ok = false; break; }
+    if (o.status == COVOF_NAN) { status = COVOF_NAN; break; }
+    // x += ||r|| S y on own cells; the next residual pass reads neighbours'
+    // x, hence the barrier.
+    for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+      const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
+      const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
+      if (i <= D.nx && j <= D.ny) {
+        const int k = D.id(i, j);
+        a.x[k] = fma(r_norm * a.isd[k], (double)a.e32[k], a.x[k]);
+      }
+    }
+    if (!grid_barrier(a.bar, gridDim.x, a.err)) { ok = false; break; }
+    if (o.iters == 0) { status = COVOF_BREAKDOWN; break; }
   }
-  if (ok && !a.pinned) ok = remove_mean(D, C, W, a.x);
+  if (ok && !a.pinned) ok = remove_mean(D, tl, R, a.x);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.res->iters = total_inner;
     a.res->relres = r_norm / b_norm;
@@ -477,7 +475,7 @@ __global__ void k_poisson_apply(Dims D, const double* __restrict__ x, double* __
   int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (i > D.nx || j > D.ny) return;
   int k = D.id(i, j);
-  y[k] = stencil<double>(D, k, x, ax, ay, aP);
+  y[k] = stencil_exact(D, k, x, ax, ay, aP);
 }
 
 }  // namespace covof

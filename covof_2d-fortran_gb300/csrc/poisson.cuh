@@ -15,13 +15,14 @@ struct PcgResult {
 struct PoissonArgs {
   Dims D;
   // FP64 system
-  double* x; const double* b; double* r; double* d; double* Ad;
-  const double* ax; const double* ay; const double* aP;
+  double* x; const double* b; double* r; double* d; double* d2; double* Ad;
+  const double* ax; const double* ay; const double* aP; const double* invD;
+  const double* isd;  // 1/sqrt(aP) (mixed path scaling), zero ghost ring
   // FP32 inner system (mixed)
-  float* e32; float* r32b; float* r32; float* d32; float* Ad32;
+  float* e32; float* r32b; float* r32; float* d32; float* d32b; float* Ad32;
   const float* ax32; const float* ay32; const float* aP32;
   // control
-  unsigned int* bar; int* err; double* part;  // part: 5 * nblocks doubles
+  unsigned int* bar; int* err; double* part;  // part: 16 * nblocks doubles
   PcgResult* res;
   double tol, inner_tol;
   int max_iter, inner_max_iter, max_refine, pinned;
@@ -34,10 +35,16 @@ __global__ void k_poisson_assemble(Dims D, double dt, double dx, double dy, int4
                                    const double* __restrict__ b_in, int pinned,
                                    double* __restrict__ ax, double* __restrict__ ay,
                                    double* __restrict__ aP, double* __restrict__ b,
-                                   float* __restrict__ ax32, float* __restrict__ ay32,
-                                   float* __restrict__ aP32);
+                                   double* __restrict__ isd, double* __restrict__ invD);
+__global__ void k_poisson_scale32(Dims D, const double* __restrict__ ax, const double* __restrict__ ay,
+                                  const double* __restrict__ isd, float* __restrict__ ax32,
+                                  float* __restrict__ ay32, float* __restrict__ aP32);
 __global__ void k_copy_interior(Dims D, const double* __restrict__ src, double* __restrict__ dst,
                                 int zero_pin);
+struct Tiles {
+  int TX, TY, ntx, nty, ntiles;
+};
+__host__ __device__ Tiles make_tiles(const Dims& D);
 __global__ void k_pcg_fp64(PoissonArgs a);
 __global__ void k_pcg_mixed(PoissonArgs a);
 __global__ void k_project_correct(Dims D, double dt, double dx, double dy, int4 wall,

