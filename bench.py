@@ -267,11 +267,11 @@ def run_ours(args, world, rank, local):
     _, hru = pinned(ru)
     _, hrv = pinned(rv)
     _, hp = pinned(np.zeros_like(b))
-    for _ in range(max(1, args.warmup)):
+    for _ in range(0 if args.skip_e2e else max(1, args.warmup)):
         hp[...] = 0.0
         s.poisson_solve_rhs(dt, hb, hru, hrv, hp)
-    e2e_ms = []
-    for _ in range(args.steps):
+    e2e_ms = [float("nan")] if args.skip_e2e else []
+    for _ in range(0 if args.skip_e2e else args.steps):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         hp[...] = 0.0
@@ -305,7 +305,7 @@ def run_ours(args, world, rank, local):
     line = None
     if rank == 0:
         orc = ge._load_oracle()
-        cpu = cpu_sample(pkg, orc, p, b, ru, rv, dt, it_f, 1, args.cpu_budget)
+        cpu = None if args.skip_cpu else cpu_sample(pkg, orc, p, b, ru, rv, dt, it_f, 1, args.cpu_budget)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
@@ -342,6 +342,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--skip-cpu", action="store_true", help="profiling runs: no CPU baseline")
+    ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: no host-API leg")
     args = ap.parse_args()
     if args.impl == "reference":
         world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -24,6 +24,7 @@ CONV_UPWIND, CONV_CENTERED = 1, 2
 RECON_PLIC, RECON_ELVIRA = 0, 1
 GAUGE_REFERENCE, GAUGE_PINNED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
+INNER_CHEBYSHEV, INNER_CG = 0, 1
 
 
 class Params(C.Structure):
@@ -41,6 +42,7 @@ class Params(C.Structure):
         ("rho1", C.c_double), ("rho2", C.c_double), ("mu1", C.c_double), ("mu2", C.c_double),
         ("sigma", C.c_double), ("gx", C.c_double), ("gy", C.c_double),
         ("recon", C.c_int),
+        ("p_inner_kind", C.c_int), ("p_cheb_lo", C.c_double),
     ]
 
     def copy(self) -> "Params":

@@ -47,13 +47,15 @@ def make_params(nx: int, ny: int, lx: float, ly: float) -> Params:
     p.p_precision = capi.PREC_FP64
     p.p_tol = 1.0e-7
     p.p_inner_tol = 1.0e-4
-    p.p_inner_max_iter = 100000
-    p.p_max_refine = 20
+    p.p_inner_max_iter = 32
+    p.p_max_refine = 1000000
     p.enable_two_phase = 0
     p.enable_surface_tension = 0
     p.rho1, p.rho2, p.mu1, p.mu2 = 1.0, 1.0, 1.0e-3, 1.0e-3
     p.sigma, p.gx, p.gy = 0.0, 0.0, 0.0
     p.recon = capi.RECON_PLIC
+    p.p_inner_kind = capi.INNER_CHEBYSHEV
+    p.p_cheb_lo = 1.0e-3
     return p
 
 

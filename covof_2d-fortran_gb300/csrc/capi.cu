@@ -62,7 +62,8 @@ struct covof_handle {
   bool have_poisson = false;
   double *px = nullptr, *pb = nullptr, *pr = nullptr, *pd = nullptr, *pAd = nullptr,
          *pax = nullptr, *pay = nullptr, *paP = nullptr, *pisd = nullptr, *pinvD = nullptr,
-         *pd2 = nullptr;
+         *pd2 = nullptr, *pz = nullptr, *pw = nullptr, *pp = nullptr, *pq = nullptr;
+  float* pxb = nullptr;  // boundary-row exchange of the shared-memory inner solver
   float *e32 = nullptr, *r32b = nullptr, *r32 = nullptr, *d32 = nullptr, *d32b = nullptr, *Ad32 = nullptr,
         *ax32 = nullptr, *ay32 = nullptr, *aP32 = nullptr;
   // momentum scratch (each 2g)
@@ -72,7 +73,7 @@ struct covof_handle {
   bool have_vof = false;
   double *cs = nullptr, *seg = nullptr, *cnx = nullptr, *cny = nullptr, *ckap = nullptr;
   // control
-  unsigned int* bar = nullptr;
+  unsigned int* bar = nullptr;  // [0] grid barrier counter, [64..) per-block publish counters
   int* err = nullptr;
   double* part = nullptr;
   int part_blocks = 0;
@@ -126,6 +127,8 @@ int ensure_poisson(covof_handle* h) {
   CS(dalloc(&h->px, g)); CS(dalloc(&h->pb, g)); CS(dalloc(&h->pr, g)); CS(dalloc(&h->pd, g));
   CS(dalloc(&h->pAd, g)); CS(dalloc(&h->pax, g)); CS(dalloc(&h->pay, g)); CS(dalloc(&h->paP, g));
   CS(dalloc(&h->pisd, g)); CS(dalloc(&h->pinvD, g)); CS(dalloc(&h->pd2, g)); CS(dalloc(&h->d32b, g));
+  CS(dalloc(&h->pz, g)); CS(dalloc(&h->pw, g)); CS(dalloc(&h->pp, g)); CS(dalloc(&h->pq, g));
+  CS(dalloc(&h->pxb, (size_t)8 * h->sm_count * (size_t)(h->D.nx + 2)));
   CS(dalloc(&h->e32, g)); CS(dalloc(&h->r32b, g)); CS(dalloc(&h->r32, g)); CS(dalloc(&h->d32, g));
   CS(dalloc(&h->Ad32, g)); CS(dalloc(&h->ax32, g)); CS(dalloc(&h->ay32, g)); CS(dalloc(&h->aP32, g));
   h->have_poisson = true;
@@ -153,9 +156,9 @@ int ensure_vof(covof_handle* h) {
 // Block count of a persistent cooperative kernel: at most one block per SM
 // (fewer arrivals per grid barrier; the 1024-thread Poisson blocks fill an
 // SM anyway), never more than the work units, never more than co-resident.
-int coop_blocks(covof_handle* h, const void* fn, int threads, long long units) {
+int coop_blocks(covof_handle* h, const void* fn, int threads, long long units, size_t smem = 0) {
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess || per_sm < 1)
     return -1;
   long long nb = h->sm_count;
   if (units < nb) nb = units < 1 ? 1 : units;
@@ -164,11 +167,12 @@ int coop_blocks(covof_handle* h, const void* fn, int threads, long long units) {
   return (int)nb;
 }
 
-int launch_coop(covof_handle* h, const void* fn, int nblocks, int threads, void** args, bool timed) {
-  CK(cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned int), h->stream));
+int launch_coop(covof_handle* h, const void* fn, int nblocks, int threads, void** args, bool timed,
+                size_t smem = 0) {
+  CK(cudaMemsetAsync(h->bar, 0, (size_t)(64 + h->sm_count) * sizeof(unsigned int), h->stream));
   CK(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
   if (timed) CK(cudaEventRecord(h->ev0, h->stream));
-  CK(cudaLaunchCooperativeKernel(fn, dim3(nblocks), dim3(threads), args, 0, h->stream));
+  CK(cudaLaunchCooperativeKernel(fn, dim3(nblocks), dim3(threads), args, smem, h->stream));
   if (timed) CK(cudaEventRecord(h->ev1, h->stream));
   return COVOF_OK;
 }
@@ -212,6 +216,8 @@ int poisson_dev(covof_handle* h, double dt, const double* u, const double* v, co
   a.D = h->D;
   a.x = h->px; a.b = h->pb; a.r = h->pr; a.d = h->pd; a.d2 = h->pd2; a.Ad = h->pAd;
   a.ax = h->pax; a.ay = h->pay; a.aP = h->paP; a.invD = h->pinvD; a.isd = h->pisd;
+  a.z = h->pz; a.w = h->pw; a.p = h->pp; a.q = h->pq; a.xb = h->pxb;
+  a.flags = h->bar + 64; a.cheb_lo = P.p_cheb_lo;
   a.e32 = h->e32; a.r32b = h->r32b; a.r32 = h->r32; a.d32 = h->d32; a.d32b = h->d32b; a.Ad32 = h->Ad32;
   a.ax32 = h->ax32; a.ay32 = h->ay32; a.aP32 = h->aP32;
   a.bar = h->bar; a.err = h->err; a.part = h->part; a.res = h->d_pres;
@@ -219,11 +225,31 @@ int poisson_dev(covof_handle* h, double dt, const double* u, const double* v, co
   a.max_iter = P.p_max_iter; a.inner_max_iter = P.p_inner_max_iter;
   a.max_refine = P.p_max_refine; a.pinned = pinned;
   const void* fn = mixed ? (const void*)k_pcg_mixed : (const void*)k_pcg_fp64;
-  const long long ntiles = (long long)make_tiles(h->D).ntiles;
-  const int nb = coop_blocks(h, fn, kPoissonThreads, ntiles);
+  long long units = (long long)make_tiles(h->D).ntiles;
+  size_t smem = 0;
+  if (mixed) {
+    // shared-memory-resident inner solver when one row strip per SM fits
+    const int G = P.ny < h->sm_count ? P.ny : h->sm_count;
+    const int Rmax = (P.ny + G - 1) / G;
+    const bool cheb = P.p_inner_kind == COVOF_INNER_CHEBYSHEV;
+    const void* sfn = cheb ? (const void*)k_pcg_mixed_cheb : (const void*)k_pcg_mixed_smem;
+    const size_t bytes = cheb ? smem_cheb_bytes(P.nx, Rmax) : smem_strip_bytes(P.nx, Rmax);
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, sfn) == cudaSuccess && bytes + fa.sharedSizeBytes <= (size_t)optin &&
+        cudaFuncSetAttribute(sfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess) {
+      fn = sfn;
+      smem = bytes;
+      units = G;
+    }
+    cudaGetLastError();
+  }
+  const int nb = coop_blocks(h, fn, kPoissonThreads, units, smem);
   if (nb < 1) return COVOF_CUDA_ERROR;
+  if (smem && nb != (int)units) return COVOF_CUDA_ERROR;  // strips are sized for exactly G blocks
   void* args[] = {&a};
-  CS(launch_coop(h, fn, nb, kPoissonThreads, args, true));
+  CS(launch_coop(h, fn, nb, kPoissonThreads, args, true, smem));
   k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, h->px, p, 0);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(h->h_pres, h->d_pres, sizeof(PcgResult), cudaMemcpyDeviceToHost, h->stream));
@@ -440,13 +466,15 @@ void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly)
   p->p_precision = COVOF_PREC_FP64;
   p->p_tol = 1.0e-7;
   p->p_inner_tol = 1.0e-4;
-  p->p_inner_max_iter = 100000;
-  p->p_max_refine = 20;
+  p->p_inner_max_iter = 32;
+  p->p_max_refine = 1000000;
   p->enable_two_phase = 0;
   p->enable_surface_tension = 0;
   p->rho1 = 1.0; p->rho2 = 1.0; p->mu1 = 1.0e-3; p->mu2 = 1.0e-3;
   p->sigma = 0.0; p->gx = 0.0; p->gy = 0.0;
   p->recon = COVOF_RECON_PLIC;
+  p->p_inner_kind = COVOF_INNER_CHEBYSHEV;
+  p->p_cheb_lo = 1.0e-3;
 }
 
 int covof_abi_version(void) { return COVOF_ABI_VERSION; }
@@ -486,7 +514,7 @@ int covof_create(const covof_params* params, covof_handle** out) {
   if (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
     return fail(COVOF_CUDA_ERROR);
   h->part_blocks = h->sm_count;  // persistent kernels run at most one block per SM
-  if (dalloc(&h->bar, 2) || dalloc(&h->err, 1) ||
+  if (dalloc(&h->bar, (size_t)64 + h->sm_count) || dalloc(&h->err, 1) ||
       dalloc(&h->part, (size_t)kMaxPartRegions * h->part_blocks) ||
       dalloc(&h->d_pres, 1) || dalloc(&h->d_kres, 1))
     return fail(COVOF_CUDA_ERROR);
@@ -503,11 +531,11 @@ int covof_destroy(covof_handle* h) {
   double** fl[] = {&h->f_u, &h->f_v, &h->f_p, &h->f_rho_u, &h->f_rho_v, &h->f_mu, &h->f_mu_node,
                    &h->f_fx, &h->f_fy, &h->f_u_old, &h->f_v_old, &h->f_C, &h->f_rho, &h->f_curv,
                    &h->f_b, &h->f_x2, &h->f_seg, &h->px, &h->pb, &h->pr, &h->pd, &h->pAd,
-                   &h->pax, &h->pay, &h->paP, &h->pisd, &h->pinvD, &h->pd2, &h->mx, &h->mrhs, &h->mdiag, &h->cs, &h->seg,
+                   &h->pax, &h->pay, &h->paP, &h->pisd, &h->pinvD, &h->pd2, &h->pz, &h->pw, &h->pp, &h->pq, &h->mx, &h->mrhs, &h->mdiag, &h->cs, &h->seg,
                    &h->cnx, &h->cny, &h->ckap, &h->part};
   for (double** q : fl) dfree(*q);
   for (int q = 0; q < 7; ++q) dfree(h->mv[q]);
-  float** ff[] = {&h->e32, &h->r32b, &h->r32, &h->d32, &h->d32b, &h->Ad32, &h->ax32, &h->ay32, &h->aP32};
+  float** ff[] = {&h->pxb, &h->e32, &h->r32b, &h->r32, &h->d32, &h->d32b, &h->Ad32, &h->ax32, &h->ay32, &h->aP32};
   for (float** q : ff) dfree(*q);
   dfree(h->bar); dfree(h->err); dfree(h->d_pres); dfree(h->d_kres);
   if (h->h_pres) cudaFreeHost(h->h_pres);

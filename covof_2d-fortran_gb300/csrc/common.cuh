@@ -23,40 +23,48 @@ struct Dims {
 
 // ---------------------------------------------------------------------------
 // Grid-wide barrier for kernels launched with cudaLaunchCooperativeKernel
-// (co-residency of all blocks is guaranteed by that launch, so the wait ends
-// in a few microseconds).  Every spin is still bounded: after kSpinLimit
-// polls the waiting block records COVOF_TIMEOUT and returns false; every
-// caller then leaves its loop, so no block can wait forever.
-//   bar[0] = arrival count, bar[1] = generation.
-constexpr long long kSpinLimit = 1LL << 25;  // ~1-2 s with the 32 ns back-off
+// (co-residency of all blocks is guaranteed by that launch).  Counting form:
+// thread 0 of every block adds 1 with release semantics to one counter and
+// polls it with acquire loads until it reaches (epoch+1) * nblocks; no reset
+// and no second word, so the critical path is one atomic and one poll.
+// Every spin is bounded: after kSpinLimit polls (~1-2 s) the block records
+// COVOF_TIMEOUT and returns false, and every caller leaves its loop; a block
+// that left never arrives again, so every other block times out at its next
+// barrier and no block can wait forever.  The counter must be zero at launch.
+constexpr long long kSpinLimit = 1LL << 21;
 
-__device__ __forceinline__ bool grid_barrier(unsigned int* bar, unsigned int nblocks, int* err) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    volatile unsigned int* gen = bar + 1;
-    unsigned int g = *gen;
-    __threadfence();
-    unsigned int arrived = atomicAdd(bar, 1u);
-    if (arrived == nblocks - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      long long spins = 0;
-      while (*gen == g) {
-        if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
-        __nanosleep(32);
-      }
-    }
-    __threadfence();
-    if (*(volatile int*)err != 0) ok = 0;
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
 }
+__device__ __forceinline__ void red_add_release_u32(unsigned int* p, unsigned int v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+struct GridSync {
+  unsigned int* count;
+  int* err;
+  unsigned int nblocks;
+  unsigned int epoch;
+  __device__ bool sync() {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int ok = 1;
+      red_add_release_u32(count, 1u);
+      const unsigned int target = (epoch + 1u) * nblocks;
+      long long spins = 0;
+      while ((int)(ld_acquire_u32(count) - target) < 0) {
+        if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+      }
+      s_ok = ok;
+    }
+    epoch++;
+    __syncthreads();
+    return s_ok != 0;
+  }
+};
 
 // ---------------------------------------------------------------------------
 // Deterministic reductions.  Block partials are combined by every block in
@@ -93,31 +101,6 @@ __device__ __forceinline__ void block_sum(T (&v)[NV]) {
   __syncthreads();
 }
 
-// Combine the per-block FP64 partials part[b*NV + k], b < nblocks, into
-// tot[k] in every block (identical order everywhere).  Reads bypass L1.
-template <int NV>
-__device__ __forceinline__ void grid_combine(const double* part, int nblocks, double (&tot)[NV]) {
-  __shared__ double sh[NV];
-  if (threadIdx.x < 32) {
-    double acc[NV];
-#pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k] = 0.0;
-    for (int b = threadIdx.x; b < nblocks; b += 32) {
-#pragma unroll
-      for (int k = 0; k < NV; ++k) acc[k] += __ldcg(part + b * NV + k);
-    }
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double t = warp_sum(acc[k]);
-      if (threadIdx.x == 0) sh[k] = t;
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < NV; ++k) tot[k] = sh[k];
-  __syncthreads();
-}
-
 // Fused hypot: sqrt(x^2+y^2) with an FMA-based residual correction (after
 // C. F. Borges, "An improved algorithm for hypot(a,b)", ACM TOMS 2021).  Each
 // operation is an explicit IEEE round-to-nearest intrinsic so the result is
@@ -145,40 +128,39 @@ __device__ __forceinline__ double fhypot(double x, double y) {
 
 namespace covof {
 
-// Grid-wide sum of up to 8 FP64 values per thread.  Consecutive reductions
-// alternate between two partial regions, so a region is rewritten only after
-// every block has passed the barrier that follows its last read.
-// part must hold 2 * 8 * nblocks doubles.
+// Grid-wide sum of up to 8 FP64 values per thread, deterministic: block
+// partials are written to one of two regions, the grid meets at the
+// barrier, then every block combines all partials in the same fixed order
+// (one partial per thread, then a block tree), so all blocks obtain
+// bit-identical totals.  Consecutive reductions alternate regions, so a
+// region is rewritten only after every block has passed the barrier that
+// follows its last read.  part must hold 2 * 8 * nblocks doubles.
 struct GridReducer {
   double* part;
-  unsigned int* bar;
-  int* err;
-  unsigned int nblocks;
+  GridSync gs;
   int region;
   template <int NV>
   __device__ bool sum(double (&v)[NV]) {
     static_assert(NV <= 8, "at most 8 values");
     block_sum<double, NV>(v);
-    double* base = part + (size_t)region * nblocks * 8;
+    double* base = part + (size_t)region * gs.nblocks * 8;
     if (threadIdx.x == 0) {
 #pragma unroll
       for (int q = 0; q < NV; ++q) base[blockIdx.x * 8 + q] = v[q];
     }
-    bool ok = grid_barrier(bar, nblocks, err);
+    const bool ok = gs.sync();
+    double w[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) w[q] = 0.0;
+    for (int b = threadIdx.x; b < (int)gs.nblocks; b += blockDim.x) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) w[q] += __ldcg(base + b * 8 + q);
+    }
+    block_sum<double, NV>(w);
     __shared__ double sh[8];
-    if (threadIdx.x < 32) {
-      double acc[NV];
+    if (threadIdx.x == 0) {
 #pragma unroll
-      for (int q = 0; q < NV; ++q) acc[q] = 0.0;
-      for (int b = threadIdx.x; b < (int)nblocks; b += 32) {
-#pragma unroll
-        for (int q = 0; q < NV; ++q) acc[q] += __ldcg(base + b * 8 + q);
-      }
-#pragma unroll
-      for (int q = 0; q < NV; ++q) {
-        double t = warp_sum(acc[q]);
-        if (threadIdx.x == 0) sh[q] = t;
-      }
+      for (int q = 0; q < NV; ++q) sh[q] = w[q];
     }
     __syncthreads();
 #pragma unroll

@@ -373,7 +373,7 @@ __device__ void krylov_finish(const MomArgs& a, int iters, int status, bool ok) 
 // src/module_linear_solvers.f90:584-730 solve_bicgstab (left Jacobi).
 __global__ void __launch_bounds__(512) k_bicgstab(MomArgs a) {
   DofWalker W(a.D);
-  GridReducer R{a.part, a.bar, a.err, gridDim.x, 0};
+  GridReducer R{a.part, GridSync{a.bar, a.err, gridDim.x, 0u}, 0};
   double *x = a.x, *bh = a.v0, *r = a.v1, *rt = a.v2, *p = a.v3, *v = a.v4, *s = a.v5, *t = a.v6;
   const double tol = a.tol;
   const int max_iter = a.max_iter;
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(512) k_bicgstab(MomArgs a) {
     FOR_DOFS(a, W, part, i, j, k) {
       p[k] = (it == 1) ? r[k] : r[k] + beta * (p[k] - omega * v[k]);
     }
-    ok = grid_barrier(a.bar, gridDim.x, a.err);
+    ok = R.gs.sync();
     if (!ok) break;
     double a1[1] = {0.0};
     FOR_DOFS(a, W, part, i, j, k) {
@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(512) k_bicgstab(MomArgs a) {
 // separate Jacobi application).
 __global__ void __launch_bounds__(512) k_cg(MomArgs a) {
   DofWalker W(a.D);
-  GridReducer R{a.part, a.bar, a.err, gridDim.x, 0};
+  GridReducer R{a.part, GridSync{a.bar, a.err, gridDim.x, 0u}, 0};
   double *x = a.x, *r = a.v1, *p = a.v3, *Ap = a.v4;
   const double tol = a.tol;
   const int max_iter = a.max_iter;
@@ -503,7 +503,7 @@ __global__ void __launch_bounds__(512) k_cg(MomArgs a) {
     const double beta = a2[1] / rz_old;
     rz_old = a2[1];
     FOR_DOFS(a, W, part, i, j, k) p[k] = prec(a, k, r[k]) + beta * p[k];
-    ok = grid_barrier(a.bar, gridDim.x, a.err);
+    ok = R.gs.sync();
   }
   krylov_finish(a, iters, status, ok);
 }
@@ -511,7 +511,7 @@ __global__ void __launch_bounds__(512) k_cg(MomArgs a) {
 // src/module_linear_solvers.f90:361-579 solve_bicgstab2 (left Jacobi).
 __global__ void __launch_bounds__(512) k_bicgstab2(MomArgs a) {
   DofWalker W(a.D);
-  GridReducer R{a.part, a.bar, a.err, gridDim.x, 0};
+  GridReducer R{a.part, GridSync{a.bar, a.err, gridDim.x, 0u}, 0};
   double *x = a.x, *rt = a.v0, *r0 = a.v1, *r1 = a.v2, *r2 = a.v3, *u0 = a.v4, *u1 = a.v5, *u2 = a.v6;
   const double tol = a.tol;
   const int max_iter = a.max_iter;
@@ -539,7 +539,7 @@ __global__ void __launch_bounds__(512) k_bicgstab2(MomArgs a) {
     double beta = alpha * (rho1 / rho0);
     rho0 = rho1;
     FOR_DOFS(a, W, part, i, j, k) u0[k] = r0[k] - beta * u0[k];
-    ok = grid_barrier(a.bar, gridDim.x, a.err);
+    ok = R.gs.sync();
     if (!ok) break;
     double g1[1] = {0.0};
     FOR_DOFS(a, W, part, i, j, k) {
@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(512) k_bicgstab2(MomArgs a) {
       r0[k] = r0[k] - alpha * u1[k];
       x[k] = x[k] + alpha * u0[k];
     }
-    ok = grid_barrier(a.bar, gridDim.x, a.err);
+    ok = R.gs.sync();
     if (!ok) break;
     double g2[1] = {0.0};
     FOR_DOFS(a, W, part, i, j, k) {
@@ -573,7 +573,7 @@ __global__ void __launch_bounds__(512) k_bicgstab2(MomArgs a) {
       u0[k] = r0[k] - beta * u0[k];
       u1[k] = r1[k] - beta * u1[k];
     }
-    ok = grid_barrier(a.bar, gridDim.x, a.err);
+    ok = R.gs.sync();
     if (!ok) break;
     double g3[1] = {0.0};
     FOR_DOFS(a, W, part, i, j, k) {
@@ -590,7 +590,7 @@ __global__ void __launch_bounds__(512) k_bicgstab2(MomArgs a) {
       r0[k] = r0[k] - alpha * u1[k];
       r1[k] = r1[k] - alpha * u2[k];
     }
-    ok = grid_barrier(a.bar, gridDim.x, a.err);
+    ok = R.gs.sync();
     if (!ok) break;
     double sg[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     FOR_DOFS(a, W, part, i, j, k) {

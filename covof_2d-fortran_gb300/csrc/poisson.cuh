@@ -18,6 +18,10 @@ struct PoissonArgs {
   double* x; const double* b; double* r; double* d; double* d2; double* Ad;
   const double* ax; const double* ay; const double* aP; const double* invD;
   const double* isd;  // 1/sqrt(aP) (mixed path scaling), zero ghost ring
+  double* z; double* w; double* p; double* q;  // FP64 flexible-CG vectors (mixed)
+  float* xb;  // boundary-row exchange of the shared-memory inner solvers
+  unsigned int* flags;  // per-block publish counters (Chebyshev inner solver)
+  double cheb_lo;
   // FP32 inner system (mixed)
   float* e32; float* r32b; float* r32; float* d32; float* d32b; float* Ad32;
   const float* ax32; const float* ay32; const float* aP32;
@@ -47,6 +51,12 @@ struct Tiles {
 __host__ __device__ Tiles make_tiles(const Dims& D);
 __global__ void k_pcg_fp64(PoissonArgs a);
 __global__ void k_pcg_mixed(PoissonArgs a);
+__global__ void k_pcg_mixed_smem(PoissonArgs a);
+__global__ void k_pcg_mixed_cheb(PoissonArgs a);
+// Shared-memory bytes of k_pcg_mixed_cheb for a strip of R rows of nx cells.
+inline size_t smem_cheb_bytes(int nx, int R) { return (size_t)(6 * R + 5) * (size_t)(nx + 2) * sizeof(float); }
+// Shared-memory bytes of k_pcg_mixed_smem for a strip of R rows of nx cells.
+inline size_t smem_strip_bytes(int nx, int R) { return (size_t)(6 * R + 7) * (size_t)(nx + 2) * sizeof(float); }
 __global__ void k_project_correct(Dims D, double dt, double dx, double dy, int4 wall,
                                   double* __restrict__ u, double* __restrict__ v,
                                   const double* __restrict__ p, const double* __restrict__ rho_u,

@@ -49,6 +49,8 @@ module covof_gpu_bridge
      integer(c_int) :: enable_two_phase, enable_surface_tension
      real(c_double) :: rho1, rho2, mu1, mu2, sigma, gx, gy
      integer(c_int) :: recon
+     integer(c_int) :: p_inner_kind
+     real(c_double) :: p_cheb_lo
   end type covof_params_t
 
   integer(c_int), parameter :: COVOF_OK = 0, COVOF_MAXITER = 1, COVOF_BREAKDOWN = 2
