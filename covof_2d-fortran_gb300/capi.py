@@ -97,6 +97,10 @@ _SIGS = {
     "covof_vof_wy_step_dev": [_VP, C.c_double, C.c_int, _VP, _VP, _VP],
     "covof_vof_advect": [_VP, C.c_double] + [_VP] * 11,
     "covof_vof_advect_dev": [_VP, C.c_double] + [_VP] * 11,
+    "covof_projection": [_VP, C.c_double] + [_VP] * 7 + [_IP, _DP],
+    "covof_projection_dev": [_VP, C.c_double] + [_VP] * 7 + [_IP, _DP],
+    "covof_projection_vjp": [_VP, C.c_double] + [_VP] * 10 + [_IP, _DP],
+    "covof_projection_vjp_dev": [_VP, C.c_double] + [_VP] * 10 + [_IP, _DP],
     "covof_update_physical_properties": [_VP] + [_VP] * 6,
     "covof_compute_curvature_and_csf": [_VP] + [_VP] * 4,
 }

@@ -11,6 +11,7 @@
 #include "momentum.cuh"
 #include "poisson.cuh"
 #include "vof.cuh"
+#include "adjoint.cuh"
 
 using namespace covof;
 
@@ -72,6 +73,11 @@ struct covof_handle {
   // VOF scratch
   bool have_vof = false;
   double *cs = nullptr, *seg = nullptr, *cnx = nullptr, *cny = nullptr, *ckap = nullptr;
+  // adjoint scratch
+  bool have_adj = false;
+  double *arhs = nullptr, *apsi = nullptr, *apart = nullptr, *asum = nullptr;
+  double *f_gu = nullptr, *f_gv = nullptr, *f_gp = nullptr, *f_gbu = nullptr, *f_gbv = nullptr,
+         *f_ou = nullptr, *f_ov = nullptr;
   // control
   unsigned int* bar = nullptr;  // [0] grid barrier counter, [64..) per-block publish counters
   int* err = nullptr;
@@ -150,6 +156,22 @@ int ensure_vof(covof_handle* h) {
   CS(dalloc(&h->cs, g)); CS(dalloc(&h->seg, 3 * g));
   CS(dalloc(&h->cnx, g)); CS(dalloc(&h->cny, g)); CS(dalloc(&h->ckap, g));
   h->have_vof = true;
+  return COVOF_OK;
+}
+
+int ensure_adj(covof_handle* h) {
+  if (h->have_adj) return COVOF_OK;
+  const size_t g = h->g;
+  CS(dalloc(&h->arhs, g)); CS(dalloc(&h->apsi, g)); CS(dalloc(&h->apart, 1024)); CS(dalloc(&h->asum, 1));
+  h->have_adj = true;
+  return COVOF_OK;
+}
+
+int ensure_adj_host(covof_handle* h) {
+  if (h->f_gu) return COVOF_OK;
+  const size_t g = h->g;
+  CS(dalloc(&h->f_gu, g)); CS(dalloc(&h->f_gv, g)); CS(dalloc(&h->f_gp, g));
+  CS(dalloc(&h->f_gbu, g)); CS(dalloc(&h->f_gbv, g)); CS(dalloc(&h->f_ou, g)); CS(dalloc(&h->f_ov, g));
   return COVOF_OK;
 }
 
@@ -285,6 +307,53 @@ int velocity_bc_dev(covof_handle* h, double* u, double* v) {
   k_vbc_corners<<<1, 32, 0, h->stream>>>(b, u, v);
   CK(cudaGetLastError());
   return COVOF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Projection and its adjoint
+int projection_dev(covof_handle* h, double dt, const double* us, const double* vs, const double* rho_u,
+                   const double* rho_v, double* p, double* u, double* v, int* iters, double* relres) {
+  if (!us || !vs || !u || !v) return COVOF_INVALID;
+  int st = poisson_dev(h, dt, us, vs, nullptr, rho_u, rho_v, p, iters, relres);
+  if (st == COVOF_CUDA_ERROR || st == COVOF_INVALID || st == COVOF_UNSUPPORTED || st == COVOF_TIMEOUT) return st;
+  if (u != us) CK(cudaMemcpyAsync(u, us, h->g * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  if (v != vs) CK(cudaMemcpyAsync(v, vs, h->g * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CS(correct_dev(h, dt, u, v, p, rho_u, rho_v));
+  CS(sync(h));
+  return st;
+}
+
+int vjp_dev(covof_handle* h, double dt, const double* rho_u, const double* rho_v, const double* p,
+            const double* gu, const double* gv, const double* gp, double* grad_u, double* grad_v,
+            double* grad_bu, double* grad_bv, int* iters, double* relres) {
+  const covof_params& P = h->prm;
+  if (!rho_u || !rho_v || !p || !gu || !gv || !grad_u || !grad_v || !grad_bu || !grad_bv) return COVOF_INVALID;
+  CS(ensure_adj(h));
+  double gp_mean = 0.0;
+  if (gp && P.p_gauge == COVOF_GAUGE_REFERENCE) {
+    // p has its mean removed: only the mean-free part of gp reaches A^-1
+    k_sum_interior<<<256, 256, 0, h->stream>>>(h->D, gp, h->apart);
+    k_sum_final<<<1, 256, 0, h->stream>>>(h->apart, 256, h->asum);
+    double s = 0.0;
+    CK(cudaMemcpyAsync(&s, h->asum, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CS(sync(h));
+    gp_mean = s / (double)((long long)P.nx * P.ny);
+  }
+  AdjArgs a;
+  a.D = h->D; a.dx = P.dx; a.dy = P.dy; a.dt = dt; a.wall = wall_flags(P);
+  a.rho_u = rho_u; a.rho_v = rho_v; a.p = p; a.gu = gu; a.gv = gv; a.gp = gp;
+  a.rhs = h->arhs; a.psi = h->apsi;
+  a.grad_u = grad_u; a.grad_v = grad_v; a.grad_bu = grad_bu; a.grad_bv = grad_bv;
+  const dim3 blk(32, 8);
+  k_adj_rhs<<<grid2(P.nx, P.ny, blk), blk, 0, h->stream>>>(a, gp_mean);
+  CK(cudaMemsetAsync(h->apsi, 0, h->g * sizeof(double), h->stream));
+  CK(cudaGetLastError());
+  int st = poisson_dev(h, dt, nullptr, nullptr, h->arhs, rho_u, rho_v, h->apsi, iters, relres);
+  if (st == COVOF_CUDA_ERROR || st == COVOF_INVALID || st == COVOF_UNSUPPORTED || st == COVOF_TIMEOUT) return st;
+  k_adj_grad<<<grid2(P.nx + 1, P.ny + 1, blk), blk, 0, h->stream>>>(a);
+  CK(cudaGetLastError());
+  CS(sync(h));
+  return st;
 }
 
 // ---------------------------------------------------------------------------
@@ -532,7 +601,8 @@ int covof_destroy(covof_handle* h) {
                    &h->f_fx, &h->f_fy, &h->f_u_old, &h->f_v_old, &h->f_C, &h->f_rho, &h->f_curv,
                    &h->f_b, &h->f_x2, &h->f_seg, &h->px, &h->pb, &h->pr, &h->pd, &h->pAd,
                    &h->pax, &h->pay, &h->paP, &h->pisd, &h->pinvD, &h->pd2, &h->pz, &h->pw, &h->pp, &h->pq, &h->mx, &h->mrhs, &h->mdiag, &h->cs, &h->seg,
-                   &h->cnx, &h->cny, &h->ckap, &h->part};
+                   &h->cnx, &h->cny, &h->ckap, &h->part, &h->arhs, &h->apsi, &h->apart, &h->asum,
+                   &h->f_gu, &h->f_gv, &h->f_gp, &h->f_gbu, &h->f_gbv, &h->f_ou, &h->f_ov};
   for (double** q : fl) dfree(*q);
   for (int q = 0; q < 7; ++q) dfree(h->mv[q]);
   float** ff[] = {&h->pxb, &h->e32, &h->r32b, &h->r32, &h->d32, &h->d32b, &h->Ad32, &h->ax32, &h->ay32, &h->aP32};
@@ -661,6 +731,61 @@ int covof_project_correct(covof_handle* h, double dt, double* u, double* v, cons
   CS(correct_dev(h, dt, h->f_u, h->f_v, h->f_p, h->f_rho_u, h->f_rho_v));
   CS(d2h(h, u, h->f_u, g)); CS(d2h(h, v, h->f_v, g));
   return sync(h);
+}
+
+// ---- projection adjoint ------------------------------------------------------
+int covof_projection_dev(covof_handle* h, double dt, const double* u_star, const double* v_star,
+                         const double* rho_u, const double* rho_v, double* p, double* u, double* v,
+                         int* iters, double* relres) {
+  if (!h) return COVOF_INVALID;
+  return projection_dev(h, dt, u_star, v_star, rho_u, rho_v, p, u, v, iters, relres);
+}
+
+int covof_projection(covof_handle* h, double dt, const double* u_star, const double* v_star,
+                     const double* rho_u, const double* rho_v, double* p, double* u, double* v,
+                     int* iters, double* relres) {
+  if (!h) return COVOF_INVALID;
+  CS(ensure_fields(h));
+  CS(ensure_adj_host(h));
+  const size_t g = h->g;
+  CS(h2d(h, h->f_u, u_star, g)); CS(h2d(h, h->f_v, v_star, g));
+  CS(h2d(h, h->f_rho_u, rho_u, g)); CS(h2d(h, h->f_rho_v, rho_v, g)); CS(h2d(h, h->f_p, p, g));
+  CS(h2d(h, h->f_ou, u, g)); CS(h2d(h, h->f_ov, v, g));
+  int st = projection_dev(h, dt, h->f_u, h->f_v, h->f_rho_u, h->f_rho_v, h->f_p, h->f_ou, h->f_ov, iters, relres);
+  if (st == COVOF_CUDA_ERROR || st == COVOF_INVALID || st == COVOF_UNSUPPORTED || st == COVOF_TIMEOUT) return st;
+  CS(d2h(h, p, h->f_p, g)); CS(d2h(h, u, h->f_ou, g)); CS(d2h(h, v, h->f_ov, g));
+  CS(sync(h));
+  return st;
+}
+
+int covof_projection_vjp_dev(covof_handle* h, double dt, const double* rho_u, const double* rho_v,
+                             const double* p, const double* gu, const double* gv, const double* gp,
+                             double* grad_u, double* grad_v, double* grad_bu, double* grad_bv,
+                             int* iters, double* relres) {
+  if (!h) return COVOF_INVALID;
+  return vjp_dev(h, dt, rho_u, rho_v, p, gu, gv, gp, grad_u, grad_v, grad_bu, grad_bv, iters, relres);
+}
+
+int covof_projection_vjp(covof_handle* h, double dt, const double* rho_u, const double* rho_v,
+                         const double* p, const double* gu, const double* gv, const double* gp,
+                         double* grad_u, double* grad_v, double* grad_bu, double* grad_bv,
+                         int* iters, double* relres) {
+  if (!h) return COVOF_INVALID;
+  CS(ensure_fields(h));
+  CS(ensure_adj_host(h));
+  const size_t g = h->g;
+  CS(h2d(h, h->f_rho_u, rho_u, g)); CS(h2d(h, h->f_rho_v, rho_v, g)); CS(h2d(h, h->f_p, p, g));
+  CS(h2d(h, h->f_gu, gu, g)); CS(h2d(h, h->f_gv, gv, g));
+  if (gp) CS(h2d(h, h->f_gp, gp, g));
+  CS(h2d(h, h->f_ou, grad_u, g)); CS(h2d(h, h->f_ov, grad_v, g));
+  CS(h2d(h, h->f_gbu, grad_bu, g)); CS(h2d(h, h->f_gbv, grad_bv, g));
+  int st = vjp_dev(h, dt, h->f_rho_u, h->f_rho_v, h->f_p, h->f_gu, h->f_gv, gp ? h->f_gp : nullptr,
+                   h->f_ou, h->f_ov, h->f_gbu, h->f_gbv, iters, relres);
+  if (st == COVOF_CUDA_ERROR || st == COVOF_INVALID || st == COVOF_UNSUPPORTED || st == COVOF_TIMEOUT) return st;
+  CS(d2h(h, grad_u, h->f_ou, g)); CS(d2h(h, grad_v, h->f_ov, g));
+  CS(d2h(h, grad_bu, h->f_gbu, g)); CS(d2h(h, grad_bv, h->f_gbv, g));
+  CS(sync(h));
+  return st;
 }
 
 // ---- momentum --------------------------------------------------------------

@@ -217,6 +217,36 @@ class Solver:
                                            _dptr(fx), _dptr(fy), _dptr(curv))
         return self._check(st, "covof_vof_advect_dev")
 
+    # -- projection and its adjoint ---------------------------------------------
+    def projection(self, dt, u_star, v_star, rho_u, rho_v, p):
+        """u = u* - dt/rho grad p with p from the Poisson solve; returns (u, v, iters, relres, status)."""
+        u, v = u_star.copy(), v_star.copy()
+        it, rr = C.c_int(), C.c_double()
+        st = self.lib.covof_projection(self.h, dt, _ptr(u_star), _ptr(v_star), _ptr(rho_u), _ptr(rho_v),
+                                       _ptr(p), _ptr(u), _ptr(v), C.byref(it), C.byref(rr))
+        return u, v, it.value, rr.value, self._check(st, "covof_projection")
+
+    def projection_vjp(self, dt, rho_u, rho_v, p, gu, gv, gp=None):
+        """(dL/du*, dL/dv*, dL/d(1/rho_u), dL/d(1/rho_v), iters, relres, status)."""
+        out = [np.zeros_like(gu) for _ in range(4)]
+        it, rr = C.c_int(), C.c_double()
+        st = self.lib.covof_projection_vjp(self.h, dt, _ptr(rho_u), _ptr(rho_v), _ptr(p), _ptr(gu), _ptr(gv),
+                                           _ptr(gp), *[_ptr(o) for o in out], C.byref(it), C.byref(rr))
+        return (*out, it.value, rr.value, self._check(st, "covof_projection_vjp"))
+
+    def projection_dev(self, dt, u_star, v_star, rho_u, rho_v, p, u, v):
+        it, rr = C.c_int(), C.c_double()
+        st = self.lib.covof_projection_dev(self.h, dt, _dptr(u_star), _dptr(v_star), _dptr(rho_u),
+                                           _dptr(rho_v), _dptr(p), _dptr(u), _dptr(v), C.byref(it), C.byref(rr))
+        return it.value, rr.value, self._check(st, "covof_projection_dev")
+
+    def projection_vjp_dev(self, dt, rho_u, rho_v, p, gu, gv, gp, gxu, gxv, gbu, gbv):
+        it, rr = C.c_int(), C.c_double()
+        st = self.lib.covof_projection_vjp_dev(self.h, dt, _dptr(rho_u), _dptr(rho_v), _dptr(p), _dptr(gu),
+                                               _dptr(gv), _dptr(gp), _dptr(gxu), _dptr(gxv), _dptr(gbu),
+                                               _dptr(gbv), C.byref(it), C.byref(rr))
+        return it.value, rr.value, self._check(st, "covof_projection_vjp_dev")
+
     # -- geometric VOF ----------------------------------------------------------
     def reconstruct_interface(self, Cf: np.ndarray) -> np.ndarray:
         seg = np.zeros(Cf.shape + (3,), dtype=np.float64)

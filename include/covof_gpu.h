@@ -187,6 +187,32 @@ int covof_last_solve_ms(const covof_handle* h, double* ms);
 /* Outer FP64 refinement steps of the last MIXED Poisson solve. */
 int covof_last_refine_steps(const covof_handle* h, int* steps);
 
+/* ---- projection adjoint ------------------------------------------------ */
+
+/* Forward projection: p from the Poisson solve on -div(u*) (as
+ * covof_poisson_solve), then u = u* - dt/rho_u dp/dx, v likewise (as
+ * covof_project_correct) into separate outputs u, v (DOF faces written). */
+int covof_projection(covof_handle* h, double dt, const double* u_star, const double* v_star,
+                     const double* rho_u, const double* rho_v, double* p, double* u, double* v,
+                     int* iters, double* relres);
+int covof_projection_dev(covof_handle* h, double dt, const double* u_star, const double* v_star,
+                         const double* rho_u, const double* rho_v, double* p, double* u, double* v,
+                         int* iters, double* relres);
+/* Vector-Jacobian product of covof_projection (no counterpart in the
+ * reference, which has no derivatives; built on its operators).  Given the
+ * forward pressure p and upstream gradients gu, gv (faces) and gp (cells, may
+ * be NULL), solves one adjoint Poisson problem with the same symmetric
+ * operator and writes dL/du* (grad_u, grad_v, every DOF face) and
+ * dL/d(1/rho_face) (grad_bu, grad_bv, interior faces; zero elsewhere). */
+int covof_projection_vjp(covof_handle* h, double dt, const double* rho_u, const double* rho_v,
+                         const double* p, const double* gu, const double* gv, const double* gp,
+                         double* grad_u, double* grad_v, double* grad_bu, double* grad_bv,
+                         int* iters, double* relres);
+int covof_projection_vjp_dev(covof_handle* h, double dt, const double* rho_u, const double* rho_v,
+                             const double* p, const double* gu, const double* gv, const double* gp,
+                             double* grad_u, double* grad_v, double* grad_bu, double* grad_bv,
+                             int* iters, double* relres);
+
 /* ---- geometric VOF ---------------------------------------------------- */
 
 /* reconstruct_interface (src/module_interface_reconstruction.f90:580-683):
