@@ -13,9 +13,9 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "_build" / "libcovof_gpu.so"
 
 # status codes (include/covof_gpu.h)
-OK, MAXITER, BREAKDOWN, NAN, TIMEOUT, UNSUPPORTED, CUDA_ERROR, INVALID = range(8)
+OK, MAXITER, BREAKDOWN, NAN, TIMEOUT, UNSUPPORTED, CUDA_ERROR, INVALID, TOO_LARGE = range(9)
 STATUS_NAMES = {0: "OK", 1: "MAXITER", 2: "BREAKDOWN", 3: "NAN", 4: "TIMEOUT",
-                5: "UNSUPPORTED", 6: "CUDA_ERROR", 7: "INVALID"}
+                5: "UNSUPPORTED", 6: "CUDA_ERROR", 7: "INVALID", 8: "TOO_LARGE"}
 # codes shared with src/module_constants.f90
 BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC, BC_FREESLIP = 1, 2, 3, 4
 LINEAR_BICGSTAB2, LINEAR_BICGSTAB, LINEAR_CG = 1, 2, 3
@@ -101,6 +101,7 @@ _SIGS = {
     "covof_projection_dev": [_VP, C.c_double] + [_VP] * 7 + [_IP, _DP],
     "covof_projection_vjp": [_VP, C.c_double] + [_VP] * 10 + [_IP, _DP],
     "covof_projection_vjp_dev": [_VP, C.c_double] + [_VP] * 10 + [_IP, _DP],
+    "covof_poisson_solve_rhs_static_dev": [C.POINTER(Params), C.c_double] + [_VP] * 4 + [_IP, _DP],
     "covof_update_physical_properties": [_VP] + [_VP] * 6,
     "covof_compute_curvature_and_csf": [_VP] + [_VP] * 4,
 }

@@ -558,6 +558,7 @@ const char* covof_strerror(int s) {
     case COVOF_UNSUPPORTED: return "option not implemented on this path";
     case COVOF_CUDA_ERROR: return "CUDA error";
     case COVOF_INVALID: return "invalid argument";
+    case COVOF_TOO_LARGE: return "mesh larger than the fixed scratch of the allocation-free entry point";
     default: return "unknown status";
   }
 }

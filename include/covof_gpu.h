@@ -38,7 +38,8 @@ enum {
   COVOF_TIMEOUT = 4,      /* a bounded device-side wait gave up */
   COVOF_UNSUPPORTED = 5,  /* option outside the implemented path */
   COVOF_CUDA_ERROR = 6,
-  COVOF_INVALID = 7       /* bad argument (null pointer, size, code) */
+  COVOF_INVALID = 7,      /* bad argument (null pointer, size, code) */
+  COVOF_TOO_LARGE = 8     /* mesh exceeds a fixed-size buffer (covof_poisson_solve_rhs_static_dev) */
 };
 
 /* Boundary codes: same values as BC_* in src/module_constants.f90:41-44. */
@@ -186,6 +187,24 @@ int covof_get_stream(const covof_handle* h, void** stream);
 int covof_last_solve_ms(const covof_handle* h, double* ms);
 /* Outer FP64 refinement steps of the last MIXED Poisson solve. */
 int covof_last_refine_steps(const covof_handle* h, int* steps);
+
+/* Allocation-free plain FP64 Poisson solve (no counterpart in the reference,
+ * which has no GPU path).  For callers that cannot allocate device memory at
+ * the call: a host code whose pool allocator reserved the whole GPU at
+ * start-up, or a time loop that must not pay cudaMalloc's device-wide
+ * synchronisation.  Same operator, solver and results as
+ * covof_poisson_solve_rhs_dev with prm->p_precision = FP64, but no handle:
+ * inputs and outputs are the caller's device pointers, the scratch is a
+ * fixed static device array (about 5.4 MB, held by every GPU that loads the
+ * library until exit) and nothing is allocated.  Limit: (nx+2)*(ny+2) <=
+ * 258*258 (256 x 256 cells); larger meshes return COVOF_TOO_LARGE.  The
+ * first call on a device looks up the array's device address, so make it
+ * before any stream capture.  Runs on the legacy default stream and is
+ * synchronous.  All calls share the array: calls that overlap on the GPU
+ * (from several host threads or streams) race. */
+int covof_poisson_solve_rhs_static_dev(const covof_params* prm, double dt, const double* b,
+                                       const double* rho_u, const double* rho_v, double* p,
+                                       int* iters, double* relres);
 
 /* ---- projection adjoint ------------------------------------------------ */
 

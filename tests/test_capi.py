@@ -66,6 +66,6 @@ def test_default_params_match_python_twin(lib, pkg):
 
 
 def test_strerror_names_every_status(lib, pkg):
-    for s in range(8):
+    for s in range(9):
         assert lib.covof_strerror(s)
     assert lib.covof_abi_version() == 1
