@@ -25,6 +25,11 @@ RECON_PLIC, RECON_ELVIRA = 0, 1
 GAUGE_REFERENCE, GAUGE_PINNED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 INNER_CHEBYSHEV, INNER_CG = 0, 1
+# resident fields (COVOF_FIELD_*), in header order; names follow the Fields dataclass
+FIELD_NAMES = ("u", "v", "p", "C", "rho", "rho_u", "rho_v", "mu", "mu_node", "fx_sigma",
+               "fy_sigma", "curvature", "u_old", "v_old")
+FIELD = {name: k for k, name in enumerate(FIELD_NAMES)}
+RUN_GRAPH = 1
 
 
 class Params(C.Structure):
@@ -56,6 +61,19 @@ class Params(C.Structure):
             v = getattr(self, name)
             out[name] = list(v) if hasattr(v, "__len__") else v
         return out
+
+
+class RunStats(C.Structure):
+    """covof_run_stats (include/covof_gpu.h)."""
+    _fields_ = [
+        ("steps", C.c_int), ("first_bad_step", C.c_int), ("first_bad_status", C.c_int),
+        ("graph", C.c_int), ("mom_iters", C.c_longlong), ("poisson_iters", C.c_longlong),
+        ("refine_steps", C.c_longlong), ("last_relres", C.c_double), ("max_relres", C.c_double),
+        ("ms", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 class CovofError(RuntimeError):
@@ -104,6 +122,10 @@ _SIGS = {
     "covof_poisson_solve_rhs_static_dev": [C.POINTER(Params), C.c_double] + [_VP] * 4 + [_IP, _DP],
     "covof_update_physical_properties": [_VP] + [_VP] * 6,
     "covof_compute_curvature_and_csf": [_VP] + [_VP] * 4,
+    "covof_state_set": [_VP, C.c_int, _VP],
+    "covof_state_get": [_VP, C.c_int, _VP],
+    "covof_state_field_dev": [_VP, C.c_int, C.POINTER(C.c_void_p)],
+    "covof_run_steps": [_VP, C.c_double, C.c_int, C.c_int, C.POINTER(RunStats)],
 }
 
 

@@ -44,6 +44,33 @@ void dfree(T*& p) {
     if (s_ != COVOF_OK) return s_;        \
   } while (0)
 
+// Device-side statistics of a resident run, folded in by k_step_log after
+// every step so that the host reads them once at the end.
+struct RunStats {
+  long long mom_iters, poisson_iters, refine_steps;
+  double last_relres, max_relres;
+  int step, first_bad_step, first_bad_status, pad;
+};
+
+// One thread: fold this step's predictor and Poisson result records in.
+__global__ void k_step_log(const KrylovResult* kr, const PcgResult* pr, RunStats* s) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int step = s->step;
+  s->mom_iters += kr->iters;
+  s->poisson_iters += pr->iters;
+  s->refine_steps += pr->outer;
+  s->last_relres = pr->relres;
+  if (!(pr->relres <= s->max_relres)) s->max_relres = pr->relres;  // also takes a NaN
+  if (s->first_bad_step < 0) {
+    const int bad = kr->status != COVOF_OK ? kr->status : pr->status;
+    if (bad != COVOF_OK) {
+      s->first_bad_step = step;
+      s->first_bad_status = bad;
+    }
+  }
+  s->step = step + 1;
+}
+
 }  // namespace
 
 struct covof_handle {
@@ -90,7 +117,23 @@ struct covof_handle {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_solve_ms = 0.0;
   int last_refine = 0;
-  int coop_max_blocks = 0;
+  // launch plans, fixed for the handle's mesh and parameters (computed once,
+  // so that a stream capture records launches only)
+  bool have_pplan = false;
+  const void* p_fn = nullptr;
+  size_t p_smem = 0;
+  int p_nb = 0;
+  bool have_mplan = false;
+  const void* m_fn = nullptr;
+  int m_nb = 0;
+  // resident time stepping
+  cudaStream_t cap_stream = nullptr;       // non-blocking stream used only while capturing
+  cudaGraphExec_t step_graph[2] = {};      // [0]: x-first Weymouth-Yue order, [1]: y-first
+  double graph_dt = 0.0;
+  bool graph_refused = false;
+  RunStats* d_run = nullptr;
+  RunStats* h_run = nullptr;
+  cudaEvent_t ev2 = nullptr, ev3 = nullptr;
 };
 
 namespace {
@@ -194,7 +237,20 @@ int launch_coop(covof_handle* h, const void* fn, int nblocks, int threads, void*
   CK(cudaMemsetAsync(h->bar, 0, (size_t)(64 + h->sm_count) * sizeof(unsigned int), h->stream));
   CK(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
   if (timed) CK(cudaEventRecord(h->ev0, h->stream));
-  CK(cudaLaunchCooperativeKernel(fn, dim3(nblocks), dim3(threads), args, smem, h->stream));
+  // cooperative launch through the extensible API: the same co-residency
+  // guarantee as cudaLaunchCooperativeKernel, and a stream capture records it
+  // as a cooperative kernel node
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblocks);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = h->stream;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  CK(cudaLaunchKernelExC(&cfg, fn, args));
   if (timed) CK(cudaEventRecord(h->ev1, h->stream));
   return COVOF_OK;
 }
@@ -217,12 +273,54 @@ int sync(covof_handle* h) {
 
 // ---------------------------------------------------------------------------
 // Poisson
-int poisson_dev(covof_handle* h, double dt, const double* u, const double* v, const double* b,
-                const double* rho_u, const double* rho_v, double* p, int* iters, double* relres) {
+//
+// Launch plan: the plain FP64 path runs k_pcg_fp64 over 1024-cell tiles; the
+// mixed path runs the shared-memory-resident inner solver (Chebyshev or CG,
+// one row strip per block) when a strip fits the opt-in shared memory, else
+// the tiled kernel.
+int poisson_plan(covof_handle* h) {
+  if (h->have_pplan) return COVOF_OK;
+  const covof_params& P = h->prm;
+  const bool mixed = P.p_precision == COVOF_PREC_MIXED;
+  const void* fn = mixed ? (const void*)k_pcg_mixed : (const void*)k_pcg_fp64;
+  long long units = (long long)make_tiles(h->D).ntiles;
+  size_t smem = 0;
+  if (mixed) {
+    const int G = P.ny < h->sm_count ? P.ny : h->sm_count;
+    const int Rmax = (P.ny + G - 1) / G;
+    const bool cheb = P.p_inner_kind == COVOF_INNER_CHEBYSHEV;
+    const void* sfn = cheb ? (const void*)k_pcg_mixed_cheb : (const void*)k_pcg_mixed_smem;
+    const size_t bytes = cheb ? smem_cheb_bytes(P.nx, Rmax) : smem_strip_bytes(P.nx, Rmax);
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, sfn) == cudaSuccess && bytes + fa.sharedSizeBytes <= (size_t)optin &&
+        cudaFuncSetAttribute(sfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess) {
+      fn = sfn;
+      smem = bytes;
+      units = G;
+    }
+    cudaGetLastError();
+  }
+  const int nb = coop_blocks(h, fn, kPoissonThreads, units, smem);
+  if (nb < 1) return COVOF_CUDA_ERROR;
+  if (smem && nb != (int)units) return COVOF_CUDA_ERROR;  // strips are sized for exactly G blocks
+  h->p_fn = fn;
+  h->p_smem = smem;
+  h->p_nb = nb;
+  h->have_pplan = true;
+  return COVOF_OK;
+}
+
+// Assembly, solve and copy-back on the handle's stream; the result record
+// stays on the device (h->d_pres).  Nothing here synchronises.
+int poisson_enqueue(covof_handle* h, double dt, const double* u, const double* v, const double* b,
+                    const double* rho_u, const double* rho_v, double* p, bool timed) {
   const covof_params& P = h->prm;
   if (!rho_u || !rho_v || !p || (!b && (!u || !v))) return COVOF_INVALID;
   if (P.p_precond == COVOF_PRECOND_SSOR) return COVOF_UNSUPPORTED;
   CS(ensure_poisson(h));
+  CS(poisson_plan(h));
   const bool mixed = P.p_precision == COVOF_PREC_MIXED;
   const int pinned = P.p_gauge == COVOF_GAUGE_PINNED;
   const dim3 blk(32, 8), grd = grid2(P.nx, P.ny, blk);
@@ -246,42 +344,30 @@ int poisson_dev(covof_handle* h, double dt, const double* u, const double* v, co
   a.tol = P.p_tol; a.inner_tol = P.p_inner_tol;
   a.max_iter = P.p_max_iter; a.inner_max_iter = P.p_inner_max_iter;
   a.max_refine = P.p_max_refine; a.pinned = pinned;
-  const void* fn = mixed ? (const void*)k_pcg_mixed : (const void*)k_pcg_fp64;
-  long long units = (long long)make_tiles(h->D).ntiles;
-  size_t smem = 0;
-  if (mixed) {
-    // shared-memory-resident inner solver when one row strip per SM fits
-    const int G = P.ny < h->sm_count ? P.ny : h->sm_count;
-    const int Rmax = (P.ny + G - 1) / G;
-    const bool cheb = P.p_inner_kind == COVOF_INNER_CHEBYSHEV;
-    const void* sfn = cheb ? (const void*)k_pcg_mixed_cheb : (const void*)k_pcg_mixed_smem;
-    const size_t bytes = cheb ? smem_cheb_bytes(P.nx, Rmax) : smem_strip_bytes(P.nx, Rmax);
-    int optin = 0;
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-    cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, sfn) == cudaSuccess && bytes + fa.sharedSizeBytes <= (size_t)optin &&
-        cudaFuncSetAttribute(sfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess) {
-      fn = sfn;
-      smem = bytes;
-      units = G;
-    }
-    cudaGetLastError();
-  }
-  const int nb = coop_blocks(h, fn, kPoissonThreads, units, smem);
-  if (nb < 1) return COVOF_CUDA_ERROR;
-  if (smem && nb != (int)units) return COVOF_CUDA_ERROR;  // strips are sized for exactly G blocks
   void* args[] = {&a};
-  CS(launch_coop(h, fn, nb, kPoissonThreads, args, true, smem));
+  CS(launch_coop(h, h->p_fn, h->p_nb, kPoissonThreads, args, timed, h->p_smem));
   k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, h->px, p, 0);
   CK(cudaGetLastError());
+  return COVOF_OK;
+}
+
+// Reads the result record back (one small copy + stream synchronisation).
+int poisson_finish(covof_handle* h, int* iters, double* relres) {
   CK(cudaMemcpyAsync(h->h_pres, h->d_pres, sizeof(PcgResult), cudaMemcpyDeviceToHost, h->stream));
   CS(sync(h));
   float ms = 0.f;
   if (cudaEventElapsedTime(&ms, h->ev0, h->ev1) == cudaSuccess) h->last_solve_ms = ms;
+  cudaGetLastError();
   h->last_refine = h->h_pres->outer;
   if (iters) *iters = h->h_pres->iters;
   if (relres) *relres = h->h_pres->relres;
   return h->h_pres->status;
+}
+
+int poisson_dev(covof_handle* h, double dt, const double* u, const double* v, const double* b,
+                const double* rho_u, const double* rho_v, double* p, int* iters, double* relres) {
+  CS(poisson_enqueue(h, dt, u, v, b, rho_u, rho_v, p, true));
+  return poisson_finish(h, iters, relres);
 }
 
 int correct_dev(covof_handle* h, double dt, double* u, double* v, const double* p,
@@ -387,13 +473,30 @@ int check_mom_params(const covof_params& P) {
   return COVOF_OK;
 }
 
-int predictor_dev(covof_handle* h, double dt, double* u, double* v, const double* rho_u,
-                  const double* rho_v, const double* mu, const double* mu_node, const double* fx,
-                  const double* fy, const double* u_old, const double* v_old, int* iters) {
+int predictor_plan(covof_handle* h) {
+  if (h->have_mplan) return COVOF_OK;
+  const covof_params& P = h->prm;
+  const void* fn = P.linear_solver == COVOF_LINEAR_BICGSTAB ? (const void*)k_bicgstab
+                 : P.linear_solver == COVOF_LINEAR_CG ? (const void*)k_cg
+                 : (const void*)k_bicgstab2;
+  const long long nseg = (long long)((P.nx + 1 + 31) / 32) * P.ny + (long long)((P.nx + 31) / 32) * (P.ny + 1);
+  const int nb = coop_blocks(h, fn, kKrylovThreads, (nseg + kKrylovThreads / 32 - 1) / (kKrylovThreads / 32));
+  if (nb < 1) return COVOF_CUDA_ERROR;
+  h->m_fn = fn;
+  h->m_nb = nb;
+  h->have_mplan = true;
+  return COVOF_OK;
+}
+
+// Predictor on the handle's stream, result record left on the device.
+int predictor_enqueue(covof_handle* h, double dt, double* u, double* v, const double* rho_u,
+                      const double* rho_v, const double* mu, const double* mu_node, const double* fx,
+                      const double* fy, const double* u_old, const double* v_old) {
   const covof_params& P = h->prm;
   if (!u || !v || !rho_u || !rho_v || !mu || !mu_node || !fx || !fy || !u_old || !v_old) return COVOF_INVALID;
   CS(check_mom_params(P));
   CS(ensure_mom(h));
+  CS(predictor_plan(h));
   // fields_old of the operator is the current field: the Krylov kernel only
   // writes its own vectors, u and v are overwritten after the solve.
   MomArgs a = mom_args(h, dt, u, v, rho_u, rho_v, mu, mu_node, fx, fy, u_old, v_old);
@@ -402,17 +505,17 @@ int predictor_dev(covof_handle* h, double dt, double* u, double* v, const double
   k_mom_rhs<<<grd, blk, 0, h->stream>>>(a);
   k_mom_pack<<<grd, blk, 0, h->stream>>>(a, u, v);
   CK(cudaGetLastError());
-  const void* fn = P.linear_solver == COVOF_LINEAR_BICGSTAB ? (const void*)k_bicgstab
-                 : P.linear_solver == COVOF_LINEAR_CG ? (const void*)k_cg
-                 : (const void*)k_bicgstab2;
-  const long long nseg = (long long)((P.nx + 1 + 31) / 32) * P.ny + (long long)((P.nx + 31) / 32) * (P.ny + 1);
-  const int nb = coop_blocks(h, fn, kKrylovThreads, (nseg + kKrylovThreads / 32 - 1) / (kKrylovThreads / 32));
-  if (nb < 1) return COVOF_CUDA_ERROR;
   void* args[] = {&a};
-  CS(launch_coop(h, fn, nb, kKrylovThreads, args, false));
+  CS(launch_coop(h, h->m_fn, h->m_nb, kKrylovThreads, args, false));
   k_mom_unpack<<<grd, blk, 0, h->stream>>>(a, u, v);
   CK(cudaGetLastError());
-  CS(velocity_bc_dev(h, u, v));
+  return velocity_bc_dev(h, u, v);
+}
+
+int predictor_dev(covof_handle* h, double dt, double* u, double* v, const double* rho_u,
+                  const double* rho_v, const double* mu, const double* mu_node, const double* fx,
+                  const double* fy, const double* u_old, const double* v_old, int* iters) {
+  CS(predictor_enqueue(h, dt, u, v, rho_u, rho_v, mu, mu_node, fx, fy, u_old, v_old));
   CK(cudaMemcpyAsync(h->h_kres, h->d_kres, sizeof(KrylovResult), cudaMemcpyDeviceToHost, h->stream));
   CS(sync(h));
   if (iters) *iters = h->h_kres->iters;
@@ -510,6 +613,137 @@ int vof_advect_dev(covof_handle* h, double dt, const double* u, const double* v,
   return COVOF_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Resident time stepping
+double** field_slot(covof_handle* h, int f) {
+  switch (f) {
+    case COVOF_FIELD_U: return &h->f_u;
+    case COVOF_FIELD_V: return &h->f_v;
+    case COVOF_FIELD_P: return &h->f_p;
+    case COVOF_FIELD_C: return &h->f_C;
+    case COVOF_FIELD_RHO: return &h->f_rho;
+    case COVOF_FIELD_RHO_U: return &h->f_rho_u;
+    case COVOF_FIELD_RHO_V: return &h->f_rho_v;
+    case COVOF_FIELD_MU: return &h->f_mu;
+    case COVOF_FIELD_MU_NODE: return &h->f_mu_node;
+    case COVOF_FIELD_FX_SIGMA: return &h->f_fx;
+    case COVOF_FIELD_FY_SIGMA: return &h->f_fy;
+    case COVOF_FIELD_CURVATURE: return &h->f_curv;
+    case COVOF_FIELD_U_OLD: return &h->f_u_old;
+    case COVOF_FIELD_V_OLD: return &h->f_v_old;
+    default: return nullptr;
+  }
+}
+
+// Everything a step launches, in stream order, with no host synchronisation
+// (src/module_simulation.f90:492-559 for Euler + STANDARD_PROJECTION).
+int enqueue_step(covof_handle* h, double dt, bool x_first) {
+  const size_t bytes = h->g * sizeof(double);
+  CK(cudaMemcpyAsync(h->f_u_old, h->f_u, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->f_v_old, h->f_v, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  if (h->prm.enable_two_phase) {
+    // advect_vof: Weymouth-Yue step, VOF BC, properties, curvature + CSF
+    CS(wy_step_dev(h, dt, x_first ? 1 : 0, h->f_u, h->f_v, h->f_C));
+    CS(vof_bc_dev(h, h->f_C));
+    CS(props_dev(h, h->f_C, h->f_rho, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node));
+    CS(csf_dev(h, h->f_C, h->f_fx, h->f_fy, h->f_curv));
+    CS(velocity_bc_dev(h, h->f_u, h->f_v));
+  }
+  CS(predictor_enqueue(h, dt, h->f_u, h->f_v, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node, h->f_fx,
+                       h->f_fy, h->f_u_old, h->f_v_old));
+  CS(poisson_enqueue(h, dt, h->f_u, h->f_v, nullptr, h->f_rho_u, h->f_rho_v, h->f_p, false));
+  CS(correct_dev(h, dt, h->f_u, h->f_v, h->f_p, h->f_rho_u, h->f_rho_v));
+  CS(velocity_bc_dev(h, h->f_u, h->f_v));
+  k_step_log<<<1, 32, 0, h->stream>>>(h->d_kres, h->d_pres, h->d_run);
+  CK(cudaGetLastError());
+  return COVOF_OK;
+}
+
+void drop_graphs(covof_handle* h) {
+  for (cudaGraphExec_t& g : h->step_graph) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+}
+
+// Capture one step per Weymouth-Yue pass order.  Capture runs on a
+// non-blocking stream of its own, so that no legacy-stream work of another
+// library joins it.  COVOF_UNSUPPORTED: the driver refused the capture.
+int capture_steps(covof_handle* h, double dt) {
+  drop_graphs(h);
+  for (int q = 0; q < 2; ++q) {
+    cudaStream_t keep = h->stream;
+    h->stream = h->cap_stream;
+    cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    int st = e == cudaSuccess ? enqueue_step(h, dt, q == 0) : COVOF_OK;
+    cudaGraph_t g = nullptr;
+    if (e == cudaSuccess) e = cudaStreamEndCapture(h->stream, &g);
+    h->stream = keep;
+    if (st == COVOF_OK && e == cudaSuccess && g) e = cudaGraphInstantiate(&h->step_graph[q], g, 0ULL);
+    if (g) cudaGraphDestroy(g);
+    if (st != COVOF_OK || e != cudaSuccess || !h->step_graph[q]) {
+      cudaGetLastError();
+      drop_graphs(h);
+      return (st != COVOF_OK && st != COVOF_CUDA_ERROR) ? st : COVOF_UNSUPPORTED;
+    }
+  }
+  h->graph_dt = dt;
+  return COVOF_OK;
+}
+
+int run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run_stats* out) {
+  if (nsteps < 0 || !(dt > 0.0)) return COVOF_INVALID;
+  const covof_params& P = h->prm;
+  if (P.p_precond == COVOF_PRECOND_SSOR) return COVOF_UNSUPPORTED;
+  CS(check_mom_params(P));
+  // every buffer and launch plan exists before a capture starts
+  CS(ensure_fields(h));
+  CS(ensure_poisson(h));
+  CS(poisson_plan(h));
+  CS(ensure_mom(h));
+  CS(predictor_plan(h));
+  CS(ensure_vof(h));
+  *h->h_run = RunStats{0, 0, 0, 0.0, 0.0, 0, -1, COVOF_OK, 0};
+  CK(cudaMemcpyAsync(h->d_run, h->h_run, sizeof(RunStats), cudaMemcpyHostToDevice, h->stream));
+  bool graph = (flags & COVOF_RUN_GRAPH) != 0 && !h->graph_refused;
+  if (graph && (!h->step_graph[0] || h->graph_dt != dt)) {
+    const int st = capture_steps(h, dt);
+    if (st == COVOF_UNSUPPORTED) {
+      h->graph_refused = true;
+      graph = false;
+    } else if (st != COVOF_OK) {
+      return st;
+    }
+  }
+  CK(cudaEventRecord(h->ev2, h->stream));
+  for (int k = 0; k < nsteps; ++k) {
+    const bool x_first = (h->vof_step_count % 2) == 0;
+    if (graph) CK(cudaGraphLaunch(h->step_graph[x_first ? 0 : 1], h->stream));
+    else CS(enqueue_step(h, dt, x_first));
+    if (P.enable_two_phase) h->vof_step_count += 1;
+  }
+  CK(cudaEventRecord(h->ev3, h->stream));
+  CK(cudaMemcpyAsync(h->h_run, h->d_run, sizeof(RunStats), cudaMemcpyDeviceToHost, h->stream));
+  CS(sync(h));
+  const RunStats& r = *h->h_run;
+  if (out) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev2, h->ev3);
+    cudaGetLastError();
+    out->steps = r.step;
+    out->first_bad_step = r.first_bad_step;
+    out->first_bad_status = r.first_bad_status;
+    out->graph = graph ? 1 : 0;
+    out->mom_iters = r.mom_iters;
+    out->poisson_iters = r.poisson_iters;
+    out->refine_steps = r.refine_steps;
+    out->last_relres = r.last_relres;
+    out->max_relres = r.max_relres;
+    out->ms = ms;
+  }
+  return r.first_bad_step < 0 ? COVOF_OK : r.first_bad_status;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -581,15 +815,19 @@ int covof_create(const covof_params* params, covof_handle** out) {
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device);
   if (!coop) return fail(COVOF_UNSUPPORTED);
   if (cudaStreamCreate(&h->stream) != cudaSuccess) return fail(COVOF_CUDA_ERROR);
-  if (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(COVOF_CUDA_ERROR);
+  if (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess ||
+      cudaEventCreate(&h->ev2) != cudaSuccess || cudaEventCreate(&h->ev3) != cudaSuccess)
     return fail(COVOF_CUDA_ERROR);
   h->part_blocks = h->sm_count;  // persistent kernels run at most one block per SM
   if (dalloc(&h->bar, (size_t)64 + h->sm_count) || dalloc(&h->err, 1) ||
       dalloc(&h->part, (size_t)kMaxPartRegions * h->part_blocks) ||
-      dalloc(&h->d_pres, 1) || dalloc(&h->d_kres, 1))
+      dalloc(&h->d_pres, 1) || dalloc(&h->d_kres, 1) || dalloc(&h->d_run, 1))
     return fail(COVOF_CUDA_ERROR);
   if (cudaMallocHost(&h->h_pres, sizeof(PcgResult)) != cudaSuccess ||
-      cudaMallocHost(&h->h_kres, sizeof(KrylovResult)) != cudaSuccess)
+      cudaMallocHost(&h->h_kres, sizeof(KrylovResult)) != cudaSuccess ||
+      cudaMallocHost(&h->h_run, sizeof(RunStats)) != cudaSuccess)
     return fail(COVOF_CUDA_ERROR);
   *out = h;
   return COVOF_OK;
@@ -608,11 +846,14 @@ int covof_destroy(covof_handle* h) {
   for (int q = 0; q < 7; ++q) dfree(h->mv[q]);
   float** ff[] = {&h->pxb, &h->e32, &h->r32b, &h->r32, &h->d32, &h->d32b, &h->Ad32, &h->ax32, &h->ay32, &h->aP32};
   for (float** q : ff) dfree(*q);
-  dfree(h->bar); dfree(h->err); dfree(h->d_pres); dfree(h->d_kres);
+  drop_graphs(h);
+  dfree(h->bar); dfree(h->err); dfree(h->d_pres); dfree(h->d_kres); dfree(h->d_run);
   if (h->h_pres) cudaFreeHost(h->h_pres);
   if (h->h_kres) cudaFreeHost(h->h_kres);
-  if (h->ev0) cudaEventDestroy(h->ev0);
-  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->h_run) cudaFreeHost(h->h_run);
+  for (cudaEvent_t e : {h->ev0, h->ev1, h->ev2, h->ev3})
+    if (e) cudaEventDestroy(e);
+  if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return COVOF_OK;
@@ -972,6 +1213,39 @@ int covof_compute_curvature_and_csf(covof_handle* h, const double* C, double* fx
   CS(csf_dev(h, h->f_C, h->f_fx, h->f_fy, h->f_curv));
   CS(d2h(h, fx_sigma, h->f_fx, g)); CS(d2h(h, fy_sigma, h->f_fy, g)); CS(d2h(h, curvature, h->f_curv, g));
   return sync(h);
+}
+
+// ---- resident time stepping -------------------------------------------------
+int covof_state_set(covof_handle* h, int field, const double* host) {
+  if (!h || !host) return COVOF_INVALID;
+  CS(ensure_fields(h));
+  double** slot = field_slot(h, field);
+  if (!slot) return COVOF_INVALID;
+  CS(h2d(h, *slot, host, h->g));
+  return sync(h);
+}
+
+int covof_state_get(covof_handle* h, int field, double* host) {
+  if (!h || !host) return COVOF_INVALID;
+  CS(ensure_fields(h));
+  double** slot = field_slot(h, field);
+  if (!slot) return COVOF_INVALID;
+  CS(d2h(h, host, *slot, h->g));
+  return sync(h);
+}
+
+int covof_state_field_dev(covof_handle* h, int field, double** dev) {
+  if (!h || !dev) return COVOF_INVALID;
+  CS(ensure_fields(h));
+  double** slot = field_slot(h, field);
+  if (!slot) return COVOF_INVALID;
+  *dev = *slot;
+  return COVOF_OK;
+}
+
+int covof_run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run_stats* stats) {
+  if (!h) return COVOF_INVALID;
+  return run_steps(h, dt, nsteps, flags, stats);
 }
 
 }  // extern "C"

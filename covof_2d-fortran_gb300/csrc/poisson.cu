@@ -356,7 +356,8 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_fp64(PoissonArgs a) {
 // the exit is certified on the true FP64 residual b - A x.
 // Reference gauge: c = sum(r)/sum(aP) removes the right-hand side's
 // rounding-level component along the scaled null vector S^-1 1 (the FP32
-// copy cannot represent the 1e-12*dvol shift).
+// copy cannot represent the 1e-12*dvol shift), and the preconditioned vector
+// is projected the same way, so the preconditioner stays symmetric.
 // Cell ownership for the FP64 outer loop.  Tiles: the 1024-cell tiles of
 // the streaming PCG.  Strips: block b owns full-width rows [r0, r0+R); thread
 // t owns strip cells t, t+1024, ... (row-major), which is also the layout of
@@ -680,13 +681,16 @@ template <class Own, class Inner>
 __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, GridReducer& R) {
   const Dims D = a.D;
   const int pk = a.pinned ? D.P + 1 : -1;
-  double* x = a.x; double* r = a.r; double* z = a.z; double* w = a.w; double* pv = a.p; double* qv = a.q;
+  double* x = a.x; double* r = a.r; double* z = a.z; double* pv = a.p; double* qv = a.q;
   bool ok = true;
   int total_inner = 0, outer = 0, status = COVOF_OK, true_checks = 0;
-  double b_norm = 1.0, r_norm = 0.0, aP_sum = 1.0, r_sum = 0.0, sigma_old = 1.0;
+  double b_norm = 1.0, r_norm = 0.0, aP_sum = 1.0, e_sum = 1.0, r_sum = 0.0, sigma_old = 1.0;
   bool fresh = true;
+  // e = A 1 (interior ones, zero ghosts): the 1e-12*dvol shift of aP, the
+  // eigenvalue of the constant vector in the reference gauge.
+  auto ones_image = [&](int k) { return a.aP[k] - a.ax[k] - a.ax[k + 1] - a.ay[k] - a.ay[k + D.P]; };
   auto true_residual = [&]() -> bool {
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     own.each([&](int k, int) {
       const double rr = (k == pk) ? 0.0 : a.b[k] - stencil64(D, k, x, a.ax, a.ay, a.aP);
       r[k] = rr;
@@ -694,14 +698,16 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       acc[1] = fma(rr, rr, acc[1]);
       acc[2] += rr;
       acc[3] += a.aP[k];
+      acc[4] += ones_image(k);
     });
-    double t[4];
-    if (!reduce<double, 4>(R, acc, t)) return false;
+    double t[5];
+    if (!reduce<double, 5>(R, acc, t)) return false;
     b_norm = sqrt(t[0]);
     if (b_norm < 1.0e-30) b_norm = 1.0;
     r_norm = sqrt(t[1]);
     r_sum = t[2];
     aP_sum = t[3];
+    e_sum = t[4];
     return true;
   };
   if (!true_residual()) ok = false;
@@ -728,36 +734,60 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     total_inner += o.iters;
     outer++;
     if (!o.ok) { ok = false; break; }
-    own.each([&](int k, int c) { z[k] = (r_norm * a.isd[k]) * (double)inner.y(k, c); });
-    if (!R.gs.sync()) { ok = false; break; }
-    double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    own.each([&](int k, int) {
-      const double wk = (k == pk) ? 0.0 : stencil64(D, k, z, a.ax, a.ay, a.aP);
-      w[k] = wk;
-      const double zk = z[k], rk = r[k];
-      acc[0] = fma(zk, wk, acc[0]);
-      acc[3] = fma(zk, rk, acc[3]);
+    // z = ||r|| S y, then (reference gauge) minus its aP-weighted mean: the
+    // deflation of the right-hand side above is the orthogonal projection
+    // off the near-null vector D^1/2 1 of S A S, and projecting the output as
+    // well keeps the preconditioner symmetric (S P K P S), which the outer
+    // conjugate-gradient recurrences need.  z keeps the unprojected values;
+    // the constant is applied where z is used (A 1 = e is evaluated from the
+    // coefficients), so no extra grid barrier is needed.
+    // One reduction gives gam and the orthogonalisation against the previous
+    // direction: beta = <z, q_old> / <p_old, q_old>.
+    double zs[3] = {0.0, 0.0, 0.0};
+    own.each([&](int k, int c) {
+      const double zk = (r_norm * a.isd[k]) * (double)inner.y(k, c);
+      z[k] = zk;
+      zs[0] = fma(a.aP[k], zk, zs[0]);
       if (!fresh) {
-        acc[1] = fma(zk, qv[k], acc[1]);
-        acc[2] = fma(pv[k], wk, acc[2]);
-        acc[4] = fma(pv[k], rk, acc[4]);
+        const double qk = qv[k];
+        zs[1] = fma(zk, qk, zs[1]);
+        zs[2] += qk;
       }
     });
-    double t[5];
-    if (!reduce<double, 5>(R, acc, t)) { ok = false; break; }
-    const double beta = fresh ? 0.0 : t[1] / sigma_old;
-    const double sigma = fresh ? t[0] : t[0] - beta * t[1] - beta * t[2] + beta * beta * sigma_old;
-    if (!(fabs(sigma) > 1.0e-300)) { status = COVOF_BREAKDOWN; break; }
-    const double alpha = (fresh ? t[3] : t[3] - beta * t[4]) / sigma;
+    double tz[3];
+    if (!reduce<double, 3>(R, zs, tz)) { ok = false; break; }
+    // Reference gauge: the projection removes gam (aP-weighted mean of z);
+    // the constant mode itself is then solved exactly, a coarse correction
+    // z += (1'r / 1'A1) 1 -- without it the iterate would stay on the
+    // hyperplane aP'x = 0 and the residual could not fall below
+    // eps * mean(p) (about 1e-6 relative for a hydrostatic pressure).
+    const double shift = a.pinned ? 0.0 : tz[0] / aP_sum - r_sum / e_sum;
+    const double beta = fresh ? 0.0 : (tz[1] - shift * tz[2]) / sigma_old;
+    // p = z - beta p_old, q = A z - beta q_old, and <p,q>, <p,r> from the
+    // formed vectors: the algebraic expansion of <p,q> cancels badly when
+    // consecutive directions are dominated by the same smooth mode.
+    double acc[2] = {0.0, 0.0};
     const bool was_fresh = fresh;
-    double acc2[2] = {0.0, 0.0};
     own.each([&](int k, int) {
-      const double pk_ = was_fresh ? z[k] : fma(-beta, pv[k], z[k]);
-      const double qk_ = was_fresh ? w[k] : fma(-beta, qv[k], w[k]);
+      double wk = (k == pk) ? 0.0 : stencil64(D, k, z, a.ax, a.ay, a.aP);
+      if (shift != 0.0) wk -= shift * ones_image(k);
+      const double zk = z[k] - shift;
+      const double pk_ = was_fresh ? zk : fma(-beta, pv[k], zk);
+      const double qk_ = was_fresh ? wk : fma(-beta, qv[k], wk);
       pv[k] = pk_;
       qv[k] = qk_;
-      x[k] = fma(alpha, pk_, x[k]);
-      const double rk = fma(-alpha, qk_, r[k]);
+      acc[0] = fma(pk_, qk_, acc[0]);
+      acc[1] = fma(pk_, r[k], acc[1]);
+    });
+    double t[2];
+    if (!reduce<double, 2>(R, acc, t)) { ok = false; break; }
+    const double sigma = t[0];
+    if (!(sigma > 0.0)) { status = COVOF_BREAKDOWN; break; }
+    const double alpha = t[1] / sigma;
+    double acc2[2] = {0.0, 0.0};
+    own.each([&](int k, int) {
+      x[k] = fma(alpha, pv[k], x[k]);
+      const double rk = fma(-alpha, qv[k], r[k]);
       r[k] = rk;
       acc2[0] = fma(rk, rk, acc2[0]);
       acc2[1] += rk;
@@ -799,7 +829,8 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
 // and the exit is certified on the true FP64 residual b - A x.
 // Reference gauge: c = sum(r)/sum(aP) removes the right-hand side's
 // rounding-level component along the scaled null vector S^-1 1 (the FP32
-// copy cannot represent the 1e-12*dvol shift).
+// copy cannot represent the 1e-12*dvol shift), and the preconditioned vector
+// is projected the same way, so the preconditioner stays symmetric.
 //
 // k_pcg_mixed: streaming tiles (any size).  k_pcg_mixed_smem: the FP32 inner
 // solver lives in shared memory (row strips; used when a strip fits).

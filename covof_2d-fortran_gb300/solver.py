@@ -273,3 +273,31 @@ class Solver:
         st = self.lib.covof_compute_curvature_and_csf(self.h, _ptr(f.C), _ptr(f.fx_sigma),
                                                       _ptr(f.fy_sigma), _ptr(f.curvature))
         self._check(st, "covof_compute_curvature_and_csf")
+
+    # -- device-resident time stepping ----------------------------------------
+    def state_set(self, f: Fields):
+        """Upload every resident field from host Fields."""
+        for name in capi.FIELD_NAMES:
+            self._check(self.lib.covof_state_set(self.h, capi.FIELD[name], _ptr(getattr(f, name))),
+                        "covof_state_set")
+
+    def state_get(self, f: Fields):
+        """Download every resident field into host Fields."""
+        for name in capi.FIELD_NAMES:
+            self._check(self.lib.covof_state_get(self.h, capi.FIELD[name], _ptr(getattr(f, name))),
+                        "covof_state_get")
+
+    def state_field_dev(self, name: str) -> int:
+        """Device address of one resident field."""
+        ptr = C.c_void_p()
+        self._check(self.lib.covof_state_field_dev(self.h, capi.FIELD[name], C.byref(ptr)),
+                    "covof_state_field_dev")
+        return ptr.value
+
+    def run_steps(self, dt: float, nsteps: int, graph: bool = True) -> tuple[int, dict]:
+        """nsteps time-loop iterations of sim_run (src/module_simulation.f90:492-559)
+        on the resident fields; returns (status, run statistics)."""
+        stats = capi.RunStats()
+        st = self.lib.covof_run_steps(self.h, dt, int(nsteps), capi.RUN_GRAPH if graph else 0,
+                                      C.byref(stats))
+        return self._check(st, "covof_run_steps"), stats.as_dict()

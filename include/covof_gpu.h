@@ -263,6 +263,53 @@ int covof_update_physical_properties(covof_handle* h, double* C, double* rho, do
 int covof_compute_curvature_and_csf(covof_handle* h, const double* C, double* fx_sigma,
                                     double* fy_sigma, double* curvature);
 
+/* ---- device-resident time stepping ------------------------------------ */
+
+/* The members of flow_fields_t (src/module_fields.f90:27-92) that the hot
+ * path reads or writes, kept on the device inside the handle. */
+enum {
+  COVOF_FIELD_U = 0, COVOF_FIELD_V = 1, COVOF_FIELD_P = 2, COVOF_FIELD_C = 3,
+  COVOF_FIELD_RHO = 4, COVOF_FIELD_RHO_U = 5, COVOF_FIELD_RHO_V = 6, COVOF_FIELD_MU = 7,
+  COVOF_FIELD_MU_NODE = 8, COVOF_FIELD_FX_SIGMA = 9, COVOF_FIELD_FY_SIGMA = 10,
+  COVOF_FIELD_CURVATURE = 11, COVOF_FIELD_U_OLD = 12, COVOF_FIELD_V_OLD = 13, COVOF_NFIELDS = 14
+};
+/* Copy one (nx+2)*(ny+2) field between the host and the handle's resident
+ * copy (synchronous). */
+int covof_state_set(covof_handle* h, int field, const double* host);
+int covof_state_get(covof_handle* h, int field, double* host);
+/* Device address of the resident copy (valid until covof_destroy). */
+int covof_state_field_dev(covof_handle* h, int field, double** dev);
+
+typedef struct covof_run_stats {
+  int steps;               /* time steps run */
+  int first_bad_step;      /* -1 when every solve returned COVOF_OK */
+  int first_bad_status;    /* status of that step's first failing solve */
+  int graph;               /* 1 when the steps replayed captured CUDA graphs */
+  long long mom_iters;     /* predictor Krylov iterations, summed over steps */
+  long long poisson_iters; /* Poisson iterations (mixed: FP32 inner steps), summed */
+  long long refine_steps;  /* mixed: FP64 outer steps, summed */
+  double last_relres;      /* Poisson ||r||/||b|| of the last step */
+  double max_relres;       /* largest Poisson ||r||/||b|| of the run */
+  double ms;               /* device time of the run (CUDA events) */
+} covof_run_stats;
+
+#define COVOF_RUN_GRAPH 1  /* flag: replay each step as a captured CUDA graph */
+
+/* nsteps iterations of the time loop body of sim_run
+ * (src/module_simulation.f90:492-559) on the resident fields, for a fixed dt
+ * (adaptive_dt = .false.), Euler time stepping and STANDARD_PROJECTION:
+ *   u_old = u, v_old = v;
+ *   if enable_two_phase: advect_vof (WEYMOUTH_YUE), apply_velocity_bc;
+ *   sim_solve_standard_projection.
+ * No host synchronisation between steps: each solve's status is folded into
+ * device-side statistics that are read once at the end.  A failing step does
+ * not stop the run (the reference's Krylov exits are silent too); the first
+ * one is reported.  With COVOF_RUN_GRAPH each step is one graph launch (two
+ * graphs, for the two Weymouth-Yue pass orders), captured on the first call
+ * for a given dt; where capture is refused the steps run eagerly and
+ * stats->graph is 0. */
+int covof_run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

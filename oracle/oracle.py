@@ -194,3 +194,16 @@ def vof_advect(prm, dt, step_count, f):
                               _p(f.rho_u), _p(f.rho_v), _p(f.mu), _p(f.mu_node), _p(f.fx_sigma),
                               _p(f.fy_sigma), _p(f.curvature))
     assert st == 0, st
+
+
+def time_step(prm, dt, step_count, f):
+    """One iteration of the time loop body of sim_run (src/module_simulation.f90:
+    492-559) for a fixed dt, Euler stepping and STANDARD_PROJECTION:
+    u_old = u, v_old = v; advect_vof + apply_velocity_bc when two-phase;
+    sim_solve_standard_projection.  Returns (iters_u, iters_p, relres, status)."""
+    f.u_old[...] = f.u
+    f.v_old[...] = f.v
+    if prm.enable_two_phase:
+        vof_advect(prm, dt, step_count, f)
+        apply_velocity_bc(prm, f.u, f.v, False)
+    return sp_step(prm, dt, f)

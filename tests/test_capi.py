@@ -37,16 +37,18 @@ def test_python_mirror_covers_the_header(pkg):
     assert sorted(pkg.capi.exported_symbols()) == _declared()
 
 
-def test_params_struct_layout_matches_c(pkg, tmp_path):
+@pytest.mark.parametrize("cname,pyname", [("covof_params", "Params"), ("covof_run_stats", "RunStats")])
+def test_struct_layout_matches_c(pkg, tmp_path, cname, pyname):
+    struct = getattr(pkg.capi, pyname)
     src = tmp_path / "probe.c"
-    fields = [f for f, _ in pkg.capi.Params._fields_]
-    body = "\n".join(f'  printf("%s %zu\\n", "{f}", offsetof(covof_params, {f}));' for f in fields)
+    fields = [f for f, _ in struct._fields_]
+    body = "\n".join(f'  printf("%s %zu\\n", "{f}", offsetof({cname}, {f}));' for f in fields)
     src.write_text(textwrap.dedent(f"""
         #include <stdio.h>
         #include <stddef.h>
         #include "{HEADER}"
         int main(void) {{
-          printf("sizeof %zu\\n", sizeof(covof_params));
+          printf("sizeof %zu\\n", sizeof({cname}));
         {body}
           return 0;
         }}"""))
@@ -54,9 +56,22 @@ def test_params_struct_layout_matches_c(pkg, tmp_path):
     subprocess.run(["gcc", "-o", str(exe), str(src)], check=True)
     out = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
                                                          check=True).stdout.splitlines())
-    assert int(out["sizeof"]) == C.sizeof(pkg.capi.Params)
+    assert int(out["sizeof"]) == C.sizeof(struct)
     for f in fields:
-        assert int(out[f]) == getattr(pkg.capi.Params, f).offset, f
+        assert int(out[f]) == getattr(struct, f).offset, f
+
+
+def test_field_ids_match_c(pkg, tmp_path):
+    src = tmp_path / "ids.c"
+    names = [f"COVOF_FIELD_{n.upper()}" for n in pkg.capi.FIELD_NAMES]
+    body = "\n".join(f'  printf("%d\\n", {n});' for n in names)
+    src.write_text(f'#include <stdio.h>\n#include "{HEADER}"\nint main(void) {{\n{body}\n'
+                   f'  printf("%d\\n", COVOF_NFIELDS);\n  return 0;\n}}\n')
+    exe = tmp_path / "ids"
+    subprocess.run(["gcc", "-o", str(exe), str(src)], check=True)
+    vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                           check=True).stdout.split()]
+    assert vals == list(range(len(names))) + [len(names)]
 
 
 def test_default_params_match_python_twin(lib, pkg):

@@ -1,0 +1,116 @@
+"""Device-resident time stepping (covof_run_steps), eager and CUDA-graph
+replay, against the oracle's time loop on the rising-bubble case."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _bubble(pkg, orc, nx=32, ny=64, mixed=False):
+    p, C0, dt = pkg.cases.bubble_case(nx=nx, ny=ny, nsub=8)
+    if mixed:
+        p.p_precision = pkg.capi.PREC_MIXED
+    f = pkg.Fields.allocate(p)
+    f.C[...] = C0
+    orc.apply_vof_bc(p, f.C)
+    orc.update_physical_properties(p, f)
+    orc.compute_curvature_and_csf(p, f)
+    return p, f, dt
+
+
+def _close(g, f, rel=1e-9):
+    for name in ("u", "v", "p"):
+        a, b = getattr(g, name), getattr(f, name)
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < rel, name
+    assert np.abs(g.C - f.C).max() <= 1e-12
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_resident_steps_match_oracle(gpu_pkg, orc, graph):
+    pkg = gpu_pkg
+    p, f, dt = _bubble(pkg, orc)
+    g = f.copy()
+    nsteps = 6
+    iters = 0
+    for k in range(nsteps):
+        iu, ip, rr, st = orc.time_step(p, dt, k, f)
+        assert st == 0
+        iters += iu
+    with pkg.Solver(p) as s:
+        s.state_set(g)
+        st, stats = s.run_steps(dt, nsteps, graph=graph)
+        assert st == 0 and stats["first_bad_step"] == -1
+        assert stats["steps"] == nsteps
+        assert stats["graph"] == int(graph)
+        assert stats["last_relres"] <= 1e-10
+        assert s.vof_step_count == nsteps
+        s.state_get(g)
+    _close(g, f)
+
+
+def test_graph_replay_equals_eager_bitwise(gpu_pkg, orc):
+    """Two calls in a row (odd step count, so both pass orders replay from
+    both parities), graph vs eager: identical bits."""
+    pkg = gpu_pkg
+    p, f, dt = _bubble(pkg, orc, mixed=True)
+    out = []
+    for graph in (False, True):
+        g = f.copy()
+        with pkg.Solver(p) as s:
+            s.state_set(g)
+            for n in (3, 4):
+                st, stats = s.run_steps(dt, n, graph=graph)
+                assert st == 0 and stats["graph"] == int(graph)
+            s.state_get(g)
+        out.append(g)
+    for name in pkg.capi.FIELD_NAMES:
+        assert np.array_equal(getattr(out[0], name), getattr(out[1], name)), name
+
+
+def test_resident_steps_equal_host_calls(gpu_pkg, orc):
+    """run_steps == the per-call host API (advect_vof + BC + SP step) bitwise."""
+    pkg = gpu_pkg
+    p, f, dt = _bubble(pkg, orc)
+    g = f.copy()
+    with pkg.Solver(p) as s:
+        for _ in range(4):
+            f.u_old[...] = f.u
+            f.v_old[...] = f.v
+            s.advect_vof(dt, f)
+            orc.apply_velocity_bc(p, f.u, f.v, False)
+            s.sim_solve_standard_projection(dt, f)
+    with pkg.Solver(p) as s:
+        s.state_set(g)
+        st, _ = s.run_steps(dt, 4, graph=True)
+        assert st == 0
+        s.state_get(g)
+    for name in ("u", "v", "p", "C", "rho_u", "rho_v", "fx_sigma", "fy_sigma"):
+        assert np.array_equal(getattr(g, name), getattr(f, name)), name
+
+
+def test_new_dt_recaptures(gpu_pkg, orc):
+    pkg = gpu_pkg
+    p, f, dt = _bubble(pkg, orc)
+    g = f.copy()
+    for k, d in enumerate((dt, 0.5 * dt)):
+        orc.time_step(p, d, k, f)
+    with pkg.Solver(p) as s:
+        s.state_set(g)
+        for d in (dt, 0.5 * dt):
+            st, stats = s.run_steps(d, 1, graph=True)
+            assert st == 0 and stats["graph"] == 1
+        s.state_get(g)
+    _close(g, f)
+
+
+def test_state_field_ids_rejected(gpu_pkg):
+    pkg = gpu_pkg
+    p = pkg.cases.make_params(16, 16, 1.0, 1.0)
+    with pkg.Solver(p) as s:
+        buf = np.zeros((18, 18))
+        assert s.lib.covof_state_set(s.h, 99, buf.ctypes.data) == pkg.capi.INVALID
+        assert s.lib.covof_state_get(s.h, -1, buf.ctypes.data) == pkg.capi.INVALID
+        with pytest.raises(pkg.CovofError):
+            s.run_steps(-1.0, 1)
