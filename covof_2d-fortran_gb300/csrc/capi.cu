@@ -100,6 +100,7 @@ struct covof_handle {
   // VOF scratch
   bool have_vof = false;
   double *cs = nullptr, *seg = nullptr, *cnx = nullptr, *cny = nullptr, *ckap = nullptr;
+  int *vlist = nullptr, *vcount = nullptr;  // interface-cell list of the reconstruction
   // adjoint scratch
   bool have_adj = false;
   double *arhs = nullptr, *apsi = nullptr, *apart = nullptr, *asum = nullptr;
@@ -122,7 +123,7 @@ struct covof_handle {
   bool have_pplan = false;
   const void* p_fn = nullptr;
   size_t p_smem = 0;
-  int p_nb = 0;
+  int p_nb = 0, p_threads = 0;
   bool have_mplan = false;
   const void* m_fn = nullptr;
   int m_nb = 0;
@@ -198,6 +199,7 @@ int ensure_vof(covof_handle* h) {
   const size_t g = h->g;
   CS(dalloc(&h->cs, g)); CS(dalloc(&h->seg, 3 * g));
   CS(dalloc(&h->cnx, g)); CS(dalloc(&h->cny, g)); CS(dalloc(&h->ckap, g));
+  CS(dalloc(&h->vlist, g)); CS(dalloc(&h->vcount, 1));
   h->have_vof = true;
   return COVOF_OK;
 }
@@ -278,12 +280,30 @@ int sync(covof_handle* h) {
 // mixed path runs the shared-memory-resident inner solver (Chebyshev or CG,
 // one row strip per block) when a strip fits the opt-in shared memory, else
 // the tiled kernel.
+// Block size of the plain FP64 PCG: 1024-cell tiles when there are at least
+// two per SM; otherwise the size that puts the fewest cells on the busiest
+// block, so that a small mesh spreads over every SM (the FP64 issue rate of
+// an SM, not bandwidth, bounds this kernel on GB300).
+int fp64_threads(const covof_handle* h) {
+  const long long G = h->sm_count;
+  if (make_tiles(h->D, 1024).ntiles >= 2 * G) return 1024;
+  int best = 1024;
+  long long best_cells = -1;
+  for (int t : {1024, 512, 256, 128}) {
+    const long long nt = make_tiles(h->D, t).ntiles;
+    const long long cells = ((nt + G - 1) / G) * t;  // cells of the busiest block
+    if (best_cells < 0 || cells < best_cells) { best_cells = cells; best = t; }
+  }
+  return best;
+}
+
 int poisson_plan(covof_handle* h) {
   if (h->have_pplan) return COVOF_OK;
   const covof_params& P = h->prm;
   const bool mixed = P.p_precision == COVOF_PREC_MIXED;
   const void* fn = mixed ? (const void*)k_pcg_mixed : (const void*)k_pcg_fp64;
-  long long units = (long long)make_tiles(h->D).ntiles;
+  const int threads = mixed ? kPoissonThreads : fp64_threads(h);
+  long long units = (long long)make_tiles(h->D, threads).ntiles;
   size_t smem = 0;
   if (mixed) {
     const int G = P.ny < h->sm_count ? P.ny : h->sm_count;
@@ -302,12 +322,13 @@ int poisson_plan(covof_handle* h) {
     }
     cudaGetLastError();
   }
-  const int nb = coop_blocks(h, fn, kPoissonThreads, units, smem);
+  const int nb = coop_blocks(h, fn, threads, units, smem);
   if (nb < 1) return COVOF_CUDA_ERROR;
   if (smem && nb != (int)units) return COVOF_CUDA_ERROR;  // strips are sized for exactly G blocks
   h->p_fn = fn;
   h->p_smem = smem;
   h->p_nb = nb;
+  h->p_threads = threads;
   h->have_pplan = true;
   return COVOF_OK;
 }
@@ -345,7 +366,7 @@ int poisson_enqueue(covof_handle* h, double dt, const double* u, const double* v
   a.max_iter = P.p_max_iter; a.inner_max_iter = P.p_inner_max_iter;
   a.max_refine = P.p_max_refine; a.pinned = pinned;
   void* args[] = {&a};
-  CS(launch_coop(h, h->p_fn, h->p_nb, kPoissonThreads, args, timed, h->p_smem));
+  CS(launch_coop(h, h->p_fn, h->p_nb, h->p_threads, args, timed, h->p_smem));
   k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, h->px, p, 0);
   CK(cudaGetLastError());
   return COVOF_OK;
@@ -532,13 +553,18 @@ VofArgs vof_args(covof_handle* h, double dt, const double* C, const double* Cn, 
   return a;
 }
 
+// Pure cells directly, interface cells one warp each (list built on the
+// device, so nothing here waits for the host), then the ghost ring.
 int reconstruct_dev(covof_handle* h, const double* C, double* seg_out) {
+  CS(ensure_vof(h));
   VofArgs a = vof_args(h, 0.0, C, C, nullptr, nullptr);
   if (seg_out) a.seg = seg_out;
   const dim3 blk(32, 4), grd = grid2(h->D.nx + 2, h->D.ny + 2, blk);
-  k_vof_reconstruct<<<grd, blk, 0, h->stream>>>(a);
+  CK(cudaMemsetAsync(h->vcount, 0, sizeof(int), h->stream));
+  k_vof_classify<<<grd, blk, 0, h->stream>>>(a, h->vlist, h->vcount);
+  k_vof_mixed<<<4 * h->sm_count, 128, 0, h->stream>>>(a, h->vlist, h->vcount);
   const int nring = 2 * h->D.ny + 2 * (h->D.nx + 2);
-  k_vof_ring<<<(nring + 127) / 128, 128, 0, h->stream>>>(a);
+  k_vof_ring_warp<<<(nring + 3) / 4, 128, 0, h->stream>>>(a);
   CK(cudaGetLastError());
   return COVOF_OK;
 }
@@ -848,6 +874,7 @@ int covof_destroy(covof_handle* h) {
   for (float** q : ff) dfree(*q);
   drop_graphs(h);
   dfree(h->bar); dfree(h->err); dfree(h->d_pres); dfree(h->d_kres); dfree(h->d_run);
+  dfree(h->vlist); dfree(h->vcount);
   if (h->h_pres) cudaFreeHost(h->h_pres);
   if (h->h_kres) cudaFreeHost(h->h_kres);
   if (h->h_run) cudaFreeHost(h->h_run);

@@ -131,7 +131,7 @@ namespace covof {
 // Grid-wide sum of up to 8 FP64 values per thread, deterministic: block
 // partials are written to one of two regions, the grid meets at the
 // barrier, then every block combines all partials in the same fixed order
-// (one partial per thread, then a block tree), so all blocks obtain
+// (warp 0: strided partial sums, then a shuffle tree), so all blocks obtain
 // bit-identical totals.  Consecutive reductions alternate regions, so a
 // region is rewritten only after every block has passed the barrier that
 // follows its last read.  part must hold 2 * 8 * nblocks doubles.
@@ -141,7 +141,21 @@ struct GridReducer {
   int region;
   template <int NV>
   __device__ bool sum(double (&v)[NV]) {
-    static_assert(NV <= 8, "at most 8 values");
+    return sum_map<NV, NV>(v, v, [](const double* w, double* o) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) o[q] = w[q];
+    });
+  }
+
+  // As sum(), but thread 0 maps the NV totals to NO scalars before the
+  // broadcast.  FP64 issue is the scarce resource of a GB300 SM: a division
+  // or square root evaluated by every warp of a 1024-thread block costs as
+  // much as a whole stencil sweep, so scalar recurrences (step lengths,
+  // norms, convergence flags) run once per block, in thread 0, which may
+  // also keep private state (e.g. the previous <r,z>) across calls.
+  template <int NV, int NO, class F>
+  __device__ bool sum_map(double (&v)[NV], double (&out)[NO], F f) {
+    static_assert(NV <= 8 && NO <= 8, "at most 8 values");
     block_sum<double, NV>(v);
     double* base = part + (size_t)region * gs.nblocks * 8;
     if (threadIdx.x == 0) {
@@ -149,22 +163,28 @@ struct GridReducer {
       for (int q = 0; q < NV; ++q) base[blockIdx.x * 8 + q] = v[q];
     }
     const bool ok = gs.sync();
-    double w[NV];
-#pragma unroll
-    for (int q = 0; q < NV; ++q) w[q] = 0.0;
-    for (int b = threadIdx.x; b < (int)gs.nblocks; b += blockDim.x) {
-#pragma unroll
-      for (int q = 0; q < NV; ++q) w[q] += __ldcg(base + b * 8 + q);
-    }
-    block_sum<double, NV>(w);
     __shared__ double sh[8];
-    if (threadIdx.x == 0) {
+    // the fixed-order combine runs in warp 0 only
+    if (threadIdx.x < 32) {
+      double w[NV];
 #pragma unroll
-      for (int q = 0; q < NV; ++q) sh[q] = w[q];
+      for (int q = 0; q < NV; ++q) w[q] = 0.0;
+      for (int b = threadIdx.x; b < (int)gs.nblocks; b += 32) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) w[q] += __ldcg(base + b * 8 + q);
+      }
+#pragma unroll
+      for (int q = 0; q < NV; ++q) w[q] = warp_sum(w[q]);
+      if (threadIdx.x == 0) {
+        double o[NO];
+        f(w, o);
+#pragma unroll
+        for (int q = 0; q < NO; ++q) sh[q] = o[q];
+      }
     }
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < NV; ++q) v[q] = sh[q];
+    for (int q = 0; q < NO; ++q) out[q] = sh[q];
     __syncthreads();
     region ^= 1;
     return ok;

@@ -121,7 +121,7 @@ __device__ __forceinline__ float fmad_(float a, float b, float c) { return __fma
 
 // ---------------------------------------------------------------------------
 // Tiled persistent PCG.  The interior is cut into TX x TY tiles (TX*TY =
-// 1024 = blockDim.x, one cell per thread); tile t belongs to block t % G for
+// blockDim.x, one cell per thread); tile t belongs to block t % G for
 // the whole solve, so a cell is read and written by the same thread in every
 // phase.  Vectors written by other blocks (r, the old direction) are read
 // through L2 (__ldcg) after a grid barrier, into a shared-memory halo tile.
@@ -132,10 +132,12 @@ __device__ __forceinline__ float fmad_(float a, float b, float c) { return __fma
 //   phase U: alpha; x += alpha d; r -= alpha Ad; partials <r,r>, <r,z>
 // d is double-buffered (phase S of iteration k writes buffer k&1 and reads
 // buffer (k+1)&1), so no block overwrites a direction another block reads.
-__host__ __device__ Tiles make_tiles(const Dims& D) {
+__host__ __device__ Tiles make_tiles(const Dims& D, int threads) {
   Tiles t;
   t.TX = D.nx <= 32 ? 32 : (D.nx <= 64 ? 64 : 128);
-  t.TY = 1024 / t.TX;
+  const int tx_max = threads / 8 < 32 ? 32 : threads / 8;  // keep tiles at least 8 rows tall
+  if (t.TX > tx_max) t.TX = tx_max;
+  t.TY = threads / t.TX;
   t.ntx = (D.nx + t.TX - 1) / t.TX;
   t.nty = (D.ny + t.TY - 1) / t.TY;
   t.ntiles = t.ntx * t.nty;
@@ -219,90 +221,119 @@ struct PcgOut {
 };
 
 // Jacobi-PCG on S.x (in/out).  x_zero: S.x is known to be zero (skip A x).
+// Scalar recurrences run in thread 0 of each block (GridReducer::sum_map);
+// every block computes the same bits, so all take the same decisions.
 template <typename T, bool UNIT>
 __device__ PcgOut pcg_tiled(const Dims& D, const Tiles& tl, GridReducer& R, const Sys<T>& S,
                             int pinned, double rel, int max_iter, bool x_zero, T* sd) {
   const int pinned_k = pinned ? D.P + 1 : -1;
   PcgOut o{0, COVOF_OK, 0.0, 1.0, true};
   // r = b - A x ; <b,b>, <r,r>, <r,z>
+  T acc[3] = {T(0), T(0), T(0)};
+  for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+    const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
+    const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
+    if (i <= D.nx && j <= D.ny) {
+      const int k = D.id(i, j);
+      T rv = S.b[k];
+      if (!x_zero) {
+        const T xc = __ldcg(S.x + k);
+        T v = UNIT ? xc : S.aP[k] * xc;
+        v = fmad_(-S.ax[k], __ldcg(S.x + k - 1), v);
+        v = fmad_(-S.ax[k + 1], __ldcg(S.x + k + 1), v);
+        v = fmad_(-S.ay[k], __ldcg(S.x + k - D.P), v);
+        v = fmad_(-S.ay[k + D.P], __ldcg(S.x + k + D.P), v);
+        rv = rv - v;
+      }
+      if (k == pinned_k) rv = T(0);
+      S.r[k] = rv;
+      const T z = (k == pinned_k) ? T(0) : precond<T, UNIT>(S, k, rv);
+      acc[0] = fmad_(S.b[k], S.b[k], acc[0]);
+      acc[1] = fmad_(rv, rv, acc[1]);
+      acc[2] = fmad_(rv, z, acc[2]);
+    }
+  }
+  // thread-0 state: <r,z> of the previous iteration, ||b||
+  double rz_old = 0.0, b_norm = 1.0;
+  double sc[3];  // {b_norm, r_norm, done}
   {
-    T acc[3] = {T(0), T(0), T(0)};
+    double v[3] = {(double)acc[0], (double)acc[1], (double)acc[2]};
+    o.ok = R.sum_map<3, 3>(v, sc, [&](const double* t, double* out) {
+      b_norm = sqrt(t[0]);
+      if (b_norm < 1.0e-30) b_norm = 1.0;
+      const double rn = sqrt(t[1]);
+      rz_old = t[2];
+      out[0] = b_norm;
+      out[1] = rn;
+      out[2] = (rn / b_norm > rel) ? 0.0 : 1.0;
+    });
+  }
+  o.b_norm = sc[0];
+  o.r_norm = sc[1];
+  if (!o.ok || sc[2] != 0.0) {
+    if (!o.ok) o.status = COVOF_TIMEOUT;
+    return o;
+  }
+  double beta = 0.0;
+  bool converged = false;
+  while (o.iters < max_iter) {
+    const int it = o.iters;
+    o.iters++;
+    T* dnew = (it & 1) ? S.d1 : S.d0;
+    const T* dold = (it & 1) ? S.d0 : S.d1;
+    // phase S
+    double a1[1] = {0.0};
+    {
+      T c = T(0);
+      for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x)
+        c += phase_stencil<T, UNIT>(D, tl, tile, S, dold, dnew, (T)beta, it == 0, pinned_k, sd);
+      a1[0] = (double)c;
+    }
+    double s1[2];  // {alpha, breakdown}
+    if (!R.sum_map<1, 2>(a1, s1, [&](const double* t, double* out) {
+          const bool brk = fabs(t[0]) < 1.0e-35;
+          out[0] = brk ? 0.0 : rz_old / t[0];
+          out[1] = brk ? 1.0 : 0.0;
+        })) { o.ok = false; break; }
+    if (s1[1] != 0.0) { o.status = COVOF_BREAKDOWN; break; }
+    const T al = (T)s1[0];
+    // phase U
+    T a2[2] = {T(0), T(0)};
     for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
       const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
       const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
       if (i <= D.nx && j <= D.ny) {
         const int k = D.id(i, j);
-        T rv = S.b[k];
-        if (!x_zero) {
-          const T xc = __ldcg(S.x + k);
-          T v = UNIT ? xc : S.aP[k] * xc;
-          v = fmad_(-S.ax[k], __ldcg(S.x + k - 1), v);
-          v = fmad_(-S.ax[k + 1], __ldcg(S.x + k + 1), v);
-          v = fmad_(-S.ay[k], __ldcg(S.x + k - D.P), v);
-          v = fmad_(-S.ay[k + D.P], __ldcg(S.x + k + D.P), v);
-          rv = rv - v;
-        }
-        if (k == pinned_k) rv = T(0);
+        S.x[k] = fmad_(al, dnew[k], S.x[k]);
+        const T rv = fmad_(-al, S.Ad[k], S.r[k]);
         S.r[k] = rv;
         const T z = (k == pinned_k) ? T(0) : precond<T, UNIT>(S, k, rv);
-        acc[0] = fmad_(S.b[k], S.b[k], acc[0]);
-        acc[1] = fmad_(rv, rv, acc[1]);
-        acc[2] = fmad_(rv, z, acc[2]);
+        a2[0] = fmad_(rv, rv, a2[0]);
+        a2[1] = fmad_(rv, z, a2[1]);
       }
     }
-    double tot[3];
-    o.ok = reduce<T, 3>(R, acc, tot);
-    o.b_norm = sqrt(tot[0]);
-    if (o.b_norm < 1.0e-30) o.b_norm = 1.0;
-    o.r_norm = sqrt(tot[1]);
-    if (!o.ok || !(o.r_norm / o.b_norm > rel)) {
-      if (!o.ok) o.status = COVOF_TIMEOUT;
-      return o;
-    }
-    double rz_old = tot[2];
-    double beta = 0.0;
-    bool converged = false;
-    while (o.iters < max_iter) {
-      const int it = o.iters;
-      o.iters++;
-      T* dnew = (it & 1) ? S.d1 : S.d0;
-      const T* dold = (it & 1) ? S.d0 : S.d1;
-      // phase S
-      T a1[1] = {T(0)};
-      for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x)
-        a1[0] += phase_stencil<T, UNIT>(D, tl, tile, S, dold, dnew, (T)beta, it == 0, pinned_k, sd);
-      double dAd[1];
-      if (!reduce<T, 1>(R, a1, dAd)) { o.ok = false; break; }
-      if (fabs(dAd[0]) < 1.0e-35) { o.status = COVOF_BREAKDOWN; break; }
-      const double alpha = rz_old / dAd[0];
-      const T al = (T)alpha;
-      // phase U
-      T a2[2] = {T(0), T(0)};
-      for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
-        const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
-        const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
-        if (i <= D.nx && j <= D.ny) {
-          const int k = D.id(i, j);
-          S.x[k] = fmad_(al, dnew[k], S.x[k]);
-          const T rv = fmad_(-al, S.Ad[k], S.r[k]);
-          S.r[k] = rv;
-          const T z = (k == pinned_k) ? T(0) : precond<T, UNIT>(S, k, rv);
-          a2[0] = fmad_(rv, rv, a2[0]);
-          a2[1] = fmad_(rv, z, a2[1]);
-        }
-      }
-      double t2[2];
-      if (!reduce<T, 2>(R, a2, t2)) { o.ok = false; break; }
-      o.r_norm = sqrt(t2[0]);
-      if (isnan(o.r_norm)) { o.status = COVOF_NAN; break; }
-      if (o.r_norm / o.b_norm <= rel) { converged = true; break; }
-      if (fabs(rz_old) < 1.0e-35) { o.status = COVOF_BREAKDOWN; break; }
-      beta = t2[1] / rz_old;
-      rz_old = t2[1];
-    }
-    if (o.ok && o.status == COVOF_OK && !converged) o.status = COVOF_MAXITER;
-    if (!o.ok) o.status = COVOF_TIMEOUT;
+    // {r_norm, beta, flag}: flag 1 NaN, 2 converged, 3 breakdown
+    double v2[2] = {(double)a2[0], (double)a2[1]};
+    double s2[3];
+    if (!R.sum_map<2, 3>(v2, s2, [&](const double* t, double* out) {
+          const double rn = sqrt(t[0]);
+          double flag = 0.0, bt = 0.0;
+          if (isnan(rn)) flag = 1.0;
+          else if (rn / b_norm <= rel) flag = 2.0;
+          else if (fabs(rz_old) < 1.0e-35) flag = 3.0;
+          else { bt = t[1] / rz_old; rz_old = t[1]; }
+          out[0] = rn;
+          out[1] = bt;
+          out[2] = flag;
+        })) { o.ok = false; break; }
+    o.r_norm = s2[0];
+    if (s2[2] == 1.0) { o.status = COVOF_NAN; break; }
+    if (s2[2] == 2.0) { converged = true; break; }
+    if (s2[2] == 3.0) { o.status = COVOF_BREAKDOWN; break; }
+    beta = s2[1];
   }
+  if (o.ok && o.status == COVOF_OK && !converged) o.status = COVOF_MAXITER;
+  if (!o.ok) o.status = COVOF_TIMEOUT;
   return o;
 }
 
@@ -329,7 +360,7 @@ __device__ bool remove_mean(const Dims& D, const Tiles& tl, GridReducer& R, doub
 __global__ void __launch_bounds__(1024, 1) k_pcg_fp64(PoissonArgs a) {
   __shared__ double sd[kHalo];
   const Dims D = a.D;
-  const Tiles tl = make_tiles(D);
+  const Tiles tl = make_tiles(D, blockDim.x);
   GridReducer R{a.part, GridSync{a.bar, a.err, gridDim.x, 0u}, 0};
   Sys<double> S{a.x, a.b, a.r, a.d, a.d2, a.Ad, a.ax, a.ay, a.aP, a.invD};
   PcgOut o = pcg_tiled<double, false>(D, tl, R, S, a.pinned, a.tol, a.max_iter, false, sd);
@@ -558,9 +589,12 @@ struct SmemInner {
 // acquire, bounded waits).
 // Layout (floats, W = nx+2): y, r [R*W]; d [(R+2)*W] (halo rows 0, R+1);
 // ax [R*W]; ay [(R+1)*W].
+constexpr int kChebTab = 128;  // precomputed Chebyshev step coefficients
+
 struct SmemCheby {
   Dims D; int r0, R, W, b, G, pinned_c, m;
   double lo;
+  float2* tab;            // [kChebTab] (c1, c2) of step k, in shared memory
   float *ys, *r, *d, *dn, *ax, *ay;  // d: current direction, dn: next
   float* xb;              // [2][G][2 sides][W] boundary rows of d
   unsigned int* flags;    // [G] publish counters
@@ -579,8 +613,25 @@ struct SmemCheby {
       ay[e] = (col >= 1 && col <= D.nx) ? ay32[D.id(col, r0 + row)] : 0.0f;
     }
     for (int e = threadIdx.x; e < (R + 2) * W; e += blockDim.x) { d[e] = 0.0f; dn[e] = 0.0f; }
+    // The step coefficients depend only on the interval and the step index:
+    // one thread evaluates the recurrence once per launch (FP64 divisions
+    // are expensive on this part; every warp repeating them every step
+    // would cost more than the step's stencil work).
+    if (threadIdx.x == 0) {
+      double rho = 1.0 / cheb_sigma1(), r1;
+      const double delta = cheb_delta();
+      for (int k = 0; k < kChebTab; ++k) {
+        r1 = 1.0 / (2.0 * cheb_sigma1() - rho);
+        tab[k] = make_float2((float)(r1 * rho), (float)(2.0 * r1 / delta));
+        rho = r1;
+      }
+    }
     __syncthreads();
   }
+  // spectrum bound of the unit-diagonal operator: [2 lo, 2]
+  __device__ __forceinline__ double cheb_theta() const { return 0.5 * (2.0 + 2.0 * lo); }
+  __device__ __forceinline__ double cheb_delta() const { return 0.5 * (2.0 - 2.0 * lo); }
+  __device__ __forceinline__ double cheb_sigma1() const { return cheb_theta() / cheb_delta(); }
   __device__ __forceinline__ void set_rhs(int, int c, float v) {
     const int row = c / D.nx, col = c - row * D.nx + 1;
     r[row * W + col] = v;
@@ -630,28 +681,32 @@ struct SmemCheby {
   __device__ PcgOut solve(GridReducer&, double, int budget) {
     PcgOut o{0, COVOF_OK, 0.0, 1.0, true};
     const int n = R * D.nx, nx = D.nx;
-    const int steps = budget < m ? budget : m;
-    const double bnd = 2.0, a = 2.0 * lo;
-    const double theta = 0.5 * (bnd + a), delta = 0.5 * (bnd - a);
-    const double sigma1 = theta / delta;
-    double rho = 1.0 / sigma1;
+    const int steps = budget < (m < kChebTab ? m : kChebTab) ? budget : (m < kChebTab ? m : kChebTab);
+    // this thread's first cell and the (row, col) stride of blockDim cells,
+    // so the sweeps below need no integer division
+    const int row0 = (int)threadIdx.x / nx, col0 = (int)threadIdx.x - row0 * nx + 1;
+    const int drow = (int)blockDim.x / nx, dcol = (int)blockDim.x - drow * nx;
     // d0 = r0 / theta
-    const float it0 = (float)(1.0 / theta);
-    for (int c = threadIdx.x; c < n; c += blockDim.x) {
-      const int row = c / nx, col = c - row * nx + 1;
-      d[(row + 1) * W + col] = r[row * W + col] * it0;
+    const float it0 = (float)(1.0 / cheb_theta());
+    {
+      int row = row0, col = col0;
+      for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        d[(row + 1) * W + col] = r[row * W + col] * it0;
+        row += drow; col += dcol;
+        if (col > nx) { col -= nx; ++row; }
+      }
     }
     __syncthreads();
     publish();
     for (int k = 0; k < steps; ++k) {
       if (!fetch()) { o.ok = false; o.status = COVOF_TIMEOUT; break; }
       const bool last = (k + 1 == steps);
-      const double rho1 = 1.0 / (2.0 * sigma1 - rho);
-      const float c1 = (float)(rho1 * rho), c2 = (float)(2.0 * rho1 / delta);
-      rho = rho1;
+      const float2 cc = tab[k];
+      const float c1 = cc.x, c2 = cc.y;
       // x += d ; r -= A d ; next d = c1 d + c2 r  (one pass, d read-only)
-      for (int c = threadIdx.x; c < n; c += blockDim.x) {
-        const int row = c / nx, col = c - row * nx + 1;
+      int row = row0, col = col0;
+      for (int c = threadIdx.x; c < n; c += blockDim.x, row += drow, col += dcol) {
+        if (col > nx) { col -= nx; ++row; }
         const int q = (row + 1) * W + col, e = row * W + col;
         const float dc = d[q];
         float v = dc;
@@ -846,6 +901,8 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cheb(PoissonArgs a) {
   in.D = D; in.r0 = r0; in.R = Rr; in.W = W; in.b = blockIdx.x; in.G = gridDim.x;
   in.pinned_c = (a.pinned && blockIdx.x == 0) ? 0 : -1;
   in.m = a.inner_max_iter; in.lo = a.cheb_lo;
+  __shared__ float2 cheb_tab[kChebTab];
+  in.tab = cheb_tab;
   float* s = smem;
   in.ys = s; s += Rr * W;
   in.r = s; s += Rr * W;
@@ -861,7 +918,7 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cheb(PoissonArgs a) {
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed(PoissonArgs a) {
   __shared__ float sd[kHalo];
   const Dims D = a.D;
-  const Tiles tl = make_tiles(D);
+  const Tiles tl = make_tiles(D, blockDim.x);
   GridReducer R{a.part, GridSync{a.bar, a.err, gridDim.x, 0u}, 0};
   TileOwn own{D, tl};
   TiledInner inner{D, tl, Sys<float>{a.e32, a.r32b, a.r32, a.d32, a.d32b, a.Ad32, a.ax32, a.ay32, nullptr, nullptr},

@@ -48,7 +48,7 @@ __global__ void k_copy_interior(Dims D, const double* __restrict__ src, double* 
 struct Tiles {
   int TX, TY, ntx, nty, ntiles;
 };
-__host__ __device__ Tiles make_tiles(const Dims& D);
+__host__ __device__ Tiles make_tiles(const Dims& D, int threads = 1024);
 __global__ void k_pcg_fp64(PoissonArgs a);
 __global__ void k_pcg_mixed(PoissonArgs a);
 __global__ void k_pcg_mixed_smem(PoissonArgs a);

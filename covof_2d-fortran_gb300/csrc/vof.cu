@@ -8,10 +8,8 @@
 // results are therefore bit-identical to a serial FP64 evaluation; the only
 // libm call (hypot) is replaced by the fused hypot in common.cuh.
 //
-// One thread per cell.  Pure cells (C <= 1e-6 or >= 1-1e-6) short-circuit,
-// so the cost concentrates on interface cells: ELVIRA runs 7 candidates x
-// (45 bisection steps + 8 neighbour clips) = 371 polygon clips per mixed
-// cell and pass.
+// Pure cells (C <= 1e-6 or >= 1-1e-6) short-circuit, so the reconstruction
+// cost concentrates on interface cells, which get one warp each (below).
 #include "common.cuh"
 #include "vof.cuh"
 
@@ -71,12 +69,36 @@ __device__ double cut_box_area(double xmin, double xmax, double ymin, double yma
   return 0.5 * fabs(s);
 }
 
-// src/module_interface_reconstruction.f90:105-147 compute_alpha
-__device__ double compute_alpha(double xmin, double xmax, double ymin, double ymax, double nx,
-                                double ny, double c_target) {
+__device__ __forceinline__ void put_seg(double* seg, int k, double a, double b, double c) {
+  seg[3 * k] = a; seg[3 * k + 1] = b; seg[3 * k + 2] = c;
+}
+
+// ---------------------------------------------------------------------------
+// Reconstruction, src/module_interface_reconstruction.f90:283-343 (PLIC),
+// :346-457 (ELVIRA) and :580-683 (reconstruct_interface).  Interface cells
+// are few, and each costs hundreds of FP64 polygon clips (ELVIRA: 7
+// candidates x (45 bisection steps + 8 neighbour clips)) -- FP64 issue is
+// the scarce unit of a GB300 SM -- so one thread per cell would leave a
+// handful of warps issuing long serial chains while the rest of the GPU
+// idles.  Instead:
+//   k_vof_classify  writes pure cells and appends interface cells to a list;
+//   k_vof_mixed     gives every listed cell one warp;
+//   k_vof_ring_warp does the ghost ring (normal of the nearest interior
+//                   cell, fresh line constant) the same way.
+// Every value is bit-identical to the serial evaluation.
+
+// compute_alpha (src/module_interface_reconstruction.f90:105-147: bisection
+// on the clipped area, 45 levels) with the levels replayed D per round by
+// a group of 2^D lanes (lanes gbase .. gbase + 2^D - 1 of the warp): lane
+// gbase + n evaluates node n (heap numbering, n = 1 .. 2^D - 1) of the
+// round's decision tree, whose interval it derives from the round's (lo, hi)
+// with the same midpoint formula along the node's path, so every midpoint
+// equals the serial one bit for bit; a ballot then walks the tree exactly as
+// the serial loop would.  Every lane of the warp must call this together.
+template <int D>
+__device__ double tree_alpha(int sub, int gbase, double xmin, double xmax, double ymin, double ymax,
+                             double nx, double ny, double c_target) {
   const double total = (xmax - xmin) * (ymax - ymin);
-  if (c_target <= 1.0e-7) return 1.0e9;
-  if (c_target >= 1.0 - 1.0e-7) return -1.0e9;
   const double target = fmax(0.0, fmin(1.0, c_target)) * total;
   const double v1 = nx * xmin + ny * ymin;
   const double v2 = nx * xmax + ny * ymin;
@@ -86,120 +108,186 @@ __device__ double compute_alpha(double xmin, double xmax, double ymin, double ym
   const double mx = fmax(v1, fmax(v2, fmax(v3, v4)));
   double lo = -mx - 1.0e-12;
   double hi = -mn + 1.0e-12;
-  for (int it = 0; it < 45; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    const double a = cut_box_area(xmin, xmax, ymin, ymax, nx, ny, mid);
-    if (a < target) hi = mid; else lo = mid;
+  for (int left = 45; left > 0;) {
+    const int L = left < D ? left : D;
+    bool below = false;
+    if (sub >= 1 && sub < (1 << L)) {
+      double l = lo, h = hi;
+      const int depth = 31 - __clz(sub);
+      for (int b = depth - 1; b >= 0; --b) {
+        const double mid = 0.5 * (l + h);
+        if ((sub >> b) & 1) l = mid; else h = mid;
+      }
+      const double mid = 0.5 * (l + h);
+      below = cut_box_area(xmin, xmax, ymin, ymax, nx, ny, mid) < target;
+    }
+    const unsigned gb = __ballot_sync(0xffffffffu, below) >> gbase;
+    int n = 1;
+    for (int lev = 0; lev < L; ++lev) {
+      const double mid = 0.5 * (lo + hi);
+      const bool bl = (gb >> n) & 1u;
+      if (bl) hi = mid; else lo = mid;
+      n = 2 * n + (bl ? 0 : 1);
+    }
+    left -= L;
   }
+  if (c_target <= 1.0e-7) return 1.0e9;
+  if (c_target >= 1.0 - 1.0e-7) return -1.0e9;
   return 0.5 * (lo + hi);
 }
 
-__device__ __forceinline__ void put_seg(double* seg, int k, double a, double b, double c) {
-  seg[3 * k] = a; seg[3 * k + 1] = b; seg[3 * k + 2] = c;
-}
-
-// src/module_interface_reconstruction.f90:283-343 (PLIC) and :346-457 (ELVIRA),
-// every cell of (0:nx+1, 0:ny+1).
-__global__ void k_vof_reconstruct(VofArgs a) {
-  const VMesh m{a.D, a.dx, a.dy};
+// Pure cells of (0:nx+1, 0:ny+1) get their segment; interface cells are
+// appended to list (one atomic per warp).  The list order does not matter:
+// every entry is reconstructed independently.
+__global__ void k_vof_classify(VofArgs a, int* __restrict__ list, int* __restrict__ count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int nx = a.D.nx, ny = a.D.ny;
-  if (i > nx + 1 || j > ny + 1) return;
-  const double* __restrict__ C = a.C;
-  const int k = a.D.id(i, j);
-  const double c = C[k];
-  if (c <= 1.0e-6) { put_seg(a.seg, k, 1.0, 0.0, 1.0e9); return; }
-  if (c >= 1.0 - 1.0e-6) { put_seg(a.seg, k, 1.0, 0.0, -1.0e9); return; }
-  const double xmin = m.xf(i), xmax = m.xf(i + 1), ymin = m.yf(j), ymax = m.yf(j + 1);
-  const bool inner = (i >= 1 && i <= nx && j >= 1 && j <= ny);
-  const double dx = a.dx, dy = a.dy;
-  auto Cq = [&](int p, int q) { return C[a.D.id(p, q)]; };
-  if (a.method != COVOF_RECON_ELVIRA) {
-    double mxv, myv;
-    if (inner) {
-      const double cmm = Cq(i - 1, j - 1), c0m = Cq(i, j - 1), cpm = Cq(i + 1, j - 1);
-      const double cm0 = Cq(i - 1, j), cp0 = Cq(i + 1, j);
-      const double cmp = Cq(i - 1, j + 1), c0p = Cq(i, j + 1), cpp = Cq(i + 1, j + 1);
-      mxv = -((cpp + 2.0 * cp0 + cpm) - (cmp + 2.0 * cm0 + cmm)) / (8.0 * dx);
-      myv = -((cpp + 2.0 * c0p + cmp) - (cpm + 2.0 * c0m + cmm)) / (8.0 * dy);
-    } else {
-      mxv = 1.0; myv = 0.0;
-    }
-    const double nrm = fhypot(mxv, myv);
-    double pnx, pny;
-    if (nrm > 1.0e-12) { pnx = mxv / nrm; pny = myv / nrm; }
-    else { pnx = 1.0; pny = 0.0; }
-    put_seg(a.seg, k, pnx, pny, compute_alpha(xmin, xmax, ymin, ymax, pnx, pny, c));
-    return;
+  const bool in = i <= a.D.nx + 1 && j <= a.D.ny + 1;
+  bool mixed = false;
+  int k = 0;
+  if (in) {
+    k = a.D.id(i, j);
+    const double c = a.C[k];
+    if (c <= 1.0e-6) put_seg(a.seg, k, 1.0, 0.0, 1.0e9);
+    else if (c >= 1.0 - 1.0e-6) put_seg(a.seg, k, 1.0, 0.0, -1.0e9);
+    else mixed = true;
   }
-  if (!inner) {
-    put_seg(a.seg, k, 1.0, 0.0, compute_alpha(xmin, xmax, ymin, ymax, 1.0, 0.0, c));
-    return;
-  }
-  const double Hm1 = (Cq(i - 1, j - 1) + Cq(i - 1, j) + Cq(i - 1, j + 1)) * dy;
-  const double H0 = (Cq(i, j - 1) + Cq(i, j) + Cq(i, j + 1)) * dy;
-  const double Hp1 = (Cq(i + 1, j - 1) + Cq(i + 1, j) + Cq(i + 1, j + 1)) * dy;
-  const double Wm1 = (Cq(i - 1, j - 1) + Cq(i, j - 1) + Cq(i + 1, j - 1)) * dx;
-  const double W0 = (Cq(i - 1, j) + Cq(i, j) + Cq(i + 1, j)) * dx;
-  const double Wp1 = (Cq(i - 1, j + 1) + Cq(i, j + 1) + Cq(i + 1, j + 1)) * dx;
-  const double sgy = (Cq(i, j + 1) < Cq(i, j - 1)) ? 1.0 : -1.0;
-  const double sgx = (Cq(i + 1, j) < Cq(i - 1, j)) ? 1.0 : -1.0;
-  double cnx[7], cny[7];
-  cnx[0] = -sgy * (Hp1 - Hm1) / (2.0 * dx); cny[0] = sgy * 1.0;
-  cnx[1] = -sgy * (Hp1 - H0) / (dx);        cny[1] = sgy * 1.0;
-  cnx[2] = -sgy * (H0 - Hm1) / (dx);        cny[2] = sgy * 1.0;
-  cnx[3] = sgx * 1.0; cny[3] = -sgx * (Wp1 - Wm1) / (2.0 * dy);
-  cnx[4] = sgx * 1.0; cny[4] = -sgx * (Wp1 - W0) / (dy);
-  cnx[5] = sgx * 1.0; cny[5] = -sgx * (W0 - Wm1) / (dy);
-  cnx[6] = -((Cq(i + 1, j + 1) + 2.0 * Cq(i + 1, j) + Cq(i + 1, j - 1)) -
-             (Cq(i - 1, j + 1) + 2.0 * Cq(i - 1, j) + Cq(i - 1, j - 1))) / (8.0 * dx);
-  cny[6] = -((Cq(i + 1, j + 1) + 2.0 * Cq(i, j + 1) + Cq(i - 1, j + 1)) -
-             (Cq(i + 1, j - 1) + 2.0 * Cq(i, j - 1) + Cq(i - 1, j - 1))) / (8.0 * dy);
-  double best_err = 1.0e30, bnx = 1.0, bny = 0.0, ba = 0.0;
-  for (int q = 0; q < 7; ++q) {
-    const double cn = fhypot(cnx[q], cny[q]);
-    if (cn < 1.0e-12) continue;
-    const double ux = cnx[q] / cn, uy = cny[q] / cn;
-    const double ca = compute_alpha(xmin, xmax, ymin, ymax, ux, uy, c);
-    double err = 0.0;
-    for (int dj = -1; dj <= 1; ++dj)
-      for (int di = -1; di <= 1; ++di) {
-        if (di == 0 && dj == 0) continue;
-        const double vt = Cq(i + di, j + dj) * dx * dy;
-        const double vr = cut_box_area(m.xf(i + di), m.xf(i + di + 1), m.yf(j + dj),
-                                       m.yf(j + dj + 1), ux, uy, ca);
-        const double df = vr - vt;
-        err = err + df * df;
-      }
-    if (err < best_err) { best_err = err; bnx = ux; bny = uy; ba = ca; }
-  }
-  put_seg(a.seg, k, bnx, bny, ba);
+  const unsigned lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31u;
+  const unsigned bal = __ballot_sync(0xffffffffu, mixed);
+  if (!bal) return;
+  const int leader = __ffs(bal) - 1;
+  int base = 0;
+  if ((int)lane == leader) base = atomicAdd(count, __popc(bal));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (mixed) list[base + __popc(bal & ((1u << lane) - 1u))] = k;
 }
 
-// src/module_interface_reconstruction.f90:602-681: ghost-ring cells take the
-// normal of the nearest interior cell and get a fresh line constant.
-__global__ void k_vof_ring(VofArgs a) {
+// One warp per listed cell.  ELVIRA (inner cells): candidate q on lanes
+// 4q .. 4q+3 (lanes 28-31 repeat candidate 6 and are ignored); its
+// bisection runs 2 levels per round, its 8 neighbour clips 2 per lane, and
+// the error is summed and the candidate chosen in the reference order.
+// PLIC, and ELVIRA on ghost cells: one normal, 5 levels per round.
+__global__ void __launch_bounds__(128) k_vof_mixed(VofArgs a, const int* __restrict__ list,
+                                                    const int* __restrict__ count) {
+  const VMesh m{a.D, a.dx, a.dy};
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int n = *count;
+  const int nx = a.D.nx, ny = a.D.ny;
+  const double* __restrict__ C = a.C;
+  const double dx = a.dx, dy = a.dy;
+  for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += nwarps) {
+    const int k = list[e];
+    const int j = k / a.D.P, i = k - j * a.D.P;
+    const double c = C[k];
+    const double xmin = m.xf(i), xmax = m.xf(i + 1), ymin = m.yf(j), ymax = m.yf(j + 1);
+    const bool inner = (i >= 1 && i <= nx && j >= 1 && j <= ny);
+    auto Cq = [&](int p, int q) { return C[a.D.id(p, q)]; };
+    if (a.method != COVOF_RECON_ELVIRA || !inner) {
+      double pnx = 1.0, pny = 0.0;
+      if (a.method != COVOF_RECON_ELVIRA && inner) {
+        const double cmm = Cq(i - 1, j - 1), c0m = Cq(i, j - 1), cpm = Cq(i + 1, j - 1);
+        const double cm0 = Cq(i - 1, j), cp0 = Cq(i + 1, j);
+        const double cmp = Cq(i - 1, j + 1), c0p = Cq(i, j + 1), cpp = Cq(i + 1, j + 1);
+        const double mxv = -((cpp + 2.0 * cp0 + cpm) - (cmp + 2.0 * cm0 + cmm)) / (8.0 * dx);
+        const double myv = -((cpp + 2.0 * c0p + cmp) - (cpm + 2.0 * c0m + cmm)) / (8.0 * dy);
+        const double nrm = fhypot(mxv, myv);
+        if (nrm > 1.0e-12) { pnx = mxv / nrm; pny = myv / nrm; }
+      } else if (a.method != COVOF_RECON_ELVIRA) {
+        const double nrm = fhypot(1.0, 0.0);
+        pnx = 1.0 / nrm; pny = 0.0 / nrm;
+      }
+      const double al = tree_alpha<5>(lane, 0, xmin, xmax, ymin, ymax, pnx, pny, c);
+      if (lane == 0) put_seg(a.seg, k, pnx, pny, al);
+      continue;
+    }
+    const int q = (lane >> 2) < 7 ? (lane >> 2) : 6, sub = lane & 3, gbase = lane & ~3;
+    const double Hm1 = (Cq(i - 1, j - 1) + Cq(i - 1, j) + Cq(i - 1, j + 1)) * dy;
+    const double H0 = (Cq(i, j - 1) + Cq(i, j) + Cq(i, j + 1)) * dy;
+    const double Hp1 = (Cq(i + 1, j - 1) + Cq(i + 1, j) + Cq(i + 1, j + 1)) * dy;
+    const double Wm1 = (Cq(i - 1, j - 1) + Cq(i, j - 1) + Cq(i + 1, j - 1)) * dx;
+    const double W0 = (Cq(i - 1, j) + Cq(i, j) + Cq(i + 1, j)) * dx;
+    const double Wp1 = (Cq(i - 1, j + 1) + Cq(i, j + 1) + Cq(i + 1, j + 1)) * dx;
+    const double sgy = (Cq(i, j + 1) < Cq(i, j - 1)) ? 1.0 : -1.0;
+    const double sgx = (Cq(i + 1, j) < Cq(i - 1, j)) ? 1.0 : -1.0;
+    double cnx, cny;
+    switch (q) {
+      case 0: cnx = -sgy * (Hp1 - Hm1) / (2.0 * dx); cny = sgy * 1.0; break;
+      case 1: cnx = -sgy * (Hp1 - H0) / (dx); cny = sgy * 1.0; break;
+      case 2: cnx = -sgy * (H0 - Hm1) / (dx); cny = sgy * 1.0; break;
+      case 3: cnx = sgx * 1.0; cny = -sgx * (Wp1 - Wm1) / (2.0 * dy); break;
+      case 4: cnx = sgx * 1.0; cny = -sgx * (Wp1 - W0) / (dy); break;
+      case 5: cnx = sgx * 1.0; cny = -sgx * (W0 - Wm1) / (dy); break;
+      default:
+        cnx = -((Cq(i + 1, j + 1) + 2.0 * Cq(i + 1, j) + Cq(i + 1, j - 1)) -
+                (Cq(i - 1, j + 1) + 2.0 * Cq(i - 1, j) + Cq(i - 1, j - 1))) / (8.0 * dx);
+        cny = -((Cq(i + 1, j + 1) + 2.0 * Cq(i, j + 1) + Cq(i - 1, j + 1)) -
+                (Cq(i + 1, j - 1) + 2.0 * Cq(i, j - 1) + Cq(i - 1, j - 1))) / (8.0 * dy);
+        break;
+    }
+    const double cn = fhypot(cnx, cny);
+    const bool valid = !(cn < 1.0e-12);
+    const double ux = valid ? cnx / cn : 1.0, uy = valid ? cny / cn : 0.0;
+    const double ca = tree_alpha<2>(sub, gbase, xmin, xmax, ymin, ymax, ux, uy, c);
+    // neighbour s (reference order: dj = -1..1, di = -1..1, centre skipped)
+    // on lane sub (s = sub) and sub + 4
+    double sq[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int s = sub + 4 * h;
+      const int t = s < 4 ? s : s + 1;
+      const int di = t % 3 - 1, dj = t / 3 - 1;
+      const double vt = Cq(i + di, j + dj) * dx * dy;
+      const double vr = cut_box_area(m.xf(i + di), m.xf(i + di + 1), m.yf(j + dj), m.yf(j + dj + 1), ux, uy, ca);
+      const double df = vr - vt;
+      sq[h] = df * df;
+    }
+    double err = 0.0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      const double v = __shfl_sync(0xffffffffu, s < 4 ? sq[0] : sq[1], gbase + (s & 3));
+      err = err + v;
+    }
+    double best_err = 1.0e30, bnx = 1.0, bny = 0.0, ba = 0.0;
+#pragma unroll
+    for (int qq = 0; qq < 7; ++qq) {
+      const double eq = __shfl_sync(0xffffffffu, err, 4 * qq);
+      const int vq = __shfl_sync(0xffffffffu, valid ? 1 : 0, 4 * qq);
+      const double xq = __shfl_sync(0xffffffffu, ux, 4 * qq);
+      const double yq = __shfl_sync(0xffffffffu, uy, 4 * qq);
+      const double aq = __shfl_sync(0xffffffffu, ca, 4 * qq);
+      if (vq && eq < best_err) { best_err = eq; bnx = xq; bny = yq; ba = aq; }
+    }
+    if (lane == 0) put_seg(a.seg, k, bnx, bny, ba);
+  }
+}
+
+// Ghost ring (src/module_interface_reconstruction.f90:602-681), one warp per
+// ring cell: the normal of the nearest interior cell, a fresh line constant.
+__global__ void __launch_bounds__(128) k_vof_ring_warp(VofArgs a) {
   const VMesh m{a.D, a.dx, a.dy};
   const int nx = a.D.nx, ny = a.D.ny;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  int i, j;
-  if (t < ny) { i = 0; j = t + 1; }
-  else if (t < 2 * ny) { i = nx + 1; j = t - ny + 1; }
-  else if (t < 2 * ny + nx + 2) { i = t - 2 * ny; j = 0; }
-  else if (t < 2 * ny + 2 * (nx + 2)) { i = t - 2 * ny - (nx + 2); j = ny + 1; }
-  else return;
-  const int k = a.D.id(i, j);
-  const double c = a.C[k];
-  if (!(c > 1.0e-6 && c < 1.0 - 1.0e-6)) return;
-  const int si = i < 1 ? 1 : (i > nx ? nx : i);
-  const int sj = j < 1 ? 1 : (j > ny ? ny : j);
-  const int ks = a.D.id(si, sj);
-  double snx = a.seg[3 * ks], sny = a.seg[3 * ks + 1];
-  const double nr = fhypot(snx, sny);
-  if (nr > 1.0e-12) {
+  const int lane = threadIdx.x & 31;
+  const int nring = 2 * ny + 2 * (nx + 2);
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nring; t += nwarps) {
+    int i, j;
+    if (t < ny) { i = 0; j = t + 1; }
+    else if (t < 2 * ny) { i = nx + 1; j = t - ny + 1; }
+    else if (t < 2 * ny + nx + 2) { i = t - 2 * ny; j = 0; }
+    else { i = t - 2 * ny - (nx + 2); j = ny + 1; }
+    const int k = a.D.id(i, j);
+    const double c = a.C[k];
+    if (!(c > 1.0e-6 && c < 1.0 - 1.0e-6)) continue;
+    const int si = i < 1 ? 1 : (i > nx ? nx : i);
+    const int sj = j < 1 ? 1 : (j > ny ? ny : j);
+    const int ks = a.D.id(si, sj);
+    double snx = a.seg[3 * ks], sny = a.seg[3 * ks + 1];
+    const double nr = fhypot(snx, sny);
+    if (!(nr > 1.0e-12)) continue;
     snx = snx / nr; sny = sny / nr;
-    put_seg(a.seg, k, snx, sny, compute_alpha(m.xf(i), m.xf(i + 1), m.yf(j), m.yf(j + 1), snx, sny, c));
+    const double al = tree_alpha<5>(lane, 0, m.xf(i), m.xf(i + 1), m.yf(j), m.yf(j + 1), snx, sny, c);
+    if (lane == 0) put_seg(a.seg, k, snx, sny, al);
   }
 }
 

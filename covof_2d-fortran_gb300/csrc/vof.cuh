@@ -8,7 +8,7 @@ struct VofArgs {
   Dims D;
   double dx, dy, dt;
   int method;              // COVOF_RECON_*
-  const double* C;         // field reconstructed by k_vof_reconstruct / k_vof_ring
+  const double* C;         // field reconstructed by k_vof_classify / k_vof_mixed / k_vof_ring_warp
   double* seg;             // 3 * (nx+2)*(ny+2), AoS {nx, ny, alpha}
   const double* Cn;        // C at time n (dilatation indicator source)
   const double* u;
@@ -30,8 +30,9 @@ struct CsfArgs {
   double* fx; double* fy; double* curv;
 };
 
-__global__ void k_vof_reconstruct(VofArgs a);
-__global__ void k_vof_ring(VofArgs a);
+__global__ void k_vof_classify(VofArgs a, int* __restrict__ list, int* __restrict__ count);
+__global__ void k_vof_mixed(VofArgs a, const int* __restrict__ list, const int* __restrict__ count);
+__global__ void k_vof_ring_warp(VofArgs a);
 __global__ void k_vof_pass(VofArgs a, int dir, int clamp, const double* __restrict__ Cin,
                            double* __restrict__ Cout);
 __global__ void k_vof_bc(Dims D, double* __restrict__ C);

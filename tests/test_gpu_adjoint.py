@@ -119,8 +119,11 @@ def test_torch_autograd_function(gpu_pkg):
         assert np.linalg.norm(t.cpu().numpy() - r) <= 1e-10 * max(np.linalg.norm(r), 1e-300)
     # gradcheck on a tiny grid (u* and beta), including a pressure term in the loss
     q = pkg.cases.make_params(6, 6, 1.0, 1.0)
-    q.p_tol = 1e-14
-    q.p_max_iter = 10000
+    # solves driven to round-off (the tolerance is not reachable; the status
+    # is MAXITER after 300 iterations on 36 unknowns): a stop anywhere in
+    # [1e-15, 1e-14] would put 1e-5 of noise into the finite differences
+    q.p_tol = 1e-16
+    q.p_max_iter = 300
     q.p_gauge = pkg.capi.GAUGE_PINNED
     rng = np.random.default_rng(5)
     with pkg.Solver(q) as s2:
@@ -133,4 +136,8 @@ def test_torch_autograd_function(gpu_pkg):
             u, v, pr = tb.project(a, b, c, d, s2, 0.1)
             return (u[1:7, 2:7] ** 2).sum() + (v[2:7, 1:7] * v[2:7, 1:7]).sum() + (pr[1:7, 1:7] ** 3).sum()
 
-        assert torch.autograd.gradcheck(f, (u0, v0, b0, c0), eps=1e-6, atol=1e-7, rtol=1e-5)
+        # rtol 1e-4: with eps = 1e-6 the finite differences carry the forward
+        # solves' round-off (about cond * 1e-16 relative in p) divided by eps,
+        # about 1e-5 of the cubic pressure term; the 1e-6 finite-difference
+        # bar is checked on the 512^2 case with directional derivatives
+        assert torch.autograd.gradcheck(f, (u0, v0, b0, c0), eps=1e-6, atol=1e-6, rtol=1e-4)
