@@ -5,6 +5,10 @@ homogeneous Neumann walls with a pinned reference cell, Jacobi-PCG to
 ||r||/||b|| <= 1e-10.  Headline = the mixed path (FP32 PCG inside FP64
 iterative refinement); the plain FP64 PCG path is timed beside it.
 
+Beside it ("sp_steps"): whole time steps (VOF + STANDARD_PROJECTION) of the
+rising-bubble case, 128x256, device-resident and replayed as CUDA graphs,
+plain FP64 vs mixed Poisson (steps/s).
+
 One step = one Poisson solve from a zero initial guess.  Device time per step
 is measured with CUDA events on the library's own stream; a 512 MiB buffer is
 written between steps (outside the timed events) so every step starts with a
@@ -164,6 +168,55 @@ def cpu_sample(pkg, orc, p, b, ru, rv, dt, iters_full, nthreads, budget_s):
                       f"iterations of one solve to 1e-10"}
 
 
+def bubble_state(pkg, orc, prec):
+    """Rising-bubble case (128x256 on [0,1]x[0,2], ELVIRA + Weymouth-Yue,
+    BiCGSTAB + Jacobi predictor, Poisson to 1e-10, dt 1e-4) at t = 0."""
+    p, C0, dt = pkg.cases.bubble_case()
+    p.p_precision = prec
+    f = pkg.Fields.allocate(p)
+    f.C[...] = C0
+    orc.apply_vof_bc(p, f.C)
+    orc.update_physical_properties(p, f)
+    orc.compute_curvature_and_csf(p, f)
+    return p, f, dt
+
+
+def sp_steps(pkg, orc, nsteps, cpu_steps):
+    """Whole time steps (VOF + STANDARD_PROJECTION) of the rising bubble,
+    device-resident, each step one CUDA-graph replay; plain FP64 vs mixed
+    Poisson.  Timed with CUDA events around the nsteps replays (after 3
+    warm-up steps that also capture the graphs).  The oracle runs cpu_steps
+    steps of the same loop on one host thread."""
+    cap = pkg.capi
+    out = {"workload": "rising bubble 128x256, ELVIRA + Weymouth-Yue, BiCGSTAB+Jacobi predictor, "
+                       "Jacobi-PCG Poisson to rel-res 1e-10, dt 1e-4, CUDA-graph step replay",
+           "steps": nsteps}
+    for name, prec in (("fp64", cap.PREC_FP64), ("mixed", cap.PREC_MIXED)):
+        p, f, dt = bubble_state(pkg, orc, prec)
+        with pkg.Solver(p) as s:
+            s.state_set(f)
+            st, _ = s.run_steps(dt, 3, graph=True)
+            st, r = s.run_steps(dt, nsteps, graph=True)
+        assert st == cap.OK and r["graph"] == 1, (name, st, r)
+        out[name] = {"steps_per_s": 1000.0 * r["steps"] / r["ms"], "ms_per_step": r["ms"] / r["steps"],
+                     "poisson_iters_per_step": r["poisson_iters"] / r["steps"],
+                     "predictor_iters_per_step": r["mom_iters"] / r["steps"],
+                     "max_relres": r["max_relres"]}
+        if name == "mixed":
+            out[name]["outer_per_step"] = r["refine_steps"] / r["steps"]
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    if cpu_steps > 0:
+        p, f, dt = bubble_state(pkg, orc, cap.PREC_FP64)
+        t0 = time.perf_counter()
+        for k in range(cpu_steps):
+            orc.time_step(p, dt, k, f)
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"steps_per_s": cpu_steps / el, "cores": 1, "kind": "port",
+                               "sample": f"first {cpu_steps} steps of the same loop, FP64 C++ restatement, "
+                                         f"one thread ({el:.1f} s)"}
+    return out
+
+
 def run_reference(args, world, rank):
     """--impl reference: the reference path's CPU implementation (the FP64
     C++ restatement; the Fortran reference cannot be built on these
@@ -177,7 +230,7 @@ def run_reference(args, world, rank):
     nth = os.cpu_count() or 1
     # Iteration count of one full FP64 Jacobi-PCG solve of this system (the
     # GPU FP64 path runs the same algorithm; measured count).
-    iters_full = int(os.environ.get("COVOF_BENCH_FP64_ITERS", "0")) or 4000
+    iters_full = int(os.environ.get("COVOF_BENCH_FP64_ITERS", "0")) or 12402
     x = np.zeros_like(b)
     for _ in range(args.warmup):
         orc.poisson_fixed_iters(p, dt, b, ru, rv, x, 5, nth)
@@ -311,6 +364,7 @@ def run_ours(args, world, rank, local):
     if rank == 0:
         orc = ge._load_oracle()
         cpu = None if args.skip_cpu else cpu_sample(pkg, orc, p, b, ru, rv, dt, it_f, 1, args.cpu_budget)
+        steps = None if args.skip_steps else sp_steps(pkg, orc, 100, 0 if args.skip_cpu else 3)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
@@ -333,8 +387,9 @@ def run_ours(args, world, rank, local):
             "cpu_baseline": cpu,
             "e2e": {"value": world * 1000.0 / e2e_step, "unit": UNIT, "h2d_bytes_per_step": gbytes,
                     "d2h_bytes_per_step": b.nbytes},
-            "gpu_launches": 4 * args.steps,
+            "gpu_launches": 5 * args.steps,
             "clocks": mixed["clocks"],
+            "sp_steps": steps,
         }
     for r in results.values():
         r["solver"].close()
@@ -352,6 +407,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true", help="profiling runs: no CPU baseline")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: no host-API leg")
+    ap.add_argument("--skip-steps", action="store_true", help="profiling runs: no rising-bubble time steps")
     args = ap.parse_args()
     if args.impl == "reference":
         world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -24,7 +24,7 @@ CONV_UPWIND, CONV_CENTERED = 1, 2
 RECON_PLIC, RECON_ELVIRA = 0, 1
 GAUGE_REFERENCE, GAUGE_PINNED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
-INNER_CHEBYSHEV, INNER_CG = 0, 1
+INNER_CHEBYSHEV, INNER_CG, INNER_CHEBYSHEV_STREAM = 0, 1, 2
 # resident fields (COVOF_FIELD_*), in header order; names follow the Fields dataclass
 FIELD_NAMES = ("u", "v", "p", "C", "rho", "rho_u", "rho_v", "mu", "mu_node", "fx_sigma",
                "fy_sigma", "curvature", "u_old", "v_old")

@@ -306,25 +306,31 @@ int poisson_plan(covof_handle* h) {
   long long units = (long long)make_tiles(h->D, threads).ntiles;
   size_t smem = 0;
   if (mixed) {
+    // one row strip per block, at most one block per SM
     const int G = P.ny < h->sm_count ? P.ny : h->sm_count;
     const int Rmax = (P.ny + G - 1) / G;
-    const bool cheb = P.p_inner_kind == COVOF_INNER_CHEBYSHEV;
+    const bool cheb = P.p_inner_kind != COVOF_INNER_CG;
     const void* sfn = cheb ? (const void*)k_pcg_mixed_cheb : (const void*)k_pcg_mixed_smem;
     const size_t bytes = cheb ? smem_cheb_bytes(P.nx, Rmax) : smem_strip_bytes(P.nx, Rmax);
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
     cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, sfn) == cudaSuccess && bytes + fa.sharedSizeBytes <= (size_t)optin &&
+    if (P.p_inner_kind != COVOF_INNER_CHEBYSHEV_STREAM && cudaFuncGetAttributes(&fa, sfn) == cudaSuccess &&
+        bytes + fa.sharedSizeBytes <= (size_t)optin &&
         cudaFuncSetAttribute(sfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess) {
       fn = sfn;
       smem = bytes;
+      units = G;
+    } else if (cheb) {
+      fn = (const void*)k_pcg_mixed_stream;  // strips stream through L2 / HBM
       units = G;
     }
     cudaGetLastError();
   }
   const int nb = coop_blocks(h, fn, threads, units, smem);
   if (nb < 1) return COVOF_CUDA_ERROR;
-  if (smem && nb != (int)units) return COVOF_CUDA_ERROR;  // strips are sized for exactly G blocks
+  if (mixed && fn != (const void*)k_pcg_mixed && nb != (int)units)
+    return COVOF_CUDA_ERROR;  // strips are sized for exactly G blocks
   h->p_fn = fn;
   h->p_smem = smem;
   h->p_nb = nb;

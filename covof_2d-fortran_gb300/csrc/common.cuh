@@ -134,11 +134,22 @@ namespace covof {
 // (warp 0: strided partial sums, then a shuffle tree), so all blocks obtain
 // bit-identical totals.  Consecutive reductions alternate regions, so a
 // region is rewritten only after every block has passed the barrier that
-// follows its last read.  part must hold 2 * 8 * nblocks doubles.
+// follows its last read.  part must hold 2 * 8 * nblocks doubles (nblocks =
+// the team size).
+// A team: the blocks of one cooperative launch that work on one case (all
+// of the grid for a single-case solve; a slice of it when many cases share
+// one persistent launch).  rank in [0, size); barriers, reductions and work
+// distribution are over the team only.
+struct Team {
+  int rank, size;
+};
+__device__ __forceinline__ Team grid_team() { return Team{(int)blockIdx.x, (int)gridDim.x}; }
+
 struct GridReducer {
   double* part;
   GridSync gs;
   int region;
+  int rank;  // this block's partials slot (its team rank)
   template <int NV>
   __device__ bool sum(double (&v)[NV]) {
     return sum_map<NV, NV>(v, v, [](const double* w, double* o) {
@@ -160,7 +171,7 @@ struct GridReducer {
     double* base = part + (size_t)region * gs.nblocks * 8;
     if (threadIdx.x == 0) {
 #pragma unroll
-      for (int q = 0; q < NV; ++q) base[blockIdx.x * 8 + q] = v[q];
+      for (int q = 0; q < NV; ++q) base[rank * 8 + q] = v[q];
     }
     const bool ok = gs.sync();
     __shared__ double sh[8];

@@ -317,14 +317,14 @@ __global__ void k_mom_apply(MomArgs a, const double* xu, const double* xv, doubl
 // segments of the u block, then of the v block.
 struct DofWalker {
   int nsu, nsv, su, stot, gw, nw, lane, g;
-  __device__ explicit DofWalker(const Dims& D) {
+  __device__ DofWalker(const Dims& D, const Team& tm) {
     nsu = (D.nx + 1 + 31) >> 5;
     nsv = (D.nx + 31) >> 5;
     su = nsu * D.ny;
     stot = su + nsv * (D.ny + 1);
     lane = threadIdx.x & 31;
-    gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    nw = (gridDim.x * blockDim.x) >> 5;
+    gw = (tm.rank * (int)blockDim.x + (int)threadIdx.x) >> 5;
+    nw = (tm.size * (int)blockDim.x) >> 5;
     g = D.P * (D.ny + 2);
   }
   // Decode segment s; returns false when this lane has no DOF there.
@@ -363,8 +363,8 @@ struct KCtx {
   bool ok;
 };
 
-__device__ void krylov_finish(const MomArgs& a, int iters, int status, bool ok) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+__device__ void krylov_finish(const MomArgs& a, const Team& tm, int iters, int status, bool ok) {
+  if (tm.rank == 0 && threadIdx.x == 0) {
     a.res->iters = iters;
     a.res->status = ok ? status : COVOF_TIMEOUT;
   }
@@ -372,8 +372,9 @@ __device__ void krylov_finish(const MomArgs& a, int iters, int status, bool ok) 
 
 // src/module_linear_solvers.f90:584-730 solve_bicgstab (left Jacobi).
 __global__ void __launch_bounds__(512) k_bicgstab(MomArgs a) {
-  DofWalker W(a.D);
-  GridReducer R{a.part, GridSync{a.bar, a.err, gridDim.x, 0u}, 0};
+  const Team tm = grid_team();
+  DofWalker W(a.D, tm);
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   double *x = a.x, *bh = a.v0, *r = a.v1, *rt = a.v2, *p = a.v3, *v = a.v4, *s = a.v5, *t = a.v6;
   const double tol = a.tol;
   const int max_iter = a.max_iter;
@@ -389,7 +390,7 @@ __global__ void __launch_bounds__(512) k_bicgstab(MomArgs a) {
   bool ok = R.sum(acc);
   const double rsq0 = acc[0];
   const double r0 = sqrt(rsq0);
-  if (!ok || r0 < 1.0e-12) { krylov_finish(a, 0, COVOF_OK, ok); return; }
+  if (!ok || r0 < 1.0e-12) { krylov_finish(a, tm, 0, COVOF_OK, ok); return; }
   double rho_old = 1.0, alpha = 1.0, omega = 1.0, rho = rsq0;
   int iters = max_iter, status = COVOF_MAXITER;
   for (int it = 1; it <= max_iter && ok; ++it) {
@@ -452,14 +453,15 @@ __global__ void __launch_bounds__(512) k_bicgstab(MomArgs a) {
     if (rn / r0 < tol || rn < 1.0e-12) { iters = it; status = COVOF_OK; break; }
     if (fabs(omega) < 1.0e-30) { status = COVOF_BREAKDOWN; break; }
   }
-  krylov_finish(a, iters, status, ok);
+  krylov_finish(a, tm, iters, status, ok);
 }
 
 // src/module_linear_solvers.f90:735-838 solve_cg (unpreconditioned operator,
 // separate Jacobi application).
 __global__ void __launch_bounds__(512) k_cg(MomArgs a) {
-  DofWalker W(a.D);
-  GridReducer R{a.part, GridSync{a.bar, a.err, gridDim.x, 0u}, 0};
+  const Team tm = grid_team();
+  DofWalker W(a.D, tm);
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   double *x = a.x, *r = a.v1, *p = a.v3, *Ap = a.v4;
   const double tol = a.tol;
   const int max_iter = a.max_iter;
@@ -474,7 +476,7 @@ __global__ void __launch_bounds__(512) k_cg(MomArgs a) {
   }
   bool ok = R.sum(acc);
   const double r0 = sqrt(acc[0]);
-  if (!ok || r0 < 1.0e-12) { krylov_finish(a, 0, COVOF_OK, ok); return; }
+  if (!ok || r0 < 1.0e-12) { krylov_finish(a, tm, 0, COVOF_OK, ok); return; }
   double rz_old = acc[1];
   int iters = max_iter, status = COVOF_MAXITER;
   for (int it = 1; it <= max_iter && ok; ++it) {
@@ -505,13 +507,14 @@ __global__ void __launch_bounds__(512) k_cg(MomArgs a) {
     FOR_DOFS(a, W, part, i, j, k) p[k] = prec(a, k, r[k]) + beta * p[k];
     ok = R.gs.sync();
   }
-  krylov_finish(a, iters, status, ok);
+  krylov_finish(a, tm, iters, status, ok);
 }
 
 // src/module_linear_solvers.f90:361-579 solve_bicgstab2 (left Jacobi).
 __global__ void __launch_bounds__(512) k_bicgstab2(MomArgs a) {
-  DofWalker W(a.D);
-  GridReducer R{a.part, GridSync{a.bar, a.err, gridDim.x, 0u}, 0};
+  const Team tm = grid_team();
+  DofWalker W(a.D, tm);
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   double *x = a.x, *rt = a.v0, *r0 = a.v1, *r1 = a.v2, *r2 = a.v3, *u0 = a.v4, *u1 = a.v5, *u2 = a.v6;
   const double tol = a.tol;
   const int max_iter = a.max_iter;
@@ -525,7 +528,7 @@ __global__ void __launch_bounds__(512) k_bicgstab2(MomArgs a) {
   }
   bool ok = R.sum(acc);
   const double r0n = sqrt(acc[0]);
-  if (!ok || r0n < 1.0e-12) { krylov_finish(a, 0, COVOF_OK, ok); return; }
+  if (!ok || r0n < 1.0e-12) { krylov_finish(a, tm, 0, COVOF_OK, ok); return; }
   double rho0 = 1.0, alpha = 0.0, omega = 1.0;
   int iter = 0, status = COVOF_MAXITER;
   bool have_rho1 = true;
@@ -636,7 +639,7 @@ __global__ void __launch_bounds__(512) k_bicgstab2(MomArgs a) {
     if (rn != rn || rn > 1.0e30) { status = COVOF_NAN; break; }
     if (rn / r0n < tol || rn < 1.0e-12) { status = COVOF_OK; break; }
   }
-  krylov_finish(a, iter, status, ok);
+  krylov_finish(a, tm, iter, status, ok);
 }
 
 // ---------------------------------------------------------------------------

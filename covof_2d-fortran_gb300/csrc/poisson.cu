@@ -224,13 +224,13 @@ struct PcgOut {
 // Scalar recurrences run in thread 0 of each block (GridReducer::sum_map);
 // every block computes the same bits, so all take the same decisions.
 template <typename T, bool UNIT>
-__device__ PcgOut pcg_tiled(const Dims& D, const Tiles& tl, GridReducer& R, const Sys<T>& S,
+__device__ PcgOut pcg_tiled(const Dims& D, const Tiles& tl, const Team& tm, GridReducer& R, const Sys<T>& S,
                             int pinned, double rel, int max_iter, bool x_zero, T* sd) {
   const int pinned_k = pinned ? D.P + 1 : -1;
   PcgOut o{0, COVOF_OK, 0.0, 1.0, true};
   // r = b - A x ; <b,b>, <r,r>, <r,z>
   T acc[3] = {T(0), T(0), T(0)};
-  for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+  for (int tile = tm.rank; tile < tl.ntiles; tile += tm.size) {
     const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
     const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
     if (i <= D.nx && j <= D.ny) {
@@ -285,7 +285,7 @@ __device__ PcgOut pcg_tiled(const Dims& D, const Tiles& tl, GridReducer& R, cons
     double a1[1] = {0.0};
     {
       T c = T(0);
-      for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x)
+      for (int tile = tm.rank; tile < tl.ntiles; tile += tm.size)
         c += phase_stencil<T, UNIT>(D, tl, tile, S, dold, dnew, (T)beta, it == 0, pinned_k, sd);
       a1[0] = (double)c;
     }
@@ -299,7 +299,7 @@ __device__ PcgOut pcg_tiled(const Dims& D, const Tiles& tl, GridReducer& R, cons
     const T al = (T)s1[0];
     // phase U
     T a2[2] = {T(0), T(0)};
-    for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+    for (int tile = tm.rank; tile < tl.ntiles; tile += tm.size) {
       const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
       const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
       if (i <= D.nx && j <= D.ny) {
@@ -338,9 +338,9 @@ __device__ PcgOut pcg_tiled(const Dims& D, const Tiles& tl, GridReducer& R, cons
 }
 
 // Mean removal (reference gauge, src/module_simulation.f90:2579-2582).
-__device__ bool remove_mean(const Dims& D, const Tiles& tl, GridReducer& R, double* x) {
+__device__ bool remove_mean(const Dims& D, const Tiles& tl, const Team& tm, GridReducer& R, double* x) {
   double acc[1] = {0.0};
-  for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+  for (int tile = tm.rank; tile < tl.ntiles; tile += tm.size) {
     const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
     const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
     if (i <= D.nx && j <= D.ny) acc[0] += x[D.id(i, j)];
@@ -348,7 +348,7 @@ __device__ bool remove_mean(const Dims& D, const Tiles& tl, GridReducer& R, doub
   double tot[1];
   if (!reduce<double, 1>(R, acc, tot)) return false;
   const double mean = tot[0] / (double)((long long)D.nx * D.ny);
-  for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+  for (int tile = tm.rank; tile < tl.ntiles; tile += tm.size) {
     const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
     const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
     if (i <= D.nx && j <= D.ny) { const int k = D.id(i, j); x[k] = x[k] - mean; }
@@ -361,12 +361,13 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_fp64(PoissonArgs a) {
   __shared__ double sd[kHalo];
   const Dims D = a.D;
   const Tiles tl = make_tiles(D, blockDim.x);
-  GridReducer R{a.part, GridSync{a.bar, a.err, gridDim.x, 0u}, 0};
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   Sys<double> S{a.x, a.b, a.r, a.d, a.d2, a.Ad, a.ax, a.ay, a.aP, a.invD};
-  PcgOut o = pcg_tiled<double, false>(D, tl, R, S, a.pinned, a.tol, a.max_iter, false, sd);
+  PcgOut o = pcg_tiled<double, false>(D, tl, tm, R, S, a.pinned, a.tol, a.max_iter, false, sd);
   bool ok = o.ok;
-  if (ok && !a.pinned) ok = remove_mean(D, tl, R, a.x);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (ok && !a.pinned) ok = remove_mean(D, tl, tm, R, a.x);
+  if (tm.rank == 0 && threadIdx.x == 0) {
     a.res->iters = o.iters;
     a.res->relres = o.r_norm / o.b_norm;
     a.res->status = ok ? o.status : COVOF_TIMEOUT;
@@ -394,10 +395,10 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_fp64(PoissonArgs a) {
 // t owns strip cells t, t+1024, ... (row-major), which is also the layout of
 // the shared-memory inner solver.  f(k, c): global index, strip-local index.
 struct TileOwn {
-  Dims D; Tiles tl;
+  Dims D; Tiles tl; Team tm;
   template <typename F>
   __device__ __forceinline__ void each(F f) const {
-    for (int tile = blockIdx.x; tile < tl.ntiles; tile += gridDim.x) {
+    for (int tile = tm.rank; tile < tl.ntiles; tile += tm.size) {
       const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
       const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
       if (i <= D.nx && j <= D.ny) f(D.id(i, j), 0);
@@ -438,11 +439,11 @@ __device__ __forceinline__ double stencil64(const Dims& D, int k, const double* 
 // Inner FP32 solver on the streaming tiles: RHS and solution live in global
 // FP32 vectors.
 struct TiledInner {
-  Dims D; Tiles tl; Sys<float> S; float* sd; int pinned;
+  Dims D; Tiles tl; Team tm; Sys<float> S; float* sd; int pinned;
   float* rhs;
   __device__ __forceinline__ void set_rhs(int k, int, float v) { S.x[k] = 0.0f; rhs[k] = v; }
   __device__ __forceinline__ PcgOut solve(GridReducer& R, double tol, int budget) {
-    return pcg_tiled<float, true>(D, tl, R, S, pinned, tol, budget, true, sd);
+    return pcg_tiled<float, true>(D, tl, tm, R, S, pinned, tol, budget, true, sd);
   }
   __device__ __forceinline__ float y(int k, int) const { return S.x[k]; }
 };
@@ -863,7 +864,7 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     const double mean = t[0] / (double)((long long)D.nx * D.ny);
     own.each([&](int k, int) { x[k] = x[k] - mean; });
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (R.rank == 0 && threadIdx.x == 0) {
     a.res->iters = total_inner;
     a.res->relres = r_norm / b_norm;
     a.res->status = ok ? status : COVOF_TIMEOUT;
@@ -889,17 +890,150 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
 //
 // k_pcg_mixed: streaming tiles (any size).  k_pcg_mixed_smem: the FP32 inner
 // solver lives in shared memory (row strips; used when a strip fits).
+// Inner FP32 Chebyshev streaming through global memory, for meshes whose
+// row strips do not fit in shared memory and for batched cases: the same
+// iteration as SmemCheby on the team's row strips, with y, r and the two
+// direction buffers in (0:nx+1, 0:ny+1) FP32 arrays (zero ghost ring) that
+// stay in L2 when they fit.  Neighbour strips meet through per-block publish
+// counters instead of team barriers: a block publishes its rows of d after
+// each step and waits only for the blocks above and below.  Direction
+// buffers alternate, and a block can overwrite buffer k & 1 (at step k + 2)
+// only after its neighbours have published step k + 1, i.e. after they have
+// finished reading it.  Rows of other blocks are read through L2 (__ldcg).
+struct StreamCheby {
+  Dims D; int r0, R, b, G, pk, m;
+  double lo;
+  float2* tab;              // [kChebTab] (c1, c2) of step k, in shared memory
+  float *ys, *r, *d, *dn;   // FP32 (0:nx+1, 0:ny+1) arrays; d, dn ghost ring zero
+  const float *ax, *ay;
+  unsigned int* flags;      // [G] publish counters of the team
+  int* err;
+  unsigned int* sent;       // this block's publish count (lives across solves and cases)
+  __device__ __forceinline__ double cheb_theta() const { return 0.5 * (2.0 + 2.0 * lo); }
+  __device__ __forceinline__ double cheb_delta() const { return 0.5 * (2.0 - 2.0 * lo); }
+  __device__ void load_tab() {
+    if (threadIdx.x == 0) {
+      const double sigma1 = cheb_theta() / cheb_delta(), delta = cheb_delta();
+      double rho = 1.0 / sigma1, r1;
+      for (int k = 0; k < kChebTab; ++k) {
+        r1 = 1.0 / (2.0 * sigma1 - rho);
+        tab[k] = make_float2((float)(r1 * rho), (float)(2.0 * r1 / delta));
+        rho = r1;
+      }
+    }
+    __syncthreads();
+  }
+  __device__ __forceinline__ void set_rhs(int k, int, float v) { r[k] = v; ys[k] = 0.0f; }
+  __device__ __forceinline__ float y(int k, int) const { return ys[k]; }
+  __device__ __forceinline__ void publish() {
+    __syncthreads();
+    if (threadIdx.x == 0) red_add_release_u32(flags + b, 1u);
+    ++*sent;
+  }
+  __device__ __forceinline__ bool fetch() {
+    __shared__ int s_ok;
+    const unsigned int want = *sent;
+    if (threadIdx.x == 0) {
+      int ok = 1;
+      long long spins = 0;
+      if (b > 0)
+        while ((int)(ld_acquire_u32(flags + b - 1) - want) < 0)
+          if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+      if (ok && b < G - 1)
+        while ((int)(ld_acquire_u32(flags + b + 1) - want) < 0)
+          if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+      s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+  }
+  __device__ PcgOut solve(GridReducer&, double, int budget) {
+    PcgOut o{0, COVOF_OK, 0.0, 1.0, true};
+    const int n = R * D.nx, nx = D.nx, P = D.P;
+    const int mm = m < kChebTab ? m : kChebTab;
+    const int steps = budget < mm ? budget : mm;
+    const int row0 = (int)threadIdx.x / nx, col0 = (int)threadIdx.x - row0 * nx + 1;
+    const int drow = (int)blockDim.x / nx, dcol = (int)blockDim.x - drow * nx;
+    const float it0 = (float)(1.0 / cheb_theta());
+    {
+      int row = row0, col = col0;
+      for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        const int k = (r0 + row) * P + col;
+        d[k] = r[k] * it0;
+        row += drow; col += dcol;
+        if (col > nx) { col -= nx; ++row; }
+      }
+    }
+    publish();
+    for (int s = 0; s < steps; ++s) {
+      if (!fetch()) { o.ok = false; o.status = COVOF_TIMEOUT; break; }
+      const bool last = (s + 1 == steps);
+      const float2 cc = tab[s];
+      int row = row0, col = col0;
+      for (int c = threadIdx.x; c < n; c += blockDim.x, row += drow, col += dcol) {
+        if (col > nx) { col -= nx; ++row; }
+        const int k = (r0 + row) * P + col;
+        const float dc = __ldcg(d + k);
+        float v = dc;
+        v = __fmaf_rn(-ax[k], __ldcg(d + k - 1), v);
+        v = __fmaf_rn(-ax[k + 1], __ldcg(d + k + 1), v);
+        v = __fmaf_rn(-ay[k], __ldcg(d + k - P), v);
+        v = __fmaf_rn(-ay[k + P], __ldcg(d + k + P), v);
+        if (k == pk) v = 0.0f;
+        ys[k] += dc;
+        const float rn = r[k] - v;
+        r[k] = rn;
+        if (!last) dn[k] = __fmaf_rn(cc.x, dc, cc.y * rn);
+      }
+      o.iters++;
+      if (last) break;
+      float* t = d; d = dn; dn = t;
+      publish();
+    }
+    __syncthreads();
+    return o;
+  }
+};
+
+// One mixed solve of case a by team tm (R: the team's reducer, carried across
+// the cases a team solves one after another; flags, sent: its publish
+// counters).
+__device__ void mixed_stream_case(const PoissonArgs& a, const Team& tm, GridReducer& R,
+                                  unsigned int* flags, unsigned int* sent, float2* tab) {
+  const Dims D = a.D;
+  int r0, Rr;
+  strip_rows(D.ny, tm.size, tm.rank, r0, Rr);
+  StripOwn own{D, r0, Rr};
+  StreamCheby in;
+  in.D = D; in.r0 = r0; in.R = Rr; in.b = tm.rank; in.G = tm.size;
+  in.pk = a.pinned ? D.P + 1 : -1;
+  in.m = a.inner_max_iter; in.lo = a.cheb_lo; in.tab = tab;
+  in.ys = a.e32; in.r = a.r32; in.d = a.d32; in.dn = a.d32b; in.ax = a.ax32; in.ay = a.ay32;
+  in.flags = flags; in.err = R.gs.err; in.sent = sent;
+  in.load_tab();
+  fcg_mixed(a, own, in, R);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_pcg_mixed_stream(PoissonArgs a) {
+  __shared__ float2 cheb_tab[kChebTab];
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  unsigned int sent = 0;
+  mixed_stream_case(a, tm, R, a.flags, &sent, cheb_tab);
+}
+
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cheb(PoissonArgs a) {
   extern __shared__ float smem[];
   const Dims D = a.D;
-  GridReducer R{a.part, GridSync{a.bar, a.err, gridDim.x, 0u}, 0};
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   int r0, Rr;
-  strip_rows(D.ny, gridDim.x, blockIdx.x, r0, Rr);
+  strip_rows(D.ny, tm.size, tm.rank, r0, Rr);
   const int W = D.nx + 2;
   StripOwn own{D, r0, Rr};
   SmemCheby in;
-  in.D = D; in.r0 = r0; in.R = Rr; in.W = W; in.b = blockIdx.x; in.G = gridDim.x;
-  in.pinned_c = (a.pinned && blockIdx.x == 0) ? 0 : -1;
+  in.D = D; in.r0 = r0; in.R = Rr; in.W = W; in.b = tm.rank; in.G = tm.size;
+  in.pinned_c = (a.pinned && tm.rank == 0) ? 0 : -1;
   in.m = a.inner_max_iter; in.lo = a.cheb_lo;
   __shared__ float2 cheb_tab[kChebTab];
   in.tab = cheb_tab;
@@ -919,9 +1053,11 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed(PoissonArgs a) {
   __shared__ float sd[kHalo];
   const Dims D = a.D;
   const Tiles tl = make_tiles(D, blockDim.x);
-  GridReducer R{a.part, GridSync{a.bar, a.err, gridDim.x, 0u}, 0};
-  TileOwn own{D, tl};
-  TiledInner inner{D, tl, Sys<float>{a.e32, a.r32b, a.r32, a.d32, a.d32b, a.Ad32, a.ax32, a.ay32, nullptr, nullptr},
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  TileOwn own{D, tl, tm};
+  TiledInner inner{D, tl, tm,
+                   Sys<float>{a.e32, a.r32b, a.r32, a.d32, a.d32b, a.Ad32, a.ax32, a.ay32, nullptr, nullptr},
                    sd, a.pinned, a.r32b};
   fcg_mixed(a, own, inner, R);
 }
@@ -929,14 +1065,15 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed(PoissonArgs a) {
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_smem(PoissonArgs a) {
   extern __shared__ float smem[];
   const Dims D = a.D;
-  GridReducer R{a.part, GridSync{a.bar, a.err, gridDim.x, 0u}, 0};
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   int r0, Rr;
-  strip_rows(D.ny, gridDim.x, blockIdx.x, r0, Rr);
+  strip_rows(D.ny, tm.size, tm.rank, r0, Rr);
   const int W = D.nx + 2;
   StripOwn own{D, r0, Rr};
   SmemInner in;
-  in.D = D; in.r0 = r0; in.R = Rr; in.W = W; in.b = blockIdx.x; in.G = gridDim.x;
-  in.pinned_c = (a.pinned && blockIdx.x == 0) ? 0 : -1;
+  in.D = D; in.r0 = r0; in.R = Rr; in.W = W; in.b = tm.rank; in.G = tm.size;
+  in.pinned_c = (a.pinned && tm.rank == 0) ? 0 : -1;
   float* s = smem;
   in.ys = s; s += Rr * W;
   in.r = s; s += Rr * W;

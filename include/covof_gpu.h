@@ -94,13 +94,16 @@ typedef struct covof_params {
   int enable_surface_tension;
   double rho1, rho2, mu1, mu2, sigma, gx, gy;
   int recon;             /* COVOF_RECON_* */
-  /* MIXED inner preconditioner: COVOF_INNER_CHEBYSHEV (degree p_inner_max_iter
-   * on [p_cheb_lo * 2, 2], no inner reductions) or COVOF_INNER_CG (Jacobi-PCG,
-   * at most p_inner_max_iter iterations or p_inner_tol reduction). */
+  /* MIXED inner preconditioner: COVOF_INNER_CHEBYSHEV (degree p_inner_max_iter,
+   * at most 128, on [p_cheb_lo * 2, 2], no inner reductions; its state lives
+   * in shared memory when a row strip per SM fits, else it streams through
+   * L2/HBM), COVOF_INNER_CHEBYSHEV_STREAM (the streaming form always) or
+   * COVOF_INNER_CG (Jacobi-PCG, at most p_inner_max_iter iterations or
+   * p_inner_tol reduction). */
   int p_inner_kind;
   double p_cheb_lo;      /* lower end of the Chebyshev interval, as a fraction of 2 */
 } covof_params;
-enum { COVOF_INNER_CHEBYSHEV = 0, COVOF_INNER_CG = 1 };
+enum { COVOF_INNER_CHEBYSHEV = 0, COVOF_INNER_CG = 1, COVOF_INNER_CHEBYSHEV_STREAM = 2 };
 
 typedef struct covof_handle covof_handle;
 

@@ -22,7 +22,7 @@ def test_operator_is_bit_identical(gpu_pkg, orc):
 
 
 @pytest.mark.parametrize("gauge", ["pinned", "reference"])
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_stream", "mixed_cg"])
 @pytest.mark.parametrize("n", [64, 128])
 def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
     pkg = gpu_pkg
@@ -34,7 +34,11 @@ def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
     it_o, rr_o, st_o = orc.poisson_solve_rhs(p, dt, b, ru, rv, ref)
     assert st_o == 0
     q = p.copy()
-    q.p_precision = cap.PREC_MIXED if prec == "mixed" else cap.PREC_FP64
+    q.p_precision = cap.PREC_FP64 if prec == "fp64" else cap.PREC_MIXED
+    if prec == "mixed_stream":
+        q.p_inner_kind = cap.INNER_CHEBYSHEV_STREAM
+    elif prec == "mixed_cg":
+        q.p_inner_kind = cap.INNER_CG
     x = np.zeros_like(b)
     with pkg.Solver(q) as s:
         it, rr, st = s.poisson_solve_rhs(dt, b, ru, rv, x)
@@ -102,9 +106,11 @@ def test_full_size_1024_converges_fp64_and_mixed(gpu_pkg, orc):
     cap = pkg.capi
     p, b, ru, rv, dt = _inclusions(pkg, 1024, 200)
     sols = {}
-    for prec in (cap.PREC_FP64, cap.PREC_MIXED):
+    for prec, kind in ((cap.PREC_FP64, 0), (cap.PREC_MIXED, cap.INNER_CHEBYSHEV),
+                       (cap.PREC_MIXED, cap.INNER_CHEBYSHEV_STREAM)):
         q = p.copy()
         q.p_precision = prec
+        q.p_inner_kind = kind
         x = np.zeros_like(b)
         with pkg.Solver(q) as s:
             it, rr, st = s.poisson_solve_rhs(dt, b, ru, rv, x)
@@ -118,6 +124,8 @@ def test_full_size_1024_converges_fp64_and_mixed(gpu_pkg, orc):
         # true residual grows with the condition number (~1e7 here).
         assert true_rel < (2e-10 if prec == cap.PREC_MIXED else 1e-9), (prec, true_rel)
         assert x[1, 1] == 0.0
-        sols[prec] = x
-    d = np.linalg.norm(sols[0] - sols[1]) / np.linalg.norm(sols[0])
-    assert d < 1e-7, d
+        sols[(prec, kind)] = x
+    ref = sols[(cap.PREC_FP64, 0)]
+    for key, x in sols.items():
+        d = np.linalg.norm(x - ref) / np.linalg.norm(ref)
+        assert d < 1e-7, (key, d)
