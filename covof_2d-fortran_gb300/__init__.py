@@ -10,7 +10,7 @@ The directory name is not a Python identifier; load the package with
 """
 from . import capi, cases  # noqa: F401
 from .capi import CovofError, Params, default_params, load_library  # noqa: F401
-from .solver import Fields, Solver, new_field  # noqa: F401
+from .solver import Batch, Fields, Solver, new_field  # noqa: F401
 
-__all__ = ["capi", "cases", "CovofError", "Params", "Fields", "Solver", "default_params",
+__all__ = ["capi", "cases", "CovofError", "Params", "Batch", "Fields", "Solver", "default_params",
            "load_library", "new_field"]

@@ -126,6 +126,12 @@ _SIGS = {
     "covof_state_get": [_VP, C.c_int, _VP],
     "covof_state_field_dev": [_VP, C.c_int, C.POINTER(C.c_void_p)],
     "covof_run_steps": [_VP, C.c_double, C.c_int, C.c_int, C.POINTER(RunStats)],
+    "covof_batch_create": [C.POINTER(Params), C.c_int, C.POINTER(C.c_void_p)],
+    "covof_batch_destroy": [_VP],
+    "covof_batch_state_set": [_VP, C.c_int, C.c_int, _VP],
+    "covof_batch_state_get": [_VP, C.c_int, C.c_int, _VP],
+    "covof_batch_run_steps": [_VP, _DP, C.c_int, C.c_int, C.POINTER(RunStats), _DP],
+    "covof_batch_info": [_VP, _IP, _IP, _IP, _IP],
 }
 
 

@@ -12,6 +12,8 @@ base + k with numpy's PCG64.  Arrays use the reference layout (ny+2, nx+2).
   Gaussian RHS, homogeneous Neumann walls.
 * ``vortex_case``      -- Rider-Kothe single-vortex VOF transport
   (src/module_simulation.f90:2175-2416).
+* ``droplet_batch``    -- many independent droplet / bubble cases of uneven
+  sizes (64..512 cells per direction) for the batch engine.
 """
 from __future__ import annotations
 
@@ -190,3 +192,57 @@ def random_velocity(p: Params, scale: float, seed: int):
     v[1, 1:p.nx + 1] = 0.0
     v[p.ny + 1, 1:p.nx + 1] = 0.0
     return u, v
+
+
+def droplet_batch(n_cases: int = 256, seed: int = SEED + 4, sizes=(64, 128, 256, 512), nsub: int = 4,
+                  mixed: bool = True):
+    """Independent droplet / bubble cases: nx, ny drawn from sizes, square
+    cells of side 1/nx on [0, 1] x [0, ny/nx]; 1-3 circles with radii 0.1-0.3
+    of the short side (fluid 1 inside for a droplet, outside for a bubble);
+    density ratio log-uniform in [10, 1000] (rho1 = 1000), viscosity ratio
+    log-uniform in [1, 100] (mu1 = 1e-2), sigma uniform in [0.01, 25],
+    g = (0, -0.98); ELVIRA + Weymouth-Yue, BiCGSTAB + Jacobi predictor and the
+    Poisson to 1e-10.  dt = min(1e-4, half the capillary limit
+    sqrt((rho1 + rho2) h^3 / (4 pi sigma))).  Returns [(params, C, dt)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_cases):
+        nx, ny = (int(v) for v in rng.choice(sizes, 2))
+        lx, ly = 1.0, ny / nx
+        p = make_params(nx, ny, lx, ly)
+        short = min(lx, ly)
+        k = int(rng.integers(1, 4))
+        circles = []
+        for _ in range(k):
+            r = rng.uniform(0.1, 0.3) * short
+            cx = rng.uniform(r, lx - r)
+            cy = rng.uniform(r, ly - r)
+            circles.append((cx, cy, r))
+        droplet = bool(rng.integers(0, 2))
+
+        def inside(X, Y):
+            m = np.zeros(np.broadcast(X, Y).shape, dtype=bool)
+            for cx, cy, r in circles:
+                m |= np.hypot(X - cx, Y - cy) < r
+            return m if droplet else ~m
+
+        Cf = subsample_fraction(nx, ny, p.dx, p.dy, inside, nsub)
+        ratio = math.exp(rng.uniform(math.log(10.0), math.log(1000.0)))
+        vratio = math.exp(rng.uniform(0.0, math.log(100.0)))
+        p.enable_two_phase = 1
+        p.enable_surface_tension = 1
+        p.rho1, p.rho2 = 1000.0, 1000.0 / ratio
+        p.mu1, p.mu2 = 1.0e-2, 1.0e-2 / vratio
+        p.sigma = rng.uniform(0.01, 25.0)
+        p.gx, p.gy = 0.0, -0.98
+        p.linear_solver = capi.LINEAR_BICGSTAB
+        p.tol = 1.0e-10
+        p.p_tol = 1.0e-10
+        p.p_max_iter = 200000
+        p.recon = capi.RECON_ELVIRA
+        p.p_precision = capi.PREC_MIXED if mixed else capi.PREC_FP64
+        h = p.dx
+        dt_sigma = math.sqrt((p.rho1 + p.rho2) * h ** 3 / (4.0 * math.pi * p.sigma))
+        out.append((p, Cf, min(1.0e-4, 0.5 * dt_sigma)))
+    return out
+

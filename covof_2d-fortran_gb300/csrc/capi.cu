@@ -7,50 +7,12 @@
 #include <cstring>
 #include <new>
 
-#include "common.cuh"
-#include "momentum.cuh"
-#include "poisson.cuh"
-#include "vof.cuh"
-#include "adjoint.cuh"
+#include "handle.cuh"
 
 using namespace covof;
 
-namespace {
-
-constexpr int kPoissonThreads = 1024;  // one cell per thread per 1024-cell tile
-constexpr int kKrylovThreads = 512;    // momentum Krylov kernels (80 registers)
-constexpr int kMaxPartRegions = 16;  // doubles per block in the partials array
-
-template <typename T>
-int dalloc(T** p, size_t n) {
-  if (cudaMalloc((void**)p, n * sizeof(T)) != cudaSuccess) { *p = nullptr; return COVOF_CUDA_ERROR; }
-  if (cudaMemset(*p, 0, n * sizeof(T)) != cudaSuccess) return COVOF_CUDA_ERROR;
-  return COVOF_OK;
-}
-template <typename T>
-void dfree(T*& p) {
-  if (p) cudaFree(p);
-  p = nullptr;
-}
-
-#define CK(call)                                      \
-  do {                                                \
-    cudaError_t e_ = (call);                          \
-    if (e_ != cudaSuccess) return COVOF_CUDA_ERROR;   \
-  } while (0)
-#define CS(call)                          \
-  do {                                    \
-    int s_ = (call);                      \
-    if (s_ != COVOF_OK) return s_;        \
-  } while (0)
-
-// Device-side statistics of a resident run, folded in by k_step_log after
-// every step so that the host reads them once at the end.
-struct RunStats {
-  long long mom_iters, poisson_iters, refine_steps;
-  double last_relres, max_relres;
-  int step, first_bad_step, first_bad_status, pad;
-};
+namespace covof {
+namespace host {
 
 // One thread: fold this step's predictor and Poisson result records in.
 __global__ void k_step_log(const KrylovResult* kr, const PcgResult* pr, RunStats* s) {
@@ -71,73 +33,6 @@ __global__ void k_step_log(const KrylovResult* kr, const PcgResult* pr, RunStats
   s->step = step + 1;
 }
 
-}  // namespace
-
-struct covof_handle {
-  covof_params prm;
-  int device = 0, sm_count = 0;
-  cudaStream_t stream = nullptr;
-  Dims D{};
-  size_t g = 0;
-  int vof_step_count = 0;
-  // caller-field mirrors (host-pointer entry points)
-  bool have_fields = false;
-  double *f_u = nullptr, *f_v = nullptr, *f_p = nullptr, *f_rho_u = nullptr, *f_rho_v = nullptr,
-         *f_mu = nullptr, *f_mu_node = nullptr, *f_fx = nullptr, *f_fy = nullptr,
-         *f_u_old = nullptr, *f_v_old = nullptr, *f_C = nullptr, *f_rho = nullptr,
-         *f_curv = nullptr, *f_b = nullptr, *f_x2 = nullptr, *f_seg = nullptr;
-  // Poisson scratch
-  bool have_poisson = false;
-  double *px = nullptr, *pb = nullptr, *pr = nullptr, *pd = nullptr, *pAd = nullptr,
-         *pax = nullptr, *pay = nullptr, *paP = nullptr, *pisd = nullptr, *pinvD = nullptr,
-         *pd2 = nullptr, *pz = nullptr, *pw = nullptr, *pp = nullptr, *pq = nullptr;
-  float* pxb = nullptr;  // boundary-row exchange of the shared-memory inner solver
-  float *e32 = nullptr, *r32b = nullptr, *r32 = nullptr, *d32 = nullptr, *d32b = nullptr, *Ad32 = nullptr,
-        *ax32 = nullptr, *ay32 = nullptr, *aP32 = nullptr;
-  // momentum scratch (each 2g)
-  bool have_mom = false;
-  double *mx = nullptr, *mrhs = nullptr, *mdiag = nullptr, *mv[7] = {};
-  // VOF scratch
-  bool have_vof = false;
-  double *cs = nullptr, *seg = nullptr, *cnx = nullptr, *cny = nullptr, *ckap = nullptr;
-  int *vlist = nullptr, *vcount = nullptr;  // interface-cell list of the reconstruction
-  // adjoint scratch
-  bool have_adj = false;
-  double *arhs = nullptr, *apsi = nullptr, *apart = nullptr, *asum = nullptr;
-  double *f_gu = nullptr, *f_gv = nullptr, *f_gp = nullptr, *f_gbu = nullptr, *f_gbv = nullptr,
-         *f_ou = nullptr, *f_ov = nullptr;
-  // control
-  unsigned int* bar = nullptr;  // [0] grid barrier counter, [64..) per-block publish counters
-  int* err = nullptr;
-  double* part = nullptr;
-  int part_blocks = 0;
-  PcgResult* d_pres = nullptr;
-  KrylovResult* d_kres = nullptr;
-  PcgResult* h_pres = nullptr;
-  KrylovResult* h_kres = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  double last_solve_ms = 0.0;
-  int last_refine = 0;
-  // launch plans, fixed for the handle's mesh and parameters (computed once,
-  // so that a stream capture records launches only)
-  bool have_pplan = false;
-  const void* p_fn = nullptr;
-  size_t p_smem = 0;
-  int p_nb = 0, p_threads = 0;
-  bool have_mplan = false;
-  const void* m_fn = nullptr;
-  int m_nb = 0;
-  // resident time stepping
-  cudaStream_t cap_stream = nullptr;       // non-blocking stream used only while capturing
-  cudaGraphExec_t step_graph[2] = {};      // [0]: x-first Weymouth-Yue order, [1]: y-first
-  double graph_dt = 0.0;
-  bool graph_refused = false;
-  RunStats* d_run = nullptr;
-  RunStats* h_run = nullptr;
-  cudaEvent_t ev2 = nullptr, ev3 = nullptr;
-};
-
-namespace {
 
 int check_params(const covof_params* p) {
   if (!p) return COVOF_INVALID;
@@ -339,10 +234,9 @@ int poisson_plan(covof_handle* h) {
   return COVOF_OK;
 }
 
-// Assembly, solve and copy-back on the handle's stream; the result record
-// stays on the device (h->d_pres).  Nothing here synchronises.
-int poisson_enqueue(covof_handle* h, double dt, const double* u, const double* v, const double* b,
-                    const double* rho_u, const double* rho_v, double* p, bool timed) {
+// Assembly on the handle's stream and the argument block of the solve.
+int pois_pre(covof_handle* h, double dt, const double* u, const double* v, const double* b,
+             const double* rho_u, const double* rho_v, double* p, PoissonArgs* out) {
   const covof_params& P = h->prm;
   if (!rho_u || !rho_v || !p || (!b && (!u || !v))) return COVOF_INVALID;
   if (P.p_precond == COVOF_PRECOND_SSOR) return COVOF_UNSUPPORTED;
@@ -359,7 +253,8 @@ int poisson_enqueue(covof_handle* h, double dt, const double* u, const double* v
                                                                            h->ax32, h->ay32, h->aP32);
   k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, p, h->px, pinned);
   CK(cudaGetLastError());
-  PoissonArgs a;
+  PoissonArgs& a = *out;
+  std::memset(&a, 0, sizeof(a));
   a.D = h->D;
   a.x = h->px; a.b = h->pb; a.r = h->pr; a.d = h->pd; a.d2 = h->pd2; a.Ad = h->pAd;
   a.ax = h->pax; a.ay = h->pay; a.aP = h->paP; a.invD = h->pinvD; a.isd = h->pisd;
@@ -371,11 +266,26 @@ int poisson_enqueue(covof_handle* h, double dt, const double* u, const double* v
   a.tol = P.p_tol; a.inner_tol = P.p_inner_tol;
   a.max_iter = P.p_max_iter; a.inner_max_iter = P.p_inner_max_iter;
   a.max_refine = P.p_max_refine; a.pinned = pinned;
-  void* args[] = {&a};
-  CS(launch_coop(h, h->p_fn, h->p_nb, h->p_threads, args, timed, h->p_smem));
+  return COVOF_OK;
+}
+
+// Solution back into the caller's field.
+int pois_post(covof_handle* h, double* p) {
+  const dim3 blk(32, 8), grd = grid2(h->prm.nx, h->prm.ny, blk);
   k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, h->px, p, 0);
   CK(cudaGetLastError());
   return COVOF_OK;
+}
+
+// Assembly, solve and copy-back on the handle's stream; the result record
+// stays on the device (h->d_pres).  Nothing here synchronises.
+int poisson_enqueue(covof_handle* h, double dt, const double* u, const double* v, const double* b,
+                    const double* rho_u, const double* rho_v, double* p, bool timed) {
+  PoissonArgs a;
+  CS(pois_pre(h, dt, u, v, b, rho_u, rho_v, p, &a));
+  void* args[] = {&a};
+  CS(launch_coop(h, h->p_fn, h->p_nb, h->p_threads, args, timed, h->p_smem));
+  return pois_post(h, p);
 }
 
 // Reads the result record back (one small copy + stream synchronisation).
@@ -485,7 +395,7 @@ MomArgs mom_args(covof_handle* h, double dt, const double* u_n, const double* v_
   a.v0 = h->mv[0]; a.v1 = h->mv[1]; a.v2 = h->mv[2]; a.v3 = h->mv[3];
   a.v4 = h->mv[4]; a.v5 = h->mv[5]; a.v6 = h->mv[6];
   a.precond_on = P.use_precond && (P.precond == COVOF_PRECOND_JACOBI || P.precond == COVOF_PRECOND_ILU0);
-  a.max_iter = P.max_iter; a.tol = P.tol;
+  a.max_iter = P.max_iter; a.tol = P.tol; a.method = P.linear_solver;
   a.bar = h->bar; a.err = h->err; a.part = h->part; a.res = h->d_kres;
   return a;
 }
@@ -515,10 +425,11 @@ int predictor_plan(covof_handle* h) {
   return COVOF_OK;
 }
 
-// Predictor on the handle's stream, result record left on the device.
-int predictor_enqueue(covof_handle* h, double dt, double* u, double* v, const double* rho_u,
-                      const double* rho_v, const double* mu, const double* mu_node, const double* fx,
-                      const double* fy, const double* u_old, const double* v_old) {
+// Predictor assembly (Jacobi diagonal, right-hand side, packed initial
+// guess) on the handle's stream and the argument block of the Krylov solve.
+int mom_pre(covof_handle* h, double dt, double* u, double* v, const double* rho_u, const double* rho_v,
+            const double* mu, const double* mu_node, const double* fx, const double* fy, const double* u_old,
+            const double* v_old, MomArgs* out) {
   const covof_params& P = h->prm;
   if (!u || !v || !rho_u || !rho_v || !mu || !mu_node || !fx || !fy || !u_old || !v_old) return COVOF_INVALID;
   CS(check_mom_params(P));
@@ -526,17 +437,33 @@ int predictor_enqueue(covof_handle* h, double dt, double* u, double* v, const do
   CS(predictor_plan(h));
   // fields_old of the operator is the current field: the Krylov kernel only
   // writes its own vectors, u and v are overwritten after the solve.
-  MomArgs a = mom_args(h, dt, u, v, rho_u, rho_v, mu, mu_node, fx, fy, u_old, v_old);
+  MomArgs& a = *out;
+  a = mom_args(h, dt, u, v, rho_u, rho_v, mu, mu_node, fx, fy, u_old, v_old);
   const dim3 blk(32, 8), grd = grid2(P.nx + 1, P.ny + 1, blk);
   k_mom_diag<<<grd, blk, 0, h->stream>>>(a);
   k_mom_rhs<<<grd, blk, 0, h->stream>>>(a);
   k_mom_pack<<<grd, blk, 0, h->stream>>>(a, u, v);
   CK(cudaGetLastError());
-  void* args[] = {&a};
-  CS(launch_coop(h, h->m_fn, h->m_nb, kKrylovThreads, args, false));
+  return COVOF_OK;
+}
+
+// Solved velocities back into u, v, then the velocity boundary conditions.
+int mom_post(covof_handle* h, const MomArgs& a, double* u, double* v) {
+  const dim3 blk(32, 8), grd = grid2(h->prm.nx + 1, h->prm.ny + 1, blk);
   k_mom_unpack<<<grd, blk, 0, h->stream>>>(a, u, v);
   CK(cudaGetLastError());
   return velocity_bc_dev(h, u, v);
+}
+
+// Predictor on the handle's stream, result record left on the device.
+int predictor_enqueue(covof_handle* h, double dt, double* u, double* v, const double* rho_u,
+                      const double* rho_v, const double* mu, const double* mu_node, const double* fx,
+                      const double* fy, const double* u_old, const double* v_old) {
+  MomArgs a;
+  CS(mom_pre(h, dt, u, v, rho_u, rho_v, mu, mu_node, fx, fy, u_old, v_old, &a));
+  void* args[] = {&a};
+  CS(launch_coop(h, h->m_fn, h->m_nb, kKrylovThreads, args, false));
+  return mom_post(h, a, u, v);
 }
 
 int predictor_dev(covof_handle* h, double dt, double* u, double* v, const double* rho_u,
@@ -776,7 +703,10 @@ int run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run_stats
   return r.first_bad_step < 0 ? COVOF_OK : r.first_bad_status;
 }
 
-}  // namespace
+}  // namespace host
+}  // namespace covof
+
+using namespace covof::host;
 
 // ===========================================================================
 extern "C" {

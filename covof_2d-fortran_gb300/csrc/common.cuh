@@ -145,6 +145,25 @@ struct Team {
 };
 __device__ __forceinline__ Team grid_team() { return Team{(int)blockIdx.x, (int)gridDim.x}; }
 
+// Many cases in one persistent cooperative launch: the grid is cut into
+// teams (contiguous block ranges); each team solves its list of cases one
+// after another with barriers, reductions and publish counters of its own.
+struct BatchTeams {
+  const int* block_team;   // [nblocks] team of each block
+  const int4* team;        // [nteams] first block, size, [begin, end) in case_list
+  const int* case_list;    // case indices, grouped by team
+  unsigned int* bar;       // [32 * nteams] barrier counter per team (one 128-byte line each)
+  unsigned int* flags;     // [nblocks] publish counters (Chebyshev neighbour exchange)
+  int* err;                // [nteams] error words
+  double* part;            // [16 * nblocks] reduction partials (2 regions x 8 per block)
+};
+
+// This block's team, its reducer (partials, barrier and error word of the team).
+__device__ __forceinline__ Team batch_team(const BatchTeams& bt, int4& T) {
+  T = bt.team[bt.block_team[blockIdx.x]];
+  return Team{(int)blockIdx.x - T.x, T.y};
+}
+
 struct GridReducer {
   double* part;
   GridSync gs;

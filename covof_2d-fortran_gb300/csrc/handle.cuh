@@ -1,0 +1,156 @@
+// handle.cuh -- internal: the handle behind covof_handle* and the enqueue
+// helpers of capi.cu that the batch engine (batch.cu) reuses.  Not part of
+// the C ABI.
+#pragma once
+#include <cstring>
+
+#include "common.cuh"
+#include "momentum.cuh"
+#include "poisson.cuh"
+#include "vof.cuh"
+#include "adjoint.cuh"
+
+namespace covof {
+namespace host {
+
+constexpr int kPoissonThreads = 1024;  // one cell per thread per 1024-cell tile
+constexpr int kKrylovThreads = 512;    // momentum Krylov kernels (80 registers)
+constexpr int kMaxPartRegions = 16;  // doubles per block in the partials array
+
+template <typename T>
+inline int dalloc(T** p, size_t n) {
+  if (cudaMalloc((void**)p, n * sizeof(T)) != cudaSuccess) { *p = nullptr; return COVOF_CUDA_ERROR; }
+  if (cudaMemset(*p, 0, n * sizeof(T)) != cudaSuccess) return COVOF_CUDA_ERROR;
+  return COVOF_OK;
+}
+template <typename T>
+inline void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+#define CK(call)                                      \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return COVOF_CUDA_ERROR;   \
+  } while (0)
+#define CS(call)                          \
+  do {                                    \
+    int s_ = (call);                      \
+    if (s_ != COVOF_OK) return s_;        \
+  } while (0)
+
+// Device-side statistics of a resident run, folded in by k_step_log after
+// every step so that the host reads them once at the end.
+struct RunStats {
+  long long mom_iters, poisson_iters, refine_steps;
+  double last_relres, max_relres;
+  int step, first_bad_step, first_bad_status, pad;
+};
+
+// One thread: fold this step's predictor and Poisson result records in.
+__global__ void k_step_log(const KrylovResult* kr, const PcgResult* pr, RunStats* s);
+
+}  // namespace host
+}  // namespace covof
+
+struct covof_handle {
+  using Dims = covof::Dims;
+  using PcgResult = covof::PcgResult;
+  using KrylovResult = covof::KrylovResult;
+  covof_params prm;
+  int device = 0, sm_count = 0;
+  cudaStream_t stream = nullptr;
+  Dims D{};
+  size_t g = 0;
+  int vof_step_count = 0;
+  // caller-field mirrors (host-pointer entry points)
+  bool have_fields = false;
+  double *f_u = nullptr, *f_v = nullptr, *f_p = nullptr, *f_rho_u = nullptr, *f_rho_v = nullptr,
+         *f_mu = nullptr, *f_mu_node = nullptr, *f_fx = nullptr, *f_fy = nullptr,
+         *f_u_old = nullptr, *f_v_old = nullptr, *f_C = nullptr, *f_rho = nullptr,
+         *f_curv = nullptr, *f_b = nullptr, *f_x2 = nullptr, *f_seg = nullptr;
+  // Poisson scratch
+  bool have_poisson = false;
+  double *px = nullptr, *pb = nullptr, *pr = nullptr, *pd = nullptr, *pAd = nullptr,
+         *pax = nullptr, *pay = nullptr, *paP = nullptr, *pisd = nullptr, *pinvD = nullptr,
+         *pd2 = nullptr, *pz = nullptr, *pw = nullptr, *pp = nullptr, *pq = nullptr;
+  float* pxb = nullptr;  // boundary-row exchange of the shared-memory inner solver
+  float *e32 = nullptr, *r32b = nullptr, *r32 = nullptr, *d32 = nullptr, *d32b = nullptr, *Ad32 = nullptr,
+        *ax32 = nullptr, *ay32 = nullptr, *aP32 = nullptr;
+  // momentum scratch (each 2g)
+  bool have_mom = false;
+  double *mx = nullptr, *mrhs = nullptr, *mdiag = nullptr, *mv[7] = {};
+  // VOF scratch
+  bool have_vof = false;
+  double *cs = nullptr, *seg = nullptr, *cnx = nullptr, *cny = nullptr, *ckap = nullptr;
+  int *vlist = nullptr, *vcount = nullptr;  // interface-cell list of the reconstruction
+  // adjoint scratch
+  bool have_adj = false;
+  double *arhs = nullptr, *apsi = nullptr, *apart = nullptr, *asum = nullptr;
+  double *f_gu = nullptr, *f_gv = nullptr, *f_gp = nullptr, *f_gbu = nullptr, *f_gbv = nullptr,
+         *f_ou = nullptr, *f_ov = nullptr;
+  // control
+  unsigned int* bar = nullptr;  // [0] grid barrier counter, [64..) per-block publish counters
+  int* err = nullptr;
+  double* part = nullptr;
+  int part_blocks = 0;
+  PcgResult* d_pres = nullptr;
+  KrylovResult* d_kres = nullptr;
+  PcgResult* h_pres = nullptr;
+  KrylovResult* h_kres = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_solve_ms = 0.0;
+  int last_refine = 0;
+  // launch plans, fixed for the handle's mesh and parameters (computed once,
+  // so that a stream capture records launches only)
+  bool have_pplan = false;
+  const void* p_fn = nullptr;
+  size_t p_smem = 0;
+  int p_nb = 0, p_threads = 0;
+  bool have_mplan = false;
+  const void* m_fn = nullptr;
+  int m_nb = 0;
+  // resident time stepping
+  cudaStream_t cap_stream = nullptr;       // non-blocking stream used only while capturing
+  cudaGraphExec_t step_graph[2] = {};      // [0]: x-first Weymouth-Yue order, [1]: y-first
+  double graph_dt = 0.0;
+  bool graph_refused = false;
+  covof::host::RunStats* d_run = nullptr;
+  covof::host::RunStats* h_run = nullptr;
+  cudaEvent_t ev2 = nullptr, ev3 = nullptr;
+};
+
+namespace covof {
+namespace host {
+
+// Helpers of capi.cu shared with the batch engine (batch.cu).
+int ensure_fields(covof_handle* h);
+int ensure_poisson(covof_handle* h);
+int ensure_mom(covof_handle* h);
+int ensure_vof(covof_handle* h);
+int check_mom_params(const covof_params& P);
+int poisson_plan(covof_handle* h);
+int predictor_plan(covof_handle* h);
+int4 wall_flags(const covof_params& p);
+dim3 grid2(int ni, int nj, dim3 b);
+int sync(covof_handle* h);
+int pois_pre(covof_handle* h, double dt, const double* u, const double* v, const double* b,
+             const double* rho_u, const double* rho_v, double* p, PoissonArgs* out);
+int pois_post(covof_handle* h, double* p);
+int mom_pre(covof_handle* h, double dt, double* u, double* v, const double* rho_u, const double* rho_v,
+            const double* mu, const double* mu_node, const double* fx, const double* fy, const double* u_old,
+            const double* v_old, MomArgs* out);
+int mom_post(covof_handle* h, const MomArgs& a, double* u, double* v);
+int wy_step_dev(covof_handle* h, double dt, int x_first, const double* u, const double* v, double* C);
+int vof_bc_dev(covof_handle* h, double* C);
+int props_dev(covof_handle* h, double* C, double* rho, double* rho_u, double* rho_v, double* mu,
+              double* mu_node);
+int csf_dev(covof_handle* h, const double* C, double* fx, double* fy, double* curv);
+int velocity_bc_dev(covof_handle* h, double* u, double* v);
+int correct_dev(covof_handle* h, double dt, double* u, double* v, const double* p, const double* rho_u,
+                const double* rho_v);
+double** field_slot(covof_handle* h, int f);
+
+}  // namespace host
+}  // namespace covof

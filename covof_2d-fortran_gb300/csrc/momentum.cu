@@ -371,10 +371,8 @@ __device__ void krylov_finish(const MomArgs& a, const Team& tm, int iters, int s
 }
 
 // src/module_linear_solvers.f90:584-730 solve_bicgstab (left Jacobi).
-__global__ void __launch_bounds__(512) k_bicgstab(MomArgs a) {
-  const Team tm = grid_team();
+__device__ void bicgstab_case(const MomArgs& a, const Team& tm, GridReducer& R) {
   DofWalker W(a.D, tm);
-  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   double *x = a.x, *bh = a.v0, *r = a.v1, *rt = a.v2, *p = a.v3, *v = a.v4, *s = a.v5, *t = a.v6;
   const double tol = a.tol;
   const int max_iter = a.max_iter;
@@ -456,12 +454,16 @@ __global__ void __launch_bounds__(512) k_bicgstab(MomArgs a) {
   krylov_finish(a, tm, iters, status, ok);
 }
 
+__global__ void __launch_bounds__(512) k_bicgstab(MomArgs a) {
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  bicgstab_case(a, tm, R);
+}
+
 // src/module_linear_solvers.f90:735-838 solve_cg (unpreconditioned operator,
 // separate Jacobi application).
-__global__ void __launch_bounds__(512) k_cg(MomArgs a) {
-  const Team tm = grid_team();
+__device__ void cg_case(const MomArgs& a, const Team& tm, GridReducer& R) {
   DofWalker W(a.D, tm);
-  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   double *x = a.x, *r = a.v1, *p = a.v3, *Ap = a.v4;
   const double tol = a.tol;
   const int max_iter = a.max_iter;
@@ -510,11 +512,15 @@ __global__ void __launch_bounds__(512) k_cg(MomArgs a) {
   krylov_finish(a, tm, iters, status, ok);
 }
 
-// src/module_linear_solvers.f90:361-579 solve_bicgstab2 (left Jacobi).
-__global__ void __launch_bounds__(512) k_bicgstab2(MomArgs a) {
+__global__ void __launch_bounds__(512) k_cg(MomArgs a) {
   const Team tm = grid_team();
-  DofWalker W(a.D, tm);
   GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  cg_case(a, tm, R);
+}
+
+// src/module_linear_solvers.f90:361-579 solve_bicgstab2 (left Jacobi).
+__device__ void bicgstab2_case(const MomArgs& a, const Team& tm, GridReducer& R) {
+  DofWalker W(a.D, tm);
   double *x = a.x, *rt = a.v0, *r0 = a.v1, *r1 = a.v2, *r2 = a.v3, *u0 = a.v4, *u1 = a.v5, *u2 = a.v6;
   const double tol = a.tol;
   const int max_iter = a.max_iter;
@@ -642,6 +648,12 @@ __global__ void __launch_bounds__(512) k_bicgstab2(MomArgs a) {
   krylov_finish(a, tm, iter, status, ok);
 }
 
+__global__ void __launch_bounds__(512) k_bicgstab2(MomArgs a) {
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  bicgstab2_case(a, tm, R);
+}
+
 // ---------------------------------------------------------------------------
 // Copy the solution DOFs back into (u, v); ghosts come from k_vbc_*.
 __global__ void k_mom_unpack(MomArgs a, double* u, double* v) {
@@ -722,6 +734,21 @@ __global__ void k_vbc_corners(BcArgs b, double* u, double* v) {
   u[D.id(nx + 1, ny + 1)] = u[D.id(nx + 1, ny)];
   v[D.id(nx + 1, ny + 1)] = v[D.id(nx, ny + 1)];
   v[D.id(0, ny + 1)] = v[D.id(1, ny + 1)];
+}
+
+// Predictor Krylov solves of many cases in one persistent launch (teams,
+// see BatchTeams); each case's method is its own linear_solver.
+__global__ void __launch_bounds__(512) k_mom_krylov_batch(const MomArgs* __restrict__ cases, BatchTeams bt) {
+  int4 T;
+  const Team tm = batch_team(bt, T);
+  const int t = bt.block_team[blockIdx.x];
+  GridReducer R{bt.part + (size_t)16 * T.x, GridSync{bt.bar + 32 * t, bt.err + t, (unsigned)T.y, 0u}, 0, tm.rank};
+  for (int q = T.z; q < T.w; ++q) {
+    const MomArgs& a = cases[bt.case_list[q]];
+    if (a.method == COVOF_LINEAR_BICGSTAB) bicgstab_case(a, tm, R);
+    else if (a.method == COVOF_LINEAR_CG) cg_case(a, tm, R);
+    else bicgstab2_case(a, tm, R);
+  }
 }
 
 }  // namespace covof

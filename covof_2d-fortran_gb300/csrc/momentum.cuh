@@ -24,6 +24,7 @@ struct MomArgs {
   double* x; double* rhs; double* diag;
   double* v0; double* v1; double* v2; double* v3; double* v4; double* v5; double* v6;
   int precond_on, max_iter;
+  int method;  // COVOF_LINEAR_* (the batch kernel dispatches on it)
   double tol;
   unsigned int* bar; int* err; double* part;  // part: 16 * nblocks doubles
   KrylovResult* res;
@@ -41,6 +42,7 @@ __global__ void k_mom_apply(MomArgs a, const double* xu, const double* xv, doubl
 __global__ void k_bicgstab(MomArgs a);
 __global__ void k_bicgstab2(MomArgs a);
 __global__ void k_cg(MomArgs a);
+__global__ void k_mom_krylov_batch(const MomArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_mom_unpack(MomArgs a, double* u, double* v);
 __global__ void k_mom_pack(MomArgs a, const double* u, const double* v);
 __global__ void k_vbc_we(BcArgs b, double* u, double* v);

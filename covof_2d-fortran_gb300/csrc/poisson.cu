@@ -356,13 +356,10 @@ __device__ bool remove_mean(const Dims& D, const Tiles& tl, const Team& tm, Grid
   return true;
 }
 
-// Plain FP64 Jacobi-PCG solve.
-__global__ void __launch_bounds__(1024, 1) k_pcg_fp64(PoissonArgs a) {
-  __shared__ double sd[kHalo];
+// Plain FP64 Jacobi-PCG solve of case a by team tm.
+__device__ void fp64_case(const PoissonArgs& a, const Team& tm, GridReducer& R, double* sd) {
   const Dims D = a.D;
   const Tiles tl = make_tiles(D, blockDim.x);
-  const Team tm = grid_team();
-  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   Sys<double> S{a.x, a.b, a.r, a.d, a.d2, a.Ad, a.ax, a.ay, a.aP, a.invD};
   PcgOut o = pcg_tiled<double, false>(D, tl, tm, R, S, a.pinned, a.tol, a.max_iter, false, sd);
   bool ok = o.ok;
@@ -373,6 +370,13 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_fp64(PoissonArgs a) {
     a.res->status = ok ? o.status : COVOF_TIMEOUT;
     a.res->outer = 0;
   }
+}
+
+__global__ void __launch_bounds__(1024, 1) k_pcg_fp64(PoissonArgs a) {
+  __shared__ double sd[kHalo];
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  fp64_case(a, tm, R, sd);
 }
 
 // ---------------------------------------------------------------------------
@@ -1086,6 +1090,29 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_smem(PoissonArgs a) {
   in.xb = a.xb;
   in.load_coeffs(a.ax32, a.ay32);
   fcg_mixed(a, own, in, R);
+}
+
+// Poisson solves of many cases in one persistent launch (teams, see
+// BatchTeams): plain FP64 PCG, or the mixed solver with the streaming
+// Chebyshev inner iteration.
+__global__ void __launch_bounds__(1024, 1) k_pcg_fp64_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt) {
+  __shared__ double sd[kHalo];
+  int4 T;
+  const Team tm = batch_team(bt, T);
+  const int t = bt.block_team[blockIdx.x];
+  GridReducer R{bt.part + (size_t)16 * T.x, GridSync{bt.bar + 32 * t, bt.err + t, (unsigned)T.y, 0u}, 0, tm.rank};
+  for (int q = T.z; q < T.w; ++q) fp64_case(cases[bt.case_list[q]], tm, R, sd);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_pcg_mixed_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt) {
+  __shared__ float2 cheb_tab[kChebTab];
+  int4 T;
+  const Team tm = batch_team(bt, T);
+  const int t = bt.block_team[blockIdx.x];
+  GridReducer R{bt.part + (size_t)16 * T.x, GridSync{bt.bar + 32 * t, bt.err + t, (unsigned)T.y, 0u}, 0, tm.rank};
+  unsigned int sent = 0;
+  for (int q = T.z; q < T.w; ++q)
+    mixed_stream_case(cases[bt.case_list[q]], tm, R, bt.flags + T.x, &sent, cheb_tab);
 }
 
 // Velocity correction u -= dt/rho_u (p_e - p_w)/dx, v likewise

@@ -301,3 +301,68 @@ class Solver:
         st = self.lib.covof_run_steps(self.h, dt, int(nsteps), capi.RUN_GRAPH if graph else 0,
                                       C.byref(stats))
         return self._check(st, "covof_run_steps"), stats.as_dict()
+
+
+class Batch:
+    """Many independent cases stepped together (covof_batch_*): one entry of
+    params per case, uneven mesh sizes allowed."""
+
+    def __init__(self, params_list):
+        self.lib = capi.load_library()
+        self.params = [p.copy() for p in params_list]
+        self.n = len(self.params)
+        arr = (Params * self.n)(*self.params)
+        h = C.c_void_p()
+        st = self.lib.covof_batch_create(arr, self.n, C.byref(h))
+        if st != capi.OK:
+            raise CovofError(st, "covof_batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.covof_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int, where: str) -> int:
+        if st in _RAISE:
+            raise CovofError(st, where)
+        return st
+
+    def state_set(self, i: int, f: Fields):
+        for name in capi.FIELD_NAMES:
+            self._check(self.lib.covof_batch_state_set(self.h, i, capi.FIELD[name], _ptr(getattr(f, name))),
+                        "covof_batch_state_set")
+
+    def state_get(self, i: int, f: Fields):
+        for name in capi.FIELD_NAMES:
+            self._check(self.lib.covof_batch_state_get(self.h, i, capi.FIELD[name], _ptr(getattr(f, name))),
+                        "covof_batch_state_get")
+
+    def run_steps(self, dt, nsteps: int, graph: bool = True):
+        """nsteps steps of every case (dt: one value per case, or a scalar);
+        returns (status, per-case statistics, device ms)."""
+        dts = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, dtype=np.float64), (self.n,)))
+        stats = (capi.RunStats * self.n)()
+        ms = C.c_double()
+        st = self.lib.covof_batch_run_steps(self.h, dts.ctypes.data_as(C.POINTER(C.c_double)), int(nsteps),
+                                            capi.RUN_GRAPH if graph else 0, stats, C.byref(ms))
+        return self._check(st, "covof_batch_run_steps"), [x.as_dict() for x in stats], ms.value
+
+    def info(self) -> dict:
+        v = [C.c_int() for _ in range(4)]
+        self._check(self.lib.covof_batch_info(self.h, *[C.byref(x) for x in v]), "covof_batch_info")
+        return dict(zip(("poisson_teams", "poisson_blocks", "predictor_teams", "predictor_blocks"),
+                        (x.value for x in v)))
+

@@ -313,6 +313,33 @@ typedef struct covof_run_stats {
  * stats->graph is 0. */
 int covof_run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run_stats* stats);
 
+/* ---- batches of independent cases ------------------------------------- */
+
+/* Many independent cases (each its own mesh size and parameters) stepped
+ * together.  No reference counterpart: the reference runs one case per MPI
+ * job.  A batch step runs, for every case, what covof_run_steps runs, with
+ * the predictor and Poisson Krylov solves of ALL cases in one persistent
+ * cooperative launch each (teams of blocks, one case per team at a time);
+ * with COVOF_RUN_GRAPH a whole batch step is one CUDA-graph launch.  All
+ * cases of a batch use the same Poisson arithmetic (p_precision); the mixed
+ * batch runs the streaming Chebyshev inner form (COVOF_INNER_CG is
+ * rejected).  The Weymouth-Yue pass order follows the batch's own step count
+ * (x first on its first step). */
+typedef struct covof_batch covof_batch;
+int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out);
+int covof_batch_destroy(covof_batch* b);
+/* Resident fields of one case (COVOF_FIELD_*), as covof_state_set/get. */
+int covof_batch_state_set(covof_batch* b, int icase, int field, const double* host);
+int covof_batch_state_get(covof_batch* b, int icase, int field, double* host);
+/* nsteps steps of every case, dt[icase] each (fixed per call); stats (one per
+ * case, may be NULL) as covof_run_steps; ms = device time of the call.
+ * Returns the first failing case's first failing status, else COVOF_OK. */
+int covof_batch_run_steps(covof_batch* b, const double* dt, int nsteps, int flags,
+                          covof_run_stats* stats, double* ms);
+/* Team layout of the two batched solves. */
+int covof_batch_info(const covof_batch* b, int* poisson_teams, int* poisson_blocks,
+                     int* predictor_teams, int* predictor_blocks);
+
 #ifdef __cplusplus
 }
 #endif
