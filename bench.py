@@ -7,7 +7,9 @@ iterative refinement); the plain FP64 PCG path is timed beside it.
 
 Beside it ("sp_steps"): whole time steps (VOF + STANDARD_PROJECTION) of the
 rising-bubble case, 128x256, device-resident and replayed as CUDA graphs,
-plain FP64 vs mixed Poisson (steps/s).
+plain FP64 vs mixed Poisson (steps/s); and ("batch") 256 independent
+droplet / bubble cases of uneven sizes stepped together by the batch engine
+(steps/s of the whole batch, mixed vs plain FP64).
 
 One step = one Poisson solve from a zero initial guess.  Device time per step
 is measured with CUDA events on the library's own stream; a 512 MiB buffer is
@@ -217,6 +219,37 @@ def sp_steps(pkg, orc, nsteps, cpu_steps):
     return out
 
 
+def batch_steps(pkg, orc, ncases, nsteps):
+    """Many independent droplet / bubble cases (sizes 64..512 per direction,
+    density ratio 10..1000) stepped together by the batch engine, each batch
+    step one CUDA-graph launch with the predictor and Poisson solves of all
+    cases in one persistent launch each: mixed vs plain FP64 Poisson."""
+    out = {"workload": f"{ncases} droplet/bubble cases, nx, ny in {{64,128,256,512}}, density ratio "
+                       "log-uniform 10..1000, viscosity ratio 1..100, sigma 0.01..25, Poisson to rel-res 1e-10, "
+                       "CUDA-graph batch step", "cases": ncases, "steps": nsteps}
+    for name, mixed in (("mixed", True), ("fp64", False)):
+        cases = pkg.cases.droplet_batch(n_cases=ncases, mixed=mixed)
+        with pkg.Batch([c[0] for c in cases]) as b:
+            for i, (p, C0, dt) in enumerate(cases):
+                f = pkg.Fields.allocate(p)
+                f.C[...] = C0
+                orc.apply_vof_bc(p, f.C)
+                orc.update_physical_properties(p, f)
+                orc.compute_curvature_and_csf(p, f)
+                b.state_set(i, f)
+            dts = [c[2] for c in cases]
+            st, _, _ = b.run_steps(dts, 2, graph=True)
+            st, stats, ms = b.run_steps(dts, nsteps, graph=True)
+            info = b.info()
+        assert st == pkg.capi.OK, (name, st)
+        out["cells"] = sum(c[0].nx * c[0].ny for c in cases)
+        out[name] = {"steps_per_s": 1000.0 * nsteps / ms, "ms_per_step": ms / nsteps,
+                     "poisson_iters_per_step": sum(x["poisson_iters"] for x in stats) / nsteps,
+                     "max_relres": max(x["max_relres"] for x in stats), **info}
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    return out
+
+
 def run_reference(args, world, rank):
     """--impl reference: the reference path's CPU implementation (the FP64
     C++ restatement; the Fortran reference cannot be built on these
@@ -365,6 +398,7 @@ def run_ours(args, world, rank, local):
         orc = ge._load_oracle()
         cpu = None if args.skip_cpu else cpu_sample(pkg, orc, p, b, ru, rv, dt, it_f, 1, args.cpu_budget)
         steps = None if args.skip_steps else sp_steps(pkg, orc, 100, 0 if args.skip_cpu else 3)
+        batch = None if args.skip_steps else batch_steps(pkg, orc, 256, 5)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
@@ -390,6 +424,7 @@ def run_ours(args, world, rank, local):
             "gpu_launches": 5 * args.steps,
             "clocks": mixed["clocks"],
             "sp_steps": steps,
+            "batch": batch,
         }
     for r in results.values():
         r["solver"].close()

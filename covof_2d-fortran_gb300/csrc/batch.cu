@@ -43,8 +43,11 @@ struct Plan {
   unsigned int* d_flags = nullptr;
   int* d_err = nullptr;
   double* d_part = nullptr;
+  float* d_xb = nullptr;  // boundary rows of the shared-memory inner form
+  int xbw = 0;
+  size_t smem = 0;        // dynamic shared memory per block of the launch
   BatchTeams dev() const {
-    return BatchTeams{d_block_team, d_team, d_case_list, d_bar, d_flags, d_err, d_part};
+    return BatchTeams{d_block_team, d_team, d_case_list, d_bar, d_flags, d_err, d_part, d_xb, xbw};
   }
 };
 
@@ -63,6 +66,7 @@ struct covof_batch {
   MomArgs* h_margs = nullptr;
   PoissonArgs* d_pargs = nullptr;
   MomArgs* d_margs = nullptr;
+  const void* pfn = nullptr;  // the batched Poisson kernel
   cudaGraphExec_t graph[2] = {};
   std::vector<double> graph_dt;
   bool graph_refused = false;
@@ -78,23 +82,31 @@ int next_pow2(long long v) {
 }
 
 // Teams for a batched solve over at most max_blocks co-resident blocks.
-// Team size grows with the case (a power of two, about cells_per_block
-// cells per block, at most 16 blocks and never more blocks than rows); the
-// blocks are shared among the size classes in proportion to their work, and
-// the cases of a class go to its teams longest first.
+// The makespan is the busiest block's load, so a case gets about as many
+// blocks as its share of the batch's work (work ~ cells x the longer side,
+// the growth of the iteration count), rounded up to a power of two, at most
+// 16 and never more blocks than rows.  Blocks are then shared among the
+// size classes in proportion to their work, and the cases of a class go to
+// its teams longest first.
+// min_team (optional): a lower bound on the team size of each case (the
+// shared-memory form needs enough blocks for the strips to fit).
 int make_plan(Plan& pl, const std::vector<covof_handle*>& hs, int max_blocks, int threads,
-              long long cells_per_block) {
+              const std::vector<int>* min_team = nullptr) {
   const int n = (int)hs.size();
   std::vector<long long> work(n), cls(n);
   long long wtot = 0;
   for (int c = 0; c < n; ++c) {
     const long long cells = (long long)hs[c]->prm.nx * hs[c]->prm.ny;
-    work[c] = cells * std::max(hs[c]->prm.nx, hs[c]->prm.ny);  // iterations grow with the side
-    int t = next_pow2((cells + cells_per_block - 1) / cells_per_block);
+    work[c] = cells * std::max(hs[c]->prm.nx, hs[c]->prm.ny);
+    wtot += work[c];
+  }
+  for (int c = 0; c < n; ++c) {
+    const double share = (double)work[c] * max_blocks / (double)wtot;
+    int t = next_pow2((long long)std::ceil(share));
     t = std::min(t, 16);
     while (t > 1 && t > hs[c]->prm.ny) t >>= 1;
+    if (min_team) t = std::max(t, (*min_team)[c]);
     cls[c] = t;
-    wtot += work[c];
   }
   // blocks per class
   std::vector<int> sizes;
@@ -111,6 +123,24 @@ int make_plan(Plan& pl, const std::vector<covof_handle*>& hs, int max_blocks, in
     nt = (int)std::max(1LL, std::min((long long)nt, cnt));
     nteams[s] = nt;
     used += nt * sizes[s];
+  }
+  // hand leftover blocks to the class with the most work per block, while
+  // it has more cases than teams
+  std::vector<long long> wcls(sizes.size(), 0), ncls(sizes.size(), 0);
+  for (size_t s = 0; s < sizes.size(); ++s)
+    for (int c = 0; c < n; ++c)
+      if (cls[c] == sizes[s]) { wcls[s] += work[c]; ++ncls[s]; }
+  for (;;) {
+    int best = -1;
+    double best_load = -1.0;
+    for (size_t s = 0; s < sizes.size(); ++s) {
+      if (nteams[s] >= ncls[s] || used + sizes[s] > max_blocks) continue;
+      const double load = (double)wcls[s] / ((double)nteams[s] * sizes[s]);
+      if (load > best_load) { best_load = load; best = (int)s; }
+    }
+    if (best < 0) break;
+    nteams[best] += 1;
+    used += sizes[best];
   }
   // shrink the largest classes until the teams fit
   while (used > max_blocks) {
@@ -166,7 +196,23 @@ int make_plan(Plan& pl, const std::vector<covof_handle*>& hs, int max_blocks, in
 
 void free_plan(Plan& pl) {
   dfree(pl.d_block_team); dfree(pl.d_team); dfree(pl.d_case_list);
-  dfree(pl.d_bar); dfree(pl.d_flags); dfree(pl.d_err); dfree(pl.d_part);
+  dfree(pl.d_bar); dfree(pl.d_flags); dfree(pl.d_err); dfree(pl.d_part); dfree(pl.d_xb);
+}
+
+// Shared-memory form of the mixed batch: the smallest power-of-two team per
+// case whose row strips fit one block's shared memory (at most 32 blocks,
+// never more blocks than rows).  Returns false when some case does not fit.
+bool smem_teams(const std::vector<covof_handle*>& hs, size_t budget, std::vector<int>& tmin, size_t& bytes) {
+  bytes = 0;
+  tmin.assign(hs.size(), 1);
+  for (size_t c = 0; c < hs.size(); ++c) {
+    const int nx = hs[c]->prm.nx, ny = hs[c]->prm.ny;
+    int t = 1;
+    while (t <= 32 && t <= ny && smem_cheb_bytes(nx, (ny + t - 1) / t) > budget) t <<= 1;
+    if (t > 32 || t > ny) return false;
+    tmin[c] = t;
+  }
+  return true;
 }
 
 int max_coresident(const covof_batch* b, const void* fn, int threads) {
@@ -176,6 +222,7 @@ int max_coresident(const covof_batch* b, const void* fn, int threads) {
 }
 
 int launch_batch(covof_batch* b, const Plan& pl, const void* fn, const void* cases) {
+  // (pl.smem: dynamic shared memory of the shared-memory inner form)
   CK(cudaMemsetAsync(pl.d_bar, 0, (size_t)32 * pl.nteams * sizeof(unsigned int), b->stream));
   CK(cudaMemsetAsync(pl.d_flags, 0, (size_t)pl.nblocks * sizeof(unsigned int), b->stream));
   CK(cudaMemsetAsync(pl.d_err, 0, (size_t)pl.nteams * sizeof(int), b->stream));
@@ -187,6 +234,7 @@ int launch_batch(covof_batch* b, const Plan& pl, const void* fn, const void* cas
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(pl.nblocks);
   cfg.blockDim = dim3(pl.threads);
+  cfg.dynamicSmemBytes = pl.smem;
   cfg.stream = b->stream;
   cfg.attrs = at;
   cfg.numAttrs = 1;
@@ -240,8 +288,7 @@ int enqueue_batch_step(covof_batch* b, const double* dt, bool x_first) {
   }));
   CK(cudaMemcpyAsync(b->d_pargs, b->h_pargs, sizeof(PoissonArgs) * b->ncases, cudaMemcpyHostToDevice,
                      b->stream));
-  CS(launch_batch(b, b->pplan, b->mixed ? (const void*)k_pcg_mixed_batch : (const void*)k_pcg_fp64_batch,
-                  b->d_pargs));
+  CS(launch_batch(b, b->pplan, b->pfn, b->d_pargs));
   CS(per_case(b, [&](int c, covof_handle* h) -> int {
     CS(pois_post(h, h->f_p));
     CS(correct_dev(h, dt[c], h->f_u, h->f_v, h->f_p, h->f_rho_u, h->f_rho_v));
@@ -347,13 +394,56 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
   if (cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
     return fail(COVOF_CUDA_ERROR);
-  const void* pfn = b->mixed ? (const void*)k_pcg_mixed_batch : (const void*)k_pcg_fp64_batch;
-  const int pmax = max_coresident(b, pfn, 1024);
+  // Poisson: the mixed batch keeps each case's inner state in shared-memory
+  // row strips when every case fits a team of at most 32 blocks, else it
+  // streams the inner state through L2 / HBM
+  b->pfn = b->mixed ? (const void*)k_pcg_mixed_batch : (const void*)k_pcg_fp64_batch;
+  std::vector<int> tmin;
+  bool smem_form = false;
+  bool want_stream = false;
+  for (int c = 0; c < ncases; ++c) want_stream |= cases[c].p_inner_kind == COVOF_INNER_CHEBYSHEV_STREAM;
+  if (b->mixed && !want_stream) {
+    int optin = 0;
+    cudaFuncAttributes fa;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+    if (cudaFuncGetAttributes(&fa, (const void*)k_pcg_mixed_smem_batch) == cudaSuccess &&
+        optin > (int)fa.sharedSizeBytes &&
+        smem_teams(b->h, (size_t)optin - fa.sharedSizeBytes, tmin, b->pplan.smem)) {
+      smem_form = true;
+      b->pfn = (const void*)k_pcg_mixed_smem_batch;
+    }
+    cudaGetLastError();
+  }
+  int pmax = 0;
+  if (smem_form) {
+    // the launch's shared memory: the largest strip over the cases, with
+    // teams no smaller than tmin (larger teams only shorten strips)
+    size_t bytes = 0;
+    for (int c = 0; c < ncases; ++c) {
+      const int nx = b->h[c]->prm.nx, ny = b->h[c]->prm.ny;
+      bytes = std::max(bytes, smem_cheb_bytes(nx, (ny + tmin[c] - 1) / tmin[c]));
+    }
+    b->pplan.smem = bytes;
+    if (cudaFuncSetAttribute(b->pfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+      return fail(COVOF_CUDA_ERROR);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->pfn, 1024, bytes) != cudaSuccess || per_sm < 1)
+      return fail(COVOF_CUDA_ERROR);
+    pmax = per_sm * b->sm_count;
+  } else {
+    pmax = max_coresident(b, b->pfn, 1024);
+  }
   const int mmax = max_coresident(b, (const void*)k_mom_krylov_batch, 512);
   if (pmax < 1 || mmax < 1) return fail(COVOF_CUDA_ERROR);
-  int s = make_plan(b->pplan, b->h, pmax, 1024, 64 * 1024);
+  int s = make_plan(b->pplan, b->h, pmax, 1024, smem_form ? &tmin : nullptr);
   if (s != COVOF_OK) return fail(s);
-  s = make_plan(b->mplan, b->h, mmax, 512, 32 * 1024);
+  if (smem_form) {
+    int wmax = 0;
+    for (covof_handle* h : b->h) wmax = std::max(wmax, h->prm.nx + 2);
+    b->pplan.xbw = wmax;
+    if (dalloc(&b->pplan.d_xb, (size_t)4 * b->pplan.nblocks * wmax)) return fail(COVOF_CUDA_ERROR);
+  }
+  s = make_plan(b->mplan, b->h, mmax, 512);
   if (s != COVOF_OK) return fail(s);
   if (dalloc(&b->d_pargs, (size_t)ncases) || dalloc(&b->d_margs, (size_t)ncases) ||
       cudaMallocHost(&b->h_pargs, sizeof(PoissonArgs) * ncases) != cudaSuccess ||

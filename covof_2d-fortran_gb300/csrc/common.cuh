@@ -156,6 +156,8 @@ struct BatchTeams {
   unsigned int* flags;     // [nblocks] publish counters (Chebyshev neighbour exchange)
   int* err;                // [nteams] error words
   double* part;            // [16 * nblocks] reduction partials (2 regions x 8 per block)
+  float* xb;               // [4 * nblocks * xbw] boundary-row exchange (shared-memory inner form)
+  int xbw;                 // row length of xb: largest nx + 2 of the batch
 };
 
 // This block's team, its reducer (partials, barrier and error word of the team).

@@ -398,6 +398,19 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_fp64(PoissonArgs a) {
 // the streaming PCG.  Strips: block b owns full-width rows [r0, r0+R); thread
 // t owns strip cells t, t+1024, ... (row-major), which is also the layout of
 // the shared-memory inner solver.  f(k, c): global index, strip-local index.
+// FP64 five-point operator; every load through L2 (other blocks write x).
+__device__ __forceinline__ double stencil64(const Dims& D, int k, const double* __restrict__ x,
+                                            const double* __restrict__ ax,
+                                            const double* __restrict__ ay,
+                                            const double* __restrict__ aP) {
+  double v = aP[k] * __ldcg(x + k);
+  v = fma(-ax[k], __ldcg(x + k - 1), v);
+  v = fma(-ax[k + 1], __ldcg(x + k + 1), v);
+  v = fma(-ay[k], __ldcg(x + k - D.P), v);
+  v = fma(-ay[k + D.P], __ldcg(x + k + D.P), v);
+  return v;
+}
+
 struct TileOwn {
   Dims D; Tiles tl; Team tm;
   template <typename F>
@@ -407,6 +420,10 @@ struct TileOwn {
       const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
       if (i <= D.nx && j <= D.ny) f(D.id(i, j), 0);
     }
+  }
+  __device__ __forceinline__ double stencil(int k, int, const double* __restrict__ x, const double* __restrict__ ax,
+                                            const double* __restrict__ ay, const double* __restrict__ aP) const {
+    return stencil64(D, k, x, ax, ay, aP);
   }
 };
 
@@ -426,19 +443,24 @@ struct StripOwn {
       f(D.id(col, r0 + row), c);
     }
   }
+  // Rows of this strip were written by this block (visible after
+  // __syncthreads through L1); only the rows above and below come from other
+  // blocks and are read through L2.
+  __device__ __forceinline__ double stencil(int k, int c, const double* __restrict__ x,
+                                            const double* __restrict__ ax, const double* __restrict__ ay,
+                                            const double* __restrict__ aP) const {
+    const int P = D.P;
+    const double xs = c < D.nx ? __ldcg(x + k - P) : x[k - P];
+    const double xn = c >= (R - 1) * D.nx ? __ldcg(x + k + P) : x[k + P];
+    double v = aP[k] * x[k];
+    v = fma(-ax[k], x[k - 1], v);
+    v = fma(-ax[k + 1], x[k + 1], v);
+    v = fma(-ay[k], xs, v);
+    v = fma(-ay[k + P], xn, v);
+    return v;
+  }
 };
 
-__device__ __forceinline__ double stencil64(const Dims& D, int k, const double* __restrict__ x,
-                                            const double* __restrict__ ax,
-                                            const double* __restrict__ ay,
-                                            const double* __restrict__ aP) {
-  double v = aP[k] * __ldcg(x + k);
-  v = fma(-ax[k], __ldcg(x + k - 1), v);
-  v = fma(-ax[k + 1], __ldcg(x + k + 1), v);
-  v = fma(-ay[k], __ldcg(x + k - D.P), v);
-  v = fma(-ay[k + D.P], __ldcg(x + k + D.P), v);
-  return v;
-}
 
 // Inner FP32 solver on the streaming tiles: RHS and solution live in global
 // FP32 vectors.
@@ -604,7 +626,7 @@ struct SmemCheby {
   float* xb;              // [2][G][2 sides][W] boundary rows of d
   unsigned int* flags;    // [G] publish counters
   int* err;
-  unsigned int sent;      // this block's publish count
+  unsigned int* sent;     // this block's publish count (lives across solves and cases)
   __device__ __forceinline__ float* xrow(int par, int blk, int side) const {
     return xb + (((size_t)par * G + blk) * 2 + side) * W;
   }
@@ -648,21 +670,21 @@ struct SmemCheby {
   }
   // write the boundary rows of d, then count the publish (release)
   __device__ __forceinline__ void publish() {
-    const int par = sent & 1;
+    const int par = *sent & 1;
     for (int col = threadIdx.x; col < W; col += blockDim.x) {
       xrow(par, b, 0)[col] = d[W + col];
       xrow(par, b, 1)[col] = d[R * W + col];
     }
     __syncthreads();
     if (threadIdx.x == 0) red_add_release_u32(flags + b, 1u);
-    sent++;
+    ++*sent;
   }
   // wait for the neighbours' publish number `sent` (1-based), copy their rows
   // into the halo rows of d.  Returns false after a bounded wait gave up.
   __device__ __forceinline__ bool fetch() {
     __shared__ int s_ok;
-    const unsigned int want = sent;  // every block has published `sent` times
-    const int par = (sent - 1) & 1;
+    const unsigned int want = *sent;  // every block has published `sent` times
+    const int par = (want - 1) & 1;
     if (threadIdx.x == 0) {
       int ok = 1;
       long long spins = 0;
@@ -751,8 +773,8 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
   auto ones_image = [&](int k) { return a.aP[k] - a.ax[k] - a.ax[k + 1] - a.ay[k] - a.ay[k + D.P]; };
   auto true_residual = [&]() -> bool {
     double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    own.each([&](int k, int) {
-      const double rr = (k == pk) ? 0.0 : a.b[k] - stencil64(D, k, x, a.ax, a.ay, a.aP);
+    own.each([&](int k, int c) {
+      const double rr = (k == pk) ? 0.0 : a.b[k] - own.stencil(k, c, x, a.ax, a.ay, a.aP);
       r[k] = rr;
       acc[0] = fma(a.b[k], a.b[k], acc[0]);
       acc[1] = fma(rr, rr, acc[1]);
@@ -828,8 +850,8 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     // consecutive directions are dominated by the same smooth mode.
     double acc[2] = {0.0, 0.0};
     const bool was_fresh = fresh;
-    own.each([&](int k, int) {
-      double wk = (k == pk) ? 0.0 : stencil64(D, k, z, a.ax, a.ay, a.aP);
+    own.each([&](int k, int c) {
+      double wk = (k == pk) ? 0.0 : own.stencil(k, c, z, a.ax, a.ay, a.aP);
       if (shift != 0.0) wk -= shift * ones_image(k);
       const double zk = z[k] - shift;
       const double pk_ = was_fresh ? zk : fma(-beta, pv[k], zk);
@@ -969,25 +991,36 @@ struct StreamCheby {
       }
     }
     publish();
+    const float* __restrict__ axr = ax;
+    const float* __restrict__ ayr = ay;
+    float* __restrict__ yr = ys;
+    float* __restrict__ rr = r;
     for (int s = 0; s < steps; ++s) {
       if (!fetch()) { o.ok = false; o.status = COVOF_TIMEOUT; break; }
       const bool last = (s + 1 == steps);
       const float2 cc = tab[s];
+      const float* __restrict__ dr = d;
+      float* __restrict__ dw = dn;
       int row = row0, col = col0;
+#pragma unroll 2
       for (int c = threadIdx.x; c < n; c += blockDim.x, row += drow, col += dcol) {
         if (col > nx) { col -= nx; ++row; }
         const int k = (r0 + row) * P + col;
-        const float dc = __ldcg(d + k);
+        // own rows were written by this block (L1 is coherent for them after
+        // __syncthreads); the rows above and below belong to other blocks
+        const float dc = dr[k];
+        const float ds = row == 0 ? __ldcg(dr + k - P) : dr[k - P];
+        const float dnn = row == R - 1 ? __ldcg(dr + k + P) : dr[k + P];
         float v = dc;
-        v = __fmaf_rn(-ax[k], __ldcg(d + k - 1), v);
-        v = __fmaf_rn(-ax[k + 1], __ldcg(d + k + 1), v);
-        v = __fmaf_rn(-ay[k], __ldcg(d + k - P), v);
-        v = __fmaf_rn(-ay[k + P], __ldcg(d + k + P), v);
+        v = __fmaf_rn(-axr[k], dr[k - 1], v);
+        v = __fmaf_rn(-axr[k + 1], dr[k + 1], v);
+        v = __fmaf_rn(-ayr[k], ds, v);
+        v = __fmaf_rn(-ayr[k + P], dnn, v);
         if (k == pk) v = 0.0f;
-        ys[k] += dc;
-        const float rn = r[k] - v;
-        r[k] = rn;
-        if (!last) dn[k] = __fmaf_rn(cc.x, dc, cc.y * rn);
+        yr[k] += dc;
+        const float rn = rr[k] - v;
+        rr[k] = rn;
+        if (!last) dw[k] = __fmaf_rn(cc.x, dc, cc.y * rn);
       }
       o.iters++;
       if (last) break;
@@ -1026,11 +1059,13 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_stream(PoissonArgs a) {
   mixed_stream_case(a, tm, R, a.flags, &sent, cheb_tab);
 }
 
-__global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cheb(PoissonArgs a) {
-  extern __shared__ float smem[];
+// One mixed solve of case a by team tm with the shared-memory-resident
+// Chebyshev inner iteration (smem: the strip's dynamic shared memory, at
+// least smem_cheb_bytes(nx, rows) bytes; xb: the team's boundary-row
+// exchange, 4 * tm.size * (nx + 2) floats).
+__device__ void mixed_smem_case(const PoissonArgs& a, const Team& tm, GridReducer& R, unsigned int* flags,
+                                unsigned int* sent, float* xb, float2* tab, float* smem) {
   const Dims D = a.D;
-  const Team tm = grid_team();
-  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   int r0, Rr;
   strip_rows(D.ny, tm.size, tm.rank, r0, Rr);
   const int W = D.nx + 2;
@@ -1039,8 +1074,7 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cheb(PoissonArgs a) {
   in.D = D; in.r0 = r0; in.R = Rr; in.W = W; in.b = tm.rank; in.G = tm.size;
   in.pinned_c = (a.pinned && tm.rank == 0) ? 0 : -1;
   in.m = a.inner_max_iter; in.lo = a.cheb_lo;
-  __shared__ float2 cheb_tab[kChebTab];
-  in.tab = cheb_tab;
+  in.tab = tab;
   float* s = smem;
   in.ys = s; s += Rr * W;
   in.r = s; s += Rr * W;
@@ -1048,9 +1082,18 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cheb(PoissonArgs a) {
   in.dn = s; s += (Rr + 2) * W;
   in.ax = s; s += Rr * W;
   in.ay = s; s += (Rr + 1) * W;
-  in.xb = a.xb; in.flags = a.flags; in.err = a.err; in.sent = 0;
+  in.xb = xb; in.flags = flags; in.err = R.gs.err; in.sent = sent;
   in.load_coeffs(a.ax32, a.ay32);
   fcg_mixed(a, own, in, R);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cheb(PoissonArgs a) {
+  extern __shared__ float smem[];
+  __shared__ float2 cheb_tab[kChebTab];
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  unsigned int sent = 0;
+  mixed_smem_case(a, tm, R, a.flags, &sent, a.xb, cheb_tab, smem);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed(PoissonArgs a) {
@@ -1102,6 +1145,22 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_fp64_batch(const PoissonArgs* _
   const int t = bt.block_team[blockIdx.x];
   GridReducer R{bt.part + (size_t)16 * T.x, GridSync{bt.bar + 32 * t, bt.err + t, (unsigned)T.y, 0u}, 0, tm.rank};
   for (int q = T.z; q < T.w; ++q) fp64_case(cases[bt.case_list[q]], tm, R, sd);
+}
+
+// Shared-memory-resident form: every case's strips fit the launch's dynamic
+// shared memory (the planner sizes the teams so).
+__global__ void __launch_bounds__(1024, 1) k_pcg_mixed_smem_batch(const PoissonArgs* __restrict__ cases,
+                                                                  BatchTeams bt) {
+  extern __shared__ float smem[];
+  __shared__ float2 cheb_tab[kChebTab];
+  int4 T;
+  const Team tm = batch_team(bt, T);
+  const int t = bt.block_team[blockIdx.x];
+  GridReducer R{bt.part + (size_t)16 * T.x, GridSync{bt.bar + 32 * t, bt.err + t, (unsigned)T.y, 0u}, 0, tm.rank};
+  unsigned int sent = 0;
+  float* xb = bt.xb + (size_t)4 * T.x * bt.xbw;
+  for (int q = T.z; q < T.w; ++q)
+    mixed_smem_case(cases[bt.case_list[q]], tm, R, bt.flags + T.x, &sent, xb, cheb_tab, smem);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt) {

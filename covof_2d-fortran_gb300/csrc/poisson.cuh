@@ -56,6 +56,7 @@ __global__ void k_pcg_mixed_cheb(PoissonArgs a);
 __global__ void k_pcg_mixed_stream(PoissonArgs a);
 __global__ void k_pcg_fp64_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
+__global__ void k_pcg_mixed_smem_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 // Shared-memory bytes of k_pcg_mixed_cheb for a strip of R rows of nx cells.
 inline size_t smem_cheb_bytes(int nx, int R) { return (size_t)(6 * R + 5) * (size_t)(nx + 2) * sizeof(float); }
 // Shared-memory bytes of k_pcg_mixed_smem for a strip of R rows of nx cells.

@@ -321,10 +321,13 @@ int covof_run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run
  * the predictor and Poisson Krylov solves of ALL cases in one persistent
  * cooperative launch each (teams of blocks, one case per team at a time);
  * with COVOF_RUN_GRAPH a whole batch step is one CUDA-graph launch.  All
- * cases of a batch use the same Poisson arithmetic (p_precision); the mixed
- * batch runs the streaming Chebyshev inner form (COVOF_INNER_CG is
- * rejected).  The Weymouth-Yue pass order follows the batch's own step count
- * (x first on its first step). */
+ * cases of a batch use the same Poisson arithmetic (p_precision).  The mixed
+ * batch runs the Chebyshev inner iteration with each case's state in
+ * shared-memory row strips of a team sized to fit (at most 32 blocks), or
+ * streamed through L2 / HBM when a case does not fit or any case asks for
+ * COVOF_INNER_CHEBYSHEV_STREAM; COVOF_INNER_CG is rejected.  The
+ * Weymouth-Yue pass order follows the batch's own step count (x first on its
+ * first step). */
 typedef struct covof_batch covof_batch;
 int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out);
 int covof_batch_destroy(covof_batch* b);

@@ -21,10 +21,14 @@ def _cases(pkg, orc, mixed, n=6, sizes=(32, 48, 64), seed=7):
     return out
 
 
-@pytest.mark.parametrize("mixed", [False, True])
-def test_batch_matches_oracle_per_case(gpu_pkg, orc, mixed):
+@pytest.mark.parametrize("mode", ["fp64", "mixed", "mixed_stream"])
+def test_batch_matches_oracle_per_case(gpu_pkg, orc, mode):
     pkg = gpu_pkg
+    mixed = mode != "fp64"
     cases = _cases(pkg, orc, mixed)
+    if mode == "mixed_stream":
+        for p, f, dt in cases:
+            p.p_inner_kind = pkg.capi.INNER_CHEBYSHEV_STREAM
     nsteps = 3
     ref = []
     for p, f, dt in cases:
