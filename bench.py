@@ -415,9 +415,10 @@ def run_ours(args, world, rank, local):
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_pcg_mixed_cheb", "peak_source": peak_kind,
                          "note": "achieved = algorithmic bytes (8 FP32 words/cell per inner Chebyshev step + "
-                                 "21 FP64 words/cell per outer FCG iteration) / CUDA-event kernel time; traffic = "
-                                 "measured DRAM bytes per launch (ncu): the FP32 inner state is shared-memory "
-                                 "resident"},
+                                 "21 FP64 words/cell per outer FCG iteration, the streaming model) / CUDA-event "
+                                 "kernel time, an effective rate; traffic = measured DRAM bytes per launch "
+                                 "(ncu), far below it because the FP32 inner state is shared-memory resident: "
+                                 "the kernel is issue / exchange-latency bound, not HBM-bound"},
             "cpu_baseline": cpu,
             "e2e": {"value": world * 1000.0 / e2e_step, "unit": UNIT, "h2d_bytes_per_step": gbytes,
                     "d2h_bytes_per_step": b.nbytes},

@@ -76,6 +76,14 @@ class RunStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class Launch(C.Structure):
+    """covof_launch (include/covof_gpu.h)."""
+    _fields_ = [("p_threads", C.c_int), ("p_blocks", C.c_int), ("p_inner_form", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class CovofError(RuntimeError):
     def __init__(self, status: int, where: str):
         self.status = status
@@ -126,6 +134,8 @@ _SIGS = {
     "covof_state_get": [_VP, C.c_int, _VP],
     "covof_state_field_dev": [_VP, C.c_int, C.POINTER(C.c_void_p)],
     "covof_run_steps": [_VP, C.c_double, C.c_int, C.c_int, C.POINTER(RunStats)],
+    "covof_set_launch": [_VP, C.POINTER(Launch)],
+    "covof_get_launch": [_VP, C.POINTER(Launch)],
     "covof_batch_create": [C.POINTER(Params), C.c_int, C.POINTER(C.c_void_p)],
     "covof_batch_destroy": [_VP],
     "covof_batch_state_set": [_VP, C.c_int, C.c_int, _VP],

@@ -14,6 +14,8 @@ base + k with numpy's PCG64.  Arrays use the reference layout (ny+2, nx+2).
   (src/module_simulation.f90:2175-2416).
 * ``droplet_batch``    -- many independent droplet / bubble cases of uneven
   sizes (64..512 cells per direction) for the batch engine.
+* ``rt_case``          -- Rayleigh-Taylor instability, 4096^2 cells on
+  [0,1] x [0,4], heavy fluid over light.
 """
 from __future__ import annotations
 
@@ -197,8 +199,9 @@ def random_velocity(p: Params, scale: float, seed: int):
 def droplet_batch(n_cases: int = 256, seed: int = SEED + 4, sizes=(64, 128, 256, 512), nsub: int = 4,
                   mixed: bool = True):
     """Independent droplet / bubble cases: nx, ny drawn from sizes, square
-    cells of side 1/nx on [0, 1] x [0, ny/nx]; 1-3 circles with radii 0.1-0.3
-    of the short side (fluid 1 inside for a droplet, outside for a bubble);
+    cells, short side of the domain 1 (dx = dy = 1/min(nx, ny)); 1-3 circles
+    with radii 0.1-0.3 of the short side (fluid 1 inside for a droplet,
+    outside for a bubble);
     density ratio log-uniform in [10, 1000] (rho1 = 1000), viscosity ratio
     log-uniform in [1, 100] (mu1 = 1e-2), sigma uniform in [0.01, 25],
     g = (0, -0.98); ELVIRA + Weymouth-Yue, BiCGSTAB + Jacobi predictor and the
@@ -208,7 +211,8 @@ def droplet_batch(n_cases: int = 256, seed: int = SEED + 4, sizes=(64, 128, 256,
     out = []
     for _ in range(n_cases):
         nx, ny = (int(v) for v in rng.choice(sizes, 2))
-        lx, ly = 1.0, ny / nx
+        m = min(nx, ny)
+        lx, ly = nx / m, ny / m
         p = make_params(nx, ny, lx, ly)
         short = min(lx, ly)
         k = int(rng.integers(1, 4))
@@ -241,8 +245,46 @@ def droplet_batch(n_cases: int = 256, seed: int = SEED + 4, sizes=(64, 128, 256,
         p.p_max_iter = 200000
         p.recon = capi.RECON_ELVIRA
         p.p_precision = capi.PREC_MIXED if mixed else capi.PREC_FP64
-        h = p.dx
+        h = min(p.dx, p.dy)
         dt_sigma = math.sqrt((p.rho1 + p.rho2) * h ** 3 / (4.0 * math.pi * p.sigma))
         out.append((p, Cf, min(1.0e-4, 0.5 * dt_sigma)))
     return out
+
+
+def rt_case(nx: int = 4096, ny: int = 4096, seed: int = SEED + 5, nsub: int = 4, mixed: bool = True):
+    """Rayleigh-Taylor: [0,1] x [0,4], heavy fluid (rho 3, fluid 1, C = 1)
+    above y = 2 + 0.05 cos(2 pi x) + sum_{k=3..32} 1e-3 cos(2 pi k x + phi_k),
+    light fluid (rho 1) below, mu = 1e-3 in both, no surface tension,
+    g = (0, -9.81), no-slip walls, dt = 2e-5; ELVIRA + Weymouth-Yue,
+    BiCGSTAB + Jacobi predictor and the Poisson to 1e-10.  C is the exact
+    fraction of each cell above the interface, averaged over nsub x-samples
+    (the interface is a graph over x).  Returns (params, C, dt)."""
+    lx, ly = 1.0, 4.0
+    p = make_params(nx, ny, lx, ly)
+    rng = np.random.default_rng(seed)
+    ks = np.arange(3, 33)
+    phases = rng.uniform(0.0, 2.0 * math.pi, size=ks.size)
+    i = np.arange(0, nx + 2)
+    xs = ((i[:, None] - 1) + (np.arange(nsub) + 0.5)[None, :] / nsub) * p.dx       # (nx+2, nsub)
+    eta = 2.0 + 0.05 * np.cos(2.0 * math.pi * xs)
+    for k, ph in zip(ks, phases):
+        eta += 1.0e-3 * np.cos(2.0 * math.pi * k * xs + ph)
+    C = np.empty((ny + 2, nx + 2), dtype=np.float64)
+    for j0 in range(0, ny + 2, 256):
+        j = np.arange(j0, min(j0 + 256, ny + 2))
+        ylo = ((j - 1) * p.dy)[:, None, None]
+        frac = np.clip((ylo + p.dy - eta[None, :, :]) / p.dy, 0.0, 1.0)        # part above eta
+        C[j0:j0 + j.size] = frac.mean(axis=2)
+    p.enable_two_phase = 1
+    p.enable_surface_tension = 0
+    p.rho1, p.rho2 = 3.0, 1.0
+    p.mu1, p.mu2 = 1.0e-3, 1.0e-3
+    p.sigma, p.gx, p.gy = 0.0, 0.0, -9.81
+    p.linear_solver = capi.LINEAR_BICGSTAB
+    p.tol = 1.0e-10
+    p.p_tol = 1.0e-10
+    p.p_max_iter = 2000000
+    p.recon = capi.RECON_ELVIRA
+    p.p_precision = capi.PREC_MIXED if mixed else capi.PREC_FP64
+    return p, C, 2.0e-5
 

@@ -196,13 +196,15 @@ int poisson_plan(covof_handle* h) {
   if (h->have_pplan) return COVOF_OK;
   const covof_params& P = h->prm;
   const bool mixed = P.p_precision == COVOF_PREC_MIXED;
+  const covof_launch& L = h->launch;
   const void* fn = mixed ? (const void*)k_pcg_mixed : (const void*)k_pcg_fp64;
-  const int threads = mixed ? kPoissonThreads : fp64_threads(h);
+  const int threads = mixed ? kPoissonThreads : (L.p_threads ? L.p_threads : fp64_threads(h));
   long long units = (long long)make_tiles(h->D, threads).ntiles;
   size_t smem = 0;
   if (mixed) {
     // one row strip per block, at most one block per SM
-    const int G = P.ny < h->sm_count ? P.ny : h->sm_count;
+    int G = P.ny < h->sm_count ? P.ny : h->sm_count;
+    if (L.p_blocks > 0 && L.p_blocks < G) G = L.p_blocks;
     const int Rmax = (P.ny + G - 1) / G;
     const bool cheb = P.p_inner_kind != COVOF_INNER_CG;
     const void* sfn = cheb ? (const void*)k_pcg_mixed_cheb : (const void*)k_pcg_mixed_smem;
@@ -210,17 +212,21 @@ int poisson_plan(covof_handle* h) {
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
     cudaFuncAttributes fa;
-    if (P.p_inner_kind != COVOF_INNER_CHEBYSHEV_STREAM && cudaFuncGetAttributes(&fa, sfn) == cudaSuccess &&
-        bytes + fa.sharedSizeBytes <= (size_t)optin &&
+    const bool stream = P.p_inner_kind == COVOF_INNER_CHEBYSHEV_STREAM || (cheb && L.p_inner_form == 2);
+    if (!stream && cudaFuncGetAttributes(&fa, sfn) == cudaSuccess && bytes + fa.sharedSizeBytes <= (size_t)optin &&
         cudaFuncSetAttribute(sfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess) {
       fn = sfn;
       smem = bytes;
       units = G;
     } else if (cheb) {
+      cudaGetLastError();
+      if (L.p_inner_form == 1) return COVOF_UNSUPPORTED;  // strips asked for do not fit
       fn = (const void*)k_pcg_mixed_stream;  // strips stream through L2 / HBM
       units = G;
     }
     cudaGetLastError();
+  } else if (L.p_blocks > 0 && L.p_blocks < units) {
+    units = L.p_blocks;  // fewer blocks than tiles: each block walks several tiles
   }
   const int nb = coop_blocks(h, fn, threads, units, smem);
   if (nb < 1) return COVOF_CUDA_ERROR;
@@ -1176,6 +1182,38 @@ int covof_compute_curvature_and_csf(covof_handle* h, const double* C, double* fx
   CS(csf_dev(h, h->f_C, h->f_fx, h->f_fy, h->f_curv));
   CS(d2h(h, fx_sigma, h->f_fx, g)); CS(d2h(h, fy_sigma, h->f_fy, g)); CS(d2h(h, curvature, h->f_curv, g));
   return sync(h);
+}
+
+// ---- launch shapes ------------------------------------------------------------
+int covof_set_launch(covof_handle* h, const covof_launch* launch) {
+  if (!h || !launch) return COVOF_INVALID;
+  const covof_launch& L = *launch;
+  if (L.p_threads != 0 && L.p_threads != 128 && L.p_threads != 256 && L.p_threads != 512 && L.p_threads != 1024)
+    return COVOF_INVALID;
+  if (L.p_blocks < 0 || L.p_blocks > h->sm_count || L.p_inner_form < 0 || L.p_inner_form > 2)
+    return COVOF_INVALID;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  const covof_launch keep = h->launch;
+  h->launch = L;
+  h->have_pplan = false;
+  drop_graphs(h);
+  const int st = poisson_plan(h);
+  if (st != COVOF_OK) {
+    h->launch = keep;
+    h->have_pplan = false;
+    return st;
+  }
+  return COVOF_OK;
+}
+
+int covof_get_launch(covof_handle* h, covof_launch* launch) {
+  if (!h || !launch) return COVOF_INVALID;
+  CS(poisson_plan(h));
+  launch->p_threads = h->p_threads;
+  launch->p_blocks = h->p_nb;
+  launch->p_inner_form = h->p_fn == (const void*)k_pcg_mixed_cheb ? 1
+                       : h->p_fn == (const void*)k_pcg_mixed_stream ? 2 : 0;
+  return COVOF_OK;
 }
 
 // ---- resident time stepping -------------------------------------------------

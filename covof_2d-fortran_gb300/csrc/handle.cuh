@@ -105,6 +105,7 @@ struct covof_handle {
   // launch plans, fixed for the handle's mesh and parameters (computed once,
   // so that a stream capture records launches only)
   bool have_pplan = false;
+  covof_launch launch{};   // overrides of the planning rules (zero: rule)
   const void* p_fn = nullptr;
   size_t p_smem = 0;
   int p_nb = 0, p_threads = 0;

@@ -313,6 +313,23 @@ typedef struct covof_run_stats {
  * stats->graph is 0. */
 int covof_run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run_stats* stats);
 
+/* ---- launch shapes (autotuning) --------------------------------------- */
+
+/* Launch shape of the Poisson solver of a handle.  Zero fields leave the
+ * choice to the built-in rules; the autotuner (autotune.py) times candidates
+ * and sets the fastest.  No reference counterpart. */
+typedef struct covof_launch {
+  int p_threads;     /* plain FP64 PCG: threads per block, 128, 256, 512 or 1024 */
+  int p_blocks;      /* blocks of the persistent solve (mixed: row strips), at most one per SM */
+  int p_inner_form;  /* mixed Chebyshev inner state: 1 shared-memory strips, 2 streamed */
+} covof_launch;
+/* Set the overrides (validated: COVOF_INVALID for out-of-range values,
+ * COVOF_UNSUPPORTED for shared-memory strips that do not fit); drops the
+ * handle's launch plan and captured graphs. */
+int covof_set_launch(covof_handle* h, const covof_launch* launch);
+/* The shape in effect (after planning): every field filled in. */
+int covof_get_launch(covof_handle* h, covof_launch* launch);
+
 /* ---- batches of independent cases ------------------------------------- */
 
 /* Many independent cases (each its own mesh size and parameters) stepped
