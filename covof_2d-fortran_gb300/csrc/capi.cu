@@ -84,6 +84,7 @@ int ensure_mom(covof_handle* h) {
   if (h->have_mom) return COVOF_OK;
   const size_t g2 = 2 * h->g;
   CS(dalloc(&h->mx, g2)); CS(dalloc(&h->mrhs, g2)); CS(dalloc(&h->mdiag, g2));
+  CS(dalloc(&h->mcoef, 9 * g2)); CS(dalloc(&h->midiag, g2));
   for (int q = 0; q < 7; ++q) CS(dalloc(&h->mv[q], g2));
   h->have_mom = true;
   return COVOF_OK;
@@ -397,7 +398,7 @@ MomArgs mom_args(covof_handle* h, double dt, const double* u_n, const double* v_
   a.conv = P.enable_convection; a.scheme = P.convective_scheme;
   a.u_n = u_n; a.v_n = v_n; a.rho_u = rho_u; a.rho_v = rho_v; a.mu = mu; a.mu_node = mu_node;
   a.fx = fx; a.fy = fy; a.u_old = u_old; a.v_old = v_old;
-  a.x = h->mx; a.rhs = h->mrhs; a.diag = h->mdiag;
+  a.x = h->mx; a.rhs = h->mrhs; a.diag = h->mdiag; a.coef = h->mcoef; a.idiag = h->midiag;
   a.v0 = h->mv[0]; a.v1 = h->mv[1]; a.v2 = h->mv[2]; a.v3 = h->mv[3];
   a.v4 = h->mv[4]; a.v5 = h->mv[5]; a.v6 = h->mv[6];
   a.precond_on = P.use_precond && (P.precond == COVOF_PRECOND_JACOBI || P.precond == COVOF_PRECOND_ILU0);
@@ -448,6 +449,7 @@ int mom_pre(covof_handle* h, double dt, double* u, double* v, const double* rho_
   const dim3 blk(32, 8), grd = grid2(P.nx + 1, P.ny + 1, blk);
   k_mom_diag<<<grd, blk, 0, h->stream>>>(a);
   k_mom_rhs<<<grd, blk, 0, h->stream>>>(a);
+  k_mom_assemble<<<grd, blk, 0, h->stream>>>(a);
   k_mom_pack<<<grd, blk, 0, h->stream>>>(a, u, v);
   CK(cudaGetLastError());
   return COVOF_OK;
@@ -807,7 +809,7 @@ int covof_destroy(covof_handle* h) {
   double** fl[] = {&h->f_u, &h->f_v, &h->f_p, &h->f_rho_u, &h->f_rho_v, &h->f_mu, &h->f_mu_node,
                    &h->f_fx, &h->f_fy, &h->f_u_old, &h->f_v_old, &h->f_C, &h->f_rho, &h->f_curv,
                    &h->f_b, &h->f_x2, &h->f_seg, &h->px, &h->pb, &h->pr, &h->pd, &h->pAd,
-                   &h->pax, &h->pay, &h->paP, &h->pisd, &h->pinvD, &h->pd2, &h->pz, &h->pw, &h->pp, &h->pq, &h->mx, &h->mrhs, &h->mdiag, &h->cs, &h->seg,
+                   &h->pax, &h->pay, &h->paP, &h->pisd, &h->pinvD, &h->pd2, &h->pz, &h->pw, &h->pp, &h->pq, &h->mx, &h->mrhs, &h->mdiag, &h->cs, &h->seg, &h->mcoef, &h->midiag,
                    &h->cnx, &h->cny, &h->ckap, &h->part, &h->arhs, &h->apsi, &h->apart, &h->asum,
                    &h->f_gu, &h->f_gv, &h->f_gp, &h->f_gbu, &h->f_gbv, &h->f_ou, &h->f_ov};
   for (double** q : fl) dfree(*q);

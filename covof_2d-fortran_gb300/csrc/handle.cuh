@@ -81,6 +81,7 @@ struct covof_handle {
   // momentum scratch (each 2g)
   bool have_mom = false;
   double *mx = nullptr, *mrhs = nullptr, *mdiag = nullptr, *mv[7] = {};
+  double *mcoef = nullptr, *midiag = nullptr;  // assembled operator rows, inverse diagonal
   // VOF scratch
   bool have_vof = false;
   double *cs = nullptr, *seg = nullptr, *cnx = nullptr, *cny = nullptr, *ckap = nullptr;

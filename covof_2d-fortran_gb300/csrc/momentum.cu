@@ -68,7 +68,8 @@ __device__ __forceinline__ double tv(const MomArgs& a, const double* xv, int i, 
 }
 
 // src/module_navier_stokes.f90:2388-2416 (UPWIND / CENTERED)
-__device__ __forceinline__ double conv_face_flux(int scheme, double flux, double pl, double pr) {
+template <class T>
+__device__ __forceinline__ T conv_face_flux(int scheme, double flux, const T& pl, const T& pr) {
   if (scheme == COVOF_CONV_CENTERED) return 0.5 * flux * (pl + pr);
   return (flux >= 0.0) ? flux * pl : flux * pr;
 }
@@ -98,9 +99,100 @@ __device__ __forceinline__ void v_fluxes(const MomArgs& a, int i, int j, double&
   FS = 0.5 * (vnS + vn) * a.dx;
 }
 
-// (A x) at one DOF (src/module_navier_stokes.f90:474-617 for u, :624-750 for v).
-__device__ double mom_apply_dof(const MomArgs& a, int part, int i, int j, const double* xu,
-                                const double* xv) {
+// Operand sources of mom_apply_gen.
+struct XSrc {
+  const MomArgs& a;
+  const double* xu;
+  const double* xv;
+  __device__ __forceinline__ double u(int i, int j) const { return tu(a, xu, i, j); }
+  __device__ __forceinline__ double v(int i, int j) const { return tv(a, xv, i, j); }
+};
+
+// A row of the operator as a linear form over 9 slots: same component
+// centre, east, west, north, south (0-4) and the 4 cross-component values the
+// row reads (5-8; u rows: v(i,j+1), v(i-1,j+1), v(i,j), v(i-1,j); v rows:
+// u(i+1,j), u(i+1,j-1), u(i,j), u(i,j-1)).  Wall ghosts fold into the slots
+// of the DOFs they are built from.
+struct LF {
+  double c[9];
+};
+__device__ __forceinline__ LF lf_zero() { LF r; for (int q = 0; q < 9; ++q) r.c[q] = 0.0; return r; }
+__device__ __forceinline__ LF lf_unit(int q) { LF r = lf_zero(); if (q >= 0) r.c[q] = 1.0; return r; }
+__device__ __forceinline__ LF operator+(const LF& x, const LF& y) { LF r; for (int q = 0; q < 9; ++q) r.c[q] = x.c[q] + y.c[q]; return r; }
+__device__ __forceinline__ LF operator-(const LF& x, const LF& y) { LF r; for (int q = 0; q < 9; ++q) r.c[q] = x.c[q] - y.c[q]; return r; }
+// constant - form: the constants of the ghost formulas are the homogeneous wall values, 0
+__device__ __forceinline__ LF operator-(double, const LF& y) { LF r; for (int q = 0; q < 9; ++q) r.c[q] = -y.c[q]; return r; }
+__device__ __forceinline__ LF operator*(double x, const LF& y) { LF r; for (int q = 0; q < 9; ++q) r.c[q] = x * y.c[q]; return r; }
+__device__ __forceinline__ LF operator*(const LF& y, double x) { return x * y; }
+__device__ __forceinline__ LF operator/(const LF& y, double x) { LF r; for (int q = 0; q < 9; ++q) r.c[q] = y.c[q] / x; return r; }
+
+struct LFSrc {
+  const MomArgs& a;
+  int part, i0, j0;
+  // slot of DOF (i, j) of component comp (0 u, 1 v) in this row, -1 if none
+  __device__ int slot(int comp, int i, int j) const {
+    if (comp == part) {
+      if (i == i0 && j == j0) return 0;
+      if (i == i0 + 1 && j == j0) return 1;
+      if (i == i0 - 1 && j == j0) return 2;
+      if (i == i0 && j == j0 + 1) return 3;
+      if (i == i0 && j == j0 - 1) return 4;
+      return -1;
+    }
+    if (part == 0) {  // v values read by a u row
+      if (i == i0 && j == j0 + 1) return 5;
+      if (i == i0 - 1 && j == j0 + 1) return 6;
+      if (i == i0 && j == j0) return 7;
+      if (i == i0 - 1 && j == j0) return 8;
+      return -1;
+    }
+    if (i == i0 + 1 && j == j0) return 5;  // u values read by a v row
+    if (i == i0 + 1 && j == j0 - 1) return 6;
+    if (i == i0 && j == j0) return 7;
+    if (i == i0 && j == j0 - 1) return 8;
+    return -1;
+  }
+  // tu / tv with the operand replaced by unit forms (same ghost rules)
+  __device__ LF u(int i, int j) const {
+    const int ny = a.D.ny;
+    if (j >= 1 && j <= ny) return i >= 1 ? lf_unit(slot(0, i, j)) : lf_zero();
+    if (j == 0) {
+      const LF u1 = lf_unit(slot(0, i, 1));
+      if (a.bc[SB] == COVOF_BC_DIRICHLET) {
+        if (ny >= 2) return (8.0 * 0.0 - 6.0 * u1 + lf_unit(slot(0, i, 2))) / 3.0;
+        return 2.0 * 0.0 - u1;
+      }
+      return u1;
+    }
+    const LF un = lf_unit(slot(0, i, ny));
+    if (a.bc[ST] == COVOF_BC_DIRICHLET) {
+      if (ny >= 2) return (8.0 * 0.0 - 6.0 * un + lf_unit(slot(0, i, ny - 1))) / 3.0;
+      return 2.0 * 0.0 - un;
+    }
+    return un;
+  }
+  __device__ LF v(int i, int j) const {
+    const int nx = a.D.nx;
+    if (j == 0) return lf_zero();
+    if (i == 0) {
+      const LF v1 = lf_unit(slot(1, 1, j));
+      return a.bc[SL] == COVOF_BC_DIRICHLET ? 2.0 * 0.0 - v1 : v1;
+    }
+    if (i == nx + 1) {
+      const LF vn = lf_unit(slot(1, nx, j));
+      return a.bc[SR] == COVOF_BC_DIRICHLET ? 2.0 * 0.0 - vn : vn;
+    }
+    return lf_unit(slot(1, i, j));
+  }
+};
+
+// (A x) at one DOF (src/module_navier_stokes.f90:474-617 for u, :624-750 for v),
+// written once over a value source: src.u(i, j) / src.v(i, j) give the
+// operand with its homogeneous ghost values.  Evaluated on doubles (XSrc) it
+// is the operator application, bit for bit the reference's term order;
+// evaluated on linear forms (LFSrc) it yields the row's coefficients.
+template <class S>
+__device__ auto mom_apply_gen(const MomArgs& a, int part, int i, int j, const S& src) -> decltype(src.u(0, 0)) {
   const Dims& D = a.D;
   const int nx = D.nx, ny = D.ny;
   const double dx = a.dx, dy = a.dy, dvol = dx * dy, dt = a.dt;
@@ -108,56 +200,61 @@ __device__ double mom_apply_dof(const MomArgs& a, int part, int i, int j, const 
   if (part == 0) {
     const double rho = a.rho_u[k];
     const double diag_bc = ((1.0 * rho) / dt) * dvol;
-    if (i == 1) return diag_bc * tu(a, xu, 1, j);        // DIRICHLET / FREESLIP west
-    if (i == nx + 1) return diag_bc * tu(a, xu, nx + 1, j);
-    const double uc = tu(a, xu, i, j);
-    double val = (((1.0 * rho) / dt) * uc) * dvol;
-    const double uE = tu(a, xu, i + 1, j), uW = tu(a, xu, i - 1, j);
-    const double uN = tu(a, xu, i, j + 1), uS = tu(a, xu, i, j - 1);
+    if (i == 1) return diag_bc * src.u(1, j);        // DIRICHLET / FREESLIP west
+    if (i == nx + 1) return diag_bc * src.u(nx + 1, j);
+    const auto uc = src.u(i, j);
+    auto val = (((1.0 * rho) / dt) * uc) * dvol;
+    const auto uE = src.u(i + 1, j), uW = src.u(i - 1, j);
+    const auto uN = src.u(i, j + 1), uS = src.u(i, j - 1);
     if (a.conv) {
       double FE, FW, FN, FS;
       u_fluxes(a, i, j, FE, FW, FN, FS);
-      const double pE = conv_face_flux(a.scheme, FE, uc, uE);
-      const double pW = conv_face_flux(a.scheme, FW, uW, uc);
-      const double pN = conv_face_flux(a.scheme, FN, uc, uN);
-      const double pS = conv_face_flux(a.scheme, FS, uS, uc);
+      const auto pE = conv_face_flux(a.scheme, FE, uc, uE);
+      const auto pW = conv_face_flux(a.scheme, FW, uW, uc);
+      const auto pN = conv_face_flux(a.scheme, FN, uc, uN);
+      const auto pS = conv_face_flux(a.scheme, FS, uS, uc);
       val = val + rho * (pE - pW + pN - pS);
     }
     const double muE = a.mu[k], muW = a.mu[k - 1];
-    const double dE = 2.0 * muE * (uE - uc) / dx * dy;
-    const double dW = 2.0 * muW * (uc - uW) / dx * dy;
+    const auto dE = 2.0 * muE * (uE - uc) / dx * dy;
+    const auto dW = 2.0 * muW * (uc - uW) / dx * dy;
     val = val - (dE - dW);
     const double mN = a.mu_node[k + D.P], mS = a.mu_node[k];
-    const double sN = mN * ((uN - uc) / dy + (tv(a, xv, i, j + 1) - tv(a, xv, i - 1, j + 1)) / dx) * dx;
-    const double sS = mS * ((uc - uS) / dy + (tv(a, xv, i, j) - tv(a, xv, i - 1, j)) / dx) * dx;
+    const auto sN = mN * ((uN - uc) / dy + (src.v(i, j + 1) - src.v(i - 1, j + 1)) / dx) * dx;
+    const auto sS = mS * ((uc - uS) / dy + (src.v(i, j) - src.v(i - 1, j)) / dx) * dx;
     val = val - (sN - sS);
     return val;
   }
   const double rho = a.rho_v[k];
   const double diag_bc = ((1.0 * rho) / dt) * dvol;
-  if ((j == 1 && is_wall(a, SB)) || (j == ny + 1 && is_wall(a, ST))) return diag_bc * tv(a, xv, i, j);
-  const double vc = tv(a, xv, i, j);
-  double val = (((1.0 * rho) / dt) * vc) * dvol;
-  const double vE = tv(a, xv, i + 1, j), vW = tv(a, xv, i - 1, j);
-  const double vN = tv(a, xv, i, j + 1), vS = tv(a, xv, i, j - 1);
+  if ((j == 1 && is_wall(a, SB)) || (j == ny + 1 && is_wall(a, ST))) return diag_bc * src.v(i, j);
+  const auto vc = src.v(i, j);
+  auto val = (((1.0 * rho) / dt) * vc) * dvol;
+  const auto vE = src.v(i + 1, j), vW = src.v(i - 1, j);
+  const auto vN = src.v(i, j + 1), vS = src.v(i, j - 1);
   if (a.conv) {
     double FE, FW, FN, FS;
     v_fluxes(a, i, j, FE, FW, FN, FS);
-    const double pE = conv_face_flux(a.scheme, FE, vc, vE);
-    const double pW = conv_face_flux(a.scheme, FW, vW, vc);
-    const double pN = conv_face_flux(a.scheme, FN, vc, vN);
-    const double pS = conv_face_flux(a.scheme, FS, vS, vc);
+    const auto pE = conv_face_flux(a.scheme, FE, vc, vE);
+    const auto pW = conv_face_flux(a.scheme, FW, vW, vc);
+    const auto pN = conv_face_flux(a.scheme, FN, vc, vN);
+    const auto pS = conv_face_flux(a.scheme, FS, vS, vc);
     val = val + rho * (pE - pW + pN - pS);
   }
   const double muN = a.mu[k], muS = a.mu[k - D.P];
-  const double dN = 2.0 * muN * (vN - vc) / dy * dx;
-  const double dS = 2.0 * muS * (vc - vS) / dy * dx;
+  const auto dN = 2.0 * muN * (vN - vc) / dy * dx;
+  const auto dS = 2.0 * muS * (vc - vS) / dy * dx;
   val = val - (dN - dS);
   const double mE = a.mu_node[k + 1], mW = a.mu_node[k];
-  const double sE = mE * ((vE - vc) / dx + (tu(a, xu, i + 1, j) - tu(a, xu, i + 1, j - 1)) / dy) * dy;
-  const double sW = mW * ((vc - vW) / dx + (tu(a, xu, i, j) - tu(a, xu, i, j - 1)) / dy) * dy;
+  const auto sE = mE * ((vE - vc) / dx + (src.u(i + 1, j) - src.u(i + 1, j - 1)) / dy) * dy;
+  const auto sW = mW * ((vc - vW) / dx + (src.u(i, j) - src.u(i, j - 1)) / dy) * dy;
   val = val - (sE - sW);
   return val;
+}
+
+__device__ double mom_apply_dof(const MomArgs& a, int part, int i, int j, const double* xu,
+                                const double* xv) {
+  return mom_apply_gen(a, part, i, j, XSrc{a, xu, xv});
 }
 
 // ---------------------------------------------------------------------------
@@ -312,6 +409,25 @@ __global__ void k_mom_apply(MomArgs a, const double* xu, const double* xv, doubl
   if (i <= D.nx && j <= D.ny + 1) yv[D.id(i, j)] = mom_apply_dof(a, 1, i, j, xu, xv);
 }
 
+// Rows of the operator for the Krylov solve (coef: 9 slots x 2g, slot-major)
+// and the inverse Jacobi diagonal (after k_mom_diag).  One thread per DOF.
+__global__ void k_mom_assemble(MomArgs a) {
+  const Dims& D = a.D;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int g = D.P * (D.ny + 2);
+  const size_t g2 = 2 * (size_t)g;
+  for (int part = 0; part < 2; ++part) {
+    const bool in = part == 0 ? (i <= D.nx + 1 && j <= D.ny) : (i <= D.nx && j <= D.ny + 1);
+    if (!in) continue;
+    const int k = (part == 0 ? 0 : g) + D.id(i, j);
+    const LF row = mom_apply_gen(a, part, i, j, LFSrc{a, part, i, j});
+    for (int q = 0; q < 9; ++q) a.coef[q * g2 + k] = row.c[q];
+    const double d = a.diag[k];
+    a.idiag[k] = (a.precond_on && fabs(d) > 1.0e-15) ? 1.0 / d : 1.0;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Persistent Krylov solvers.  DOF ownership: warp w walks 32-wide row
 // segments of the u block, then of the v block.
@@ -346,16 +462,44 @@ struct DofWalker {
   for (int s_ = (W).gw; s_ < (W).stot; s_ += (W).nw)                 \
     for (int part = 0, i = 0, j = 0, k = 0, once_ = (W).at((A).D, s_, part, i, j, k); once_; once_ = 0)
 
-__device__ __forceinline__ double prec(const MomArgs& a, int k, double src) {
-  const double d = a.diag[k];
-  return (a.precond_on && fabs(d) > 1.0e-15) ? src / d : src;
-}
+// Jacobi preconditioner (src/module_linear_solvers.f90:88-135): a multiply by
+// the inverse diagonal k_mom_assemble stored (1 where the reference skips
+// the division).
+__device__ __forceinline__ double prec(const MomArgs& a, int k, double src) { return src * a.idiag[k]; }
 
-// y = M^-1 A x (or A x when with_prec = false) at own DOFs.
+// y = M^-1 A x (or A x when with_prec = false) at own DOFs, from the
+// assembled rows: 9 FMAs instead of the matrix-free expression (which costs
+// tens of FP64 divisions per DOF; FP64 issue bounds these solves on GB300).
+// Wall rows keep only their centre coefficient and read nothing else.
 __device__ __forceinline__ double pa_at(const MomArgs& a, const DofWalker& W, int part, int i,
                                         int j, int k, const double* x, bool with_prec) {
-  const double y = mom_apply_dof(a, part, i, j, x, x + W.g);
-  return with_prec ? prec(a, k, y) : y;
+  const Dims& D = a.D;
+  const size_t g2 = 2 * (size_t)W.g;
+  const double* __restrict__ cf = a.coef;
+  double y = cf[k] * __ldcg(x + k);
+  const bool wall_row = part == 0 ? (i == 1 || i == D.nx + 1)
+                                  : ((j == 1 && is_wall(a, SB)) || (j == D.ny + 1 && is_wall(a, ST)));
+  if (!wall_row) {
+    const int P = D.P;
+    const int o = part == 0 ? W.g : -W.g;  // offset of the other component's block
+    const int kc = k + o;                   // same (i, j) in the other block
+    y = fma(cf[1 * g2 + k], __ldcg(x + k + 1), y);
+    y = fma(cf[2 * g2 + k], __ldcg(x + k - 1), y);
+    y = fma(cf[3 * g2 + k], __ldcg(x + k + P), y);
+    y = fma(cf[4 * g2 + k], __ldcg(x + k - P), y);
+    if (part == 0) {
+      y = fma(cf[5 * g2 + k], __ldcg(x + kc + P), y);
+      y = fma(cf[6 * g2 + k], __ldcg(x + kc + P - 1), y);
+      y = fma(cf[7 * g2 + k], __ldcg(x + kc), y);
+      y = fma(cf[8 * g2 + k], __ldcg(x + kc - 1), y);
+    } else {
+      y = fma(cf[5 * g2 + k], __ldcg(x + kc + 1), y);
+      y = fma(cf[6 * g2 + k], __ldcg(x + kc + 1 - P), y);
+      y = fma(cf[7 * g2 + k], __ldcg(x + kc), y);
+      y = fma(cf[8 * g2 + k], __ldcg(x + kc - P), y);
+    }
+  }
+  return with_prec ? y * a.idiag[k] : y;
 }
 
 struct KCtx {

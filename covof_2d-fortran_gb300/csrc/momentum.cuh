@@ -22,6 +22,8 @@ struct MomArgs {
   const double* fx; const double* fy; const double* u_old; const double* v_old;
   // Krylov storage: each vector 2*(nx+2)*(ny+2) doubles (u block, v block)
   double* x; double* rhs; double* diag;
+  double* coef;   // assembled rows: 9 slots x 2*(nx+2)*(ny+2), slot-major (k_mom_assemble)
+  double* idiag;  // inverse Jacobi diagonal (1 where no division applies)
   double* v0; double* v1; double* v2; double* v3; double* v4; double* v5; double* v6;
   int precond_on, max_iter;
   int method;  // COVOF_LINEAR_* (the batch kernel dispatches on it)
@@ -38,6 +40,7 @@ struct BcArgs {
 
 __global__ void k_mom_diag(MomArgs a);
 __global__ void k_mom_rhs(MomArgs a);
+__global__ void k_mom_assemble(MomArgs a);
 __global__ void k_mom_apply(MomArgs a, const double* xu, const double* xv, double* yu, double* yv);
 __global__ void k_bicgstab(MomArgs a);
 __global__ void k_bicgstab2(MomArgs a);

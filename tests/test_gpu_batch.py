@@ -54,11 +54,11 @@ def test_batch_matches_oracle_per_case(gpu_pkg, orc, mode):
         assert stats[i]["last_relres"] <= 1e-10
         for name in ("u", "v", "p"):
             a, e = getattr(g, name), getattr(r, name)
-            # plain FP64: 1e-9.  Mixed: u, v 1e-9; p 1e-8 -- a different Krylov
-            # path stopped at ||r||/||b|| <= 1e-10 differs from the oracle's by
-            # up to cond(A) * 1e-10 (measured 1.7e-9 on these cases, the same
-            # as the single-case mixed path)
-            tol = 1e-8 if (mixed and name == "p") else 1e-9
+            # u, v 1e-9; p 1e-8 -- Krylov paths stopped at 1e-10 that are not
+            # the oracle's bit for bit (mixed Poisson; assembled predictor
+            # operator) differ by up to cond * 1e-10, and div(u*) amplifies
+            # predictor differences into p (measured up to 1.7e-9)
+            tol = 1e-8 if name == "p" else 1e-9
             assert np.linalg.norm(a - e) / np.linalg.norm(e) < tol, (i, name)
         assert np.abs(g.C - r.C).max() <= 1e-12, i
 

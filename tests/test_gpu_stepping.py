@@ -20,10 +20,15 @@ def _bubble(pkg, orc, nx=32, ny=64, mixed=False):
     return p, f, dt
 
 
-def _close(g, f, rel=1e-9):
+def _close(g, f, rel=1e-9, rel_p=1e-8):
+    # u, v within 1e-9 over several steps.  p within 1e-8: the predictor
+    # solves to ||r||/||r0|| <= 1e-10 along a Krylov path that is not the
+    # oracle's bit for bit (the GPU applies the assembled operator), and
+    # div(u*) -- the Poisson right-hand side -- amplifies that difference
+    # (a single SP step stays within 1e-10, test_gpu_momentum).
     for name in ("u", "v", "p"):
         a, b = getattr(g, name), getattr(f, name)
-        assert np.linalg.norm(a - b) / np.linalg.norm(b) < rel, name
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < (rel_p if name == "p" else rel), name
     assert np.abs(g.C - f.C).max() <= 1e-12
 
 
