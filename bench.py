@@ -11,6 +11,10 @@ plain FP64 vs mixed Poisson (steps/s); and ("batch") 256 independent
 droplet / bubble cases of uneven sizes stepped together by the batch engine
 (steps/s of the whole batch, mixed vs plain FP64).
 
+Before timing, the autotuner (autotune.py) picks the mixed solve's launch
+shape and Chebyshev degree / interval on the same system (bounded budget); the
+line reports the choice and the built-in rule's time.
+
 One step = one Poisson solve from a zero initial guess.  Device time per step
 is measured with CUDA events on the library's own stream; a 512 MiB buffer is
 written between steps (outside the timed events) so every step starts with a
@@ -308,11 +312,28 @@ def run_ours(args, world, rank, local):
     tp = torch.zeros_like(tb)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
+    # autotune the mixed solve on this system (launch shape, Chebyshev degree
+    # and interval; the stopping test stays the true FP64 residual at 1e-10)
+    tuned = None
+    if not args.no_tune:
+        import importlib
+        at = importlib.import_module(pkg.__name__ + ".autotune")
+        q0 = p.copy()
+        q0.p_precision = cap.PREC_MIXED
+        tuned = at.tune(q0, dt, tb, tru, trv, repeats=1, cache_path=None, budget_s=args.tune_budget)
+
     results = {}
     for name, prec in (("fp64", cap.PREC_FP64), ("mixed", cap.PREC_MIXED)):
         q = p.copy()
         q.p_precision = prec
+        if prec == cap.PREC_MIXED and tuned is not None:
+            for k, v in tuned["params"].items():
+                setattr(q, k, v)
         s = pkg.Solver(q)
+        if prec == cap.PREC_MIXED and tuned is not None:
+            import ctypes
+            launch = cap.Launch(**tuned["launch"])
+            assert s.lib.covof_set_launch(s.h, ctypes.byref(launch)) == cap.OK
         stream = torch.cuda.ExternalStream(s.stream_ptr, device=dev)
         for _ in range(args.warmup):
             tp.zero_()
@@ -410,6 +431,9 @@ def run_ours(args, world, rank, local):
                            "iters": it_f, "kernel_ms": results["fp64"]["kernel_ms"],
                            "achieved_gbs": achieved64},
             "mixed": {"inner_steps_fp32": it_m, "outer_fcg_iters": mixed["outer"], "kernel_ms": mixed["kernel_ms"]},
+            "autotune": None if tuned is None else {
+                "launch": tuned["launch"], "params": tuned["params"], "candidates": tuned["candidates"],
+                "tuned_ms": tuned["ms"], "rule_ms": tuned["rule_ms"]},
             "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
@@ -444,6 +468,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true", help="profiling runs: no CPU baseline")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: no host-API leg")
     ap.add_argument("--skip-steps", action="store_true", help="profiling runs: no rising-bubble time steps")
+    ap.add_argument("--no-tune", action="store_true", help="mixed solve with the built-in launch rules")
+    ap.add_argument("--tune-budget", type=float, default=45.0, help="seconds for the autotuner")
     args = ap.parse_args()
     if args.impl == "reference":
         world = int(os.environ.get("WORLD_SIZE", "1"))

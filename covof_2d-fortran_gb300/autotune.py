@@ -63,12 +63,15 @@ def candidates(p: Params, sm_count: int) -> list[tuple[dict, dict]]:
         for t in (128, 256, 512, 1024):
             out.append(({"p_threads": t, "p_blocks": 0, "p_inner_form": 0}, {}))
         return out
+    # most promising first (a time budget may cut the list): shared-memory
+    # strips on every SM, then higher degrees and narrower intervals, which
+    # trade FP64 outer iterations for cheap FP32 inner steps
     blocks = sorted({min(sm_count, p.ny), max(1, min(sm_count, p.ny) // 2)}, reverse=True)
     forms = (1, 2) if p.p_inner_kind != capi.INNER_CG else (0,)
     for form in forms:
         for nb in blocks:
-            for m in (16, 24, 32, 48):
-                for lo in (5.0e-4, 1.0e-3, 2.0e-3):
+            for m in (48, 64, 32, 96, 24, 16):
+                for lo in (5.0e-4, 2.5e-4, 1.0e-3, 2.0e-3):
                     out.append(({"p_threads": 0, "p_blocks": nb, "p_inner_form": form},
                                 {"p_inner_max_iter": m, "p_cheb_lo": lo}))
     return out
@@ -97,6 +100,10 @@ def tune(p: Params, dt: float, b, rho_u, rho_v, repeats: int = 2, cache_path: Pa
     by_params: dict[tuple, list] = {}
     for launch, over in candidates(p, sm):
         by_params.setdefault(tuple(sorted(over.items())), []).append(launch)
+    # the rule's own settings are always timed (the reference point)
+    rule_key = tuple(sorted({"p_inner_max_iter": p.p_inner_max_iter, "p_cheb_lo": p.p_cheb_lo}.items()))
+    if p.p_precision != capi.PREC_FP64 and rule_key in by_params:
+        by_params = {rule_key: by_params.pop(rule_key), **by_params}
     for over_t, launches in by_params.items():
         q = p.copy()
         for k, v in over_t:
@@ -119,7 +126,7 @@ def tune(p: Params, dt: float, b, rho_u, rho_v, repeats: int = 2, cache_path: Pa
                 if best is None:
                     continue
                 rec = {"ms": best, "launch": _get_launch(s), "params": dict(over_t), "iters": it,
-                       "outer": s.last_refine_steps()}
+                       "outer": s.last_refine_steps(), "t": round(time.perf_counter() - t_start, 2)}
                 results.append(rec)
                 if verbose:
                     print(json.dumps(rec), flush=True)
