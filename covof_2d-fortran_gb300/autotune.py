@@ -67,13 +67,20 @@ def candidates(p: Params, sm_count: int) -> list[tuple[dict, dict]]:
     # strips on every SM, then higher degrees and narrower intervals, which
     # trade FP64 outer iterations for cheap FP32 inner steps
     blocks = sorted({min(sm_count, p.ny), max(1, min(sm_count, p.ny) // 2)}, reverse=True)
-    forms = (1, 2) if p.p_inner_kind != capi.INNER_CG else (0,)
-    for form in forms:
-        for nb in blocks:
-            for m in (48, 64, 32, 96, 24, 16):
-                for lo in (5.0e-4, 2.5e-4, 1.0e-3, 2.0e-3):
-                    out.append(({"p_threads": 0, "p_blocks": nb, "p_inner_form": form},
-                                {"p_inner_max_iter": m, "p_cheb_lo": lo}))
+    shapes = []
+    if p.p_inner_kind == capi.INNER_CHEBYSHEV:
+        # one thread-block cluster (small meshes; covof_set_launch refuses
+        # the sizes that do not fit)
+        shapes += [(3, g) for g in (16, 8, 4) if g <= p.ny]
+    if p.p_inner_kind != capi.INNER_CG:
+        shapes += [(1, nb) for nb in blocks] + [(2, nb) for nb in blocks]
+    else:
+        shapes += [(0, nb) for nb in blocks]
+    for form, nb in shapes:
+        for m in (48, 64, 32, 96, 24, 16):
+            for lo in (5.0e-4, 2.5e-4, 1.0e-3, 2.0e-3):
+                out.append(({"p_threads": 0, "p_blocks": nb, "p_inner_form": form},
+                            {"p_inner_max_iter": m, "p_cheb_lo": lo}))
     return out
 
 
@@ -109,7 +116,11 @@ def tune(p: Params, dt: float, b, rho_u, rho_v, repeats: int = 2, cache_path: Pa
         for k, v in over_t:
             setattr(q, k, v)
         with Solver(q) as s:
+            rule_launch = _get_launch(s) if over_t == rule_key else None
+            if rule_launch is not None:
+                launches = [dict(rule_launch, rule=True)] + launches
             for launch in launches:
+                is_rule = bool(launch.pop("rule", False)) if isinstance(launch, dict) else False
                 if time.perf_counter() - t_start > budget_s:
                     break
                 if _set_launch(s, launch) != capi.OK:
@@ -126,7 +137,8 @@ def tune(p: Params, dt: float, b, rho_u, rho_v, repeats: int = 2, cache_path: Pa
                 if best is None:
                     continue
                 rec = {"ms": best, "launch": _get_launch(s), "params": dict(over_t), "iters": it,
-                       "outer": s.last_refine_steps(), "t": round(time.perf_counter() - t_start, 2)}
+                       "outer": s.last_refine_steps(), "t": round(time.perf_counter() - t_start, 2),
+                       "rule": is_rule}
                 results.append(rec)
                 if verbose:
                     print(json.dumps(rec), flush=True)
@@ -149,7 +161,7 @@ def _is_rule(r: dict, p: Params, sm: int) -> bool:
         return False
     return (r["params"].get("p_inner_max_iter") == p.p_inner_max_iter
             and r["params"].get("p_cheb_lo") == p.p_cheb_lo
-            and r["launch"]["p_blocks"] == min(sm, p.ny))
+            and r.get("rule", False))
 
 
 def apply(p: Params, cache_path: Path = DEFAULT_CACHE):

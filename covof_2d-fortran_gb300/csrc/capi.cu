@@ -153,6 +153,29 @@ int launch_coop(covof_handle* h, const void* fn, int nblocks, int threads, void*
   return COVOF_OK;
 }
 
+// One thread-block cluster of nblocks CTAs (all co-scheduled by the hardware).
+int launch_cluster(covof_handle* h, const void* fn, int nblocks, int threads, void** args, bool timed,
+                   size_t smem) {
+  CK(cudaMemsetAsync(h->bar, 0, (size_t)(64 + h->sm_count) * sizeof(unsigned int), h->stream));
+  CK(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
+  if (timed) CK(cudaEventRecord(h->ev0, h->stream));
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = nblocks;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblocks);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = h->stream;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  CK(cudaLaunchKernelExC(&cfg, fn, args));
+  if (timed) CK(cudaEventRecord(h->ev1, h->stream));
+  return COVOF_OK;
+}
+
 int h2d(covof_handle* h, double* d, const double* s, size_t n) {
   if (!s) return COVOF_INVALID;
   CK(cudaMemcpyAsync(d, s, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
@@ -202,6 +225,46 @@ int poisson_plan(covof_handle* h) {
   const int threads = mixed ? kPoissonThreads : (L.p_threads ? L.p_threads : fp64_threads(h));
   long long units = (long long)make_tiles(h->D, threads).ntiles;
   size_t smem = 0;
+  h->p_cluster = false;
+  if (mixed && P.p_inner_kind == COVOF_INNER_CHEBYSHEV && L.p_inner_form == 3) {
+    // the whole inner state in one thread-block cluster (asked for by the
+    // launch override: measured no faster than strips on every SM for the
+    // meshes that fit, so the rules do not pick it)
+    int G = L.p_blocks > 0 ? L.p_blocks : 16;
+    if (G > P.ny) G = P.ny;
+    const int Rmax = (P.ny + G - 1) / G;
+    const size_t bytes = smem_cheb_bytes(P.nx, Rmax);
+    const void* cfn = (const void*)k_pcg_mixed_cluster;
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+    cudaFuncAttributes fa;
+    bool fits = G >= 1 && G <= 16 && cudaFuncGetAttributes(&fa, cfn) == cudaSuccess &&
+                bytes + fa.sharedSizeBytes <= (size_t)optin &&
+                cudaFuncSetAttribute(cfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess &&
+                (G <= 8 || cudaFuncSetAttribute(cfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess);
+    if (fits) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = G; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3(G); cfg.blockDim = dim3(kPoissonThreads); cfg.dynamicSmemBytes = bytes;
+      cfg.attrs = at; cfg.numAttrs = 1;
+      int nclusters = 0;
+      fits = cudaOccupancyMaxActiveClusters(&nclusters, cfn, &cfg) == cudaSuccess && nclusters >= 1 &&
+             G <= h->part_blocks;
+    }
+    cudaGetLastError();
+    if (fits) {
+      h->p_fn = cfn;
+      h->p_smem = bytes;
+      h->p_nb = G;
+      h->p_threads = kPoissonThreads;
+      h->p_cluster = true;
+      h->have_pplan = true;
+      return COVOF_OK;
+    }
+    return COVOF_UNSUPPORTED;  // the cluster asked for does not fit
+  }
   if (mixed) {
     // one row strip per block, at most one block per SM
     int G = P.ny < h->sm_count ? P.ny : h->sm_count;
@@ -291,7 +354,8 @@ int poisson_enqueue(covof_handle* h, double dt, const double* u, const double* v
   PoissonArgs a;
   CS(pois_pre(h, dt, u, v, b, rho_u, rho_v, p, &a));
   void* args[] = {&a};
-  CS(launch_coop(h, h->p_fn, h->p_nb, h->p_threads, args, timed, h->p_smem));
+  if (h->p_cluster) CS(launch_cluster(h, h->p_fn, h->p_nb, h->p_threads, args, timed, h->p_smem));
+  else CS(launch_coop(h, h->p_fn, h->p_nb, h->p_threads, args, timed, h->p_smem));
   return pois_post(h, p);
 }
 
@@ -1192,7 +1256,8 @@ int covof_set_launch(covof_handle* h, const covof_launch* launch) {
   const covof_launch& L = *launch;
   if (L.p_threads != 0 && L.p_threads != 128 && L.p_threads != 256 && L.p_threads != 512 && L.p_threads != 1024)
     return COVOF_INVALID;
-  if (L.p_blocks < 0 || L.p_blocks > h->sm_count || L.p_inner_form < 0 || L.p_inner_form > 2)
+  if (L.p_blocks < 0 || L.p_blocks > h->sm_count || L.p_inner_form < 0 || L.p_inner_form > 3 ||
+      (L.p_inner_form == 3 && L.p_blocks > 16))
     return COVOF_INVALID;
   if (h->stream) cudaStreamSynchronize(h->stream);
   const covof_launch keep = h->launch;
@@ -1214,7 +1279,8 @@ int covof_get_launch(covof_handle* h, covof_launch* launch) {
   launch->p_threads = h->p_threads;
   launch->p_blocks = h->p_nb;
   launch->p_inner_form = h->p_fn == (const void*)k_pcg_mixed_cheb ? 1
-                       : h->p_fn == (const void*)k_pcg_mixed_stream ? 2 : 0;
+                       : h->p_fn == (const void*)k_pcg_mixed_stream ? 2
+                       : h->p_fn == (const void*)k_pcg_mixed_cluster ? 3 : 0;
   return COVOF_OK;
 }
 

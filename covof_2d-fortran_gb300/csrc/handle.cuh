@@ -110,6 +110,7 @@ struct covof_handle {
   const void* p_fn = nullptr;
   size_t p_smem = 0;
   int p_nb = 0, p_threads = 0;
+  bool p_cluster = false;  // the plan is one thread-block cluster (k_pcg_mixed_cluster)
   bool have_mplan = false;
   const void* m_fn = nullptr;
   int m_nb = 0;

@@ -1051,6 +1051,202 @@ __device__ void mixed_stream_case(const PoissonArgs& a, const Team& tm, GridRedu
   fcg_mixed(a, own, in, R);
 }
 
+// ---------------------------------------------------------------------------
+// Cluster-resident form for small meshes: the whole FP32 inner state lives in
+// the shared memory of one thread-block cluster (up to 16 CTAs, one row strip
+// each), and neighbours read each other's boundary rows of the direction
+// through distributed shared memory instead of global memory and publish
+// counters.  One cluster-wide barrier per inner step, a software barrier on a
+// counter in CTA 0's shared memory with a bounded wait; the hardware cluster
+// barrier is used only at entry (every CTA's shared memory exists before any
+// remote access) and just before exit (no CTA leaves while a peer may still
+// read its shared memory), and every CTA reaches both because every loop and
+// wait in between is bounded.
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_hw_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// shared::cluster address of the variable at local shared address a in CTA rank
+__device__ __forceinline__ unsigned map_rank(const void* local, unsigned rank) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(local);
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float ld_cluster_f32(unsigned addr) {
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_cluster_add_release(unsigned addr, unsigned v) {
+  asm volatile("red.release.cluster.shared::cluster.add.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_cluster_acquire_u32(unsigned addr) {
+  unsigned v;
+  asm volatile("ld.acquire.cluster.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+  return v;
+}
+
+// Layout (floats, W = nx+2, every CTA laid out for Rmax rows so that a
+// neighbour's arrays sit at the same offsets): y, r [Rmax*W]; d, dn
+// [(Rmax+2)*W] (halo rows 0 and R+1); ax [Rmax*W]; ay [(Rmax+1)*W].
+struct ClusterCheby {
+  Dims D; int r0, R, Rs, W, b, G, pinned_c, m;  // Rs: rows of the south neighbour
+  double lo;
+  float2* tab;
+  float *ys, *r, *d, *dn, *ax, *ay;
+  unsigned bar0;        // shared::cluster address of the barrier counter in CTA 0
+  unsigned epoch;
+  int* err;
+  __device__ __forceinline__ double cheb_theta() const { return 0.5 * (2.0 + 2.0 * lo); }
+  __device__ __forceinline__ double cheb_delta() const { return 0.5 * (2.0 - 2.0 * lo); }
+  __device__ void load_coeffs(const float* __restrict__ ax32, const float* __restrict__ ay32, int Rmax) {
+    for (int e = threadIdx.x; e < R * W; e += blockDim.x) {
+      const int row = e / W, col = e - row * W;
+      ax[e] = (col >= 1) ? ax32[D.id(col, r0 + row)] : 0.0f;
+    }
+    for (int e = threadIdx.x; e < (R + 1) * W; e += blockDim.x) {
+      const int row = e / W, col = e - row * W;
+      ay[e] = (col >= 1 && col <= D.nx) ? ay32[D.id(col, r0 + row)] : 0.0f;
+    }
+    for (int e = threadIdx.x; e < (Rmax + 2) * W; e += blockDim.x) { d[e] = 0.0f; dn[e] = 0.0f; }
+    if (threadIdx.x == 0) {
+      const double sigma1 = cheb_theta() / cheb_delta(), delta = cheb_delta();
+      double rho = 1.0 / sigma1, r1;
+      for (int k = 0; k < kChebTab; ++k) {
+        r1 = 1.0 / (2.0 * sigma1 - rho);
+        tab[k] = make_float2((float)(r1 * rho), (float)(2.0 * r1 / delta));
+        rho = r1;
+      }
+    }
+    __syncthreads();
+  }
+  __device__ __forceinline__ void set_rhs(int, int c, float v) {
+    const int row = c / D.nx, col = c - row * D.nx + 1;
+    r[row * W + col] = v;
+    ys[row * W + col] = 0.0f;
+  }
+  __device__ __forceinline__ float y(int, int c) const {
+    const int row = c / D.nx, col = c - row * D.nx + 1;
+    return ys[row * W + col];
+  }
+  // cluster-wide barrier with a bounded wait (false: gave up, error recorded)
+  __device__ __forceinline__ bool csync() {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int ok = 1;
+      red_cluster_add_release(bar0, 1u);
+      const unsigned target = (epoch + 1u) * (unsigned)G;
+      long long spins = 0;
+      while ((int)(ld_cluster_acquire_u32(bar0) - target) < 0)
+        if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+      s_ok = ok;
+    }
+    ++epoch;
+    __syncthreads();
+    return s_ok != 0;
+  }
+  // halo rows of the current direction from the neighbours' shared memory:
+  // row 0 <- south neighbour's last row, row R+1 <- north neighbour's row 1
+  __device__ __forceinline__ void halo() {
+    const unsigned sS = b > 0 ? map_rank(d + Rs * W, (unsigned)(b - 1)) : 0u;
+    const unsigned sN = b < G - 1 ? map_rank(d + W, (unsigned)(b + 1)) : 0u;
+    for (int col = threadIdx.x + 1; col <= D.nx; col += blockDim.x) {
+      d[col] = b > 0 ? ld_cluster_f32(sS + 4u * (unsigned)col) : 0.0f;
+      d[(R + 1) * W + col] = b < G - 1 ? ld_cluster_f32(sN + 4u * (unsigned)col) : 0.0f;
+    }
+    __syncthreads();
+  }
+  __device__ PcgOut solve(GridReducer&, double, int budget) {
+    PcgOut o{0, COVOF_OK, 0.0, 1.0, true};
+    const int n = R * D.nx, nx = D.nx;
+    const int mm = m < kChebTab ? m : kChebTab;
+    const int steps = budget < mm ? budget : mm;
+    const int row0 = (int)threadIdx.x / nx, col0 = (int)threadIdx.x - row0 * nx + 1;
+    const int drow = (int)blockDim.x / nx, dcol = (int)blockDim.x - drow * nx;
+    const float it0 = (float)(1.0 / cheb_theta());
+    {
+      int row = row0, col = col0;
+      for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        d[(row + 1) * W + col] = r[row * W + col] * it0;
+        row += drow; col += dcol;
+        if (col > nx) { col -= nx; ++row; }
+      }
+    }
+    if (!csync()) { o.ok = false; o.status = COVOF_TIMEOUT; return o; }
+    halo();
+    for (int k = 0; k < steps; ++k) {
+      const bool last = (k + 1 == steps);
+      const float2 cc = tab[k];
+      int row = row0, col = col0;
+      for (int c = threadIdx.x; c < n; c += blockDim.x, row += drow, col += dcol) {
+        if (col > nx) { col -= nx; ++row; }
+        const int q = (row + 1) * W + col, e = row * W + col;
+        const float dc = d[q];
+        float v = dc;
+        v = __fmaf_rn(-ax[e], d[q - 1], v);
+        v = __fmaf_rn(-ax[e + 1], d[q + 1], v);
+        v = __fmaf_rn(-ay[e], d[q - W], v);
+        v = __fmaf_rn(-ay[e + W], d[q + W], v);
+        if (c == pinned_c) v = 0.0f;
+        ys[e] += dc;
+        const float rn = r[e] - v;
+        r[e] = rn;
+        if (!last) dn[q] = __fmaf_rn(cc.x, dc, cc.y * rn);
+      }
+      o.iters++;
+      if (last) break;
+      float* t = d; d = dn; dn = t;
+      // every CTA has written its part of the new direction before any CTA
+      // reads halo rows of it; a CTA overwrites a buffer only after the next
+      // barrier, i.e. after every neighbour finished reading it
+      if (!csync()) { o.ok = false; o.status = COVOF_TIMEOUT; break; }
+      halo();
+    }
+    __syncthreads();
+    return o;
+  }
+};
+
+__global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cluster(PoissonArgs a) {
+  extern __shared__ float smem[];
+  __shared__ float2 cheb_tab[kChebTab];
+  __shared__ unsigned cbar;
+  const Dims D = a.D;
+  const Team tm{(int)cluster_rank(), (int)gridDim.x};  // the grid is one cluster
+  if (threadIdx.x == 0) cbar = 0u;
+  cluster_hw_sync();  // every CTA's shared memory is live and cbar is zero
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  int r0, Rr, Rs = 0, rs0;
+  strip_rows(D.ny, tm.size, tm.rank, r0, Rr);
+  if (tm.rank > 0) strip_rows(D.ny, tm.size, tm.rank - 1, rs0, Rs);
+  const int Rmax = (D.ny + tm.size - 1) / tm.size;
+  const int W = D.nx + 2;
+  StripOwn own{D, r0, Rr};
+  ClusterCheby in;
+  in.D = D; in.r0 = r0; in.R = Rr; in.Rs = Rs; in.W = W; in.b = tm.rank; in.G = tm.size;
+  in.pinned_c = (a.pinned && tm.rank == 0) ? 0 : -1;
+  in.m = a.inner_max_iter; in.lo = a.cheb_lo; in.tab = cheb_tab;
+  float* s = smem;
+  in.ys = s; s += Rmax * W;
+  in.r = s; s += Rmax * W;
+  in.d = s; s += (Rmax + 2) * W;
+  in.dn = s; s += (Rmax + 2) * W;
+  in.ax = s; s += Rmax * W;
+  in.ay = s; s += (Rmax + 1) * W;
+  in.bar0 = map_rank(&cbar, 0u);
+  in.epoch = 0u;
+  in.err = a.err;
+  in.load_coeffs(a.ax32, a.ay32, Rmax);
+  fcg_mixed(a, own, in, R);
+  cluster_hw_sync();  // no CTA leaves while a peer may still read its shared memory
+}
+
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_stream(PoissonArgs a) {
   __shared__ float2 cheb_tab[kChebTab];
   const Team tm = grid_team();

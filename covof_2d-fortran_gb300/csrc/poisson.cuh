@@ -54,6 +54,7 @@ __global__ void k_pcg_mixed(PoissonArgs a);
 __global__ void k_pcg_mixed_smem(PoissonArgs a);
 __global__ void k_pcg_mixed_cheb(PoissonArgs a);
 __global__ void k_pcg_mixed_stream(PoissonArgs a);
+__global__ void k_pcg_mixed_cluster(PoissonArgs a);
 __global__ void k_pcg_fp64_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_smem_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);

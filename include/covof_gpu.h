@@ -96,8 +96,10 @@ typedef struct covof_params {
   int recon;             /* COVOF_RECON_* */
   /* MIXED inner preconditioner: COVOF_INNER_CHEBYSHEV (degree p_inner_max_iter,
    * at most 128, on [p_cheb_lo * 2, 2], no inner reductions; its state lives
-   * in shared memory when a row strip per SM fits, else it streams through
-   * L2/HBM), COVOF_INNER_CHEBYSHEV_STREAM (the streaming form always) or
+   * in shared-memory row strips on every SM when a strip fits, else it
+   * streams through L2/HBM; covof_set_launch can place it in one
+   * thread-block cluster instead), COVOF_INNER_CHEBYSHEV_STREAM (the
+   * streaming form always) or
    * COVOF_INNER_CG (Jacobi-PCG, at most p_inner_max_iter iterations or
    * p_inner_tol reduction). */
   int p_inner_kind;
@@ -321,7 +323,9 @@ int covof_run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run
 typedef struct covof_launch {
   int p_threads;     /* plain FP64 PCG: threads per block, 128, 256, 512 or 1024 */
   int p_blocks;      /* blocks of the persistent solve (mixed: row strips), at most one per SM */
-  int p_inner_form;  /* mixed Chebyshev inner state: 1 shared-memory strips, 2 streamed */
+  int p_inner_form;  /* mixed Chebyshev inner state: 1 shared-memory strips on every SM,
+                      * 2 streamed through L2 / HBM, 3 one thread-block cluster of p_blocks
+                      * (<= 16) CTAs exchanging rows through distributed shared memory */
 } covof_launch;
 /* Set the overrides (validated: COVOF_INVALID for out-of-range values,
  * COVOF_UNSUPPORTED for shared-memory strips that do not fit); drops the

@@ -20,7 +20,7 @@ def test_candidates_cover_shapes(pkg, at):
     assert {d["p_threads"] for d, _ in c64} == {128, 256, 512, 1024}
     p.p_precision = pkg.capi.PREC_MIXED
     cm = at.candidates(p, 152)
-    assert {d["p_inner_form"] for d, _ in cm} == {1, 2}
+    assert {d["p_inner_form"] for d, _ in cm} == {1, 2, 3}
     assert {o["p_inner_max_iter"] for _, o in cm} == {16, 24, 32, 48, 64, 96}
     assert all(1 <= d["p_blocks"] <= 152 for d, _ in cm)
 

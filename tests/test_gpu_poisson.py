@@ -22,7 +22,7 @@ def test_operator_is_bit_identical(gpu_pkg, orc):
 
 
 @pytest.mark.parametrize("gauge", ["pinned", "reference"])
-@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_stream", "mixed_cg"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_strips", "mixed_cluster16", "mixed_cluster4", "mixed_stream", "mixed_cg"])
 @pytest.mark.parametrize("n", [64, 128])
 def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
     pkg = gpu_pkg
@@ -41,6 +41,16 @@ def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
         q.p_inner_kind = cap.INNER_CG
     x = np.zeros_like(b)
     with pkg.Solver(q) as s:
+        # "mixed" on these meshes is the strip form on every SM; the strip form
+        # and clusters of 16 and 4 CTAs are also selected explicitly
+        form = {"mixed_strips": (1, 0), "mixed_cluster16": (3, 16), "mixed_cluster4": (3, 4)}.get(prec)
+        if form:
+            import ctypes
+            L = cap.Launch(p_threads=0, p_blocks=form[1], p_inner_form=form[0])
+            assert s.lib.covof_set_launch(s.h, ctypes.byref(L)) == cap.OK
+            G = cap.Launch()
+            s.lib.covof_get_launch(s.h, ctypes.byref(G))
+            assert G.p_inner_form == form[0]
         it, rr, st = s.poisson_solve_rhs(dt, b, ru, rv, x)
     assert st == cap.OK
     assert rr <= 1e-12
