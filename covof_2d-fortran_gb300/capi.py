@@ -24,7 +24,7 @@ CONV_UPWIND, CONV_CENTERED = 1, 2
 RECON_PLIC, RECON_ELVIRA = 0, 1
 GAUGE_REFERENCE, GAUGE_PINNED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
-INNER_CHEBYSHEV, INNER_CG, INNER_CHEBYSHEV_STREAM = 0, 1, 2
+INNER_CHEBYSHEV, INNER_CG, INNER_CHEBYSHEV_STREAM, INNER_MG = 0, 1, 2, 3
 # resident fields (COVOF_FIELD_*), in header order; names follow the Fields dataclass
 FIELD_NAMES = ("u", "v", "p", "C", "rho", "rho_u", "rho_v", "mu", "mu_node", "fx_sigma",
                "fy_sigma", "curvature", "u_old", "v_old")
@@ -48,6 +48,7 @@ class Params(C.Structure):
         ("sigma", C.c_double), ("gx", C.c_double), ("gy", C.c_double),
         ("recon", C.c_int),
         ("p_inner_kind", C.c_int), ("p_cheb_lo", C.c_double),
+        ("p_mg_nu", C.c_int), ("p_mg_cw", C.c_double),
     ]
 
     def copy(self) -> "Params":

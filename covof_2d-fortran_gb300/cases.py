@@ -60,6 +60,8 @@ def make_params(nx: int, ny: int, lx: float, ly: float) -> Params:
     p.recon = capi.RECON_PLIC
     p.p_inner_kind = capi.INNER_CHEBYSHEV
     p.p_cheb_lo = 1.0e-3
+    p.p_mg_nu = 2
+    p.p_mg_cw = 1.0
     return p
 
 

@@ -368,7 +368,8 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
   for (int c = 0; c < ncases; ++c) {
     // one arithmetic per batch; the mixed batch uses the streaming inner form
     if ((cases[c].p_precision == COVOF_PREC_MIXED) != b->mixed) return fail(COVOF_INVALID);
-    if (b->mixed && cases[c].p_inner_kind == COVOF_INNER_CG) return fail(COVOF_UNSUPPORTED);
+    if (b->mixed && (cases[c].p_inner_kind == COVOF_INNER_CG || cases[c].p_inner_kind == COVOF_INNER_MG))
+      return fail(COVOF_UNSUPPORTED);
     if (cases[c].p_precond == COVOF_PRECOND_SSOR) return fail(COVOF_UNSUPPORTED);
     const int s = check_mom_params(cases[c]);
     if (s != COVOF_OK) return fail(s);

@@ -76,6 +76,28 @@ int ensure_poisson(covof_handle* h) {
   CS(dalloc(&h->pxb, (size_t)8 * h->sm_count * (size_t)(h->D.nx + 2)));
   CS(dalloc(&h->e32, g)); CS(dalloc(&h->r32b, g)); CS(dalloc(&h->r32, g)); CS(dalloc(&h->d32, g));
   CS(dalloc(&h->Ad32, g)); CS(dalloc(&h->ax32, g)); CS(dalloc(&h->ay32, g)); CS(dalloc(&h->aP32, g));
+  // multigrid levels: halve each dimension down to about 64 cells
+  MgHier& H = h->mg;
+  H.nl = 1;
+  H.lv[0].nx = h->D.nx; H.lv[0].ny = h->D.ny; H.lv[0].off = 0;
+  long long pool = 0;
+  while (H.nl < kMgMaxLevels && (long long)H.lv[H.nl - 1].nx * H.lv[H.nl - 1].ny > 64 &&
+         (H.lv[H.nl - 1].nx > 1 || H.lv[H.nl - 1].ny > 1)) {
+    MgLevel& c = H.lv[H.nl];
+    c.nx = (H.lv[H.nl - 1].nx + 1) / 2;
+    c.ny = (H.lv[H.nl - 1].ny + 1) / 2;
+    c.off = pool;
+    pool += 6LL * (c.nx + 2) * (c.ny + 2);
+    H.nl += 1;
+  }
+  H.tail = H.nl;
+  for (int l = 1; l < H.nl; ++l)
+    if ((long long)H.lv[l].nx * H.lv[l].ny <= 2048) { H.tail = l; break; }
+  H.omega = 0.8f;
+  H.nu = h->prm.p_mg_nu < 1 ? 1 : (h->prm.p_mg_nu > 8 ? 8 : h->prm.p_mg_nu);
+  H.cw = (float)(h->prm.p_mg_cw > 0.0 && h->prm.p_mg_cw <= 4.0 ? h->prm.p_mg_cw : 1.0);
+  H.nuc = 8;
+  if (pool > 0) CS(dalloc(&H.pool, (size_t)pool));
   h->have_poisson = true;
   return COVOF_OK;
 }
@@ -226,6 +248,20 @@ int poisson_plan(covof_handle* h) {
   long long units = (long long)make_tiles(h->D, threads).ntiles;
   size_t smem = 0;
   h->p_cluster = false;
+  if (mixed && P.p_inner_kind == COVOF_INNER_MG) {
+    // multigrid inner: one persistent block per SM, tile-owned outer
+    const void* mfn = (const void*)k_pcg_mixed_mg;
+    long long units = h->sm_count;
+    if (L.p_blocks > 0 && L.p_blocks < units) units = L.p_blocks;
+    const int nb = coop_blocks(h, mfn, kPoissonThreads, units, 0);
+    if (nb < 1) return COVOF_CUDA_ERROR;
+    h->p_fn = mfn;
+    h->p_smem = 0;
+    h->p_nb = nb;
+    h->p_threads = kPoissonThreads;
+    h->have_pplan = true;
+    return COVOF_OK;
+  }
   if (mixed && P.p_inner_kind == COVOF_INNER_CHEBYSHEV && L.p_inner_form == 3) {
     // the whole inner state in one thread-block cluster (asked for by the
     // launch override: measured no faster than strips on every SM for the
@@ -319,8 +355,8 @@ int pois_pre(covof_handle* h, double dt, const double* u, const double* v, const
                                                   b, pinned, h->pax, h->pay, h->paP, h->pb,
                                                   mixed ? h->pisd : nullptr, mixed ? nullptr : h->pinvD);
   if (mixed)
-    k_poisson_scale32<<<grid2(P.nx + 1, P.ny + 1, blk), blk, 0, h->stream>>>(h->D, h->pax, h->pay, h->pisd,
-                                                                           h->ax32, h->ay32, h->aP32);
+    k_poisson_scale32<<<grid2(P.nx + 1, P.ny + 1, blk), blk, 0, h->stream>>>(
+        h->D, h->pax, h->pay, h->pisd, h->ax32, h->ay32, h->aP32, h->paP, P.p_inner_kind == COVOF_INNER_MG ? 1 : 0);
   k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, p, h->px, pinned);
   CK(cudaGetLastError());
   PoissonArgs& a = *out;
@@ -336,6 +372,7 @@ int pois_pre(covof_handle* h, double dt, const double* u, const double* v, const
   a.tol = P.p_tol; a.inner_tol = P.p_inner_tol;
   a.max_iter = P.p_max_iter; a.inner_max_iter = P.p_inner_max_iter;
   a.max_refine = P.p_max_refine; a.pinned = pinned;
+  a.mg = h->mg;
   return COVOF_OK;
 }
 
@@ -812,6 +849,8 @@ void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly)
   p->recon = COVOF_RECON_PLIC;
   p->p_inner_kind = COVOF_INNER_CHEBYSHEV;
   p->p_cheb_lo = 1.0e-3;
+  p->p_mg_nu = 2;
+  p->p_mg_cw = 1.0;
 }
 
 int covof_abi_version(void) { return COVOF_ABI_VERSION; }
@@ -882,7 +921,7 @@ int covof_destroy(covof_handle* h) {
   for (float** q : ff) dfree(*q);
   drop_graphs(h);
   dfree(h->bar); dfree(h->err); dfree(h->d_pres); dfree(h->d_kres); dfree(h->d_run);
-  dfree(h->vlist); dfree(h->vcount);
+  dfree(h->vlist); dfree(h->vcount); dfree(h->mg.pool);
   if (h->h_pres) cudaFreeHost(h->h_pres);
   if (h->h_kres) cudaFreeHost(h->h_kres);
   if (h->h_run) cudaFreeHost(h->h_run);

@@ -78,6 +78,7 @@ struct covof_handle {
   float* pxb = nullptr;  // boundary-row exchange of the shared-memory inner solver
   float *e32 = nullptr, *r32b = nullptr, *r32 = nullptr, *d32 = nullptr, *d32b = nullptr, *Ad32 = nullptr,
         *ax32 = nullptr, *ay32 = nullptr, *aP32 = nullptr;
+  covof::MgHier mg{};  // multigrid hierarchy of the FP32 inner operator (pool: levels >= 1)
   // momentum scratch (each 2g)
   bool have_mom = false;
   double *mx = nullptr, *mrhs = nullptr, *mdiag = nullptr, *mv[7] = {};

@@ -79,13 +79,23 @@ __global__ void k_poisson_assemble(Dims D, double dt, double dx, double dy, int4
 // diagonal) for the mixed path: a face coefficient becomes
 // a_f / sqrt(aP_left aP_right).  Ghost entries of isd are zero, so an
 // outflow face (which only multiplies a zero ghost) gets a zero coefficient.
+// unscaled != 0: plain FP32 copy of the operator (the multigrid inner works on
+// A itself, whose near-null vector -- the constant -- its piecewise-constant
+// coarse spaces represent).
 __global__ void k_poisson_scale32(Dims D, const double* __restrict__ ax, const double* __restrict__ ay,
                                   const double* __restrict__ isd, float* __restrict__ ax32,
-                                  float* __restrict__ ay32, float* __restrict__ aP32) {
+                                  float* __restrict__ ay32, float* __restrict__ aP32,
+                                  const double* __restrict__ aP, int unscaled) {
   int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (i > D.nx + 1 || j > D.ny + 1) return;
   const int k = D.id(i, j);
+  if (unscaled) {
+    if (j <= D.ny) ax32[k] = (i <= D.nx) ? (float)ax[k] : 0.0f;
+    if (i <= D.nx) ay32[k] = (j <= D.ny) ? (float)ay[k] : 0.0f;
+    if (i <= D.nx && j <= D.ny) aP32[k] = (float)aP[k];
+    return;
+  }
   if (j <= D.ny) ax32[k] = (float)(ax[k] * isd[k - 1] * (i <= D.nx ? isd[k] : 0.0));
   if (i <= D.nx) ay32[k] = (float)(ay[k] * isd[k - D.P] * (j <= D.ny ? isd[k] : 0.0));
   if (i <= D.nx && j <= D.ny) aP32[k] = 1.0f;
@@ -465,6 +475,7 @@ struct StripOwn {
 // Inner FP32 solver on the streaming tiles: RHS and solution live in global
 // FP32 vectors.
 struct TiledInner {
+  static constexpr bool kScaled = true;
   Dims D; Tiles tl; Team tm; Sys<float> S; float* sd; int pinned;
   float* rhs;
   __device__ __forceinline__ void set_rhs(int k, int, float v) { S.x[k] = 0.0f; rhs[k] = v; }
@@ -481,6 +492,7 @@ struct TiledInner {
 // boundary rows of r and d travel through global memory (xb, double-buffered
 // by iteration parity), plus the reduction partials.
 struct SmemInner {
+  static constexpr bool kScaled = true;
   Dims D; int r0, R, W, b, G, pinned_c;
   float *ys, *r, *Ad, *d, *ax, *ay, *hr, *hd;
   float* xb;  // [2][G][2 sides][2 (r,d)][W]
@@ -619,6 +631,7 @@ struct SmemInner {
 constexpr int kChebTab = 128;  // precomputed Chebyshev step coefficients
 
 struct SmemCheby {
+  static constexpr bool kScaled = true;
   Dims D; int r0, R, W, b, G, pinned_c, m;
   double lo;
   float2* tab;            // [kChebTab] (c1, c2) of step k, in shared memory
@@ -771,6 +784,12 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
   // e = A 1 (interior ones, zero ghosts): the 1e-12*dvol shift of aP, the
   // eigenvalue of the constant vector in the reference gauge.
   auto ones_image = [&](int k) { return a.aP[k] - a.ax[k] - a.ax[k + 1] - a.ay[k] - a.ay[k + D.P]; };
+  // Inner solvers on the scaled operator S A S (S = D^-1/2) get S r and
+  // return y with z = S y, and deflate along the scaled near-null vector
+  // D^1/2 1, i.e. with weights aP; the multigrid inner works on A itself,
+  // whose near-null vector is the constant (weights 1, no scaling).
+  auto wgt = [&](int k) -> double { return Inner::kScaled ? a.aP[k] : 1.0; };
+  auto scl = [&](int k) -> double { return Inner::kScaled ? a.isd[k] : 1.0; };
   auto true_residual = [&]() -> bool {
     double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     own.each([&](int k, int c) {
@@ -779,7 +798,7 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       acc[0] = fma(a.b[k], a.b[k], acc[0]);
       acc[1] = fma(rr, rr, acc[1]);
       acc[2] += rr;
-      acc[3] += a.aP[k];
+      acc[3] += wgt(k);
       acc[4] += ones_image(k);
     });
     double t[5];
@@ -804,10 +823,10 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       continue;
     }
     if (outer >= a.max_refine || total_inner >= a.max_iter) { status = COVOF_MAXITER; break; }
-    const double cdef = a.pinned ? 0.0 : r_sum / aP_sum;
+    const double cdef = a.pinned ? 0.0 : r_sum / aP_sum;  // aP_sum: sum of the deflation weights
     const double scale = 1.0 / r_norm;
     own.each([&](int k, int c) {
-      inner.set_rhs(k, c, (k == pk) ? 0.0f : (float)((r[k] - cdef * a.aP[k]) * a.isd[k] * scale));
+      inner.set_rhs(k, c, (k == pk) ? 0.0f : (float)((r[k] - cdef * wgt(k)) * scl(k) * scale));
     });
     __syncthreads();
     int budget = a.max_iter - total_inner;
@@ -827,9 +846,9 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     // direction: beta = <z, q_old> / <p_old, q_old>.
     double zs[3] = {0.0, 0.0, 0.0};
     own.each([&](int k, int c) {
-      const double zk = (r_norm * a.isd[k]) * (double)inner.y(k, c);
+      const double zk = (r_norm * scl(k)) * (double)inner.y(k, c);
       z[k] = zk;
-      zs[0] = fma(a.aP[k], zk, zs[0]);
+      zs[0] = fma(wgt(k), zk, zs[0]);
       if (!fresh) {
         const double qk = qv[k];
         zs[1] = fma(zk, qk, zs[1]);
@@ -927,6 +946,7 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
 // only after its neighbours have published step k + 1, i.e. after they have
 // finished reading it.  Rows of other blocks are read through L2 (__ldcg).
 struct StreamCheby {
+  static constexpr bool kScaled = true;
   Dims D; int r0, R, b, G, pk, m;
   double lo;
   float2* tab;              // [kChebTab] (c1, c2) of step k, in shared memory
@@ -1095,6 +1115,7 @@ __device__ __forceinline__ unsigned ld_cluster_acquire_u32(unsigned addr) {
 // neighbour's arrays sit at the same offsets): y, r [Rmax*W]; d, dn
 // [(Rmax+2)*W] (halo rows 0 and R+1); ax [Rmax*W]; ay [(Rmax+1)*W].
 struct ClusterCheby {
+  static constexpr bool kScaled = true;
   Dims D; int r0, R, Rs, W, b, G, pinned_c, m;  // Rs: rows of the south neighbour
   double lo;
   float2* tab;
@@ -1245,6 +1266,234 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cluster(PoissonArgs a) {
   in.load_coeffs(a.ax32, a.ay32, Rmax);
   fcg_mixed(a, own, in, R);
   cluster_hw_sync();  // no CTA leaves while a peer may still read its shared memory
+}
+
+// ---------------------------------------------------------------------------
+// Geometric multigrid inner preconditioner (COVOF_INNER_MG): one V-cycle on
+// the scaled FP32 operator S A S per outer iteration.  Levels halve each
+// dimension (odd sizes keep a one-column tail); coarse operators are the
+// Galerkin products of piecewise-constant transfers: a coarse face
+// coefficient is the sum of the fine face coefficients it covers, a coarse
+// diagonal the sum of the aggregate's external faces.  Smoothing: damped
+// Jacobi (weight omega), nu sweeps before and after each coarse correction,
+// double-buffered; residual and restriction are fused; prolongation is
+// injection scaled by cw.  The V-cycle is symmetric (same sweeps down and
+// up, restriction = prolongation transposed), as the outer conjugate
+// recurrences need.  Levels of at most 2048 cells run in block 0 alone with
+// __syncthreads instead of grid barriers.
+struct MgLv {
+  int nx, ny, P;
+  float *xa, *xb, *b;
+  const float *ax, *ay, *dg;  // dg == nullptr: unit diagonal (level 0)
+  __device__ __forceinline__ int id(int i, int j) const { return j * P + i; }
+};
+
+struct MgInner {
+  static constexpr bool kScaled = false;
+  Team tm;
+  int pk;                  // pinned cell (level 0) or -1
+  MgHier H;
+  float *x0a, *x0b, *b0;   // level 0 solution buffers and right-hand side
+  const float *ax0, *ay0, *dg0;  // level 0: FP32 copy of A (faces, diagonal)
+  __device__ MgLv lv(int l) const {
+    MgLv L;
+    L.nx = H.lv[l].nx; L.ny = H.lv[l].ny; L.P = L.nx + 2;
+    if (l == 0) {
+      L.xa = x0a; L.xb = x0b; L.b = b0; L.ax = ax0; L.ay = ay0; L.dg = dg0;
+      return L;
+    }
+    const size_t g = (size_t)(L.nx + 2) * (size_t)(L.ny + 2);
+    float* base = H.pool + H.lv[l].off;
+    L.xa = base; L.xb = base + g; L.b = base + 2 * g;
+    L.ax = base + 3 * g; L.ay = base + 4 * g; L.dg = base + 5 * g;
+    return L;
+  }
+  // cells (i, j) of an ni x nj range, over the team or over block 0 alone
+  template <class F>
+  __device__ __forceinline__ void cells(int ni, int nj, bool local, F f) const {
+    const int n = ni * nj;
+    const int t0 = local ? (int)threadIdx.x : tm.rank * (int)blockDim.x + (int)threadIdx.x;
+    const int st = local ? (int)blockDim.x : tm.size * (int)blockDim.x;
+    for (int c = t0; c < n; c += st) {
+      const int j = c / ni, i = c - j * ni;
+      f(i + 1, j + 1);
+    }
+  }
+  __device__ __forceinline__ float apply(const MgLv& L, const float* x, int k) const {
+    const float d = L.dg ? L.dg[k] : 1.0f;
+    float v = d * __ldcg(x + k);
+    v = __fmaf_rn(-L.ax[k], __ldcg(x + k - 1), v);
+    v = __fmaf_rn(-L.ax[k + 1], __ldcg(x + k + 1), v);
+    v = __fmaf_rn(-L.ay[k], __ldcg(x + k - L.P), v);
+    v = __fmaf_rn(-L.ay[k + L.P], __ldcg(x + k + L.P), v);
+    return v;
+  }
+  // one damped Jacobi sweep from buffer cur into the other (first: x = 0)
+  __device__ void sweep(int l, bool first, bool local, int cur) const {
+    const MgLv L = lv(l);
+    const float* xs = cur ? L.xb : L.xa;
+    float* xd = cur ? L.xa : L.xb;
+    const float w = H.omega;
+    cells(L.nx, L.ny, local, [&](int i, int j) {
+      const int k = L.id(i, j);
+      const float d = L.dg ? L.dg[k] : 1.0f;
+      float v;
+      if (first) v = w * __ldcg(L.b + k) / d;
+      else v = __ldcg(xs + k) + w * (__ldcg(L.b + k) - apply(L, xs, k)) / d;
+      if (l == 0 && k == pk) v = 0.0f;
+      xd[k] = v;
+    });
+  }
+  // b_{l+1} = restriction of the residual of level l (buffer cur)
+  __device__ void restrict_(int l, bool local, int cur) const {
+    const MgLv F = lv(l), Cc = lv(l + 1);
+    const float* x = cur ? F.xb : F.xa;
+    cells(Cc.nx, Cc.ny, local, [&](int I, int J) {
+      float s = 0.0f;
+      for (int dj = 0; dj < 2; ++dj)
+        for (int di = 0; di < 2; ++di) {
+          const int i = 2 * I - 1 + di, j = 2 * J - 1 + dj;
+          if (i > F.nx || j > F.ny) continue;
+          const int k = F.id(i, j);
+          if (l == 0 && k == pk) continue;
+          s += __ldcg(F.b + k) - apply(F, x, k);
+        }
+      Cc.b[Cc.id(I, J)] = s;
+    });
+  }
+  // x_l (buffer cl) += cw * x_{l+1} (buffer cc) at the parent cell
+  __device__ void prolong(int l, bool local, int cl, int cc) const {
+    const MgLv F = lv(l), Cc = lv(l + 1);
+    float* x = cl ? F.xb : F.xa;
+    const float* xc = cc ? Cc.xb : Cc.xa;
+    const float cw = H.cw;
+    cells(F.nx, F.ny, local, [&](int i, int j) {
+      const int k = F.id(i, j);
+      if (l == 0 && k == pk) return;
+      x[k] = __ldcg(x + k) + cw * __ldcg(xc + Cc.id((i + 1) / 2, (j + 1) / 2));
+    });
+  }
+  // coarse operators of levels 1 .. nl-1 from the fine ones (once per solve)
+  __device__ bool setup(GridReducer& R) const {
+    for (int l = 1; l < H.nl; ++l) {
+      const MgLv F = lv(l - 1), Cc = lv(l);
+      float* cax = const_cast<float*>(Cc.ax);
+      float* cay = const_cast<float*>(Cc.ay);
+      float* cdg = const_cast<float*>(Cc.dg);
+      auto axf = [&](int i, int j) -> float { return (i <= F.nx + 1 && j <= F.ny) ? F.ax[F.id(i, j)] : 0.0f; };
+      auto ayf = [&](int i, int j) -> float { return (i <= F.nx && j <= F.ny + 1) ? F.ay[F.id(i, j)] : 0.0f; };
+      cells(Cc.nx + 1, Cc.ny + 1, false, [&](int I, int J) {
+        const int k = Cc.id(I, J);
+        if (J <= Cc.ny) cax[k] = axf(2 * I - 1, 2 * J - 1) + axf(2 * I - 1, 2 * J);
+        if (I <= Cc.nx) cay[k] = ayf(2 * I - 1, 2 * J - 1) + ayf(2 * I, 2 * J - 1);
+        if (I <= Cc.nx && J <= Cc.ny) {
+          // Galerkin: sum of the aggregate's diagonals minus twice its
+          // internal couplings (= its external faces plus its diagonal shifts)
+          auto dgf = [&](int i, int j) -> float {
+            return (i <= F.nx && j <= F.ny) ? (F.dg ? F.dg[F.id(i, j)] : 1.0f) : 0.0f;
+          };
+          const int i0 = 2 * I - 1, j0 = 2 * J - 1;
+          float d = dgf(i0, j0) + dgf(i0 + 1, j0) + dgf(i0, j0 + 1) + dgf(i0 + 1, j0 + 1);
+          float internal = 0.0f;
+          if (i0 + 1 <= F.nx) internal += axf(i0 + 1, j0) + axf(i0 + 1, j0 + 1);
+          if (j0 + 1 <= F.ny) internal += ayf(i0, j0 + 1) + ayf(i0 + 1, j0 + 1);
+          cdg[k] = d - 2.0f * internal;
+        }
+      });
+      if (!R.gs.sync()) return false;
+    }
+    return true;
+  }
+  __device__ __forceinline__ void set_rhs(int k, int, float v) { b0[k] = v; }
+  __device__ __forceinline__ float y(int k, int) const { return k == pk ? 0.0f : __ldcg(x0a + k); }
+  // levels lo .. nl-1 and back up to lo, block 0 alone (local) or the team
+  __device__ bool vcycle_part(GridReducer& R, int lo, bool local) const {
+    const int L = H.nl, nu = H.nu;
+    auto sync = [&]() -> bool {
+      if (local) { __syncthreads(); return true; }
+      return R.gs.sync();
+    };
+    for (int l = lo; l < L - 1; ++l) {
+      for (int s = 0; s < nu; ++s) {
+        if (s > 0 && !sync()) return false;
+        sweep(l, s == 0, local, s & 1);
+      }
+      if (!sync()) return false;
+      restrict_(l, local, nu & 1);
+      if (!sync()) return false;
+    }
+    for (int s = 0; s < H.nuc; ++s) {
+      if (s > 0 && !sync()) return false;
+      sweep(L - 1, s == 0, local, s & 1);
+    }
+    for (int l = L - 2; l >= lo; --l) {
+      if (!sync()) return false;
+      prolong(l, local, nu & 1, l + 1 == L - 1 ? (H.nuc & 1) : 0);
+      for (int s = 0; s < nu; ++s) {
+        if (!sync()) return false;
+        sweep(l, false, local, (nu + s) & 1);
+      }
+    }
+    return true;
+  }
+  __device__ PcgOut solve(GridReducer& R, double, int budget) {
+    PcgOut o{0, COVOF_OK, 0.0, 1.0, true};
+    if (budget < 1) return o;
+    const int L = H.nl, nu = H.nu, t = H.tail;
+    bool ok = R.gs.sync();  // right-hand side complete
+    if (t >= L) {
+      ok = ok && vcycle_part(R, 0, false);
+    } else {
+      // grid-wide levels 0 .. t-1 down, the tail in block 0, then back up
+      for (int l = 0; ok && l < t; ++l) {
+        for (int s = 0; ok && s < nu; ++s) {
+          if (s > 0) ok = R.gs.sync();
+          if (ok) sweep(l, s == 0, false, s & 1);
+        }
+        ok = ok && R.gs.sync();
+        if (ok) restrict_(l, false, nu & 1);
+        ok = ok && R.gs.sync();
+      }
+      if (ok && tm.rank == 0) {
+        const bool tail_ok = vcycle_part(R, t, true);
+        __syncthreads();
+        (void)tail_ok;  // block-local steps have no waits that can give up
+      }
+      ok = ok && R.gs.sync();
+      for (int l = t - 1; ok && l >= 0; --l) {
+        prolong(l, false, nu & 1, l + 1 == L - 1 ? (H.nuc & 1) : 0);
+        for (int s = 0; ok && s < nu; ++s) {
+          ok = R.gs.sync();
+          if (ok) sweep(l, false, false, (nu + s) & 1);
+        }
+        ok = ok && R.gs.sync();
+      }
+    }
+    if (t >= L) ok = ok && R.gs.sync();
+    o.iters = 1;
+    if (!ok) { o.ok = false; o.status = COVOF_TIMEOUT; }
+    return o;
+  }
+};
+
+__global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg(PoissonArgs a) {
+  const Dims D = a.D;
+  const Tiles tl = make_tiles(D, blockDim.x);
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  TileOwn own{D, tl, tm};
+  MgInner in;
+  in.tm = tm;
+  in.pk = a.pinned ? D.P + 1 : -1;
+  in.H = a.mg;
+  in.x0a = a.e32; in.x0b = a.d32; in.b0 = a.r32; in.ax0 = a.ax32; in.ay0 = a.ay32; in.dg0 = a.aP32;
+  if (!in.setup(R)) {
+    if (tm.rank == 0 && threadIdx.x == 0) {
+      a.res->iters = 0; a.res->relres = 1.0; a.res->status = COVOF_TIMEOUT; a.res->outer = 0;
+    }
+    return;
+  }
+  fcg_mixed(a, own, in, R);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_stream(PoissonArgs a) {

@@ -12,6 +12,25 @@ struct PcgResult {
   double relres;  // ||r||/||b|| at exit (mixed: true FP64 residual)
 };
 
+// Geometric multigrid hierarchy of the mixed path's FP32 inner operator
+// (levels 1 .. nl-1; level 0 is the scaled fine operator itself).  Level l
+// owns 7 arrays of (nx+2)*(ny+2) floats at pool + off: two solution buffers,
+// right-hand side, west / south face coefficients, diagonal, scratch.
+constexpr int kMgMaxLevels = 16;
+struct MgLevel {
+  int nx, ny;
+  long long off;
+};
+struct MgHier {
+  MgLevel lv[kMgMaxLevels];
+  int nl;      // levels including level 0
+  int tail;    // first level run by block 0 alone (<= 2048 cells), nl if none
+  float* pool;
+  float omega; // Jacobi weight
+  float cw;    // coarse-correction weight
+  int nu, nuc; // sweeps before / after each coarse correction; sweeps on the coarsest level
+};
+
 struct PoissonArgs {
   Dims D;
   // FP64 system
@@ -25,6 +44,7 @@ struct PoissonArgs {
   // FP32 inner system (mixed)
   float* e32; float* r32b; float* r32; float* d32; float* d32b; float* Ad32;
   const float* ax32; const float* ay32; const float* aP32;
+  MgHier mg;  // COVOF_INNER_MG
   // control
   unsigned int* bar; int* err; double* part;  // part: 16 * nblocks doubles
   PcgResult* res;
@@ -42,7 +62,8 @@ __global__ void k_poisson_assemble(Dims D, double dt, double dx, double dy, int4
                                    double* __restrict__ isd, double* __restrict__ invD);
 __global__ void k_poisson_scale32(Dims D, const double* __restrict__ ax, const double* __restrict__ ay,
                                   const double* __restrict__ isd, float* __restrict__ ax32,
-                                  float* __restrict__ ay32, float* __restrict__ aP32);
+                                  float* __restrict__ ay32, float* __restrict__ aP32,
+                                  const double* __restrict__ aP, int unscaled);
 __global__ void k_copy_interior(Dims D, const double* __restrict__ src, double* __restrict__ dst,
                                 int zero_pin);
 struct Tiles {
@@ -55,6 +76,7 @@ __global__ void k_pcg_mixed_smem(PoissonArgs a);
 __global__ void k_pcg_mixed_cheb(PoissonArgs a);
 __global__ void k_pcg_mixed_stream(PoissonArgs a);
 __global__ void k_pcg_mixed_cluster(PoissonArgs a);
+__global__ void k_pcg_mixed_mg(PoissonArgs a);
 __global__ void k_pcg_fp64_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_smem_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);

@@ -51,6 +51,8 @@ module covof_gpu_bridge
      integer(c_int) :: recon
      integer(c_int) :: p_inner_kind
      real(c_double) :: p_cheb_lo
+     integer(c_int) :: p_mg_nu
+     real(c_double) :: p_mg_cw
   end type covof_params_t
 
   integer(c_int), parameter :: COVOF_OK = 0, COVOF_MAXITER = 1, COVOF_BREAKDOWN = 2

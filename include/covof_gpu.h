@@ -99,13 +99,17 @@ typedef struct covof_params {
    * in shared-memory row strips on every SM when a strip fits, else it
    * streams through L2/HBM; covof_set_launch can place it in one
    * thread-block cluster instead), COVOF_INNER_CHEBYSHEV_STREAM (the
-   * streaming form always) or
+   * streaming form always), COVOF_INNER_MG (one geometric multigrid V-cycle
+   * per outer iteration: Galerkin piecewise-constant coarsening, damped
+   * Jacobi smoothing; p_max_iter then counts V-cycles) or
    * COVOF_INNER_CG (Jacobi-PCG, at most p_inner_max_iter iterations or
    * p_inner_tol reduction). */
   int p_inner_kind;
   double p_cheb_lo;      /* lower end of the Chebyshev interval, as a fraction of 2 */
+  int p_mg_nu;           /* COVOF_INNER_MG: Jacobi sweeps before and after each coarse correction (1-8) */
+  double p_mg_cw;        /* COVOF_INNER_MG: coarse-correction weight (0, 4] */
 } covof_params;
-enum { COVOF_INNER_CHEBYSHEV = 0, COVOF_INNER_CG = 1, COVOF_INNER_CHEBYSHEV_STREAM = 2 };
+enum { COVOF_INNER_CHEBYSHEV = 0, COVOF_INNER_CG = 1, COVOF_INNER_CHEBYSHEV_STREAM = 2, COVOF_INNER_MG = 3 };
 
 typedef struct covof_handle covof_handle;
 
@@ -346,7 +350,8 @@ int covof_get_launch(covof_handle* h, covof_launch* launch);
  * batch runs the Chebyshev inner iteration with each case's state in
  * shared-memory row strips of a team sized to fit (at most 32 blocks), or
  * streamed through L2 / HBM when a case does not fit or any case asks for
- * COVOF_INNER_CHEBYSHEV_STREAM; COVOF_INNER_CG is rejected.  The
+ * COVOF_INNER_CHEBYSHEV_STREAM; COVOF_INNER_CG and COVOF_INNER_MG are
+ * rejected (COVOF_UNSUPPORTED).  The
  * Weymouth-Yue pass order follows the batch's own step count (x first on its
  * first step). */
 typedef struct covof_batch covof_batch;

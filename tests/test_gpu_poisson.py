@@ -22,7 +22,7 @@ def test_operator_is_bit_identical(gpu_pkg, orc):
 
 
 @pytest.mark.parametrize("gauge", ["pinned", "reference"])
-@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_strips", "mixed_cluster16", "mixed_cluster4", "mixed_stream", "mixed_cg"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_strips", "mixed_cluster16", "mixed_cluster4", "mixed_stream", "mixed_cg", "mixed_mg"])
 @pytest.mark.parametrize("n", [64, 128])
 def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
     pkg = gpu_pkg
@@ -39,6 +39,8 @@ def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
         q.p_inner_kind = cap.INNER_CHEBYSHEV_STREAM
     elif prec == "mixed_cg":
         q.p_inner_kind = cap.INNER_CG
+    elif prec == "mixed_mg":
+        q.p_inner_kind = cap.INNER_MG
     x = np.zeros_like(b)
     with pkg.Solver(q) as s:
         # "mixed" on these meshes is the strip form on every SM; the strip form
@@ -117,7 +119,7 @@ def test_full_size_1024_converges_fp64_and_mixed(gpu_pkg, orc):
     p, b, ru, rv, dt = _inclusions(pkg, 1024, 200)
     sols = {}
     for prec, kind in ((cap.PREC_FP64, 0), (cap.PREC_MIXED, cap.INNER_CHEBYSHEV),
-                       (cap.PREC_MIXED, cap.INNER_CHEBYSHEV_STREAM)):
+                       (cap.PREC_MIXED, cap.INNER_CHEBYSHEV_STREAM), (cap.PREC_MIXED, cap.INNER_MG)):
         q = p.copy()
         q.p_precision = prec
         q.p_inner_kind = kind
