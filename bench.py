@@ -2,8 +2,10 @@
 """Benchmark: standalone variable-density pressure Poisson, 1024^2 cells,
 200 circular heavy inclusions (rho 1000 / 1), zero-mean Gaussian RHS,
 homogeneous Neumann walls with a pinned reference cell, Jacobi-PCG to
-||r||/||b|| <= 1e-10.  Headline = the mixed path (FP32 PCG inside FP64
-iterative refinement); the plain FP64 PCG path is timed beside it.
+||r||/||b|| <= 1e-10.  Headline = the mixed path (flexible CG in FP64,
+preconditioned by one FP32 geometric-multigrid V-cycle per iteration); the
+plain FP64 Jacobi-PCG path (the reference's algorithm) and the mixed path
+with the FP32 Chebyshev inner iteration are timed beside it.
 
 Beside it ("sp_steps"): whole time steps (VOF + STANDARD_PROJECTION) of the
 rising-bubble case, 128x256, device-resident and replayed as CUDA graphs,
@@ -12,8 +14,8 @@ droplet / bubble cases of uneven sizes stepped together by the batch engine
 (steps/s of the whole batch, mixed vs plain FP64).
 
 Before timing, the autotuner (autotune.py) picks the mixed solve's launch
-shape and Chebyshev degree / interval on the same system (bounded budget); the
-line reports the choice and the built-in rule's time.
+shape and multigrid smoothing / coarse-correction weight on the same system
+(bounded budget); the line reports the choice and the built-in rule's time.
 
 One step = one Poisson solve from a zero initial guess.  Device time per step
 is measured with CUDA events on the library's own stream; a 512 MiB buffer is
@@ -51,9 +53,20 @@ WORKLOAD = "variable-density pressure Poisson 1024x1024, 200 inclusions rho 1000
 #   (read r, aP, isd: 3), z (write 1), w = A z (read z, ax, ay, aP; write w: 5),
 #   update pass (read z, w, p, q, x, r; write p, q, x, r: 10), dots (2)
 #   = 21 words = 168 B.
+# Multigrid V-cycle (FP32, per fine cell): on a level of n cells, the first
+#   pre-smoothing sweep from x = 0 reads b, diag and writes x (3 words), each
+#   further sweep reads x, b, ax, ay, diag and writes x (6), the fused
+#   residual-restriction reads x, b, ax, ay, diag (5) and writes n/4 coarse
+#   values, the prolongation reads x and n/4 coarse values and writes x
+#   (2.25): 12 nu + 4.5 words for nu sweeps each way; the coarser levels add
+#   1/4 + 1/16 + ... = 1/3 of that.
 W_ITER_FP64 = 15 * 8
 W_STEP_FP32 = 8 * 4
 W_OUTER_FP64 = 21 * 8
+
+
+def w_vcycle_fp32(nu: int) -> float:
+    return (12 * nu + 4.5) * 4.0 / 3.0 * 4
 
 
 def load_peaks():
@@ -312,25 +325,30 @@ def run_ours(args, world, rank, local):
     tp = torch.zeros_like(tb)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    # autotune the mixed solve on this system (launch shape, Chebyshev degree
-    # and interval; the stopping test stays the true FP64 residual at 1e-10)
+    # autotune the mixed solve on this system (launch shape, multigrid
+    # smoothing and coarse weight; the stopping test stays the true FP64
+    # residual at 1e-10)
     tuned = None
     if not args.no_tune:
         import importlib
         at = importlib.import_module(pkg.__name__ + ".autotune")
         q0 = p.copy()
         q0.p_precision = cap.PREC_MIXED
+        q0.p_inner_kind = cap.INNER_MG
         tuned = at.tune(q0, dt, tb, tru, trv, repeats=1, cache_path=None, budget_s=args.tune_budget)
 
     results = {}
-    for name, prec in (("fp64", cap.PREC_FP64), ("mixed", cap.PREC_MIXED)):
+    arms = (("fp64", cap.PREC_FP64, cap.INNER_MG), ("mixed", cap.PREC_MIXED, cap.INNER_MG),
+            ("mixed_chebyshev", cap.PREC_MIXED, cap.INNER_CHEBYSHEV))
+    for name, prec, kind in arms:
         q = p.copy()
         q.p_precision = prec
-        if prec == cap.PREC_MIXED and tuned is not None:
+        q.p_inner_kind = kind
+        if name == "mixed" and tuned is not None:
             for k, v in tuned["params"].items():
                 setattr(q, k, v)
         s = pkg.Solver(q)
-        if prec == cap.PREC_MIXED and tuned is not None:
+        if name == "mixed" and tuned is not None:
             import ctypes
             launch = cap.Launch(**tuned["launch"])
             assert s.lib.covof_set_launch(s.h, ctypes.byref(launch)) == cap.OK
@@ -365,7 +383,7 @@ def run_ours(args, world, rank, local):
         clk = clocks.stop() if clocks else None
         results[name] = {"ms_per_step": statistics.mean(step_ms), "kernel_ms": statistics.mean(kern_ms),
                          "iters": int(statistics.median(iters)), "outer": int(statistics.median(outer)),
-                         "wall_s": wall, "clocks": clk, "solver": s}
+                         "wall_s": wall, "clocks": clk, "solver": s, "nu": q.p_mg_nu, "cw": q.p_mg_cw}
 
     # e2e through the host C ABI: pinned host arrays, copies inside the region
     mixed = results["mixed"]
@@ -398,19 +416,22 @@ def run_ours(args, world, rank, local):
     ms_fp64 = max_over_ranks(results["fp64"]["ms_per_step"], world)
     value = world * 1000.0 / ms_mixed
 
-    # roofline of the dominant kernel (the persistent mixed-path kernel)
+    # roofline of the dominant kernel (the persistent mixed-path kernel:
+    # one V-cycle and one FP64 flexible-CG iteration per outer step)
     cells = n * n
     it_m, out_m = mixed["iters"], max(mixed["outer"], 1)
-    alg_bytes = it_m * cells * W_STEP_FP32 + out_m * cells * W_OUTER_FP64
+    w_outer = w_vcycle_fp32(mixed["nu"]) + W_OUTER_FP64
+    alg_bytes = out_m * cells * w_outer
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / (mixed["kernel_ms"] * 1e-3) / 1e9
     it_f = results["fp64"]["iters"]
     achieved64 = it_f * cells * W_ITER_FP64 / (results["fp64"]["kernel_ms"] * 1e-3) / 1e9
+    cheb = results["mixed_chebyshev"]
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():
         try:
-            traffic = json.loads(tfile.read_text()).get("k_pcg_mixed_bytes_per_launch")
+            traffic = json.loads(tfile.read_text()).get("k_pcg_mixed_mg_bytes_per_launch")
         except Exception:
             traffic = None
 
@@ -430,19 +451,24 @@ def run_ours(args, world, rank, local):
             "plain_fp64": {"ms_per_step": ms_fp64, "solves_per_s": world * 1000.0 / ms_fp64,
                            "iters": it_f, "kernel_ms": results["fp64"]["kernel_ms"],
                            "achieved_gbs": achieved64},
-            "mixed": {"inner_steps_fp32": it_m, "outer_fcg_iters": mixed["outer"], "kernel_ms": mixed["kernel_ms"]},
+            "mixed": {"inner": "multigrid V-cycle", "vcycles": it_m, "outer_fcg_iters": mixed["outer"],
+                      "kernel_ms": mixed["kernel_ms"], "mg_nu": mixed["nu"], "mg_cw": mixed["cw"]},
+            "mixed_chebyshev": {"ms_per_step": cheb["ms_per_step"], "solves_per_s": world * 1000.0 / cheb["ms_per_step"],
+                                "inner_steps_fp32": cheb["iters"], "outer_fcg_iters": cheb["outer"],
+                                "kernel_ms": cheb["kernel_ms"]},
             "autotune": None if tuned is None else {
                 "launch": tuned["launch"], "params": tuned["params"], "candidates": tuned["candidates"],
                 "tuned_ms": tuned["ms"], "rule_ms": tuned["rule_ms"]},
             "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_pcg_mixed_cheb", "peak_source": peak_kind,
-                         "note": "achieved = algorithmic bytes (8 FP32 words/cell per inner Chebyshev step + "
-                                 "21 FP64 words/cell per outer FCG iteration, the streaming model) / CUDA-event "
-                                 "kernel time, an effective rate; traffic = measured DRAM bytes per launch "
-                                 "(ncu), far below it because the FP32 inner state is shared-memory resident: "
-                                 "the kernel is issue / exchange-latency bound, not HBM-bound"},
+                         "kernel": "k_pcg_mixed_mg", "peak_source": peak_kind,
+                         "bytes_per_cell_per_outer": w_outer,
+                         "note": "achieved = algorithmic bytes (one FP32 V-cycle, (12 nu + 4.5) words/cell on "
+                                 "each level, x 4/3 over the levels, + 21 FP64 words/cell per outer FCG "
+                                 "iteration) / CUDA-event kernel time, an effective rate; traffic = measured "
+                                 "DRAM bytes per launch (ncu): most FP32 level data stays in L2, so the "
+                                 "kernel is bound by grid-barrier latency and FP64 issue, not HBM"},
             "cpu_baseline": cpu,
             "e2e": {"value": world * 1000.0 / e2e_step, "unit": UNIT, "h2d_bytes_per_step": gbytes,
                     "d2h_bytes_per_step": b.nbytes},

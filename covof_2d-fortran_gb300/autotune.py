@@ -2,10 +2,11 @@
 
 For one mesh and parameter set, times candidate launch shapes
 (covof_set_launch: FP64 block size, block count, shared-memory vs streamed
-Chebyshev state) and, on the mixed path, candidate Chebyshev degrees and
-interval ends, on the case's own Poisson system; keeps the fastest candidate
-that reaches the tolerance; caches the choice in a JSON file keyed by device,
-mesh and arithmetic.  The tuned Chebyshev settings change the inner
+Chebyshev state) and, on the mixed path, candidate inner settings (Chebyshev
+degree and interval end; multigrid smoothing sweeps and coarse-correction
+weight), on the case's own Poisson system; keeps the fastest candidate that
+reaches the tolerance; caches the choice in a JSON file keyed by device,
+mesh, arithmetic and inner kind.  The tuned inner settings change the inner
 iteration, not the answer: the outer FP64 iteration still stops on the true
 residual at p_tol.
 
@@ -67,6 +68,16 @@ def candidates(p: Params, sm_count: int) -> list[tuple[dict, dict]]:
     # strips on every SM, then higher degrees and narrower intervals, which
     # trade FP64 outer iterations for cheap FP32 inner steps
     blocks = sorted({min(sm_count, p.ny), max(1, min(sm_count, p.ny) // 2)}, reverse=True)
+    if p.p_inner_kind == capi.INNER_MG:
+        # the over-correction weight matters most (aggregation coarse
+        # operators are about twice too stiff), then the smoothing sweeps
+        mg_blocks = sorted({sm_count, max(1, sm_count // 2)}, reverse=True)
+        for nb in mg_blocks:
+            for nu in (2, 3, 1):
+                for cw in (1.9, 2.0, 1.8):
+                    out.append(({"p_threads": 0, "p_blocks": nb, "p_inner_form": 0},
+                                {"p_mg_nu": nu, "p_mg_cw": cw}))
+        return out
     shapes = []
     if p.p_inner_kind == capi.INNER_CHEBYSHEV:
         # one thread-block cluster (small meshes; covof_set_launch refuses
@@ -108,7 +119,7 @@ def tune(p: Params, dt: float, b, rho_u, rho_v, repeats: int = 2, cache_path: Pa
     for launch, over in candidates(p, sm):
         by_params.setdefault(tuple(sorted(over.items())), []).append(launch)
     # the rule's own settings are always timed (the reference point)
-    rule_key = tuple(sorted({"p_inner_max_iter": p.p_inner_max_iter, "p_cheb_lo": p.p_cheb_lo}.items()))
+    rule_key = tuple(sorted({k: getattr(p, k) for k in tuned_fields(p)}.items()))
     if p.p_precision != capi.PREC_FP64 and rule_key in by_params:
         by_params = {rule_key: by_params.pop(rule_key), **by_params}
     for over_t, launches in by_params.items():
@@ -155,13 +166,20 @@ def tune(p: Params, dt: float, b, rho_u, rho_v, repeats: int = 2, cache_path: Pa
     return best
 
 
+def tuned_fields(p: Params) -> tuple[str, ...]:
+    """The parameters the tuner varies for p's arithmetic and inner kind."""
+    if p.p_precision == capi.PREC_FP64:
+        return ()
+    if p.p_inner_kind == capi.INNER_MG:
+        return ("p_mg_nu", "p_mg_cw")
+    return ("p_inner_max_iter", "p_cheb_lo")
+
+
 def _is_rule(r: dict, p: Params, sm: int) -> bool:
     """Whether a timed record is what the built-in rules would have chosen."""
     if p.p_precision == capi.PREC_FP64:
         return False
-    return (r["params"].get("p_inner_max_iter") == p.p_inner_max_iter
-            and r["params"].get("p_cheb_lo") == p.p_cheb_lo
-            and r.get("rule", False))
+    return all(r["params"].get(k) == getattr(p, k) for k in tuned_fields(p)) and r.get("rule", False)
 
 
 def apply(p: Params, cache_path: Path = DEFAULT_CACHE):

@@ -48,7 +48,7 @@ class Params(C.Structure):
         ("sigma", C.c_double), ("gx", C.c_double), ("gy", C.c_double),
         ("recon", C.c_int),
         ("p_inner_kind", C.c_int), ("p_cheb_lo", C.c_double),
-        ("p_mg_nu", C.c_int), ("p_mg_cw", C.c_double),
+        ("p_mg_nu", C.c_int), ("p_mg_cw", C.c_double), ("p_mg_tail", C.c_int),
     ]
 
     def copy(self) -> "Params":

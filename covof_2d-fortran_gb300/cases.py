@@ -58,10 +58,11 @@ def make_params(nx: int, ny: int, lx: float, ly: float) -> Params:
     p.rho1, p.rho2, p.mu1, p.mu2 = 1.0, 1.0, 1.0e-3, 1.0e-3
     p.sigma, p.gx, p.gy = 0.0, 0.0, 0.0
     p.recon = capi.RECON_PLIC
-    p.p_inner_kind = capi.INNER_CHEBYSHEV
+    p.p_inner_kind = capi.INNER_MG
     p.p_cheb_lo = 1.0e-3
     p.p_mg_nu = 2
-    p.p_mg_cw = 1.0
+    p.p_mg_cw = 1.9
+    p.p_mg_tail = 2048
     return p
 
 

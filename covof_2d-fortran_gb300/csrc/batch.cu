@@ -9,7 +9,8 @@
 //      cases (k_mom_krylov_batch);
 //   3. per case: unpack + velocity BC; Poisson assembly;
 //   4. ONE persistent cooperative launch: the Poisson solves of all cases
-//      (k_pcg_mixed_batch, or k_pcg_fp64_batch for FP64 batches);
+//      (k_pcg_mixed_mg_batch / k_pcg_mixed_smem_batch / k_pcg_mixed_batch,
+//      or k_pcg_fp64_batch for FP64 batches);
 //   5. per case: copy-back, velocity correction, velocity BC, status log.
 // The grid of a batched solve is cut into teams (contiguous block ranges,
 // common.cuh: BatchTeams); a team solves its cases one after another with
@@ -365,11 +366,13 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
   auto fail = [&](int code) { covof_batch_destroy(b); return code; };
   b->ncases = ncases;
   b->mixed = cases[0].p_precision == COVOF_PREC_MIXED;
+  const bool mg = b->mixed && cases[0].p_inner_kind == COVOF_INNER_MG;
   for (int c = 0; c < ncases; ++c) {
-    // one arithmetic per batch; the mixed batch uses the streaming inner form
+    // one arithmetic per batch; a mixed batch runs either the multigrid inner
+    // iteration for every case or Chebyshev for every case
     if ((cases[c].p_precision == COVOF_PREC_MIXED) != b->mixed) return fail(COVOF_INVALID);
-    if (b->mixed && (cases[c].p_inner_kind == COVOF_INNER_CG || cases[c].p_inner_kind == COVOF_INNER_MG))
-      return fail(COVOF_UNSUPPORTED);
+    if (b->mixed && (cases[c].p_inner_kind == COVOF_INNER_MG) != mg) return fail(COVOF_UNSUPPORTED);
+    if (b->mixed && cases[c].p_inner_kind == COVOF_INNER_CG) return fail(COVOF_UNSUPPORTED);
     if (cases[c].p_precond == COVOF_PRECOND_SSOR) return fail(COVOF_UNSUPPORTED);
     const int s = check_mom_params(cases[c]);
     if (s != COVOF_OK) return fail(s);
@@ -395,15 +398,17 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
   if (cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
     return fail(COVOF_CUDA_ERROR);
-  // Poisson: the mixed batch keeps each case's inner state in shared-memory
-  // row strips when every case fits a team of at most 32 blocks, else it
-  // streams the inner state through L2 / HBM
+  // Poisson: a multigrid batch runs k_pcg_mixed_mg_batch; a Chebyshev batch
+  // keeps each case's inner state in shared-memory row strips when every
+  // case fits a team of at most 32 blocks, else it streams the inner state
+  // through L2 / HBM
   b->pfn = b->mixed ? (const void*)k_pcg_mixed_batch : (const void*)k_pcg_fp64_batch;
   std::vector<int> tmin;
   bool smem_form = false;
   bool want_stream = false;
   for (int c = 0; c < ncases; ++c) want_stream |= cases[c].p_inner_kind == COVOF_INNER_CHEBYSHEV_STREAM;
-  if (b->mixed && !want_stream) {
+  if (mg) b->pfn = (const void*)k_pcg_mixed_mg_batch;
+  if (b->mixed && !want_stream && !mg) {
     int optin = 0;
     cudaFuncAttributes fa;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
@@ -426,6 +431,18 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
     }
     b->pplan.smem = bytes;
     if (cudaFuncSetAttribute(b->pfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+      return fail(COVOF_CUDA_ERROR);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->pfn, 1024, bytes) != cudaSuccess || per_sm < 1)
+      return fail(COVOF_CUDA_ERROR);
+    pmax = per_sm * b->sm_count;
+  } else if (mg) {
+    // the largest multigrid tail of the batch in every block
+    size_t bytes = 0;
+    for (covof_handle* h : b->h) bytes = std::max(bytes, (size_t)h->mg.tail_smem);
+    b->pplan.smem = bytes;
+    if (bytes > 48 * 1024 &&
+        cudaFuncSetAttribute(b->pfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
       return fail(COVOF_CUDA_ERROR);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->pfn, 1024, bytes) != cudaSuccess || per_sm < 1)

@@ -90,9 +90,20 @@ int ensure_poisson(covof_handle* h) {
     pool += 6LL * (c.nx + 2) * (c.ny + 2);
     H.nl += 1;
   }
+  // the tail: from the first level of at most p_mg_tail cells whose levels
+  // down to the coarsest fit in kMgTailSmem bytes of shared memory
+  const long long tail_cells = h->prm.p_mg_tail > 0 ? h->prm.p_mg_tail : 2048;
   H.tail = H.nl;
-  for (int l = 1; l < H.nl; ++l)
-    if ((long long)H.lv[l].nx * H.lv[l].ny <= 2048) { H.tail = l; break; }
+  H.tail_smem = 0;
+  for (int l = 1; l < H.nl; ++l) {
+    long long bytes = 0;
+    for (int q = l; q < H.nl; ++q) bytes += 24LL * (H.lv[q].nx + 2) * (H.lv[q].ny + 2);
+    if ((long long)H.lv[l].nx * H.lv[l].ny <= tail_cells && bytes <= kMgTailSmem) {
+      H.tail = l;
+      H.tail_smem = (int)bytes;
+      break;
+    }
+  }
   H.omega = 0.8f;
   H.nu = h->prm.p_mg_nu < 1 ? 1 : (h->prm.p_mg_nu > 8 ? 8 : h->prm.p_mg_nu);
   H.cw = (float)(h->prm.p_mg_cw > 0.0 && h->prm.p_mg_cw <= 4.0 ? h->prm.p_mg_cw : 1.0);
@@ -240,6 +251,7 @@ int fp64_threads(const covof_handle* h) {
 
 int poisson_plan(covof_handle* h) {
   if (h->have_pplan) return COVOF_OK;
+  CS(ensure_poisson(h));  // the multigrid plan sizes its shared memory from the hierarchy
   const covof_params& P = h->prm;
   const bool mixed = P.p_precision == COVOF_PREC_MIXED;
   const covof_launch& L = h->launch;
@@ -253,10 +265,14 @@ int poisson_plan(covof_handle* h) {
     const void* mfn = (const void*)k_pcg_mixed_mg;
     long long units = h->sm_count;
     if (L.p_blocks > 0 && L.p_blocks < units) units = L.p_blocks;
-    const int nb = coop_blocks(h, mfn, kPoissonThreads, units, 0);
+    const size_t tail = (size_t)h->mg.tail_smem;
+    if (tail > 48 * 1024 &&
+        cudaFuncSetAttribute(mfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail) != cudaSuccess)
+      return COVOF_CUDA_ERROR;
+    const int nb = coop_blocks(h, mfn, kPoissonThreads, units, tail);
     if (nb < 1) return COVOF_CUDA_ERROR;
     h->p_fn = mfn;
-    h->p_smem = 0;
+    h->p_smem = tail;
     h->p_nb = nb;
     h->p_threads = kPoissonThreads;
     h->have_pplan = true;
@@ -847,10 +863,11 @@ void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly)
   p->rho1 = 1.0; p->rho2 = 1.0; p->mu1 = 1.0e-3; p->mu2 = 1.0e-3;
   p->sigma = 0.0; p->gx = 0.0; p->gy = 0.0;
   p->recon = COVOF_RECON_PLIC;
-  p->p_inner_kind = COVOF_INNER_CHEBYSHEV;
+  p->p_inner_kind = COVOF_INNER_MG;
   p->p_cheb_lo = 1.0e-3;
   p->p_mg_nu = 2;
-  p->p_mg_cw = 1.0;
+  p->p_mg_cw = 1.9;
+  p->p_mg_tail = 2048;
 }
 
 int covof_abi_version(void) { return COVOF_ABI_VERSION; }

@@ -1270,21 +1270,28 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cluster(PoissonArgs a) {
 
 // ---------------------------------------------------------------------------
 // Geometric multigrid inner preconditioner (COVOF_INNER_MG): one V-cycle on
-// the scaled FP32 operator S A S per outer iteration.  Levels halve each
-// dimension (odd sizes keep a one-column tail); coarse operators are the
-// Galerkin products of piecewise-constant transfers: a coarse face
-// coefficient is the sum of the fine face coefficients it covers, a coarse
-// diagonal the sum of the aggregate's external faces.  Smoothing: damped
-// Jacobi (weight omega), nu sweeps before and after each coarse correction,
-// double-buffered; residual and restriction are fused; prolongation is
-// injection scaled by cw.  The V-cycle is symmetric (same sweeps down and
-// up, restriction = prolongation transposed), as the outer conjugate
-// recurrences need.  Levels of at most 2048 cells run in block 0 alone with
-// __syncthreads instead of grid barriers.
+// the FP32 copy of A itself (not the diagonally scaled operator: the
+// near-null vector of A is the constant, which piecewise-constant transfers
+// carry exactly) per outer iteration.  Levels halve each dimension (odd
+// sizes keep a one-column tail); coarse operators are the Galerkin products
+// of piecewise-constant transfers: a coarse face coefficient is the sum of
+// the fine face coefficients it covers, a coarse diagonal the sum of the
+// aggregate's diagonals minus twice its internal couplings.  Smoothing:
+// damped Jacobi (weight omega), nu sweeps before and after each coarse
+// correction, double-buffered; residual and restriction are fused;
+// prolongation is injection scaled by cw -- Galerkin operators of 2x2
+// aggregates are about twice as stiff as the operator rediscretised on the
+// coarse mesh, so smooth errors are under-corrected by about one half and a
+// weight near 2 (over-correction) restores the step.  The V-cycle is
+// symmetric (same sweeps down and up, restriction = prolongation transposed)
+// as the outer conjugate recurrences need.  The coarsest levels (the tail,
+// chosen on the host by cell count and shared-memory size) run in block 0
+// alone out of its shared memory, with __syncthreads instead of grid
+// barriers; their coefficients are loaded once per solve.
 struct MgLv {
   int nx, ny, P;
   float *xa, *xb, *b;
-  const float *ax, *ay, *dg;  // dg == nullptr: unit diagonal (level 0)
+  const float *ax, *ay, *dg;
   __device__ __forceinline__ int id(int i, int j) const { return j * P + i; }
 };
 
@@ -1295,85 +1302,110 @@ struct MgInner {
   MgHier H;
   float *x0a, *x0b, *b0;   // level 0 solution buffers and right-hand side
   const float *ax0, *ay0, *dg0;  // level 0: FP32 copy of A (faces, diagonal)
-  __device__ MgLv lv(int l) const {
+  float* sm;               // block 0: tail levels (6 fields each), H.tail_smem bytes
+  // level l in global memory (S = false) or, for tail levels, in block 0's
+  // shared memory (S = true)
+  __device__ MgLv lv(int l, bool S = false) const {
     MgLv L;
     L.nx = H.lv[l].nx; L.ny = H.lv[l].ny; L.P = L.nx + 2;
+    const size_t g = (size_t)(L.nx + 2) * (size_t)(L.ny + 2);
     if (l == 0) {
       L.xa = x0a; L.xb = x0b; L.b = b0; L.ax = ax0; L.ay = ay0; L.dg = dg0;
       return L;
     }
-    const size_t g = (size_t)(L.nx + 2) * (size_t)(L.ny + 2);
-    float* base = H.pool + H.lv[l].off;
+    float* base;
+    if (S) {
+      base = sm;
+      for (int q = H.tail; q < l; ++q) base += 6 * (size_t)(H.lv[q].nx + 2) * (size_t)(H.lv[q].ny + 2);
+    } else {
+      base = H.pool + H.lv[l].off;
+    }
     L.xa = base; L.xb = base + g; L.b = base + 2 * g;
     L.ax = base + 3 * g; L.ay = base + 4 * g; L.dg = base + 5 * g;
     return L;
   }
+  // shared-memory views read with plain loads; global ones through L2 (other
+  // blocks wrote them since this block last looked)
+  template <bool S>
+  __device__ __forceinline__ static float ld(const float* p) {
+    if constexpr (S) return *p;
+    else return __ldcg(p);
+  }
   // cells (i, j) of an ni x nj range, over the team or over block 0 alone
-  template <class F>
-  __device__ __forceinline__ void cells(int ni, int nj, bool local, F f) const {
+  template <bool S, class F>
+  __device__ __forceinline__ void cells(int ni, int nj, F f) const {
     const int n = ni * nj;
-    const int t0 = local ? (int)threadIdx.x : tm.rank * (int)blockDim.x + (int)threadIdx.x;
-    const int st = local ? (int)blockDim.x : tm.size * (int)blockDim.x;
+    const int t0 = S ? (int)threadIdx.x : tm.rank * (int)blockDim.x + (int)threadIdx.x;
+    const int st = S ? (int)blockDim.x : tm.size * (int)blockDim.x;
     for (int c = t0; c < n; c += st) {
       const int j = c / ni, i = c - j * ni;
       f(i + 1, j + 1);
     }
   }
-  __device__ __forceinline__ float apply(const MgLv& L, const float* x, int k) const {
-    const float d = L.dg ? L.dg[k] : 1.0f;
-    float v = d * __ldcg(x + k);
-    v = __fmaf_rn(-L.ax[k], __ldcg(x + k - 1), v);
-    v = __fmaf_rn(-L.ax[k + 1], __ldcg(x + k + 1), v);
-    v = __fmaf_rn(-L.ay[k], __ldcg(x + k - L.P), v);
-    v = __fmaf_rn(-L.ay[k + L.P], __ldcg(x + k + L.P), v);
+  template <bool S>
+  __device__ __forceinline__ static float apply(const MgLv& L, const float* x, int k) {
+    float v = L.dg[k] * ld<S>(x + k);
+    v = __fmaf_rn(-L.ax[k], ld<S>(x + k - 1), v);
+    v = __fmaf_rn(-L.ax[k + 1], ld<S>(x + k + 1), v);
+    v = __fmaf_rn(-L.ay[k], ld<S>(x + k - L.P), v);
+    v = __fmaf_rn(-L.ay[k + L.P], ld<S>(x + k + L.P), v);
     return v;
   }
   // one damped Jacobi sweep from buffer cur into the other (first: x = 0)
-  __device__ void sweep(int l, bool first, bool local, int cur) const {
-    const MgLv L = lv(l);
+  template <bool S>
+  __device__ void sweep(int l, bool first, int cur) const {
+    const MgLv L = lv(l, S);
     const float* xs = cur ? L.xb : L.xa;
     float* xd = cur ? L.xa : L.xb;
     const float w = H.omega;
-    cells(L.nx, L.ny, local, [&](int i, int j) {
+    const int pin = l == 0 ? pk : -1;
+    cells<S>(L.nx, L.ny, [&](int i, int j) {
       const int k = L.id(i, j);
-      const float d = L.dg ? L.dg[k] : 1.0f;
+      const float d = L.dg[k];
       float v;
-      if (first) v = w * __ldcg(L.b + k) / d;
-      else v = __ldcg(xs + k) + w * (__ldcg(L.b + k) - apply(L, xs, k)) / d;
-      if (l == 0 && k == pk) v = 0.0f;
+      if (first) v = w * ld<S>(L.b + k) / d;
+      else v = ld<S>(xs + k) + w * (ld<S>(L.b + k) - apply<S>(L, xs, k)) / d;
+      if (k == pin) v = 0.0f;
       xd[k] = v;
     });
   }
   // b_{l+1} = restriction of the residual of level l (buffer cur)
-  __device__ void restrict_(int l, bool local, int cur) const {
-    const MgLv F = lv(l), Cc = lv(l + 1);
+  template <bool S>
+  __device__ void restrict_(int l, int cur) const {
+    const MgLv F = lv(l, S), Cc = lv(l + 1, S);
     const float* x = cur ? F.xb : F.xa;
-    cells(Cc.nx, Cc.ny, local, [&](int I, int J) {
+    const int pin = l == 0 ? pk : -1;
+    cells<S>(Cc.nx, Cc.ny, [&](int I, int J) {
       float s = 0.0f;
       for (int dj = 0; dj < 2; ++dj)
         for (int di = 0; di < 2; ++di) {
           const int i = 2 * I - 1 + di, j = 2 * J - 1 + dj;
           if (i > F.nx || j > F.ny) continue;
           const int k = F.id(i, j);
-          if (l == 0 && k == pk) continue;
-          s += __ldcg(F.b + k) - apply(F, x, k);
+          if (k == pin) continue;
+          s += ld<S>(F.b + k) - apply<S>(F, x, k);
         }
       Cc.b[Cc.id(I, J)] = s;
     });
   }
   // x_l (buffer cl) += cw * x_{l+1} (buffer cc) at the parent cell
-  __device__ void prolong(int l, bool local, int cl, int cc) const {
-    const MgLv F = lv(l), Cc = lv(l + 1);
+  template <bool S>
+  __device__ void prolong(int l, int cl, int cc) const {
+    const MgLv F = lv(l, S), Cc = lv(l + 1, S);
     float* x = cl ? F.xb : F.xa;
     const float* xc = cc ? Cc.xb : Cc.xa;
     const float cw = H.cw;
-    cells(F.nx, F.ny, local, [&](int i, int j) {
+    const int pin = l == 0 ? pk : -1;
+    cells<S>(F.nx, F.ny, [&](int i, int j) {
       const int k = F.id(i, j);
-      if (l == 0 && k == pk) return;
-      x[k] = __ldcg(x + k) + cw * __ldcg(xc + Cc.id((i + 1) / 2, (j + 1) / 2));
+      if (k == pin) return;
+      x[k] = ld<S>(x + k) + cw * ld<S>(xc + Cc.id((i + 1) / 2, (j + 1) / 2));
     });
   }
-  // coarse operators of levels 1 .. nl-1 from the fine ones (once per solve)
+  // parity of the buffer holding level l's correction after its last sweep
+  __device__ __forceinline__ int out_buf(int l) const { return l == H.nl - 1 ? (H.nuc & 1) : 0; }
+  // coarse operators of levels 1 .. nl-1 from the fine ones, then the tail
+  // levels' coefficients into block 0's shared memory (once per solve)
   __device__ bool setup(GridReducer& R) const {
     for (int l = 1; l < H.nl; ++l) {
       const MgLv F = lv(l - 1), Cc = lv(l);
@@ -1382,16 +1414,14 @@ struct MgInner {
       float* cdg = const_cast<float*>(Cc.dg);
       auto axf = [&](int i, int j) -> float { return (i <= F.nx + 1 && j <= F.ny) ? F.ax[F.id(i, j)] : 0.0f; };
       auto ayf = [&](int i, int j) -> float { return (i <= F.nx && j <= F.ny + 1) ? F.ay[F.id(i, j)] : 0.0f; };
-      cells(Cc.nx + 1, Cc.ny + 1, false, [&](int I, int J) {
+      auto dgf = [&](int i, int j) -> float { return (i <= F.nx && j <= F.ny) ? F.dg[F.id(i, j)] : 0.0f; };
+      cells<false>(Cc.nx + 1, Cc.ny + 1, [&](int I, int J) {
         const int k = Cc.id(I, J);
         if (J <= Cc.ny) cax[k] = axf(2 * I - 1, 2 * J - 1) + axf(2 * I - 1, 2 * J);
         if (I <= Cc.nx) cay[k] = ayf(2 * I - 1, 2 * J - 1) + ayf(2 * I, 2 * J - 1);
         if (I <= Cc.nx && J <= Cc.ny) {
           // Galerkin: sum of the aggregate's diagonals minus twice its
           // internal couplings (= its external faces plus its diagonal shifts)
-          auto dgf = [&](int i, int j) -> float {
-            return (i <= F.nx && j <= F.ny) ? (F.dg ? F.dg[F.id(i, j)] : 1.0f) : 0.0f;
-          };
           const int i0 = 2 * I - 1, j0 = 2 * J - 1;
           float d = dgf(i0, j0) + dgf(i0 + 1, j0) + dgf(i0, j0 + 1) + dgf(i0 + 1, j0 + 1);
           float internal = 0.0f;
@@ -1402,91 +1432,129 @@ struct MgInner {
       });
       if (!R.gs.sync()) return false;
     }
+    if (tm.rank == 0 && H.tail < H.nl) {
+      for (int l = H.tail; l < H.nl; ++l) {
+        const MgLv G = lv(l), Sm = lv(l, true);
+        const int g = Sm.P * (Sm.ny + 2);
+        for (int k = threadIdx.x; k < g; k += blockDim.x) {
+          Sm.xa[k] = 0.0f; Sm.xb[k] = 0.0f; Sm.b[k] = 0.0f;
+          const_cast<float*>(Sm.ax)[k] = __ldcg(G.ax + k);
+          const_cast<float*>(Sm.ay)[k] = __ldcg(G.ay + k);
+          const_cast<float*>(Sm.dg)[k] = __ldcg(G.dg + k);
+        }
+      }
+      __syncthreads();
+    }
     return true;
   }
   __device__ __forceinline__ void set_rhs(int k, int, float v) { b0[k] = v; }
   __device__ __forceinline__ float y(int k, int) const { return k == pk ? 0.0f : __ldcg(x0a + k); }
-  // levels lo .. nl-1 and back up to lo, block 0 alone (local) or the team
-  __device__ bool vcycle_part(GridReducer& R, int lo, bool local) const {
-    const int L = H.nl, nu = H.nu;
-    auto sync = [&]() -> bool {
-      if (local) { __syncthreads(); return true; }
-      return R.gs.sync();
-    };
-    for (int l = lo; l < L - 1; ++l) {
+  // the tail levels, block 0 alone out of shared memory: b_tail in from
+  // global memory, the tail's correction back out
+  __device__ void tail_cycle() const {
+    const int L = H.nl, nu = H.nu, t = H.tail;
+    {
+      const MgLv G = lv(t), Sm = lv(t, true);
+      const int g = Sm.P * (Sm.ny + 2);
+      for (int k = threadIdx.x; k < g; k += blockDim.x) Sm.b[k] = __ldcg(G.b + k);
+    }
+    __syncthreads();
+    for (int l = t; l < L - 1; ++l) {
       for (int s = 0; s < nu; ++s) {
-        if (s > 0 && !sync()) return false;
-        sweep(l, s == 0, local, s & 1);
+        if (s > 0) __syncthreads();
+        sweep<true>(l, s == 0, s & 1);
       }
-      if (!sync()) return false;
-      restrict_(l, local, nu & 1);
-      if (!sync()) return false;
+      __syncthreads();
+      restrict_<true>(l, nu & 1);
+      __syncthreads();
     }
     for (int s = 0; s < H.nuc; ++s) {
-      if (s > 0 && !sync()) return false;
-      sweep(L - 1, s == 0, local, s & 1);
+      if (s > 0) __syncthreads();
+      sweep<true>(L - 1, s == 0, s & 1);
     }
-    for (int l = L - 2; l >= lo; --l) {
-      if (!sync()) return false;
-      prolong(l, local, nu & 1, l + 1 == L - 1 ? (H.nuc & 1) : 0);
+    for (int l = L - 2; l >= t; --l) {
+      __syncthreads();
+      prolong<true>(l, nu & 1, out_buf(l + 1));
       for (int s = 0; s < nu; ++s) {
-        if (!sync()) return false;
-        sweep(l, false, local, (nu + s) & 1);
+        __syncthreads();
+        sweep<true>(l, false, (nu + s) & 1);
       }
     }
-    return true;
+    __syncthreads();
+    const int pb = out_buf(t);
+    const MgLv G = lv(t), Sm = lv(t, true);
+    const float* src = pb ? Sm.xb : Sm.xa;
+    float* dst = pb ? G.xb : G.xa;
+    const int g = Sm.P * (Sm.ny + 2);
+    for (int k = threadIdx.x; k < g; k += blockDim.x) dst[k] = src[k];
+  }
+  // One V-cycle on b0 into x0a.  b0 is complete on entry (a grid barrier
+  // since its last write) and x0a on return.
+  __device__ bool vcycle(GridReducer& R) const {
+    const int L = H.nl, nu = H.nu, t = H.tail;
+    bool ok = true;
+    for (int l = 0; ok && l < t && l < L - 1; ++l) {
+      for (int s = 0; ok && s < nu; ++s) {
+        if (s > 0) ok = R.gs.sync();
+        if (ok) sweep<false>(l, s == 0, s & 1);
+      }
+      ok = ok && R.gs.sync();
+      if (ok) restrict_<false>(l, nu & 1);
+      ok = ok && R.gs.sync();
+    }
+    if (!ok) return false;
+    if (t < L) {
+      if (tm.rank == 0) tail_cycle();
+    } else {
+      // no tail: the coarsest level over the grid
+      for (int s = 0; ok && s < H.nuc; ++s) {
+        if (s > 0) ok = R.gs.sync();
+        if (ok) sweep<false>(L - 1, s == 0, s & 1);
+      }
+    }
+    ok = ok && R.gs.sync();
+    for (int l = (t < L ? t : L - 1) - 1; ok && l >= 0; --l) {
+      prolong<false>(l, nu & 1, out_buf(l + 1));
+      for (int s = 0; ok && s < nu; ++s) {
+        ok = R.gs.sync();
+        if (ok) sweep<false>(l, false, (nu + s) & 1);
+      }
+      ok = ok && R.gs.sync();
+    }
+    return ok;
   }
   __device__ PcgOut solve(GridReducer& R, double, int budget) {
     PcgOut o{0, COVOF_OK, 0.0, 1.0, true};
     if (budget < 1) return o;
-    const int L = H.nl, nu = H.nu, t = H.tail;
-    bool ok = R.gs.sync();  // right-hand side complete
-    if (t >= L) {
-      ok = ok && vcycle_part(R, 0, false);
-    } else {
-      // grid-wide levels 0 .. t-1 down, the tail in block 0, then back up
-      for (int l = 0; ok && l < t; ++l) {
-        for (int s = 0; ok && s < nu; ++s) {
-          if (s > 0) ok = R.gs.sync();
-          if (ok) sweep(l, s == 0, false, s & 1);
-        }
-        ok = ok && R.gs.sync();
-        if (ok) restrict_(l, false, nu & 1);
-        ok = ok && R.gs.sync();
-      }
-      if (ok && tm.rank == 0) {
-        const bool tail_ok = vcycle_part(R, t, true);
-        __syncthreads();
-        (void)tail_ok;  // block-local steps have no waits that can give up
-      }
-      ok = ok && R.gs.sync();
-      for (int l = t - 1; ok && l >= 0; --l) {
-        prolong(l, false, nu & 1, l + 1 == L - 1 ? (H.nuc & 1) : 0);
-        for (int s = 0; ok && s < nu; ++s) {
-          ok = R.gs.sync();
-          if (ok) sweep(l, false, false, (nu + s) & 1);
-        }
-        ok = ok && R.gs.sync();
-      }
-    }
-    if (t >= L) ok = ok && R.gs.sync();
+    const bool ok = R.gs.sync() && vcycle(R);  // right-hand side complete
     o.iters = 1;
     if (!ok) { o.ok = false; o.status = COVOF_TIMEOUT; }
     return o;
   }
 };
 
-__global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg(PoissonArgs a) {
+// One mixed solve of case a by team tm with the multigrid inner iteration
+// (tail: the team's block 0 shared memory, at least a.mg.tail_smem bytes).
+__device__ void mixed_mg_case(const PoissonArgs& a, const Team& tm, GridReducer& R, float* tail) {
   const Dims D = a.D;
+  // a launch without room for the tail is refused, not run (every block of
+  // the team takes the same branch, so no barrier is left waiting)
+  unsigned int dsm;
+  asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dsm));
+  if (a.mg.tail < a.mg.nl && (unsigned int)a.mg.tail_smem > dsm) {
+    if (tm.rank == 0 && threadIdx.x == 0) {
+      a.res->iters = 0; a.res->relres = 1.0; a.res->status = COVOF_INVALID; a.res->outer = 0;
+    }
+    return;
+  }
   const Tiles tl = make_tiles(D, blockDim.x);
-  const Team tm = grid_team();
-  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   TileOwn own{D, tl, tm};
   MgInner in;
   in.tm = tm;
   in.pk = a.pinned ? D.P + 1 : -1;
   in.H = a.mg;
   in.x0a = a.e32; in.x0b = a.d32; in.b0 = a.r32; in.ax0 = a.ax32; in.ay0 = a.ay32; in.dg0 = a.aP32;
+  in.sm = tail;
   if (!in.setup(R)) {
     if (tm.rank == 0 && threadIdx.x == 0) {
       a.res->iters = 0; a.res->relres = 1.0; a.res->status = COVOF_TIMEOUT; a.res->outer = 0;
@@ -1494,6 +1562,13 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg(PoissonArgs a) {
     return;
   }
   fcg_mixed(a, own, in, R);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg(PoissonArgs a) {
+  extern __shared__ float mg_tail[];
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  mixed_mg_case(a, tm, R, mg_tail);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_stream(PoissonArgs a) {
@@ -1606,6 +1681,18 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_smem_batch(const PoissonA
   float* xb = bt.xb + (size_t)4 * T.x * bt.xbw;
   for (int q = T.z; q < T.w; ++q)
     mixed_smem_case(cases[bt.case_list[q]], tm, R, bt.flags + T.x, &sent, xb, cheb_tab, smem);
+}
+
+// Multigrid inner form: each case's hierarchy is its own; the launch's
+// dynamic shared memory holds the largest tail of the batch.
+__global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg_batch(const PoissonArgs* __restrict__ cases,
+                                                                BatchTeams bt) {
+  extern __shared__ float mg_tail[];
+  int4 T;
+  const Team tm = batch_team(bt, T);
+  const int t = bt.block_team[blockIdx.x];
+  GridReducer R{bt.part + (size_t)16 * T.x, GridSync{bt.bar + 32 * t, bt.err + t, (unsigned)T.y, 0u}, 0, tm.rank};
+  for (int q = T.z; q < T.w; ++q) mixed_mg_case(cases[bt.case_list[q]], tm, R, mg_tail);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt) {

@@ -17,6 +17,7 @@ struct PcgResult {
 // owns 7 arrays of (nx+2)*(ny+2) floats at pool + off: two solution buffers,
 // right-hand side, west / south face coefficients, diagonal, scratch.
 constexpr int kMgMaxLevels = 16;
+constexpr long long kMgTailSmem = 160 * 1024;  // cap on the shared-memory tail
 struct MgLevel {
   int nx, ny;
   long long off;
@@ -24,11 +25,12 @@ struct MgLevel {
 struct MgHier {
   MgLevel lv[kMgMaxLevels];
   int nl;      // levels including level 0
-  int tail;    // first level run by block 0 alone (<= 2048 cells), nl if none
+  int tail;    // first level run by block 0 alone out of shared memory, nl if none
   float* pool;
   float omega; // Jacobi weight
   float cw;    // coarse-correction weight
   int nu, nuc; // sweeps before / after each coarse correction; sweeps on the coarsest level
+  int tail_smem;     // bytes of block 0's shared memory holding the tail levels
 };
 
 struct PoissonArgs {
@@ -78,6 +80,7 @@ __global__ void k_pcg_mixed_stream(PoissonArgs a);
 __global__ void k_pcg_mixed_cluster(PoissonArgs a);
 __global__ void k_pcg_mixed_mg(PoissonArgs a);
 __global__ void k_pcg_fp64_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
+__global__ void k_pcg_mixed_mg_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_smem_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 // Shared-memory bytes of k_pcg_mixed_cheb for a strip of R rows of nx cells.

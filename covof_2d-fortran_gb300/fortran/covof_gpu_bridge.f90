@@ -53,6 +53,7 @@ module covof_gpu_bridge
      real(c_double) :: p_cheb_lo
      integer(c_int) :: p_mg_nu
      real(c_double) :: p_mg_cw
+     integer(c_int) :: p_mg_tail
   end type covof_params_t
 
   integer(c_int), parameter :: COVOF_OK = 0, COVOF_MAXITER = 1, COVOF_BREAKDOWN = 2

@@ -94,7 +94,8 @@ typedef struct covof_params {
   int enable_surface_tension;
   double rho1, rho2, mu1, mu2, sigma, gx, gy;
   int recon;             /* COVOF_RECON_* */
-  /* MIXED inner preconditioner: COVOF_INNER_CHEBYSHEV (degree p_inner_max_iter,
+  /* MIXED inner preconditioner (default COVOF_INNER_MG, the fastest measured
+   * on every mesh from 256^2 to 4096^2): COVOF_INNER_CHEBYSHEV (degree p_inner_max_iter,
    * at most 128, on [p_cheb_lo * 2, 2], no inner reductions; its state lives
    * in shared-memory row strips on every SM when a strip fits, else it
    * streams through L2/HBM; covof_set_launch can place it in one
@@ -107,7 +108,10 @@ typedef struct covof_params {
   int p_inner_kind;
   double p_cheb_lo;      /* lower end of the Chebyshev interval, as a fraction of 2 */
   int p_mg_nu;           /* COVOF_INNER_MG: Jacobi sweeps before and after each coarse correction (1-8) */
-  double p_mg_cw;        /* COVOF_INNER_MG: coarse-correction weight (0, 4] */
+  double p_mg_cw;        /* COVOF_INNER_MG: coarse-correction weight (0, 4]; about 1.8 offsets the
+                          * stiffness of aggregation coarse operators (over-correction) */
+  int p_mg_tail;         /* COVOF_INNER_MG: levels of at most this many cells run in one block's
+                          * shared memory (0: 2048) */
 } covof_params;
 enum { COVOF_INNER_CHEBYSHEV = 0, COVOF_INNER_CG = 1, COVOF_INNER_CHEBYSHEV_STREAM = 2, COVOF_INNER_MG = 3 };
 
@@ -346,14 +350,14 @@ int covof_get_launch(covof_handle* h, covof_launch* launch);
  * the predictor and Poisson Krylov solves of ALL cases in one persistent
  * cooperative launch each (teams of blocks, one case per team at a time);
  * with COVOF_RUN_GRAPH a whole batch step is one CUDA-graph launch.  All
- * cases of a batch use the same Poisson arithmetic (p_precision).  The mixed
- * batch runs the Chebyshev inner iteration with each case's state in
+ * cases of a batch use the same Poisson arithmetic (p_precision).  A mixed
+ * batch runs COVOF_INNER_MG for every case (each case its own hierarchy) or
+ * the Chebyshev inner iteration for every case, with each case's state in
  * shared-memory row strips of a team sized to fit (at most 32 blocks), or
  * streamed through L2 / HBM when a case does not fit or any case asks for
- * COVOF_INNER_CHEBYSHEV_STREAM; COVOF_INNER_CG and COVOF_INNER_MG are
- * rejected (COVOF_UNSUPPORTED).  The
- * Weymouth-Yue pass order follows the batch's own step count (x first on its
- * first step). */
+ * COVOF_INNER_CHEBYSHEV_STREAM; COVOF_INNER_CG, and multigrid mixed with
+ * Chebyshev cases, are rejected (COVOF_UNSUPPORTED).  The Weymouth-Yue pass
+ * order follows the batch's own step count (x first on its first step). */
 typedef struct covof_batch covof_batch;
 int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out);
 int covof_batch_destroy(covof_batch* b);

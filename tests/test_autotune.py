@@ -19,10 +19,18 @@ def test_candidates_cover_shapes(pkg, at):
     c64 = at.candidates(p, 152)
     assert {d["p_threads"] for d, _ in c64} == {128, 256, 512, 1024}
     p.p_precision = pkg.capi.PREC_MIXED
+    p.p_inner_kind = pkg.capi.INNER_CHEBYSHEV
     cm = at.candidates(p, 152)
     assert {d["p_inner_form"] for d, _ in cm} == {1, 2, 3}
     assert {o["p_inner_max_iter"] for _, o in cm} == {16, 24, 32, 48, 64, 96}
     assert all(1 <= d["p_blocks"] <= 152 for d, _ in cm)
+    assert at.tuned_fields(p) == ("p_inner_max_iter", "p_cheb_lo")
+    p.p_inner_kind = pkg.capi.INNER_MG
+    cg = at.candidates(p, 152)
+    assert {o["p_mg_nu"] for _, o in cg} == {1, 2, 3}
+    assert {o["p_mg_cw"] for _, o in cg} == {1.8, 1.9, 2.0}
+    assert {d["p_blocks"] for d, _ in cg} == {152, 76}
+    assert at.tuned_fields(p) == ("p_mg_nu", "p_mg_cw")
 
 
 def test_cache_round_trip(pkg, at, tmp_path):
@@ -54,14 +62,15 @@ def test_launch_overrides_validate(gpu_pkg):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_mg"])
 def test_tuned_choice_solves_to_tolerance(gpu_pkg, orc, at, tmp_path, prec):
     import torch
     pkg = gpu_pkg
     p, b, ru, rv, dt = pkg.cases.poisson_inclusions(n=128, n_incl=20)
     p.p_gauge = pkg.capi.GAUGE_PINNED
     p.p_tol = 1e-10
-    p.p_precision = pkg.capi.PREC_MIXED if prec == "mixed" else pkg.capi.PREC_FP64
+    p.p_precision = pkg.capi.PREC_FP64 if prec == "fp64" else pkg.capi.PREC_MIXED
+    p.p_inner_kind = pkg.capi.INNER_MG if prec == "mixed_mg" else pkg.capi.INNER_CHEBYSHEV
     T = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
     path = tmp_path / "tune.json"
     best = at.tune(p, dt, T(b), T(ru), T(rv), repeats=1, cache_path=path, budget_s=60.0)

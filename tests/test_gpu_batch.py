@@ -21,14 +21,16 @@ def _cases(pkg, orc, mixed, n=6, sizes=(32, 48, 64), seed=7):
     return out
 
 
-@pytest.mark.parametrize("mode", ["fp64", "mixed", "mixed_stream"])
+@pytest.mark.parametrize("mode", ["fp64", "mixed", "mixed_stream", "mixed_mg"])
 def test_batch_matches_oracle_per_case(gpu_pkg, orc, mode):
     pkg = gpu_pkg
     mixed = mode != "fp64"
     cases = _cases(pkg, orc, mixed)
-    if mode == "mixed_stream":
+    kind = {"mixed": pkg.capi.INNER_CHEBYSHEV, "mixed_stream": pkg.capi.INNER_CHEBYSHEV_STREAM,
+            "mixed_mg": pkg.capi.INNER_MG}.get(mode)
+    if kind is not None:
         for p, f, dt in cases:
-            p.p_inner_kind = pkg.capi.INNER_CHEBYSHEV_STREAM
+            p.p_inner_kind = kind
     nsteps = 3
     ref = []
     for p, f, dt in cases:
@@ -90,5 +92,15 @@ def test_batch_rejects_mixed_arithmetic(gpu_pkg, orc):
     cases = _cases(pkg, orc, True, n=2)
     ps = [c[0] for c in cases]
     ps[1].p_precision = pkg.capi.PREC_FP64
+    with pytest.raises(pkg.CovofError):
+        pkg.Batch(ps)
+
+
+def test_batch_rejects_mixed_inner_kinds(gpu_pkg, orc):
+    pkg = gpu_pkg
+    cases = _cases(pkg, orc, True, n=2)
+    ps = [c[0] for c in cases]
+    ps[0].p_inner_kind = pkg.capi.INNER_MG
+    ps[1].p_inner_kind = pkg.capi.INNER_CHEBYSHEV
     with pytest.raises(pkg.CovofError):
         pkg.Batch(ps)

@@ -22,7 +22,8 @@ def test_operator_is_bit_identical(gpu_pkg, orc):
 
 
 @pytest.mark.parametrize("gauge", ["pinned", "reference"])
-@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_strips", "mixed_cluster16", "mixed_cluster4", "mixed_stream", "mixed_cg", "mixed_mg"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_strips", "mixed_cluster16", "mixed_cluster4", "mixed_stream", "mixed_cg", "mixed_mg",
+                                  "mixed_mg_plain", "mixed_mg_gridtail"])
 @pytest.mark.parametrize("n", [64, 128])
 def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
     pkg = gpu_pkg
@@ -35,12 +36,22 @@ def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
     assert st_o == 0
     q = p.copy()
     q.p_precision = cap.PREC_FP64 if prec == "fp64" else cap.PREC_MIXED
+    q.p_inner_kind = cap.INNER_CHEBYSHEV
     if prec == "mixed_stream":
         q.p_inner_kind = cap.INNER_CHEBYSHEV_STREAM
     elif prec == "mixed_cg":
         q.p_inner_kind = cap.INNER_CG
     elif prec == "mixed_mg":
         q.p_inner_kind = cap.INNER_MG
+    elif prec == "mixed_mg_plain":
+        # plain coarse correction, one smoothing sweep each way
+        q.p_inner_kind = cap.INNER_MG
+        q.p_mg_nu = 1
+        q.p_mg_cw = 1.0
+    elif prec == "mixed_mg_gridtail":
+        # no shared-memory tail: every level over the grid
+        q.p_inner_kind = cap.INNER_MG
+        q.p_mg_tail = 1
     x = np.zeros_like(b)
     with pkg.Solver(q) as s:
         # "mixed" on these meshes is the strip form on every SM; the strip form
