@@ -78,7 +78,7 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks + throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks + throttle reasons sampled every 100 ms."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -94,7 +94,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
             return
@@ -427,11 +427,17 @@ def run_ours(args, world, rank, local):
     it_f = results["fp64"]["iters"]
     achieved64 = it_f * cells * W_ITER_FP64 / (results["fp64"]["kernel_ms"] * 1e-3) / 1e9
     cheb = results["mixed_chebyshev"]
+    # measured DRAM bytes of one launch: the ncu capture's bytes per outer
+    # iteration (rule settings) x this launch's outer iterations, scaled by
+    # the model's bytes-per-iteration ratio when the tuned sweep count differs
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():
         try:
-            traffic = json.loads(tfile.read_text()).get("k_pcg_mixed_mg_bytes_per_launch")
+            t = json.loads(tfile.read_text())
+            per_outer = t["k_pcg_mixed_mg_bytes_per_outer"]
+            nu0 = int(t["k_pcg_mixed_mg_nu"])
+            traffic = per_outer * out_m * w_outer / (w_vcycle_fp32(nu0) + W_OUTER_FP64)
         except Exception:
             traffic = None
 
@@ -466,9 +472,10 @@ def run_ours(args, world, rank, local):
                          "bytes_per_cell_per_outer": w_outer,
                          "note": "achieved = algorithmic bytes (one FP32 V-cycle, (12 nu + 4.5) words/cell on "
                                  "each level, x 4/3 over the levels, + 21 FP64 words/cell per outer FCG "
-                                 "iteration) / CUDA-event kernel time, an effective rate; traffic = measured "
-                                 "DRAM bytes per launch (ncu): most FP32 level data stays in L2, so the "
-                                 "kernel is bound by grid-barrier latency and FP64 issue, not HBM"},
+                                 "iteration) / CUDA-event kernel time, an effective rate; traffic = DRAM bytes per "
+                                 "launch from the ncu capture (bytes per outer iteration x this launch's "
+                                 "outer iterations): much of the level data stays in L2, and the kernel is "
+                                 "bound by grid-barrier latency and FP64 issue, not HBM"},
             "cpu_baseline": cpu,
             "e2e": {"value": world * 1000.0 / e2e_step, "unit": UNIT, "h2d_bytes_per_step": gbytes,
                     "d2h_bytes_per_step": b.nbytes},
@@ -486,7 +493,7 @@ def run_ours(args, world, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=1024)
