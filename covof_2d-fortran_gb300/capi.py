@@ -20,14 +20,16 @@ STATUS_NAMES = {0: "OK", 1: "MAXITER", 2: "BREAKDOWN", 3: "NAN", 4: "TIMEOUT",
 BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC, BC_FREESLIP = 1, 2, 3, 4
 LINEAR_BICGSTAB2, LINEAR_BICGSTAB, LINEAR_CG = 1, 2, 3
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_SSOR, PRECOND_ILU0 = 0, 1, 2, 3
-CONV_UPWIND, CONV_CENTERED = 1, 2
+CONV_UPWIND, CONV_CENTERED, CONV_TVD_SUPERBEE = 1, 2, 3
+TIME_EULER, TIME_GEAR = 1, 2
+CONV_LIN_PICARD, CONV_LIN_AB2, CONV_LIN_NEWTON = 1, 2, 3
 RECON_PLIC, RECON_ELVIRA = 0, 1
 GAUGE_REFERENCE, GAUGE_PINNED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 INNER_CHEBYSHEV, INNER_CG, INNER_CHEBYSHEV_STREAM, INNER_MG = 0, 1, 2, 3
 # resident fields (COVOF_FIELD_*), in header order; names follow the Fields dataclass
 FIELD_NAMES = ("u", "v", "p", "C", "rho", "rho_u", "rho_v", "mu", "mu_node", "fx_sigma",
-               "fy_sigma", "curvature", "u_old", "v_old")
+               "fy_sigma", "curvature", "u_old", "v_old", "u_nm1", "v_nm1")
 FIELD = {name: k for k, name in enumerate(FIELD_NAMES)}
 RUN_GRAPH = 1
 
@@ -49,6 +51,7 @@ class Params(C.Structure):
         ("recon", C.c_int),
         ("p_inner_kind", C.c_int), ("p_cheb_lo", C.c_double),
         ("p_mg_nu", C.c_int), ("p_mg_cw", C.c_double), ("p_mg_tail", C.c_int),
+        ("time_scheme", C.c_int), ("convective_linearization", C.c_int),
     ]
 
     def copy(self) -> "Params":
@@ -134,6 +137,9 @@ _SIGS = {
     "covof_state_set": [_VP, C.c_int, _VP],
     "covof_state_get": [_VP, C.c_int, _VP],
     "covof_state_field_dev": [_VP, C.c_int, C.POINTER(C.c_void_p)],
+    "covof_set_has_nm1": [_VP, C.c_int],
+    "covof_get_has_nm1": [_VP, C.POINTER(C.c_int)],
+    "covof_batch_set_has_nm1": [_VP, C.c_int],
     "covof_run_steps": [_VP, C.c_double, C.c_int, C.c_int, C.POINTER(RunStats)],
     "covof_set_launch": [_VP, C.POINTER(Launch)],
     "covof_get_launch": [_VP, C.POINTER(Launch)],

@@ -63,6 +63,8 @@ def make_params(nx: int, ny: int, lx: float, ly: float) -> Params:
     p.p_mg_nu = 2
     p.p_mg_cw = 1.9
     p.p_mg_tail = 2048
+    p.time_scheme = capi.TIME_EULER
+    p.convective_linearization = capi.CONV_LIN_PICARD
     return p
 
 

@@ -269,6 +269,7 @@ int per_case(covof_batch* b, F f) {
 int enqueue_batch_step(covof_batch* b, const double* dt, bool x_first) {
   CS(per_case(b, [&](int c, covof_handle* h) -> int {
     const size_t bytes = h->g * sizeof(double);
+    CS(rotate_history(h));
     CK(cudaMemcpyAsync(h->f_u_old, h->f_u, bytes, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->f_v_old, h->f_v, bytes, cudaMemcpyDeviceToDevice, h->stream));
     if (h->prm.enable_two_phase) {
@@ -471,6 +472,14 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
   return COVOF_OK;
 }
 
+int covof_batch_set_has_nm1(covof_batch* b, int has_nm1) {
+  if (!b) return COVOF_INVALID;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  drop_graphs(b);
+  for (covof_handle* h : b->h) CS(covof_set_has_nm1(h, has_nm1));
+  return COVOF_OK;
+}
+
 int covof_batch_state_set(covof_batch* b, int icase, int field, const double* host) {
   if (!b || icase < 0 || icase >= b->ncases) return COVOF_INVALID;
   return covof_state_set(b->h[icase], field, host);
@@ -503,7 +512,13 @@ int covof_batch_run_steps(covof_batch* b, const double* dt, int nsteps, int flag
     CK(cudaStreamSynchronize(h->stream));
   }
   bool graph = (flags & COVOF_RUN_GRAPH) != 0 && !b->graph_refused;
-  if (graph) {
+  // the first step of a case with Gear / Adams-Bashforth and no history yet
+  // runs eagerly; the graphs are captured with every has_nm1 set
+  bool first_plain = false;
+  for (covof_handle* h : b->h) first_plain |= needs_history(h->prm) && !h->has_nm1;
+  first_plain = first_plain && nsteps > 0;
+  auto ensure_graphs = [&]() -> int {
+    if (!graph) return COVOF_OK;
     bool same = b->graph[0] && b->graph_dt.size() == (size_t)b->ncases;
     for (int c = 0; same && c < b->ncases; ++c) same = b->graph_dt[c] == dt[c];
     if (!same) {
@@ -515,13 +530,24 @@ int covof_batch_run_steps(covof_batch* b, const double* dt, int nsteps, int flag
         return st;
       }
     }
-  }
+    return COVOF_OK;
+  };
+  if (!first_plain) CS(ensure_graphs());
   CK(cudaEventRecord(b->ev0, b->stream));
   for (int k = 0; k < nsteps; ++k) {
     const bool x_first = (b->step_count % 2) == 0;
-    if (graph) CK(cudaGraphLaunch(b->graph[x_first ? 0 : 1], b->stream));
+    if (graph && !(first_plain && k == 0)) CK(cudaGraphLaunch(b->graph[x_first ? 0 : 1], b->stream));
     else CS(enqueue_batch_step(b, dt, x_first));
     b->step_count += 1;
+    if (k == 0) {
+      for (covof_handle* h : b->h) h->has_nm1 = true;
+      if (first_plain) {
+        // the fork streams are idle before they join a capture
+        CK(cudaStreamSynchronize(b->stream));
+        drop_graphs(b);
+        CS(ensure_graphs());
+      }
+    }
   }
   CK(cudaEventRecord(b->ev1, b->stream));
   CK(cudaStreamSynchronize(b->stream));

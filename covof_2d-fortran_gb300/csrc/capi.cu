@@ -60,6 +60,7 @@ int ensure_fields(covof_handle* h) {
   CS(dalloc(&h->f_rho_u, g)); CS(dalloc(&h->f_rho_v, g)); CS(dalloc(&h->f_mu, g));
   CS(dalloc(&h->f_mu_node, g)); CS(dalloc(&h->f_fx, g)); CS(dalloc(&h->f_fy, g));
   CS(dalloc(&h->f_u_old, g)); CS(dalloc(&h->f_v_old, g)); CS(dalloc(&h->f_C, g));
+  CS(dalloc(&h->f_u_nm1, g)); CS(dalloc(&h->f_v_nm1, g));
   CS(dalloc(&h->f_rho, g)); CS(dalloc(&h->f_curv, g)); CS(dalloc(&h->f_b, g));
   CS(dalloc(&h->f_x2, 2 * g)); CS(dalloc(&h->f_seg, 3 * g));
   h->have_fields = true;
@@ -513,6 +514,14 @@ MomArgs mom_args(covof_handle* h, double dt, const double* u_n, const double* v_
   a.D = h->D; a.dx = P.dx; a.dy = P.dy; a.dt = dt; a.gx = P.gx; a.gy = P.gy;
   for (int s = 0; s < 4; ++s) { a.bc[s] = P.bc_type[s]; a.bcu[s] = P.bc_u[s]; a.bcv[s] = P.bc_v[s]; }
   a.conv = P.enable_convection; a.scheme = P.convective_scheme;
+  // history: the handle's u_nm1 / v_nm1 fields once has_nm1 is set
+  // (src/module_simulation.f90:508-520)
+  const bool gear = P.time_scheme == COVOF_TIME_GEAR && h->has_nm1;
+  a.alpha = gear ? 1.5 : 1.0;
+  a.gear_rhs = gear ? 1 : 0;
+  a.ab2 = P.convective_linearization == COVOF_CONV_LIN_AB2 ? 1 : 0;
+  a.ab2_ext = (a.ab2 && h->has_nm1) ? 1 : 0;
+  a.u_nm1 = h->f_u_nm1; a.v_nm1 = h->f_v_nm1;
   a.u_n = u_n; a.v_n = v_n; a.rho_u = rho_u; a.rho_v = rho_v; a.mu = mu; a.mu_node = mu_node;
   a.fx = fx; a.fy = fy; a.u_old = u_old; a.v_old = v_old;
   a.x = h->mx; a.rhs = h->mrhs; a.diag = h->mdiag; a.coef = h->mcoef; a.idiag = h->midiag;
@@ -525,7 +534,13 @@ MomArgs mom_args(covof_handle* h, double dt, const double* u_n, const double* v_
 }
 
 int check_mom_params(const covof_params& P) {
-  if (P.convective_scheme != COVOF_CONV_UPWIND && P.convective_scheme != COVOF_CONV_CENTERED)
+  if (P.convective_scheme != COVOF_CONV_UPWIND && P.convective_scheme != COVOF_CONV_CENTERED &&
+      P.convective_scheme != COVOF_CONV_TVD_SUPERBEE)
+    return COVOF_UNSUPPORTED;
+  if (P.time_scheme != 0 && P.time_scheme != COVOF_TIME_EULER && P.time_scheme != COVOF_TIME_GEAR)
+    return COVOF_UNSUPPORTED;
+  if (P.convective_linearization != 0 && P.convective_linearization != COVOF_CONV_LIN_PICARD &&
+      P.convective_linearization != COVOF_CONV_LIN_AB2)
     return COVOF_UNSUPPORTED;
   if (P.linear_solver != COVOF_LINEAR_BICGSTAB && P.linear_solver != COVOF_LINEAR_BICGSTAB2 &&
       P.linear_solver != COVOF_LINEAR_CG)
@@ -715,14 +730,32 @@ double** field_slot(covof_handle* h, int f) {
     case COVOF_FIELD_CURVATURE: return &h->f_curv;
     case COVOF_FIELD_U_OLD: return &h->f_u_old;
     case COVOF_FIELD_V_OLD: return &h->f_v_old;
+    case COVOF_FIELD_U_NM1: return &h->f_u_nm1;
+    case COVOF_FIELD_V_NM1: return &h->f_v_nm1;
     default: return nullptr;
   }
 }
 
+// Gear / BDF2 and Adams-Bashforth read the velocity of step n-1.
+bool needs_history(const covof_params& P) {
+  return P.time_scheme == COVOF_TIME_GEAR || P.convective_linearization == COVOF_CONV_LIN_AB2;
+}
+
+// u_nm1 = u_old (or u on a first step), src/module_simulation.f90:508-520;
+// enqueued before u_old = u.
+int rotate_history(covof_handle* h) {
+  if (!needs_history(h->prm)) return COVOF_OK;
+  const size_t bytes = h->g * sizeof(double);
+  CK(cudaMemcpyAsync(h->f_u_nm1, h->has_nm1 ? h->f_u_old : h->f_u, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->f_v_nm1, h->has_nm1 ? h->f_v_old : h->f_v, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  return COVOF_OK;
+}
+
 // Everything a step launches, in stream order, with no host synchronisation
-// (src/module_simulation.f90:492-559 for Euler + STANDARD_PROJECTION).
+// (src/module_simulation.f90:492-559 for STANDARD_PROJECTION).
 int enqueue_step(covof_handle* h, double dt, bool x_first) {
   const size_t bytes = h->g * sizeof(double);
+  CS(rotate_history(h));
   CK(cudaMemcpyAsync(h->f_u_old, h->f_u, bytes, cudaMemcpyDeviceToDevice, h->stream));
   CK(cudaMemcpyAsync(h->f_v_old, h->f_v, bytes, cudaMemcpyDeviceToDevice, h->stream));
   if (h->prm.enable_two_phase) {
@@ -790,21 +823,36 @@ int run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run_stats
   *h->h_run = RunStats{0, 0, 0, 0.0, 0.0, 0, -1, COVOF_OK, 0};
   CK(cudaMemcpyAsync(h->d_run, h->h_run, sizeof(RunStats), cudaMemcpyHostToDevice, h->stream));
   bool graph = (flags & COVOF_RUN_GRAPH) != 0 && !h->graph_refused;
-  if (graph && (!h->step_graph[0] || h->graph_dt != dt)) {
-    const int st = capture_steps(h, dt);
-    if (st == COVOF_UNSUPPORTED) {
-      h->graph_refused = true;
-      graph = false;
-    } else if (st != COVOF_OK) {
-      return st;
+  // A step without history (the first of a Gear / Adams-Bashforth run)
+  // differs from the later ones: it runs eagerly, and the graphs are
+  // captured with has_nm1 set.
+  const bool first_plain = needs_history(P) && !h->has_nm1 && nsteps > 0;
+  auto ensure_graphs = [&]() -> int {
+    if (graph && (!h->step_graph[0] || h->graph_dt != dt)) {
+      const int st = capture_steps(h, dt);
+      if (st == COVOF_UNSUPPORTED) {
+        h->graph_refused = true;
+        graph = false;
+      } else if (st != COVOF_OK) {
+        return st;
+      }
     }
-  }
+    return COVOF_OK;
+  };
+  if (!first_plain) CS(ensure_graphs());
   CK(cudaEventRecord(h->ev2, h->stream));
   for (int k = 0; k < nsteps; ++k) {
     const bool x_first = (h->vof_step_count % 2) == 0;
-    if (graph) CK(cudaGraphLaunch(h->step_graph[x_first ? 0 : 1], h->stream));
+    if (graph && !(first_plain && k == 0)) CK(cudaGraphLaunch(h->step_graph[x_first ? 0 : 1], h->stream));
     else CS(enqueue_step(h, dt, x_first));
     if (P.enable_two_phase) h->vof_step_count += 1;
+    if (!h->has_nm1) {
+      h->has_nm1 = true;
+      if (first_plain) {
+        drop_graphs(h);
+        CS(ensure_graphs());
+      }
+    }
   }
   CK(cudaEventRecord(h->ev3, h->stream));
   CK(cudaMemcpyAsync(h->h_run, h->d_run, sizeof(RunStats), cudaMemcpyDeviceToHost, h->stream));
@@ -868,6 +916,8 @@ void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly)
   p->p_mg_nu = 2;
   p->p_mg_cw = 1.9;
   p->p_mg_tail = 2048;
+  p->time_scheme = COVOF_TIME_EULER;
+  p->convective_linearization = COVOF_CONV_LIN_PICARD;
 }
 
 int covof_abi_version(void) { return COVOF_ABI_VERSION; }
@@ -927,7 +977,7 @@ int covof_destroy(covof_handle* h) {
   if (!h) return COVOF_INVALID;
   if (h->stream) cudaStreamSynchronize(h->stream);
   double** fl[] = {&h->f_u, &h->f_v, &h->f_p, &h->f_rho_u, &h->f_rho_v, &h->f_mu, &h->f_mu_node,
-                   &h->f_fx, &h->f_fy, &h->f_u_old, &h->f_v_old, &h->f_C, &h->f_rho, &h->f_curv,
+                   &h->f_fx, &h->f_fy, &h->f_u_old, &h->f_v_old, &h->f_u_nm1, &h->f_v_nm1, &h->f_C, &h->f_rho, &h->f_curv,
                    &h->f_b, &h->f_x2, &h->f_seg, &h->px, &h->pb, &h->pr, &h->pd, &h->pAd,
                    &h->pax, &h->pay, &h->paP, &h->pisd, &h->pinvD, &h->pd2, &h->pz, &h->pw, &h->pp, &h->pq, &h->mx, &h->mrhs, &h->mdiag, &h->cs, &h->seg, &h->mcoef, &h->midiag,
                    &h->cnx, &h->cny, &h->ckap, &h->part, &h->arhs, &h->apsi, &h->apart, &h->asum,
@@ -1163,13 +1213,15 @@ int covof_momentum_apply(covof_handle* h, double dt, const double* xu, const dou
   CS(h2d(h, h->f_rho_u, rho_u, g)); CS(h2d(h, h->f_rho_v, rho_v, g));
   CS(h2d(h, h->f_mu, mu, g)); CS(h2d(h, h->f_mu_node, mu_node, g));
   CS(h2d(h, h->f_x2, xu, g)); CS(h2d(h, h->f_x2 + g, xv, g));
-  CS(h2d(h, h->f_u_old, yu, g)); CS(h2d(h, h->f_v_old, yv, g));
+  double* y = h->mv[0];  // 2g doubles
+  CS(h2d(h, y, yu, g)); CS(h2d(h, y + g, yv, g));
+  // u_old / v_old / u_nm1 / v_nm1 (Adams-Bashforth, Gear) are the resident fields
   MomArgs a = mom_args(h, dt, h->f_u, h->f_v, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node,
-                       nullptr, nullptr, nullptr, nullptr);
+                       nullptr, nullptr, h->f_u_old, h->f_v_old);
   const dim3 blk(32, 8), grd = grid2(h->prm.nx + 1, h->prm.ny + 1, blk);
-  k_mom_apply<<<grd, blk, 0, h->stream>>>(a, h->f_x2, h->f_x2 + g, h->f_u_old, h->f_v_old);
+  k_mom_apply<<<grd, blk, 0, h->stream>>>(a, h->f_x2, h->f_x2 + g, y, y + g);
   CK(cudaGetLastError());
-  CS(d2h(h, yu, h->f_u_old, g)); CS(d2h(h, yv, h->f_v_old, g));
+  CS(d2h(h, yu, y, g)); CS(d2h(h, yv, y + g, g));
   return sync(h);
 }
 
@@ -1357,6 +1409,22 @@ int covof_state_get(covof_handle* h, int field, double* host) {
   if (!slot) return COVOF_INVALID;
   CS(d2h(h, host, *slot, h->g));
   return sync(h);
+}
+
+int covof_set_has_nm1(covof_handle* h, int has_nm1) {
+  if (!h) return COVOF_INVALID;
+  if (h->has_nm1 != (has_nm1 != 0)) {
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    drop_graphs(h);  // the captured steps bake the flag in
+  }
+  h->has_nm1 = has_nm1 != 0;
+  return COVOF_OK;
+}
+
+int covof_get_has_nm1(const covof_handle* h, int* has_nm1) {
+  if (!h || !has_nm1) return COVOF_INVALID;
+  *has_nm1 = h->has_nm1 ? 1 : 0;
+  return COVOF_OK;
 }
 
 int covof_state_field_dev(covof_handle* h, int field, double** dev) {

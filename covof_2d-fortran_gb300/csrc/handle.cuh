@@ -64,11 +64,13 @@ struct covof_handle {
   Dims D{};
   size_t g = 0;
   int vof_step_count = 0;
+  bool has_nm1 = false;  // u_nm1 / v_nm1 hold step n-1 (fields%has_nm1)
   // caller-field mirrors (host-pointer entry points)
   bool have_fields = false;
   double *f_u = nullptr, *f_v = nullptr, *f_p = nullptr, *f_rho_u = nullptr, *f_rho_v = nullptr,
          *f_mu = nullptr, *f_mu_node = nullptr, *f_fx = nullptr, *f_fy = nullptr,
-         *f_u_old = nullptr, *f_v_old = nullptr, *f_C = nullptr, *f_rho = nullptr,
+         *f_u_old = nullptr, *f_v_old = nullptr, *f_u_nm1 = nullptr, *f_v_nm1 = nullptr,
+         *f_C = nullptr, *f_rho = nullptr,
          *f_curv = nullptr, *f_b = nullptr, *f_x2 = nullptr, *f_seg = nullptr;
   // Poisson scratch
   bool have_poisson = false;
@@ -147,6 +149,9 @@ int mom_pre(covof_handle* h, double dt, double* u, double* v, const double* rho_
             const double* v_old, MomArgs* out);
 int mom_post(covof_handle* h, const MomArgs& a, double* u, double* v);
 int wy_step_dev(covof_handle* h, double dt, int x_first, const double* u, const double* v, double* C);
+bool needs_history(const covof_params& P);
+int rotate_history(covof_handle* h);
+void drop_graphs(covof_handle* h);
 int vof_bc_dev(covof_handle* h, double* C);
 int props_dev(covof_handle* h, double* C, double* rho, double* rho_u, double* rho_v, double* mu,
               double* mu_node);

@@ -1,6 +1,7 @@
 // momentum.cu -- momentum predictor of the STANDARD_PROJECTION step on one
-// GB300: matrix-free MAC momentum operator (unsteady + upwind/centred
-// convection with Picard linearisation + 2 mu normal stress + mu_node shear),
+// GB300: matrix-free MAC momentum operator (Euler or Gear/BDF2 unsteady
+// term + upwind / centred / TVD-Superbee convection, Picard or
+// Adams-Bashforth linearisation + 2 mu normal stress + mu_node shear),
 // its Jacobi diagonal and right-hand side, and persistent cooperative
 // BiCGSTAB / BiCGSTAB(2) / CG kernels that run a whole Krylov solve in one
 // launch with device-side convergence tests.
@@ -67,32 +68,75 @@ __device__ __forceinline__ double tv(const MomArgs& a, const double* xv, int i, 
   return __ldcg(xv + D.id(i, j));
 }
 
-// src/module_navier_stokes.f90:2388-2416 (UPWIND / CENTERED)
+// src/module_navier_stokes.f90:2388-2416 conv_face_flux.  The operand
+// values pl, pr are of type T (doubles, or linear forms for the row
+// coefficients); the TVD limiter reads only fields_old values (q*), so the
+// face flux stays linear in the operand.
 template <class T>
-__device__ __forceinline__ T conv_face_flux(int scheme, double flux, const T& pl, const T& pr) {
+__device__ __forceinline__ T conv_face_flux(int scheme, double flux, const T& pl, const T& pr, double qLL,
+                                            double qL, double qR, double qRR, bool hasLL, bool hasRR) {
   if (scheme == COVOF_CONV_CENTERED) return 0.5 * flux * (pl + pr);
-  return (flux >= 0.0) ? flux * pl : flux * pr;
+  if (scheme == COVOF_CONV_UPWIND) return (flux >= 0.0) ? flux * pl : flux * pr;
+  // TVD, Superbee limiter
+  const double dq = qR - qL;
+  double psi = 0.0;
+  if (flux >= 0.0) {
+    if (hasLL && fabs(dq) > 1.0e-14) {
+      const double r = (qL - qLL) / dq;
+      psi = fmax(fmax(0.0, fmin(2.0 * r, 1.0)), fmin(r, 2.0));
+    }
+    return flux * (pl + 0.5 * psi * (pr - pl));
+  }
+  if (hasRR && fabs(dq) > 1.0e-14) {
+    const double r = (qRR - qR) / dq;
+    psi = fmax(fmax(0.0, fmin(2.0 * r, 1.0)), fmin(r, 2.0));
+  }
+  return flux * (pr + 0.5 * psi * (pl - pr));
 }
 
-// src/module_navier_stokes.f90:2418-2457 compute_u_conv_fluxes (PICARD)
+// src/module_navier_stokes.f90:2418-2457 compute_u_conv_fluxes: the
+// advecting velocity is fields%u (PICARD) or fields%u_old (AB2),
+// extrapolated 2 u^n - u^(n-1) when the history exists
 __device__ __forceinline__ void u_fluxes(const MomArgs& a, int i, int j, double& FE, double& FW,
                                          double& FN, double& FS) {
   const Dims& D = a.D;
-  const double un = a.u_n[D.id(i, j)], unE = a.u_n[D.id(i + 1, j)], unW = a.u_n[D.id(i - 1, j)];
-  const double vnN = 0.5 * (a.v_n[D.id(i - 1, j + 1)] + a.v_n[D.id(i, j + 1)]);
-  const double vnS = 0.5 * (a.v_n[D.id(i - 1, j)] + a.v_n[D.id(i, j)]);
+  const double* ub = a.ab2 ? a.u_old : a.u_n;
+  const double* vb = a.ab2 ? a.v_old : a.v_n;
+  double un = ub[D.id(i, j)], unE = ub[D.id(i + 1, j)], unW = ub[D.id(i - 1, j)];
+  double vnN = 0.5 * (vb[D.id(i - 1, j + 1)] + vb[D.id(i, j + 1)]);
+  double vnS = 0.5 * (vb[D.id(i - 1, j)] + vb[D.id(i, j)]);
+  if (a.ab2_ext) {
+    un = 2.0 * un - a.u_nm1[D.id(i, j)];
+    unE = 2.0 * unE - a.u_nm1[D.id(i + 1, j)];
+    unW = 2.0 * unW - a.u_nm1[D.id(i - 1, j)];
+    const double vmN = 0.5 * (a.v_nm1[D.id(i - 1, j + 1)] + a.v_nm1[D.id(i, j + 1)]);
+    const double vmS = 0.5 * (a.v_nm1[D.id(i - 1, j)] + a.v_nm1[D.id(i, j)]);
+    vnN = 2.0 * vnN - vmN;
+    vnS = 2.0 * vnS - vmS;
+  }
   FE = 0.5 * (un + unE) * a.dy;
   FW = 0.5 * (unW + un) * a.dy;
   FN = vnN * a.dx;
   FS = vnS * a.dx;
 }
-// src/module_navier_stokes.f90:2459-2498 compute_v_conv_fluxes (PICARD)
+// src/module_navier_stokes.f90:2459-2498 compute_v_conv_fluxes
 __device__ __forceinline__ void v_fluxes(const MomArgs& a, int i, int j, double& FE, double& FW,
                                          double& FN, double& FS) {
   const Dims& D = a.D;
-  const double vn = a.v_n[D.id(i, j)], vnN = a.v_n[D.id(i, j + 1)], vnS = a.v_n[D.id(i, j - 1)];
-  const double unE = 0.5 * (a.u_n[D.id(i + 1, j - 1)] + a.u_n[D.id(i + 1, j)]);
-  const double unW = 0.5 * (a.u_n[D.id(i, j - 1)] + a.u_n[D.id(i, j)]);
+  const double* ub = a.ab2 ? a.u_old : a.u_n;
+  const double* vb = a.ab2 ? a.v_old : a.v_n;
+  double vn = vb[D.id(i, j)], vnN = vb[D.id(i, j + 1)], vnS = vb[D.id(i, j - 1)];
+  double unE = 0.5 * (ub[D.id(i + 1, j - 1)] + ub[D.id(i + 1, j)]);
+  double unW = 0.5 * (ub[D.id(i, j - 1)] + ub[D.id(i, j)]);
+  if (a.ab2_ext) {
+    vn = 2.0 * vn - a.v_nm1[D.id(i, j)];
+    vnN = 2.0 * vnN - a.v_nm1[D.id(i, j + 1)];
+    vnS = 2.0 * vnS - a.v_nm1[D.id(i, j - 1)];
+    const double umE = 0.5 * (a.u_nm1[D.id(i + 1, j - 1)] + a.u_nm1[D.id(i + 1, j)]);
+    const double umW = 0.5 * (a.u_nm1[D.id(i, j - 1)] + a.u_nm1[D.id(i, j)]);
+    unE = 2.0 * unE - umE;
+    unW = 2.0 * unW - umW;
+  }
   FE = unE * a.dy;
   FW = unW * a.dy;
   FN = 0.5 * (vn + vnN) * a.dx;
@@ -199,20 +243,28 @@ __device__ auto mom_apply_gen(const MomArgs& a, int part, int i, int j, const S&
   const int k = D.id(i, j);
   if (part == 0) {
     const double rho = a.rho_u[k];
-    const double diag_bc = ((1.0 * rho) / dt) * dvol;
+    const double diag_bc = ((a.alpha * rho) / dt) * dvol;
     if (i == 1) return diag_bc * src.u(1, j);        // DIRICHLET / FREESLIP west
     if (i == nx + 1) return diag_bc * src.u(nx + 1, j);
     const auto uc = src.u(i, j);
-    auto val = (((1.0 * rho) / dt) * uc) * dvol;
+    auto val = (((a.alpha * rho) / dt) * uc) * dvol;
     const auto uE = src.u(i + 1, j), uW = src.u(i - 1, j);
     const auto uN = src.u(i, j + 1), uS = src.u(i, j - 1);
     if (a.conv) {
       double FE, FW, FN, FS;
       u_fluxes(a, i, j, FE, FW, FN, FS);
-      const auto pE = conv_face_flux(a.scheme, FE, uc, uE);
-      const auto pW = conv_face_flux(a.scheme, FW, uW, uc);
-      const auto pN = conv_face_flux(a.scheme, FN, uc, uN);
-      const auto pS = conv_face_flux(a.scheme, FS, uS, uc);
+      // limiter inputs: fields_old%u around the face (:533-547)
+      const double* q = a.u_n;
+      const bool has_ee = i + 2 <= nx + 1, has_ww = i - 2 >= 0, has_nn = j + 2 <= ny + 1, has_ss = j - 2 >= 0;
+      const double q_ee = has_ee ? q[D.id(i + 2, j)] : 0.0;
+      const double q_ww = has_ww ? q[D.id(i - 2, j)] : 0.0;
+      const double q_nn = has_nn ? q[D.id(i, j + 2)] : 0.0;
+      const double q_ss = has_ss ? q[D.id(i, j - 2)] : 0.0;
+      const double qc = q[k], qE = q[k + 1], qW = q[k - 1], qN = q[k + D.P], qS = q[k - D.P];
+      const auto pE = conv_face_flux(a.scheme, FE, uc, uE, qW, qc, qE, q_ee, true, has_ee);
+      const auto pW = conv_face_flux(a.scheme, FW, uW, uc, q_ww, qW, qc, qE, has_ww, true);
+      const auto pN = conv_face_flux(a.scheme, FN, uc, uN, qS, qc, qN, q_nn, true, has_nn);
+      const auto pS = conv_face_flux(a.scheme, FS, uS, uc, q_ss, qS, qc, qN, has_ss, true);
       val = val + rho * (pE - pW + pN - pS);
     }
     const double muE = a.mu[k], muW = a.mu[k - 1];
@@ -226,19 +278,27 @@ __device__ auto mom_apply_gen(const MomArgs& a, int part, int i, int j, const S&
     return val;
   }
   const double rho = a.rho_v[k];
-  const double diag_bc = ((1.0 * rho) / dt) * dvol;
+  const double diag_bc = ((a.alpha * rho) / dt) * dvol;
   if ((j == 1 && is_wall(a, SB)) || (j == ny + 1 && is_wall(a, ST))) return diag_bc * src.v(i, j);
   const auto vc = src.v(i, j);
-  auto val = (((1.0 * rho) / dt) * vc) * dvol;
+  auto val = (((a.alpha * rho) / dt) * vc) * dvol;
   const auto vE = src.v(i + 1, j), vW = src.v(i - 1, j);
   const auto vN = src.v(i, j + 1), vS = src.v(i, j - 1);
   if (a.conv) {
     double FE, FW, FN, FS;
     v_fluxes(a, i, j, FE, FW, FN, FS);
-    const auto pE = conv_face_flux(a.scheme, FE, vc, vE);
-    const auto pW = conv_face_flux(a.scheme, FW, vW, vc);
-    const auto pN = conv_face_flux(a.scheme, FN, vc, vN);
-    const auto pS = conv_face_flux(a.scheme, FS, vS, vc);
+    // limiter inputs: fields_old%v around the face (:666-680)
+    const double* q = a.v_n;
+    const bool has_ee = i + 2 <= nx + 1, has_ww = i - 2 >= 0, has_nn = j + 2 <= ny + 1, has_ss = j - 2 >= 0;
+    const double q_ee = has_ee ? q[D.id(i + 2, j)] : 0.0;
+    const double q_ww = has_ww ? q[D.id(i - 2, j)] : 0.0;
+    const double q_nn = has_nn ? q[D.id(i, j + 2)] : 0.0;
+    const double q_ss = has_ss ? q[D.id(i, j - 2)] : 0.0;
+    const double qc = q[k], qE = q[k + 1], qW = q[k - 1], qN = q[k + D.P], qS = q[k - D.P];
+    const auto pE = conv_face_flux(a.scheme, FE, vc, vE, qW, qc, qE, q_ee, true, has_ee);
+    const auto pW = conv_face_flux(a.scheme, FW, vW, vc, q_ww, qW, qc, qE, has_ww, true);
+    const auto pN = conv_face_flux(a.scheme, FN, vc, vN, qS, qc, qN, q_nn, true, has_nn);
+    const auto pS = conv_face_flux(a.scheme, FS, vS, vc, q_ss, qS, qc, qN, has_ss, true);
     val = val + rho * (pE - pW + pN - pS);
   }
   const double muN = a.mu[k], muS = a.mu[k - D.P];
@@ -270,7 +330,7 @@ __global__ void k_mom_diag(MomArgs a) {
   if (i <= nx + 1 && j <= ny) {
     const int k = D.id(i, j);
     const double rho = a.rho_u[k];
-    double Du = ((1.0 * rho) / dt_safe) * dvol;
+    double Du = ((a.alpha * rho) / dt_safe) * dvol;
     if (Du <= 1.0e-30) Du = 1.0;
     double out;
     if (i == 1 || i == nx + 1) {
@@ -304,7 +364,7 @@ __global__ void k_mom_diag(MomArgs a) {
   if (i <= nx && j <= ny + 1) {
     const int k = D.id(i, j);
     const double rho = a.rho_v[k];
-    double Dv = ((1.0 * rho) / dt_safe) * dvol;
+    double Dv = ((a.alpha * rho) / dt_safe) * dvol;
     if (Dv <= 1.0e-30) Dv = 1.0;
     double out;
     if ((j == 1 && is_wall(a, SB)) || (j == ny + 1 && is_wall(a, ST))) {
@@ -337,7 +397,8 @@ __global__ void k_mom_diag(MomArgs a) {
   }
 }
 
-// Right-hand side, src/module_navier_stokes.f90:817-1088 (SP, Euler, constant walls).
+// Right-hand side, src/module_navier_stokes.f90:817-1088 (SP, constant walls;
+// Euler, or the Gear / BDF2 inertial term rho (2 u^n - u^(n-1) / 2) / dt).
 __global__ void k_mom_rhs(MomArgs a) {
   const Dims& D = a.D;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -348,14 +409,20 @@ __global__ void k_mom_rhs(MomArgs a) {
   if (i <= nx + 1 && j <= ny) {
     const int k = D.id(i, j);
     const double rho = a.rho_u[k];
-    const double diag_bc = ((1.0 * rho) / dt) * dvol;
+    const double diag_bc = ((a.alpha * rho) / dt) * dvol;
     double out;
     if (i == 1) {
       out = diag_bc * (a.bc[SL] == COVOF_BC_DIRICHLET ? a.bcu[SL] : 0.0);
     } else if (i == nx + 1) {
       out = diag_bc * (a.bc[SR] == COVOF_BC_DIRICHLET ? a.bcu[SR] : 0.0);
     } else {
-      double val = (rho / dt) * a.u_old[k] * dvol;
+      double val;
+      if (a.gear_rhs) {
+        const double u_in = rho * (2.0 * a.u_old[k] - 0.5 * a.u_nm1[k]);
+        val = (u_in / dt) * dvol;
+      } else {
+        val = (rho / dt) * a.u_old[k] * dvol;
+      }
       val = val + rho * a.gx * dvol;
       val = val + a.fx[k] * dvol;
       if (j == ny && a.bc[ST] == COVOF_BC_DIRICHLET) {
@@ -375,14 +442,20 @@ __global__ void k_mom_rhs(MomArgs a) {
   if (i <= nx && j <= ny + 1) {
     const int k = D.id(i, j);
     const double rho = a.rho_v[k];
-    const double diag_bc = ((1.0 * rho) / dt) * dvol;
+    const double diag_bc = ((a.alpha * rho) / dt) * dvol;
     double out;
     if (j == 1 && is_wall(a, SB)) {
       out = diag_bc * (a.bc[SB] == COVOF_BC_DIRICHLET ? a.bcv[SB] : 0.0);
     } else if (j == ny + 1 && is_wall(a, ST)) {
       out = diag_bc * (a.bc[ST] == COVOF_BC_DIRICHLET ? a.bcv[ST] : 0.0);
     } else {
-      double val = (rho / dt) * a.v_old[k] * dvol;
+      double val;
+      if (a.gear_rhs) {
+        const double v_in = rho * (2.0 * a.v_old[k] - 0.5 * a.v_nm1[k]);
+        val = (v_in / dt) * dvol;
+      } else {
+        val = (rho / dt) * a.v_old[k] * dvol;
+      }
       val = val + rho * a.gy * dvol;
       val = val + a.fy[k] * dvol;
       if (i == 1 && a.bc[SL] == COVOF_BC_DIRICHLET) {

@@ -15,6 +15,13 @@ struct MomArgs {
   int bc[4];
   double bcu[4], bcv[4];
   int conv, scheme;
+  // time scheme and linearisation with the history they need
+  // (src/module_navier_stokes.f90:481-486, 2427-2457): alpha = 1.5 for Gear
+  // once step n-1 is known, else 1; gear_rhs: the BDF2 inertial term; ab2:
+  // advect with u_old / v_old; ab2_ext: extrapolate 2 u^n - u^(n-1)
+  double alpha;
+  int gear_rhs, ab2, ab2_ext;
+  const double* u_nm1; const double* v_nm1;
   // fields_old of the operator (u^n with ghosts) and material properties
   const double* u_n; const double* v_n;
   const double* rho_u; const double* rho_v; const double* mu; const double* mu_node;

@@ -54,9 +54,12 @@ module covof_gpu_bridge
      integer(c_int) :: p_mg_nu
      real(c_double) :: p_mg_cw
      integer(c_int) :: p_mg_tail
+     integer(c_int) :: time_scheme
+     integer(c_int) :: convective_linearization
   end type covof_params_t
 
   integer(c_int), parameter :: COVOF_OK = 0, COVOF_MAXITER = 1, COVOF_BREAKDOWN = 2
+  integer(c_int), parameter :: COVOF_FIELD_U_NM1 = 14, COVOF_FIELD_V_NM1 = 15
 
   interface
      subroutine covof_params_default(p, nx, ny, lx, ly) bind(C, name="covof_params_default")
@@ -89,6 +92,19 @@ module covof_gpu_bridge
        integer(c_int), intent(out) :: total_iters
        real(c_double), intent(out) :: relres
      end function covof_sp_step
+
+     integer(c_int) function covof_state_set(h, field, host) bind(C, name="covof_state_set")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: field
+       real(c_double), intent(in) :: host(*)
+     end function covof_state_set
+
+     integer(c_int) function covof_set_has_nm1(h, has_nm1) bind(C, name="covof_set_has_nm1")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int), value :: has_nm1
+     end function covof_set_has_nm1
 
      integer(c_int) function covof_vof_wy_step(h, dt, x_first, u, v, c) &
                                                bind(C, name="covof_vof_wy_step")
@@ -129,10 +145,10 @@ contains
        write(*, '(A)') "covof_gpu_bridge: the GPU path runs one single-domain rank"
        error stop 1
     end if
-    if (cfg%time_scheme /= TIME_SCHEME_EULER .or. cfg%convective_linearization /= CONV_LIN_PICARD .or. &
+    if (cfg%convective_linearization == CONV_LIN_NEWTON .or. &
         cfg%obs_enabled .or. cfg%enable_ssp_rk3_momentum .or. cfg%compressible .or. &
         cfg%enable_svof_smoothing .or. cfg%use_markers .or. cfg%enable_diffusion_smoothing) then
-       write(*, '(A)') "covof_gpu_bridge: option outside the GPU path (Euler/Picard, no obstacle/SVOF/markers)"
+       write(*, '(A)') "covof_gpu_bridge: option outside the GPU path (no Newton/obstacle/SVOF/markers)"
        error stop 1
     end if
     call covof_params_default(p, int(mesh%nx_global, c_int), int(mesh%ny_global, c_int), &
@@ -149,6 +165,8 @@ contains
     p%tol = cfg%tol
     p%enable_convection = merge(1_c_int, 0_c_int, cfg%enable_convection)
     p%convective_scheme = cfg%convective_scheme
+    p%time_scheme = cfg%time_scheme
+    p%convective_linearization = cfg%convective_linearization
     ! Poisson: the reference's hard-coded tolerance and cap
     ! (src/module_simulation.f90:2437-2438), Jacobi-PCG on the GPU.
     p%p_tol = 1.0e-7_c_double
@@ -188,6 +206,14 @@ contains
     integer(c_int) :: st, it
     real(c_double) :: rr
     call ensure_handle(mesh, cfg)
+    ! Gear / BDF2 and Adams-Bashforth read the n-1 history (fields%u_nm1,
+    ! has_nm1, set by the loop at src/module_simulation.f90:508-520)
+    if (cfg%time_scheme == TIME_SCHEME_GEAR .or. cfg%convective_linearization == CONV_LIN_ADAMS_BASHFORTH) then
+       st = covof_state_set(handle, COVOF_FIELD_U_NM1, fields%u_nm1)
+       if (st == COVOF_OK) st = covof_state_set(handle, COVOF_FIELD_V_NM1, fields%v_nm1)
+       if (st == COVOF_OK) st = covof_set_has_nm1(handle, merge(1_c_int, 0_c_int, fields%has_nm1))
+       if (st /= COVOF_OK) call fail("covof_state_set", st)
+    end if
     st = covof_sp_step(handle, real(dt, c_double), fields%u, fields%v, fields%p, &
                        fields%rho_u, fields%rho_v, fields%mu, fields%mu_node, &
                        fields%fx_sigma, fields%fy_sigma, fields%u_old, fields%v_old, it, rr)

@@ -70,13 +70,15 @@ class Fields:
     curvature: np.ndarray
     u_old: np.ndarray
     v_old: np.ndarray
+    u_nm1: np.ndarray   # velocity of step n-1 (Gear / BDF2, Adams-Bashforth)
+    v_nm1: np.ndarray
 
     @classmethod
     def allocate(cls, p: Params) -> "Fields":
         z = lambda val=0.0: new_field(p, val)  # noqa: E731
         return cls(u=z(), v=z(), p=z(), C=z(1.0), rho=z(1.0), rho_u=z(1.0), rho_v=z(1.0),
                    mu=z(1.0e-3), mu_node=z(1.0e-3), fx_sigma=z(), fy_sigma=z(), curvature=z(),
-                   u_old=z(), v_old=z())
+                   u_old=z(), v_old=z(), u_nm1=z(), v_nm1=z())
 
     def copy(self) -> "Fields":
         return Fields(**{k: getattr(self, k).copy() for k in self.__dataclass_fields__})
@@ -143,9 +145,32 @@ class Solver:
     def vof_step_count(self, n: int):
         self._check(self.lib.covof_set_vof_step_count(self.h, int(n)), "set_vof_step_count")
 
+    # -- time history (Gear / BDF2, Adams-Bashforth) ---------------------------
+    @property
+    def has_nm1(self) -> int:
+        n = C.c_int()
+        self._check(self.lib.covof_get_has_nm1(self.h, C.byref(n)), "get_has_nm1")
+        return n.value
+
+    @has_nm1.setter
+    def has_nm1(self, flag: int):
+        self._check(self.lib.covof_set_has_nm1(self.h, int(bool(flag))), "set_has_nm1")
+
+    def _history(self, f: Fields | None, has_nm1):
+        """Upload f.u_nm1 / f.v_nm1 and set has_nm1 (when given) before a
+        predictor call; the C entry points read the handle's history."""
+        if has_nm1 is not None:
+            self.has_nm1 = has_nm1
+        if f is not None:
+            for name in ("u_nm1", "v_nm1"):
+                self._check(self.lib.covof_state_set(self.h, capi.FIELD[name], _ptr(getattr(f, name))),
+                            "covof_state_set")
+
     # -- STANDARD_PROJECTION --------------------------------------------------
-    def sim_solve_standard_projection(self, dt: float, f: Fields):
-        """One SP step on host fields; returns (total_iters, poisson_relres, status)."""
+    def sim_solve_standard_projection(self, dt: float, f: Fields, has_nm1=None):
+        """One SP step on host fields; returns (total_iters, poisson_relres, status).
+        has_nm1 (with f.u_nm1, f.v_nm1): the n-1 history for Gear / AB2."""
+        self._history(f, has_nm1)
         it, rr = C.c_int(), C.c_double()
         st = self.lib.covof_sp_step(self.h, dt, _ptr(f.u), _ptr(f.v), _ptr(f.p), _ptr(f.rho_u),
                                     _ptr(f.rho_v), _ptr(f.mu), _ptr(f.mu_node), _ptr(f.fx_sigma),
@@ -153,14 +178,22 @@ class Solver:
                                     C.byref(it), C.byref(rr))
         return it.value, rr.value, self._check(st, "covof_sp_step")
 
-    def predictor(self, dt: float, f: Fields):
+    def predictor(self, dt: float, f: Fields, has_nm1=None):
+        self._history(f, has_nm1)
         it = C.c_int()
         st = self.lib.covof_predictor(self.h, dt, _ptr(f.u), _ptr(f.v), _ptr(f.rho_u), _ptr(f.rho_v),
                                       _ptr(f.mu), _ptr(f.mu_node), _ptr(f.fx_sigma), _ptr(f.fy_sigma),
                                       _ptr(f.u_old), _ptr(f.v_old), C.byref(it))
         return it.value, self._check(st, "covof_predictor")
 
-    def momentum_apply(self, dt, xu, xv, u_n, v_n, rho_u, rho_v, mu, mu_node):
+    def momentum_apply(self, dt, xu, xv, u_n, v_n, rho_u, rho_v, mu, mu_node, u_old=None, v_old=None,
+                       u_nm1=None, v_nm1=None, has_nm1=0):
+        """A x on host arrays.  u_old .. has_nm1: the history Adams-Bashforth
+        and Gear read (uploaded to the resident u_old / v_old / u_nm1 / v_nm1)."""
+        for name, a in (("u_old", u_old), ("v_old", v_old), ("u_nm1", u_nm1), ("v_nm1", v_nm1)):
+            if a is not None:
+                self._check(self.lib.covof_state_set(self.h, capi.FIELD[name], _ptr(a)), "covof_state_set")
+        self.has_nm1 = has_nm1
         yu = np.zeros_like(xu)
         yv = np.zeros_like(xv)
         st = self.lib.covof_momentum_apply(self.h, dt, _ptr(xu), _ptr(xv), _ptr(yu), _ptr(yv),
@@ -339,6 +372,9 @@ class Batch:
         if st in _RAISE:
             raise CovofError(st, where)
         return st
+
+    def set_has_nm1(self, flag: int):
+        self._check(self.lib.covof_batch_set_has_nm1(self.h, int(bool(flag))), "covof_batch_set_has_nm1")
 
     def state_set(self, i: int, f: Fields):
         for name in capi.FIELD_NAMES:

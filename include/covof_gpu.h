@@ -52,8 +52,18 @@ enum { COVOF_LINEAR_BICGSTAB2 = 1, COVOF_LINEAR_BICGSTAB = 2, COVOF_LINEAR_CG = 
  * Poisson only, where it names the reference's symmetric Gauss-Seidel sweep
  * pair (src/module_simulation.f90:2709-2758). */
 enum { COVOF_PRECOND_NONE = 0, COVOF_PRECOND_JACOBI = 1, COVOF_PRECOND_SSOR = 2, COVOF_PRECOND_ILU0 = 3 };
-/* Convective schemes: CONV_* in src/module_constants.f90:76-78. */
-enum { COVOF_CONV_UPWIND = 1, COVOF_CONV_CENTERED = 2 };
+/* Convective schemes: CONV_* in src/module_constants.f90:81-85. */
+enum { COVOF_CONV_UPWIND = 1, COVOF_CONV_CENTERED = 2, COVOF_CONV_TVD_SUPERBEE = 3 };
+/* Momentum time scheme: TIME_SCHEME_* in src/module_constants.f90:132-134
+ * (0 is read as EULER).  GEAR (BDF2) applies once the velocity of step n-1
+ * is known (has_nm1, covof_set_has_nm1). */
+enum { COVOF_TIME_EULER = 1, COVOF_TIME_GEAR = 2 };
+/* Linearisation of the convective term: CONV_LIN_* in
+ * src/module_constants.f90:137-140 (0 is read as PICARD).  PICARD advects with
+ * the current velocity, AB2 with the velocity at the start of the step,
+ * extrapolated 2 u^n - u^(n-1) once has_nm1 holds.  NEWTON returns
+ * COVOF_UNSUPPORTED. */
+enum { COVOF_CONV_LIN_PICARD = 1, COVOF_CONV_LIN_AB2 = 2, COVOF_CONV_LIN_NEWTON = 3 };
 /* Interface reconstruction (cfg%reconstruction_method). */
 enum { COVOF_RECON_PLIC = 0, COVOF_RECON_ELVIRA = 1 };
 /* Pressure gauge.  REFERENCE: 1e-12*dvol diagonal shift + mean removal
@@ -112,6 +122,10 @@ typedef struct covof_params {
                           * stiffness of aggregation coarse operators (over-correction) */
   int p_mg_tail;         /* COVOF_INNER_MG: levels of at most this many cells run in one block's
                           * shared memory (0: 2048) */
+  /* momentum time scheme and convective linearisation (cfg%time_scheme,
+   * cfg%convective_linearization): COVOF_TIME_*, COVOF_CONV_LIN_* */
+  int time_scheme;
+  int convective_linearization;
 } covof_params;
 enum { COVOF_INNER_CHEBYSHEV = 0, COVOF_INNER_CG = 1, COVOF_INNER_CHEBYSHEV_STREAM = 2, COVOF_INNER_MG = 3 };
 
@@ -284,7 +298,8 @@ enum {
   COVOF_FIELD_U = 0, COVOF_FIELD_V = 1, COVOF_FIELD_P = 2, COVOF_FIELD_C = 3,
   COVOF_FIELD_RHO = 4, COVOF_FIELD_RHO_U = 5, COVOF_FIELD_RHO_V = 6, COVOF_FIELD_MU = 7,
   COVOF_FIELD_MU_NODE = 8, COVOF_FIELD_FX_SIGMA = 9, COVOF_FIELD_FY_SIGMA = 10,
-  COVOF_FIELD_CURVATURE = 11, COVOF_FIELD_U_OLD = 12, COVOF_FIELD_V_OLD = 13, COVOF_NFIELDS = 14
+  COVOF_FIELD_CURVATURE = 11, COVOF_FIELD_U_OLD = 12, COVOF_FIELD_V_OLD = 13,
+  COVOF_FIELD_U_NM1 = 14, COVOF_FIELD_V_NM1 = 15, COVOF_NFIELDS = 16
 };
 /* Copy one (nx+2)*(ny+2) field between the host and the handle's resident
  * copy (synchronous). */
@@ -292,6 +307,14 @@ int covof_state_set(covof_handle* h, int field, const double* host);
 int covof_state_get(covof_handle* h, int field, double* host);
 /* Device address of the resident copy (valid until covof_destroy). */
 int covof_state_field_dev(covof_handle* h, int field, double** dev);
+/* Whether the resident u_nm1 / v_nm1 hold the velocity of step n-1
+ * (fields%has_nm1, src/module_simulation.f90:508-520): Gear / BDF2 and the
+ * Adams-Bashforth extrapolation use them only then.  Every predictor entry
+ * point reads the handle's u_nm1 / v_nm1 and this flag; covof_run_steps
+ * rotates u_nm1 = u_old (or u on a first step) itself and sets the flag
+ * after its first step.  A new handle starts with has_nm1 = 0. */
+int covof_set_has_nm1(covof_handle* h, int has_nm1);
+int covof_get_has_nm1(const covof_handle* h, int* has_nm1);
 
 typedef struct covof_run_stats {
   int steps;               /* time steps run */
@@ -362,6 +385,9 @@ typedef struct covof_batch covof_batch;
 int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out);
 int covof_batch_destroy(covof_batch* b);
 /* Resident fields of one case (COVOF_FIELD_*), as covof_state_set/get. */
+/* covof_set_has_nm1 for every case of the batch (a new batch starts with 0;
+ * its first step sets it). */
+int covof_batch_set_has_nm1(covof_batch* b, int has_nm1);
 int covof_batch_state_set(covof_batch* b, int icase, int field, const double* host);
 int covof_batch_state_get(covof_batch* b, int icase, int field, double* host);
 /* nsteps steps of every case, dt[icase] each (fixed per call); stats (one per

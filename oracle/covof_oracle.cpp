@@ -488,48 +488,94 @@ void project_correct(const covof_params* prm, const Mesh& m, double dt, double* 
 
 // ---------------------------------------------------------------------------
 // Momentum predictor (SP: DOFs = u then v, src/module_navier_stokes.f90:164-169)
+// Time history of the predictor (fields%u_old, u_nm1, has_nm1;
+// src/module_simulation.f90:508-529).
+struct Hist {
+  const double *u_old = nullptr, *v_old = nullptr, *u_nm1 = nullptr, *v_nm1 = nullptr;
+  int has_nm1 = 0;
+};
+
 struct MomCtx {
   const covof_params* prm;
   Mesh m;
   double dt;
   const double *u_n, *v_n, *rho_u, *rho_v, *mu, *mu_node;
+  double alpha;                  // 1.5: Gear / BDF2 with history (:481-486), else 1
+  bool gear_rhs;                 // BDF2 inertial term (:841-848)
+  const double *u_adv, *v_adv;   // advecting velocity: fields%u (PICARD) or u_old (AB2)
+  const double *u_nm1, *v_nm1;   // AB2 extrapolation partner, nullptr without history
+  const double *u_nm1_rhs, *v_nm1_rhs;  // fields%u_nm1 for the Gear right-hand side
   int u_nx, v_ny;
   size_t nu, nv;
 };
 
-// src/module_navier_stokes.f90:2388-2416 conv_face_flux (UPWIND / CENTERED)
-inline double conv_face_flux(int scheme, double flux, double phiL, double phiR) {
+// src/module_navier_stokes.f90:2388-2416 conv_face_flux (UPWIND / CENTERED /
+// TVD_SUPERBEE; the limiter reads fields_old values q*)
+inline double conv_face_flux(int scheme, double flux, double phiL, double phiR, double qLL, double qL,
+                             double qR, double qRR, bool hasLL, bool hasRR) {
   if (scheme == COVOF_CONV_CENTERED) return 0.5 * flux * (phiL + phiR);
-  return (flux >= 0.0) ? flux * phiL : flux * phiR;
+  if (scheme == COVOF_CONV_UPWIND) return (flux >= 0.0) ? flux * phiL : flux * phiR;
+  double dq = qR - qL;
+  double psi = 0.0;
+  if (flux >= 0.0) {
+    if (hasLL && std::fabs(dq) > 1.0e-14) {
+      double r = (qL - qLL) / dq;
+      psi = std::max(std::max(0.0, std::min(2.0 * r, 1.0)), std::min(r, 2.0));
+    }
+    return flux * (phiL + 0.5 * psi * (phiR - phiL));
+  }
+  if (hasRR && std::fabs(dq) > 1.0e-14) {
+    double r = (qRR - qR) / dq;
+    psi = std::max(std::max(0.0, std::min(2.0 * r, 1.0)), std::min(r, 2.0));
+  }
+  return flux * (phiR + 0.5 * psi * (phiL - phiR));
 }
 
-// src/module_navier_stokes.f90:2418-2457 compute_u_conv_fluxes (PICARD)
+// src/module_navier_stokes.f90:2418-2457 compute_u_conv_fluxes
 inline void u_conv_fluxes(const MomCtx& c, int i, int j, double& FE, double& FW, double& FN,
                           double& FS) {
   const Mesh& m = c.m;
-  double un = c.u_n[m.id(i, j)], unE = c.u_n[m.id(i + 1, j)], unW = c.u_n[m.id(i - 1, j)];
-  double vnN = 0.5 * (c.v_n[m.id(i - 1, j + 1)] + c.v_n[m.id(i, j + 1)]);
-  double vnS = 0.5 * (c.v_n[m.id(i - 1, j)] + c.v_n[m.id(i, j)]);
+  double un = c.u_adv[m.id(i, j)], unE = c.u_adv[m.id(i + 1, j)], unW = c.u_adv[m.id(i - 1, j)];
+  double vnN = 0.5 * (c.v_adv[m.id(i - 1, j + 1)] + c.v_adv[m.id(i, j + 1)]);
+  double vnS = 0.5 * (c.v_adv[m.id(i - 1, j)] + c.v_adv[m.id(i, j)]);
+  if (c.u_nm1) {
+    un = 2.0 * un - c.u_nm1[m.id(i, j)];
+    unE = 2.0 * unE - c.u_nm1[m.id(i + 1, j)];
+    unW = 2.0 * unW - c.u_nm1[m.id(i - 1, j)];
+    double vmN = 0.5 * (c.v_nm1[m.id(i - 1, j + 1)] + c.v_nm1[m.id(i, j + 1)]);
+    double vmS = 0.5 * (c.v_nm1[m.id(i - 1, j)] + c.v_nm1[m.id(i, j)]);
+    vnN = 2.0 * vnN - vmN;
+    vnS = 2.0 * vnS - vmS;
+  }
   FE = 0.5 * (un + unE) * m.dy;
   FW = 0.5 * (unW + un) * m.dy;
   FN = vnN * m.dx;
   FS = vnS * m.dx;
 }
-// src/module_navier_stokes.f90:2459-2498 compute_v_conv_fluxes (PICARD)
+// src/module_navier_stokes.f90:2459-2498 compute_v_conv_fluxes
 inline void v_conv_fluxes(const MomCtx& c, int i, int j, double& FE, double& FW, double& FN,
                           double& FS) {
   const Mesh& m = c.m;
-  double vn = c.v_n[m.id(i, j)], vnN = c.v_n[m.id(i, j + 1)], vnS = c.v_n[m.id(i, j - 1)];
-  double unE = 0.5 * (c.u_n[m.id(i + 1, j - 1)] + c.u_n[m.id(i + 1, j)]);
-  double unW = 0.5 * (c.u_n[m.id(i, j - 1)] + c.u_n[m.id(i, j)]);
+  double vn = c.v_adv[m.id(i, j)], vnN = c.v_adv[m.id(i, j + 1)], vnS = c.v_adv[m.id(i, j - 1)];
+  double unE = 0.5 * (c.u_adv[m.id(i + 1, j - 1)] + c.u_adv[m.id(i + 1, j)]);
+  double unW = 0.5 * (c.u_adv[m.id(i, j - 1)] + c.u_adv[m.id(i, j)]);
+  if (c.u_nm1) {
+    vn = 2.0 * vn - c.v_nm1[m.id(i, j)];
+    vnN = 2.0 * vnN - c.v_nm1[m.id(i, j + 1)];
+    vnS = 2.0 * vnS - c.v_nm1[m.id(i, j - 1)];
+    double umE = 0.5 * (c.u_nm1[m.id(i + 1, j - 1)] + c.u_nm1[m.id(i + 1, j)]);
+    double umW = 0.5 * (c.u_nm1[m.id(i, j - 1)] + c.u_nm1[m.id(i, j)]);
+    unE = 2.0 * unE - umE;
+    unW = 2.0 * unW - umW;
+  }
   FE = unE * m.dy;
   FW = unW * m.dy;
   FN = 0.5 * (vn + vnN) * m.dx;
   FS = 0.5 * (vnS + vn) * m.dx;
 }
 
-// src/module_navier_stokes.f90:380-780 ns_apply_system_matrix (SP, Euler,
-// PICARD, no AL/obstacle terms).  tu/tv: the unpacked operand with the
+// src/module_navier_stokes.f90:380-780 ns_apply_system_matrix (SP; Euler or
+// Gear; PICARD or AB2; UPWIND / CENTERED / TVD_SUPERBEE; no AL/obstacle terms).  tu/tv: the unpacked operand with the
 // homogeneous ghost conditions applied (:458 -> src/module_mpi_comm.f90:290-537).
 void mom_apply(const MomCtx& c, const double* tu, const double* tv, double* yu, double* yv) {
   const Mesh& m = c.m;
@@ -540,7 +586,7 @@ void mom_apply(const MomCtx& c, const double* tu, const double* tv, double* yu, 
     for (int i = 1; i <= u_nx; ++i) {
       size_t k = m.id(i, j);
       double rho = c.rho_u[k];
-      double diag_bc = ((1.0 * rho) / dt) * dvol;
+      double diag_bc = ((c.alpha * rho) / dt) * dvol;
       if (i == 1) {
         if (prm->bc_type[L] == COVOF_BC_NEUMANN) yu[k] = diag_bc * (tu[m.id(1, j)] - tu[m.id(2, j)]);
         else yu[k] = diag_bc * tu[m.id(1, j)];
@@ -552,15 +598,26 @@ void mom_apply(const MomCtx& c, const double* tu, const double* tv, double* yu, 
         else yu[k] = diag_bc * tu[m.id(u_nx, j)];
         continue;
       }
-      double val = (((1.0 * rho) / dt) * tu[k]) * dvol;
+      double val = (((c.alpha * rho) / dt) * tu[k]) * dvol;
       if (prm->enable_convection) {
         double FE, FW, FN, FS;
         u_conv_fluxes(c, i, j, FE, FW, FN, FS);
+        // :533-547: the limiter's neighbours come from fields_old%u
+        const double* q = c.u_n;
+        bool has_ee = i + 2 <= nx + 1, has_ww = i - 2 >= 0, has_nn = j + 2 <= ny + 1, has_ss = j - 2 >= 0;
+        double q_ee = has_ee ? q[m.id(std::min(i + 2, nx + 1), j)] : 0.0;
+        double q_ww = has_ww ? q[m.id(std::max(i - 2, 0), j)] : 0.0;
+        double q_nn = has_nn ? q[m.id(i, std::min(j + 2, ny + 1))] : 0.0;
+        double q_ss = has_ss ? q[m.id(i, std::max(j - 2, 0))] : 0.0;
         int s = prm->convective_scheme;
-        double pE = conv_face_flux(s, FE, tu[k], tu[m.id(i + 1, j)]);
-        double pW = conv_face_flux(s, FW, tu[m.id(i - 1, j)], tu[k]);
-        double pN = conv_face_flux(s, FN, tu[k], tu[m.id(i, j + 1)]);
-        double pS = conv_face_flux(s, FS, tu[m.id(i, j - 1)], tu[k]);
+        double pE = conv_face_flux(s, FE, tu[k], tu[m.id(i + 1, j)], q[m.id(i - 1, j)], q[k],
+                                   q[m.id(i + 1, j)], q_ee, true, has_ee);
+        double pW = conv_face_flux(s, FW, tu[m.id(i - 1, j)], tu[k], q_ww, q[m.id(i - 1, j)], q[k],
+                                   q[m.id(i + 1, j)], has_ww, true);
+        double pN = conv_face_flux(s, FN, tu[k], tu[m.id(i, j + 1)], q[m.id(i, j - 1)], q[k],
+                                   q[m.id(i, j + 1)], q_nn, true, has_nn);
+        double pS = conv_face_flux(s, FS, tu[m.id(i, j - 1)], tu[k], q_ss, q[m.id(i, j - 1)], q[k],
+                                   q[m.id(i, j + 1)], has_ss, true);
         val = val + rho * (pE - pW + pN - pS);
       }
       double muE = c.mu[m.id(i, j)], muW = c.mu[m.id(i - 1, j)];
@@ -577,19 +634,30 @@ void mom_apply(const MomCtx& c, const double* tu, const double* tv, double* yu, 
     for (int i = 1; i <= nx; ++i) {
       size_t k = m.id(i, j);
       double rho = c.rho_v[k];
-      double diag_bc = ((1.0 * rho) / dt) * dvol;
+      double diag_bc = ((c.alpha * rho) / dt) * dvol;
       bool wb = (j == 1 && is_wall(prm, B));
       bool wt = (j == v_ny && is_wall(prm, T));
       if (wb || wt) { yv[k] = diag_bc * tv[k]; continue; }
-      double val = (((1.0 * rho) / dt) * tv[k]) * dvol;
+      double val = (((c.alpha * rho) / dt) * tv[k]) * dvol;
       if (prm->enable_convection) {
         double FE, FW, FN, FS;
         v_conv_fluxes(c, i, j, FE, FW, FN, FS);
+        // :666-680: the limiter's neighbours come from fields_old%v
+        const double* q = c.v_n;
+        bool has_ee = i + 2 <= nx + 1, has_ww = i - 2 >= 0, has_nn = j + 2 <= ny + 1, has_ss = j - 2 >= 0;
+        double q_ee = has_ee ? q[m.id(std::min(i + 2, nx + 1), j)] : 0.0;
+        double q_ww = has_ww ? q[m.id(std::max(i - 2, 0), j)] : 0.0;
+        double q_nn = has_nn ? q[m.id(i, std::min(j + 2, ny + 1))] : 0.0;
+        double q_ss = has_ss ? q[m.id(i, std::max(j - 2, 0))] : 0.0;
         int s = prm->convective_scheme;
-        double pE = conv_face_flux(s, FE, tv[k], tv[m.id(i + 1, j)]);
-        double pW = conv_face_flux(s, FW, tv[m.id(i - 1, j)], tv[k]);
-        double pN = conv_face_flux(s, FN, tv[k], tv[m.id(i, j + 1)]);
-        double pS = conv_face_flux(s, FS, tv[m.id(i, j - 1)], tv[k]);
+        double pE = conv_face_flux(s, FE, tv[k], tv[m.id(i + 1, j)], q[m.id(i - 1, j)], q[k],
+                                   q[m.id(i + 1, j)], q_ee, true, has_ee);
+        double pW = conv_face_flux(s, FW, tv[m.id(i - 1, j)], tv[k], q_ww, q[m.id(i - 1, j)], q[k],
+                                   q[m.id(i + 1, j)], has_ww, true);
+        double pN = conv_face_flux(s, FN, tv[k], tv[m.id(i, j + 1)], q[m.id(i, j - 1)], q[k],
+                                   q[m.id(i, j + 1)], q_nn, true, has_nn);
+        double pS = conv_face_flux(s, FS, tv[m.id(i, j - 1)], tv[k], q_ss, q[m.id(i, j - 1)], q[k],
+                                   q[m.id(i, j + 1)], has_ss, true);
         val = val + rho * (pE - pW + pN - pS);
       }
       double muN = c.mu[m.id(i, j)], muS = c.mu[m.id(i, j - 1)];
@@ -605,7 +673,7 @@ void mom_apply(const MomCtx& c, const double* tu, const double* tv, double* yu, 
 }
 
 // src/module_navier_stokes.f90:1268-1539 ns_assemble_preconditioner_blocks
-// (diag_u / diag_v only; Euler, no AL / obstacle / Newton terms).
+// (diag_u / diag_v only; no AL / obstacle / Newton terms).
 void mom_diag(const MomCtx& c, double* du, double* dv) {
   const Mesh& m = c.m;
   const covof_params* prm = c.prm;
@@ -616,7 +684,7 @@ void mom_diag(const MomCtx& c, double* du, double* dv) {
     for (int i = 1; i <= u_nx; ++i) {
       size_t k = m.id(i, j);
       double rho = c.rho_u[k];
-      double Du = ((1.0 * rho) / dt_safe) * dvol;
+      double Du = ((c.alpha * rho) / dt_safe) * dvol;
       if (Du <= 1.0e-30) Du = 1.0;
       if (i == 1 || i == u_nx) { du[k] = Du; continue; }
       double mue = c.mu[m.id(i, j)], muw = c.mu[m.id(i - 1, j)];
@@ -646,7 +714,7 @@ void mom_diag(const MomCtx& c, double* du, double* dv) {
     for (int i = 1; i <= nx; ++i) {
       size_t k = m.id(i, j);
       double rho = c.rho_v[k];
-      double Dv = ((1.0 * rho) / dt_safe) * dvol;
+      double Dv = ((c.alpha * rho) / dt_safe) * dvol;
       if (Dv <= 1.0e-30) Dv = 1.0;
       bool wall = (j == 1 && is_wall(prm, B)) || (j == v_ny && is_wall(prm, T));
       if (wall) { dv[k] = Dv; continue; }
@@ -677,7 +745,8 @@ void mom_diag(const MomCtx& c, double* du, double* dv) {
     }
 }
 
-// src/module_navier_stokes.f90:785-1101 ns_assemble_rhs (SP, Euler, constant walls)
+// src/module_navier_stokes.f90:785-1101 ns_assemble_rhs (SP, constant walls;
+// Euler or the Gear / BDF2 inertial term, :841-848 and :1022-1029)
 void mom_rhs(const MomCtx& c, const double* mu_node, const double* fx, const double* fy,
              const double* u_old, const double* v_old, double* ru, double* rv) {
   const Mesh& m = c.m;
@@ -688,7 +757,7 @@ void mom_rhs(const MomCtx& c, const double* mu_node, const double* fx, const dou
     for (int i = 1; i <= u_nx; ++i) {
       size_t k = m.id(i, j);
       double rho = c.rho_u[k];
-      double diag_bc = ((1.0 * rho) / dt) * dvol;
+      double diag_bc = ((c.alpha * rho) / dt) * dvol;
       if (i == 1) {
         double ubc = prm->bc_type[L] == COVOF_BC_DIRICHLET ? prm->bc_u[L] : 0.0;
         ru[k] = diag_bc * ubc;
@@ -699,7 +768,13 @@ void mom_rhs(const MomCtx& c, const double* mu_node, const double* fx, const dou
         ru[k] = diag_bc * ubc;
         continue;
       }
-      double val = (rho / dt) * u_old[k] * dvol;
+      double val;
+      if (c.gear_rhs) {
+        double u_in = rho * (2.0 * u_old[k] - 0.5 * c.u_nm1_rhs[k]);
+        val = (u_in / dt) * dvol;
+      } else {
+        val = (rho / dt) * u_old[k] * dvol;
+      }
       val = val + rho * prm->gx * dvol;
       val = val + fx[k] * dvol;
       if (j == ny && prm->bc_type[T] == COVOF_BC_DIRICHLET) {
@@ -718,7 +793,7 @@ void mom_rhs(const MomCtx& c, const double* mu_node, const double* fx, const dou
     for (int i = 1; i <= nx; ++i) {
       size_t k = m.id(i, j);
       double rho = c.rho_v[k];
-      double diag_bc = ((1.0 * rho) / dt) * dvol;
+      double diag_bc = ((c.alpha * rho) / dt) * dvol;
       if (j == 1 && is_wall(prm, B)) {
         double vbc = prm->bc_type[B] == COVOF_BC_DIRICHLET ? prm->bc_v[B] : 0.0;
         rv[k] = diag_bc * vbc;
@@ -729,7 +804,13 @@ void mom_rhs(const MomCtx& c, const double* mu_node, const double* fx, const dou
         rv[k] = diag_bc * vbc;
         continue;
       }
-      double val = (rho / dt) * v_old[k] * dvol;
+      double val;
+      if (c.gear_rhs) {
+        double v_in = rho * (2.0 * v_old[k] - 0.5 * c.v_nm1_rhs[k]);
+        val = (v_in / dt) * dvol;
+      } else {
+        val = (rho / dt) * v_old[k] * dvol;
+      }
       val = val + rho * prm->gy * dvol;
       val = val + fy[k] * dvol;
       if (i == 1 && prm->bc_type[L] == COVOF_BC_DIRICHLET) {
@@ -954,10 +1035,20 @@ int solve_cg(Krylov& K, const double* b, double* x, int* iters) {
 }
 
 MomCtx make_ctx(const covof_params* prm, double dt, const double* u_n, const double* v_n,
-                const double* rho_u, const double* rho_v, const double* mu, const double* mu_node) {
+                const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                const Hist& h = Hist()) {
   MomCtx c;
   c.prm = prm; c.m = mesh_of(prm); c.dt = dt;
   c.u_n = u_n; c.v_n = v_n; c.rho_u = rho_u; c.rho_v = rho_v; c.mu = mu; c.mu_node = mu_node;
+  const bool gear = prm->time_scheme == COVOF_TIME_GEAR && h.has_nm1;
+  const bool ab2 = prm->convective_linearization == COVOF_CONV_LIN_AB2;
+  c.alpha = gear ? 1.5 : 1.0;
+  c.gear_rhs = gear;
+  c.u_adv = (ab2 && h.u_old) ? h.u_old : u_n;
+  c.v_adv = (ab2 && h.v_old) ? h.v_old : v_n;
+  c.u_nm1 = (ab2 && h.has_nm1) ? h.u_nm1 : nullptr;
+  c.v_nm1 = (ab2 && h.has_nm1) ? h.v_nm1 : nullptr;
+  c.u_nm1_rhs = h.u_nm1; c.v_nm1_rhs = h.v_nm1;
   c.u_nx = prm->nx + 1; c.v_ny = prm->ny + 1;
   c.nu = (size_t)c.u_nx * prm->ny; c.nv = (size_t)prm->nx * c.v_ny;
   return c;
@@ -966,11 +1057,12 @@ MomCtx make_ctx(const covof_params* prm, double dt, const double* u_n, const dou
 // src/module_simulation.f90:2454-2470: diag, rhs, pack, solve, unpack, BC
 int predictor(const covof_params* prm, double dt, double* u, double* v, const double* rho_u,
               const double* rho_v, const double* mu, const double* mu_node, const double* fx,
-              const double* fy, const double* u_old, const double* v_old, int* iters) {
+              const double* fy, const double* u_old, const double* v_old, const Hist& hist,
+              int* iters) {
   // fields_old for the operator is the current field (u^n) itself.
   size_t g = (size_t)(prm->nx + 2) * (prm->ny + 2);
   std::vector<double> un(u, u + g), vn(v, v + g);
-  MomCtx c = make_ctx(prm, dt, un.data(), vn.data(), rho_u, rho_v, mu, mu_node);
+  MomCtx c = make_ctx(prm, dt, un.data(), vn.data(), rho_u, rho_v, mu, mu_node, hist);
   Krylov K(c);
   std::vector<double> du(g, 1.0), dv(g, 1.0), ru(g, 0.0), rv(g, 0.0);
   mom_diag(c, du.data(), dv.data());
@@ -1358,13 +1450,39 @@ int orc_project_correct(const covof_params* prm, double dt, double* u, double* v
   return COVOF_OK;
 }
 
+Hist hist_of(const double* u_old, const double* v_old, const double* u_nm1, const double* v_nm1,
+             int has_nm1) {
+  Hist h;
+  h.u_old = u_old; h.v_old = v_old; h.u_nm1 = u_nm1; h.v_nm1 = v_nm1;
+  h.has_nm1 = (has_nm1 && u_nm1 && v_nm1) ? 1 : 0;
+  return h;
+}
+
+int check_mom(const covof_params* prm, const double* u_old, const double* u_nm1, int has_nm1) {
+  if (prm->time_scheme != 0 && prm->time_scheme != COVOF_TIME_EULER && prm->time_scheme != COVOF_TIME_GEAR)
+    return COVOF_UNSUPPORTED;
+  if (prm->convective_linearization != 0 && prm->convective_linearization != COVOF_CONV_LIN_PICARD &&
+      prm->convective_linearization != COVOF_CONV_LIN_AB2)
+    return COVOF_UNSUPPORTED;
+  if (prm->convective_scheme != COVOF_CONV_UPWIND && prm->convective_scheme != COVOF_CONV_CENTERED &&
+      prm->convective_scheme != COVOF_CONV_TVD_SUPERBEE)
+    return COVOF_UNSUPPORTED;
+  if (prm->convective_linearization == COVOF_CONV_LIN_AB2 && !u_old) return COVOF_INVALID;
+  if (has_nm1 && !u_nm1 && (prm->time_scheme == COVOF_TIME_GEAR ||
+                            prm->convective_linearization == COVOF_CONV_LIN_AB2))
+    return COVOF_INVALID;
+  return COVOF_OK;
+}
+
 int orc_momentum_apply(const covof_params* prm, double dt, const double* xu, const double* xv,
                        double* yu, double* yv, const double* u_n, const double* v_n,
                        const double* rho_u, const double* rho_v, const double* mu,
-                       const double* mu_node) {
+                       const double* mu_node, const double* u_old, const double* v_old,
+                       const double* u_nm1, const double* v_nm1, int has_nm1) {
   int st = check_params(prm, false);
   if (st) return st;
-  MomCtx c = make_ctx(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node);
+  if ((st = check_mom(prm, u_old, u_nm1, has_nm1))) return st;
+  MomCtx c = make_ctx(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node, hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1));
   size_t g = (size_t)(prm->nx + 2) * (prm->ny + 2);
   // tf is a fresh field set: ghosts start at zero, then the DOFs are copied
   // in and the homogeneous ghost conditions applied.
@@ -1380,10 +1498,12 @@ int orc_momentum_apply(const covof_params* prm, double dt, const double* xu, con
 
 int orc_momentum_diag(const covof_params* prm, double dt, const double* u_n, const double* v_n,
                       const double* rho_u, const double* rho_v, const double* mu,
-                      const double* mu_node, double* diag_u, double* diag_v) {
+                      const double* mu_node, double* diag_u, double* diag_v, const double* u_old,
+                      const double* v_old, const double* u_nm1, const double* v_nm1, int has_nm1) {
   int st = check_params(prm, false);
   if (st) return st;
-  MomCtx c = make_ctx(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node);
+  if ((st = check_mom(prm, u_old, u_nm1, has_nm1))) return st;
+  MomCtx c = make_ctx(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node, hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1));
   mom_diag(c, diag_u, diag_v);
   return COVOF_OK;
 }
@@ -1391,10 +1511,12 @@ int orc_momentum_diag(const covof_params* prm, double dt, const double* u_n, con
 int orc_momentum_rhs(const covof_params* prm, double dt, const double* u_n, const double* v_n,
                      const double* rho_u, const double* rho_v, const double* mu_node,
                      const double* fx_sigma, const double* fy_sigma, const double* u_old,
-                     const double* v_old, double* rhs_u, double* rhs_v) {
+                     const double* v_old, double* rhs_u, double* rhs_v, const double* u_nm1,
+                     const double* v_nm1, int has_nm1) {
   int st = check_params(prm, false);
   if (st) return st;
-  MomCtx c = make_ctx(prm, dt, u_n, v_n, rho_u, rho_v, nullptr, mu_node);
+  if ((st = check_mom(prm, u_old, u_nm1, has_nm1))) return st;
+  MomCtx c = make_ctx(prm, dt, u_n, v_n, rho_u, rho_v, nullptr, mu_node, hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1));
   mom_rhs(c, mu_node, fx_sigma, fy_sigma, u_old, v_old, rhs_u, rhs_v);
   return COVOF_OK;
 }
@@ -1402,11 +1524,14 @@ int orc_momentum_rhs(const covof_params* prm, double dt, const double* u_n, cons
 int orc_predictor(const covof_params* prm, double dt, double* u, double* v, const double* rho_u,
                   const double* rho_v, const double* mu, const double* mu_node,
                   const double* fx_sigma, const double* fy_sigma, const double* u_old,
-                  const double* v_old, int* iters) {
+                  const double* v_old, const double* u_nm1, const double* v_nm1, int has_nm1,
+                  int* iters) {
   int st = check_params(prm, false);
   if (st) return st;
+  if ((st = check_mom(prm, u_old, u_nm1, has_nm1))) return st;
   int it = 0;
-  st = predictor(prm, dt, u, v, rho_u, rho_v, mu, mu_node, fx_sigma, fy_sigma, u_old, v_old, &it);
+  st = predictor(prm, dt, u, v, rho_u, rho_v, mu, mu_node, fx_sigma, fy_sigma, u_old, v_old,
+                 hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1), &it);
   if (iters) *iters = it;
   return st;
 }
@@ -1415,12 +1540,14 @@ int orc_predictor(const covof_params* prm, double dt, double* u, double* v, cons
 int orc_sp_step(const covof_params* prm, double dt, double* u, double* v, double* p,
                 const double* rho_u, const double* rho_v, const double* mu,
                 const double* mu_node, const double* fx_sigma, const double* fy_sigma,
-                const double* u_old, const double* v_old, int* iters_u, int* iters_p,
-                double* relres) {
+                const double* u_old, const double* v_old, const double* u_nm1, const double* v_nm1,
+                int has_nm1, int* iters_u, int* iters_p, double* relres) {
   int st = check_params(prm, false);
   if (st) return st;
+  if ((st = check_mom(prm, u_old, u_nm1, has_nm1))) return st;
   int iu = 0, ip = 0;
-  int s1 = predictor(prm, dt, u, v, rho_u, rho_v, mu, mu_node, fx_sigma, fy_sigma, u_old, v_old, &iu);
+  int s1 = predictor(prm, dt, u, v, rho_u, rho_v, mu, mu_node, fx_sigma, fy_sigma, u_old, v_old,
+                     hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1), &iu);
   if (s1 == COVOF_NAN) return s1;
   int s2 = poisson_driver(prm, dt, u, v, nullptr, rho_u, rho_v, p, &ip, relres, 1, 0);
   Mesh m = mesh_of(prm);

@@ -62,26 +62,33 @@ int orc_project_correct(const covof_params* prm, double dt, double* u, double* v
                         const double* p, const double* rho_u, const double* rho_v);
 
 /* momentum predictor */
+/* The momentum entry points take the time history: u_old / v_old
+ * (fields%u_old), u_nm1 / v_nm1 and has_nm1 (src/module_simulation.f90:
+ * 508-529), read by Gear / BDF2 and Adams-Bashforth only. */
 int orc_momentum_apply(const covof_params* prm, double dt, const double* xu, const double* xv,
                        double* yu, double* yv, const double* u_n, const double* v_n,
                        const double* rho_u, const double* rho_v, const double* mu,
-                       const double* mu_node);
+                       const double* mu_node, const double* u_old, const double* v_old,
+                       const double* u_nm1, const double* v_nm1, int has_nm1);
 int orc_momentum_diag(const covof_params* prm, double dt, const double* u_n, const double* v_n,
                       const double* rho_u, const double* rho_v, const double* mu,
-                      const double* mu_node, double* diag_u, double* diag_v);
+                      const double* mu_node, double* diag_u, double* diag_v, const double* u_old,
+                      const double* v_old, const double* u_nm1, const double* v_nm1, int has_nm1);
 int orc_momentum_rhs(const covof_params* prm, double dt, const double* u_n, const double* v_n,
                      const double* rho_u, const double* rho_v, const double* mu_node,
                      const double* fx_sigma, const double* fy_sigma, const double* u_old,
-                     const double* v_old, double* rhs_u, double* rhs_v);
+                     const double* v_old, double* rhs_u, double* rhs_v, const double* u_nm1,
+                     const double* v_nm1, int has_nm1);
 int orc_predictor(const covof_params* prm, double dt, double* u, double* v, const double* rho_u,
                   const double* rho_v, const double* mu, const double* mu_node,
                   const double* fx_sigma, const double* fy_sigma, const double* u_old,
-                  const double* v_old, int* iters);
+                  const double* v_old, const double* u_nm1, const double* v_nm1, int has_nm1,
+                  int* iters);
 int orc_sp_step(const covof_params* prm, double dt, double* u, double* v, double* p,
                 const double* rho_u, const double* rho_v, const double* mu,
                 const double* mu_node, const double* fx_sigma, const double* fy_sigma,
-                const double* u_old, const double* v_old, int* iters_u, int* iters_p,
-                double* relres);
+                const double* u_old, const double* v_old, const double* u_nm1, const double* v_nm1,
+                int has_nm1, int* iters_u, int* iters_p, double* relres);
 
 /* geometric VOF */
 int orc_reconstruct(const covof_params* prm, const double* C, double* seg);

@@ -42,11 +42,11 @@ def lib():
             "orc_poisson_solve_rhs": (i, [v, d] + [v] * 4 + [v, v, i]),
             "orc_poisson_fixed_iters": (i, [v, d] + [v] * 4 + [i, i, v]),
             "orc_project_correct": (i, [v, d] + [v] * 5),
-            "orc_momentum_apply": (i, [v, d] + [v] * 10),
-            "orc_momentum_diag": (i, [v, d] + [v] * 8),
-            "orc_momentum_rhs": (i, [v, d] + [v] * 11),
-            "orc_predictor": (i, [v, d] + [v] * 10 + [v]),
-            "orc_sp_step": (i, [v, d] + [v] * 11 + [v, v, v]),
+            "orc_momentum_apply": (i, [v, d] + [v] * 10 + [v] * 4 + [i]),
+            "orc_momentum_diag": (i, [v, d] + [v] * 8 + [v] * 4 + [i]),
+            "orc_momentum_rhs": (i, [v, d] + [v] * 11 + [v, v, i]),
+            "orc_predictor": (i, [v, d] + [v] * 10 + [v, v, i] + [v]),
+            "orc_sp_step": (i, [v, d] + [v] * 11 + [v, v, i] + [v, v, v]),
             "orc_reconstruct": (i, [v, v, v]),
             "orc_wy_step": (i, [v, d, i, v, v, v]),
             "orc_update_physical_properties": (i, [v] * 7),
@@ -125,43 +125,53 @@ def project_correct(prm, dt, u, v, p, rho_u, rho_v):
     return lib().orc_project_correct(_params(prm), dt, _p(u), _p(v), _p(p), _p(rho_u), _p(rho_v))
 
 
-def momentum_apply(prm, dt, xu, xv, u_n, v_n, rho_u, rho_v, mu, mu_node):
+# Momentum entry points take the time history (u_old, v_old, u_nm1, v_nm1,
+# has_nm1; src/module_simulation.f90:508-529), read by Gear / BDF2 and
+# Adams-Bashforth only; None leaves it out.
+def momentum_apply(prm, dt, xu, xv, u_n, v_n, rho_u, rho_v, mu, mu_node, u_old=None, v_old=None,
+                   u_nm1=None, v_nm1=None, has_nm1=0):
     yu, yv = np.zeros_like(xu), np.zeros_like(xv)
     st = lib().orc_momentum_apply(_params(prm), dt, _p(xu), _p(xv), _p(yu), _p(yv), _p(u_n), _p(v_n),
-                                  _p(rho_u), _p(rho_v), _p(mu), _p(mu_node))
+                                  _p(rho_u), _p(rho_v), _p(mu), _p(mu_node), _p(u_old), _p(v_old),
+                                  _p(u_nm1), _p(v_nm1), int(has_nm1))
     assert st == 0, st
     return yu, yv
 
 
-def momentum_diag(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node):
+def momentum_diag(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node, u_old=None, v_old=None, u_nm1=None,
+                  v_nm1=None, has_nm1=0):
     du, dv = np.zeros_like(u_n), np.zeros_like(v_n)
     st = lib().orc_momentum_diag(_params(prm), dt, _p(u_n), _p(v_n), _p(rho_u), _p(rho_v), _p(mu),
-                                 _p(mu_node), _p(du), _p(dv))
+                                 _p(mu_node), _p(du), _p(dv), _p(u_old), _p(v_old), _p(u_nm1), _p(v_nm1),
+                                 int(has_nm1))
     assert st == 0, st
     return du, dv
 
 
-def momentum_rhs(prm, dt, u_n, v_n, rho_u, rho_v, mu_node, fx, fy, u_old, v_old):
+def momentum_rhs(prm, dt, u_n, v_n, rho_u, rho_v, mu_node, fx, fy, u_old, v_old, u_nm1=None, v_nm1=None,
+                 has_nm1=0):
     ru, rv = np.zeros_like(u_n), np.zeros_like(v_n)
     st = lib().orc_momentum_rhs(_params(prm), dt, _p(u_n), _p(v_n), _p(rho_u), _p(rho_v), _p(mu_node),
-                                _p(fx), _p(fy), _p(u_old), _p(v_old), _p(ru), _p(rv))
+                                _p(fx), _p(fy), _p(u_old), _p(v_old), _p(ru), _p(rv), _p(u_nm1), _p(v_nm1),
+                                int(has_nm1))
     assert st == 0, st
     return ru, rv
 
 
-def predictor(prm, dt, f):
+def predictor(prm, dt, f, has_nm1=0):
     it = C.c_int()
     st = lib().orc_predictor(_params(prm), dt, _p(f.u), _p(f.v), _p(f.rho_u), _p(f.rho_v), _p(f.mu),
                              _p(f.mu_node), _p(f.fx_sigma), _p(f.fy_sigma), _p(f.u_old), _p(f.v_old),
-                             C.byref(it))
+                             _p(f.u_nm1), _p(f.v_nm1), int(has_nm1), C.byref(it))
     return it.value, st
 
 
-def sp_step(prm, dt, f):
+def sp_step(prm, dt, f, has_nm1=0):
     iu, ip, rr = C.c_int(), C.c_int(), C.c_double()
     st = lib().orc_sp_step(_params(prm), dt, _p(f.u), _p(f.v), _p(f.p), _p(f.rho_u), _p(f.rho_v),
                            _p(f.mu), _p(f.mu_node), _p(f.fx_sigma), _p(f.fy_sigma), _p(f.u_old),
-                           _p(f.v_old), C.byref(iu), C.byref(ip), C.byref(rr))
+                           _p(f.v_old), _p(f.u_nm1), _p(f.v_nm1), int(has_nm1), C.byref(iu), C.byref(ip),
+                           C.byref(rr))
     return iu.value, ip.value, rr.value, st
 
 
@@ -198,12 +208,22 @@ def vof_advect(prm, dt, step_count, f):
 
 def time_step(prm, dt, step_count, f):
     """One iteration of the time loop body of sim_run (src/module_simulation.f90:
-    492-559) for a fixed dt, Euler stepping and STANDARD_PROJECTION:
-    u_old = u, v_old = v; advect_vof + apply_velocity_bc when two-phase;
-    sim_solve_standard_projection.  Returns (iters_u, iters_p, relres, status)."""
+    492-559) for a fixed dt and STANDARD_PROJECTION: the n-1 history
+    (u_nm1 = u_old from step 2 on, has_nm1; :508-520), u_old = u, v_old = v;
+    advect_vof + apply_velocity_bc when two-phase;
+    sim_solve_standard_projection.  step_count counts the steps already
+    taken (the reference's step - 1).  Returns (iters_u, iters_p, relres,
+    status)."""
+    has_nm1 = 1 if step_count > 0 else 0
+    if has_nm1:
+        f.u_nm1[...] = f.u_old
+        f.v_nm1[...] = f.v_old
+    else:
+        f.u_nm1[...] = f.u
+        f.v_nm1[...] = f.v
     f.u_old[...] = f.u
     f.v_old[...] = f.v
     if prm.enable_two_phase:
         vof_advect(prm, dt, step_count, f)
         apply_velocity_bc(prm, f.u, f.v, False)
-    return sp_step(prm, dt, f)
+    return sp_step(prm, dt, f, has_nm1)
