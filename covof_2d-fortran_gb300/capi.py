@@ -29,7 +29,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 INNER_CHEBYSHEV, INNER_CG, INNER_CHEBYSHEV_STREAM, INNER_MG = 0, 1, 2, 3
 # resident fields (COVOF_FIELD_*), in header order; names follow the Fields dataclass
 FIELD_NAMES = ("u", "v", "p", "C", "rho", "rho_u", "rho_v", "mu", "mu_node", "fx_sigma",
-               "fy_sigma", "curvature", "u_old", "v_old", "u_nm1", "v_nm1")
+               "fy_sigma", "curvature", "u_old", "v_old", "u_nm1", "v_nm1", "C_s", "C_tilde")
 FIELD = {name: k for k, name in enumerate(FIELD_NAMES)}
 RUN_GRAPH = 1
 
@@ -52,6 +52,8 @@ class Params(C.Structure):
         ("p_inner_kind", C.c_int), ("p_cheb_lo", C.c_double),
         ("p_mg_nu", C.c_int), ("p_mg_cw", C.c_double), ("p_mg_tail", C.c_int),
         ("time_scheme", C.c_int), ("convective_linearization", C.c_int),
+        ("enable_svof_smoothing", C.c_int), ("svof_filter_width", C.c_double),
+        ("enable_diffusion_smoothing", C.c_int), ("diffusion_smoothing_steps", C.c_int),
     ]
 
     def copy(self) -> "Params":
@@ -138,6 +140,8 @@ _SIGS = {
     "covof_state_get": [_VP, C.c_int, _VP],
     "covof_state_field_dev": [_VP, C.c_int, C.POINTER(C.c_void_p)],
     "covof_set_has_nm1": [_VP, C.c_int],
+    "covof_svof_smooth": [_VP, _VP, _VP],
+    "covof_diffusion_smooth": [_VP, _VP, _VP],
     "covof_get_has_nm1": [_VP, C.POINTER(C.c_int)],
     "covof_batch_set_has_nm1": [_VP, C.c_int],
     "covof_run_steps": [_VP, C.c_double, C.c_int, C.c_int, C.POINTER(RunStats)],

@@ -65,6 +65,10 @@ def make_params(nx: int, ny: int, lx: float, ly: float) -> Params:
     p.p_mg_tail = 2048
     p.time_scheme = capi.TIME_EULER
     p.convective_linearization = capi.CONV_LIN_PICARD
+    p.enable_svof_smoothing = 0
+    p.svof_filter_width = 1.0
+    p.enable_diffusion_smoothing = 0
+    p.diffusion_smoothing_steps = 3
     return p
 
 

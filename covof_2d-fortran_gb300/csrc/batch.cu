@@ -275,8 +275,22 @@ int enqueue_batch_step(covof_batch* b, const double* dt, bool x_first) {
     if (h->prm.enable_two_phase) {
       CS(wy_step_dev(h, dt[c], x_first ? 1 : 0, h->f_u, h->f_v, h->f_C));
       CS(vof_bc_dev(h, h->f_C));
-      CS(props_dev(h, h->f_C, h->f_rho, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node));
-      CS(csf_dev(h, h->f_C, h->f_fx, h->f_fy, h->f_curv));
+    }
+    return COVOF_OK;
+  }));
+  // SVOF's cooperative wavefront launches run one case at a time on the
+  // batch stream (one spinning cooperative grid on the device at a time)
+  for (covof_handle* h : b->h) {
+    if (!h->prm.enable_two_phase || !h->prm.enable_svof_smoothing) continue;
+    cudaStream_t keep = h->stream;
+    h->stream = b->stream;
+    const int st = svof_dev(h, h->f_C, h->f_Cs);
+    h->stream = keep;
+    CS(st);
+  }
+  CS(per_case(b, [&](int c, covof_handle* h) -> int {
+    if (h->prm.enable_two_phase) {
+      CS(smooth_props_csf(h, false));
       CS(velocity_bc_dev(h, h->f_u, h->f_v));
     }
     return mom_pre(h, dt[c], h->f_u, h->f_v, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node, h->f_fx,

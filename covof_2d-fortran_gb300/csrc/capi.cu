@@ -61,6 +61,7 @@ int ensure_fields(covof_handle* h) {
   CS(dalloc(&h->f_mu_node, g)); CS(dalloc(&h->f_fx, g)); CS(dalloc(&h->f_fy, g));
   CS(dalloc(&h->f_u_old, g)); CS(dalloc(&h->f_v_old, g)); CS(dalloc(&h->f_C, g));
   CS(dalloc(&h->f_u_nm1, g)); CS(dalloc(&h->f_v_nm1, g));
+  CS(dalloc(&h->f_Cs, g)); CS(dalloc(&h->f_Ct, g));
   CS(dalloc(&h->f_rho, g)); CS(dalloc(&h->f_curv, g)); CS(dalloc(&h->f_b, g));
   CS(dalloc(&h->f_x2, 2 * g)); CS(dalloc(&h->f_seg, 3 * g));
   h->have_fields = true;
@@ -130,6 +131,15 @@ int ensure_vof(covof_handle* h) {
   CS(dalloc(&h->cs, g)); CS(dalloc(&h->seg, 3 * g));
   CS(dalloc(&h->cnx, g)); CS(dalloc(&h->cny, g)); CS(dalloc(&h->ckap, g));
   CS(dalloc(&h->vlist, g)); CS(dalloc(&h->vcount, 1));
+  CS(dalloc(&h->dscr, g));
+  const int nb = (h->D.ny + 31) / 32;
+  CS(dalloc(&h->svof_prog, (size_t)32 * nb));
+  // the SVOF wavefront: one 32-thread block per band of 32 rows, all resident
+  int per_sm = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_svof_sgs, 32, 0));
+  const int cap = per_sm * h->sm_count;
+  if (cap < 1) return COVOF_CUDA_ERROR;
+  h->svof_nb = nb < cap ? nb : cap;
   h->have_vof = true;
   return COVOF_OK;
 }
@@ -666,12 +676,13 @@ int wy_step_dev(covof_handle* h, double dt, int x_first, const double* u, const 
 }
 
 int props_dev(covof_handle* h, double* C, double* rho, double* rho_u, double* rho_v, double* mu,
-              double* mu_node) {
+              double* mu_node, const double* Cs) {
   const covof_params& P = h->prm;
   PropsArgs a;
   a.D = h->D; a.two_phase = P.enable_two_phase;
   a.rho1 = P.rho1; a.rho2 = P.rho2; a.mu1 = P.mu1; a.mu2 = P.mu2;
   a.C = C; a.rho = rho; a.rho_u = rho_u; a.rho_v = rho_v; a.mu = mu; a.mu_node = mu_node;
+  a.Cs = P.enable_svof_smoothing ? Cs : nullptr;
   const dim3 blk(32, 8);
   k_props_cells<<<grid2(h->D.nx + 2, h->D.ny + 2, blk), blk, 0, h->stream>>>(a);
   k_props_faces<<<grid2(h->D.nx + 1, h->D.ny + 1, blk), blk, 0, h->stream>>>(a);
@@ -679,7 +690,8 @@ int props_dev(covof_handle* h, double* C, double* rho, double* rho_u, double* rh
   return COVOF_OK;
 }
 
-int csf_dev(covof_handle* h, const double* C, double* fx, double* fy, double* curv) {
+int csf_dev(covof_handle* h, const double* C, double* fx, double* fy, double* curv, const double* Cs,
+            const double* Ct) {
   const covof_params& P = h->prm;
   if (!P.enable_surface_tension || P.sigma <= 0.0) {
     CK(cudaMemsetAsync(fx, 0, h->g * sizeof(double), h->stream));
@@ -691,6 +703,9 @@ int csf_dev(covof_handle* h, const double* C, double* fx, double* fy, double* cu
   CsfArgs a;
   a.D = h->D; a.dx = P.dx; a.dy = P.dy; a.sigma = P.sigma;
   a.C = C; a.nxv = h->cnx; a.nyv = h->cny; a.kappa = h->ckap; a.fx = fx; a.fy = fy; a.curv = curv;
+  // normals from C_tilde (diffusion smoothing), else C_s (SVOF), else C
+  // (src/module_interface_vof.f90:682-690)
+  a.N = (P.enable_diffusion_smoothing && Ct) ? Ct : (P.enable_svof_smoothing && Cs) ? Cs : C;
   const dim3 blk(32, 8);
   k_csf_normals<<<grid2(h->D.nx, h->D.ny, blk), blk, 0, h->stream>>>(a);
   k_csf_kappa<<<grid2(h->D.nx, h->D.ny, blk), blk, 0, h->stream>>>(a);
@@ -699,16 +714,76 @@ int csf_dev(covof_handle* h, const double* C, double* fx, double* fy, double* cu
   return COVOF_OK;
 }
 
+// src/module_interface_vof.f90:387-476 smooth_svof_helmholtz: C_s = C, the
+// wavefront Gauss-Seidel sweeps (svof.cu), then the clamp and ghost ring.
+int svof_dev(covof_handle* h, const double* C, double* Cs) {
+  CS(ensure_vof(h));
+  const covof_params& P = h->prm;
+  double kw = P.svof_filter_width;
+  if (kw <= 0.0) kw = 1.0;
+  const double Dw = kw * P.dx * P.dy;
+  SvofArgs a;
+  a.D = h->D; a.wx = Dw / (P.dx * P.dx); a.wy = Dw / (P.dy * P.dy);
+  a.C = C; a.Cs = Cs; a.prog = h->svof_prog; a.err = h->err;
+  const int nb = (h->D.ny + 31) / 32;
+  CK(cudaMemcpyAsync(Cs, C, h->g * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemsetAsync(h->svof_prog, 0, (size_t)32 * nb * sizeof(unsigned int), h->stream));
+  void* args[] = {&a};
+  CS(launch_coop(h, (const void*)k_svof_sgs, h->svof_nb, 32, args, false));
+  const dim3 blk(32, 8);
+  k_svof_finish<<<grid2(h->D.nx + 2, h->D.ny + 2, blk), blk, 0, h->stream>>>(h->D, Cs);
+  CK(cudaGetLastError());
+  return COVOF_OK;
+}
+
+// src/module_interface_vof.f90:1416-1461 vof_smooth_diffusion: C -> C_tilde
+int diffusion_dev(covof_handle* h, const double* C, double* Ct) {
+  CS(ensure_vof(h));
+  const covof_params& P = h->prm;
+  int steps = P.diffusion_smoothing_steps;
+  if (steps < 1) steps = 3;
+  const double dtau = 0.2 * fmin(P.dx * P.dx, P.dy * P.dy);
+  const dim3 blk(32, 8);
+  // ping-pong so that the last step writes Ct; the interior of the first
+  // source is C itself (ghost reads map to the interior)
+  const double* src = C;
+  for (int s = 0; s < steps; ++s) {
+    double* dst = ((steps - 1 - s) % 2 == 0) ? Ct : h->dscr;
+    k_diffusion_step<<<grid2(h->D.nx, h->D.ny, blk), blk, 0, h->stream>>>(h->D, dtau, P.dx * P.dx, P.dy * P.dy,
+                                                                          src, dst);
+    src = dst;
+  }
+  k_diffusion_ghosts<<<grid2(h->D.nx + 2, h->D.ny + 2, blk), blk, 0, h->stream>>>(h->D, Ct);
+  CK(cudaGetLastError());
+  return COVOF_OK;
+}
+
+// The interface-derived fields of the resident state after a VOF step
+// (src/module_interface_vof.f90:811-824): C_s (SVOF, when svof_now),
+// properties, C_tilde (diffusion smoothing), curvature + CSF.
+int smooth_props_csf(covof_handle* h, bool svof_now) {
+  const covof_params& P = h->prm;
+  if (svof_now && P.enable_svof_smoothing) CS(svof_dev(h, h->f_C, h->f_Cs));
+  CS(props_dev(h, h->f_C, h->f_rho, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node, h->f_Cs));
+  if (P.enable_diffusion_smoothing) CS(diffusion_dev(h, h->f_C, h->f_Ct));
+  return csf_dev(h, h->f_C, h->f_fx, h->f_fy, h->f_curv, h->f_Cs, h->f_Ct);
+}
+
 int vof_advect_dev(covof_handle* h, double dt, const double* u, const double* v, double* C,
                    double* rho, double* rho_u, double* rho_v, double* mu, double* mu_node,
                    double* fx, double* fy, double* curv) {
   if (!u || !v || !C || !rho || !rho_u || !rho_v || !mu || !mu_node || !fx || !fy || !curv)
     return COVOF_INVALID;
+  CS(ensure_fields(h));
+  const covof_params& P = h->prm;
   CS(wy_step_dev(h, dt, (h->vof_step_count % 2) == 0, u, v, C));
   h->vof_step_count += 1;
   CS(vof_bc_dev(h, C));
-  CS(props_dev(h, C, rho, rho_u, rho_v, mu, mu_node));
-  CS(csf_dev(h, C, fx, fy, curv));
+  // the smoothed indicators are the handle's resident C_s / C_tilde
+  if (P.enable_svof_smoothing) CS(svof_dev(h, C, h->f_Cs));
+  CS(props_dev(h, C, rho, rho_u, rho_v, mu, mu_node, h->f_Cs));
+  if (P.enable_diffusion_smoothing) CS(diffusion_dev(h, C, h->f_Ct));
+  CS(csf_dev(h, C, fx, fy, curv, h->f_Cs, h->f_Ct));
   return COVOF_OK;
 }
 
@@ -732,6 +807,8 @@ double** field_slot(covof_handle* h, int f) {
     case COVOF_FIELD_V_OLD: return &h->f_v_old;
     case COVOF_FIELD_U_NM1: return &h->f_u_nm1;
     case COVOF_FIELD_V_NM1: return &h->f_v_nm1;
+    case COVOF_FIELD_C_S: return &h->f_Cs;
+    case COVOF_FIELD_C_TILDE: return &h->f_Ct;
     default: return nullptr;
   }
 }
@@ -762,8 +839,7 @@ int enqueue_step(covof_handle* h, double dt, bool x_first) {
     // advect_vof: Weymouth-Yue step, VOF BC, properties, curvature + CSF
     CS(wy_step_dev(h, dt, x_first ? 1 : 0, h->f_u, h->f_v, h->f_C));
     CS(vof_bc_dev(h, h->f_C));
-    CS(props_dev(h, h->f_C, h->f_rho, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node));
-    CS(csf_dev(h, h->f_C, h->f_fx, h->f_fy, h->f_curv));
+    CS(smooth_props_csf(h, true));
     CS(velocity_bc_dev(h, h->f_u, h->f_v));
   }
   CS(predictor_enqueue(h, dt, h->f_u, h->f_v, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node, h->f_fx,
@@ -918,6 +994,10 @@ void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly)
   p->p_mg_tail = 2048;
   p->time_scheme = COVOF_TIME_EULER;
   p->convective_linearization = COVOF_CONV_LIN_PICARD;
+  p->enable_svof_smoothing = 0;
+  p->svof_filter_width = 1.0;
+  p->enable_diffusion_smoothing = 0;
+  p->diffusion_smoothing_steps = 3;
 }
 
 int covof_abi_version(void) { return COVOF_ABI_VERSION; }
@@ -977,7 +1057,8 @@ int covof_destroy(covof_handle* h) {
   if (!h) return COVOF_INVALID;
   if (h->stream) cudaStreamSynchronize(h->stream);
   double** fl[] = {&h->f_u, &h->f_v, &h->f_p, &h->f_rho_u, &h->f_rho_v, &h->f_mu, &h->f_mu_node,
-                   &h->f_fx, &h->f_fy, &h->f_u_old, &h->f_v_old, &h->f_u_nm1, &h->f_v_nm1, &h->f_C, &h->f_rho, &h->f_curv,
+                   &h->f_fx, &h->f_fy, &h->f_u_old, &h->f_v_old, &h->f_u_nm1, &h->f_v_nm1, &h->f_Cs, &h->f_Ct, &h->dscr,
+                   &h->f_C, &h->f_rho, &h->f_curv,
                    &h->f_b, &h->f_x2, &h->f_seg, &h->px, &h->pb, &h->pr, &h->pd, &h->pAd,
                    &h->pax, &h->pay, &h->paP, &h->pisd, &h->pinvD, &h->pd2, &h->pz, &h->pw, &h->pp, &h->pq, &h->mx, &h->mrhs, &h->mdiag, &h->cs, &h->seg, &h->mcoef, &h->midiag,
                    &h->cnx, &h->cny, &h->ckap, &h->part, &h->arhs, &h->apsi, &h->apart, &h->asum,
@@ -1333,6 +1414,27 @@ int covof_vof_advect(covof_handle* h, double dt, const double* u, const double* 
   return sync(h);
 }
 
+int covof_svof_smooth(covof_handle* h, const double* C, double* C_s) {
+  if (!h || !C) return COVOF_INVALID;
+  CS(ensure_fields(h));
+  CS(h2d(h, h->f_C, C, h->g));
+  CS(svof_dev(h, h->f_C, h->f_Cs));
+  if (C_s) CS(d2h(h, C_s, h->f_Cs, h->g));
+  int err = 0;
+  CK(cudaMemcpyAsync(&err, h->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CS(sync(h));
+  return err != 0 ? err : COVOF_OK;  // a wavefront wait that gave up: COVOF_TIMEOUT
+}
+
+int covof_diffusion_smooth(covof_handle* h, const double* C, double* C_tilde) {
+  if (!h || !C) return COVOF_INVALID;
+  CS(ensure_fields(h));
+  CS(h2d(h, h->f_C, C, h->g));
+  CS(diffusion_dev(h, h->f_C, h->f_Ct));
+  if (C_tilde) CS(d2h(h, C_tilde, h->f_Ct, h->g));
+  return sync(h);
+}
+
 int covof_update_physical_properties(covof_handle* h, double* C, double* rho, double* rho_u,
                                      double* rho_v, double* mu, double* mu_node) {
   if (!h) return COVOF_INVALID;
@@ -1340,7 +1442,8 @@ int covof_update_physical_properties(covof_handle* h, double* C, double* rho, do
   const size_t g = h->g;
   CS(h2d(h, h->f_C, C, g)); CS(h2d(h, h->f_rho, rho, g)); CS(h2d(h, h->f_rho_u, rho_u, g));
   CS(h2d(h, h->f_rho_v, rho_v, g)); CS(h2d(h, h->f_mu, mu, g)); CS(h2d(h, h->f_mu_node, mu_node, g));
-  CS(props_dev(h, h->f_C, h->f_rho, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node));
+  // with SVOF the properties follow the resident C_s (covof_svof_smooth)
+  CS(props_dev(h, h->f_C, h->f_rho, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node, h->f_Cs));
   CS(d2h(h, C, h->f_C, g)); CS(d2h(h, rho, h->f_rho, g)); CS(d2h(h, rho_u, h->f_rho_u, g));
   CS(d2h(h, rho_v, h->f_rho_v, g)); CS(d2h(h, mu, h->f_mu, g)); CS(d2h(h, mu_node, h->f_mu_node, g));
   return sync(h);
@@ -1353,7 +1456,8 @@ int covof_compute_curvature_and_csf(covof_handle* h, const double* C, double* fx
   const size_t g = h->g;
   CS(h2d(h, h->f_C, C, g)); CS(h2d(h, h->f_fx, fx_sigma, g)); CS(h2d(h, h->f_fy, fy_sigma, g));
   CS(h2d(h, h->f_curv, curvature, g));
-  CS(csf_dev(h, h->f_C, h->f_fx, h->f_fy, h->f_curv));
+  // normals from the resident C_tilde / C_s when smoothing is on
+  CS(csf_dev(h, h->f_C, h->f_fx, h->f_fy, h->f_curv, h->f_Cs, h->f_Ct));
   CS(d2h(h, fx_sigma, h->f_fx, g)); CS(d2h(h, fy_sigma, h->f_fy, g)); CS(d2h(h, curvature, h->f_curv, g));
   return sync(h);
 }

@@ -65,11 +65,14 @@ struct covof_handle {
   size_t g = 0;
   int vof_step_count = 0;
   bool has_nm1 = false;  // u_nm1 / v_nm1 hold step n-1 (fields%has_nm1)
+  unsigned int* svof_prog = nullptr;  // SVOF band progress (32 words per band)
+  int svof_nb = 0;                    // blocks of the SVOF launch (planned by ensure_vof)
   // caller-field mirrors (host-pointer entry points)
   bool have_fields = false;
   double *f_u = nullptr, *f_v = nullptr, *f_p = nullptr, *f_rho_u = nullptr, *f_rho_v = nullptr,
          *f_mu = nullptr, *f_mu_node = nullptr, *f_fx = nullptr, *f_fy = nullptr,
          *f_u_old = nullptr, *f_v_old = nullptr, *f_u_nm1 = nullptr, *f_v_nm1 = nullptr,
+         *f_Cs = nullptr, *f_Ct = nullptr, *dscr = nullptr,
          *f_C = nullptr, *f_rho = nullptr,
          *f_curv = nullptr, *f_b = nullptr, *f_x2 = nullptr, *f_seg = nullptr;
   // Poisson scratch
@@ -154,8 +157,12 @@ int rotate_history(covof_handle* h);
 void drop_graphs(covof_handle* h);
 int vof_bc_dev(covof_handle* h, double* C);
 int props_dev(covof_handle* h, double* C, double* rho, double* rho_u, double* rho_v, double* mu,
-              double* mu_node);
-int csf_dev(covof_handle* h, const double* C, double* fx, double* fy, double* curv);
+              double* mu_node, const double* Cs = nullptr);
+int csf_dev(covof_handle* h, const double* C, double* fx, double* fy, double* curv,
+            const double* Cs = nullptr, const double* Ct = nullptr);
+int svof_dev(covof_handle* h, const double* C, double* Cs);
+int diffusion_dev(covof_handle* h, const double* C, double* Ct);
+int smooth_props_csf(covof_handle* h, bool svof_now);
 int velocity_bc_dev(covof_handle* h, double* u, double* v);
 int correct_dev(covof_handle* h, double dt, double* u, double* v, const double* p, const double* rho_u,
                 const double* rho_v);

@@ -386,7 +386,8 @@ __global__ void k_props_cells(PropsArgs a) {
   } else {
     cv = a.C[k];
   }
-  const double c = fmax(0.0, fmin(1.0, cv));
+  // SVOF: the properties follow the smoothed indicator (:541-545)
+  const double c = fmax(0.0, fmin(1.0, a.Cs ? a.Cs[k] : cv));
   a.rho[k] = c * a.rho1 + (1.0 - c) * a.rho2;
   a.mu[k] = c * a.mu1 + (1.0 - c) * a.mu2;
 }
@@ -401,19 +402,28 @@ __global__ void k_props_faces(PropsArgs a) {
   const int k = a.D.id(i, j);
   if (j <= ny) a.rho_u[k] = 0.5 * (a.rho[k - 1] + a.rho[k]);
   if (i <= nx) a.rho_v[k] = 0.5 * (a.rho[k - a.D.P] + a.rho[k]);
+  if (a.Cs) {
+    // SVOF (:596-601): harmonic blend at the node of the smoothed indicator
+    double cn = 0.25 * (a.Cs[k - a.D.P - 1] + a.Cs[k - a.D.P] + a.Cs[k - 1] + a.Cs[k]);
+    cn = fmax(0.0, fmin(1.0, cn));
+    const double denom = a.mu2 * cn + a.mu1 * (1.0 - cn);
+    a.mu_node[k] = (a.mu1 * a.mu2) / fmax(1.0e-30, denom);
+    return;
+  }
   const double sw = a.mu[k - a.D.P - 1], se = a.mu[k - a.D.P];
   const double nw = a.mu[k - 1], ne = a.mu[k];
   a.mu_node[k] = 4.0 / (1.0 / sw + 1.0 / se + 1.0 / nw + 1.0 / ne);
 }
 
-// src/module_interface_vof.f90:663-686: unit normal of grad C at interior cells.
+// src/module_interface_vof.f90:663-686: unit normal of the gradient of C
+// (or of C_s / C_tilde with smoothing) at interior cells.
 __global__ void k_csf_normals(CsfArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (i > a.D.nx || j > a.D.ny) return;
   const int k = a.D.id(i, j);
-  const double dcx = (a.C[k + 1] - a.C[k - 1]) / (2.0 * a.dx);
-  const double dcy = (a.C[k + a.D.P] - a.C[k - a.D.P]) / (2.0 * a.dy);
+  const double dcx = (a.N[k + 1] - a.N[k - 1]) / (2.0 * a.dx);
+  const double dcy = (a.N[k + a.D.P] - a.N[k - a.D.P]) / (2.0 * a.dy);
   const double gm = sqrt(dcx * dcx + dcy * dcy);
   double nxv = 0.0, nyv = 0.0;
   if (gm > 1.0e-3 / a.dx) { nxv = dcx / gm; nyv = dcy / gm; }

@@ -20,12 +20,14 @@ struct PropsArgs {
   int two_phase;
   double rho1, rho2, mu1, mu2;
   double* C; double* rho; double* rho_u; double* rho_v; double* mu; double* mu_node;
+  const double* Cs;  // SVOF-smoothed indicator, nullptr without SVOF
 };
 
 struct CsfArgs {
   Dims D;
   double dx, dy, sigma;
   const double* C;
+  const double* N;   // field the normals are taken from (C, C_s or C_tilde)
   double* nxv; double* nyv; double* kappa;   // scratch, zero ghost ring
   double* fx; double* fy; double* curv;
 };
@@ -41,5 +43,21 @@ __global__ void k_props_faces(PropsArgs a);
 __global__ void k_csf_normals(CsfArgs a);
 __global__ void k_csf_kappa(CsfArgs a);
 __global__ void k_csf_force(CsfArgs a);
+
+// Interface smoothing (svof.cu)
+constexpr int kSvofIters = 25;  // sweep pairs (src/module_interface_vof.f90:409)
+struct SvofArgs {
+  Dims D;
+  double wx, wy;             // D / dx^2, D / dy^2
+  const double* C;
+  double* Cs;                // in: a copy of C; out: before the clamp
+  unsigned int* prog;        // per band (stride 32): chunks published, zero at launch
+  int* err;
+};
+__global__ void k_svof_sgs(SvofArgs a);
+__global__ void k_svof_finish(Dims D, double* __restrict__ Cs);
+__global__ void k_diffusion_step(Dims D, double dtau, double dx2, double dy2, const double* __restrict__ src,
+                                 double* __restrict__ dst);
+__global__ void k_diffusion_ghosts(Dims D, double* __restrict__ Ct);
 
 }  // namespace covof

@@ -56,6 +56,10 @@ module covof_gpu_bridge
      integer(c_int) :: p_mg_tail
      integer(c_int) :: time_scheme
      integer(c_int) :: convective_linearization
+     integer(c_int) :: enable_svof_smoothing
+     real(c_double) :: svof_filter_width
+     integer(c_int) :: enable_diffusion_smoothing
+     integer(c_int) :: diffusion_smoothing_steps
   end type covof_params_t
 
   integer(c_int), parameter :: COVOF_OK = 0, COVOF_MAXITER = 1, COVOF_BREAKDOWN = 2

@@ -72,13 +72,15 @@ class Fields:
     v_old: np.ndarray
     u_nm1: np.ndarray   # velocity of step n-1 (Gear / BDF2, Adams-Bashforth)
     v_nm1: np.ndarray
+    C_s: np.ndarray     # SVOF-smoothed indicator
+    C_tilde: np.ndarray  # diffusion-smoothed indicator (CSF normals)
 
     @classmethod
     def allocate(cls, p: Params) -> "Fields":
         z = lambda val=0.0: new_field(p, val)  # noqa: E731
         return cls(u=z(), v=z(), p=z(), C=z(1.0), rho=z(1.0), rho_u=z(1.0), rho_v=z(1.0),
                    mu=z(1.0e-3), mu_node=z(1.0e-3), fx_sigma=z(), fy_sigma=z(), curvature=z(),
-                   u_old=z(), v_old=z(), u_nm1=z(), v_nm1=z())
+                   u_old=z(), v_old=z(), u_nm1=z(), v_nm1=z(), C_s=z(1.0), C_tilde=z(1.0))
 
     def copy(self) -> "Fields":
         return Fields(**{k: getattr(self, k).copy() for k in self.__dataclass_fields__})
@@ -291,18 +293,40 @@ class Solver:
         st = self.lib.covof_vof_wy_step(self.h, dt, int(bool(x_first)), _ptr(u), _ptr(v), _ptr(Cf))
         self._check(st, "covof_vof_wy_step")
 
+    def _smoothed(self, f: Fields, upload: bool):
+        """Move f.C_s / f.C_tilde to (upload) or from the resident copies the
+        property and CSF entry points read, for the enabled smoothings."""
+        fn = self.lib.covof_state_set if upload else self.lib.covof_state_get
+        for name, on in (("C_s", self.params.enable_svof_smoothing),
+                         ("C_tilde", self.params.enable_diffusion_smoothing)):
+            if on:
+                self._check(fn(self.h, capi.FIELD[name], _ptr(getattr(f, name))), "covof_state_" +
+                            ("set" if upload else "get"))
+
     def advect_vof(self, dt: float, f: Fields):
         st = self.lib.covof_vof_advect(self.h, dt, _ptr(f.u), _ptr(f.v), _ptr(f.C), _ptr(f.rho),
                                        _ptr(f.rho_u), _ptr(f.rho_v), _ptr(f.mu), _ptr(f.mu_node),
                                        _ptr(f.fx_sigma), _ptr(f.fy_sigma), _ptr(f.curvature))
         self._check(st, "covof_vof_advect")
+        self._smoothed(f, upload=False)
+
+    def svof_smooth(self, f: Fields):
+        """smooth_svof_helmholtz: f.C -> f.C_s."""
+        self._check(self.lib.covof_svof_smooth(self.h, _ptr(f.C), _ptr(f.C_s)), "covof_svof_smooth")
+
+    def diffusion_smooth(self, f: Fields):
+        """vof_smooth_diffusion: f.C -> f.C_tilde."""
+        self._check(self.lib.covof_diffusion_smooth(self.h, _ptr(f.C), _ptr(f.C_tilde)),
+                    "covof_diffusion_smooth")
 
     def update_physical_properties(self, f: Fields):
+        self._smoothed(f, upload=True)
         st = self.lib.covof_update_physical_properties(self.h, _ptr(f.C), _ptr(f.rho), _ptr(f.rho_u),
                                                        _ptr(f.rho_v), _ptr(f.mu), _ptr(f.mu_node))
         self._check(st, "covof_update_physical_properties")
 
     def compute_curvature_and_csf(self, f: Fields):
+        self._smoothed(f, upload=True)
         st = self.lib.covof_compute_curvature_and_csf(self.h, _ptr(f.C), _ptr(f.fx_sigma),
                                                       _ptr(f.fy_sigma), _ptr(f.curvature))
         self._check(st, "covof_compute_curvature_and_csf")

@@ -126,6 +126,17 @@ typedef struct covof_params {
    * cfg%convective_linearization): COVOF_TIME_*, COVOF_CONV_LIN_* */
   int time_scheme;
   int convective_linearization;
+  /* interface smoothing (cfg%enable_svof_smoothing, svof_filter_width,
+   * enable_diffusion_smoothing, diffusion_smoothing_steps;
+   * src/module_interface_vof.f90:387-476, 1416-1461): SVOF smooths C into
+   * C_s (25 symmetric Gauss-Seidel sweeps of (I - D lap) C_s = C, D =
+   * width * dx * dy; 0 reads as 1), which then gives rho, mu, mu_node and
+   * the CSF normals; diffusion smoothing gives C_tilde (explicit steps; 0
+   * reads as 3), which takes over the CSF normals. */
+  int enable_svof_smoothing;
+  double svof_filter_width;
+  int enable_diffusion_smoothing;
+  int diffusion_smoothing_steps;
 } covof_params;
 enum { COVOF_INNER_CHEBYSHEV = 0, COVOF_INNER_CG = 1, COVOF_INNER_CHEBYSHEV_STREAM = 2, COVOF_INNER_MG = 3 };
 
@@ -282,11 +293,23 @@ int covof_vof_advect_dev(covof_handle* h, double dt, const double* u, const doub
                          double* fx_sigma, double* fy_sigma, double* curvature);
 int covof_get_vof_step_count(const covof_handle* h, int* count);
 int covof_set_vof_step_count(covof_handle* h, int count);
+/* smooth_svof_helmholtz (src/module_interface_vof.f90:387-476): C -> C_s,
+ * also kept as the resident C_s that the property and CSF entry points read
+ * when enable_svof_smoothing is set.  C_s may be NULL (resident copy only).
+ * On the device the Gauss-Seidel sweeps run as a wavefront and give the
+ * serial loop's values. */
+int covof_svof_smooth(covof_handle* h, const double* C, double* C_s);
+/* vof_smooth_diffusion (:1416-1461): C -> C_tilde, also kept resident (the
+ * CSF normals read it when enable_diffusion_smoothing is set). */
+int covof_diffusion_smooth(covof_handle* h, const double* C, double* C_tilde);
 /* update_physical_properties (src/module_interface_vof.f90:479-616); C's
- * physical corners are rewritten as in the reference. */
+ * physical corners are rewritten as in the reference.  With SVOF the cell
+ * properties and mu_node follow the resident C_s. */
 int covof_update_physical_properties(covof_handle* h, double* C, double* rho, double* rho_u,
                                      double* rho_v, double* mu, double* mu_node);
-/* compute_curvature_and_csf (src/module_interface_vof.f90:627-789). */
+/* compute_curvature_and_csf (src/module_interface_vof.f90:627-789); the
+ * normals come from the resident C_tilde (diffusion smoothing) or C_s (SVOF)
+ * when those are enabled. */
 int covof_compute_curvature_and_csf(covof_handle* h, const double* C, double* fx_sigma,
                                     double* fy_sigma, double* curvature);
 
@@ -299,7 +322,8 @@ enum {
   COVOF_FIELD_RHO = 4, COVOF_FIELD_RHO_U = 5, COVOF_FIELD_RHO_V = 6, COVOF_FIELD_MU = 7,
   COVOF_FIELD_MU_NODE = 8, COVOF_FIELD_FX_SIGMA = 9, COVOF_FIELD_FY_SIGMA = 10,
   COVOF_FIELD_CURVATURE = 11, COVOF_FIELD_U_OLD = 12, COVOF_FIELD_V_OLD = 13,
-  COVOF_FIELD_U_NM1 = 14, COVOF_FIELD_V_NM1 = 15, COVOF_NFIELDS = 16
+  COVOF_FIELD_U_NM1 = 14, COVOF_FIELD_V_NM1 = 15, COVOF_FIELD_C_S = 16, COVOF_FIELD_C_TILDE = 17,
+  COVOF_NFIELDS = 18
 };
 /* Copy one (nx+2)*(ny+2) field between the host and the handle's resident
  * copy (synchronous). */

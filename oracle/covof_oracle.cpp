@@ -1279,9 +1279,82 @@ void wy_step(const covof_params* prm, const Mesh& m, double dt, bool x_first, co
   std::memcpy(C, cf.data(), g * sizeof(double));
 }
 
-// src/module_interface_vof.f90:479-616 (two-phase, incompressible, no SVOF)
+// src/module_interface_vof.f90:387-476 smooth_svof_helmholtz: 25 symmetric
+// Gauss-Seidel sweep pairs of (I - D lap) C_s = C with dC_s/dn = 0, then
+// the clamp to [0, 1] and the ghost ring (corners included).
+void svof_smooth(const covof_params* prm, const Mesh& m, const double* C, double* Cs) {
+  const int nx = m.nx, ny = m.ny;
+  const double dx = m.dx, dy = m.dy;
+  double kw = prm->svof_filter_width;
+  if (kw <= 0.0) kw = 1.0;
+  const double D = kw * dx * dy;
+  const double wx = D / (dx * dx), wy = D / (dy * dy);
+  size_t g = (size_t)(nx + 2) * (ny + 2);
+  for (size_t k = 0; k < g; ++k) Cs[k] = C[k];
+  auto cell = [&](int i, int j) {
+    double aE = (i == nx) ? 0.0 : wx;
+    double aW = (i == 1) ? 0.0 : wx;
+    double aN = (j == ny) ? 0.0 : wy;
+    double aS = (j == 1) ? 0.0 : wy;
+    double aP = 1.0 + aE + aW + aN + aS;
+    double sum = aE * Cs[m.id(i + 1, j)] + aW * Cs[m.id(i - 1, j)] + aN * Cs[m.id(i, j + 1)] +
+                 aS * Cs[m.id(i, j - 1)];
+    Cs[m.id(i, j)] = (C[m.id(i, j)] + sum) / aP;
+  };
+  for (int it = 0; it < 25; ++it) {
+    for (int j = 1; j <= ny; ++j) { Cs[m.id(0, j)] = Cs[m.id(1, j)]; Cs[m.id(nx + 1, j)] = Cs[m.id(nx, j)]; }
+    for (int i = 1; i <= nx; ++i) { Cs[m.id(i, 0)] = Cs[m.id(i, 1)]; Cs[m.id(i, ny + 1)] = Cs[m.id(i, ny)]; }
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) cell(i, j);
+    for (int j = ny; j >= 1; --j)
+      for (int i = nx; i >= 1; --i) cell(i, j);
+  }
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) Cs[m.id(i, j)] = std::max(0.0, std::min(1.0, Cs[m.id(i, j)]));
+  for (int j = 1; j <= ny; ++j) { Cs[m.id(0, j)] = Cs[m.id(1, j)]; Cs[m.id(nx + 1, j)] = Cs[m.id(nx, j)]; }
+  for (int i = 1; i <= nx; ++i) { Cs[m.id(i, 0)] = Cs[m.id(i, 1)]; Cs[m.id(i, ny + 1)] = Cs[m.id(i, ny)]; }
+  Cs[m.id(0, 0)] = Cs[m.id(1, 1)];
+  Cs[m.id(nx + 1, 0)] = Cs[m.id(nx, 1)];
+  Cs[m.id(0, ny + 1)] = Cs[m.id(1, ny)];
+  Cs[m.id(nx + 1, ny + 1)] = Cs[m.id(nx, ny)];
+}
+
+// src/module_interface_vof.f90:1416-1461 vof_smooth_diffusion: explicit
+// diffusion steps (dtau = 0.2 min(dx^2, dy^2)) of C into C_tilde.
+void diffusion_smooth(const covof_params* prm, const Mesh& m, const double* C, double* Ct) {
+  const int nx = m.nx, ny = m.ny;
+  const double dx = m.dx, dy = m.dy;
+  size_t g = (size_t)(nx + 2) * (ny + 2);
+  for (size_t k = 0; k < g; ++k) Ct[k] = C[k];
+  const double dtau = 0.2 * std::min(dx * dx, dy * dy);
+  int steps = prm->diffusion_smoothing_steps;
+  if (steps < 1) steps = 3;
+  auto ghosts = [&]() {
+    for (int j = 1; j <= ny; ++j) Ct[m.id(0, j)] = Ct[m.id(1, j)];
+    for (int j = 1; j <= ny; ++j) Ct[m.id(nx + 1, j)] = Ct[m.id(nx, j)];
+    for (int i = 0; i <= nx + 1; ++i) Ct[m.id(i, 0)] = Ct[m.id(i, 1)];
+    for (int i = 0; i <= nx + 1; ++i) Ct[m.id(i, ny + 1)] = Ct[m.id(i, ny)];
+  };
+  std::vector<double> next(g);
+  for (int s = 0; s < steps; ++s) {
+    ghosts();
+    for (size_t k = 0; k < g; ++k) next[k] = Ct[k];
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        size_t k = m.id(i, j);
+        double lx = (Ct[m.id(i + 1, j)] - 2.0 * Ct[k] + Ct[m.id(i - 1, j)]) / (dx * dx);
+        double ly = (Ct[m.id(i, j + 1)] - 2.0 * Ct[k] + Ct[m.id(i, j - 1)]) / (dy * dy);
+        next[k] = Ct[k] + dtau * (lx + ly);
+      }
+    for (size_t k = 0; k < g; ++k) Ct[k] = next[k];
+  }
+  ghosts();
+}
+
+// src/module_interface_vof.f90:479-616 (two-phase, incompressible; with
+// SVOF the cell properties and mu_node come from C_s, :541-545, 596-601)
 void update_props(const covof_params* prm, const Mesh& m, double* C, double* rho, double* rho_u,
-                  double* rho_v, double* mu, double* mu_node) {
+                  double* rho_v, double* mu, double* mu_node, const double* Cs) {
   const int nx = m.nx, ny = m.ny;
   size_t g = (size_t)(nx + 2) * (ny + 2);
   if (!prm->enable_two_phase) {
@@ -1295,10 +1368,11 @@ void update_props(const covof_params* prm, const Mesh& m, double* C, double* rho
   C[m.id(nx + 1, 0)] = C[m.id(nx, 1)];
   C[m.id(0, ny + 1)] = C[m.id(1, ny)];
   C[m.id(nx + 1, ny + 1)] = C[m.id(nx, ny)];
+  const bool svof = prm->enable_svof_smoothing && Cs;
   for (int j = 0; j <= ny + 1; ++j)
     for (int i = 0; i <= nx + 1; ++i) {
       size_t k = m.id(i, j);
-      double c = std::max(0.0, std::min(1.0, C[k]));
+      double c = std::max(0.0, std::min(1.0, svof ? Cs[k] : C[k]));
       rho[k] = c * prm->rho1 + (1.0 - c) * prm->rho2;
       mu[k] = c * prm->mu1 + (1.0 - c) * prm->mu2;
     }
@@ -1314,15 +1388,24 @@ void update_props(const covof_params* prm, const Mesh& m, double* C, double* rho
       rho_v[m.id(i, j)] = 0.5 * (rho[m.id(i, j - 1)] + rho[m.id(i, j)]);
   for (int j = 1; j <= ny + 1; ++j)
     for (int i = 1; i <= nx + 1; ++i) {
-      double sw = mu[m.id(i - 1, j - 1)], se = mu[m.id(i, j - 1)];
-      double nw = mu[m.id(i - 1, j)], ne = mu[m.id(i, j)];
-      mu_node[m.id(i, j)] = 4.0 / (1.0 / sw + 1.0 / se + 1.0 / nw + 1.0 / ne);
+      if (svof) {
+        double cn = 0.25 * (Cs[m.id(i - 1, j - 1)] + Cs[m.id(i, j - 1)] + Cs[m.id(i - 1, j)] + Cs[m.id(i, j)]);
+        cn = std::max(0.0, std::min(1.0, cn));
+        double denom = prm->mu2 * cn + prm->mu1 * (1.0 - cn);
+        mu_node[m.id(i, j)] = (prm->mu1 * prm->mu2) / std::max(1.0e-30, denom);
+      } else {
+        double sw = mu[m.id(i - 1, j - 1)], se = mu[m.id(i, j - 1)];
+        double nw = mu[m.id(i - 1, j)], ne = mu[m.id(i, j)];
+        mu_node[m.id(i, j)] = 4.0 / (1.0 / sw + 1.0 / se + 1.0 / nw + 1.0 / ne);
+      }
     }
 }
 
-// src/module_interface_vof.f90:627-789 (no markers, no smoothing)
+// src/module_interface_vof.f90:627-789 (no markers): the normals come from
+// C_tilde (diffusion smoothing), else C_s (SVOF), else C (:682-690); the
+// face gradient from C.
 void csf(const covof_params* prm, const Mesh& m, const double* C, double* fx, double* fy,
-         double* curv) {
+         double* curv, const double* Cs, const double* Ct) {
   const int nx = m.nx, ny = m.ny;
   const double dx = m.dx, dy = m.dy;
   size_t g = (size_t)(nx + 2) * (ny + 2);
@@ -1331,10 +1414,11 @@ void csf(const covof_params* prm, const Mesh& m, const double* C, double* fx, do
     return;
   }
   std::vector<double> nxv(g, 0.0), nyv(g, 0.0), kap(g, 0.0);
+  const double* N = (prm->enable_diffusion_smoothing && Ct) ? Ct : (prm->enable_svof_smoothing && Cs) ? Cs : C;
   for (int j = 1; j <= ny; ++j)
     for (int i = 1; i <= nx; ++i) {
-      double dcx = (C[m.id(i + 1, j)] - C[m.id(i - 1, j)]) / (2.0 * dx);
-      double dcy = (C[m.id(i, j + 1)] - C[m.id(i, j - 1)]) / (2.0 * dy);
+      double dcx = (N[m.id(i + 1, j)] - N[m.id(i - 1, j)]) / (2.0 * dx);
+      double dcy = (N[m.id(i, j + 1)] - N[m.id(i, j - 1)]) / (2.0 * dy);
       double gm = std::sqrt(dcx * dcx + dcy * dcy);
       if (gm > 1.0e-3 / dx) { nxv[m.id(i, j)] = dcx / gm; nyv[m.id(i, j)] = dcy / gm; }
     }
@@ -1577,34 +1661,53 @@ int orc_wy_step(const covof_params* prm, double dt, int x_first, const double* u
   return COVOF_OK;
 }
 
-int orc_update_physical_properties(const covof_params* prm, double* C, double* rho,
-                                   double* rho_u, double* rho_v, double* mu, double* mu_node) {
+int orc_svof_smooth(const covof_params* prm, const double* C, double* C_s) {
   int st = check_params(prm, true);
   if (st) return st;
-  update_props(prm, mesh_of(prm), C, rho, rho_u, rho_v, mu, mu_node);
+  svof_smooth(prm, mesh_of(prm), C, C_s);
+  return COVOF_OK;
+}
+
+int orc_diffusion_smooth(const covof_params* prm, const double* C, double* C_tilde) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  diffusion_smooth(prm, mesh_of(prm), C, C_tilde);
+  return COVOF_OK;
+}
+
+int orc_update_physical_properties(const covof_params* prm, double* C, double* rho,
+                                   double* rho_u, double* rho_v, double* mu, double* mu_node,
+                                   const double* C_s) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  update_props(prm, mesh_of(prm), C, rho, rho_u, rho_v, mu, mu_node, C_s);
   return COVOF_OK;
 }
 
 int orc_compute_curvature_and_csf(const covof_params* prm, const double* C, double* fx_sigma,
-                                  double* fy_sigma, double* curvature) {
+                                  double* fy_sigma, double* curvature, const double* C_s,
+                                  const double* C_tilde) {
   int st = check_params(prm, true);
   if (st) return st;
-  csf(prm, mesh_of(prm), C, fx_sigma, fy_sigma, curvature);
+  csf(prm, mesh_of(prm), C, fx_sigma, fy_sigma, curvature, C_s, C_tilde);
   return COVOF_OK;
 }
 
-// src/module_interface_vof.f90:792-825 advect_vof (WEYMOUTH_YUE branch)
+// src/module_interface_vof.f90:792-825 advect_vof (WEYMOUTH_YUE branch):
+// transport, VOF BC, SVOF, properties, diffusion smoothing, curvature + CSF
 int orc_vof_advect(const covof_params* prm, double dt, int step_count, const double* u,
                    const double* v, double* C, double* rho, double* rho_u, double* rho_v,
                    double* mu, double* mu_node, double* fx_sigma, double* fy_sigma,
-                   double* curvature) {
+                   double* curvature, double* C_s, double* C_tilde) {
   int st = check_params(prm, true);
   if (st) return st;
   Mesh m = mesh_of(prm);
   wy_step(prm, m, dt, (step_count % 2) == 0, u, v, C);
   vof_bc(m, C);
-  update_props(prm, m, C, rho, rho_u, rho_v, mu, mu_node);
-  csf(prm, m, C, fx_sigma, fy_sigma, curvature);
+  if (prm->enable_svof_smoothing && C_s) svof_smooth(prm, m, C, C_s);
+  update_props(prm, m, C, rho, rho_u, rho_v, mu, mu_node, C_s);
+  if (prm->enable_diffusion_smoothing && C_tilde) diffusion_smooth(prm, m, C, C_tilde);
+  csf(prm, m, C, fx_sigma, fy_sigma, curvature, C_s, C_tilde);
   return COVOF_OK;
 }
 

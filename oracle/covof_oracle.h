@@ -94,14 +94,20 @@ int orc_sp_step(const covof_params* prm, double dt, double* u, double* v, double
 int orc_reconstruct(const covof_params* prm, const double* C, double* seg);
 int orc_wy_step(const covof_params* prm, double dt, int x_first, const double* u,
                 const double* v, double* C);
+/* interface smoothing: SVOF (C -> C_s) and diffusion (C -> C_tilde) */
+int orc_svof_smooth(const covof_params* prm, const double* C, double* C_s);
+int orc_diffusion_smooth(const covof_params* prm, const double* C, double* C_tilde);
+/* C_s / C_tilde: read when the matching smoothing is enabled (may be NULL otherwise) */
 int orc_update_physical_properties(const covof_params* prm, double* C, double* rho,
-                                   double* rho_u, double* rho_v, double* mu, double* mu_node);
+                                   double* rho_u, double* rho_v, double* mu, double* mu_node,
+                                   const double* C_s);
 int orc_compute_curvature_and_csf(const covof_params* prm, const double* C, double* fx_sigma,
-                                  double* fy_sigma, double* curvature);
+                                  double* fy_sigma, double* curvature, const double* C_s,
+                                  const double* C_tilde);
 int orc_vof_advect(const covof_params* prm, double dt, int step_count, const double* u,
                    const double* v, double* C, double* rho, double* rho_u, double* rho_v,
                    double* mu, double* mu_node, double* fx_sigma, double* fy_sigma,
-                   double* curvature);
+                   double* curvature, double* C_s, double* C_tilde);
 
 #ifdef __cplusplus
 }

@@ -49,9 +49,11 @@ def lib():
             "orc_sp_step": (i, [v, d] + [v] * 11 + [v, v, i] + [v, v, v]),
             "orc_reconstruct": (i, [v, v, v]),
             "orc_wy_step": (i, [v, d, i, v, v, v]),
-            "orc_update_physical_properties": (i, [v] * 7),
-            "orc_compute_curvature_and_csf": (i, [v] * 5),
-            "orc_vof_advect": (i, [v, d, i] + [v] * 11),
+            "orc_update_physical_properties": (i, [v] * 8),
+            "orc_compute_curvature_and_csf": (i, [v] * 7),
+            "orc_vof_advect": (i, [v, d, i] + [v] * 13),
+            "orc_svof_smooth": (i, [v, v, v]),
+            "orc_diffusion_smooth": (i, [v, v, v]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -187,22 +189,45 @@ def wy_step(prm, dt, x_first, u, v, Cf):
     assert st == 0, st
 
 
+def svof_smooth(prm, f):
+    """smooth_svof_helmholtz: f.C -> f.C_s."""
+    st = lib().orc_svof_smooth(_params(prm), _p(f.C), _p(f.C_s))
+    assert st == 0, st
+
+
+def diffusion_smooth(prm, f):
+    """vof_smooth_diffusion: f.C -> f.C_tilde."""
+    st = lib().orc_diffusion_smooth(_params(prm), _p(f.C), _p(f.C_tilde))
+    assert st == 0, st
+
+
 def update_physical_properties(prm, f):
     st = lib().orc_update_physical_properties(_params(prm), _p(f.C), _p(f.rho), _p(f.rho_u), _p(f.rho_v),
-                                              _p(f.mu), _p(f.mu_node))
+                                              _p(f.mu), _p(f.mu_node), _p(f.C_s))
     assert st == 0, st
 
 
 def compute_curvature_and_csf(prm, f):
     st = lib().orc_compute_curvature_and_csf(_params(prm), _p(f.C), _p(f.fx_sigma), _p(f.fy_sigma),
-                                             _p(f.curvature))
+                                             _p(f.curvature), _p(f.C_s), _p(f.C_tilde))
     assert st == 0, st
+
+
+def prepare_interface(prm, f):
+    """The interface-derived fields at t = 0, as after advect_vof: C_s
+    (SVOF), properties, C_tilde (diffusion smoothing), curvature + CSF."""
+    if prm.enable_svof_smoothing:
+        svof_smooth(prm, f)
+    update_physical_properties(prm, f)
+    if prm.enable_diffusion_smoothing:
+        diffusion_smooth(prm, f)
+    compute_curvature_and_csf(prm, f)
 
 
 def vof_advect(prm, dt, step_count, f):
     st = lib().orc_vof_advect(_params(prm), dt, int(step_count), _p(f.u), _p(f.v), _p(f.C), _p(f.rho),
                               _p(f.rho_u), _p(f.rho_v), _p(f.mu), _p(f.mu_node), _p(f.fx_sigma),
-                              _p(f.fy_sigma), _p(f.curvature))
+                              _p(f.fy_sigma), _p(f.curvature), _p(f.C_s), _p(f.C_tilde))
     assert st == 0, st
 
 
