@@ -724,6 +724,12 @@ int svof_dev(covof_handle* h, const double* C, double* Cs) {
   const double Dw = kw * P.dx * P.dy;
   SvofArgs a;
   a.D = h->D; a.wx = Dw / (P.dx * P.dx); a.wy = Dw / (P.dy * P.dy);
+  for (int f = 0; f < 16; ++f) {
+    const double aE = (f & 1) ? 0.0 : a.wx, aW = (f & 2) ? 0.0 : a.wx;
+    const double aN = (f & 4) ? 0.0 : a.wy, aS = (f & 8) ? 0.0 : a.wy;
+    a.aP[f] = 1.0 + aE + aW + aN + aS;
+    a.rP[f] = 1.0 / a.aP[f];
+  }
   a.C = C; a.Cs = Cs; a.prog = h->svof_prog; a.err = h->err;
   const int nb = (h->D.ny + 31) / 32;
   CK(cudaMemcpyAsync(Cs, C, h->g * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));

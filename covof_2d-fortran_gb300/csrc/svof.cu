@@ -33,6 +33,18 @@ __device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v) 
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// x / b, correctly rounded, from yb = RN(1 / b): q0 = RN(x yb) is within one
+// ulp of x / b, the remainder x - b q0 is exact in one FMA, and one FMA
+// correction step q0 + r yb rounds to the correctly rounded quotient
+// (P. Markstein, "IA-64 and Elementary Functions", 2000, Theorem 8.10; x, b
+// normal, x / b in range -- here x in [0, 1 + 4 w], b in [1, 1 + 4 w]).
+// Three dependent FP64 operations instead of a full division.
+__device__ __forceinline__ double div_rcp(double x, double b, double yb) {
+  const double q0 = __dmul_rn(x, yb);
+  const double r = __fma_rn(-b, q0, x);
+  return __fma_rn(r, yb, q0);
+}
+
 // lane 0 waits until *p >= need (bounded); the warp learns the outcome
 __device__ __forceinline__ bool warp_wait_ge(const unsigned int* p, unsigned int need, int* err) {
   int ok = 1;
@@ -48,6 +60,18 @@ __device__ __forceinline__ bool warp_wait_ge(const unsigned int* p, unsigned int
 // One sweep of one band.  Forward: lane r on row 32 b + r + 1, columns left
 // to right.  Backward: lane r on row 32 b + 32 - r, columns right to left.
 // Returns false when a wait gave up.
+//
+// The operands that are still old when the step runs (C, the value along the
+// sweep direction ahead, the value across in the row the sweep reaches next)
+// are loaded kSvofAhead steps early into a register ring, so a step waits on
+// the shuffle and the FP64 chain only, not on an L2 round trip.  They are
+// still old at prefetch time: the lane's own row ahead is written by itself
+// later; the next row's cell is written by lane r+1 one step after this
+// lane's step; the neighbouring band's edge row is written only after this
+// band publishes the chunk holding that column, which follows this lane's
+// step.
+constexpr int kSvofAhead = 8;
+
 __device__ bool svof_band(const SvofArgs& a, int s, int b) {
   const Dims& D = a.D;
   const int nx = D.nx, ny = D.ny, P = D.P;
@@ -62,51 +86,79 @@ __device__ bool svof_band(const SvofArgs& a, int s, int b) {
   const int dep = fwd ? b - 1 : b + 1;
   const bool has_dep = fwd ? b > 0 : b < nb - 1;
   const double wx = a.wx, wy = a.wy;
-  double prev = 0.0;  // this lane's value of the previous step
-  for (int t = 0; t < nx + 31; ++t) {
-    // lane 0 starts a chunk of columns (t < nx: past the last column no
-    // chunk is left to wait for)
-    if ((t & 31) == 0 && t < nx && has_dep) {
-      if (!warp_wait_ge(a.prog + 32 * dep, base + (unsigned int)(t >> 5) + 1u, a.err)) return false;
-    }
-    // lane r-1's previous value: the new neighbour across the band's rows
-    const double across = __shfl_up_sync(0xffffffffu, prev, 1);
+  // neighbour offsets: along = ahead in the sweep direction (old),
+  // ahead_row = the row the sweep reaches next (old), back_row = the row
+  // already swept (new: shuffle, or the band edge for lane 0)
+  const int along = fwd ? 1 : -1;
+  const int ahead_row = fwd ? P : -P;
+  const bool edge_ahead_row = fwd ? (j == ny) : (j == 1);
+  const bool edge_back_row = fwd ? (j == 1) : (j == ny);
+  // operands of step t: C, old along, old ahead-row
+  auto fetch = [&](int t, double& xc, double& xa, double& xr) {
     const int c = t - lane;
+    xc = 0.0; xa = 0.0; xr = 0.0;
     if (valid && c >= 0 && c < nx) {
       const int i = fwd ? c + 1 : nx - c;
       const int k = D.id(i, j);
-      const double aE = (i == nx) ? 0.0 : wx;
-      const double aW = (i == 1) ? 0.0 : wx;
-      const double aN = (j == ny) ? 0.0 : wy;
-      const double aS = (j == 1) ? 0.0 : wy;
-      const double aP = 1.0 + aE + aW + aN + aS;
-      // neighbours across a wall enter with a zero coefficient; they are
-      // read as 0 (the reference multiplies its Neumann ghost copy by 0)
-      double vE, vW, vN, vS;
-      if (fwd) {
-        vW = (i == 1) ? 0.0 : prev;                                      // new
-        vE = (i == nx) ? 0.0 : __ldcg(a.Cs + k + 1);                     // old
-        vN = (j == ny) ? 0.0 : __ldcg(a.Cs + k + P);                     // old
-        vS = (j == 1) ? 0.0 : (lane == 0 ? __ldcg(a.Cs + k - P) : across);  // new
-      } else {
-        vE = (i == nx) ? 0.0 : prev;                                     // new
-        vW = (i == 1) ? 0.0 : __ldcg(a.Cs + k - 1);                      // old
-        vS = (j == 1) ? 0.0 : __ldcg(a.Cs + k - P);                      // old
-        vN = (j == ny) ? 0.0 : (lane == 0 ? __ldcg(a.Cs + k + P) : across);  // new
-      }
-      const double sum = aE * vE + aW * vW + aN * vN + aS * vS;
-      const double v = (__ldg(a.C + k) + sum) / aP;
-      __stcg(a.Cs + k, v);
-      prev = v;
+      const bool edge_along = fwd ? (i == nx) : (i == 1);
+      xc = __ldg(a.C + k);
+      if (!edge_along) xa = __ldcg(a.Cs + k + along);
+      if (!edge_ahead_row) xr = __ldcg(a.Cs + k + ahead_row);
     }
-    // lane 31 (the band's edge row towards the waiting band) finished a
-    // chunk of 32 columns: publish it
-    const int c31 = t - 31;
-    if (c31 >= 0 && ((c31 & 31) == 31 || c31 == nx - 1)) {
-      __syncwarp();
-      if (lane == 31) {
-        __threadfence();
-        st_release_u32(a.prog + 32 * b, base + (unsigned int)(c31 >> 5) + 1u);
+  };
+  double rc[kSvofAhead], ra[kSvofAhead], rr[kSvofAhead];
+#pragma unroll
+  for (int q = 0; q < kSvofAhead; ++q) fetch(q, rc[q], ra[q], rr[q]);
+  double prev = 0.0;  // this lane's value of the previous step
+  const int T = nx + 31;
+  for (int tt = 0; tt < T; tt += kSvofAhead) {
+#pragma unroll
+    for (int q = 0; q < kSvofAhead; ++q) {
+      const int t = tt + q;
+      if (t >= T) break;  // uniform across the warp
+      // lane 0 starts a chunk of columns (t < nx: past the last column no
+      // chunk is left to wait for)
+      if ((t & 31) == 0 && t < nx && has_dep) {
+        if (!warp_wait_ge(a.prog + 32 * dep, base + (unsigned int)(t >> 5) + 1u, a.err)) return false;
+      }
+      // lane r-1's previous value: the new neighbour across the band's rows
+      const double across = __shfl_up_sync(0xffffffffu, prev, 1);
+      const int c = t - lane;
+      if (valid && c >= 0 && c < nx) {
+        const int i = fwd ? c + 1 : nx - c;
+        const int k = D.id(i, j);
+        const bool edge_back = fwd ? (i == 1) : (i == nx);
+        const double aE = (i == nx) ? 0.0 : wx;
+        const double aW = (i == 1) ? 0.0 : wx;
+        const double aN = (j == ny) ? 0.0 : wy;
+        const double aS = (j == 1) ? 0.0 : wy;
+        // 1 + aE + aW + aN + aS and its reciprocal, per wall pattern (host)
+        const int wf = (i == nx ? 1 : 0) | (i == 1 ? 2 : 0) | (j == ny ? 4 : 0) | (j == 1 ? 8 : 0);
+        const double aP = a.aP[wf], yP = a.rP[wf];
+        // neighbours across a wall enter with a zero coefficient; they are
+        // read as 0 (the reference multiplies its Neumann ghost copy by 0)
+        const double back = edge_back ? 0.0 : prev;  // new, this lane's previous step
+        const double back_row = edge_back_row ? 0.0
+                              : (lane == 0 ? __ldcg(a.Cs + k - ahead_row) : across);  // new
+        double vE, vW, vN, vS;
+        if (fwd) { vE = ra[q]; vW = back; vN = rr[q]; vS = back_row; }
+        else     { vW = ra[q]; vE = back; vS = rr[q]; vN = back_row; }
+        const double sum = aE * vE + aW * vW + aN * vN + aS * vS;
+        const double v = div_rcp(rc[q] + sum, aP, yP);
+        __stcg(a.Cs + k, v);
+        prev = v;
+      }
+      // refill this slot for step t + kSvofAhead
+      fetch(t + kSvofAhead, rc[q], ra[q], rr[q]);
+      // lane 31 (the band's edge row towards the waiting band) finished a
+      // chunk of 32 columns: publish it
+      const int c31 = t - 31;
+      if (c31 >= 0 && ((c31 & 31) == 31 || c31 == nx - 1)) {
+        __syncwarp();
+        if (lane == 31) {
+          __threadfence();
+          st_release_u32(a.prog + 32 * b, base + (unsigned int)(c31 >> 5) + 1u);
+        }
       }
     }
   }

@@ -49,6 +49,9 @@ constexpr int kSvofIters = 25;  // sweep pairs (src/module_interface_vof.f90:409
 struct SvofArgs {
   Dims D;
   double wx, wy;             // D / dx^2, D / dy^2
+  // per wall pattern f = (i==nx) | (i==1)<<1 | (j==ny)<<2 | (j==1)<<3:
+  // aP = 1 + aE + aW + aN + aS in the reference's order, and RN(1 / aP)
+  double aP[16], rP[16];
   const double* C;
   double* Cs;                // in: a copy of C; out: before the clamp
   unsigned int* prog;        // per band (stride 32): chunks published, zero at launch

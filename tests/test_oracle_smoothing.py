@@ -133,3 +133,34 @@ def test_time_loop_with_smoothing_runs(pkg, orc):
         iu, ip, rr, st = orc.time_step(p, dt, k, f)
         assert st == 0 and rr <= p.p_tol
     assert np.isfinite(f.u).all()
+
+
+def _div_rcp(x: float, b: float, y: float) -> float:
+    """The device's SVOF quotient restated exactly: q0 = RN(x y),
+    r = RN(x - b q0) (one FMA), q = RN(q0 + r y) (one FMA); Fractions give
+    the exact values that each FMA rounds once."""
+    from fractions import Fraction as F
+    q0 = x * y
+    r = float(F(x) - F(b) * F(q0))
+    return float(F(r) * F(y) + F(q0))
+
+
+@pytest.mark.parametrize("width,aspect", [(1.0, 1.0), (2.5, 1.0), (1.0, 4.0), (0.5, 0.25), (10.0, 1.0)])
+def test_reciprocal_division_is_correctly_rounded(width, aspect):
+    """The SVOF kernel divides by 1 + aE + aW + aN + aS through a
+    precomputed reciprocal and one FMA correction (Markstein); on every wall
+    pattern and operands across the range C_s takes it equals IEEE x / b."""
+    dx, dy = 1.0 / 64, aspect / 64
+    D = width * dx * dy
+    wx, wy = D / (dx * dx), D / (dy * dy)
+    rng = np.random.default_rng(int(width * 10 + aspect * 100))
+    for f in range(16):
+        aE = 0.0 if f & 1 else wx
+        aW = 0.0 if f & 2 else wx
+        aN = 0.0 if f & 4 else wy
+        aS = 0.0 if f & 8 else wy
+        b = 1.0 + aE + aW + aN + aS
+        y = 1.0 / b
+        xs = list(rng.uniform(0.0, b, 300)) + list(rng.uniform(0.0, 1.0, 100)) + [0.0, 1.0, b, 1e-300]
+        for x in xs:
+            assert _div_rcp(float(x), b, y) == float(x) / b, (x, b)
