@@ -24,6 +24,8 @@ CONV_UPWIND, CONV_CENTERED, CONV_TVD_SUPERBEE = 1, 2, 3
 TIME_EULER, TIME_GEAR = 1, 2
 CONV_LIN_PICARD, CONV_LIN_AB2, CONV_LIN_NEWTON = 1, 2, 3
 RECON_PLIC, RECON_ELVIRA = 0, 1
+ADVECT_WEYMOUTH_YUE, ADVECT_CIAM, ADVECT_TVD = 0, 1, 2
+LIMITER_SUPERBEE, LIMITER_VAN_LEER, LIMITER_MUSCL, LIMITER_HRIC = 0, 1, 2, 3
 GAUGE_REFERENCE, GAUGE_PINNED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 INNER_CHEBYSHEV, INNER_CG, INNER_CHEBYSHEV_STREAM, INNER_MG = 0, 1, 2, 3
@@ -54,6 +56,7 @@ class Params(C.Structure):
         ("time_scheme", C.c_int), ("convective_linearization", C.c_int),
         ("enable_svof_smoothing", C.c_int), ("svof_filter_width", C.c_double),
         ("enable_diffusion_smoothing", C.c_int), ("diffusion_smoothing_steps", C.c_int),
+        ("advection_method", C.c_int), ("tvd_limiter", C.c_int),
     ]
 
     def copy(self) -> "Params":

@@ -69,6 +69,8 @@ def make_params(nx: int, ny: int, lx: float, ly: float) -> Params:
     p.svof_filter_width = 1.0
     p.enable_diffusion_smoothing = 0
     p.diffusion_smoothing_steps = 3
+    p.advection_method = capi.ADVECT_WEYMOUTH_YUE
+    p.tvd_limiter = capi.LIMITER_SUPERBEE
     return p
 
 

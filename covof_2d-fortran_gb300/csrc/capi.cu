@@ -43,6 +43,8 @@ int check_params(const covof_params* p) {
     if (t == COVOF_BC_PERIODIC || t == COVOF_BC_NEUMANN) return COVOF_UNSUPPORTED;
     if (t != COVOF_BC_DIRICHLET && t != COVOF_BC_FREESLIP) return COVOF_INVALID;
   }
+  if (p->advection_method < COVOF_ADVECT_WEYMOUTH_YUE || p->advection_method > COVOF_ADVECT_TVD) return COVOF_INVALID;
+  if (p->tvd_limiter < COVOF_LIMITER_SUPERBEE || p->tvd_limiter > COVOF_LIMITER_HRIC) return COVOF_INVALID;
   return COVOF_OK;
 }
 
@@ -659,18 +661,31 @@ int vof_bc_dev(covof_handle* h, double* C) {
 }
 
 // src/module_interface_vof.f90:1162-1377
+// The configured transport (src/module_interface_vof.f90:801-808): the
+// geometric schemes reconstruct, pass, apply the VOF BC, reconstruct, pass;
+// TVD is one explicit update.
 int wy_step_dev(covof_handle* h, double dt, int x_first, const double* u, const double* v, double* C) {
   CS(ensure_vof(h));
   const dim3 blk(32, 4), grd = grid2(h->D.nx + 2, h->D.ny + 2, blk);
+  const int method = h->prm.advection_method;
+  VofArgs a = vof_args(h, dt, C, C, u, v);
+  if (method == COVOF_ADVECT_TVD) {
+    CK(cudaMemcpyAsync(h->cs, C, h->g * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    k_tvd_advect<<<grd, blk, 0, h->stream>>>(a, h->prm.tvd_limiter, h->cs, C);
+    CK(cudaGetLastError());
+    return COVOF_OK;
+  }
+  const bool ciam = method == COVOF_ADVECT_CIAM;
   const int d1 = x_first ? 0 : 1, d2 = x_first ? 1 : 0;
   CS(reconstruct_dev(h, C, nullptr));
-  VofArgs a = vof_args(h, dt, C, C, u, v);
-  k_vof_pass<<<grd, blk, 0, h->stream>>>(a, d1, 0, C, h->cs);
+  if (ciam) k_ciam_pass<<<grd, blk, 0, h->stream>>>(a, d1, C, h->cs);
+  else k_vof_pass<<<grd, blk, 0, h->stream>>>(a, d1, 0, C, h->cs);
   CK(cudaGetLastError());
   CS(vof_bc_dev(h, h->cs));
   CS(reconstruct_dev(h, h->cs, nullptr));
   a.C = h->cs;
-  k_vof_pass<<<grd, blk, 0, h->stream>>>(a, d2, 1, h->cs, C);
+  if (ciam) k_ciam_pass<<<grd, blk, 0, h->stream>>>(a, d2, h->cs, C);
+  else k_vof_pass<<<grd, blk, 0, h->stream>>>(a, d2, 1, h->cs, C);
   CK(cudaGetLastError());
   return COVOF_OK;
 }
@@ -1004,6 +1019,8 @@ void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly)
   p->svof_filter_width = 1.0;
   p->enable_diffusion_smoothing = 0;
   p->diffusion_smoothing_steps = 3;
+  p->advection_method = COVOF_ADVECT_WEYMOUTH_YUE;
+  p->tvd_limiter = COVOF_LIMITER_SUPERBEE;
 }
 
 int covof_abi_version(void) { return COVOF_ABI_VERSION; }

@@ -348,6 +348,97 @@ __global__ void k_vof_pass(VofArgs a, int dir, int clamp, const double* __restri
   Cout[k] = c;
 }
 
+// One CIAM direction pass (src/module_interface_vof.f90:963-1073): the
+// Weymouth-Yue donor flux volumes, then the Lagrangian remap
+// (C dh - dF / dh') / (dh - dt du) (plain divergence where the remapped width
+// would vanish), clamped; ghost cells copy Cin.
+__global__ void k_ciam_pass(VofArgs a, int dir, const double* __restrict__ Cin, double* __restrict__ Cout) {
+  const VMesh m{a.D, a.dx, a.dy};
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.D.nx, ny = a.D.ny;
+  if (i > nx + 1 || j > ny + 1) return;
+  const int k = a.D.id(i, j);
+  if (i < 1 || i > nx || j < 1 || j > ny) { Cout[k] = Cin[k]; return; }
+  double c;
+  if (dir == 0) {
+    const double fw = x_flux(m, a.seg, a.u, a.dt, i, j);
+    const double fe = x_flux(m, a.seg, a.u, a.dt, i + 1, j);
+    const double denom = a.dx - a.dt * (a.u[k + 1] - a.u[k]);
+    const double df = fe - fw;
+    c = denom > 1.0e-12 ? (Cin[k] * a.dx - df / a.dy) / denom : Cin[k] - df / (a.dx * a.dy);
+  } else {
+    const double fs = y_flux(m, a.seg, a.v, a.dt, i, j);
+    const double fn = y_flux(m, a.seg, a.v, a.dt, i, j + 1);
+    const double denom = a.dy - a.dt * (a.v[k + a.D.P] - a.v[k]);
+    const double df = fn - fs;
+    c = denom > 1.0e-12 ? (Cin[k] * a.dy - df / a.dx) / denom : Cin[k] - df / (a.dx * a.dy);
+  }
+  Cout[k] = fmax(0.0, fmin(1.0, c));
+}
+
+// src/module_interface_reconstruction.f90:686-725 evaluate_limiter
+__device__ __forceinline__ double tvd_limiter(int lim, double r, double cd, double cu, double ca) {
+  switch (lim) {
+    case COVOF_LIMITER_VAN_LEER:
+      return r > 0.0 ? 2.0 * r / (1.0 + r) : 0.0;
+    case COVOF_LIMITER_MUSCL:
+      return fmax(0.0, fmin(2.0 * r, fmin(0.5 * (1.0 + r), 2.0)));
+    case COVOF_LIMITER_HRIC: {
+      const double denom = ca - cu;
+      if (fabs(denom) < 1.0e-12) return 0.0;
+      const double ctD = (cd - cu) / denom;
+      double ctf = ctD;
+      if (ctD >= 0.0 && ctD <= 1.0) ctf = ctD < 0.5 ? 2.0 * ctD : 1.0;
+      if (fabs(1.0 - ctD) > 1.0e-12) {
+        const double phi = 2.0 * (ctf - ctD) / (1.0 - ctD);
+        return fmax(0.0, fmin(2.0, phi));
+      }
+      return 1.0;
+    }
+    default:
+      return fmax(0.0, fmax(fmin(2.0 * r, 1.0), fmin(r, 2.0)));
+  }
+}
+
+// Limited upwind flux through x face i (between cells i-1 and i), or y face j
+// (src/module_interface_vof.f90:853-913); `o` is the stride along the face
+// normal, lo / hi the first and last ghost index along it.
+__device__ __forceinline__ double tvd_face_flux(int lim, double uf, double dt, double dh, const double* C, int k,
+                                                int o, int idx, int hi) {
+  const double cl = C[k - o], cr = C[k];
+  const double cfl = 1.0 - fmin(1.0, fabs(uf) * dt / dh);
+  if (uf >= 0.0) {
+    const double cu = C[k - (idx - 2 >= 0 ? 2 : idx) * o];
+    const double dup = cl - cu, dloc = cr - cl;
+    const double r = fabs(dloc) > 1.0e-12 ? dup / dloc : 0.0;
+    const double phi = tvd_limiter(lim, r, cl, cu, cr);
+    return uf * (cl + 0.5 * phi * cfl * dloc);
+  }
+  const double cu = C[k + (idx + 1 <= hi ? 1 : 0) * o];
+  const double dup = cu - cr, dloc = cr - cl;
+  const double r = fabs(dloc) > 1.0e-12 ? dup / dloc : 0.0;
+  const double phi = tvd_limiter(lim, r, cr, cu, cl);
+  return uf * (cr - 0.5 * phi * cfl * dloc);
+}
+
+// src/module_interface_vof.f90:828-935 advect_vof_tvd: one conservative
+// update from the four face fluxes of C^n, clamped; ghost cells copy Cin.
+__global__ void k_tvd_advect(VofArgs a, int lim, const double* __restrict__ Cin, double* __restrict__ Cout) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.D.nx, ny = a.D.ny, P = a.D.P;
+  if (i > nx + 1 || j > ny + 1) return;
+  const int k = a.D.id(i, j);
+  if (i < 1 || i > nx || j < 1 || j > ny) { Cout[k] = Cin[k]; return; }
+  const double fw = tvd_face_flux(lim, a.u[k], a.dt, a.dx, Cin, k, 1, i, nx + 1);
+  const double fe = tvd_face_flux(lim, a.u[k + 1], a.dt, a.dx, Cin, k + 1, 1, i + 1, nx + 1);
+  const double fs = tvd_face_flux(lim, a.v[k], a.dt, a.dy, Cin, k, P, j, ny + 1);
+  const double fn = tvd_face_flux(lim, a.v[k + P], a.dt, a.dy, Cin, k + P, P, j + 1, ny + 1);
+  const double c = Cin[k] - (a.dt / a.dx) * (fe - fw) - (a.dt / a.dy) * (fn - fs);
+  Cout[k] = fmax(0.0, fmin(1.0, c));
+}
+
 // src/module_mpi_comm.f90:636-683 apply_vof_bc (np = 1): zero-gradient
 // edge ghosts, corners untouched.
 __global__ void k_vof_bc(Dims D, double* __restrict__ C) {

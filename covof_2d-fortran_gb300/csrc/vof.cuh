@@ -37,6 +37,8 @@ __global__ void k_vof_mixed(VofArgs a, const int* __restrict__ list, const int* 
 __global__ void k_vof_ring_warp(VofArgs a);
 __global__ void k_vof_pass(VofArgs a, int dir, int clamp, const double* __restrict__ Cin,
                            double* __restrict__ Cout);
+__global__ void k_ciam_pass(VofArgs a, int dir, const double* __restrict__ Cin, double* __restrict__ Cout);
+__global__ void k_tvd_advect(VofArgs a, int lim, const double* __restrict__ Cin, double* __restrict__ Cout);
 __global__ void k_vof_bc(Dims D, double* __restrict__ C);
 __global__ void k_props_cells(PropsArgs a);
 __global__ void k_props_faces(PropsArgs a);

@@ -60,6 +60,8 @@ module covof_gpu_bridge
      real(c_double) :: svof_filter_width
      integer(c_int) :: enable_diffusion_smoothing
      integer(c_int) :: diffusion_smoothing_steps
+     integer(c_int) :: advection_method
+     integer(c_int) :: tvd_limiter
   end type covof_params_t
 
   integer(c_int), parameter :: COVOF_OK = 0, COVOF_MAXITER = 1, COVOF_BREAKDOWN = 2

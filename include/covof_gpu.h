@@ -66,6 +66,13 @@ enum { COVOF_TIME_EULER = 1, COVOF_TIME_GEAR = 2 };
 enum { COVOF_CONV_LIN_PICARD = 1, COVOF_CONV_LIN_AB2 = 2, COVOF_CONV_LIN_NEWTON = 3 };
 /* Interface reconstruction (cfg%reconstruction_method). */
 enum { COVOF_RECON_PLIC = 0, COVOF_RECON_ELVIRA = 1 };
+/* VOF transport (cfg%advection_method, src/module_interface_vof.f90:801-808):
+ * WEYMOUTH_YUE (:1162-1377), CIAM (:938-1159, geometric with a Lagrangian
+ * remap of the cell width) or the algebraic TVD scheme (:828-935). */
+enum { COVOF_ADVECT_WEYMOUTH_YUE = 0, COVOF_ADVECT_CIAM = 1, COVOF_ADVECT_TVD = 2 };
+/* Limiter of the TVD transport (cfg%tvd_limiter,
+ * src/module_interface_reconstruction.f90:686-725). */
+enum { COVOF_LIMITER_SUPERBEE = 0, COVOF_LIMITER_VAN_LEER = 1, COVOF_LIMITER_MUSCL = 2, COVOF_LIMITER_HRIC = 3 };
 /* Pressure gauge.  REFERENCE: 1e-12*dvol diagonal shift + mean removal
  * (src/module_simulation.f90:2531,2579-2582).  PINNED: same operator with
  * cell (1,1) held at p = 0 (no mean removal). */
@@ -137,6 +144,8 @@ typedef struct covof_params {
   double svof_filter_width;
   int enable_diffusion_smoothing;
   int diffusion_smoothing_steps;
+  int advection_method;  /* COVOF_ADVECT_* */
+  int tvd_limiter;       /* COVOF_LIMITER_* (TVD transport only) */
 } covof_params;
 enum { COVOF_INNER_CHEBYSHEV = 0, COVOF_INNER_CG = 1, COVOF_INNER_CHEBYSHEV_STREAM = 2, COVOF_INNER_MG = 3 };
 

@@ -1267,6 +1267,160 @@ void wy_pass(const covof_params* prm, const Mesh& m, double dt, int dir, const d
 }
 
 // src/module_interface_vof.f90:1162-1377 advect_vof_weymouth_yue
+// src/module_interface_vof.f90:938-1159 advect_vof_ciam: the same donor-cell
+// flux volumes as Weymouth-Yue, then a Lagrangian remap of the cell width
+// (denom = dh - dt (u_e - u_w)), clamped after each pass.
+void ciam_pass(const covof_params* prm, const Mesh& m, double dt, int dir, const double* u,
+               const double* v, const double* Cin, double* Cout) {
+  const int nx = m.nx, ny = m.ny;
+  const double dx = m.dx, dy = m.dy;
+  size_t g = (size_t)(nx + 2) * (ny + 2);
+  std::vector<Seg> seg(g);
+  reconstruct_interface(prm, m, Cin, seg.data());
+  std::vector<double> flux(g, 0.0);
+  std::memcpy(Cout, Cin, g * sizeof(double));
+  if (dir == 0) {
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx + 1; ++i) {
+        double uf = u[m.id(i, j)];
+        double d = std::fabs(uf) * dt;
+        if (d <= 1.0e-14) continue;
+        double xp = m.x_face(i);
+        if (uf > 0.0) {
+          const Seg& s = seg[m.id(i - 1, j)];
+          flux[m.id(i, j)] = cut_box_area(xp - d, xp, m.y_face(j), m.y_face(j + 1), s.nx, s.ny, s.alpha);
+        } else {
+          const Seg& s = seg[m.id(i, j)];
+          flux[m.id(i, j)] = -cut_box_area(xp, xp + d, m.y_face(j), m.y_face(j + 1), s.nx, s.ny, s.alpha);
+        }
+      }
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        double denom = dx - dt * (u[m.id(i + 1, j)] - u[m.id(i, j)]);
+        double df = flux[m.id(i + 1, j)] - flux[m.id(i, j)];
+        double c = denom > 1.0e-12 ? (Cin[m.id(i, j)] * dx - df / dy) / denom : Cin[m.id(i, j)] - df / (dx * dy);
+        Cout[m.id(i, j)] = std::max(0.0, std::min(1.0, c));
+      }
+  } else {
+    for (int j = 1; j <= ny + 1; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        double vf = v[m.id(i, j)];
+        double d = std::fabs(vf) * dt;
+        if (d <= 1.0e-14) continue;
+        double yp = m.y_face(j);
+        if (vf > 0.0) {
+          const Seg& s = seg[m.id(i, j - 1)];
+          flux[m.id(i, j)] = cut_box_area(m.x_face(i), m.x_face(i + 1), yp - d, yp, s.nx, s.ny, s.alpha);
+        } else {
+          const Seg& s = seg[m.id(i, j)];
+          flux[m.id(i, j)] = -cut_box_area(m.x_face(i), m.x_face(i + 1), yp, yp + d, s.nx, s.ny, s.alpha);
+        }
+      }
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        double denom = dy - dt * (v[m.id(i, j + 1)] - v[m.id(i, j)]);
+        double df = flux[m.id(i, j + 1)] - flux[m.id(i, j)];
+        double c = denom > 1.0e-12 ? (Cin[m.id(i, j)] * dy - df / dx) / denom : Cin[m.id(i, j)] - df / (dx * dy);
+        Cout[m.id(i, j)] = std::max(0.0, std::min(1.0, c));
+      }
+  }
+}
+
+void ciam_step(const covof_params* prm, const Mesh& m, double dt, bool x_first, const double* u,
+               const double* v, double* C) {
+  size_t g = (size_t)(m.nx + 2) * (m.ny + 2);
+  std::vector<double> cs(g), cf(g);
+  int d1 = x_first ? 0 : 1, d2 = x_first ? 1 : 0;
+  ciam_pass(prm, m, dt, d1, u, v, C, cs.data());
+  vof_bc(m, cs.data());  // :1002-1004
+  ciam_pass(prm, m, dt, d2, u, v, cs.data(), cf.data());
+  std::memcpy(C, cf.data(), g * sizeof(double));
+}
+
+// src/module_interface_reconstruction.f90:686-725 evaluate_limiter
+double tvd_limiter(int lim, double r, double c_donor, double c_upwind, double c_acceptor) {
+  switch (lim) {
+    case COVOF_LIMITER_VAN_LEER:
+      return r > 0.0 ? 2.0 * r / (1.0 + r) : 0.0;
+    case COVOF_LIMITER_MUSCL:
+      return std::max(0.0, std::min(2.0 * r, std::min(0.5 * (1.0 + r), 2.0)));
+    case COVOF_LIMITER_HRIC: {
+      double denom = c_acceptor - c_upwind;
+      if (std::fabs(denom) < 1.0e-12) return 0.0;
+      double ctD = (c_donor - c_upwind) / denom;
+      double ctf = ctD;
+      if (ctD >= 0.0 && ctD <= 1.0) ctf = ctD < 0.5 ? 2.0 * ctD : 1.0;
+      if (std::fabs(1.0 - ctD) > 1.0e-12) {
+        double phi = 2.0 * (ctf - ctD) / (1.0 - ctD);
+        return std::max(0.0, std::min(2.0, phi));
+      }
+      return 1.0;
+    }
+    default:
+      return std::max(0.0, std::max(std::min(2.0 * r, 1.0), std::min(r, 2.0)));
+  }
+}
+
+// src/module_interface_vof.f90:828-935 advect_vof_tvd: limited upwind face
+// fluxes in both directions from C^n, one conservative update, clamp.
+void tvd_step(const covof_params* prm, const Mesh& m, double dt, const double* u, const double* v,
+              double* C) {
+  const int nx = m.nx, ny = m.ny;
+  const double dx = m.dx, dy = m.dy;
+  size_t g = (size_t)(nx + 2) * (ny + 2);
+  std::vector<double> fx(g, 0.0), fy(g, 0.0), cn(C, C + g);
+  const int lim = prm->tvd_limiter;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx + 1; ++i) {
+      double uf = u[m.id(i, j)];
+      double cl = C[m.id(i - 1, j)], cr = C[m.id(i, j)];
+      double cfl = 1.0 - std::min(1.0, std::fabs(uf) * dt / dx);
+      if (uf >= 0.0) {
+        double cu = C[m.id(std::max(0, i - 2), j)];
+        double dup = cl - cu, dloc = cr - cl;
+        double r = std::fabs(dloc) > 1.0e-12 ? dup / dloc : 0.0;
+        double phi = tvd_limiter(lim, r, cl, cu, cr);
+        fx[m.id(i, j)] = uf * (cl + 0.5 * phi * cfl * dloc);
+      } else {
+        double cu = C[m.id(std::min(nx + 1, i + 1), j)];
+        double dup = cu - cr, dloc = cr - cl;
+        double r = std::fabs(dloc) > 1.0e-12 ? dup / dloc : 0.0;
+        double phi = tvd_limiter(lim, r, cr, cu, cl);
+        fx[m.id(i, j)] = uf * (cr - 0.5 * phi * cfl * dloc);
+      }
+    }
+  for (int j = 1; j <= ny + 1; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      double vf = v[m.id(i, j)];
+      double cb = C[m.id(i, j - 1)], ct = C[m.id(i, j)];
+      double cfl = 1.0 - std::min(1.0, std::fabs(vf) * dt / dy);
+      if (vf >= 0.0) {
+        double cu = C[m.id(i, std::max(0, j - 2))];
+        double dup = cb - cu, dloc = ct - cb;
+        double r = std::fabs(dloc) > 1.0e-12 ? dup / dloc : 0.0;
+        double phi = tvd_limiter(lim, r, cb, cu, ct);
+        fy[m.id(i, j)] = vf * (cb + 0.5 * phi * cfl * dloc);
+      } else {
+        double cu = C[m.id(i, std::min(ny + 1, j + 1))];
+        double dup = cu - ct, dloc = ct - cb;
+        double r = std::fabs(dloc) > 1.0e-12 ? dup / dloc : 0.0;
+        double phi = tvd_limiter(lim, r, ct, cu, cb);
+        fy[m.id(i, j)] = vf * (ct - 0.5 * phi * cfl * dloc);
+      }
+    }
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t k = m.id(i, j);
+      double c = C[k] - (dt / dx) * (fx[m.id(i + 1, j)] - fx[k]) - (dt / dy) * (fy[m.id(i, j + 1)] - fy[k]);
+      cn[k] = std::max(0.0, std::min(1.0, c));
+    }
+  std::memcpy(C, cn.data(), g * sizeof(double));
+}
+
+// src/module_interface_vof.f90:801-808: the transport method of advect_vof
+void vof_transport(const covof_params* prm, const Mesh& m, double dt, bool x_first, const double* u,
+                   const double* v, double* C);
+
 void wy_step(const covof_params* prm, const Mesh& m, double dt, bool x_first, const double* u,
              const double* v, double* C) {
   size_t g = (size_t)(m.nx + 2) * (m.ny + 2);
@@ -1277,6 +1431,13 @@ void wy_step(const covof_params* prm, const Mesh& m, double dt, bool x_first, co
   vof_bc(m, cs.data());  // :1240-1243
   wy_pass(prm, m, dt, d2, u, v, cd.data(), cs.data(), cf.data(), true);
   std::memcpy(C, cf.data(), g * sizeof(double));
+}
+
+void vof_transport(const covof_params* prm, const Mesh& m, double dt, bool x_first, const double* u,
+                   const double* v, double* C) {
+  if (prm->advection_method == COVOF_ADVECT_CIAM) ciam_step(prm, m, dt, x_first, u, v, C);
+  else if (prm->advection_method == COVOF_ADVECT_TVD) tvd_step(prm, m, dt, u, v, C);
+  else wy_step(prm, m, dt, x_first, u, v, C);
 }
 
 // src/module_interface_vof.f90:387-476 smooth_svof_helmholtz: 25 symmetric
@@ -1661,6 +1822,16 @@ int orc_wy_step(const covof_params* prm, double dt, int x_first, const double* u
   return COVOF_OK;
 }
 
+// the configured transport alone (Weymouth-Yue, CIAM or TVD)
+int orc_vof_transport(const covof_params* prm, double dt, int x_first, const double* u,
+                      const double* v, double* C) {
+  int st = check_params(prm, true);
+  if (st) return st;
+  if (prm->advection_method < 0 || prm->advection_method > COVOF_ADVECT_TVD) return COVOF_INVALID;
+  vof_transport(prm, mesh_of(prm), dt, x_first != 0, u, v, C);
+  return COVOF_OK;
+}
+
 int orc_svof_smooth(const covof_params* prm, const double* C, double* C_s) {
   int st = check_params(prm, true);
   if (st) return st;
@@ -1702,7 +1873,7 @@ int orc_vof_advect(const covof_params* prm, double dt, int step_count, const dou
   int st = check_params(prm, true);
   if (st) return st;
   Mesh m = mesh_of(prm);
-  wy_step(prm, m, dt, (step_count % 2) == 0, u, v, C);
+  vof_transport(prm, m, dt, (step_count % 2) == 0, u, v, C);
   vof_bc(m, C);
   if (prm->enable_svof_smoothing && C_s) svof_smooth(prm, m, C, C_s);
   update_props(prm, m, C, rho, rho_u, rho_v, mu, mu_node, C_s);

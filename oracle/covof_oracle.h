@@ -94,6 +94,9 @@ int orc_sp_step(const covof_params* prm, double dt, double* u, double* v, double
 int orc_reconstruct(const covof_params* prm, const double* C, double* seg);
 int orc_wy_step(const covof_params* prm, double dt, int x_first, const double* u,
                 const double* v, double* C);
+/* the configured VOF transport alone (advection_method), pass order x_first */
+int orc_vof_transport(const covof_params* prm, double dt, int x_first, const double* u,
+                      const double* v, double* C);
 /* interface smoothing: SVOF (C -> C_s) and diffusion (C -> C_tilde) */
 int orc_svof_smooth(const covof_params* prm, const double* C, double* C_s);
 int orc_diffusion_smooth(const covof_params* prm, const double* C, double* C_tilde);

@@ -53,6 +53,7 @@ def lib():
             "orc_compute_curvature_and_csf": (i, [v] * 7),
             "orc_vof_advect": (i, [v, d, i] + [v] * 13),
             "orc_svof_smooth": (i, [v, v, v]),
+            "orc_vof_transport": (i, [v, d, i, v, v, v]),
             "orc_diffusion_smooth": (i, [v, v, v]),
         }
         for name, (res, args) in sig.items():
@@ -186,6 +187,12 @@ def reconstruct(prm, Cf):
 
 def wy_step(prm, dt, x_first, u, v, Cf):
     st = lib().orc_wy_step(_params(prm), dt, int(bool(x_first)), _p(u), _p(v), _p(Cf))
+    assert st == 0, st
+
+
+def vof_transport(prm, dt, x_first, u, v, Cf):
+    """The configured transport (Weymouth-Yue / CIAM / TVD) alone."""
+    st = lib().orc_vof_transport(_params(prm), dt, int(bool(x_first)), _p(u), _p(v), _p(Cf))
     assert st == 0, st
 
 
