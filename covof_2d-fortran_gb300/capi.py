@@ -25,6 +25,7 @@ TIME_EULER, TIME_GEAR = 1, 2
 CONV_LIN_PICARD, CONV_LIN_AB2, CONV_LIN_NEWTON = 1, 2, 3
 RECON_PLIC, RECON_ELVIRA = 0, 1
 ADVECT_WEYMOUTH_YUE, ADVECT_CIAM, ADVECT_TVD = 0, 1, 2
+SOLVER_AUGMENTED_LAGRANGIAN, SOLVER_MONOLITHIC, SOLVER_STANDARD_PROJECTION, SOLVER_AAL, SOLVER_CAAL = 1, 2, 3, 4, 5
 LIMITER_SUPERBEE, LIMITER_VAN_LEER, LIMITER_MUSCL, LIMITER_HRIC = 0, 1, 2, 3
 GAUGE_REFERENCE, GAUGE_PINNED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
@@ -57,6 +58,9 @@ class Params(C.Structure):
         ("enable_svof_smoothing", C.c_int), ("svof_filter_width", C.c_double),
         ("enable_diffusion_smoothing", C.c_int), ("diffusion_smoothing_steps", C.c_int),
         ("advection_method", C.c_int), ("tvd_limiter", C.c_int),
+        ("solver_type", C.c_int), ("r_al", C.c_double), ("adaptative_al", C.c_int), ("k_aal", C.c_double),
+        ("l0_ref", C.c_double), ("t0_ref", C.c_double), ("u0_ref", C.c_double), ("p0_ref", C.c_double),
+        ("ic_radius", C.c_double), ("uzawa_iter", C.c_int), ("uzawa_tol", C.c_double),
     ]
 
     def copy(self) -> "Params":
@@ -144,6 +148,7 @@ _SIGS = {
     "covof_state_field_dev": [_VP, C.c_int, C.POINTER(C.c_void_p)],
     "covof_set_has_nm1": [_VP, C.c_int],
     "covof_svof_smooth": [_VP, _VP, _VP],
+    "covof_al_step": [_VP, C.c_double] + [_VP] * 12 + [_IP, _IP],
     "covof_diffusion_smooth": [_VP, _VP, _VP],
     "covof_get_has_nm1": [_VP, C.POINTER(C.c_int)],
     "covof_batch_set_has_nm1": [_VP, C.c_int],

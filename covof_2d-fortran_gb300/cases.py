@@ -71,6 +71,14 @@ def make_params(nx: int, ny: int, lx: float, ly: float) -> Params:
     p.diffusion_smoothing_steps = 3
     p.advection_method = capi.ADVECT_WEYMOUTH_YUE
     p.tvd_limiter = capi.LIMITER_SUPERBEE
+    p.solver_type = capi.SOLVER_STANDARD_PROJECTION
+    p.r_al = 100.0
+    p.adaptative_al = 0
+    p.k_aal = 100.0
+    p.l0_ref = p.t0_ref = p.u0_ref = p.p0_ref = 0.0
+    p.ic_radius = 0.25
+    p.uzawa_iter = 1
+    p.uzawa_tol = 1.0e-12
     return p
 
 

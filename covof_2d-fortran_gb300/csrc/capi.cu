@@ -122,6 +122,7 @@ int ensure_mom(covof_handle* h) {
   const size_t g2 = 2 * h->g;
   CS(dalloc(&h->mx, g2)); CS(dalloc(&h->mrhs, g2)); CS(dalloc(&h->mdiag, g2));
   CS(dalloc(&h->mcoef, 9 * g2)); CS(dalloc(&h->midiag, g2));
+  CS(dalloc(&h->al_r, h->g)); CS(dalloc(&h->al_max, 4));
   for (int q = 0; q < 7; ++q) CS(dalloc(&h->mv[q], g2));
   h->have_mom = true;
   return COVOF_OK;
@@ -534,6 +535,7 @@ MomArgs mom_args(covof_handle* h, double dt, const double* u_n, const double* v_
   a.ab2 = P.convective_linearization == COVOF_CONV_LIN_AB2 ? 1 : 0;
   a.ab2_ext = (a.ab2 && h->has_nm1) ? 1 : 0;
   a.u_nm1 = h->f_u_nm1; a.v_nm1 = h->f_v_nm1;
+  a.r_al = nullptr; a.p_al = nullptr;  // set by al_enqueue
   a.u_n = u_n; a.v_n = v_n; a.rho_u = rho_u; a.rho_v = rho_v; a.mu = mu; a.mu_node = mu_node;
   a.fx = fx; a.fy = fy; a.u_old = u_old; a.v_old = v_old;
   a.x = h->mx; a.rhs = h->mrhs; a.diag = h->mdiag; a.coef = h->mcoef; a.idiag = h->midiag;
@@ -605,6 +607,104 @@ int mom_post(covof_handle* h, const MomArgs& a, double* u, double* v) {
   k_mom_unpack<<<grd, blk, 0, h->stream>>>(a, u, v);
   CK(cudaGetLastError());
   return velocity_bc_dev(h, u, v);
+}
+
+// ---------------------------------------------------------------------------
+// Augmented Lagrangian coupling (solver_type AUGMENTED_LAGRANGIAN / AAL)
+bool is_al(const covof_params& P) {
+  return P.solver_type == COVOF_SOLVER_AUGMENTED_LAGRANGIAN || P.solver_type == COVOF_SOLVER_AAL;
+}
+
+int check_coupling(const covof_params& P) {
+  if (P.solver_type == 0 || P.solver_type == COVOF_SOLVER_STANDARD_PROJECTION || is_al(P)) return COVOF_OK;
+  if (P.solver_type == COVOF_SOLVER_MONOLITHIC || P.solver_type == COVOF_SOLVER_CAAL) return COVOF_UNSUPPORTED;
+  return COVOF_INVALID;
+}
+
+AlArgs al_args(covof_handle* h, double dt, const double* u, const double* v, double* p, const double* rho,
+               const double* mu) {
+  const covof_params& P = h->prm;
+  AlArgs a;
+  a.D = h->D; a.dx = P.dx; a.dy = P.dy; a.dt = dt;
+  a.u = u; a.v = v; a.rho = rho; a.mu = mu; a.p = p; a.r = h->al_r; a.maxv = h->al_max;
+  a.adaptive = P.adaptative_al ? 1 : 0;
+  a.r_al = P.r_al; a.k_aal = P.k_aal;
+  // src/module_navier_stokes.f90:1137-1147 (the domain lengths are nx dx, ny dy)
+  const double lx = P.nx * P.dx, ly = P.ny * P.dy;
+  if (P.l0_ref > 0.0) a.L0 = P.l0_ref;
+  else if (P.enable_two_phase && P.ic_radius > 0.0) a.L0 = 2.0 * P.ic_radius;
+  else a.L0 = fmin(lx, ly);
+  a.t0 = P.t0_ref > 0.0 ? P.t0_ref : dt;
+  a.g_norm = sqrt(P.gx * P.gx + P.gy * P.gy);
+  a.sigma = P.enable_two_phase ? P.sigma : 0.0;
+  a.alpha_time = (P.time_scheme == COVOF_TIME_GEAR && h->has_nm1) ? 1.5 : 1.0;
+  a.u0_ref = P.u0_ref; a.p0_ref = P.p0_ref;
+  a.mu_max = fmax(P.mu1, P.mu2);
+  return a;
+}
+
+// src/module_simulation.f90:546-607: the penalty field, the preconditioner
+// diagonal once (from the fields at the start of the coupling), then Uzawa
+// iterations of rhs (with -grad p), assembly (linearised about the current
+// u), pack, the Krylov solve, unpack + velocity BC and p -= r div u.  The
+// max |div u| exit test (uzawa_iter > 1, uzawa_tol > 0) reads one scalar
+// back per iteration (host_check); without it nothing waits for the host.
+int al_enqueue(covof_handle* h, double dt, double* u, double* v, double* p, const double* rho,
+               const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+               const double* fx, const double* fy, const double* u_old, const double* v_old, bool host_check,
+               int* total_iters, int* uzawa_done) {
+  const covof_params& P = h->prm;
+  if (!u || !v || !p || !rho || !rho_u || !rho_v || !mu || !mu_node || !fx || !fy || !u_old || !v_old)
+    return COVOF_INVALID;
+  CS(check_mom_params(P));
+  CS(ensure_mom(h));
+  CS(predictor_plan(h));
+  const dim3 blk(32, 8);
+  const dim3 gc = grid2(P.nx, P.ny, blk), gg = grid2(P.nx + 2, P.ny + 2, blk), gf = grid2(P.nx + 1, P.ny + 1, blk);
+  AlArgs al = al_args(h, dt, u, v, p, rho, mu);
+  if (al.adaptive) {
+    CK(cudaMemsetAsync(h->al_max, 0, 2 * sizeof(unsigned long long), h->stream));
+    k_al_maxima<<<gc, blk, 0, h->stream>>>(al);
+  }
+  k_al_penalty<<<gg, blk, 0, h->stream>>>(al);
+  MomArgs a = mom_args(h, dt, u, v, rho_u, rho_v, mu, mu_node, fx, fy, u_old, v_old);
+  a.r_al = h->al_r;
+  a.p_al = p;
+  k_mom_diag<<<gf, blk, 0, h->stream>>>(a);
+  CK(cudaGetLastError());
+  const int umax = P.uzawa_iter > 0 ? P.uzawa_iter : 1;
+  int total = 0, done = 0, status = COVOF_OK;
+  for (int m = 1; m <= umax; ++m) {
+    done = m;
+    k_mom_rhs<<<gf, blk, 0, h->stream>>>(a);
+    k_mom_assemble<<<gf, blk, 0, h->stream>>>(a);
+    k_mom_pack<<<gf, blk, 0, h->stream>>>(a, u, v);
+    CK(cudaGetLastError());
+    void* args[] = {&a};
+    CS(launch_coop(h, h->m_fn, h->m_nb, kKrylovThreads, args, false));
+    CS(mom_post(h, a, u, v));
+    k_al_pressure<<<gc, blk, 0, h->stream>>>(al);
+    CK(cudaGetLastError());
+    if (host_check || total_iters) {
+      CK(cudaMemcpyAsync(h->h_kres, h->d_kres, sizeof(KrylovResult), cudaMemcpyDeviceToHost, h->stream));
+      unsigned long long dm = 0;
+      if (host_check) {
+        CK(cudaMemsetAsync(h->al_max + 2, 0, sizeof(unsigned long long), h->stream));
+        k_al_divmax<<<gc, blk, 0, h->stream>>>(al);
+        CK(cudaMemcpyAsync(&dm, h->al_max + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+      }
+      CS(sync(h));
+      total += h->h_kres->iters;
+      if (h->h_kres->status != COVOF_OK) status = h->h_kres->status;
+      if (status == COVOF_NAN || status == COVOF_TIMEOUT) break;
+      double dmax;
+      std::memcpy(&dmax, &dm, sizeof(double));
+      if (host_check && umax > 1 && P.uzawa_tol > 0.0 && dmax <= P.uzawa_tol) break;
+    }
+  }
+  if (total_iters) *total_iters = total;
+  if (uzawa_done) *uzawa_done = done;
+  return status;
 }
 
 // Predictor on the handle's stream, result record left on the device.
@@ -863,11 +963,18 @@ int enqueue_step(covof_handle* h, double dt, bool x_first) {
     CS(smooth_props_csf(h, true));
     CS(velocity_bc_dev(h, h->f_u, h->f_v));
   }
-  CS(predictor_enqueue(h, dt, h->f_u, h->f_v, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node, h->f_fx,
-                       h->f_fy, h->f_u_old, h->f_v_old));
-  CS(poisson_enqueue(h, dt, h->f_u, h->f_v, nullptr, h->f_rho_u, h->f_rho_v, h->f_p, false));
-  CS(correct_dev(h, dt, h->f_u, h->f_v, h->f_p, h->f_rho_u, h->f_rho_v));
-  CS(velocity_bc_dev(h, h->f_u, h->f_v));
+  if (is_al(h->prm)) {
+    CS(al_enqueue(h, dt, h->f_u, h->f_v, h->f_p, h->f_rho, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node,
+                  h->f_fx, h->f_fy, h->f_u_old, h->f_v_old, h->al_check, nullptr, nullptr));
+    // no Poisson solve in this coupling: its record reads COVOF_OK, 0 iterations
+    CK(cudaMemsetAsync(h->d_pres, 0, sizeof(PcgResult), h->stream));
+  } else {
+    CS(predictor_enqueue(h, dt, h->f_u, h->f_v, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node, h->f_fx,
+                         h->f_fy, h->f_u_old, h->f_v_old));
+    CS(poisson_enqueue(h, dt, h->f_u, h->f_v, nullptr, h->f_rho_u, h->f_rho_v, h->f_p, false));
+    CS(correct_dev(h, dt, h->f_u, h->f_v, h->f_p, h->f_rho_u, h->f_rho_v));
+    CS(velocity_bc_dev(h, h->f_u, h->f_v));
+  }
   k_step_log<<<1, 32, 0, h->stream>>>(h->d_kres, h->d_pres, h->d_run);
   CK(cudaGetLastError());
   return COVOF_OK;
@@ -910,6 +1017,10 @@ int run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run_stats
   const covof_params& P = h->prm;
   if (P.p_precond == COVOF_PRECOND_SSOR) return COVOF_UNSUPPORTED;
   CS(check_mom_params(P));
+  CS(check_coupling(P));
+  // the Uzawa exit test reads a scalar back per iteration: eager steps
+  h->al_check = is_al(P) && P.uzawa_iter > 1 && P.uzawa_tol > 0.0;
+  if (h->al_check) flags &= ~COVOF_RUN_GRAPH;
   // every buffer and launch plan exists before a capture starts
   CS(ensure_fields(h));
   CS(ensure_poisson(h));
@@ -1021,6 +1132,14 @@ void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly)
   p->diffusion_smoothing_steps = 3;
   p->advection_method = COVOF_ADVECT_WEYMOUTH_YUE;
   p->tvd_limiter = COVOF_LIMITER_SUPERBEE;
+  p->solver_type = COVOF_SOLVER_STANDARD_PROJECTION;
+  p->r_al = 100.0;
+  p->adaptative_al = 0;
+  p->k_aal = 100.0;
+  p->l0_ref = p->t0_ref = p->u0_ref = p->p0_ref = 0.0;
+  p->ic_radius = 0.25;
+  p->uzawa_iter = 1;
+  p->uzawa_tol = 1.0e-12;
 }
 
 int covof_abi_version(void) { return COVOF_ABI_VERSION; }
@@ -1080,7 +1199,7 @@ int covof_destroy(covof_handle* h) {
   if (!h) return COVOF_INVALID;
   if (h->stream) cudaStreamSynchronize(h->stream);
   double** fl[] = {&h->f_u, &h->f_v, &h->f_p, &h->f_rho_u, &h->f_rho_v, &h->f_mu, &h->f_mu_node,
-                   &h->f_fx, &h->f_fy, &h->f_u_old, &h->f_v_old, &h->f_u_nm1, &h->f_v_nm1, &h->f_Cs, &h->f_Ct, &h->dscr,
+                   &h->f_fx, &h->f_fy, &h->f_u_old, &h->f_v_old, &h->f_u_nm1, &h->f_v_nm1, &h->f_Cs, &h->f_Ct, &h->dscr, &h->al_r,
                    &h->f_C, &h->f_rho, &h->f_curv,
                    &h->f_b, &h->f_x2, &h->f_seg, &h->px, &h->pb, &h->pr, &h->pd, &h->pAd,
                    &h->pax, &h->pay, &h->paP, &h->pisd, &h->pinvD, &h->pd2, &h->pz, &h->pw, &h->pp, &h->pq, &h->mx, &h->mrhs, &h->mdiag, &h->cs, &h->seg, &h->mcoef, &h->midiag,
@@ -1373,6 +1492,31 @@ int covof_sp_step(covof_handle* h, double dt, double* u, double* v, double* p,
     return st;
   CS(d2h(h, u, h->f_u, g)); CS(d2h(h, v, h->f_v, g)); CS(d2h(h, p, h->f_p, g));
   CS(sync(h));
+  return st;
+}
+
+// ---- augmented Lagrangian step -------------------------------------------------
+int covof_al_step(covof_handle* h, double dt, double* u, double* v, double* p, const double* rho,
+                  const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                  const double* fx_sigma, const double* fy_sigma, const double* u_old, const double* v_old,
+                  int* total_iters, int* uzawa_done) {
+  if (!h) return COVOF_INVALID;
+  if (!is_al(h->prm)) return COVOF_INVALID;
+  CS(ensure_fields(h));
+  const size_t g = h->g;
+  CS(h2d(h, h->f_u, u, g)); CS(h2d(h, h->f_v, v, g)); CS(h2d(h, h->f_p, p, g));
+  CS(h2d(h, h->f_rho, rho, g)); CS(h2d(h, h->f_rho_u, rho_u, g)); CS(h2d(h, h->f_rho_v, rho_v, g));
+  CS(h2d(h, h->f_mu, mu, g)); CS(h2d(h, h->f_mu_node, mu_node, g));
+  CS(h2d(h, h->f_fx, fx_sigma, g)); CS(h2d(h, h->f_fy, fy_sigma, g));
+  CS(h2d(h, h->f_u_old, u_old, g)); CS(h2d(h, h->f_v_old, v_old, g));
+  int it = 0, ud = 0;
+  const int st = al_enqueue(h, dt, h->f_u, h->f_v, h->f_p, h->f_rho, h->f_rho_u, h->f_rho_v, h->f_mu,
+                            h->f_mu_node, h->f_fx, h->f_fy, h->f_u_old, h->f_v_old, true, &it, &ud);
+  if (st == COVOF_CUDA_ERROR || st == COVOF_INVALID || st == COVOF_UNSUPPORTED || st == COVOF_TIMEOUT) return st;
+  CS(d2h(h, u, h->f_u, g)); CS(d2h(h, v, h->f_v, g)); CS(d2h(h, p, h->f_p, g));
+  CS(sync(h));
+  if (total_iters) *total_iters = it;
+  if (uzawa_done) *uzawa_done = ud;
   return st;
 }
 

@@ -65,6 +65,9 @@ struct covof_handle {
   size_t g = 0;
   int vof_step_count = 0;
   bool has_nm1 = false;  // u_nm1 / v_nm1 hold step n-1 (fields%has_nm1)
+  double* al_r = nullptr;                // augmented Lagrangian penalty field r_aal
+  unsigned long long* al_max = nullptr;  // maxima of the penalty scales and of |div u|
+  bool al_check = false;                // resident steps test the Uzawa exit on the host
   unsigned int* svof_prog = nullptr;  // SVOF band progress (32 words per band)
   int svof_nb = 0;                    // blocks of the SVOF launch (planned by ensure_vof)
   // caller-field mirrors (host-pointer entry points)
@@ -153,6 +156,12 @@ int mom_pre(covof_handle* h, double dt, double* u, double* v, const double* rho_
 int mom_post(covof_handle* h, const MomArgs& a, double* u, double* v);
 int wy_step_dev(covof_handle* h, double dt, int x_first, const double* u, const double* v, double* C);
 bool needs_history(const covof_params& P);
+bool is_al(const covof_params& P);
+int check_coupling(const covof_params& P);
+int al_enqueue(covof_handle* h, double dt, double* u, double* v, double* p, const double* rho,
+               const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+               const double* fx, const double* fy, const double* u_old, const double* v_old, bool host_check,
+               int* total_iters, int* uzawa_done);
 int rotate_history(covof_handle* h);
 void drop_graphs(covof_handle* h);
 int vof_bc_dev(covof_handle* h, double* C);

@@ -275,6 +275,12 @@ __device__ auto mom_apply_gen(const MomArgs& a, int part, int i, int j, const S&
     const auto sN = mN * ((uN - uc) / dy + (src.v(i, j + 1) - src.v(i - 1, j + 1)) / dx) * dx;
     const auto sS = mS * ((uc - uS) / dy + (src.v(i, j) - src.v(i - 1, j)) / dx) * dx;
     val = val - (sN - sS);
+    if (a.r_al) {
+      // :584-595: -(r_E div(i,j) - r_W div(i-1,j)) dy, div of the operand
+      const auto dE = (uE - uc) / dx + (src.v(i, j + 1) - src.v(i, j)) / dy;
+      const auto dW = (uc - uW) / dx + (src.v(i - 1, j + 1) - src.v(i - 1, j)) / dy;
+      val = val - (a.r_al[k] * dE - a.r_al[k - 1] * dW) * dy;
+    }
     return val;
   }
   const double rho = a.rho_v[k];
@@ -309,6 +315,12 @@ __device__ auto mom_apply_gen(const MomArgs& a, int part, int i, int j, const S&
   const auto sE = mE * ((vE - vc) / dx + (src.u(i + 1, j) - src.u(i + 1, j - 1)) / dy) * dy;
   const auto sW = mW * ((vc - vW) / dx + (src.u(i, j) - src.u(i, j - 1)) / dy) * dy;
   val = val - (sE - sW);
+  if (a.r_al) {
+    // :711-721: -(r_N div(i,j) - r_S div(i,j-1)) dx
+    const auto dN = (src.u(i + 1, j) - src.u(i, j)) / dx + (vN - vc) / dy;
+    const auto dS = (src.u(i + 1, j - 1) - src.u(i, j - 1)) / dx + (vc - vS) / dy;
+    val = val - (a.r_al[k] * dN - a.r_al[k - D.P] * dS) * dx;
+  }
   return val;
 }
 
@@ -355,7 +367,9 @@ __global__ void k_mom_diag(MomArgs a) {
         u_fluxes(a, i, j, FE, FW, FN, FS);
         conv_diag = rho * (fmax(FE, 0.0) + fmax(-FW, 0.0) + fmax(FN, 0.0) + fmax(-FS, 0.0));
       }
-      double aP = Du + dwy + conv_diag + 0.0 + 0.0 + cW + cE + cSv + cNv + 0.0 + 0.0;
+      double alW = 0.0, alE = 0.0;
+      if (a.r_al) { alW = a.r_al[k - 1] * (dy / dx); alE = a.r_al[k] * (dy / dx); }
+      double aP = Du + dwy + conv_diag + 0.0 + 0.0 + cW + cE + cSv + cNv + alW + alE;
       if (aP <= 1.0e-15) aP = 1.0;
       out = aP;
     }
@@ -389,7 +403,9 @@ __global__ void k_mom_diag(MomArgs a) {
         v_fluxes(a, i, j, FE, FW, FN, FS);
         conv_diag = rho * (fmax(FE, 0.0) + fmax(-FW, 0.0) + fmax(FN, 0.0) + fmax(-FS, 0.0));
       }
-      double aP = Dv + dwx + conv_diag + 0.0 + 0.0 + cWv + cEv + cS + cN + 0.0 + 0.0;
+      double alS = 0.0, alN = 0.0;
+      if (a.r_al) { alS = a.r_al[k - D.P] * (dx / dy); alN = a.r_al[k] * (dx / dy); }
+      double aP = Dv + dwx + conv_diag + 0.0 + 0.0 + cWv + cEv + cS + cN + alS + alN;
       if (aP <= 1.0e-15) aP = 1.0;
       out = aP;
     }
@@ -425,6 +441,7 @@ __global__ void k_mom_rhs(MomArgs a) {
       }
       val = val + rho * a.gx * dvol;
       val = val + a.fx[k] * dvol;
+      if (a.p_al) val = val - (a.p_al[k] - a.p_al[k - 1]) * dy;  // :908-913
       if (j == ny && a.bc[ST] == COVOF_BC_DIRICHLET) {
         const double mN = a.mu_node[k + D.P];
         if (ny >= 2) val = val + mN * ((8.0 / 3.0) * a.bcu[ST] / dy) * dx;
@@ -458,6 +475,7 @@ __global__ void k_mom_rhs(MomArgs a) {
       }
       val = val + rho * a.gy * dvol;
       val = val + a.fy[k] * dvol;
+      if (a.p_al) val = val - (a.p_al[k] - a.p_al[k - D.P]) * dx;  // :1053-1058
       if (i == 1 && a.bc[SL] == COVOF_BC_DIRICHLET) {
         const double mW = a.mu_node[k];
         val = val + mW * (2.0 * a.bcv[SL] / dx) * dy;
@@ -966,6 +984,97 @@ __global__ void __launch_bounds__(512) k_mom_krylov_batch(const MomArgs* __restr
     else if (a.method == COVOF_LINEAR_CG) cg_case(a, tm, R);
     else bicgstab2_case(a, tm, R);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Augmented Lagrangian (solver_type AUGMENTED_LAGRANGIAN / AAL).
+// Maxima of nonnegative doubles through their bit patterns (monotone for
+// x >= 0), so the order of the atomics does not matter.
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* p, double x) {
+  atomicMax(p, (unsigned long long)__double_as_longlong(x));
+}
+__device__ __forceinline__ double block_max(double x) {
+  for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+  return x;
+}
+
+// max over interior cells of the cell-centre speed and of |p|
+// (src/module_navier_stokes.f90:1149-1160); maxv[0..1] zero at launch.
+__global__ void k_al_maxima(AlArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  double spd = 0.0, pa = 0.0;
+  if (i <= a.D.nx && j <= a.D.ny) {
+    const int k = a.D.id(i, j);
+    const double uc = 0.5 * (a.u[k] + a.u[k + 1]);
+    const double vc = 0.5 * (a.v[k] + a.v[k + a.D.P]);
+    spd = sqrt(uc * uc + vc * vc);
+    pa = fabs(a.p[k]);
+  }
+  spd = block_max(spd);
+  pa = block_max(pa);
+  if ((threadIdx.x + threadIdx.y * blockDim.x) % 32 == 0) {
+    atomic_max_nonneg(a.maxv + 0, spd);
+    atomic_max_nonneg(a.maxv + 1, pa);
+  }
+}
+
+// r_aal (src/module_navier_stokes.f90:1120-1216, incompressible): r_al
+// everywhere, or k_aal * max(unsteady, inertial, gravity, pressure, viscous,
+// capillary) per interior cell with the velocity / pressure scales from
+// k_al_maxima.
+__global__ void k_al_penalty(AlArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.D.nx, ny = a.D.ny;
+  if (i > nx + 1 || j > ny + 1) return;
+  const int k = a.D.id(i, j);
+  if (!a.adaptive) { a.r[k] = a.r_al; return; }
+  if (i < 1 || i > nx || j < 1 || j > ny) return;  // ghosts are never read
+  const double u_max = __longlong_as_double((long long)a.maxv[0]);
+  const double p_max = __longlong_as_double((long long)a.maxv[1]);
+  const double L0 = a.L0, t0 = a.t0;
+  double u0 = a.u0_ref > 0.0 ? a.u0_ref : u_max;
+  if (u0 < 1.0e-12) {
+    const double u_grav = a.g_norm > 0.0 ? sqrt(a.g_norm * L0) : 0.0;
+    const double u_cap = (a.sigma > 0.0 && a.mu_max > 1.0e-30) ? a.sigma / a.mu_max : 0.0;
+    u0 = fmax(fmax(fmax(u_grav, u_cap), L0 / fmax(t0, 1.0e-12)), 1.0e-3);
+  }
+  const double p0 = a.p0_ref > 0.0 ? a.p0_ref : p_max;
+  const double rM = a.rho[k], mM = a.mu[k];
+  const double t_uns = a.alpha_time * rM * (L0 * L0) / fmax(t0, 1.0e-30);
+  const double t_in = rM * u0 * L0;
+  const double t_gr = rM * (L0 * L0 / u0) * a.g_norm;
+  const double t_pr = (p0 * L0) / u0;
+  const double t_vi = mM;
+  const double t_ca = a.sigma / u0;
+  const double mx = fmax(fmax(fmax(t_uns, t_in), fmax(t_gr, t_pr)), fmax(fmax(t_vi, 0.0), t_ca));
+  double r = a.k_aal * mx;
+  if (r <= 1.0e-15) r = a.r_al;
+  a.r[k] = r;
+}
+
+// p -= r div u on interior cells (src/module_navier_stokes.f90:1223-1263)
+__global__ void k_al_pressure(AlArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > a.D.nx || j > a.D.ny) return;
+  const int k = a.D.id(i, j);
+  const double dv = (a.u[k + 1] - a.u[k]) / a.dx + (a.v[k + a.D.P] - a.v[k]) / a.dy;
+  a.p[k] = a.p[k] - a.r[k] * dv;
+}
+
+// max |div u| over interior cells into maxv[2] (zero at launch)
+__global__ void k_al_divmax(AlArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  double d = 0.0;
+  if (i <= a.D.nx && j <= a.D.ny) {
+    const int k = a.D.id(i, j);
+    d = fabs((a.u[k + 1] - a.u[k]) / a.dx + (a.v[k + a.D.P] - a.v[k]) / a.dy);
+  }
+  d = block_max(d);
+  if ((threadIdx.x + threadIdx.y * blockDim.x) % 32 == 0) atomic_max_nonneg(a.maxv + 2, d);
 }
 
 }  // namespace covof

@@ -22,6 +22,9 @@ struct MomArgs {
   double alpha;
   int gear_rhs, ab2, ab2_ext;
   const double* u_nm1; const double* v_nm1;
+  // augmented Lagrangian (solver_type AL / AAL): penalty field r_aal and the
+  // pressure of the right-hand side's -grad p term; nullptr for projection
+  const double* r_al; const double* p_al;
   // fields_old of the operator (u^n with ghosts) and material properties
   const double* u_n; const double* v_n;
   const double* rho_u; const double* rho_v; const double* mu; const double* mu_node;
@@ -46,6 +49,23 @@ struct BcArgs {
 };
 
 __global__ void k_mom_diag(MomArgs a);
+
+// Augmented Lagrangian (momentum.cu)
+struct AlArgs {
+  Dims D;
+  double dx, dy, dt;
+  const double *u, *v, *rho, *mu;
+  double* p;
+  double* r;                     // penalty field r_aal
+  unsigned long long* maxv;      // [0] max |u_cell|, [1] max |p|, [2] max |div u| (bit patterns)
+  // penalty parameters (src/module_navier_stokes.f90:1106-1218)
+  int adaptive;
+  double r_al, k_aal, L0, t0, g_norm, sigma, alpha_time, u0_ref, p0_ref, mu_max;
+};
+__global__ void k_al_maxima(AlArgs a);
+__global__ void k_al_penalty(AlArgs a);
+__global__ void k_al_pressure(AlArgs a);
+__global__ void k_al_divmax(AlArgs a);
 __global__ void k_mom_rhs(MomArgs a);
 __global__ void k_mom_assemble(MomArgs a);
 __global__ void k_mom_apply(MomArgs a, const double* xu, const double* xv, double* yu, double* yv);

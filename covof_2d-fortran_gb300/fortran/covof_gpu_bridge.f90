@@ -62,6 +62,12 @@ module covof_gpu_bridge
      integer(c_int) :: diffusion_smoothing_steps
      integer(c_int) :: advection_method
      integer(c_int) :: tvd_limiter
+     integer(c_int) :: solver_type
+     real(c_double) :: r_al
+     integer(c_int) :: adaptative_al
+     real(c_double) :: k_aal, l0_ref, t0_ref, u0_ref, p0_ref, ic_radius
+     integer(c_int) :: uzawa_iter
+     real(c_double) :: uzawa_tol
   end type covof_params_t
 
   integer(c_int), parameter :: COVOF_OK = 0, COVOF_MAXITER = 1, COVOF_BREAKDOWN = 2

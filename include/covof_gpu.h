@@ -70,6 +70,14 @@ enum { COVOF_RECON_PLIC = 0, COVOF_RECON_ELVIRA = 1 };
  * WEYMOUTH_YUE (:1162-1377), CIAM (:938-1159, geometric with a Lagrangian
  * remap of the cell width) or the algebraic TVD scheme (:828-935). */
 enum { COVOF_ADVECT_WEYMOUTH_YUE = 0, COVOF_ADVECT_CIAM = 1, COVOF_ADVECT_TVD = 2 };
+/* Velocity-pressure coupling (cfg%solver_type, src/module_constants.f90:41-49;
+ * 0 reads as STANDARD_PROJECTION).  AUGMENTED_LAGRANGIAN / AAL: Uzawa
+ * iterations of the momentum solve with the penalty r grad(div u) and the
+ * update p -= r div u (src/module_simulation.f90:561-607); r is r_al, or the
+ * adaptive field of src/module_navier_stokes.f90:1106-1218 with adaptative_al.
+ * MONOLITHIC and the compressible CAAL return COVOF_UNSUPPORTED. */
+enum { COVOF_SOLVER_AUGMENTED_LAGRANGIAN = 1, COVOF_SOLVER_MONOLITHIC = 2, COVOF_SOLVER_STANDARD_PROJECTION = 3,
+       COVOF_SOLVER_AAL = 4, COVOF_SOLVER_CAAL = 5 };
 /* Limiter of the TVD transport (cfg%tvd_limiter,
  * src/module_interface_reconstruction.f90:686-725). */
 enum { COVOF_LIMITER_SUPERBEE = 0, COVOF_LIMITER_VAN_LEER = 1, COVOF_LIMITER_MUSCL = 2, COVOF_LIMITER_HRIC = 3 };
@@ -146,6 +154,16 @@ typedef struct covof_params {
   int diffusion_smoothing_steps;
   int advection_method;  /* COVOF_ADVECT_* */
   int tvd_limiter;       /* COVOF_LIMITER_* (TVD transport only) */
+  /* coupling (cfg%solver_type, r_al, adaptative_al, k_aal, l0_ref, t0_ref,
+   * u0_ref, p0_ref, ic_radius, uzawa_iter, uzawa_tol) */
+  int solver_type;       /* COVOF_SOLVER_* */
+  double r_al;           /* penalty (100) */
+  int adaptative_al;     /* adaptive penalty field */
+  double k_aal;          /* adaptive amplification (100) */
+  double l0_ref, t0_ref, u0_ref, p0_ref;  /* reference scales, 0 = automatic */
+  double ic_radius;      /* two-phase length scale 2 ic_radius when l0_ref = 0 (0.25) */
+  int uzawa_iter;        /* Uzawa iterations per step (1) */
+  double uzawa_tol;      /* stop when max |div u| <= uzawa_tol (1e-12; with uzawa_iter > 1) */
 } covof_params;
 enum { COVOF_INNER_CHEBYSHEV = 0, COVOF_INNER_CG = 1, COVOF_INNER_CHEBYSHEV_STREAM = 2, COVOF_INNER_MG = 3 };
 
@@ -321,6 +339,20 @@ int covof_update_physical_properties(covof_handle* h, double* C, double* rho, do
  * when those are enabled. */
 int covof_compute_curvature_and_csf(covof_handle* h, const double* C, double* fx_sigma,
                                     double* fy_sigma, double* curvature);
+
+/* One augmented-Lagrangian step (solver_type AUGMENTED_LAGRANGIAN / AAL,
+ * src/module_simulation.f90:546-607): the penalty field r_aal (r_al, or the
+ * adaptive field with adaptative_al), the predictor's Jacobi diagonal, then
+ * up to uzawa_iter Uzawa iterations of the penalised momentum solve and
+ * p -= r div u, stopping when max |div u| <= uzawa_tol.  Gear / AB2 read the
+ * handle's history as in covof_predictor.  total_iters: predictor Krylov
+ * iterations summed over the Uzawa iterations; uzawa_done: iterations run.
+ * covof_run_steps runs this coupling in place of STANDARD_PROJECTION when
+ * solver_type asks for it (eagerly when the Uzawa exit test is on). */
+int covof_al_step(covof_handle* h, double dt, double* u, double* v, double* p, const double* rho,
+                  const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                  const double* fx_sigma, const double* fy_sigma, const double* u_old, const double* v_old,
+                  int* total_iters, int* uzawa_done);
 
 /* ---- device-resident time stepping ------------------------------------ */
 

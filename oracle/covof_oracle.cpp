@@ -505,6 +505,10 @@ struct MomCtx {
   const double *u_adv, *v_adv;   // advecting velocity: fields%u (PICARD) or u_old (AB2)
   const double *u_nm1, *v_nm1;   // AB2 extrapolation partner, nullptr without history
   const double *u_nm1_rhs, *v_nm1_rhs;  // fields%u_nm1 for the Gear right-hand side
+  // augmented Lagrangian (solver_type AL / AAL): the penalty field r_aal and
+  // the pressure of the right-hand side's gradient term; nullptr for SP
+  const double* r_al = nullptr;
+  const double* p_al = nullptr;
   int u_nx, v_ny;
   size_t nu, nv;
 };
@@ -628,6 +632,12 @@ void mom_apply(const MomCtx& c, const double* tu, const double* tv, double* yu, 
       double sN = mN * ((tu[m.id(i, j + 1)] - tu[k]) / dy + (tv[m.id(i, j + 1)] - tv[m.id(i - 1, j + 1)]) / dx) * dx;
       double sS = mS * ((tu[k] - tu[m.id(i, j - 1)]) / dy + (tv[m.id(i, j)] - tv[m.id(i - 1, j)]) / dx) * dx;
       val = val - (sN - sS);
+      if (c.r_al) {
+        // :584-595: -(r_E div(i,j) - r_W div(i-1,j)) dy, div of the operand
+        double dE = (tu[m.id(i + 1, j)] - tu[k]) / dx + (tv[m.id(i, j + 1)] - tv[k]) / dy;
+        double dW = (tu[k] - tu[m.id(i - 1, j)]) / dx + (tv[m.id(i - 1, j + 1)] - tv[m.id(i - 1, j)]) / dy;
+        val = val - (c.r_al[k] * dE - c.r_al[m.id(i - 1, j)] * dW) * dy;
+      }
       yu[k] = val;
     }
   for (int j = 1; j <= v_ny; ++j)
@@ -668,6 +678,12 @@ void mom_apply(const MomCtx& c, const double* tu, const double* tv, double* yu, 
       double sE = mE * ((tv[m.id(i + 1, j)] - tv[k]) / dx + (tu[m.id(i + 1, j)] - tu[m.id(i + 1, j - 1)]) / dy) * dy;
       double sW = mW * ((tv[k] - tv[m.id(i - 1, j)]) / dx + (tu[m.id(i, j)] - tu[m.id(i, j - 1)]) / dy) * dy;
       val = val - (sE - sW);
+      if (c.r_al) {
+        // :711-721: -(r_N div(i,j) - r_S div(i,j-1)) dx
+        double dN = (tu[m.id(i + 1, j)] - tu[k]) / dx + (tv[m.id(i, j + 1)] - tv[k]) / dy;
+        double dS = (tu[m.id(i + 1, j - 1)] - tu[m.id(i, j - 1)]) / dx + (tv[k] - tv[m.id(i, j - 1)]) / dy;
+        val = val - (c.r_al[k] * dN - c.r_al[m.id(i, j - 1)] * dS) * dx;
+      }
       yv[k] = val;
     }
 }
@@ -706,7 +722,9 @@ void mom_diag(const MomCtx& c, double* du, double* dv) {
         u_conv_fluxes(c, i, j, FE, FW, FN, FS);
         conv_diag = rho * (std::max(FE, 0.0) + std::max(-FW, 0.0) + std::max(FN, 0.0) + std::max(-FS, 0.0));
       }
-      double aP = Du + dwy + conv_diag + 0.0 + 0.0 + cW + cE + cSv + cNv + 0.0 + 0.0;
+      double alW = 0.0, alE = 0.0;
+      if (c.r_al) { alW = c.r_al[m.id(i - 1, j)] * (dy / dx); alE = c.r_al[k] * (dy / dx); }
+      double aP = Du + dwy + conv_diag + 0.0 + 0.0 + cW + cE + cSv + cNv + alW + alE;
       if (aP <= 1.0e-15) aP = 1.0;
       du[k] = aP;
     }
@@ -739,7 +757,9 @@ void mom_diag(const MomCtx& c, double* du, double* dv) {
         v_conv_fluxes(c, i, j, FE, FW, FN, FS);
         conv_diag = rho * (std::max(FE, 0.0) + std::max(-FW, 0.0) + std::max(FN, 0.0) + std::max(-FS, 0.0));
       }
-      double aP = Dv + dwx + conv_diag + 0.0 + 0.0 + cWv + cEv + cS + cN + 0.0 + 0.0;
+      double alS = 0.0, alN = 0.0;
+      if (c.r_al) { alS = c.r_al[m.id(i, j - 1)] * (dx / dy); alN = c.r_al[k] * (dx / dy); }
+      double aP = Dv + dwx + conv_diag + 0.0 + 0.0 + cWv + cEv + cS + cN + alS + alN;
       if (aP <= 1.0e-15) aP = 1.0;
       dv[k] = aP;
     }
@@ -777,6 +797,7 @@ void mom_rhs(const MomCtx& c, const double* mu_node, const double* fx, const dou
       }
       val = val + rho * prm->gx * dvol;
       val = val + fx[k] * dvol;
+      if (c.p_al) val = val - (c.p_al[k] - c.p_al[m.id(i - 1, j)]) * dy;  // :908-913
       if (j == ny && prm->bc_type[T] == COVOF_BC_DIRICHLET) {
         double mN = mu_node[m.id(i, j + 1)];
         if (ny >= 2) val = val + mN * ((8.0 / 3.0) * prm->bc_u[T] / dy) * dx;
@@ -813,6 +834,7 @@ void mom_rhs(const MomCtx& c, const double* mu_node, const double* fx, const dou
       }
       val = val + rho * prm->gy * dvol;
       val = val + fy[k] * dvol;
+      if (c.p_al) val = val - (c.p_al[k] - c.p_al[m.id(i, j - 1)]) * dx;  // :1053-1058
       if (i == 1 && prm->bc_type[L] == COVOF_BC_DIRICHLET) {
         double mW = mu_node[m.id(i, j)];
         val = val + mW * (2.0 * prm->bc_v[L] / dx) * dy;
@@ -1080,6 +1102,129 @@ int predictor(const covof_params* prm, double dt, double* u, double* v, const do
   }
   K.pk.unpack(x.data(), u, v);
   velocity_bc(prm, c.m, u, v, false);
+  return st;
+}
+
+// src/module_navier_stokes.f90:1106-1218 ns_compute_adaptative_r_al
+// (incompressible): r_aal = r_al everywhere, or with adaptative_al the
+// per-cell k_aal * max(unsteady, inertial, gravity, pressure, viscous,
+// capillary scales).
+void al_penalty(const covof_params* prm, const Mesh& m, double dt, const double* u, const double* v,
+                const double* p, const double* rho, const double* mu, int has_nm1, double* r) {
+  const int nx = m.nx, ny = m.ny;
+  size_t g = (size_t)(nx + 2) * (ny + 2);
+  if (!prm->adaptative_al) {
+    for (size_t k = 0; k < g; ++k) r[k] = prm->r_al;
+    return;
+  }
+  const double lx = nx * m.dx, ly = ny * m.dy;
+  double L0;
+  if (prm->l0_ref > 0.0) L0 = prm->l0_ref;
+  else if (prm->enable_two_phase && prm->ic_radius > 0.0) L0 = 2.0 * prm->ic_radius;
+  else L0 = std::min(lx, ly);
+  const double t0 = prm->t0_ref > 0.0 ? prm->t0_ref : dt;
+  const double g_norm = std::sqrt(prm->gx * prm->gx + prm->gy * prm->gy);
+  const double sigma_val = prm->enable_two_phase ? prm->sigma : 0.0;
+  const double alpha_time = (prm->time_scheme == COVOF_TIME_GEAR && has_nm1) ? 1.5 : 1.0;
+  double u_max = 0.0, p_max = 0.0;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      double uc = 0.5 * (u[m.id(i, j)] + u[m.id(i + 1, j)]);
+      double vc = 0.5 * (v[m.id(i, j)] + v[m.id(i, j + 1)]);
+      double spd = std::sqrt(uc * uc + vc * vc);
+      if (spd > u_max) u_max = spd;
+      double pa = std::fabs(p[m.id(i, j)]);
+      if (pa > p_max) p_max = pa;
+    }
+  double u0 = prm->u0_ref > 0.0 ? prm->u0_ref : u_max;
+  if (u0 < 1.0e-12) {
+    double u_grav = g_norm > 0.0 ? std::sqrt(g_norm * L0) : 0.0;
+    double mu_max = std::max(prm->mu1, prm->mu2);
+    double u_cap = (sigma_val > 0.0 && mu_max > 1.0e-30) ? sigma_val / mu_max : 0.0;
+    u0 = std::max(std::max(std::max(u_grav, u_cap), L0 / std::max(t0, 1.0e-12)), 1.0e-3);
+  }
+  const double p0 = prm->p0_ref > 0.0 ? prm->p0_ref : p_max;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t k = m.id(i, j);
+      double rM = rho[k], mM = mu[k];
+      double t_uns = alpha_time * rM * (L0 * L0) / std::max(t0, 1.0e-30);
+      double t_in = rM * u0 * L0;
+      double t_gr = rM * (L0 * L0 / u0) * g_norm;
+      double t_pr = (p0 * L0) / u0;
+      double t_vi = mM;
+      double t_ca = sigma_val / u0;
+      double mx = std::max(std::max(std::max(t_uns, t_in), std::max(t_gr, t_pr)),
+                           std::max(std::max(t_vi, 0.0), t_ca));
+      double rl = prm->k_aal * mx;
+      if (rl <= 1.0e-15) rl = prm->r_al;
+      r[k] = rl;
+    }
+}
+
+// max over interior cells of |div u| (src/module_simulation.f90:590-604)
+double max_div(const Mesh& m, const double* u, const double* v) {
+  double mx = 0.0;
+  for (int j = 1; j <= m.ny; ++j)
+    for (int i = 1; i <= m.nx; ++i) {
+      double d = std::fabs((u[m.id(i + 1, j)] - u[m.id(i, j)]) / m.dx + (v[m.id(i, j + 1)] - v[m.id(i, j)]) / m.dy);
+      if (d > mx) mx = d;
+    }
+  return mx;
+}
+
+// src/module_simulation.f90:553-607 for solver_type AUGMENTED_LAGRANGIAN /
+// AAL: penalty field, preconditioner diagonal once, then Uzawa iterations of
+// rhs (with -grad p), pack, Krylov solve (operator linearised about the
+// current u), unpack + velocity BC, p -= r div u (:1223-1263), with the
+// max |div u| exit test when uzawa_iter > 1 and uzawa_tol > 0.
+int al_step(const covof_params* prm, double dt, double* u, double* v, double* p, const double* rho,
+            const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+            const double* fx, const double* fy, const Hist& hist, int* iters, int* uzawa_done) {
+  const Mesh m = mesh_of(prm);
+  const size_t g = (size_t)(prm->nx + 2) * (prm->ny + 2);
+  std::vector<double> r(g, 0.0);
+  al_penalty(prm, m, dt, u, v, p, rho, mu, hist.has_nm1, r.data());
+  std::vector<double> un(u, u + g), vn(v, v + g);
+  MomCtx c = make_ctx(prm, dt, un.data(), vn.data(), rho_u, rho_v, mu, mu_node, hist);
+  c.r_al = r.data();
+  c.p_al = p;
+  Krylov K(c);
+  std::vector<double> du(g, 1.0), dv(g, 1.0), ru(g, 0.0), rv(g, 0.0);
+  mom_diag(c, du.data(), dv.data());
+  K.diag.resize(K.pk.n());
+  K.pk.pack(du.data(), dv.data(), K.diag.data());
+  const int umax = prm->uzawa_iter > 0 ? prm->uzawa_iter : 1;
+  int total = 0, st = COVOF_OK, m_done = 0;
+  for (int mi = 1; mi <= umax; ++mi) {
+    m_done = mi;
+    mom_rhs(c, mu_node, fx, fy, hist.u_old, hist.v_old, ru.data(), rv.data());
+    std::vector<double> rhs(K.pk.n()), x(K.pk.n());
+    K.pk.pack(ru.data(), rv.data(), rhs.data());
+    K.pk.pack(u, v, x.data());
+    // the operator's fields_old is the current field
+    std::memcpy(un.data(), u, g * sizeof(double));
+    std::memcpy(vn.data(), v, g * sizeof(double));
+    int it = 0;
+    switch (prm->linear_solver) {
+      case COVOF_LINEAR_BICGSTAB: st = solve_bicgstab(K, rhs.data(), x.data(), &it); break;
+      case COVOF_LINEAR_CG: st = solve_cg(K, rhs.data(), x.data(), &it); break;
+      default: st = solve_bicgstab2(K, rhs.data(), x.data(), &it); break;
+    }
+    total += it;
+    if (st == COVOF_NAN) break;
+    K.pk.unpack(x.data(), u, v);
+    velocity_bc(prm, m, u, v, false);
+    for (int j = 1; j <= m.ny; ++j)
+      for (int i = 1; i <= m.nx; ++i) {
+        size_t k = m.id(i, j);
+        double dv_ = (u[m.id(i + 1, j)] - u[k]) / m.dx + (v[m.id(i, j + 1)] - v[k]) / m.dy;
+        p[k] = p[k] - r[k] * dv_;
+      }
+    if (umax > 1 && prm->uzawa_tol > 0.0 && max_div(m, u, v) <= prm->uzawa_tol) break;
+  }
+  if (iters) *iters = total;
+  if (uzawa_done) *uzawa_done = m_done;
   return st;
 }
 
@@ -1779,6 +1924,20 @@ int orc_predictor(const covof_params* prm, double dt, double* u, double* v, cons
                  hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1), &it);
   if (iters) *iters = it;
   return st;
+}
+
+// one augmented-Lagrangian step (solver_type AUGMENTED_LAGRANGIAN / AAL)
+int orc_al_step(const covof_params* prm, double dt, double* u, double* v, double* p, const double* rho,
+                const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                const double* fx_sigma, const double* fy_sigma, const double* u_old, const double* v_old,
+                const double* u_nm1, const double* v_nm1, int has_nm1, int* iters, int* uzawa_done) {
+  int st = check_params(prm, false);
+  if (st) return st;
+  if ((st = check_mom(prm, u_old, u_nm1, has_nm1))) return st;
+  if (prm->solver_type != COVOF_SOLVER_AUGMENTED_LAGRANGIAN && prm->solver_type != COVOF_SOLVER_AAL)
+    return COVOF_INVALID;
+  return al_step(prm, dt, u, v, p, rho, rho_u, rho_v, mu, mu_node, fx_sigma, fy_sigma,
+                 hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1), iters, uzawa_done);
 }
 
 // src/module_simulation.f90:2424-2666 sim_solve_standard_projection

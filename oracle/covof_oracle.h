@@ -90,6 +90,14 @@ int orc_sp_step(const covof_params* prm, double dt, double* u, double* v, double
                 const double* u_old, const double* v_old, const double* u_nm1, const double* v_nm1,
                 int has_nm1, int* iters_u, int* iters_p, double* relres);
 
+/* one augmented-Lagrangian step (solver_type AUGMENTED_LAGRANGIAN / AAL):
+ * Uzawa iterations of the penalised momentum solve and p -= r div u;
+ * iters = Krylov iterations summed, uzawa_done = Uzawa iterations run */
+int orc_al_step(const covof_params* prm, double dt, double* u, double* v, double* p, const double* rho,
+                const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                const double* fx_sigma, const double* fy_sigma, const double* u_old, const double* v_old,
+                const double* u_nm1, const double* v_nm1, int has_nm1, int* iters, int* uzawa_done);
+
 /* geometric VOF */
 int orc_reconstruct(const covof_params* prm, const double* C, double* seg);
 int orc_wy_step(const covof_params* prm, double dt, int x_first, const double* u,

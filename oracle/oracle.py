@@ -54,6 +54,7 @@ def lib():
             "orc_vof_advect": (i, [v, d, i] + [v] * 13),
             "orc_svof_smooth": (i, [v, v, v]),
             "orc_vof_transport": (i, [v, d, i, v, v, v]),
+            "orc_al_step": (i, [v, d] + [v] * 14 + [i, v, v]),
             "orc_diffusion_smooth": (i, [v, v, v]),
         }
         for name, (res, args) in sig.items():
@@ -178,6 +179,15 @@ def sp_step(prm, dt, f, has_nm1=0):
     return iu.value, ip.value, rr.value, st
 
 
+def al_step(prm, dt, f, has_nm1=0):
+    """One augmented-Lagrangian step (Uzawa); returns (iters, uzawa_done, status)."""
+    it, ud = C.c_int(), C.c_int()
+    st = lib().orc_al_step(_params(prm), dt, _p(f.u), _p(f.v), _p(f.p), _p(f.rho), _p(f.rho_u), _p(f.rho_v),
+                           _p(f.mu), _p(f.mu_node), _p(f.fx_sigma), _p(f.fy_sigma), _p(f.u_old), _p(f.v_old),
+                           _p(f.u_nm1), _p(f.v_nm1), int(has_nm1), C.byref(it), C.byref(ud))
+    return it.value, ud.value, st
+
+
 def reconstruct(prm, Cf):
     seg = np.zeros(Cf.shape + (3,))
     st = lib().orc_reconstruct(_params(prm), _p(Cf), seg.ctypes.data)
@@ -258,4 +268,7 @@ def time_step(prm, dt, step_count, f):
     if prm.enable_two_phase:
         vof_advect(prm, dt, step_count, f)
         apply_velocity_bc(prm, f.u, f.v, False)
+    if prm.solver_type in (1, 4):  # AUGMENTED_LAGRANGIAN / AAL
+        it, ud, st = al_step(prm, dt, f, has_nm1)
+        return it, 0, 0.0, st
     return sp_step(prm, dt, f, has_nm1)
