@@ -71,12 +71,15 @@ def candidates(p: Params, sm_count: int) -> list[tuple[dict, dict]]:
     if p.p_inner_kind == capi.INNER_MG:
         # the over-correction weight matters most (aggregation coarse
         # operators are about twice too stiff), then the smoothing sweeps
+        # (a coarse solve that leaves less error behind also counts: the
+        # coarsest level's sweeps)
         mg_blocks = sorted({sm_count, max(1, sm_count // 2)}, reverse=True)
         for nb in mg_blocks:
-            for nu in (2, 3, 1):
-                for cw in (1.9, 2.0, 1.8):
-                    out.append(({"p_threads": 0, "p_blocks": nb, "p_inner_form": 0},
-                                {"p_mg_nu": nu, "p_mg_cw": cw}))
+            for nuc in (64, 32, 128):
+                for nu in (3, 2, 4):
+                    for cw in (2.0, 1.9, 1.8):
+                        out.append(({"p_threads": 0, "p_blocks": nb, "p_inner_form": 0},
+                                    {"p_mg_nu": nu, "p_mg_cw": cw, "p_mg_nuc": nuc}))
         return out
     shapes = []
     if p.p_inner_kind == capi.INNER_CHEBYSHEV:
@@ -171,7 +174,7 @@ def tuned_fields(p: Params) -> tuple[str, ...]:
     if p.p_precision == capi.PREC_FP64:
         return ()
     if p.p_inner_kind == capi.INNER_MG:
-        return ("p_mg_nu", "p_mg_cw")
+        return ("p_mg_nu", "p_mg_cw", "p_mg_nuc")
     return ("p_inner_max_iter", "p_cheb_lo")
 
 

@@ -61,6 +61,7 @@ class Params(C.Structure):
         ("solver_type", C.c_int), ("r_al", C.c_double), ("adaptative_al", C.c_int), ("k_aal", C.c_double),
         ("l0_ref", C.c_double), ("t0_ref", C.c_double), ("u0_ref", C.c_double), ("p0_ref", C.c_double),
         ("ic_radius", C.c_double), ("uzawa_iter", C.c_int), ("uzawa_tol", C.c_double),
+        ("p_mg_nuc", C.c_int),
     ]
 
     def copy(self) -> "Params":

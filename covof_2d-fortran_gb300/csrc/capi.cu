@@ -111,7 +111,9 @@ int ensure_poisson(covof_handle* h) {
   H.omega = 0.8f;
   H.nu = h->prm.p_mg_nu < 1 ? 1 : (h->prm.p_mg_nu > 8 ? 8 : h->prm.p_mg_nu);
   H.cw = (float)(h->prm.p_mg_cw > 0.0 && h->prm.p_mg_cw <= 4.0 ? h->prm.p_mg_cw : 1.0);
-  H.nuc = 8;
+  // an even count leaves the coarsest correction in its first buffer
+  const int nuc = h->prm.p_mg_nuc > 0 ? (h->prm.p_mg_nuc > 1024 ? 1024 : h->prm.p_mg_nuc) : 8;
+  H.nuc = (nuc + 1) & ~1;
   if (pool > 0) CS(dalloc(&H.pool, (size_t)pool));
   h->have_poisson = true;
   return COVOF_OK;
@@ -1121,8 +1123,8 @@ void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly)
   p->recon = COVOF_RECON_PLIC;
   p->p_inner_kind = COVOF_INNER_MG;
   p->p_cheb_lo = 1.0e-3;
-  p->p_mg_nu = 2;
-  p->p_mg_cw = 1.9;
+  p->p_mg_nu = 3;
+  p->p_mg_cw = 2.0;
   p->p_mg_tail = 2048;
   p->time_scheme = COVOF_TIME_EULER;
   p->convective_linearization = COVOF_CONV_LIN_PICARD;
@@ -1140,6 +1142,7 @@ void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly)
   p->ic_radius = 0.25;
   p->uzawa_iter = 1;
   p->uzawa_tol = 1.0e-12;
+  p->p_mg_nuc = 64;
 }
 
 int covof_abi_version(void) { return COVOF_ABI_VERSION; }

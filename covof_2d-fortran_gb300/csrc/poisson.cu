@@ -1331,12 +1331,13 @@ struct MgInner {
     if constexpr (S) return *p;
     else return __ldcg(p);
   }
-  // cells (i, j) of an ni x nj range, over the team or over block 0 alone
-  template <bool S, class F>
+  // cells (i, j) of an ni x nj range, over the team, over block 0 alone, or
+  // over block 0's first warp (W)
+  template <bool S, bool W = false, class F>
   __device__ __forceinline__ void cells(int ni, int nj, F f) const {
     const int n = ni * nj;
-    const int t0 = S ? (int)threadIdx.x : tm.rank * (int)blockDim.x + (int)threadIdx.x;
-    const int st = S ? (int)blockDim.x : tm.size * (int)blockDim.x;
+    const int t0 = (S || W) ? (int)threadIdx.x : tm.rank * (int)blockDim.x + (int)threadIdx.x;
+    const int st = W ? 32 : (S ? (int)blockDim.x : tm.size * (int)blockDim.x);
     for (int c = t0; c < n; c += st) {
       const int j = c / ni, i = c - j * ni;
       f(i + 1, j + 1);
@@ -1352,14 +1353,14 @@ struct MgInner {
     return v;
   }
   // one damped Jacobi sweep from buffer cur into the other (first: x = 0)
-  template <bool S>
+  template <bool S, bool W = false>
   __device__ void sweep(int l, bool first, int cur) const {
     const MgLv L = lv(l, S);
     const float* xs = cur ? L.xb : L.xa;
     float* xd = cur ? L.xa : L.xb;
     const float w = H.omega;
     const int pin = l == 0 ? pk : -1;
-    cells<S>(L.nx, L.ny, [&](int i, int j) {
+    cells<S, W>(L.nx, L.ny, [&](int i, int j) {
       const int k = L.id(i, j);
       const float d = L.dg[k];
       float v;
@@ -1468,9 +1469,20 @@ struct MgInner {
       restrict_<true>(l, nu & 1);
       __syncthreads();
     }
-    for (int s = 0; s < H.nuc; ++s) {
-      if (s > 0) __syncthreads();
-      sweep<true>(L - 1, s == 0, s & 1);
+    // the coarsest level: a small one runs in the first warp alone, so its
+    // many sweeps synchronise with __syncwarp instead of block barriers
+    if ((long long)H.lv[L - 1].nx * H.lv[L - 1].ny <= kMgWarpCoarse) {
+      if (threadIdx.x < 32) {
+        for (int s = 0; s < H.nuc; ++s) {
+          if (s > 0) __syncwarp();
+          sweep<true, true>(L - 1, s == 0, s & 1);
+        }
+      }
+    } else {
+      for (int s = 0; s < H.nuc; ++s) {
+        if (s > 0) __syncthreads();
+        sweep<true>(L - 1, s == 0, s & 1);
+      }
     }
     for (int l = L - 2; l >= t; --l) {
       __syncthreads();

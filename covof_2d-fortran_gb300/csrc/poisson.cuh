@@ -18,6 +18,7 @@ struct PcgResult {
 // right-hand side, west / south face coefficients, diagonal, scratch.
 constexpr int kMgMaxLevels = 16;
 constexpr long long kMgTailSmem = 160 * 1024;  // cap on the shared-memory tail
+constexpr long long kMgWarpCoarse = 256;        // coarsest levels this small run in one warp
 struct MgLevel {
   int nx, ny;
   long long off;

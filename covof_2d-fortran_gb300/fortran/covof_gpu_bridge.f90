@@ -68,6 +68,7 @@ module covof_gpu_bridge
      real(c_double) :: k_aal, l0_ref, t0_ref, u0_ref, p0_ref, ic_radius
      integer(c_int) :: uzawa_iter
      real(c_double) :: uzawa_tol
+     integer(c_int) :: p_mg_nuc
   end type covof_params_t
 
   integer(c_int), parameter :: COVOF_OK = 0, COVOF_MAXITER = 1, COVOF_BREAKDOWN = 2

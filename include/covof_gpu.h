@@ -164,6 +164,7 @@ typedef struct covof_params {
   double ic_radius;      /* two-phase length scale 2 ic_radius when l0_ref = 0 (0.25) */
   int uzawa_iter;        /* Uzawa iterations per step (1) */
   double uzawa_tol;      /* stop when max |div u| <= uzawa_tol (1e-12; with uzawa_iter > 1) */
+  int p_mg_nuc;          /* COVOF_INNER_MG: Jacobi sweeps on the coarsest level (0: 8; default 64) */
 } covof_params;
 enum { COVOF_INNER_CHEBYSHEV = 0, COVOF_INNER_CG = 1, COVOF_INNER_CHEBYSHEV_STREAM = 2, COVOF_INNER_MG = 3 };
 

@@ -27,10 +27,11 @@ def test_candidates_cover_shapes(pkg, at):
     assert at.tuned_fields(p) == ("p_inner_max_iter", "p_cheb_lo")
     p.p_inner_kind = pkg.capi.INNER_MG
     cg = at.candidates(p, 152)
-    assert {o["p_mg_nu"] for _, o in cg} == {1, 2, 3}
+    assert {o["p_mg_nu"] for _, o in cg} == {2, 3, 4}
     assert {o["p_mg_cw"] for _, o in cg} == {1.8, 1.9, 2.0}
     assert {d["p_blocks"] for d, _ in cg} == {152, 76}
-    assert at.tuned_fields(p) == ("p_mg_nu", "p_mg_cw")
+    assert {o["p_mg_nuc"] for _, o in cg} == {32, 64, 128}
+    assert at.tuned_fields(p) == ("p_mg_nu", "p_mg_cw", "p_mg_nuc")
 
 
 def test_cache_round_trip(pkg, at, tmp_path):
