@@ -9,7 +9,11 @@
 !     this%fields, dt, total_iters) instead of this%solve_standard_projection.
 !   * advect_vof_weymouth_yue_gpu(fields, mesh, cfg, dt) has the interface of
 !     advect_vof_weymouth_yue (src/module_interface_vof.f90:1162-1166) and is
-!     called from advect_vof (:802) in its place.
+!     called from advect_vof (:802) in its place; the same subroutine runs the
+!     CIAM or TVD transport when cfg%advection_method names it (:801-808).
+!   * al_step_gpu(mesh, cfg, fields, dt, total_iters) replaces the Uzawa block
+!     of the AUGMENTED_LAGRANGIAN / AAL branch (src/module_simulation.f90:
+!     561-607).
 ! The field arrays are contiguous allocatables dimensioned (0:nx+1, 0:ny+1),
 ! so their first elements are passed by reference with no copy-in.
 !
@@ -18,9 +22,10 @@
 ! carried by the bridge's own step counter, which matches vof_step_count as
 ! long as every WY step goes through this bridge.
 !
-! Scope: one MPI rank, single domain; Euler + Picard; UPWIND or CENTERED
-! convection; DIRICHLET or FREE_SLIP walls; no obstacle; PLIC or ELVIRA.
-! Anything else stops with a message (the GPU path has no CPU fallback).
+! Scope: one MPI rank, single domain; Euler or Gear, Picard or
+! Adams-Bashforth; UPWIND / CENTERED / TVD_SUPERBEE convection; DIRICHLET or
+! FREE_SLIP walls; no obstacle, markers or Newton linearisation.  Anything
+! else stops with a message (the GPU path has no CPU fallback).
 !===============================================================================
 module covof_gpu_bridge
   use, intrinsic :: iso_c_binding
@@ -32,7 +37,7 @@ module covof_gpu_bridge
   implicit none
   private
 
-  public :: sp_step_gpu, advect_vof_weymouth_yue_gpu, covof_gpu_finalize
+  public :: sp_step_gpu, advect_vof_weymouth_yue_gpu, al_step_gpu, covof_gpu_finalize
 
   ! Mirror of covof_params (include/covof_gpu.h); bind(C) gives the C layout.
   type, bind(C) :: covof_params_t
@@ -129,6 +134,17 @@ module covof_gpu_bridge
        real(c_double) :: c(*)
      end function covof_vof_wy_step
 
+     integer(c_int) function covof_al_step(h, dt, u, v, p, rho, rho_u, rho_v, mu, mu_node, fx, fy, &
+                                           u_old, v_old, total_iters, uzawa_done) bind(C, name="covof_al_step")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       real(c_double), value :: dt
+       real(c_double) :: u(*), v(*), p(*)
+       real(c_double), intent(in) :: rho(*), rho_u(*), rho_v(*), mu(*), mu_node(*), fx(*), fy(*)
+       real(c_double), intent(in) :: u_old(*), v_old(*)
+       integer(c_int), intent(out) :: total_iters, uzawa_done
+     end function covof_al_step
+
      type(c_ptr) function covof_strerror(status) bind(C, name="covof_strerror")
        import :: c_int, c_ptr
        integer(c_int), value :: status
@@ -160,8 +176,8 @@ contains
     end if
     if (cfg%convective_linearization == CONV_LIN_NEWTON .or. &
         cfg%obs_enabled .or. cfg%enable_ssp_rk3_momentum .or. cfg%compressible .or. &
-        cfg%enable_svof_smoothing .or. cfg%use_markers .or. cfg%enable_diffusion_smoothing) then
-       write(*, '(A)') "covof_gpu_bridge: option outside the GPU path (no Newton/obstacle/SVOF/markers)"
+        cfg%use_markers .or. cfg%solver_type == SOLVER_MONOLITHIC .or. cfg%solver_type == SOLVER_CAAL) then
+       write(*, '(A)') "covof_gpu_bridge: option outside the GPU path (no Newton/obstacle/markers/monolithic)"
        error stop 1
     end if
     call covof_params_default(p, int(mesh%nx_global, c_int), int(mesh%ny_global, c_int), &
@@ -180,6 +196,39 @@ contains
     p%convective_scheme = cfg%convective_scheme
     p%time_scheme = cfg%time_scheme
     p%convective_linearization = cfg%convective_linearization
+    ! transport and interface smoothing (the smoothing itself stays in the
+    ! Fortran advect_vof; the GPU entry points accept it too)
+    select case (trim(cfg%advection_method))
+    case ("WEYMOUTH_YUE")
+       p%advection_method = 0
+    case ("CIAM")
+       p%advection_method = 1
+    case default
+       p%advection_method = 2
+    end select
+    select case (trim(cfg%tvd_limiter))
+    case ("VAN_LEER")
+       p%tvd_limiter = 1
+    case ("MUSCL")
+       p%tvd_limiter = 2
+    case ("HRIC")
+       p%tvd_limiter = 3
+    case default
+       p%tvd_limiter = 0
+    end select
+    p%enable_svof_smoothing = merge(1_c_int, 0_c_int, cfg%enable_svof_smoothing)
+    p%svof_filter_width = cfg%svof_filter_width
+    p%enable_diffusion_smoothing = merge(1_c_int, 0_c_int, cfg%enable_diffusion_smoothing)
+    p%diffusion_smoothing_steps = cfg%diffusion_smoothing_steps
+    ! coupling (src/module_config.f90:159-168)
+    p%solver_type = cfg%solver_type
+    p%r_al = cfg%r_al
+    p%adaptative_al = merge(1_c_int, 0_c_int, cfg%adaptative_al)
+    p%k_aal = cfg%k_aal
+    p%l0_ref = cfg%l0_ref; p%t0_ref = cfg%t0_ref; p%u0_ref = cfg%u0_ref; p%p0_ref = cfg%p0_ref
+    p%ic_radius = cfg%ic_radius
+    p%uzawa_iter = cfg%uzawa_iter
+    p%uzawa_tol = cfg%uzawa_tol
     ! Poisson: the reference's hard-coded tolerance and cap
     ! (src/module_simulation.f90:2437-2438), Jacobi-PCG on the GPU.
     p%p_tol = 1.0e-7_c_double
@@ -249,6 +298,31 @@ contains
     if (st /= COVOF_OK) call fail("covof_vof_wy_step", st)
     wy_step_count = wy_step_count + 1
   end subroutine advect_vof_weymouth_yue_gpu
+
+  ! Drop-in for the Uzawa block of the AUGMENTED_LAGRANGIAN / AAL branch
+  ! (src/module_simulation.f90:561-607); the caller has already assembled
+  ! nothing -- the GPU step builds the penalty field, the preconditioner
+  ! diagonal, and runs the Uzawa iterations itself.
+  subroutine al_step_gpu(mesh, cfg, fields, dt, total_iters)
+    type(mesh_2d_t), intent(in) :: mesh
+    type(config_t), intent(in) :: cfg
+    type(flow_fields_t), intent(inout) :: fields
+    real(dp), intent(in) :: dt
+    integer, intent(out) :: total_iters
+    integer(c_int) :: st, it, ud
+    call ensure_handle(mesh, cfg)
+    if (cfg%time_scheme == TIME_SCHEME_GEAR .or. cfg%convective_linearization == CONV_LIN_ADAMS_BASHFORTH) then
+       st = covof_state_set(handle, COVOF_FIELD_U_NM1, fields%u_nm1)
+       if (st == COVOF_OK) st = covof_state_set(handle, COVOF_FIELD_V_NM1, fields%v_nm1)
+       if (st == COVOF_OK) st = covof_set_has_nm1(handle, merge(1_c_int, 0_c_int, fields%has_nm1))
+       if (st /= COVOF_OK) call fail("covof_state_set", st)
+    end if
+    st = covof_al_step(handle, real(dt, c_double), fields%u, fields%v, fields%p, fields%rho, &
+                       fields%rho_u, fields%rho_v, fields%mu, fields%mu_node, &
+                       fields%fx_sigma, fields%fy_sigma, fields%u_old, fields%v_old, it, ud)
+    if (st /= COVOF_OK .and. st /= COVOF_MAXITER .and. st /= COVOF_BREAKDOWN) call fail("covof_al_step", st)
+    total_iters = it
+  end subroutine al_step_gpu
 
   subroutine covof_gpu_finalize()
     integer(c_int) :: st
