@@ -299,10 +299,9 @@ contains
     wy_step_count = wy_step_count + 1
   end subroutine advect_vof_weymouth_yue_gpu
 
-  ! Drop-in for the Uzawa block of the AUGMENTED_LAGRANGIAN / AAL branch
-  ! (src/module_simulation.f90:561-607); the caller has already assembled
-  ! nothing -- the GPU step builds the penalty field, the preconditioner
-  ! diagonal, and runs the Uzawa iterations itself.
+  ! Drop-in for the AUGMENTED_LAGRANGIAN / AAL branch of the loop body
+  ! (src/module_simulation.f90:546-607): the GPU step builds the penalty
+  ! field and the preconditioner diagonal and runs the Uzawa iterations.
   subroutine al_step_gpu(mesh, cfg, fields, dt, total_iters)
     type(mesh_2d_t), intent(in) :: mesh
     type(config_t), intent(in) :: cfg
