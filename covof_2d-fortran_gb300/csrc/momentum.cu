@@ -168,7 +168,15 @@ __device__ __forceinline__ LF operator-(const LF& x, const LF& y) { LF r; for (i
 __device__ __forceinline__ LF operator-(double, const LF& y) { LF r; for (int q = 0; q < 9; ++q) r.c[q] = -y.c[q]; return r; }
 __device__ __forceinline__ LF operator*(double x, const LF& y) { LF r; for (int q = 0; q < 9; ++q) r.c[q] = x * y.c[q]; return r; }
 __device__ __forceinline__ LF operator*(const LF& y, double x) { return x * y; }
-__device__ __forceinline__ LF operator/(const LF& y, double x) { LF r; for (int q = 0; q < 9; ++q) r.c[q] = y.c[q] / x; return r; }
+// one FP64 division per form, not nine: the assembled rows feed only the
+// Krylov solves, which already differ from the matrix-free product at
+// round-off (the product itself, XSrc, divides exactly as the reference)
+__device__ __forceinline__ LF operator/(const LF& y, double x) {
+  const double rx = 1.0 / x;
+  LF r;
+  for (int q = 0; q < 9; ++q) r.c[q] = y.c[q] * rx;
+  return r;
+}
 
 struct LFSrc {
   const MomArgs& a;
