@@ -150,6 +150,8 @@ _SIGS = {
     "covof_set_has_nm1": [_VP, C.c_int],
     "covof_svof_smooth": [_VP, _VP, _VP],
     "covof_al_step": [_VP, C.c_double] + [_VP] * 12 + [_IP, _IP],
+    "covof_vtk_write_async": [_VP, C.c_char_p, C.c_char_p, C.c_int],
+    "covof_vtk_wait": [_VP],
     "covof_diffusion_smooth": [_VP, _VP, _VP],
     "covof_get_has_nm1": [_VP, C.POINTER(C.c_int)],
     "covof_batch_set_has_nm1": [_VP, C.c_int],

@@ -1200,6 +1200,7 @@ int covof_create(const covof_params* params, covof_handle** out) {
 
 int covof_destroy(covof_handle* h) {
   if (!h) return COVOF_INVALID;
+  writer_destroy(h);
   if (h->stream) cudaStreamSynchronize(h->stream);
   double** fl[] = {&h->f_u, &h->f_v, &h->f_p, &h->f_rho_u, &h->f_rho_v, &h->f_mu, &h->f_mu_node,
                    &h->f_fx, &h->f_fy, &h->f_u_old, &h->f_v_old, &h->f_u_nm1, &h->f_v_nm1, &h->f_Cs, &h->f_Ct, &h->dscr, &h->al_r,

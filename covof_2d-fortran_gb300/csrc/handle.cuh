@@ -68,6 +68,7 @@ struct covof_handle {
   double* al_r = nullptr;                // augmented Lagrangian penalty field r_aal
   unsigned long long* al_max = nullptr;  // maxima of the penalty scales and of |div u|
   bool al_check = false;                // resident steps test the Uzawa exit on the host
+  void* writer = nullptr;               // snapshot output state (output.cu)
   unsigned int* svof_prog = nullptr;  // SVOF band progress (32 words per band)
   int svof_nb = 0;                    // blocks of the SVOF launch (planned by ensure_vof)
   // caller-field mirrors (host-pointer entry points)
@@ -156,6 +157,7 @@ int mom_pre(covof_handle* h, double dt, double* u, double* v, const double* rho_
 int mom_post(covof_handle* h, const MomArgs& a, double* u, double* v);
 int wy_step_dev(covof_handle* h, double dt, int x_first, const double* u, const double* v, double* C);
 bool needs_history(const covof_params& P);
+void writer_destroy(covof_handle* h);
 bool is_al(const covof_params& P);
 int check_coupling(const covof_params& P);
 int al_enqueue(covof_handle* h, double dt, double* u, double* v, double* p, const double* rho,

@@ -361,6 +361,15 @@ class Solver:
                     "covof_state_field_dev")
         return ptr.value
 
+    def vtk_write_async(self, out_dir: str, case_name: str, step: int) -> int:
+        """Snapshot the resident fields into the reference's .vtr / .pvtr
+        files without waiting; returns the previous snapshot's status."""
+        return self._check(self.lib.covof_vtk_write_async(self.h, str(out_dir).encode(), case_name.encode(),
+                                                          int(step)), "covof_vtk_write_async")
+
+    def vtk_wait(self) -> int:
+        return self._check(self.lib.covof_vtk_wait(self.h), "covof_vtk_wait")
+
     def run_steps(self, dt: float, nsteps: int, graph: bool = True) -> tuple[int, dict]:
         """nsteps time-loop iterations of sim_run (src/module_simulation.f90:492-559)
         on the resident fields; returns (status, run statistics)."""

@@ -412,6 +412,21 @@ typedef struct covof_run_stats {
  * stats->graph is 0. */
 int covof_run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run_stats* stats);
 
+/* ---- snapshot output --------------------------------------------------- */
+
+/* The files of the reference's vtk_write_step for one rank
+ * (src/module_vtk_writer.f90:90-386): <dir>/<case_name>_p0_<step>.vtr and
+ * <dir>/<case_name>_<step>.pvtr (step as 6 digits), ASCII, every value as
+ * Fortran ES16.8, from the resident fields at the point of the call in stream
+ * order.  Asynchronous: a device-side snapshot on the handle's stream, the
+ * host copy on a side stream and the formatting on a host thread; steps
+ * enqueued afterwards do not wait for it.  Returns the status of the previous
+ * snapshot's write.  Temperature is written as 300 (the reference's reset
+ * value; no energy equation here). */
+int covof_vtk_write_async(covof_handle* h, const char* dir, const char* case_name, int step);
+/* Waits for the last snapshot's files; returns their status. */
+int covof_vtk_wait(covof_handle* h);
+
 /* ---- launch shapes (autotuning) --------------------------------------- */
 
 /* Launch shape of the Poisson solver of a handle.  Zero fields leave the
