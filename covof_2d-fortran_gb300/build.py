@@ -28,6 +28,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-std=c++17", "-lineinfo", "-fmad=false",
     "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+    # host arithmetic (the history sums) in program order, no FMA contraction
+    "-Xcompiler", "-ffp-contract=off",
     "-diag-suppress", "177,550",
 ]
 

@@ -152,6 +152,8 @@ _SIGS = {
     "covof_al_step": [_VP, C.c_double] + [_VP] * 12 + [_IP, _IP],
     "covof_vtk_write_async": [_VP, C.c_char_p, C.c_char_p, C.c_int],
     "covof_vtk_wait": [_VP],
+    "covof_history_open": [_VP, C.c_char_p, C.c_char_p],
+    "covof_history_write_async": [_VP, C.c_char_p, C.c_char_p, C.c_int, C.c_double, C.c_double],
     "covof_diffusion_smooth": [_VP, _VP, _VP],
     "covof_get_has_nm1": [_VP, C.POINTER(C.c_int)],
     "covof_batch_set_has_nm1": [_VP, C.c_int],

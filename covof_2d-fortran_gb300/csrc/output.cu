@@ -13,6 +13,13 @@
 // The next snapshot first joins the previous writer thread, which waited for
 // its host copy, so the staging area is reused only after that copy finished;
 // the steps that follow a snapshot never wait for its host copy or its file.
+//
+// covof_history_write_async appends the line of the reference's
+// vtk_write_diagnostics (src/module_vtk_writer.f90:392-470) to
+// <dir>/<case>_history.csv through the same snapshot; its sums run on the
+// host thread in the reference's serial order (host code is built without
+// floating-point contraction), so the line matches the reference's digits.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <filesystem>
@@ -150,6 +157,53 @@ int write_files(const covof_params& P, const double* const f[S_N], const std::st
   return ok2 ? COVOF_OK : COVOF_INVALID;
 }
 
+// src/module_vtk_writer.f90:392-470 for one rank: the serial sums in the
+// reference's order and the CSV record (I0, then ES14.6 values).
+int append_history(const covof_params& P, const double* const f[S_N], const std::string& path, int step,
+                   double time, double dt) {
+  const int nx = P.nx, ny = P.ny, W = nx + 2;
+  auto at = [&](int q, int i, int j) { return f[q][(size_t)j * W + i]; };
+  const double dvol = P.dx * P.dy;
+  const double T = 300.0;  // no energy equation on this path: the reset temperature
+  double vol = 0.0, gvol = 0.0, yint = 0.0, vint = 0.0, mgas = 0.0, pgas = 0.0, ke = 0.0;
+  double umax = 0.0, dmax = 0.0;
+  for (int j = 1; j <= ny; ++j) {
+    const double y_pos = ((double)(j - 1) + 0.5) * P.dy;
+    for (int i = 1; i <= nx; ++i) {
+      const double c = at(S_C, i, j), pr = at(S_P, i, j);
+      const double ib = 1.0 - c;
+      vol = vol + ib * dvol;
+      yint = yint + y_pos * ib * dvol;
+      const double ig = 1.0 - c;
+      const double rg = pr / (287.05 * (T > 1.0 ? T : 1.0));
+      mgas = mgas + ig * rg * dvol;
+      pgas = pgas + ig * pr * dvol;
+      gvol = gvol + ig * dvol;
+      const double uw = at(S_U, i, j), ue = at(S_U, i + 1, j);
+      const double vs = at(S_V, i, j), vn = at(S_V, i, j + 1);
+      const double uc = 0.5 * (uw + ue), vc = 0.5 * (vs + vn);
+      vint = vint + vc * ib * dvol;
+      const double sp2 = uc * uc + vc * vc;
+      const double u2p = 0.5 * (uw * uw + ue * ue), v2p = 0.5 * (vs * vs + vn * vn);
+      ke = ke + 0.5 * at(S_RHO, i, j) * (u2p + v2p) * dvol;
+      const double sp = std::sqrt(sp2);
+      if (sp > umax) umax = sp;
+      const double dv = std::fabs((ue - uw) / P.dx + (vn - vs) / P.dy);
+      if (dv > dmax) dmax = dv;
+    }
+  }
+  const double yc = vol > 1.0e-12 ? yint / vol : 0.0, vcm = vol > 1.0e-12 ? vint / vol : 0.0;
+  const double rho_g = gvol > 1.0e-12 ? mgas / gvol : 0.0, p_g = gvol > 1.0e-12 ? pgas / gvol : 0.0;
+  char line[512];
+  std::snprintf(line, sizeof(line), "%d,%14.6E,%14.6E,%14.6E,%14.6E,%14.6E,%14.6E,%14.6E,%14.6E,%14.6E,%14.6E\n",
+                step, time, dt, yc, vcm, vol, ke, umax, dmax, rho_g, p_g);
+  FILE* fp = std::fopen(path.c_str(), "ab");
+  if (!fp) return COVOF_INVALID;
+  const bool ok = std::fputs(line, fp) >= 0;
+  std::fclose(fp);
+  return ok ? COVOF_OK : COVOF_INVALID;
+}
+
 Writer* writer_of(covof_handle* h) { return static_cast<Writer*>(h->writer); }
 
 }  // namespace
@@ -184,8 +238,14 @@ int covof_vtk_wait(covof_handle* h) {
   return w->status;
 }
 
-int covof_vtk_write_async(covof_handle* h, const char* dir, const char* case_name, int step) {
-  if (!h || !dir || !case_name || step < 0) return COVOF_INVALID;
+}  // extern "C"
+
+namespace {
+
+// Steps (1) and (2) of a snapshot, then `job` on the writer thread with the
+// host copies of the fields.  Returns the previous job's status.
+template <class Job>
+int snapshot_async(covof_handle* h, Job job) {
   CS(ensure_fields(h));
   if (!h->writer) {
     Writer* w = new (std::nothrow) Writer();
@@ -201,13 +261,12 @@ int covof_vtk_write_async(covof_handle* h, const char* dir, const char* case_nam
     }
   }
   Writer* w = writer_of(h);
-  // the previous file is written and its staging copies are done
+  // the previous job is done and its staging copies with it
   if (w->th.joinable()) w->th.join();
   const int prev = w->status;
   w->status = COVOF_OK;
   const size_t bytes = h->g * sizeof(double);
-  // (1) snapshot on the handle's stream (after every step enqueued so far);
-  // the staging area's previous host copy has finished (joined above)
+  // (1) snapshot on the handle's stream (after every step enqueued so far)
   const double* src[S_N] = {h->f_C, h->f_Cs, h->f_p, h->f_rho, h->f_mu, h->f_u, h->f_v, h->f_curv};
   for (int q = 0; q < S_N; ++q)
     CK(cudaMemcpyAsync(w->dstage + (size_t)q * h->g, src[q], bytes, cudaMemcpyDeviceToDevice, h->stream));
@@ -216,23 +275,60 @@ int covof_vtk_write_async(covof_handle* h, const char* dir, const char* case_nam
   CK(cudaStreamWaitEvent(w->io, w->snap, 0));
   CK(cudaMemcpyAsync(w->hstage, w->dstage, bytes * S_N, cudaMemcpyDeviceToHost, w->io));
   CK(cudaEventRecord(w->copied, w->io));
-  // (the next snapshot joins this writer, which waited for the host copy,
-  // before its device copies reuse the staging area)
-  // (3) format and write on a host thread
-  const covof_params P = h->prm;
-  const std::string d(dir), n(case_name);
+  // (the next snapshot joins this job, which waited for the host copy, before
+  // its device copies reuse the staging area)
+  // (3) the job on a host thread
   double* hs = w->hstage;
   const size_t g = h->g;
   cudaEvent_t copied = w->copied;
-  w->th = std::thread([w, P, d, n, step, hs, g, copied]() {
+  w->th = std::thread([w, hs, g, copied, job]() {
     if (cudaEventSynchronize(copied) != cudaSuccess) { w->status = COVOF_CUDA_ERROR; return; }
-    std::error_code ec;
-    std::filesystem::create_directories(d, ec);  // vtk_init's mkdir -p
     const double* f[S_N];
     for (int q = 0; q < S_N; ++q) f[q] = hs + (size_t)q * g;
-    w->status = write_files(P, f, d, n, step);
+    w->status = job(f);
   });
   return prev;
+}
+
+}  // namespace
+
+extern "C" {
+
+int covof_vtk_write_async(covof_handle* h, const char* dir, const char* case_name, int step) {
+  if (!h || !dir || !case_name || step < 0) return COVOF_INVALID;
+  const covof_params P = h->prm;
+  const std::string d(dir), n(case_name);
+  return snapshot_async(h, [P, d, n, step](const double* const* f) {
+    std::error_code ec;
+    std::filesystem::create_directories(d, ec);  // vtk_init's mkdir -p
+    return write_files(P, f, d, n, step);
+  });
+}
+
+// vtk_init's history file (src/module_vtk_writer.f90:61-70): the directory,
+// then <dir>/<case>_history.csv replaced by its header line.
+int covof_history_open(covof_handle* h, const char* dir, const char* case_name) {
+  if (!h || !dir || !case_name) return COVOF_INVALID;
+  CS(covof_vtk_wait(h));
+  std::error_code ec;
+  std::filesystem::create_directories(dir, ec);
+  const std::string path = std::string(dir) + "/" + case_name + "_history.csv";
+  FILE* fp = std::fopen(path.c_str(), "wb");
+  if (!fp) return COVOF_INVALID;
+  std::fputs("step,time,dt,center_of_mass_y,rise_velocity,bubble_volume,kinetic_energy,max_u,max_div,"
+             "avg_rho_gas,avg_p_gas\n", fp);
+  std::fclose(fp);
+  return COVOF_OK;
+}
+
+int covof_history_write_async(covof_handle* h, const char* dir, const char* case_name, int step, double time,
+                              double dt) {
+  if (!h || !dir || !case_name) return COVOF_INVALID;
+  const covof_params P = h->prm;
+  const std::string path = std::string(dir) + "/" + case_name + "_history.csv";
+  return snapshot_async(h, [P, path, step, time, dt](const double* const* f) {
+    return append_history(P, f, path, step, time, dt);
+  });
 }
 
 }  // extern "C"

@@ -370,6 +370,16 @@ class Solver:
     def vtk_wait(self) -> int:
         return self._check(self.lib.covof_vtk_wait(self.h), "covof_vtk_wait")
 
+    def history_open(self, out_dir: str, case_name: str) -> int:
+        return self._check(self.lib.covof_history_open(self.h, str(out_dir).encode(), case_name.encode()),
+                           "covof_history_open")
+
+    def history_write_async(self, out_dir: str, case_name: str, step: int, time: float, dt: float) -> int:
+        """Append the diagnostics record of the resident fields at this point."""
+        return self._check(self.lib.covof_history_write_async(self.h, str(out_dir).encode(), case_name.encode(),
+                                                              int(step), float(time), float(dt)),
+                           "covof_history_write_async")
+
     def run_steps(self, dt: float, nsteps: int, graph: bool = True) -> tuple[int, dict]:
         """nsteps time-loop iterations of sim_run (src/module_simulation.f90:492-559)
         on the resident fields; returns (status, run statistics)."""

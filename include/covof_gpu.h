@@ -426,6 +426,16 @@ int covof_run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run
 int covof_vtk_write_async(covof_handle* h, const char* dir, const char* case_name, int step);
 /* Waits for the last snapshot's files; returns their status. */
 int covof_vtk_wait(covof_handle* h);
+/* vtk_init's history file (src/module_vtk_writer.f90:61-70): creates dir and
+ * <dir>/<case_name>_history.csv with its header line. */
+int covof_history_open(covof_handle* h, const char* dir, const char* case_name);
+/* Appends the record of vtk_write_diagnostics (src/module_vtk_writer.f90:
+ * 392-470: bubble centroid height, rise velocity, volume, kinetic energy, max
+ * speed, max |div u|, gas density and pressure averages) for the resident
+ * fields at the call, computed on a host thread in the reference's serial
+ * order, like covof_vtk_write_async (which it shares the writer with). */
+int covof_history_write_async(covof_handle* h, const char* dir, const char* case_name, int step, double time,
+                              double dt);
 
 /* ---- launch shapes (autotuning) --------------------------------------- */
 

@@ -72,3 +72,48 @@ def pvtr_text(p, case_name: str, step: int) -> str:
             '    <Piece Extent="%d %d %d %d 0 0" Source="%s_p0_%06d.vtr"/>\n' % (0, p.nx, 0, p.ny, case_name, step),
             '  </PRectilinearGrid>\n', '</VTKFile>\n']
     return "".join(out)
+
+
+HISTORY_HEADER = ("step,time,dt,center_of_mass_y,rise_velocity,bubble_volume,kinetic_energy,max_u,max_div,"
+                  "avg_rho_gas,avg_p_gas\n")
+
+
+def history_line(p, step, time, dt, C, pres, rho, u, v, temperature=300.0) -> str:
+    """vtk_write_diagnostics (src/module_vtk_writer.f90:392-470), one rank:
+    the serial sums in the reference's order, then the I0 / ES14.6 record."""
+    import math
+    nx, ny, dx, dy = p.nx, p.ny, p.dx, p.dy
+    dvol = dx * dy
+    vol = gvol = yint = vint = mgas = pgas = ke = 0.0
+    umax = dmax = 0.0
+    for j in range(1, ny + 1):
+        y_pos = (float(j - 1) + 0.5) * dy
+        for i in range(1, nx + 1):
+            c = float(C[j, i]); pr = float(pres[j, i])
+            ib = 1.0 - c
+            vol = vol + ib * dvol
+            yint = yint + y_pos * ib * dvol
+            ig = 1.0 - c
+            rg = pr / (287.05 * max(1.0, temperature))
+            mgas = mgas + ig * rg * dvol
+            pgas = pgas + ig * pr * dvol
+            gvol = gvol + ig * dvol
+            uw, ue = float(u[j, i]), float(u[j, i + 1])
+            vs, vn = float(v[j, i]), float(v[j + 1, i])
+            uc = 0.5 * (uw + ue); vc = 0.5 * (vs + vn)
+            vint = vint + vc * ib * dvol
+            sp2 = uc * uc + vc * vc
+            u2p = 0.5 * (uw * uw + ue * ue); v2p = 0.5 * (vs * vs + vn * vn)
+            ke = ke + 0.5 * float(rho[j, i]) * (u2p + v2p) * dvol
+            sp = math.sqrt(sp2)
+            if sp > umax:
+                umax = sp
+            dv = abs((ue - uw) / dx + (vn - vs) / dy)
+            if dv > dmax:
+                dmax = dv
+    yc = yint / vol if vol > 1e-12 else 0.0
+    vcm = vint / vol if vol > 1e-12 else 0.0
+    rho_g = mgas / gvol if gvol > 1e-12 else 0.0
+    p_g = pgas / gvol if gvol > 1e-12 else 0.0
+    vals = (time, dt, yc, vcm, vol, ke, umax, dmax, rho_g, p_g)
+    return "%d," % step + ",".join("%14.6E" % x for x in vals) + "\n"

@@ -43,3 +43,25 @@ def test_vtk_creates_directory(gpu_pkg, tmp_path):
         s.vtk_write_async(tmp_path / "a" / "b", "c", 0)
         assert s.vtk_wait() == 0
     assert (tmp_path / "a" / "b" / "c_p0_000000.vtr").exists()
+
+
+def test_history_records(gpu_pkg, orc, tmp_path):
+    from oracle import vtk_writer as vw
+    pkg = gpu_pkg
+    p, C0, dt = pkg.cases.bubble_case(nx=24, ny=40, nsub=4)
+    f = pkg.Fields.allocate(p)
+    f.C[...] = C0
+    orc.apply_vof_bc(p, f.C)
+    orc.prepare_interface(p, f)
+    want = vw.HISTORY_HEADER
+    with pkg.Solver(p) as s:
+        s.state_set(f)
+        s.history_open(tmp_path, "bubble")
+        for k in range(1, 4):
+            s.run_steps(dt, 2, graph=True)
+            g = f.copy()
+            s.state_get(g)
+            s.history_write_async(tmp_path, "bubble", 2 * k, 2 * k * dt, dt)
+            want += vw.history_line(p, 2 * k, 2 * k * dt, dt, g.C, g.p, g.rho, g.u, g.v)
+        assert s.vtk_wait() == 0
+    assert (tmp_path / "bubble_history.csv").read_text() == want
