@@ -19,7 +19,7 @@ STATUS_NAMES = {0: "OK", 1: "MAXITER", 2: "BREAKDOWN", 3: "NAN", 4: "TIMEOUT",
 # codes shared with src/module_constants.f90
 BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC, BC_FREESLIP = 1, 2, 3, 4
 LINEAR_BICGSTAB2, LINEAR_BICGSTAB, LINEAR_CG = 1, 2, 3
-PRECOND_NONE, PRECOND_JACOBI, PRECOND_SSOR, PRECOND_ILU0 = 0, 1, 2, 3
+PRECOND_NONE, PRECOND_JACOBI, PRECOND_SSOR, PRECOND_ILU0, PRECOND_BLOCK_TRIANGULAR = 0, 1, 2, 3, 4
 CONV_UPWIND, CONV_CENTERED, CONV_TVD_SUPERBEE = 1, 2, 3
 TIME_EULER, TIME_GEAR = 1, 2
 CONV_LIN_PICARD, CONV_LIN_AB2, CONV_LIN_NEWTON = 1, 2, 3
@@ -150,6 +150,7 @@ _SIGS = {
     "covof_set_has_nm1": [_VP, C.c_int],
     "covof_svof_smooth": [_VP, _VP, _VP],
     "covof_al_step": [_VP, C.c_double] + [_VP] * 12 + [_IP, _IP],
+    "covof_monolithic_step": [_VP, C.c_double] + [_VP] * 11 + [_IP],
     "covof_vtk_write_async": [_VP, C.c_char_p, C.c_char_p, C.c_int],
     "covof_vtk_wait": [_VP],
     "covof_history_open": [_VP, C.c_char_p, C.c_char_p],

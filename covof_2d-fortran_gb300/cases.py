@@ -132,6 +132,22 @@ def bubble_case(nx: int = 128, ny: int = 256, seed: int = SEED + 0, nsub: int = 
     return p, C, dt
 
 
+def cavity_case(n: int = 32, re: float = 100.0, solver_type: int = capi.SOLVER_MONOLITHIC):
+    """Lid-driven cavity (the reference's tutorial 08 set-up): unit square,
+    one fluid (rho 1, mu 1/Re), no-slip walls and a lid moving at u = 1,
+    coupled solve with BiCGSTAB2 + Jacobi.  Returns (params, dt)."""
+    p = make_params(n, n, 1.0, 1.0)
+    p.bc_u[3] = 1.0
+    p.rho1 = p.rho2 = 1.0
+    p.mu1 = p.mu2 = 1.0 / re
+    p.solver_type = solver_type
+    p.linear_solver = capi.LINEAR_BICGSTAB2
+    p.tol = 1.0e-10
+    p.max_iter = 20000
+    dt = 0.25 * p.dx
+    return p, dt
+
+
 def poisson_inclusions(n: int = 1024, n_incl: int = 200, seed: int = SEED + 1, nsub: int = 4):
     """Standalone variable-density Poisson: returns (params, b, rho_u, rho_v, dt).
     rho = 1000 C + (1 - C) with C the sub-sampled inclusion fraction; face

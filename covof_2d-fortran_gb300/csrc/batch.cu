@@ -390,7 +390,9 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
     if (b->mixed && cases[c].p_inner_kind == COVOF_INNER_CG) return fail(COVOF_UNSUPPORTED);
     if (cases[c].p_precond == COVOF_PRECOND_SSOR) return fail(COVOF_UNSUPPORTED);
     // the batch runs the projection coupling
-    if (is_al(cases[c]) || check_coupling(cases[c]) != COVOF_OK) return fail(COVOF_UNSUPPORTED);
+    if (check_coupling(cases[c]) != COVOF_OK ||
+        (cases[c].solver_type != 0 && cases[c].solver_type != COVOF_SOLVER_STANDARD_PROJECTION))
+      return fail(COVOF_UNSUPPORTED);
     const int s = check_mom_params(cases[c]);
     if (s != COVOF_OK) return fail(s);
   }

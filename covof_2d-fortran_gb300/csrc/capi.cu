@@ -122,10 +122,13 @@ int ensure_poisson(covof_handle* h) {
 int ensure_mom(covof_handle* h) {
   if (h->have_mom) return COVOF_OK;
   const size_t g2 = 2 * h->g;
-  CS(dalloc(&h->mx, g2)); CS(dalloc(&h->mrhs, g2)); CS(dalloc(&h->mdiag, g2));
-  CS(dalloc(&h->mcoef, 9 * g2)); CS(dalloc(&h->midiag, g2));
+  // Krylov vectors: u and v blocks, and the pressure block for MONOLITHIC
+  // (zero-filled, so the pressure block's ghost entries read as zero)
+  const size_t gk = (h->prm.solver_type == COVOF_SOLVER_MONOLITHIC ? 3 : 2) * h->g;
+  CS(dalloc(&h->mx, gk)); CS(dalloc(&h->mrhs, gk)); CS(dalloc(&h->mdiag, gk));
+  CS(dalloc(&h->mcoef, 9 * g2)); CS(dalloc(&h->midiag, gk));
   CS(dalloc(&h->al_r, h->g)); CS(dalloc(&h->al_max, 4));
-  for (int q = 0; q < 7; ++q) CS(dalloc(&h->mv[q], g2));
+  for (int q = 0; q < 7; ++q) CS(dalloc(&h->mv[q], gk));
   h->have_mom = true;
   return COVOF_OK;
 }
@@ -538,6 +541,7 @@ MomArgs mom_args(covof_handle* h, double dt, const double* u_n, const double* v_
   a.ab2_ext = (a.ab2 && h->has_nm1) ? 1 : 0;
   a.u_nm1 = h->f_u_nm1; a.v_nm1 = h->f_v_nm1;
   a.r_al = nullptr; a.p_al = nullptr;  // set by al_enqueue
+  a.mono = 0; a.pm = nullptr;           // set by mono_enqueue
   a.u_n = u_n; a.v_n = v_n; a.rho_u = rho_u; a.rho_v = rho_v; a.mu = mu; a.mu_node = mu_node;
   a.fx = fx; a.fy = fy; a.u_old = u_old; a.v_old = v_old;
   a.x = h->mx; a.rhs = h->mrhs; a.diag = h->mdiag; a.coef = h->mcoef; a.idiag = h->midiag;
@@ -561,6 +565,8 @@ int check_mom_params(const covof_params& P) {
   if (P.linear_solver != COVOF_LINEAR_BICGSTAB && P.linear_solver != COVOF_LINEAR_BICGSTAB2 &&
       P.linear_solver != COVOF_LINEAR_CG)
     return COVOF_UNSUPPORTED;
+  if (P.use_precond && (P.precond == COVOF_PRECOND_SSOR || P.precond == COVOF_PRECOND_BLOCK_TRIANGULAR))
+    return COVOF_UNSUPPORTED;
   if (P.max_iter < 0) return COVOF_INVALID;
   return COVOF_OK;
 }
@@ -571,7 +577,8 @@ int predictor_plan(covof_handle* h) {
   const void* fn = P.linear_solver == COVOF_LINEAR_BICGSTAB ? (const void*)k_bicgstab
                  : P.linear_solver == COVOF_LINEAR_CG ? (const void*)k_cg
                  : (const void*)k_bicgstab2;
-  const long long nseg = (long long)((P.nx + 1 + 31) / 32) * P.ny + (long long)((P.nx + 31) / 32) * (P.ny + 1);
+  long long nseg = (long long)((P.nx + 1 + 31) / 32) * P.ny + (long long)((P.nx + 31) / 32) * (P.ny + 1);
+  if (P.solver_type == COVOF_SOLVER_MONOLITHIC) nseg += (long long)((P.nx + 31) / 32) * P.ny;
   const int nb = coop_blocks(h, fn, kKrylovThreads, (nseg + kKrylovThreads / 32 - 1) / (kKrylovThreads / 32));
   if (nb < 1) return COVOF_CUDA_ERROR;
   h->m_fn = fn;
@@ -618,8 +625,10 @@ bool is_al(const covof_params& P) {
 }
 
 int check_coupling(const covof_params& P) {
-  if (P.solver_type == 0 || P.solver_type == COVOF_SOLVER_STANDARD_PROJECTION || is_al(P)) return COVOF_OK;
-  if (P.solver_type == COVOF_SOLVER_MONOLITHIC || P.solver_type == COVOF_SOLVER_CAAL) return COVOF_UNSUPPORTED;
+  if (P.solver_type == 0 || P.solver_type == COVOF_SOLVER_STANDARD_PROJECTION || is_al(P) ||
+      P.solver_type == COVOF_SOLVER_MONOLITHIC)
+    return COVOF_OK;
+  if (P.solver_type == COVOF_SOLVER_CAAL) return COVOF_UNSUPPORTED;
   return COVOF_INVALID;
 }
 
@@ -707,6 +716,40 @@ int al_enqueue(covof_handle* h, double dt, double* u, double* v, double* p, cons
   if (total_iters) *total_iters = total;
   if (uzawa_done) *uzawa_done = done;
   return status;
+}
+
+// MONOLITHIC coupling, src/module_simulation.f90:552-583: the
+// preconditioner blocks (momentum diagonals, then the Schur diagonal of the
+// pressure block), the right-hand side (momentum without a pressure term,
+// zero continuity block, src/module_navier_stokes.f90:1079-1100), assembly
+// (linearised about the current u), pack (u, v, p), one Krylov solve of the
+// coupled system, unpack (u, v, p) and the velocity boundary conditions.
+// The Krylov result record is left on the device.
+int mono_enqueue(covof_handle* h, double dt, double* u, double* v, double* p, const double* rho_u,
+                 const double* rho_v, const double* mu, const double* mu_node, const double* fx, const double* fy,
+                 const double* u_old, const double* v_old) {
+  const covof_params& P = h->prm;
+  if (!u || !v || !p || !rho_u || !rho_v || !mu || !mu_node || !fx || !fy || !u_old || !v_old)
+    return COVOF_INVALID;
+  if (P.solver_type != COVOF_SOLVER_MONOLITHIC) return COVOF_INVALID;
+  CS(check_mom_params(P));
+  CS(ensure_mom(h));
+  CS(predictor_plan(h));
+  const dim3 blk(32, 8);
+  const dim3 gc = grid2(P.nx, P.ny, blk), gf = grid2(P.nx + 1, P.ny + 1, blk);
+  MomArgs a = mom_args(h, dt, u, v, rho_u, rho_v, mu, mu_node, fx, fy, u_old, v_old);
+  a.mono = 1;
+  a.pm = p;
+  k_mom_diag<<<gf, blk, 0, h->stream>>>(a);
+  k_mono_diag<<<gc, blk, 0, h->stream>>>(a);
+  k_mom_rhs<<<gf, blk, 0, h->stream>>>(a);
+  CK(cudaMemsetAsync(a.rhs + 2 * h->g, 0, h->g * sizeof(double), h->stream));
+  k_mom_assemble<<<gf, blk, 0, h->stream>>>(a);
+  k_mom_pack<<<gf, blk, 0, h->stream>>>(a, u, v);
+  CK(cudaGetLastError());
+  void* args[] = {&a};
+  CS(launch_coop(h, h->m_fn, h->m_nb, kKrylovThreads, args, false));
+  return mom_post(h, a, u, v);
 }
 
 // Predictor on the handle's stream, result record left on the device.
@@ -969,6 +1012,10 @@ int enqueue_step(covof_handle* h, double dt, bool x_first) {
     CS(al_enqueue(h, dt, h->f_u, h->f_v, h->f_p, h->f_rho, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node,
                   h->f_fx, h->f_fy, h->f_u_old, h->f_v_old, h->al_check, nullptr, nullptr));
     // no Poisson solve in this coupling: its record reads COVOF_OK, 0 iterations
+    CK(cudaMemsetAsync(h->d_pres, 0, sizeof(PcgResult), h->stream));
+  } else if (h->prm.solver_type == COVOF_SOLVER_MONOLITHIC) {
+    CS(mono_enqueue(h, dt, h->f_u, h->f_v, h->f_p, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node, h->f_fx,
+                    h->f_fy, h->f_u_old, h->f_v_old));
     CK(cudaMemsetAsync(h->d_pres, 0, sizeof(PcgResult), h->stream));
   } else {
     CS(predictor_enqueue(h, dt, h->f_u, h->f_v, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node, h->f_fx,
@@ -1522,6 +1569,28 @@ int covof_al_step(covof_handle* h, double dt, double* u, double* v, double* p, c
   if (total_iters) *total_iters = it;
   if (uzawa_done) *uzawa_done = ud;
   return st;
+}
+
+// ---- MONOLITHIC step ------------------------------------------------------------
+int covof_monolithic_step(covof_handle* h, double dt, double* u, double* v, double* p, const double* rho_u,
+                          const double* rho_v, const double* mu, const double* mu_node, const double* fx_sigma,
+                          const double* fy_sigma, const double* u_old, const double* v_old, int* iters) {
+  if (!h) return COVOF_INVALID;
+  if (h->prm.solver_type != COVOF_SOLVER_MONOLITHIC) return COVOF_INVALID;
+  CS(ensure_fields(h));
+  const size_t g = h->g;
+  CS(h2d(h, h->f_u, u, g)); CS(h2d(h, h->f_v, v, g)); CS(h2d(h, h->f_p, p, g));
+  CS(h2d(h, h->f_rho_u, rho_u, g)); CS(h2d(h, h->f_rho_v, rho_v, g));
+  CS(h2d(h, h->f_mu, mu, g)); CS(h2d(h, h->f_mu_node, mu_node, g));
+  CS(h2d(h, h->f_fx, fx_sigma, g)); CS(h2d(h, h->f_fy, fy_sigma, g));
+  CS(h2d(h, h->f_u_old, u_old, g)); CS(h2d(h, h->f_v_old, v_old, g));
+  CS(mono_enqueue(h, dt, h->f_u, h->f_v, h->f_p, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node, h->f_fx,
+                  h->f_fy, h->f_u_old, h->f_v_old));
+  CK(cudaMemcpyAsync(h->h_kres, h->d_kres, sizeof(KrylovResult), cudaMemcpyDeviceToHost, h->stream));
+  CS(d2h(h, u, h->f_u, g)); CS(d2h(h, v, h->f_v, g)); CS(d2h(h, p, h->f_p, g));
+  CS(sync(h));
+  if (iters) *iters = h->h_kres->iters;
+  return h->h_kres->status;
 }
 
 // ---- VOF -----------------------------------------------------------------------

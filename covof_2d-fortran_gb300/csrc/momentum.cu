@@ -527,16 +527,44 @@ __global__ void k_mom_assemble(MomArgs a) {
   }
 }
 
+// The pressure block's Jacobi diagonal for MONOLITHIC,
+// src/module_navier_stokes.f90:1541-1590: diag_p = schur_aP, the row sum of
+// B D^-1 B^T from the momentum diagonals (after k_mom_diag), plus 1e-10 dvol
+// in cell (1,1) and 1e-12 dvol elsewhere.  One thread per cell.
+__global__ void k_mono_diag(MomArgs a) {
+  const Dims& D = a.D;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > D.nx || j > D.ny) return;
+  const int g = D.P * (D.ny + 2);
+  const double dx = a.dx, dy = a.dy, dvol = dx * dy;
+  const double* du = a.diag;
+  const double* dv = a.diag + g;
+  double aW = 0.0, aE = 0.0, aS = 0.0, aN = 0.0;
+  if (!(i == 1 && is_wall(a, SL))) aW = __ddiv_rn(dy * dy, fmax(1.0e-30, du[D.id(i, j)]));
+  if (!(i == D.nx && is_wall(a, SR))) aE = __ddiv_rn(dy * dy, fmax(1.0e-30, du[D.id(i + 1, j)]));
+  if (!(j == 1 && is_wall(a, SB))) aS = __ddiv_rn(dx * dx, fmax(1.0e-30, dv[D.id(i, j)]));
+  if (!(j == D.ny && is_wall(a, ST))) aN = __ddiv_rn(dx * dx, fmax(1.0e-30, dv[D.id(i, j + 1)]));
+  const double reg = (i == 1 && j == 1) ? 1.0e-10 * dvol : 1.0e-12 * dvol;
+  const double d = aW + aE + aS + aN + 0.0 + reg;
+  const size_t k = 2 * (size_t)g + D.id(i, j);
+  a.diag[k] = d;
+  a.idiag[k] = (a.precond_on && fabs(d) > 1.0e-15) ? 1.0 / d : 1.0;
+}
+
 // ---------------------------------------------------------------------------
 // Persistent Krylov solvers.  DOF ownership: warp w walks 32-wide row
-// segments of the u block, then of the v block.
+// segments of the u block, then of the v block, then (MONOLITHIC) of the
+// pressure block.
 struct DofWalker {
-  int nsu, nsv, su, stot, gw, nw, lane, g;
-  __device__ DofWalker(const Dims& D, const Team& tm) {
+  int nsu, nsv, nsp, su, suv, stot, gw, nw, lane, g;
+  __device__ DofWalker(const Dims& D, const Team& tm, int mono = 0) {
     nsu = (D.nx + 1 + 31) >> 5;
     nsv = (D.nx + 31) >> 5;
+    nsp = nsv;
     su = nsu * D.ny;
-    stot = su + nsv * (D.ny + 1);
+    suv = su + nsv * (D.ny + 1);
+    stot = suv + (mono ? nsp * D.ny : 0);
     lane = threadIdx.x & 31;
     gw = (tm.rank * (int)blockDim.x + (int)threadIdx.x) >> 5;
     nw = (tm.size * (int)blockDim.x) >> 5;
@@ -548,11 +576,16 @@ struct DofWalker {
       part = 0; j = s / nsu + 1; i = (s - (j - 1) * nsu) * 32 + lane + 1;
       if (i > D.nx + 1) return false;
       k = D.id(i, j);
-    } else {
+    } else if (s < suv) {
       const int t = s - su;
       part = 1; j = t / nsv + 1; i = (t - (j - 1) * nsv) * 32 + lane + 1;
       if (i > D.nx) return false;
       k = g + D.id(i, j);
+    } else {
+      const int t = s - suv;
+      part = 2; j = t / nsp + 1; i = (t - (j - 1) * nsp) * 32 + lane + 1;
+      if (i > D.nx) return false;
+      k = 2 * g + D.id(i, j);
     }
     return true;
   }
@@ -570,10 +603,20 @@ __device__ __forceinline__ double prec(const MomArgs& a, int k, double src) { re
 // assembled rows: 9 FMAs instead of the matrix-free expression (which costs
 // tens of FP64 divisions per DOF; FP64 issue bounds these solves on GB300).
 // Wall rows keep only their centre coefficient and read nothing else.
+// MONOLITHIC: momentum rows add B^T p, (p(i,j) - p(i-1,j)) dy for u and
+// (p(i,j) - p(i,j-1)) dx for v (src/module_navier_stokes.f90:597-602,
+// 723-728); continuity rows are div u dvol (as (du) dy + (dv) dx) plus
+// 1e-10 dvol p(1,1) in cell (1,1) (:730-777).
 __device__ __forceinline__ double pa_at(const MomArgs& a, const DofWalker& W, int part, int i,
                                         int j, int k, const double* x, bool with_prec) {
   const Dims& D = a.D;
   const size_t g2 = 2 * (size_t)W.g;
+  if (part == 2) {
+    const int ku = k - 2 * W.g, kv = ku + W.g;
+    double y = (__ldcg(x + ku + 1) - __ldcg(x + ku)) * a.dy + (__ldcg(x + kv + D.P) - __ldcg(x + kv)) * a.dx;
+    if (i == 1 && j == 1) y = y + (1.0e-10 * (a.dx * a.dy)) * __ldcg(x + k);
+    return with_prec ? y * a.idiag[k] : y;
+  }
   const double* __restrict__ cf = a.coef;
   double y = cf[k] * __ldcg(x + k);
   const bool wall_row = part == 0 ? (i == 1 || i == D.nx + 1)
@@ -597,6 +640,11 @@ __device__ __forceinline__ double pa_at(const MomArgs& a, const DofWalker& W, in
       y = fma(cf[7 * g2 + k], __ldcg(x + kc), y);
       y = fma(cf[8 * g2 + k], __ldcg(x + kc - P), y);
     }
+    if (a.mono) {
+      // the same (i, j) in the pressure block, and its west / south neighbour
+      const int kp = k + (part == 0 ? 2 * W.g : W.g);
+      y = y + (__ldcg(x + kp) - __ldcg(x + kp - (part == 0 ? 1 : P))) * (part == 0 ? a.dy : a.dx);
+    }
   }
   return with_prec ? y * a.idiag[k] : y;
 }
@@ -615,7 +663,7 @@ __device__ void krylov_finish(const MomArgs& a, const Team& tm, int iters, int s
 
 // src/module_linear_solvers.f90:584-730 solve_bicgstab (left Jacobi).
 __device__ void bicgstab_case(const MomArgs& a, const Team& tm, GridReducer& R) {
-  DofWalker W(a.D, tm);
+  DofWalker W(a.D, tm, a.mono);
   double *x = a.x, *bh = a.v0, *r = a.v1, *rt = a.v2, *p = a.v3, *v = a.v4, *s = a.v5, *t = a.v6;
   const double tol = a.tol;
   const int max_iter = a.max_iter;
@@ -706,7 +754,7 @@ __global__ void __launch_bounds__(512) k_bicgstab(MomArgs a) {
 // src/module_linear_solvers.f90:735-838 solve_cg (unpreconditioned operator,
 // separate Jacobi application).
 __device__ void cg_case(const MomArgs& a, const Team& tm, GridReducer& R) {
-  DofWalker W(a.D, tm);
+  DofWalker W(a.D, tm, a.mono);
   double *x = a.x, *r = a.v1, *p = a.v3, *Ap = a.v4;
   const double tol = a.tol;
   const int max_iter = a.max_iter;
@@ -763,7 +811,7 @@ __global__ void __launch_bounds__(512) k_cg(MomArgs a) {
 
 // src/module_linear_solvers.f90:361-579 solve_bicgstab2 (left Jacobi).
 __device__ void bicgstab2_case(const MomArgs& a, const Team& tm, GridReducer& R) {
-  DofWalker W(a.D, tm);
+  DofWalker W(a.D, tm, a.mono);
   double *x = a.x, *rt = a.v0, *r0 = a.v1, *r1 = a.v2, *r2 = a.v3, *u0 = a.v4, *u1 = a.v5, *u2 = a.v6;
   const double tol = a.tol;
   const int max_iter = a.max_iter;
@@ -906,6 +954,7 @@ __global__ void k_mom_unpack(MomArgs a, double* u, double* v) {
   const int g = D.P * (D.ny + 2);
   if (i <= D.nx + 1 && j <= D.ny) u[D.id(i, j)] = a.x[D.id(i, j)];
   if (i <= D.nx && j <= D.ny + 1) v[D.id(i, j)] = a.x[g + D.id(i, j)];
+  if (a.mono && i <= D.nx && j <= D.ny) a.pm[D.id(i, j)] = a.x[2 * (size_t)g + D.id(i, j)];
 }
 // Pack (u, v) DOFs into the Krylov start vector.
 __global__ void k_mom_pack(MomArgs a, const double* u, const double* v) {
@@ -915,6 +964,7 @@ __global__ void k_mom_pack(MomArgs a, const double* u, const double* v) {
   const int g = D.P * (D.ny + 2);
   if (i <= D.nx + 1 && j <= D.ny) a.x[D.id(i, j)] = u[D.id(i, j)];
   if (i <= D.nx && j <= D.ny + 1) a.x[g + D.id(i, j)] = v[D.id(i, j)];
+  if (a.mono && i <= D.nx && j <= D.ny) a.x[2 * (size_t)g + D.id(i, j)] = a.pm[D.id(i, j)];
 }
 
 // Non-homogeneous velocity ghost conditions, src/module_mpi_comm.f90:290-537,

@@ -25,12 +25,19 @@ struct MomArgs {
   // augmented Lagrangian (solver_type AL / AAL): penalty field r_aal and the
   // pressure of the right-hand side's -grad p term; nullptr for projection
   const double* r_al; const double* p_al;
+  // MONOLITHIC coupling (src/module_navier_stokes.f90:281-294, 597-602,
+  // 723-777): the pressure is a third block of Krylov unknowns (cell DOFs
+  // at offset 2g of every Krylov vector); pm: the pressure field packed from
+  // and unpacked into
+  int mono;
+  double* pm;
   // fields_old of the operator (u^n with ghosts) and material properties
   const double* u_n; const double* v_n;
   const double* rho_u; const double* rho_v; const double* mu; const double* mu_node;
   // right-hand side inputs
   const double* fx; const double* fy; const double* u_old; const double* v_old;
-  // Krylov storage: each vector 2*(nx+2)*(ny+2) doubles (u block, v block)
+  // Krylov storage: each vector 2*(nx+2)*(ny+2) doubles (u block, v block),
+  // 3*(nx+2)*(ny+2) with the MONOLITHIC pressure block
   double* x; double* rhs; double* diag;
   double* coef;   // assembled rows: 9 slots x 2*(nx+2)*(ny+2), slot-major (k_mom_assemble)
   double* idiag;  // inverse Jacobi diagonal (1 where no division applies)
@@ -49,6 +56,7 @@ struct BcArgs {
 };
 
 __global__ void k_mom_diag(MomArgs a);
+__global__ void k_mono_diag(MomArgs a);
 
 // Augmented Lagrangian (momentum.cu)
 struct AlArgs {

@@ -14,6 +14,10 @@
 !   * al_step_gpu(mesh, cfg, fields, dt, total_iters) replaces the Uzawa block
 !     of the AUGMENTED_LAGRANGIAN / AAL branch (src/module_simulation.f90:
 !     561-607).
+!   * mono_step_gpu(mesh, cfg, fields, dt, total_iters) replaces the same
+!     block for MONOLITHIC (one pass: assemble_preconditioner_blocks,
+!     assemble_rhs, pack_vector, solve_linear_system, unpack_vector,
+!     src/module_simulation.f90:552-583).
 ! The field arrays are contiguous allocatables dimensioned (0:nx+1, 0:ny+1),
 ! so their first elements are passed by reference with no copy-in.
 !
@@ -37,7 +41,7 @@ module covof_gpu_bridge
   implicit none
   private
 
-  public :: sp_step_gpu, advect_vof_weymouth_yue_gpu, al_step_gpu, covof_gpu_finalize
+  public :: sp_step_gpu, advect_vof_weymouth_yue_gpu, al_step_gpu, mono_step_gpu, covof_gpu_finalize
 
   ! Mirror of covof_params (include/covof_gpu.h); bind(C) gives the C layout.
   type, bind(C) :: covof_params_t
@@ -145,6 +149,17 @@ module covof_gpu_bridge
        integer(c_int), intent(out) :: total_iters, uzawa_done
      end function covof_al_step
 
+     integer(c_int) function covof_monolithic_step(h, dt, u, v, p, rho_u, rho_v, mu, mu_node, fx, fy, &
+                                                   u_old, v_old, iters) bind(C, name="covof_monolithic_step")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       real(c_double), value :: dt
+       real(c_double) :: u(*), v(*), p(*)
+       real(c_double), intent(in) :: rho_u(*), rho_v(*), mu(*), mu_node(*), fx(*), fy(*)
+       real(c_double), intent(in) :: u_old(*), v_old(*)
+       integer(c_int), intent(out) :: iters
+     end function covof_monolithic_step
+
      type(c_ptr) function covof_strerror(status) bind(C, name="covof_strerror")
        import :: c_int, c_ptr
        integer(c_int), value :: status
@@ -176,8 +191,13 @@ contains
     end if
     if (cfg%convective_linearization == CONV_LIN_NEWTON .or. &
         cfg%obs_enabled .or. cfg%enable_ssp_rk3_momentum .or. cfg%compressible .or. &
-        cfg%use_markers .or. cfg%solver_type == SOLVER_MONOLITHIC .or. cfg%solver_type == SOLVER_CAAL) then
-       write(*, '(A)') "covof_gpu_bridge: option outside the GPU path (no Newton/obstacle/markers/monolithic)"
+        cfg%use_markers .or. cfg%solver_type == SOLVER_CAAL) then
+       write(*, '(A)') "covof_gpu_bridge: option outside the GPU path (no Newton/obstacle/markers/CAAL)"
+       error stop 1
+    end if
+    if (cfg%use_precond .and. (cfg%precond_type == PRECOND_SSOR .or. &
+                               cfg%precond_type == PRECOND_BLOCK_TRIANGULAR)) then
+       write(*, '(A)') "covof_gpu_bridge: the GPU Krylov solves take JACOBI / ILU0 / no preconditioner"
        error stop 1
     end if
     call covof_params_default(p, int(mesh%nx_global, c_int), int(mesh%ny_global, c_int), &
@@ -322,6 +342,29 @@ contains
     if (st /= COVOF_OK .and. st /= COVOF_MAXITER .and. st /= COVOF_BREAKDOWN) call fail("covof_al_step", st)
     total_iters = it
   end subroutine al_step_gpu
+
+  ! Drop-in for the MONOLITHIC branch of the loop body (src/module_simulation.f90:
+  ! 552-583, uzawa_max = 1): the coupled (u, v, p) solve on the GPU.
+  subroutine mono_step_gpu(mesh, cfg, fields, dt, total_iters)
+    type(mesh_2d_t), intent(in) :: mesh
+    type(config_t), intent(in) :: cfg
+    type(flow_fields_t), intent(inout) :: fields
+    real(dp), intent(in) :: dt
+    integer, intent(out) :: total_iters
+    integer(c_int) :: st, it
+    call ensure_handle(mesh, cfg)
+    if (cfg%time_scheme == TIME_SCHEME_GEAR .or. cfg%convective_linearization == CONV_LIN_ADAMS_BASHFORTH) then
+       st = covof_state_set(handle, COVOF_FIELD_U_NM1, fields%u_nm1)
+       if (st == COVOF_OK) st = covof_state_set(handle, COVOF_FIELD_V_NM1, fields%v_nm1)
+       if (st == COVOF_OK) st = covof_set_has_nm1(handle, merge(1_c_int, 0_c_int, fields%has_nm1))
+       if (st /= COVOF_OK) call fail("covof_state_set", st)
+    end if
+    st = covof_monolithic_step(handle, real(dt, c_double), fields%u, fields%v, fields%p, &
+                               fields%rho_u, fields%rho_v, fields%mu, fields%mu_node, &
+                               fields%fx_sigma, fields%fy_sigma, fields%u_old, fields%v_old, it)
+    if (st /= COVOF_OK .and. st /= COVOF_MAXITER .and. st /= COVOF_BREAKDOWN) call fail("covof_monolithic_step", st)
+    total_iters = it
+  end subroutine mono_step_gpu
 
   subroutine covof_gpu_finalize()
     integer(c_int) :: st

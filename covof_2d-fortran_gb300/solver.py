@@ -190,6 +190,16 @@ class Solver:
                                     _ptr(f.fy_sigma), _ptr(f.u_old), _ptr(f.v_old), C.byref(it), C.byref(ud))
         return it.value, ud.value, self._check(st, "covof_al_step")
 
+    def monolithic_step(self, dt: float, f: Fields, has_nm1=None):
+        """One MONOLITHIC step on host fields (the coupled u, v, p solve);
+        returns (Krylov iterations, status)."""
+        self._history(f, has_nm1)
+        it = C.c_int()
+        st = self.lib.covof_monolithic_step(self.h, dt, _ptr(f.u), _ptr(f.v), _ptr(f.p), _ptr(f.rho_u),
+                                            _ptr(f.rho_v), _ptr(f.mu), _ptr(f.mu_node), _ptr(f.fx_sigma),
+                                            _ptr(f.fy_sigma), _ptr(f.u_old), _ptr(f.v_old), C.byref(it))
+        return it.value, self._check(st, "covof_monolithic_step")
+
     def predictor(self, dt: float, f: Fields, has_nm1=None):
         self._history(f, has_nm1)
         it = C.c_int()

@@ -50,8 +50,11 @@ enum { COVOF_LINEAR_BICGSTAB2 = 1, COVOF_LINEAR_BICGSTAB = 2, COVOF_LINEAR_CG = 
  * ILU0 is the same diagonal scaling as JACOBI in the reference
  * (src/module_linear_solvers.f90:280-304).  SSOR is accepted for the pressure
  * Poisson only, where it names the reference's symmetric Gauss-Seidel sweep
- * pair (src/module_simulation.f90:2709-2758). */
-enum { COVOF_PRECOND_NONE = 0, COVOF_PRECOND_JACOBI = 1, COVOF_PRECOND_SSOR = 2, COVOF_PRECOND_ILU0 = 3 };
+ * pair (src/module_simulation.f90:2709-2758).  The momentum / coupled
+ * Krylov solves take NONE, JACOBI and ILU0; SSOR and BLOCK_TRIANGULAR there
+ * return COVOF_UNSUPPORTED. */
+enum { COVOF_PRECOND_NONE = 0, COVOF_PRECOND_JACOBI = 1, COVOF_PRECOND_SSOR = 2, COVOF_PRECOND_ILU0 = 3,
+       COVOF_PRECOND_BLOCK_TRIANGULAR = 4 };
 /* Convective schemes: CONV_* in src/module_constants.f90:81-85. */
 enum { COVOF_CONV_UPWIND = 1, COVOF_CONV_CENTERED = 2, COVOF_CONV_TVD_SUPERBEE = 3 };
 /* Momentum time scheme: TIME_SCHEME_* in src/module_constants.f90:132-134
@@ -75,7 +78,10 @@ enum { COVOF_ADVECT_WEYMOUTH_YUE = 0, COVOF_ADVECT_CIAM = 1, COVOF_ADVECT_TVD = 
  * iterations of the momentum solve with the penalty r grad(div u) and the
  * update p -= r div u (src/module_simulation.f90:561-607); r is r_al, or the
  * adaptive field of src/module_navier_stokes.f90:1106-1218 with adaptative_al.
- * MONOLITHIC and the compressible CAAL return COVOF_UNSUPPORTED. */
+ * MONOLITHIC: one Krylov solve of the coupled (u, v, p) system with the
+ * continuity rows (src/module_navier_stokes.f90:730-777) and the Schur
+ * diagonal as the pressure block's Jacobi preconditioner (:1541-1590).  The
+ * compressible CAAL returns COVOF_UNSUPPORTED. */
 enum { COVOF_SOLVER_AUGMENTED_LAGRANGIAN = 1, COVOF_SOLVER_MONOLITHIC = 2, COVOF_SOLVER_STANDARD_PROJECTION = 3,
        COVOF_SOLVER_AAL = 4, COVOF_SOLVER_CAAL = 5 };
 /* Limiter of the TVD transport (cfg%tvd_limiter,
@@ -354,6 +360,20 @@ int covof_al_step(covof_handle* h, double dt, double* u, double* v, double* p, c
                   const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
                   const double* fx_sigma, const double* fy_sigma, const double* u_old, const double* v_old,
                   int* total_iters, int* uzawa_done);
+
+/* One MONOLITHIC step (solver_type MONOLITHIC, src/module_simulation.f90:
+ * 552-583): the preconditioner blocks (momentum diagonals, Schur diagonal
+ * diag_p), the right-hand side without a pressure term, one Krylov solve
+ * (linear_solver) of the coupled system for (u, v, p) from the given fields,
+ * then the velocity boundary conditions.  Replaces the reference's
+ * assemble_preconditioner_blocks + assemble_rhs + pack_vector +
+ * solve_linear_system + unpack_vector sequence (src/module_simulation.f90:
+ * 552-583, src/module_navier_stokes.f90:231-375, 785-1101, 1268-1595).
+ * Gear / AB2 read the handle's history as in covof_predictor.  Returns the
+ * Krylov status; iters: Krylov iterations. */
+int covof_monolithic_step(covof_handle* h, double dt, double* u, double* v, double* p, const double* rho_u,
+                          const double* rho_v, const double* mu, const double* mu_node, const double* fx_sigma,
+                          const double* fy_sigma, const double* u_old, const double* v_old, int* iters);
 
 /* ---- device-resident time stepping ------------------------------------ */
 

@@ -509,8 +509,11 @@ struct MomCtx {
   // the pressure of the right-hand side's gradient term; nullptr for SP
   const double* r_al = nullptr;
   const double* p_al = nullptr;
+  // MONOLITHIC coupling: the pressure is a Krylov unknown (np cell DOFs
+  // after the velocity DOFs), src/module_navier_stokes.f90:281-294
+  bool mono = false;
   int u_nx, v_ny;
-  size_t nu, nv;
+  size_t nu, nv, np = 0;
 };
 
 // src/module_navier_stokes.f90:2388-2416 conv_face_flux (UPWIND / CENTERED /
@@ -579,9 +582,13 @@ inline void v_conv_fluxes(const MomCtx& c, int i, int j, double& FE, double& FW,
 }
 
 // src/module_navier_stokes.f90:380-780 ns_apply_system_matrix (SP; Euler or
-// Gear; PICARD or AB2; UPWIND / CENTERED / TVD_SUPERBEE; no AL/obstacle terms).  tu/tv: the unpacked operand with the
-// homogeneous ghost conditions applied (:458 -> src/module_mpi_comm.f90:290-537).
-void mom_apply(const MomCtx& c, const double* tu, const double* tv, double* yu, double* yv) {
+// Gear; PICARD or AB2; UPWIND / CENTERED / TVD_SUPERBEE; AL penalty; no
+// obstacle terms).  tu/tv: the unpacked operand with the homogeneous ghost
+// conditions applied (:458 -> src/module_mpi_comm.f90:290-537).  tp/yp
+// (MONOLITHIC only): the operand's pressure (ghosts zero) and the
+// continuity rows' image.
+void mom_apply(const MomCtx& c, const double* tu, const double* tv, double* yu, double* yv,
+               const double* tp = nullptr, double* yp = nullptr) {
   const Mesh& m = c.m;
   const covof_params* prm = c.prm;
   const double dx = m.dx, dy = m.dy, dvol = dx * dy, dt = c.dt;
@@ -638,6 +645,7 @@ void mom_apply(const MomCtx& c, const double* tu, const double* tv, double* yu, 
         double dW = (tu[k] - tu[m.id(i - 1, j)]) / dx + (tv[m.id(i - 1, j + 1)] - tv[m.id(i - 1, j)]) / dy;
         val = val - (c.r_al[k] * dE - c.r_al[m.id(i - 1, j)] * dW) * dy;
       }
+      if (tp) val = val + (tp[k] - tp[m.id(i - 1, j)]) * dy;  // :597-602, B_u^T p
       yu[k] = val;
     }
   for (int j = 1; j <= v_ny; ++j)
@@ -684,7 +692,39 @@ void mom_apply(const MomCtx& c, const double* tu, const double* tv, double* yu, 
         double dS = (tu[m.id(i + 1, j - 1)] - tu[m.id(i, j - 1)]) / dx + (tv[k] - tv[m.id(i, j - 1)]) / dy;
         val = val - (c.r_al[k] * dN - c.r_al[m.id(i, j - 1)] * dS) * dx;
       }
+      if (tp) val = val + (tp[k] - tp[m.id(i, j - 1)]) * dx;  // :723-728
       yv[k] = val;
+    }
+  if (!tp || !yp) return;
+  // :730-777 continuity rows: div u dvol, plus 1e-10 p(1,1) dvol in cell
+  // (1,1) (the pressure level of the incompressible system)
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t k = m.id(i, j);
+      double div = (tu[m.id(i + 1, j)] - tu[k]) / dx + (tv[m.id(i, j + 1)] - tv[k]) / dy;
+      if (i == 1 && j == 1) yp[k] = div * dvol + 1.0e-10 * tp[k] * dvol;
+      else yp[k] = div * dvol;
+    }
+}
+
+// src/module_navier_stokes.f90:1541-1590: the pressure block's diagonal
+// diag_p = schur_aP, the row sum of the Schur complement approximation
+// B D^-1 B^T with D the momentum diagonals (du, dv after mom_diag), plus
+// 1e-10 dvol in cell (1,1) and 1e-12 dvol elsewhere.
+void schur_diag(const MomCtx& c, const double* du, const double* dv, double* dp) {
+  const Mesh& m = c.m;
+  const covof_params* prm = c.prm;
+  const double dx = m.dx, dy = m.dy, dvol = dx * dy;
+  const int nx = m.nx, ny = m.ny;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      double aW = 0.0, aE = 0.0, aS = 0.0, aN = 0.0;
+      if (!(i == 1 && is_wall(prm, L))) aW = (dy * dy) / std::max(1.0e-30, du[m.id(i, j)]);
+      if (!(i == nx && is_wall(prm, R))) aE = (dy * dy) / std::max(1.0e-30, du[m.id(i + 1, j)]);
+      if (!(j == 1 && is_wall(prm, B))) aS = (dx * dx) / std::max(1.0e-30, dv[m.id(i, j)]);
+      if (!(j == ny && is_wall(prm, T))) aN = (dx * dx) / std::max(1.0e-30, dv[m.id(i, j + 1)]);
+      const double reg = (i == 1 && j == 1) ? 1.0e-10 * dvol : 1.0e-12 * dvol;
+      dp[m.id(i, j)] = aW + aE + aS + aN + 0.0 + reg;
     }
 }
 
@@ -849,37 +889,49 @@ void mom_rhs(const MomCtx& c, const double* mu_node, const double* fx, const dou
 
 // Packed Krylov vectors: u DOFs (i=1..u_nx, j=1..ny) then v DOFs
 // (i=1..nx, j=1..v_ny), src/module_navier_stokes.f90:231-296.
+// MONOLITHIC adds the pressure DOFs (i=1..nx, j=1..ny) after them
+// (:281-294, :352-371).
 struct Packer {
   const MomCtx& c;
-  size_t n() const { return c.nu + c.nv; }
-  void pack(const double* u, const double* v, double* x) const {
+  size_t n() const { return c.nu + c.nv + (c.mono ? c.np : 0); }
+  void pack(const double* u, const double* v, double* x, const double* p = nullptr) const {
     const Mesh& m = c.m;
     size_t d = 0;
     for (int j = 1; j <= m.ny; ++j) for (int i = 1; i <= c.u_nx; ++i) x[d++] = u[m.id(i, j)];
     for (int j = 1; j <= c.v_ny; ++j) for (int i = 1; i <= m.nx; ++i) x[d++] = v[m.id(i, j)];
+    if (c.mono)
+      for (int j = 1; j <= m.ny; ++j) for (int i = 1; i <= m.nx; ++i) x[d++] = p ? p[m.id(i, j)] : 0.0;
   }
-  void unpack(const double* x, double* u, double* v) const {
+  void unpack(const double* x, double* u, double* v, double* p = nullptr) const {
     const Mesh& m = c.m;
     size_t d = 0;
     for (int j = 1; j <= m.ny; ++j) for (int i = 1; i <= c.u_nx; ++i) u[m.id(i, j)] = x[d++];
     for (int j = 1; j <= c.v_ny; ++j) for (int i = 1; i <= m.nx; ++i) v[m.id(i, j)] = x[d++];
+    if (c.mono && p)
+      for (int j = 1; j <= m.ny; ++j) for (int i = 1; i <= m.nx; ++i) p[m.id(i, j)] = x[d++];
   }
 };
 
 struct Krylov {
   const MomCtx& c;
   Packer pk;
-  std::vector<double> tu, tv, yu, yv, diag;  // tf (saved operand), diag packed
+  std::vector<double> tu, tv, yu, yv, tp, yp, diag;  // tf (saved operand), diag packed
   explicit Krylov(const MomCtx& cc) : c(cc), pk{cc} {
     size_t g = (size_t)(c.m.nx + 2) * (c.m.ny + 2);
     tu.assign(g, 0.0); tv.assign(g, 0.0); yu.assign(g, 0.0); yv.assign(g, 0.0);
+    tp.assign(g, 0.0); yp.assign(g, 0.0);  // tf%p: ghosts stay zero
   }
   // ns_apply_system_matrix with unpack + homogeneous BC (:397-458)
   void A(const double* x, double* y) {
-    pk.unpack(x, tu.data(), tv.data());
+    pk.unpack(x, tu.data(), tv.data(), tp.data());
     velocity_bc(c.prm, c.m, tu.data(), tv.data(), true);
-    mom_apply(c, tu.data(), tv.data(), yu.data(), yv.data());
-    pk.pack(yu.data(), yv.data(), y);
+    if (c.mono) {
+      mom_apply(c, tu.data(), tv.data(), yu.data(), yv.data(), tp.data(), yp.data());
+      pk.pack(yu.data(), yv.data(), y, yp.data());
+    } else {
+      mom_apply(c, tu.data(), tv.data(), yu.data(), yv.data());
+      pk.pack(yu.data(), yv.data(), y);
+    }
   }
   // src/module_linear_solvers.f90:88-117 (JACOBI) / :280-304 (ILU0 = same)
   void M(const double* src, double* dst) {
@@ -1225,6 +1277,43 @@ int al_step(const covof_params* prm, double dt, double* u, double* v, double* p,
   }
   if (iters) *iters = total;
   if (uzawa_done) *uzawa_done = m_done;
+  return st;
+}
+
+// src/module_simulation.f90:552-583 for solver_type MONOLITHIC: the
+// preconditioner blocks (momentum diagonals and the Schur diagonal diag_p),
+// the right-hand side (momentum without a pressure term, zero continuity
+// block, :1079-1100), pack (u, v, p), one Krylov solve of the coupled system,
+// unpack (u, v, p) and the velocity boundary conditions.
+int mono_step(const covof_params* prm, double dt, double* u, double* v, double* p, const double* rho_u,
+              const double* rho_v, const double* mu, const double* mu_node, const double* fx,
+              const double* fy, const Hist& hist, int* iters) {
+  const Mesh m = mesh_of(prm);
+  const size_t g = (size_t)(prm->nx + 2) * (prm->ny + 2);
+  std::vector<double> un(u, u + g), vn(v, v + g);
+  MomCtx c = make_ctx(prm, dt, un.data(), vn.data(), rho_u, rho_v, mu, mu_node, hist);
+  c.mono = true;
+  c.np = (size_t)prm->nx * prm->ny;
+  Krylov K(c);
+  std::vector<double> du(g, 1.0), dv(g, 1.0), dp(g, 1.0), ru(g, 0.0), rv(g, 0.0);
+  mom_diag(c, du.data(), dv.data());
+  schur_diag(c, du.data(), dv.data(), dp.data());
+  K.diag.resize(K.pk.n());
+  K.pk.pack(du.data(), dv.data(), K.diag.data(), dp.data());
+  mom_rhs(c, mu_node, fx, fy, hist.u_old, hist.v_old, ru.data(), rv.data());
+  std::vector<double> rhs(K.pk.n()), x(K.pk.n());
+  K.pk.pack(ru.data(), rv.data(), rhs.data(), nullptr);
+  K.pk.pack(u, v, x.data(), p);
+  int st, it = 0;
+  switch (prm->linear_solver) {
+    case COVOF_LINEAR_BICGSTAB: st = solve_bicgstab(K, rhs.data(), x.data(), &it); break;
+    case COVOF_LINEAR_CG: st = solve_cg(K, rhs.data(), x.data(), &it); break;
+    default: st = solve_bicgstab2(K, rhs.data(), x.data(), &it); break;
+  }
+  if (iters) *iters = it;
+  if (st == COVOF_NAN) return st;
+  K.pk.unpack(x.data(), u, v, p);
+  velocity_bc(prm, m, u, v, false);
   return st;
 }
 
@@ -1857,6 +1946,8 @@ int check_mom(const covof_params* prm, const double* u_old, const double* u_nm1,
   if (prm->convective_scheme != COVOF_CONV_UPWIND && prm->convective_scheme != COVOF_CONV_CENTERED &&
       prm->convective_scheme != COVOF_CONV_TVD_SUPERBEE)
     return COVOF_UNSUPPORTED;
+  if (prm->use_precond && (prm->precond == COVOF_PRECOND_SSOR || prm->precond == COVOF_PRECOND_BLOCK_TRIANGULAR))
+    return COVOF_UNSUPPORTED;
   if (prm->convective_linearization == COVOF_CONV_LIN_AB2 && !u_old) return COVOF_INVALID;
   if (has_nm1 && !u_nm1 && (prm->time_scheme == COVOF_TIME_GEAR ||
                             prm->convective_linearization == COVOF_CONV_LIN_AB2))
@@ -1883,6 +1974,39 @@ int orc_momentum_apply(const covof_params* prm, double dt, const double* xu, con
   pk.unpack(x.data(), tu.data(), tv.data());
   velocity_bc(prm, c.m, tu.data(), tv.data(), true);
   mom_apply(c, tu.data(), tv.data(), yu, yv);
+  return COVOF_OK;
+}
+
+// The MONOLITHIC operator (:380-780 with the pressure DOFs): momentum rows
+// with B^T p, continuity rows; the operand's pressure ghosts are zero.
+int orc_mono_apply(const covof_params* prm, double dt, const double* xu, const double* xv, const double* xp,
+                   double* yu, double* yv, double* yp, const double* u_n, const double* v_n,
+                   const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                   const double* u_old, const double* v_old, const double* u_nm1, const double* v_nm1,
+                   int has_nm1) {
+  int st = check_params(prm, false);
+  if (st) return st;
+  if ((st = check_mom(prm, u_old, u_nm1, has_nm1))) return st;
+  MomCtx c = make_ctx(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node, hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1));
+  c.mono = true;
+  c.np = (size_t)prm->nx * prm->ny;
+  size_t g = (size_t)(prm->nx + 2) * (prm->ny + 2);
+  std::vector<double> tu(g, 0.0), tv(g, 0.0), tp(g, 0.0);
+  Packer pk{c};
+  std::vector<double> x(pk.n());
+  pk.pack(xu, xv, x.data(), xp);
+  pk.unpack(x.data(), tu.data(), tv.data(), tp.data());
+  velocity_bc(prm, c.m, tu.data(), tv.data(), true);
+  mom_apply(c, tu.data(), tv.data(), yu, yv, tp.data(), yp);
+  return COVOF_OK;
+}
+
+// diag_p (the Schur diagonal) from the momentum diagonals du, dv
+int orc_schur_diag(const covof_params* prm, double dt, const double* du, const double* dv, double* dp) {
+  int st = check_params(prm, false);
+  if (st) return st;
+  MomCtx c = make_ctx(prm, dt, du, dv, du, dv, du, du);
+  schur_diag(c, du, dv, dp);
   return COVOF_OK;
 }
 
@@ -1938,6 +2062,18 @@ int orc_al_step(const covof_params* prm, double dt, double* u, double* v, double
     return COVOF_INVALID;
   return al_step(prm, dt, u, v, p, rho, rho_u, rho_v, mu, mu_node, fx_sigma, fy_sigma,
                  hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1), iters, uzawa_done);
+}
+
+int orc_mono_step(const covof_params* prm, double dt, double* u, double* v, double* p, const double* rho_u,
+                  const double* rho_v, const double* mu, const double* mu_node, const double* fx_sigma,
+                  const double* fy_sigma, const double* u_old, const double* v_old, const double* u_nm1,
+                  const double* v_nm1, int has_nm1, int* iters) {
+  int st = check_params(prm, false);
+  if (st) return st;
+  if ((st = check_mom(prm, u_old, u_nm1, has_nm1))) return st;
+  if (prm->solver_type != COVOF_SOLVER_MONOLITHIC) return COVOF_INVALID;
+  return mono_step(prm, dt, u, v, p, rho_u, rho_v, mu, mu_node, fx_sigma, fy_sigma,
+                   hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1), iters);
 }
 
 // src/module_simulation.f90:2424-2666 sim_solve_standard_projection

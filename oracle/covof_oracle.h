@@ -70,6 +70,12 @@ int orc_momentum_apply(const covof_params* prm, double dt, const double* xu, con
                        const double* rho_u, const double* rho_v, const double* mu,
                        const double* mu_node, const double* u_old, const double* v_old,
                        const double* u_nm1, const double* v_nm1, int has_nm1);
+int orc_mono_apply(const covof_params* prm, double dt, const double* xu, const double* xv, const double* xp,
+                   double* yu, double* yv, double* yp, const double* u_n, const double* v_n,
+                   const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                   const double* u_old, const double* v_old, const double* u_nm1, const double* v_nm1,
+                   int has_nm1);
+int orc_schur_diag(const covof_params* prm, double dt, const double* du, const double* dv, double* dp);
 int orc_momentum_diag(const covof_params* prm, double dt, const double* u_n, const double* v_n,
                       const double* rho_u, const double* rho_v, const double* mu,
                       const double* mu_node, double* diag_u, double* diag_v, const double* u_old,
@@ -97,6 +103,13 @@ int orc_al_step(const covof_params* prm, double dt, double* u, double* v, double
                 const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
                 const double* fx_sigma, const double* fy_sigma, const double* u_old, const double* v_old,
                 const double* u_nm1, const double* v_nm1, int has_nm1, int* iters, int* uzawa_done);
+/* one MONOLITHIC step: the coupled (u, v, p) system with the Schur
+ * diagonal as the pressure block's Jacobi preconditioner; iters = Krylov
+ * iterations */
+int orc_mono_step(const covof_params* prm, double dt, double* u, double* v, double* p, const double* rho_u,
+                  const double* rho_v, const double* mu, const double* mu_node, const double* fx_sigma,
+                  const double* fy_sigma, const double* u_old, const double* v_old, const double* u_nm1,
+                  const double* v_nm1, int has_nm1, int* iters);
 
 /* geometric VOF */
 int orc_reconstruct(const covof_params* prm, const double* C, double* seg);

@@ -55,6 +55,9 @@ def lib():
             "orc_svof_smooth": (i, [v, v, v]),
             "orc_vof_transport": (i, [v, d, i, v, v, v]),
             "orc_al_step": (i, [v, d] + [v] * 14 + [i, v, v]),
+            "orc_mono_step": (i, [v, d] + [v] * 13 + [i, v]),
+            "orc_mono_apply": (i, [v, d] + [v] * 16 + [i]),
+            "orc_schur_diag": (i, [v, d, v, v, v]),
             "orc_diffusion_smooth": (i, [v, v, v]),
         }
         for name, (res, args) in sig.items():
@@ -140,6 +143,24 @@ def momentum_apply(prm, dt, xu, xv, u_n, v_n, rho_u, rho_v, mu, mu_node, u_old=N
                                   _p(u_nm1), _p(v_nm1), int(has_nm1))
     assert st == 0, st
     return yu, yv
+
+
+def mono_apply(prm, dt, xu, xv, xp, u_n, v_n, rho_u, rho_v, mu, mu_node, u_old=None, v_old=None,
+               u_nm1=None, v_nm1=None, has_nm1=0):
+    """The MONOLITHIC operator on (xu, xv, xp); returns (yu, yv, yp)."""
+    yu, yv, yp = np.zeros_like(xu), np.zeros_like(xv), np.zeros_like(xp)
+    st = lib().orc_mono_apply(_params(prm), dt, _p(xu), _p(xv), _p(xp), _p(yu), _p(yv), _p(yp), _p(u_n),
+                              _p(v_n), _p(rho_u), _p(rho_v), _p(mu), _p(mu_node), _p(u_old), _p(v_old),
+                              _p(u_nm1), _p(v_nm1), int(has_nm1))
+    assert st == 0, st
+    return yu, yv, yp
+
+
+def schur_diag(prm, dt, du, dv):
+    dp = np.zeros_like(du)
+    st = lib().orc_schur_diag(_params(prm), dt, _p(du), _p(dv), _p(dp))
+    assert st == 0, st
+    return dp
 
 
 def momentum_diag(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node, u_old=None, v_old=None, u_nm1=None,
@@ -248,6 +269,15 @@ def vof_advect(prm, dt, step_count, f):
     assert st == 0, st
 
 
+def mono_step(prm, dt, f, has_nm1=0):
+    """One MONOLITHIC step (the coupled u, v, p solve); returns (iters, status)."""
+    it = C.c_int()
+    st = lib().orc_mono_step(_params(prm), dt, _p(f.u), _p(f.v), _p(f.p), _p(f.rho_u), _p(f.rho_v), _p(f.mu),
+                             _p(f.mu_node), _p(f.fx_sigma), _p(f.fy_sigma), _p(f.u_old), _p(f.v_old),
+                             _p(f.u_nm1), _p(f.v_nm1), int(has_nm1), C.byref(it))
+    return it.value, st
+
+
 def time_step(prm, dt, step_count, f):
     """One iteration of the time loop body of sim_run (src/module_simulation.f90:
     492-559) for a fixed dt and STANDARD_PROJECTION: the n-1 history
@@ -270,5 +300,8 @@ def time_step(prm, dt, step_count, f):
         apply_velocity_bc(prm, f.u, f.v, False)
     if prm.solver_type in (1, 4):  # AUGMENTED_LAGRANGIAN / AAL
         it, ud, st = al_step(prm, dt, f, has_nm1)
+        return it, 0, 0.0, st
+    if prm.solver_type == 2:  # MONOLITHIC
+        it, st = mono_step(prm, dt, f, has_nm1)
         return it, 0, 0.0, st
     return sp_step(prm, dt, f, has_nm1)

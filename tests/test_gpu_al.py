@@ -101,10 +101,10 @@ def test_batch_rejects_al(gpu_pkg):
         pkg.Batch(ps)
 
 
-def test_monolithic_is_unsupported(gpu_pkg, orc):
+def test_caal_is_unsupported(gpu_pkg, orc):
     pkg = gpu_pkg
     p, f, dt = _state(pkg, orc)
-    p.solver_type = pkg.capi.SOLVER_MONOLITHIC
+    p.solver_type = pkg.capi.SOLVER_CAAL
     with pkg.Solver(p) as s:
         s.state_set(f)
         with pytest.raises(pkg.CovofError):
