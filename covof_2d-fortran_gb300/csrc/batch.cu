@@ -389,6 +389,8 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
     if (b->mixed && (cases[c].p_inner_kind == COVOF_INNER_MG) != mg) return fail(COVOF_UNSUPPORTED);
     if (b->mixed && cases[c].p_inner_kind == COVOF_INNER_CG) return fail(COVOF_UNSUPPORTED);
     if (cases[c].p_precond == COVOF_PRECOND_SSOR) return fail(COVOF_UNSUPPORTED);
+    // the batch's Krylov kernels are the persistent ones (no sweep preconditioners)
+    if (uses_sweeps(cases[c])) return fail(COVOF_UNSUPPORTED);
     // the batch runs the projection coupling
     if (check_coupling(cases[c]) != COVOF_OK ||
         (cases[c].solver_type != 0 && cases[c].solver_type != COVOF_SOLVER_STANDARD_PROJECTION))

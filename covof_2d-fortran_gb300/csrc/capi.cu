@@ -565,8 +565,9 @@ int check_mom_params(const covof_params& P) {
   if (P.linear_solver != COVOF_LINEAR_BICGSTAB && P.linear_solver != COVOF_LINEAR_BICGSTAB2 &&
       P.linear_solver != COVOF_LINEAR_CG)
     return COVOF_UNSUPPORTED;
-  if (P.use_precond && (P.precond == COVOF_PRECOND_SSOR || P.precond == COVOF_PRECOND_BLOCK_TRIANGULAR))
-    return COVOF_UNSUPPORTED;
+  if (P.use_precond && P.precond != COVOF_PRECOND_NONE && P.precond != COVOF_PRECOND_JACOBI &&
+      P.precond != COVOF_PRECOND_ILU0 && !uses_sweeps(P))
+    return COVOF_INVALID;
   if (P.max_iter < 0) return COVOF_INVALID;
   return COVOF_OK;
 }
@@ -608,6 +609,18 @@ int mom_pre(covof_handle* h, double dt, double* u, double* v, const double* rho_
   k_mom_pack<<<grd, blk, 0, h->stream>>>(a, u, v);
   CK(cudaGetLastError());
   return COVOF_OK;
+}
+
+// The Krylov solve of a prepared argument block: the persistent kernel of
+// the configured method, or with SSOR / BLOCK_TRIANGULAR the host-driven
+// iterations over the sweep stencils (assembled here from a's fields).
+int krylov_run(covof_handle* h, MomArgs& a) {
+  if (uses_sweeps(h->prm)) {
+    CS(prec_blocks_dev(h, a));
+    return sweep_solve(h, a);
+  }
+  void* args[] = {&a};
+  return launch_coop(h, h->m_fn, h->m_nb, kKrylovThreads, args, false);
 }
 
 // Solved velocities back into u, v, then the velocity boundary conditions.
@@ -683,6 +696,9 @@ int al_enqueue(covof_handle* h, double dt, double* u, double* v, double* p, cons
   a.p_al = p;
   k_mom_diag<<<gf, blk, 0, h->stream>>>(a);
   CK(cudaGetLastError());
+  // the preconditioner blocks once, from the fields at the coupling's start
+  const bool sweeps = uses_sweeps(P);
+  if (sweeps) CS(prec_blocks_dev(h, a));
   const int umax = P.uzawa_iter > 0 ? P.uzawa_iter : 1;
   int total = 0, done = 0, status = COVOF_OK;
   for (int m = 1; m <= umax; ++m) {
@@ -691,8 +707,12 @@ int al_enqueue(covof_handle* h, double dt, double* u, double* v, double* p, cons
     k_mom_assemble<<<gf, blk, 0, h->stream>>>(a);
     k_mom_pack<<<gf, blk, 0, h->stream>>>(a, u, v);
     CK(cudaGetLastError());
-    void* args[] = {&a};
-    CS(launch_coop(h, h->m_fn, h->m_nb, kKrylovThreads, args, false));
+    if (sweeps) {
+      CS(sweep_solve(h, a));
+    } else {
+      void* args[] = {&a};
+      CS(launch_coop(h, h->m_fn, h->m_nb, kKrylovThreads, args, false));
+    }
     CS(mom_post(h, a, u, v));
     k_al_pressure<<<gc, blk, 0, h->stream>>>(al);
     CK(cudaGetLastError());
@@ -747,8 +767,7 @@ int mono_enqueue(covof_handle* h, double dt, double* u, double* v, double* p, co
   k_mom_assemble<<<gf, blk, 0, h->stream>>>(a);
   k_mom_pack<<<gf, blk, 0, h->stream>>>(a, u, v);
   CK(cudaGetLastError());
-  void* args[] = {&a};
-  CS(launch_coop(h, h->m_fn, h->m_nb, kKrylovThreads, args, false));
+  CS(krylov_run(h, a));
   return mom_post(h, a, u, v);
 }
 
@@ -758,8 +777,7 @@ int predictor_enqueue(covof_handle* h, double dt, double* u, double* v, const do
                       const double* fy, const double* u_old, const double* v_old) {
   MomArgs a;
   CS(mom_pre(h, dt, u, v, rho_u, rho_v, mu, mu_node, fx, fy, u_old, v_old, &a));
-  void* args[] = {&a};
-  CS(launch_coop(h, h->m_fn, h->m_nb, kKrylovThreads, args, false));
+  CS(krylov_run(h, a));
   return mom_post(h, a, u, v);
 }
 
@@ -1070,6 +1088,8 @@ int run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run_stats
   // the Uzawa exit test reads a scalar back per iteration: eager steps
   h->al_check = is_al(P) && P.uzawa_iter > 1 && P.uzawa_tol > 0.0;
   if (h->al_check) flags &= ~COVOF_RUN_GRAPH;
+  // the sweep preconditioners' Krylov iterations are driven from the host
+  if (uses_sweeps(P)) flags &= ~COVOF_RUN_GRAPH;
   // every buffer and launch plan exists before a capture starts
   CS(ensure_fields(h));
   CS(ensure_poisson(h));
@@ -1249,6 +1269,7 @@ int covof_destroy(covof_handle* h) {
   if (!h) return COVOF_INVALID;
   writer_destroy(h);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  sweep_free(h);
   double** fl[] = {&h->f_u, &h->f_v, &h->f_p, &h->f_rho_u, &h->f_rho_v, &h->f_mu, &h->f_mu_node,
                    &h->f_fx, &h->f_fy, &h->f_u_old, &h->f_v_old, &h->f_u_nm1, &h->f_v_nm1, &h->f_Cs, &h->f_Ct, &h->dscr, &h->al_r,
                    &h->f_C, &h->f_rho, &h->f_curv,
@@ -1497,6 +1518,46 @@ int covof_momentum_apply(covof_handle* h, double dt, const double* xu, const dou
   CK(cudaGetLastError());
   CS(d2h(h, yu, y, g)); CS(d2h(h, yv, y + g, g));
   return sync(h);
+}
+
+int covof_precond_apply(covof_handle* h, double dt, const double* zu, const double* zv, const double* zp,
+                        double* yu, double* yv, double* yp, const double* u_n, const double* v_n,
+                        const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                        const double* r_al) {
+  const bool mono = h && h->prm.solver_type == COVOF_SOLVER_MONOLITHIC;
+  if (!h || !zu || !zv || !yu || !yv || (mono && (!zp || !yp))) return COVOF_INVALID;
+  CS(check_mom_params(h->prm));
+  CS(ensure_fields(h));
+  CS(ensure_mom(h));
+  const size_t g = h->g;
+  CS(h2d(h, h->f_u, u_n, g)); CS(h2d(h, h->f_v, v_n, g));
+  CS(h2d(h, h->f_rho_u, rho_u, g)); CS(h2d(h, h->f_rho_v, rho_v, g));
+  CS(h2d(h, h->f_mu, mu, g)); CS(h2d(h, h->f_mu_node, mu_node, g));
+  double* z = h->mv[0];
+  double* y = h->mv[1];
+  CK(cudaMemsetAsync(z, 0, (mono ? 3 : 2) * g * sizeof(double), h->stream));
+  CS(h2d(h, z, zu, g)); CS(h2d(h, z + g, zv, g));
+  if (mono) CS(h2d(h, z + 2 * g, zp, g));
+  MomArgs a = mom_args(h, dt, h->f_u, h->f_v, h->f_rho_u, h->f_rho_v, h->f_mu, h->f_mu_node, nullptr, nullptr,
+                       h->f_u_old, h->f_v_old);
+  a.mono = mono ? 1 : 0;
+  if (is_al(h->prm) && r_al) {
+    CS(h2d(h, h->al_r, r_al, g));
+    a.r_al = h->al_r;
+  }
+  const dim3 blk(32, 8), gf = grid2(h->prm.nx + 1, h->prm.ny + 1, blk), gc = grid2(h->prm.nx, h->prm.ny, blk);
+  k_mom_diag<<<gf, blk, 0, h->stream>>>(a);
+  if (mono) k_mono_diag<<<gc, blk, 0, h->stream>>>(a);
+  k_mom_assemble<<<gf, blk, 0, h->stream>>>(a);
+  CK(cudaGetLastError());
+  CK(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
+  CS(precond_apply_dev(h, a, z, y));
+  CS(d2h(h, yu, y, g)); CS(d2h(h, yv, y + g, g));
+  if (mono) CS(d2h(h, yp, y + 2 * g, g));
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, h->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CS(sync(h));
+  return e != 0 ? COVOF_TIMEOUT : COVOF_OK;
 }
 
 // ---- SP step -----------------------------------------------------------------

@@ -41,6 +41,33 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
 __device__ __forceinline__ void red_add_release_u32(unsigned int* p, unsigned int v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// lane 0 waits until *p >= need (bounded); the warp learns the outcome
+__device__ __forceinline__ bool warp_wait_ge(const unsigned int* p, unsigned int need, int* err) {
+  int ok = 1;
+  if ((threadIdx.x & 31) == 0) {
+    long long spins = 0;
+    while ((int)(ld_acquire_u32(p) - need) < 0) {
+      if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+    }
+  }
+  return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+// x / b, correctly rounded, from yb = RN(1 / b): q0 = RN(x yb) is within one
+// ulp of x / b, the remainder x - b q0 is exact in one FMA, and one FMA
+// correction step q0 + r yb rounds to the correctly rounded quotient
+// (P. Markstein, "IA-64 and Elementary Functions", 2000, Theorem 8.10; x, b
+// normal, x / b in range).  Three dependent FP64 operations instead of a
+// full division.
+__device__ __forceinline__ double div_rcp(double x, double b, double yb) {
+  const double q0 = __dmul_rn(x, yb);
+  const double r = __fma_rn(-b, q0, x);
+  return __fma_rn(r, yb, q0);
+}
 
 struct GridSync {
   unsigned int* count;

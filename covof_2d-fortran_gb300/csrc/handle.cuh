@@ -51,6 +51,19 @@ struct RunStats {
 // One thread: fold this step's predictor and Poisson result records in.
 __global__ void k_step_log(const KrylovResult* kr, const PcgResult* pr, RunStats* s);
 
+// Buffers of the sweep preconditioners (SSOR, BLOCK_TRIANGULAR; precond.cu),
+// allocated on first use.
+struct SweepKit {
+  bool ready = false;
+  size_t n = 0;                 // entries of a packed Krylov vector
+  double* coef = nullptr;       // 18 arrays of (nx+2)*(ny+2): the u, v, Schur stencils
+  PBlk blk{};
+  double* t[3] = {};            // scratch vectors: A x, the block-triangular rhs, M^-1 b
+  unsigned int* prog = nullptr; // wavefront progress, per job and band
+  int max_bands = 0, cap = 0, dot_blocks = 0;
+  double *part = nullptr, *dsum = nullptr, *hdot = nullptr;  // dot products (hdot pinned)
+};
+
 }  // namespace host
 }  // namespace covof
 
@@ -92,6 +105,7 @@ struct covof_handle {
   bool have_mom = false;
   double *mx = nullptr, *mrhs = nullptr, *mdiag = nullptr, *mv[7] = {};
   double *mcoef = nullptr, *midiag = nullptr;  // assembled operator rows, inverse diagonal
+  covof::host::SweepKit sweep;                   // SSOR / BLOCK_TRIANGULAR preconditioners
   // VOF scratch
   bool have_vof = false;
   double *cs = nullptr, *seg = nullptr, *cnx = nullptr, *cny = nullptr, *ckap = nullptr;
@@ -178,6 +192,14 @@ int velocity_bc_dev(covof_handle* h, double* u, double* v);
 int correct_dev(covof_handle* h, double dt, double* u, double* v, const double* p, const double* rho_u,
                 const double* rho_v);
 double** field_slot(covof_handle* h, int f);
+// precond.cu
+bool uses_sweeps(const covof_params& P);
+int ensure_sweeps(covof_handle* h);
+void sweep_free(covof_handle* h);
+int prec_blocks_dev(covof_handle* h, const MomArgs& a);
+int sweep_precond(covof_handle* h, const MomArgs& a, const double* src, double* dst);
+int sweep_solve(covof_handle* h, const MomArgs& a);
+int precond_apply_dev(covof_handle* h, const MomArgs& a, const double* src, double* dst);
 
 }  // namespace host
 }  // namespace covof

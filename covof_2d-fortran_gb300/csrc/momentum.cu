@@ -421,6 +421,131 @@ __global__ void k_mom_diag(MomArgs a) {
   }
 }
 
+// Stencils of the sweep preconditioners, src/module_navier_stokes.f90:
+// 1312-1590 (the u block :1312-1425, v block :1428-1539, Schur :1542-1590);
+// the centres equal k_mom_diag's diagonals.  Every DOF entry of every array
+// is written (zero where the reference leaves a coefficient at zero), so the
+// arrays need no clearing between assemblies.  One thread per (i, j).
+__device__ __forceinline__ void put_stencil(const Stencil& t, int k, double W, double E, double S, double N,
+                                            double P) {
+  t.W[k] = W; t.E[k] = E; t.S[k] = S; t.N[k] = N; t.P[k] = P;
+  const double d = fabs(P) < 1.0e-30 ? 1.0 : P;
+  t.rP[k] = __drcp_rn(d);
+}
+
+__global__ void k_prec_blocks(MomArgs a, PBlk b) {
+  const Dims& D = a.D;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int nx = D.nx, ny = D.ny;
+  const double dx = a.dx, dy = a.dy, dvol = dx * dy;
+  const double dt_safe = a.dt > 1.0e-30 ? a.dt : 1.0;
+  if (i <= nx + 1 && j <= ny) {
+    const int k = D.id(i, j);
+    const double rho = a.rho_u[k];
+    double Du = ((a.alpha * rho) / dt_safe) * dvol;
+    if (Du <= 1.0e-30) Du = 1.0;
+    if (i == 1) {
+      put_stencil(b.u, k, 0.0, (a.bc[SL] == COVOF_BC_NEUMANN && nx + 1 >= 2) ? Du : 0.0, 0.0, 0.0, Du);
+    } else if (i == nx + 1) {
+      put_stencil(b.u, k, (a.bc[SR] == COVOF_BC_NEUMANN && nx + 1 >= 2) ? Du : 0.0, 0.0, 0.0, 0.0, Du);
+    } else {
+      const double mue = a.mu[k], muw = a.mu[k - 1];
+      const double cE = 2.0 * mue * (dy / dx), cW = 2.0 * muw * (dy / dx);
+      const double cNr = a.mu_node[k + D.P] * (dx / dy);
+      const double cSr = a.mu_node[k] * (dx / dy);
+      double cNv = cNr, cSv = cSr, dwy = 0.0, cNx = 0.0, cSx = 0.0;
+      if (j == 1) {
+        if (a.bc[SB] == COVOF_BC_DIRICHLET) {
+          if (ny >= 2) { dwy = dwy + 3.0 * cSr; cNx = cNx + cSr / 3.0; }
+          else dwy = dwy + 2.0 * cSr;
+        }
+        cSv = 0.0;
+      }
+      if (j == ny) {
+        if (a.bc[ST] == COVOF_BC_DIRICHLET) {
+          if (ny >= 2) { dwy = dwy + 3.0 * cNr; cSx = cSx + cNr / 3.0; }
+          else dwy = dwy + 2.0 * cNr;
+        }
+        cNv = 0.0;
+      }
+      double cd = 0.0, cvW = 0.0, cvE = 0.0, cvS = 0.0, cvN = 0.0;
+      if (a.conv) {
+        double FE, FW, FN, FS;
+        u_fluxes(a, i, j, FE, FW, FN, FS);
+        cd = rho * (fmax(FE, 0.0) + fmax(-FW, 0.0) + fmax(FN, 0.0) + fmax(-FS, 0.0));
+        cvE = rho * fmax(-FE, 0.0);
+        cvW = rho * fmax(FW, 0.0);
+        cvN = (j == ny) ? 0.0 : rho * fmax(-FN, 0.0);
+        cvS = (j == 1) ? 0.0 : rho * fmax(FS, 0.0);
+      }
+      double alE = 0.0, alW = 0.0;
+      if (a.r_al) { alE = a.r_al[k] * (dy / dx); alW = a.r_al[k - 1] * (dy / dx); }
+      double aP = Du + dwy + cd + 0.0 + 0.0 + cW + cE + cSv + cNv + alW + alE;
+      if (aP <= 1.0e-15) aP = 1.0;
+      put_stencil(b.u, k, cW + cvW + alW, cE + cvE + alE, cSv + cvS + cSx, cNv + cvN + cNx, aP);
+    }
+  }
+  if (i <= nx && j <= ny + 1) {
+    const int k = D.id(i, j);
+    const double rho = a.rho_v[k];
+    double Dv = ((a.alpha * rho) / dt_safe) * dvol;
+    if (Dv <= 1.0e-30) Dv = 1.0;
+    if ((j == 1 && is_wall(a, SB)) || (j == ny + 1 && is_wall(a, ST))) {
+      put_stencil(b.v, k, 0.0, 0.0, 0.0, 0.0, Dv);
+    } else if (j == 1 && a.bc[SB] == COVOF_BC_NEUMANN && ny + 1 >= 2) {
+      put_stencil(b.v, k, 0.0, 0.0, 0.0, Dv, Dv);
+    } else if (j == ny + 1 && a.bc[ST] == COVOF_BC_NEUMANN && ny + 1 >= 2) {
+      put_stencil(b.v, k, 0.0, 0.0, Dv, 0.0, Dv);
+    } else {
+      const double mun = a.mu[k], mus = a.mu[k - D.P];
+      const double cN = 2.0 * mun * (dx / dy), cS = 2.0 * mus * (dx / dy);
+      const double cEr = a.mu_node[k + 1] * (dy / dx);
+      const double cWr = a.mu_node[k] * (dy / dx);
+      double cEv = cEr, cWv = cWr, dwx = 0.0;
+      if (i == 1) {
+        if (a.bc[SL] == COVOF_BC_DIRICHLET) dwx = dwx + 2.0 * cWr;
+        cWv = 0.0;
+      }
+      if (i == nx) {
+        if (a.bc[SR] == COVOF_BC_DIRICHLET) dwx = dwx + 2.0 * cEr;
+        cEv = 0.0;
+      }
+      double cd = 0.0, cvW = 0.0, cvE = 0.0, cvS = 0.0, cvN = 0.0;
+      if (a.conv) {
+        double FE, FW, FN, FS;
+        v_fluxes(a, i, j, FE, FW, FN, FS);
+        cd = rho * (fmax(FE, 0.0) + fmax(-FW, 0.0) + fmax(FN, 0.0) + fmax(-FS, 0.0));
+        cvE = (i == nx) ? 0.0 : rho * fmax(-FE, 0.0);
+        cvW = (i == 1) ? 0.0 : rho * fmax(FW, 0.0);
+        cvN = rho * fmax(-FN, 0.0);
+        cvS = rho * fmax(FS, 0.0);
+      }
+      double alN = 0.0, alS = 0.0;
+      if (a.r_al) { alN = a.r_al[k] * (dx / dy); alS = a.r_al[k - D.P] * (dx / dy); }
+      double aP = Dv + dwx + cd + 0.0 + 0.0 + cWv + cEv + cS + cN + alS + alN;
+      if (aP <= 1.0e-15) aP = 1.0;
+      put_stencil(b.v, k, cWv + cvW, cEv + cvE, cS + cvS + alS, cN + cvN + alN, aP);
+    }
+  }
+}
+
+// The Schur stencil from the u / v centres (after k_prec_blocks).
+__global__ void k_prec_schur(MomArgs a, PBlk b) {
+  const Dims& D = a.D;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > D.nx || j > D.ny) return;
+  const double dx = a.dx, dy = a.dy, dvol = dx * dy;
+  double sW = 0.0, sE = 0.0, sS = 0.0, sN = 0.0;
+  if (!(i == 1 && is_wall(a, SL))) sW = __ddiv_rn(dy * dy, fmax(1.0e-30, b.u.P[D.id(i, j)]));
+  if (!(i == D.nx && is_wall(a, SR))) sE = __ddiv_rn(dy * dy, fmax(1.0e-30, b.u.P[D.id(i + 1, j)]));
+  if (!(j == 1 && is_wall(a, SB))) sS = __ddiv_rn(dx * dx, fmax(1.0e-30, b.v.P[D.id(i, j)]));
+  if (!(j == D.ny && is_wall(a, ST))) sN = __ddiv_rn(dx * dx, fmax(1.0e-30, b.v.P[D.id(i, j + 1)]));
+  const double reg = (i == 1 && j == 1) ? 1.0e-10 * dvol : 1.0e-12 * dvol;
+  put_stencil(b.s, D.id(i, j), sW, sE, sS, sN, sW + sE + sS + sN + 0.0 + reg);
+}
+
 // Right-hand side, src/module_navier_stokes.f90:817-1088 (SP, constant walls;
 // Euler, or the Gear / BDF2 inertial term rho (2 u^n - u^(n-1) / 2) / dt).
 __global__ void k_mom_rhs(MomArgs a) {
@@ -647,6 +772,14 @@ __device__ __forceinline__ double pa_at(const MomArgs& a, const DofWalker& W, in
     }
   }
   return with_prec ? y * a.idiag[k] : y;
+}
+
+// y = A x at every DOF from the assembled rows (one launch; the Krylov
+// iterations driven from the host for the sweep preconditioners).
+__global__ void k_mom_matvec(MomArgs a, const double* x, double* y) {
+  const Team tm{(int)blockIdx.x, (int)gridDim.x};
+  DofWalker W(a.D, tm, a.mono);
+  FOR_DOFS(a, W, part, i, j, k) y[k] = pa_at(a, W, part, i, j, k, x, false);
 }
 
 struct KCtx {

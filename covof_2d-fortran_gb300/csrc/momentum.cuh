@@ -55,8 +55,24 @@ struct BcArgs {
   double bcu[4], bcv[4];
 };
 
+// Five-point stencils of the SSOR / BLOCK_TRIANGULAR preconditioners
+// (ns_assemble_preconditioner_blocks, src/module_navier_stokes.f90:
+// 1268-1595): per block (u faces, v faces, Schur cells) the neighbour
+// coefficients W, E, S, N (M-matrix form), the centre P (the reference's
+// aP, or 1 where |aP| < 1e-30 as the sweeps read it) and rP = RN(1 / P).
+// Each array (nx+2)*(ny+2) doubles in the field layout.
+struct Stencil {
+  double *W, *E, *S, *N, *P, *rP;
+};
+struct PBlk {
+  Stencil u, v, s;
+};
+
 __global__ void k_mom_diag(MomArgs a);
 __global__ void k_mono_diag(MomArgs a);
+__global__ void k_prec_blocks(MomArgs a, PBlk b);
+__global__ void k_prec_schur(MomArgs a, PBlk b);
+__global__ void k_mom_matvec(MomArgs a, const double* x, double* y);
 
 // Augmented Lagrangian (momentum.cu)
 struct AlArgs {

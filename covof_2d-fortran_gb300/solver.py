@@ -190,6 +190,16 @@ class Solver:
                                     _ptr(f.fy_sigma), _ptr(f.u_old), _ptr(f.v_old), C.byref(it), C.byref(ud))
         return it.value, ud.value, self._check(st, "covof_al_step")
 
+    def precond_apply(self, dt, zu, zv, zp, u_n, v_n, rho_u, rho_v, mu, mu_node, r_al=None):
+        """The Krylov preconditioner M^-1 on host arrays (zp / yp: the
+        MONOLITHIC pressure block); returns (yu, yv, yp)."""
+        yu, yv, yp = np.zeros_like(zu), np.zeros_like(zv), np.zeros_like(zu)
+        st = self.lib.covof_precond_apply(self.h, dt, _ptr(zu), _ptr(zv), _ptr(zp), _ptr(yu), _ptr(yv),
+                                          _ptr(yp), _ptr(u_n), _ptr(v_n), _ptr(rho_u), _ptr(rho_v), _ptr(mu),
+                                          _ptr(mu_node), _ptr(r_al))
+        self._check(st, "covof_precond_apply")
+        return yu, yv, yp
+
     def monolithic_step(self, dt: float, f: Fields, has_nm1=None):
         """One MONOLITHIC step on host fields (the coupled u, v, p solve);
         returns (Krylov iterations, status)."""

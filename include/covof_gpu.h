@@ -50,9 +50,11 @@ enum { COVOF_LINEAR_BICGSTAB2 = 1, COVOF_LINEAR_BICGSTAB = 2, COVOF_LINEAR_CG = 
  * ILU0 is the same diagonal scaling as JACOBI in the reference
  * (src/module_linear_solvers.f90:280-304).  SSOR is accepted for the pressure
  * Poisson only, where it names the reference's symmetric Gauss-Seidel sweep
- * pair (src/module_simulation.f90:2709-2758).  The momentum / coupled
- * Krylov solves take NONE, JACOBI and ILU0; SSOR and BLOCK_TRIANGULAR there
- * return COVOF_UNSUPPORTED. */
+ * pair (src/module_simulation.f90:2709-2758).  In the momentum / coupled
+ * Krylov solves SSOR is two symmetric lexicographic sweeps per block and
+ * BLOCK_TRIANGULAR the Schur-complement sweeps then the velocity sweeps
+ * (src/module_linear_solvers.f90:137-278); their Krylov iterations are driven
+ * from the host, so covof_run_steps runs them eagerly. */
 enum { COVOF_PRECOND_NONE = 0, COVOF_PRECOND_JACOBI = 1, COVOF_PRECOND_SSOR = 2, COVOF_PRECOND_ILU0 = 3,
        COVOF_PRECOND_BLOCK_TRIANGULAR = 4 };
 /* Convective schemes: CONV_* in src/module_constants.f90:81-85. */
@@ -224,6 +226,20 @@ int covof_momentum_apply(covof_handle* h, double dt, const double* xu, const dou
                          double* yu, double* yv, const double* u_n, const double* v_n,
                          const double* rho_u, const double* rho_v, const double* mu,
                          const double* mu_node);
+
+/* The momentum / coupled Krylov solve's preconditioner M^-1 on one operand
+ * (apply_precond, src/module_linear_solvers.f90:88-304): JACOBI / ILU0
+ * diagonal scaling, or the SSOR / BLOCK_TRIANGULAR sweeps over the stencils
+ * of ns_assemble_preconditioner_blocks (src/module_navier_stokes.f90:
+ * 1268-1595), assembled from fields_old = (u_n, v_n, rho_u, rho_v, mu,
+ * mu_node) and the handle's history.  zp / yp: the pressure block
+ * (MONOLITHIC only, else may be NULL); r_al: the penalty field for
+ * AUGMENTED_LAGRANGIAN / AAL (else NULL).  Exposed for parity tests of the
+ * preconditioner itself. */
+int covof_precond_apply(covof_handle* h, double dt, const double* zu, const double* zv, const double* zp,
+                        double* yu, double* yv, double* yp, const double* u_n, const double* v_n,
+                        const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                        const double* r_al);
 
 /* Pressure Poisson from a predicted velocity (src/module_simulation.f90:2476-2584):
  * assembly, PCG, gauge.  p: warm start in, solution out (interior). */

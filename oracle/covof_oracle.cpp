@@ -887,6 +887,172 @@ void mom_rhs(const MomCtx& c, const double* mu_node, const double* fx, const dou
     }
 }
 
+// src/module_navier_stokes.f90:1268-1595 ns_assemble_preconditioner_blocks:
+// the five-point stencils of the u and v blocks for the SSOR sweeps (M-matrix
+// form: aP r = z + aW r_W + aE r_E + aS r_S + aN r_N, convection upwinded),
+// and for MONOLITHIC the Schur complement approximation B D^-1 B^T.  All
+// arrays in the (0:nx+1, 0:ny+1) layout; u at faces i = 1..u_nx, v at faces
+// j = 1..v_ny, the Schur stencil at cells.
+struct PBlocks {
+  std::vector<double> uW, uE, uS, uN, uP, vW, vE, vS, vN, vP, sW, sE, sS, sN, sP;
+};
+
+void prec_blocks(const MomCtx& c, PBlocks& Q) {
+  const Mesh& m = c.m;
+  const covof_params* prm = c.prm;
+  const double dx = m.dx, dy = m.dy, dvol = dx * dy;
+  const double dt_safe = c.dt > 1.0e-30 ? c.dt : 1.0;
+  const int nx = m.nx, ny = m.ny, u_nx = c.u_nx, v_ny = c.v_ny;
+  const size_t g = (size_t)(nx + 2) * (ny + 2);
+  for (auto* v : {&Q.uW, &Q.uE, &Q.uS, &Q.uN, &Q.vW, &Q.vE, &Q.vS, &Q.vN, &Q.sW, &Q.sE, &Q.sS, &Q.sN})
+    v->assign(g, 0.0);
+  for (auto* v : {&Q.uP, &Q.vP, &Q.sP}) v->assign(g, 1.0);
+  // 1. u block (:1312-1425)
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= u_nx; ++i) {
+      size_t k = m.id(i, j);
+      double rho = c.rho_u[k];
+      double Du = ((c.alpha * rho) / dt_safe) * dvol;
+      if (Du <= 1.0e-30) Du = 1.0;
+      if (i == 1) {
+        Q.uP[k] = Du;
+        Q.uE[k] = (prm->bc_type[L] == COVOF_BC_NEUMANN && u_nx >= 2) ? Du : 0.0;
+        continue;
+      }
+      if (i == u_nx) {
+        Q.uP[k] = Du;
+        Q.uW[k] = (prm->bc_type[R] == COVOF_BC_NEUMANN && u_nx >= 2) ? Du : 0.0;
+        continue;
+      }
+      double mue = c.mu[m.id(i, j)], muw = c.mu[m.id(i - 1, j)];
+      double cE = 2.0 * mue * (dy / dx), cW = 2.0 * muw * (dy / dx);
+      double cNr = c.mu_node[m.id(i, j + 1)] * (dx / dy);
+      double cSr = c.mu_node[m.id(i, j)] * (dx / dy);
+      double cNv = cNr, cSv = cSr, dwy = 0.0, cNx = 0.0, cSx = 0.0;
+      if (j == 1) {
+        if (prm->bc_type[B] == COVOF_BC_DIRICHLET) {
+          if (ny >= 2) { dwy = dwy + 3.0 * cSr; cNx = cNx + cSr / 3.0; }
+          else dwy = dwy + 2.0 * cSr;
+        }
+        cSv = 0.0;
+      }
+      if (j == ny) {
+        if (prm->bc_type[T] == COVOF_BC_DIRICHLET) {
+          if (ny >= 2) { dwy = dwy + 3.0 * cNr; cSx = cSx + cNr / 3.0; }
+          else dwy = dwy + 2.0 * cNr;
+        }
+        cNv = 0.0;
+      }
+      double cd = 0.0, cvW = 0.0, cvE = 0.0, cvS = 0.0, cvN = 0.0;
+      if (prm->enable_convection) {
+        double FE, FW, FN, FS;
+        u_conv_fluxes(c, i, j, FE, FW, FN, FS);
+        cd = rho * (std::max(FE, 0.0) + std::max(-FW, 0.0) + std::max(FN, 0.0) + std::max(-FS, 0.0));
+        cvE = rho * std::max(-FE, 0.0);
+        cvW = rho * std::max(FW, 0.0);
+        cvN = (j == ny) ? 0.0 : rho * std::max(-FN, 0.0);
+        cvS = (j == 1) ? 0.0 : rho * std::max(FS, 0.0);
+      }
+      double alE = 0.0, alW = 0.0;
+      if (c.r_al) { alE = c.r_al[k] * (dy / dx); alW = c.r_al[m.id(i - 1, j)] * (dy / dx); }
+      Q.uW[k] = cW + cvW + alW;
+      Q.uE[k] = cE + cvE + alE;
+      Q.uS[k] = cSv + cvS + cSx;
+      Q.uN[k] = cNv + cvN + cNx;
+      double aP = Du + dwy + cd + 0.0 + 0.0 + cW + cE + cSv + cNv + alW + alE;
+      if (aP <= 1.0e-15) aP = 1.0;
+      Q.uP[k] = aP;
+    }
+  // 2. v block (:1428-1539)
+  for (int j = 1; j <= v_ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t k = m.id(i, j);
+      double rho = c.rho_v[k];
+      double Dv = ((c.alpha * rho) / dt_safe) * dvol;
+      if (Dv <= 1.0e-30) Dv = 1.0;
+      bool wall = (j == 1 && is_wall(prm, B)) || (j == v_ny && is_wall(prm, T));
+      if (wall) { Q.vP[k] = Dv; continue; }
+      if (j == 1 && prm->bc_type[B] == COVOF_BC_NEUMANN && v_ny >= 2) { Q.vP[k] = Dv; Q.vN[k] = Dv; continue; }
+      if (j == v_ny && prm->bc_type[T] == COVOF_BC_NEUMANN && v_ny >= 2) { Q.vP[k] = Dv; Q.vS[k] = Dv; continue; }
+      double mun = c.mu[m.id(i, j)], mus = c.mu[m.id(i, j - 1)];
+      double cN = 2.0 * mun * (dx / dy), cS = 2.0 * mus * (dx / dy);
+      double cEr = c.mu_node[m.id(i + 1, j)] * (dy / dx);
+      double cWr = c.mu_node[m.id(i, j)] * (dy / dx);
+      double cEv = cEr, cWv = cWr, dwx = 0.0;
+      if (i == 1) {
+        if (prm->bc_type[L] == COVOF_BC_DIRICHLET) dwx = dwx + 2.0 * cWr;
+        cWv = 0.0;
+      }
+      if (i == nx) {
+        if (prm->bc_type[R] == COVOF_BC_DIRICHLET) dwx = dwx + 2.0 * cEr;
+        cEv = 0.0;
+      }
+      double cd = 0.0, cvW = 0.0, cvE = 0.0, cvS = 0.0, cvN = 0.0;
+      if (prm->enable_convection) {
+        double FE, FW, FN, FS;
+        v_conv_fluxes(c, i, j, FE, FW, FN, FS);
+        cd = rho * (std::max(FE, 0.0) + std::max(-FW, 0.0) + std::max(FN, 0.0) + std::max(-FS, 0.0));
+        cvE = (i == nx) ? 0.0 : rho * std::max(-FE, 0.0);
+        cvW = (i == 1) ? 0.0 : rho * std::max(FW, 0.0);
+        cvN = rho * std::max(-FN, 0.0);
+        cvS = rho * std::max(FS, 0.0);
+      }
+      double alN = 0.0, alS = 0.0;
+      if (c.r_al) { alN = c.r_al[k] * (dx / dy); alS = c.r_al[m.id(i, j - 1)] * (dx / dy); }
+      Q.vW[k] = cWv + cvW;
+      Q.vE[k] = cEv + cvE;
+      Q.vS[k] = cS + cvS + alS;
+      Q.vN[k] = cN + cvN + alN;
+      double aP = Dv + dwx + cd + 0.0 + 0.0 + cWv + cEv + cS + cN + alS + alN;
+      if (aP <= 1.0e-15) aP = 1.0;
+      Q.vP[k] = aP;
+    }
+  // 3 & 4. Schur stencil (:1542-1590), from the blocks' diagonals
+  if (!c.mono) return;
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      size_t k = m.id(i, j);
+      if (!(i == 1 && is_wall(prm, L))) Q.sW[k] = (dy * dy) / std::max(1.0e-30, Q.uP[m.id(i, j)]);
+      if (!(i == nx && is_wall(prm, R))) Q.sE[k] = (dy * dy) / std::max(1.0e-30, Q.uP[m.id(i + 1, j)]);
+      if (!(j == 1 && is_wall(prm, B))) Q.sS[k] = (dx * dx) / std::max(1.0e-30, Q.vP[m.id(i, j)]);
+      if (!(j == ny && is_wall(prm, T))) Q.sN[k] = (dx * dx) / std::max(1.0e-30, Q.vP[m.id(i, j + 1)]);
+      const double reg = (i == 1 && j == 1) ? 1.0e-10 * dvol : 1.0e-12 * dvol;
+      Q.sP[k] = Q.sW[k] + Q.sE[k] + Q.sS[k] + Q.sN[k] + 0.0 + reg;
+    }
+}
+
+// src/module_linear_solvers.f90:1278-1401 ssor_solve_p / _u / _v: r = 0,
+// then n_sweeps pairs of lexicographic Gauss-Seidel sweeps (rows j = 1..nj,
+// columns i = 1..ni, then the reverse), each cell relaxed
+// r = (1 - omega) r + omega (z + sum of the non-zero a_nb r_nb) / aP.
+// Ghost entries of r stay zero (one rank, no halo exchange).
+void ssor_solve(const Mesh& m, int ni, int nj, const double* aW, const double* aE, const double* aS,
+                const double* aN, const double* aP, const double* z, double* r, int n_sweeps, double omega) {
+  const size_t g = (size_t)(m.nx + 2) * (m.ny + 2);
+  std::fill(r, r + g, 0.0);
+  auto cell = [&](int i, int j) {
+    const size_t k = m.id(i, j);
+    double d = aP[k];
+    if (std::fabs(d) < 1.0e-30) d = 1.0;
+    double val = z[k];
+    if (aW[k] != 0.0) val = val + aW[k] * r[k - 1];
+    if (aE[k] != 0.0) val = val + aE[k] * r[k + 1];
+    if (aS[k] != 0.0) val = val + aS[k] * r[k - m.P];
+    if (aN[k] != 0.0) val = val + aN[k] * r[k + m.P];
+    r[k] = (1.0 - omega) * r[k] + omega * (val / d);
+  };
+  for (int s = 0; s < n_sweeps; ++s) {
+    for (int j = 1; j <= nj; ++j)
+      for (int i = 1; i <= ni; ++i) cell(i, j);
+    for (int j = nj; j >= 1; --j)
+      for (int i = ni; i >= 1; --i) cell(i, j);
+  }
+}
+
+inline bool uses_sweeps(const covof_params* prm) {
+  return prm->use_precond && (prm->precond == COVOF_PRECOND_SSOR || prm->precond == COVOF_PRECOND_BLOCK_TRIANGULAR);
+}
+
 // Packed Krylov vectors: u DOFs (i=1..u_nx, j=1..ny) then v DOFs
 // (i=1..nx, j=1..v_ny), src/module_navier_stokes.f90:231-296.
 // MONOLITHIC adds the pressure DOFs (i=1..nx, j=1..ny) after them
@@ -916,6 +1082,7 @@ struct Krylov {
   const MomCtx& c;
   Packer pk;
   std::vector<double> tu, tv, yu, yv, tp, yp, diag;  // tf (saved operand), diag packed
+  PBlocks blk;  // SSOR / BLOCK_TRIANGULAR stencils (prec_blocks)
   explicit Krylov(const MomCtx& cc) : c(cc), pk{cc} {
     size_t g = (size_t)(c.m.nx + 2) * (c.m.ny + 2);
     tu.assign(g, 0.0); tv.assign(g, 0.0); yu.assign(g, 0.0); yv.assign(g, 0.0);
@@ -933,15 +1100,67 @@ struct Krylov {
       pk.pack(yu.data(), yv.data(), y);
     }
   }
-  // src/module_linear_solvers.f90:88-117 (JACOBI) / :280-304 (ILU0 = same)
+  // src/module_linear_solvers.f90:88-117 (JACOBI) / :280-304 (ILU0 = same),
+  // :137-278 (SSOR, BLOCK_TRIANGULAR)
   void M(const double* src, double* dst) {
     size_t n = pk.n();
-    bool on = c.prm->use_precond && (c.prm->precond == COVOF_PRECOND_JACOBI ||
-                                     c.prm->precond == COVOF_PRECOND_ILU0);
+    const int pc = c.prm->use_precond ? c.prm->precond : COVOF_PRECOND_NONE;
+    if (pc == COVOF_PRECOND_SSOR || pc == COVOF_PRECOND_BLOCK_TRIANGULAR) { sweeps(src, dst, pc); return; }
+    bool on = pc == COVOF_PRECOND_JACOBI || pc == COVOF_PRECOND_ILU0;
     for (size_t q = 0; q < n; ++q) {
       double d = diag[q];
       dst[q] = (on && std::fabs(d) > 1.0e-15) ? src[q] / d : src[q];
     }
+  }
+  // SSOR: two symmetric sweeps with omega = 1 on each block (the Schur
+  // stencil for the pressure).  BLOCK_TRIANGULAR with MONOLITHIC: twelve
+  // sweeps with omega = 1.25 on the Schur complement, its mean removed, then
+  // four sweeps on each velocity block with the right-hand side z - B^T r_p
+  // (wall DOFs keep z); without MONOLITHIC it is the SSOR of the velocity
+  // blocks (:265-276).
+  void sweeps(const double* src, double* dst, int pc) {
+    const Mesh& m = c.m;
+    const size_t g = (size_t)(m.nx + 2) * (m.ny + 2);
+    const int nx = m.nx, ny = m.ny, u_nx = c.u_nx, v_ny = c.v_ny;
+    std::vector<double> zu(g, 0.0), zv(g, 0.0), zp(g, 0.0), ru(g), rv(g), rp(g, 0.0);
+    pk.unpack(src, zu.data(), zv.data(), zp.data());
+    const PBlocks& Q = blk;
+    if (pc == COVOF_PRECOND_SSOR || !c.mono) {
+      ssor_solve(m, u_nx, ny, Q.uW.data(), Q.uE.data(), Q.uS.data(), Q.uN.data(), Q.uP.data(), zu.data(),
+                 ru.data(), 2, 1.0);
+      ssor_solve(m, nx, v_ny, Q.vW.data(), Q.vE.data(), Q.vS.data(), Q.vN.data(), Q.vP.data(), zv.data(),
+                 rv.data(), 2, 1.0);
+      if (c.mono)
+        ssor_solve(m, nx, ny, Q.sW.data(), Q.sE.data(), Q.sS.data(), Q.sN.data(), Q.sP.data(), zp.data(),
+                   rp.data(), 2, 1.0);
+      pk.pack(ru.data(), rv.data(), dst, rp.data());
+      return;
+    }
+    ssor_solve(m, nx, ny, Q.sW.data(), Q.sE.data(), Q.sS.data(), Q.sN.data(), Q.sP.data(), zp.data(),
+               rp.data(), 12, 1.25);
+    double sum = 0.0;
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) sum += rp[m.id(i, j)];
+    const double mean = sum / (double)((long long)nx * ny);
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) rp[m.id(i, j)] = rp[m.id(i, j)] - mean;
+    std::vector<double> hu(g, 0.0), hv(g, 0.0);
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= u_nx; ++i) {
+        const size_t k = m.id(i, j);
+        hu[k] = (i == 1 || i == u_nx) ? zu[k] : zu[k] - (rp[k] - rp[k - 1]) * m.dy;
+      }
+    ssor_solve(m, u_nx, ny, Q.uW.data(), Q.uE.data(), Q.uS.data(), Q.uN.data(), Q.uP.data(), hu.data(),
+               ru.data(), 4, 1.0);
+    for (int j = 1; j <= v_ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        const size_t k = m.id(i, j);
+        const bool wall = (j == 1 && is_wall(c.prm, B)) || (j == v_ny && is_wall(c.prm, T));
+        hv[k] = wall ? zv[k] : zv[k] - (rp[k] - rp[k - m.P]) * m.dx;
+      }
+    ssor_solve(m, nx, v_ny, Q.vW.data(), Q.vE.data(), Q.vS.data(), Q.vN.data(), Q.vP.data(), hv.data(),
+               rv.data(), 4, 1.0);
+    pk.pack(ru.data(), rv.data(), dst, rp.data());
   }
   void PA(const double* src, double* dst) {  // apply_PA (:323-356)
     std::vector<double> tmp(pk.n());
@@ -1142,6 +1361,7 @@ int predictor(const covof_params* prm, double dt, double* u, double* v, const do
   mom_diag(c, du.data(), dv.data());
   K.diag.resize(K.pk.n());
   K.pk.pack(du.data(), dv.data(), K.diag.data());
+  if (uses_sweeps(prm)) prec_blocks(c, K.blk);
   mom_rhs(c, mu_node, fx, fy, u_old, v_old, ru.data(), rv.data());
   std::vector<double> rhs(K.pk.n()), x(K.pk.n());
   K.pk.pack(ru.data(), rv.data(), rhs.data());
@@ -1246,6 +1466,7 @@ int al_step(const covof_params* prm, double dt, double* u, double* v, double* p,
   mom_diag(c, du.data(), dv.data());
   K.diag.resize(K.pk.n());
   K.pk.pack(du.data(), dv.data(), K.diag.data());
+  if (uses_sweeps(prm)) prec_blocks(c, K.blk);
   const int umax = prm->uzawa_iter > 0 ? prm->uzawa_iter : 1;
   int total = 0, st = COVOF_OK, m_done = 0;
   for (int mi = 1; mi <= umax; ++mi) {
@@ -1300,6 +1521,7 @@ int mono_step(const covof_params* prm, double dt, double* u, double* v, double* 
   schur_diag(c, du.data(), dv.data(), dp.data());
   K.diag.resize(K.pk.n());
   K.pk.pack(du.data(), dv.data(), K.diag.data(), dp.data());
+  if (uses_sweeps(prm)) prec_blocks(c, K.blk);
   mom_rhs(c, mu_node, fx, fy, hist.u_old, hist.v_old, ru.data(), rv.data());
   std::vector<double> rhs(K.pk.n()), x(K.pk.n());
   K.pk.pack(ru.data(), rv.data(), rhs.data(), nullptr);
@@ -1946,8 +2168,6 @@ int check_mom(const covof_params* prm, const double* u_old, const double* u_nm1,
   if (prm->convective_scheme != COVOF_CONV_UPWIND && prm->convective_scheme != COVOF_CONV_CENTERED &&
       prm->convective_scheme != COVOF_CONV_TVD_SUPERBEE)
     return COVOF_UNSUPPORTED;
-  if (prm->use_precond && (prm->precond == COVOF_PRECOND_SSOR || prm->precond == COVOF_PRECOND_BLOCK_TRIANGULAR))
-    return COVOF_UNSUPPORTED;
   if (prm->convective_linearization == COVOF_CONV_LIN_AB2 && !u_old) return COVOF_INVALID;
   if (has_nm1 && !u_nm1 && (prm->time_scheme == COVOF_TIME_GEAR ||
                             prm->convective_linearization == COVOF_CONV_LIN_AB2))
@@ -2007,6 +2227,61 @@ int orc_schur_diag(const covof_params* prm, double dt, const double* du, const d
   if (st) return st;
   MomCtx c = make_ctx(prm, dt, du, dv, du, dv, du, du);
   schur_diag(c, du, dv, dp);
+  return COVOF_OK;
+}
+
+// The Krylov preconditioner M^-1 of the configured precond (JACOBI / ILU0 /
+// SSOR / BLOCK_TRIANGULAR, or none) on (zu, zv[, zp]) -> (yu, yv[, yp]),
+// assembled from the fields as the solve would (r_al: the AL penalty field
+// for AUGMENTED_LAGRANGIAN / AAL, else nullptr).
+int orc_precond_apply(const covof_params* prm, double dt, const double* zu, const double* zv, const double* zp,
+                      double* yu, double* yv, double* yp, const double* u_n, const double* v_n,
+                      const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                      const double* u_old, const double* v_old, const double* u_nm1, const double* v_nm1,
+                      int has_nm1, const double* r_al) {
+  int st = check_params(prm, false);
+  if (st) return st;
+  if ((st = check_mom(prm, u_old, u_nm1, has_nm1))) return st;
+  MomCtx c = make_ctx(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node, hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1));
+  const bool al = prm->solver_type == COVOF_SOLVER_AUGMENTED_LAGRANGIAN || prm->solver_type == COVOF_SOLVER_AAL;
+  if (al) c.r_al = r_al;
+  c.mono = prm->solver_type == COVOF_SOLVER_MONOLITHIC;
+  c.np = c.mono ? (size_t)prm->nx * prm->ny : 0;
+  const size_t g = (size_t)(prm->nx + 2) * (prm->ny + 2);
+  Krylov K(c);
+  std::vector<double> du(g, 1.0), dv(g, 1.0), dp(g, 1.0);
+  mom_diag(c, du.data(), dv.data());
+  if (c.mono) schur_diag(c, du.data(), dv.data(), dp.data());
+  K.diag.resize(K.pk.n());
+  K.pk.pack(du.data(), dv.data(), K.diag.data(), dp.data());
+  if (uses_sweeps(prm)) prec_blocks(c, K.blk);
+  std::vector<double> z(K.pk.n()), y(K.pk.n());
+  K.pk.pack(zu, zv, z.data(), zp);
+  K.M(z.data(), y.data());
+  K.pk.unpack(y.data(), yu, yv, yp);
+  return COVOF_OK;
+}
+
+// The sweep preconditioners' stencils: out holds 15 arrays of (nx+2)*(ny+2)
+// doubles, u W E S N P, v W E S N P, Schur W E S N P (the Schur ones for
+// MONOLITHIC only, else W..N zero and P one).
+int orc_prec_blocks(const covof_params* prm, double dt, const double* u_n, const double* v_n,
+                    const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                    const double* u_old, const double* v_old, const double* u_nm1, const double* v_nm1,
+                    int has_nm1, const double* r_al, double* out) {
+  int st = check_params(prm, false);
+  if (st) return st;
+  if ((st = check_mom(prm, u_old, u_nm1, has_nm1))) return st;
+  MomCtx c = make_ctx(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node, hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1));
+  const bool al = prm->solver_type == COVOF_SOLVER_AUGMENTED_LAGRANGIAN || prm->solver_type == COVOF_SOLVER_AAL;
+  if (al) c.r_al = r_al;
+  c.mono = prm->solver_type == COVOF_SOLVER_MONOLITHIC;
+  PBlocks Q;
+  prec_blocks(c, Q);
+  const size_t g = (size_t)(prm->nx + 2) * (prm->ny + 2);
+  const std::vector<double>* arr[15] = {&Q.uW, &Q.uE, &Q.uS, &Q.uN, &Q.uP, &Q.vW, &Q.vE, &Q.vS, &Q.vN, &Q.vP,
+                                        &Q.sW, &Q.sE, &Q.sS, &Q.sN, &Q.sP};
+  for (int q = 0; q < 15; ++q) std::memcpy(out + q * g, arr[q]->data(), g * sizeof(double));
   return COVOF_OK;
 }
 

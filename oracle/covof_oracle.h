@@ -76,6 +76,18 @@ int orc_mono_apply(const covof_params* prm, double dt, const double* xu, const d
                    const double* u_old, const double* v_old, const double* u_nm1, const double* v_nm1,
                    int has_nm1);
 int orc_schur_diag(const covof_params* prm, double dt, const double* du, const double* dv, double* dp);
+/* the SSOR / BLOCK_TRIANGULAR stencils: 15 arrays (u, v, Schur; W E S N P) */
+int orc_prec_blocks(const covof_params* prm, double dt, const double* u_n, const double* v_n,
+                    const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                    const double* u_old, const double* v_old, const double* u_nm1, const double* v_nm1,
+                    int has_nm1, const double* r_al, double* out);
+/* the Krylov preconditioner M^-1 of prm->precond on (zu, zv, zp) (zp, yp:
+ * MONOLITHIC only); r_al: the AL penalty field or NULL */
+int orc_precond_apply(const covof_params* prm, double dt, const double* zu, const double* zv, const double* zp,
+                      double* yu, double* yv, double* yp, const double* u_n, const double* v_n,
+                      const double* rho_u, const double* rho_v, const double* mu, const double* mu_node,
+                      const double* u_old, const double* v_old, const double* u_nm1, const double* v_nm1,
+                      int has_nm1, const double* r_al);
 int orc_momentum_diag(const covof_params* prm, double dt, const double* u_n, const double* v_n,
                       const double* rho_u, const double* rho_v, const double* mu,
                       const double* mu_node, double* diag_u, double* diag_v, const double* u_old,

@@ -58,6 +58,8 @@ def lib():
             "orc_mono_step": (i, [v, d] + [v] * 13 + [i, v]),
             "orc_mono_apply": (i, [v, d] + [v] * 16 + [i]),
             "orc_schur_diag": (i, [v, d, v, v, v]),
+            "orc_precond_apply": (i, [v, d] + [v] * 16 + [i, v]),
+            "orc_prec_blocks": (i, [v, d] + [v] * 10 + [i, v, v]),
             "orc_diffusion_smooth": (i, [v, v, v]),
         }
         for name, (res, args) in sig.items():
@@ -154,6 +156,28 @@ def mono_apply(prm, dt, xu, xv, xp, u_n, v_n, rho_u, rho_v, mu, mu_node, u_old=N
                               _p(u_nm1), _p(v_nm1), int(has_nm1))
     assert st == 0, st
     return yu, yv, yp
+
+
+def precond_apply(prm, dt, zu, zv, zp, u_n, v_n, rho_u, rho_v, mu, mu_node, u_old=None, v_old=None,
+                  u_nm1=None, v_nm1=None, has_nm1=0, r_al=None):
+    """M^-1 of prm.precond on (zu, zv, zp); returns (yu, yv, yp)."""
+    yu, yv, yp = np.zeros_like(zu), np.zeros_like(zv), np.zeros_like(zp)
+    st = lib().orc_precond_apply(_params(prm), dt, _p(zu), _p(zv), _p(zp), _p(yu), _p(yv), _p(yp), _p(u_n),
+                                 _p(v_n), _p(rho_u), _p(rho_v), _p(mu), _p(mu_node), _p(u_old), _p(v_old),
+                                 _p(u_nm1), _p(v_nm1), int(has_nm1), _p(r_al))
+    assert st == 0, st
+    return yu, yv, yp
+
+
+def prec_blocks(prm, dt, u_n, v_n, rho_u, rho_v, mu, mu_node, u_old=None, v_old=None, u_nm1=None,
+                v_nm1=None, has_nm1=0, r_al=None):
+    """The sweep preconditioners' stencils: dict block -> dict W/E/S/N/P arrays."""
+    shape = u_n.shape
+    out = np.zeros((15,) + shape)
+    st = lib().orc_prec_blocks(_params(prm), dt, _p(u_n), _p(v_n), _p(rho_u), _p(rho_v), _p(mu), _p(mu_node),
+                               _p(u_old), _p(v_old), _p(u_nm1), _p(v_nm1), int(has_nm1), _p(r_al), _p(out))
+    assert st == 0, st
+    return {b: {c: out[5 * q + k] for k, c in enumerate("WESNP")} for q, b in enumerate("uvs")}
 
 
 def schur_diag(prm, dt, du, dv):

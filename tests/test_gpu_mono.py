@@ -102,16 +102,6 @@ def test_resident_steps_match_oracle(gpu_pkg, orc, graph, scheme):
     _close(g, f, p.nx, p.ny)
 
 
-@pytest.mark.parametrize("prec", ["PRECOND_SSOR", "PRECOND_BLOCK_TRIANGULAR"])
-def test_sequential_preconditioners_are_refused(gpu_pkg, orc, prec):
-    pkg = gpu_pkg
-    p, f, dt = _cavity(pkg, orc, 16)
-    p.precond = getattr(pkg.capi, prec)
-    with pkg.Solver(p) as s:
-        with pytest.raises(Exception):
-            s.monolithic_step(dt, f, has_nm1=0)
-
-
 def test_batch_rejects_monolithic(gpu_pkg):
     pkg = gpu_pkg
     cases = pkg.cases.droplet_batch(n_cases=2, seed=3, sizes=(32,), nsub=4)

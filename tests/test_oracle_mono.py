@@ -132,14 +132,6 @@ def test_krylov_matches_a_dense_solve(pkg, orc):
     assert np.abs(pk_ - pd_).max() < 1e-6 * np.abs(pd_).max()
 
 
-@pytest.mark.parametrize("prec", ["PRECOND_SSOR", "PRECOND_BLOCK_TRIANGULAR"])
-def test_sequential_preconditioners_are_refused(pkg, orc, prec):
-    p, f, dt = _cavity(pkg, orc)
-    p.precond = getattr(pkg.capi, prec)
-    it, st = orc.mono_step(p, dt, f, 0)
-    assert st == pkg.capi.UNSUPPORTED
-
-
 def test_cavity_time_loop(pkg, orc):
     """Three coupled steps of the driven cavity converge; the lid drags the
     top row forward and the flow stays discretely divergence-free to the
