@@ -380,10 +380,11 @@ int pois_pre(covof_handle* h, double dt, const double* u, const double* v, const
              const double* rho_u, const double* rho_v, double* p, PoissonArgs* out) {
   const covof_params& P = h->prm;
   if (!rho_u || !rho_v || !p || (!b && (!u || !v))) return COVOF_INVALID;
-  if (P.p_precond == COVOF_PRECOND_SSOR) return COVOF_UNSUPPORTED;
+  const bool mixed = P.p_precision == COVOF_PREC_MIXED;
+  // the symmetric Gauss-Seidel preconditioner belongs to the FP64 PCG
+  if (P.p_precond == COVOF_PRECOND_SSOR && mixed) return COVOF_UNSUPPORTED;
   CS(ensure_poisson(h));
   CS(poisson_plan(h));
-  const bool mixed = P.p_precision == COVOF_PREC_MIXED;
   const int pinned = P.p_gauge == COVOF_GAUGE_PINNED;
   const dim3 blk(32, 8), grd = grid2(P.nx, P.ny, blk);
   k_poisson_assemble<<<grd, blk, 0, h->stream>>>(h->D, dt, P.dx, P.dy, wall_flags(P), rho_u, rho_v, u, v,
@@ -425,6 +426,13 @@ int poisson_enqueue(covof_handle* h, double dt, const double* u, const double* v
                     const double* rho_u, const double* rho_v, double* p, bool timed) {
   PoissonArgs a;
   CS(pois_pre(h, dt, u, v, b, rho_u, rho_v, p, &a));
+  if (h->prm.p_precond == COVOF_PRECOND_SSOR) {
+    // FP64 PCG with the Gauss-Seidel sweep pair, iterated from the host
+    if (timed) CK(cudaEventRecord(h->ev0, h->stream));
+    CS(pcg_sgs(h, a));
+    if (timed) CK(cudaEventRecord(h->ev1, h->stream));
+    return pois_post(h, p);
+  }
   void* args[] = {&a};
   if (h->p_cluster) CS(launch_cluster(h, h->p_fn, h->p_nb, h->p_threads, args, timed, h->p_smem));
   else CS(launch_coop(h, h->p_fn, h->p_nb, h->p_threads, args, timed, h->p_smem));
@@ -1082,14 +1090,14 @@ int capture_steps(covof_handle* h, double dt) {
 int run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run_stats* out) {
   if (nsteps < 0 || !(dt > 0.0)) return COVOF_INVALID;
   const covof_params& P = h->prm;
-  if (P.p_precond == COVOF_PRECOND_SSOR) return COVOF_UNSUPPORTED;
+  if (P.p_precond == COVOF_PRECOND_SSOR && P.p_precision == COVOF_PREC_MIXED) return COVOF_UNSUPPORTED;
   CS(check_mom_params(P));
   CS(check_coupling(P));
   // the Uzawa exit test reads a scalar back per iteration: eager steps
   h->al_check = is_al(P) && P.uzawa_iter > 1 && P.uzawa_tol > 0.0;
   if (h->al_check) flags &= ~COVOF_RUN_GRAPH;
   // the sweep preconditioners' Krylov iterations are driven from the host
-  if (uses_sweeps(P)) flags &= ~COVOF_RUN_GRAPH;
+  if (uses_sweeps(P) || P.p_precond == COVOF_PRECOND_SSOR) flags &= ~COVOF_RUN_GRAPH;
   // every buffer and launch plan exists before a capture starts
   CS(ensure_fields(h));
   CS(ensure_poisson(h));

@@ -200,6 +200,7 @@ int prec_blocks_dev(covof_handle* h, const MomArgs& a);
 int sweep_precond(covof_handle* h, const MomArgs& a, const double* src, double* dst);
 int sweep_solve(covof_handle* h, const MomArgs& a);
 int precond_apply_dev(covof_handle* h, const MomArgs& a, const double* src, double* dst);
+int pcg_sgs(covof_handle* h, const PoissonArgs& a);
 
 }  // namespace host
 }  // namespace covof

@@ -91,13 +91,29 @@ __device__ bool ssor_band(const SsorArgs& A, const SsorJob& J, int s, int b) {
         double vW, vE, vS, vN;
         if (fwd) { vW = back; vE = o.e; vS = back_row; vN = o.n; }
         else     { vE = back; vW = o.e; vN = back_row; vS = o.n; }
-        double val = o.z;
-        if (o.W != 0.0) val = val + o.W * vW;
-        if (o.E != 0.0) val = val + o.E * vE;
-        if (o.S != 0.0) val = val + o.S * vS;
-        if (o.N != 0.0) val = val + o.N * vN;
-        const double d = fabs(o.P) < 1.0e-30 ? 1.0 : o.P;
-        const double v = om1 * o.c + omega * div_rcp(val, d, o.y);
+        double v;
+        if (J.kind == 0) {
+          double val = o.z;
+          if (o.W != 0.0) val = val + o.W * vW;
+          if (o.E != 0.0) val = val + o.E * vE;
+          if (o.S != 0.0) val = val + o.S * vS;
+          if (o.N != 0.0) val = val + o.N * vN;
+          const double d = fabs(o.P) < 1.0e-30 ? 1.0 : o.P;
+          v = om1 * o.c + omega * div_rcp(val, d, o.y);
+        } else {
+          double val;
+          if (fwd) {
+            val = o.z;
+            if (i > 1) val = val + o.W * vW;
+            if (j > 1) val = val + o.S * vS;
+          } else {
+            val = o.P * o.c;
+            if (i < ni) val = val + o.E * vE;
+            if (j < nj) val = val + o.N * vN;
+          }
+          v = div_rcp(val, o.P, o.y);
+          if (J.pin && i == 1 && j == 1) v = 0.0;
+        }
         __stcg(J.r + k, v);
         prev = v;
       }
@@ -229,6 +245,15 @@ __global__ void __launch_bounds__(kDotThreads) k_dots_final(int nparts, const do
     for (int p = 0; p < kDotMax; ++p) out[p] = acc[p];
 }
 
+// Zero the ghost ring of a field-layout array (so flat reductions over it
+// see the cells only).
+__global__ void k_zero_ghosts(Dims D, double* __restrict__ a) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int W = D.nx + 2, H = D.ny + 2;
+  if (t < W) { a[D.id(t, 0)] = 0.0; a[D.id(t, H - 1)] = 0.0; }
+  if (t < H) { a[D.id(0, t)] = 0.0; a[D.id(W - 1, t)] = 0.0; }
+}
+
 // BLOCK_TRIANGULAR, after the Schur solve: r_p -= mean(r_p) over the cells
 // (sum: the block's total, its ghost entries are zero).
 __global__ void k_bt_center(Dims D, double* __restrict__ rp, const double* __restrict__ sum) {
@@ -338,6 +363,7 @@ int launch_ssor(covof_handle* h, SsorJob* jobs, int njob) {
 SsorJob job(const Stencil& st, const double* z, double* r, int ni, int nj, int sweeps, double omega) {
   SsorJob j;
   j.st = st; j.z = z; j.r = r; j.ni = ni; j.nj = nj; j.sweeps = sweeps; j.omega = omega; j.prog = nullptr;
+  j.kind = 0; j.pin = 0;
   return j;
 }
 
@@ -376,6 +402,26 @@ int sweep_precond(covof_handle* h, const MomArgs& a, const double* src, double* 
 
 namespace {
 
+// Up to five dot products over n flat entries (y = nullptr: the plain sum
+// of x), read back to the host; also reads the kernels' error flag.
+int read_dots(covof_handle* h, size_t n, std::initializer_list<std::pair<const double*, const double*>> prs,
+              double* out) {
+  SweepKit& K = h->sweep;
+  DotSet d{};
+  d.np = 0;
+  for (auto& p : prs) { d.x[d.np] = p.first; d.y[d.np] = p.second; ++d.np; }
+  k_dots<<<K.dot_blocks, kDotThreads, 0, h->stream>>>(n, d, K.part);
+  k_dots_final<<<1, kDotThreads, 0, h->stream>>>(K.dot_blocks, K.part, K.dsum);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(K.hdot, K.dsum, kDotMax * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, h->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CS(sync(h));
+  if (e != 0) return COVOF_TIMEOUT;
+  for (int p = 0; p < d.np; ++p) out[p] = K.hdot[p];
+  return COVOF_OK;
+}
+
 // The host-driven Krylov state: the persistent kernels' vectors (a.x, a.v*)
 // plus the handle's sweep scratch.
 struct HostKrylov {
@@ -403,20 +449,7 @@ struct HostKrylov {
   // up to five dot products (y = nullptr: plain sum), read back; also reads
   // the kernels' error flag
   int dots(std::initializer_list<std::pair<const double*, const double*>> prs, double* out) {
-    SweepKit& K = h->sweep;
-    DotSet d{};
-    d.np = 0;
-    for (auto& p : prs) { d.x[d.np] = p.first; d.y[d.np] = p.second; ++d.np; }
-    k_dots<<<K.dot_blocks, kDotThreads, 0, h->stream>>>(n, d, K.part);
-    k_dots_final<<<1, kDotThreads, 0, h->stream>>>(K.dot_blocks, K.part, K.dsum);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(K.hdot, K.dsum, kDotMax * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    int e = 0;
-    CK(cudaMemcpyAsync(&e, h->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    CS(sync(h));
-    if (e != 0) return COVOF_TIMEOUT;
-    for (int p = 0; p < d.np; ++p) out[p] = K.hdot[p];
-    return COVOF_OK;
+    return read_dots(h, n, prs, out);
   }
 };
 
@@ -629,6 +662,86 @@ int sweep_solve(covof_handle* h, const MomArgs& a) {
   if (st == COVOF_CUDA_ERROR || st == COVOF_TIMEOUT) return st;
   *h->h_kres = KrylovResult{it, st};
   CK(cudaMemcpyAsync(h->d_kres, h->h_kres, sizeof(KrylovResult), cudaMemcpyHostToDevice, h->stream));
+  return sync(h);
+}
+
+// The pressure Poisson's PCG with the symmetric Gauss-Seidel preconditioner
+// (p_precond SSOR; src/module_simulation.f90:2587-2758), FP64, iterated
+// from the host around the wavefront sweep pair: the recurrences, stopping
+// test and gauge handling of the Jacobi-PCG kernel (pinned cell held at
+// zero; otherwise the mean removed at the end).  Writes the result record to
+// the device.
+int pcg_sgs(covof_handle* h, const PoissonArgs& a) {
+  CS(ensure_sweeps(h));
+  const Dims D = h->D;
+  const size_t g = h->g;
+  const int nx = D.nx, ny = D.ny;
+  const int pin = a.pinned ? D.id(1, 1) : -1;
+  double *x = a.x, *r = a.r, *z = a.z, *d = a.d, *Ad = a.Ad;
+  const double* b = a.b;
+  CK(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
+  const int zg = (nx + 2 > ny + 2 ? nx + 2 : ny + 2);
+  k_zero_ghosts<<<(zg + 255) / 256, 256, 0, h->stream>>>(D, x);
+  for (double* v : {r, z, d, Ad}) CK(cudaMemsetAsync(v, 0, g * sizeof(double), h->stream));
+  const int grid = 4 * h->sm_count;
+  const dim3 blk(32, 8), gc((nx + 31) / 32, (ny + 7) / 8);
+  auto matvec = [&](const double* in, double* out) -> int {
+    k_poisson_apply<<<gc, blk, 0, h->stream>>>(D, in, out, a.ax, a.ay, a.aP);
+    if (pin >= 0) CK(cudaMemsetAsync(out + pin, 0, sizeof(double), h->stream));
+    CK(cudaGetLastError());
+    return COVOF_OK;
+  };
+  SsorJob J = job(Stencil{const_cast<double*>(a.ax), const_cast<double*>(a.ax) + 1, const_cast<double*>(a.ay),
+                          const_cast<double*>(a.ay) + D.P, const_cast<double*>(a.aP), const_cast<double*>(a.invD)},
+                  r, z, nx, ny, 1, 1.0);
+  J.kind = 1;
+  J.pin = a.pinned;
+  auto vop = [&](int op, double* y, const double* x0, const double* x1, double c0) {
+    k_vop<<<grid, 256, 0, h->stream>>>(op, g, y, x0, x1, c0, 0.0);
+  };
+  CS(matvec(x, Ad));
+  vop(kSub, r, b, Ad, 0.0);
+  double t[5];
+  CS(read_dots(h, g, {{b, b}, {r, r}}, t));
+  double b_norm = sqrt(t[0]);
+  if (b_norm < 1.0e-30) b_norm = 1.0;
+  double r_norm = sqrt(t[1]);
+  int iters = 0, status = COVOF_OK;
+  bool converged = false;
+  if (r_norm / b_norm > a.tol) {
+    CS(launch_ssor(h, &J, 1));
+    vop(kCopy, d, z, nullptr, 0.0);
+    CS(read_dots(h, g, {{r, z}}, t));
+    double rz_old = t[0];
+    for (int it = 1; it <= a.max_iter; ++it) {
+      iters = iters + 1;
+      CS(matvec(d, Ad));
+      CS(read_dots(h, g, {{d, Ad}}, t));
+      if (fabs(t[0]) < 1.0e-35) { status = COVOF_BREAKDOWN; break; }
+      const double alpha = rz_old / t[0];
+      vop(kAxpy, x, d, nullptr, alpha);
+      vop(kAxpy, r, Ad, nullptr, -alpha);
+      CS(read_dots(h, g, {{r, r}}, t));
+      r_norm = sqrt(t[0]);
+      if (r_norm != r_norm) { status = COVOF_NAN; break; }
+      if (r_norm / b_norm <= a.tol) { converged = true; break; }
+      CS(launch_ssor(h, &J, 1));
+      CS(read_dots(h, g, {{r, z}}, t));
+      if (fabs(rz_old) < 1.0e-35) { status = COVOF_BREAKDOWN; break; }
+      const double beta = t[0] / rz_old;
+      rz_old = t[0];
+      vop(kXpby, d, z, nullptr, beta);
+    }
+    if (status == COVOF_OK && !converged) status = COVOF_MAXITER;
+  }
+  if (!a.pinned) {
+    CS(read_dots(h, g, {{x, nullptr}}, t));
+    CK(cudaMemcpyAsync(h->sweep.dsum, &t[0], sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    k_bt_center<<<gc, blk, 0, h->stream>>>(D, x, h->sweep.dsum);
+    CK(cudaGetLastError());
+  }
+  *h->h_pres = PcgResult{iters, status, 0, 0, r_norm / b_norm};
+  CK(cudaMemcpyAsync(h->d_pres, h->h_pres, sizeof(PcgResult), cudaMemcpyHostToDevice, h->stream));
   return sync(h);
 }
 

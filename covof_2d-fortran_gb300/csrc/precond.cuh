@@ -18,6 +18,12 @@ struct SsorJob {
   int sweeps;          // symmetric pairs
   double omega;
   unsigned int* prog;  // per band (stride 32): chunks published, zero at launch
+  // kind 0: the relaxed sweeps above.  kind 1: the pressure Poisson's
+  // symmetric Gauss-Seidel pair (src/module_simulation.f90:2709-2758):
+  // forward r = (z + aW r_W + aS r_S) / aP, backward
+  // r = (aP r + aE r_E + aN r_N) / aP, neighbours inside the domain only;
+  // pin: cell (1,1) held at zero (the pinned gauge)
+  int kind, pin;
 };
 
 // Independent solves run side by side in one launch.

@@ -48,9 +48,9 @@ enum { COVOF_BC_DIRICHLET = 1, COVOF_BC_NEUMANN = 2, COVOF_BC_PERIODIC = 3, COVO
 enum { COVOF_LINEAR_BICGSTAB2 = 1, COVOF_LINEAR_BICGSTAB = 2, COVOF_LINEAR_CG = 3 };
 /* Preconditioners: PRECOND_* in src/module_constants.f90:67-72.
  * ILU0 is the same diagonal scaling as JACOBI in the reference
- * (src/module_linear_solvers.f90:280-304).  SSOR is accepted for the pressure
- * Poisson only, where it names the reference's symmetric Gauss-Seidel sweep
- * pair (src/module_simulation.f90:2709-2758).  In the momentum / coupled
+ * (src/module_linear_solvers.f90:280-304).  For the pressure Poisson
+ * (p_precond) SSOR names the reference's symmetric Gauss-Seidel sweep pair
+ * (src/module_simulation.f90:2709-2758).  In the momentum / coupled
  * Krylov solves SSOR is two symmetric lexicographic sweeps per block and
  * BLOCK_TRIANGULAR the Schur-complement sweeps then the velocity sweeps
  * (src/module_linear_solvers.f90:137-278); their Krylov iterations are driven
@@ -114,7 +114,8 @@ typedef struct covof_params {
   int enable_convection;
   int convective_scheme;
   /* pressure Poisson */
-  int p_precond;         /* JACOBI (GPU and oracle) or SSOR (oracle only) */
+  int p_precond;         /* JACOBI, or SSOR: the symmetric Gauss-Seidel pair (FP64 only;
+                            the PCG then iterates from the host, steps run eagerly) */
   int p_max_iter;
   int p_gauge;
   int p_precision;

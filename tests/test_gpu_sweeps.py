@@ -213,3 +213,55 @@ def test_resident_monolithic_block_triangular(gpu_pkg, orc):
         assert stats["graph"] == 0
         s.state_get(g)
     _close(g, f, p.nx, p.ny)
+
+
+@pytest.mark.parametrize("gauge", ["pinned", "reference"])
+@pytest.mark.parametrize("n", [48, 130])
+def test_poisson_gauss_seidel_pcg(gpu_pkg, orc, n, gauge):
+    """The pressure Poisson with p_precond SSOR (the reference's symmetric
+    Gauss-Seidel pair, src/module_simulation.f90:2709-2758): the GPU's
+    wavefront sweeps inside a host-driven FP64 PCG against the oracle."""
+    pkg = gpu_pkg
+    cap = pkg.capi
+    p, b, ru, rv, dt = pkg.cases.poisson_inclusions(n=n, n_incl=12)
+    p.p_gauge = cap.GAUGE_PINNED if gauge == "pinned" else cap.GAUGE_REFERENCE
+    p.p_tol = 1e-12
+    p.p_precond = cap.PRECOND_SSOR
+    p.p_precision = cap.PREC_FP64
+    ref = np.zeros_like(b)
+    it_o, rr_o, st_o = orc.poisson_solve_rhs(p, dt, b, ru, rv, ref)
+    assert st_o == 0
+    x = np.zeros_like(b)
+    with pkg.Solver(p) as s:
+        it, rr, st = s.poisson_solve_rhs(dt, b, ru, rv, x)
+    assert st == cap.OK and rr <= 1e-12
+    assert abs(it - it_o) <= max(2, it_o // 50), (it, it_o)
+    err = np.linalg.norm(x[1:-1, 1:-1] - ref[1:-1, 1:-1]) / np.linalg.norm(ref[1:-1, 1:-1])
+    assert err < 1e-10, err
+
+
+def test_sp_steps_with_gauss_seidel_poisson(gpu_pkg, orc):
+    pkg = gpu_pkg
+    cap = pkg.capi
+    p, C0, dt = pkg.cases.bubble_case(nx=32, ny=64, nsub=4)
+    p.p_precond = cap.PRECOND_SSOR
+    p.p_tol = 1e-12
+    f = pkg.Fields.allocate(p)
+    f.C[...] = C0
+    orc.apply_vof_bc(p, f.C)
+    orc.update_physical_properties(p, f)
+    orc.compute_curvature_and_csf(p, f)
+    g = f.copy()
+    nsteps = 3
+    for k in range(nsteps):
+        it, ip, rr, st = orc.time_step(p, dt, k, f)
+        assert st == 0
+    with pkg.Solver(p) as s:
+        s.state_set(g)
+        st, stats = s.run_steps(dt, nsteps, graph=True)
+        assert st == 0, stats
+        assert stats["graph"] == 0
+        s.state_get(g)
+    for name in ("u", "v", "p"):
+        a, b = getattr(g, name), getattr(f, name)
+        assert _rel(a, b) < (1e-8 if name == "p" else 1e-9), name
