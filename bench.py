@@ -337,6 +337,44 @@ def rt_steps(pkg, orc, nsteps):
             "plain_fp64_ms_per_step_measured_separately": 37000.0}
 
 
+def mono_steps(pkg, orc, n, nsteps, cpu_steps):
+    """The MONOLITHIC coupling on a lid-driven cavity (n x n, Re 100): whole
+    time steps on the resident fields with BiCGSTAB(2) and the
+    BLOCK_TRIANGULAR Schur preconditioner (eager: its Krylov iterations are
+    driven from the host) and with JACOBI (graph-captured); the oracle's
+    serial time loop on the same steps for the CPU side."""
+    import time as _t
+    cap = pkg.capi
+    out = {"workload": f"lid-driven cavity {n}x{n}, Re 100, MONOLITHIC coupling, BiCGSTAB(2) to 1e-10",
+           "steps": nsteps}
+    for name, prec in (("block_triangular", cap.PRECOND_BLOCK_TRIANGULAR), ("jacobi", cap.PRECOND_JACOBI)):
+        p, dt = pkg.cases.cavity_case(n)
+        p.precond = prec
+        f = pkg.Fields.allocate(p)
+        orc.apply_vof_bc(p, f.C)
+        orc.update_physical_properties(p, f)
+        orc.apply_velocity_bc(p, f.u, f.v, False)
+        g = f.copy()
+        with pkg.Solver(p) as s:
+            s.state_set(f)
+            st, _ = s.run_steps(dt, 2, graph=True)          # warm-up (history, plans)
+            st, r = s.run_steps(dt, nsteps, graph=True)
+        assert st == cap.OK, (name, st)
+        rec = {"ms_per_step": r["ms"] / r["steps"], "krylov_iters_per_step": r["mom_iters"] / r["steps"],
+               "graph": r["graph"]}
+        if name == "block_triangular" and cpu_steps > 0:
+            t0 = _t.perf_counter()
+            its = 0
+            for k in range(cpu_steps):
+                it, ip, rr, st = orc.time_step(p, dt, k, g)
+                its += it
+            rec["cpu_ms_per_step"] = 1000.0 * (_t.perf_counter() - t0) / cpu_steps
+            rec["cpu_krylov_iters_per_step"] = its / cpu_steps
+            rec["cpu"] = "oracle (serial FP64 C++ restatement), 1 thread"
+        out[name] = rec
+    return out
+
+
 def run_reference(args, world, rank):
     """--impl reference: the reference path's CPU implementation (the FP64
     C++ restatement; the Fortran reference cannot be built on these
@@ -519,6 +557,7 @@ def run_ours(args, world, rank, local):
         batch = None if args.skip_steps else batch_steps(pkg, orc, 256, 5)
         adjoint = None if args.skip_steps else adjoint_steps(pkg, 512, 3)
         rt = None if (args.skip_steps or args.skip_rt) else rt_steps(pkg, orc, 3)
+        mono = None if args.skip_steps else mono_steps(pkg, orc, 256, 5, 0 if args.skip_cpu else 2)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
@@ -557,6 +596,7 @@ def run_ours(args, world, rank, local):
             "batch": batch,
             "adjoint": adjoint,
             "rayleigh_taylor": rt,
+            "monolithic": mono,
         }
     for r in results.values():
         r["solver"].close()

@@ -428,8 +428,9 @@ __global__ void k_mom_diag(MomArgs a) {
 // arrays need no clearing between assemblies.  One thread per (i, j).
 __device__ __forceinline__ void put_stencil(const Stencil& t, int k, double W, double E, double S, double N,
                                             double P) {
-  t.W[k] = W; t.E[k] = E; t.S[k] = S; t.N[k] = N; t.P[k] = P;
+  // the sweeps divide by aP, or by 1 where |aP| < 1e-30
   const double d = fabs(P) < 1.0e-30 ? 1.0 : P;
+  t.W[k] = W; t.E[k] = E; t.S[k] = S; t.N[k] = N; t.P[k] = d;
   t.rP[k] = __drcp_rn(d);
 }
 

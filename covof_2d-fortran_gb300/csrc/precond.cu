@@ -23,6 +23,8 @@ namespace {
 
 constexpr int kSsorAhead = 4;
 
+__device__ __forceinline__ bool nz(double a) { return (__double_as_longlong(a) << 1) != 0; }
+
 struct SsorOps {
   double z, e, n, c, W, E, S, N, P, y;
 };
@@ -93,13 +95,15 @@ __device__ bool ssor_band(const SsorArgs& A, const SsorJob& J, int s, int b) {
         else     { vE = back; vW = o.e; vN = back_row; vS = o.n; }
         double v;
         if (J.kind == 0) {
+          // "coefficient /= 0" tested on the bit patterns (integer pipe; +0
+          // and -0 both read as zero), the FP64 pipe being the scarce one
           double val = o.z;
-          if (o.W != 0.0) val = val + o.W * vW;
-          if (o.E != 0.0) val = val + o.E * vE;
-          if (o.S != 0.0) val = val + o.S * vS;
-          if (o.N != 0.0) val = val + o.N * vN;
-          const double d = fabs(o.P) < 1.0e-30 ? 1.0 : o.P;
-          v = om1 * o.c + omega * div_rcp(val, d, o.y);
+          if (nz(o.W)) val = val + o.W * vW;
+          if (nz(o.E)) val = val + o.E * vE;
+          if (nz(o.S)) val = val + o.S * vS;
+          if (nz(o.N)) val = val + o.N * vN;
+          // o.P is the centre as the sweeps read it (1 where |aP| < 1e-30)
+          v = om1 * o.c + omega * div_rcp(val, o.P, o.y);
         } else {
           double val;
           if (fwd) {
