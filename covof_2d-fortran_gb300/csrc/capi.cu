@@ -95,13 +95,14 @@ int ensure_poisson(covof_handle* h) {
     H.nl += 1;
   }
   // the tail: from the first level of at most p_mg_tail cells whose levels
-  // down to the coarsest fit in kMgTailSmem bytes of shared memory
+  // down to the coarsest (seven FP32 fields each) fit in kMgTailSmem bytes of
+  // shared memory
   const long long tail_cells = h->prm.p_mg_tail > 0 ? h->prm.p_mg_tail : 2048;
   H.tail = H.nl;
   H.tail_smem = 0;
   for (int l = 1; l < H.nl; ++l) {
     long long bytes = 0;
-    for (int q = l; q < H.nl; ++q) bytes += 24LL * (H.lv[q].nx + 2) * (H.lv[q].ny + 2);
+    for (int q = l; q < H.nl; ++q) bytes += 28LL * (H.lv[q].nx + 2) * (H.lv[q].ny + 2);
     if ((long long)H.lv[l].nx * H.lv[l].ny <= tail_cells && bytes <= kMgTailSmem) {
       H.tail = l;
       H.tail_smem = (int)bytes;

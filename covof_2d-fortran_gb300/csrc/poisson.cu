@@ -776,10 +776,17 @@ template <class Own, class Inner>
 __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, GridReducer& R) {
   const Dims D = a.D;
   const int pk = a.pinned ? D.P + 1 : -1;
+  const bool pinned = a.pinned != 0;
   double* x = a.x; double* r = a.r; double* z = a.z; double* pv = a.p; double* qv = a.q;
   bool ok = true;
   int total_inner = 0, outer = 0, status = COVOF_OK, true_checks = 0;
+  // Scalar state, identical in every thread.  Every division and square
+  // root of the recurrences runs once per block, in thread 0, inside the
+  // reductions (GridReducer::sum_map), and is broadcast: FP64 issue is the
+  // scarce resource of a GB300 SM, and one division evaluated by all 32
+  // warps of a block costs microseconds.
   double b_norm = 1.0, r_norm = 0.0, aP_sum = 1.0, e_sum = 1.0, r_sum = 0.0, sigma_old = 1.0;
+  double rel = 0.0, cdef = 0.0, inv_r = 0.0;  // r_norm / b_norm, deflation, 1 / r_norm
   bool fresh = true;
   // e = A 1 (interior ones, zero ghosts): the 1e-12*dvol shift of aP, the
   // eigenvalue of the constant vector in the reference gauge.
@@ -790,6 +797,16 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
   // whose near-null vector is the constant (weights 1, no scaling).
   auto wgt = [&](int k) -> double { return Inner::kScaled ? a.aP[k] : 1.0; };
   auto scl = [&](int k) -> double { return Inner::kScaled ? a.isd[k] : 1.0; };
+  // from ||r||^2 and sum(r): ||r||, ||r|| / ||b||, the deflation r_sum /
+  // aP_sum and 1 / ||r|| (thread 0 only)
+  auto residual_scalars = [&](double rr, double rsum, double bn, double apsum, double* o) {
+    const double rn = sqrt(rr);
+    o[0] = rn;
+    o[1] = rsum;
+    o[2] = rn / bn;
+    o[3] = pinned ? 0.0 : rsum / apsum;
+    o[4] = 1.0 / rn;
+  };
   auto true_residual = [&]() -> bool {
     double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     own.each([&](int k, int c) {
@@ -801,32 +818,33 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       acc[3] += wgt(k);
       acc[4] += ones_image(k);
     });
-    double t[5];
-    if (!reduce<double, 5>(R, acc, t)) return false;
-    b_norm = sqrt(t[0]);
-    if (b_norm < 1.0e-30) b_norm = 1.0;
-    r_norm = sqrt(t[1]);
-    r_sum = t[2];
-    aP_sum = t[3];
-    e_sum = t[4];
+    double t[8];
+    if (!R.sum_map<5, 8>(acc, t, [&](const double* w, double* o) {
+          double bn = sqrt(w[0]);
+          if (bn < 1.0e-30) bn = 1.0;
+          residual_scalars(w[1], w[2], bn, w[3], o);
+          o[5] = bn; o[6] = w[3]; o[7] = w[4];
+        }))
+      return false;
+    r_norm = t[0]; r_sum = t[1]; rel = t[2]; cdef = t[3]; inv_r = t[4];
+    b_norm = t[5]; aP_sum = t[6]; e_sum = t[7];
     return true;
   };
   if (!true_residual()) ok = false;
   while (ok) {
     if (isnan(r_norm)) { status = COVOF_NAN; break; }
-    if (r_norm / b_norm <= a.tol) {
+    if (rel <= a.tol) {
       if (fresh) break;  // r is already the true residual
       if (++true_checks > 8) break;
       if (!true_residual()) { ok = false; break; }
       fresh = true;
-      if (r_norm / b_norm <= a.tol) break;
+      if (rel <= a.tol) break;
       continue;
     }
     if (outer >= a.max_refine || total_inner >= a.max_iter) { status = COVOF_MAXITER; break; }
-    const double cdef = a.pinned ? 0.0 : r_sum / aP_sum;  // aP_sum: sum of the deflation weights
-    const double scale = 1.0 / r_norm;
+    // cdef: aP_sum is the sum of the deflation weights
     own.each([&](int k, int c) {
-      inner.set_rhs(k, c, (k == pk) ? 0.0f : (float)((r[k] - cdef * wgt(k)) * scl(k) * scale));
+      inner.set_rhs(k, c, (k == pk) ? 0.0f : (float)((r[k] - cdef * wgt(k)) * scl(k) * inv_r));
     });
     __syncthreads();
     int budget = a.max_iter - total_inner;
@@ -855,15 +873,21 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
         zs[2] += qk;
       }
     });
-    double tz[3];
-    if (!reduce<double, 3>(R, zs, tz)) { ok = false; break; }
     // Reference gauge: the projection removes gam (aP-weighted mean of z);
     // the constant mode itself is then solved exactly, a coarse correction
     // z += (1'r / 1'A1) 1 -- without it the iterate would stay on the
     // hyperplane aP'x = 0 and the residual could not fall below
     // eps * mean(p) (about 1e-6 relative for a hydrostatic pressure).
-    const double shift = a.pinned ? 0.0 : tz[0] / aP_sum - r_sum / e_sum;
-    const double beta = fresh ? 0.0 : (tz[1] - shift * tz[2]) / sigma_old;
+    double sb[2];
+    if (!R.sum_map<3, 2>(zs, sb, [&](const double* w, double* o) {
+          const double sh = pinned ? 0.0 : w[0] / aP_sum - r_sum / e_sum;
+          o[0] = sh;
+          o[1] = fresh ? 0.0 : (w[1] - sh * w[2]) / sigma_old;
+        })) {
+      ok = false;
+      break;
+    }
+    const double shift = sb[0], beta = sb[1];
     // p = z - beta p_old, q = A z - beta q_old, and <p,q>, <p,r> from the
     // formed vectors: the algebraic expansion of <p,q> cancels badly when
     // consecutive directions are dominated by the same smooth mode.
@@ -880,11 +904,17 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       acc[0] = fma(pk_, qk_, acc[0]);
       acc[1] = fma(pk_, r[k], acc[1]);
     });
-    double t[2];
-    if (!reduce<double, 2>(R, acc, t)) { ok = false; break; }
-    const double sigma = t[0];
+    double sa[2];
+    if (!R.sum_map<2, 2>(acc, sa, [&](const double* w, double* o) {
+          o[0] = w[0];
+          o[1] = w[0] > 0.0 ? w[1] / w[0] : 0.0;
+        })) {
+      ok = false;
+      break;
+    }
+    const double sigma = sa[0];
     if (!(sigma > 0.0)) { status = COVOF_BREAKDOWN; break; }
-    const double alpha = t[1] / sigma;
+    const double alpha = sa[1];
     double acc2[2] = {0.0, 0.0};
     own.each([&](int k, int) {
       x[k] = fma(alpha, pv[k], x[k]);
@@ -893,10 +923,14 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       acc2[0] = fma(rk, rk, acc2[0]);
       acc2[1] += rk;
     });
-    double t2[2];
-    if (!reduce<double, 2>(R, acc2, t2)) { ok = false; break; }
-    r_norm = sqrt(t2[0]);
-    r_sum = t2[1];
+    double t2[5];
+    if (!R.sum_map<2, 5>(acc2, t2, [&](const double* w, double* o) {
+          residual_scalars(w[0], w[1], b_norm, aP_sum, o);
+        })) {
+      ok = false;
+      break;
+    }
+    r_norm = t2[0]; r_sum = t2[1]; rel = t2[2]; cdef = t2[3]; inv_r = t2[4];
     sigma_old = sigma;
     fresh = false;
   }
@@ -905,13 +939,14 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     double acc[1] = {0.0};
     own.each([&](int k, int) { acc[0] += x[k]; });
     double t[1];
-    ok = reduce<double, 1>(R, acc, t);
-    const double mean = t[0] / (double)((long long)D.nx * D.ny);
+    const double ncell = (double)((long long)D.nx * D.ny);
+    ok = R.sum_map<1, 1>(acc, t, [&](const double* w, double* o) { o[0] = w[0] / ncell; });
+    const double mean = t[0];
     own.each([&](int k, int) { x[k] = x[k] - mean; });
   }
   if (R.rank == 0 && threadIdx.x == 0) {
     a.res->iters = total_inner;
-    a.res->relres = r_norm / b_norm;
+    a.res->relres = rel;
     a.res->status = ok ? status : COVOF_TIMEOUT;
     a.res->outer = outer;
   }
@@ -1292,6 +1327,7 @@ struct MgLv {
   int nx, ny, P;
   float *xa, *xb, *b;
   const float *ax, *ay, *dg;
+  const float* wd;  // tail levels: omega / dg (the sweeps multiply instead of dividing)
   __device__ __forceinline__ int id(int i, int j) const { return j * P + i; }
 };
 
@@ -1302,21 +1338,24 @@ struct MgInner {
   MgHier H;
   float *x0a, *x0b, *b0;   // level 0 solution buffers and right-hand side
   const float *ax0, *ay0, *dg0;  // level 0: FP32 copy of A (faces, diagonal)
-  float* sm;               // block 0: tail levels (6 fields each), H.tail_smem bytes
+  float* sm;               // block 0: tail levels (7 fields each), H.tail_smem bytes
   // level l in global memory (S = false) or, for tail levels, in block 0's
   // shared memory (S = true)
   __device__ MgLv lv(int l, bool S = false) const {
     MgLv L;
     L.nx = H.lv[l].nx; L.ny = H.lv[l].ny; L.P = L.nx + 2;
     const size_t g = (size_t)(L.nx + 2) * (size_t)(L.ny + 2);
+    L.wd = nullptr;
     if (l == 0) {
       L.xa = x0a; L.xb = x0b; L.b = b0; L.ax = ax0; L.ay = ay0; L.dg = dg0;
       return L;
     }
     float* base;
     if (S) {
+      // shared-memory levels hold a seventh field, omega / dg
       base = sm;
-      for (int q = H.tail; q < l; ++q) base += 6 * (size_t)(H.lv[q].nx + 2) * (size_t)(H.lv[q].ny + 2);
+      for (int q = H.tail; q < l; ++q) base += 7 * (size_t)(H.lv[q].nx + 2) * (size_t)(H.lv[q].ny + 2);
+      L.wd = base + 6 * g;
     } else {
       base = H.pool + H.lv[l].off;
     }
@@ -1362,10 +1401,18 @@ struct MgInner {
     const int pin = l == 0 ? pk : -1;
     cells<S, W>(L.nx, L.ny, [&](int i, int j) {
       const int k = L.id(i, j);
-      const float d = L.dg[k];
       float v;
-      if (first) v = w * ld<S>(L.b + k) / d;
-      else v = ld<S>(xs + k) + w * (ld<S>(L.b + k) - apply<S>(L, xs, k)) / d;
+      if constexpr (S) {
+        // shared-memory levels: a multiply by omega / dg (block 0's
+        // sequential tail is bound by the dependent chain, not by memory)
+        const float q = L.wd[k];
+        if (first) v = ld<S>(L.b + k) * q;
+        else v = ld<S>(xs + k) + (ld<S>(L.b + k) - apply<S>(L, xs, k)) * q;
+      } else {
+        const float d = L.dg[k];
+        if (first) v = w * ld<S>(L.b + k) / d;
+        else v = ld<S>(xs + k) + w * (ld<S>(L.b + k) - apply<S>(L, xs, k)) / d;
+      }
       if (k == pin) v = 0.0f;
       xd[k] = v;
     });
@@ -1441,7 +1488,9 @@ struct MgInner {
           Sm.xa[k] = 0.0f; Sm.xb[k] = 0.0f; Sm.b[k] = 0.0f;
           const_cast<float*>(Sm.ax)[k] = __ldcg(G.ax + k);
           const_cast<float*>(Sm.ay)[k] = __ldcg(G.ay + k);
-          const_cast<float*>(Sm.dg)[k] = __ldcg(G.dg + k);
+          const float dk = __ldcg(G.dg + k);
+          const_cast<float*>(Sm.dg)[k] = dk;
+          const_cast<float*>(Sm.wd)[k] = dk != 0.0f ? H.omega / dk : 0.0f;
         }
       }
       __syncthreads();
@@ -1450,6 +1499,53 @@ struct MgInner {
   }
   __device__ __forceinline__ void set_rhs(int k, int, float v) { b0[k] = v; }
   __device__ __forceinline__ float y(int k, int) const { return k == pk ? 0.0f : __ldcg(x0a + k); }
+  // The nuc sweeps of a coarsest level of at most 64 cells in the first
+  // warp: each lane's (at most two) cells keep their coefficients and
+  // right-hand side in registers across the sweeps, so a sweep is five
+  // shared-memory reads and a few FMAs per cell (the same arithmetic as
+  // sweep<true>, bit for bit).
+  __device__ void coarsest_warp(int l) const {
+    const MgLv L = lv(l, true);
+    const int n = L.nx * L.ny, lane = threadIdx.x & 31;
+    const int pin = l == 0 ? pk : -1;
+    int kk[2];
+    float cb[2], cq[2], cd[2], cw_[2], ce[2], cs[2], cn[2];
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+      const int c = lane + 32 * m;
+      kk[m] = -1;
+      if (c < n) {
+        const int j = c / L.nx, i = c - j * L.nx;
+        const int k = L.id(i + 1, j + 1);
+        kk[m] = k;
+        cb[m] = L.b[k]; cq[m] = L.wd[k]; cd[m] = L.dg[k];
+        cw_[m] = L.ax[k]; ce[m] = L.ax[k + 1]; cs[m] = L.ay[k]; cn[m] = L.ay[k + L.P];
+      }
+    }
+    for (int s = 0; s < H.nuc; ++s) {
+      if (s > 0) __syncwarp();
+      const float* xs = (s & 1) ? L.xb : L.xa;
+      float* xd = (s & 1) ? L.xa : L.xb;
+#pragma unroll
+      for (int m = 0; m < 2; ++m) {
+        const int k = kk[m];
+        if (k < 0) continue;
+        float v;
+        if (s == 0) {
+          v = cb[m] * cq[m];
+        } else {
+          float a = cd[m] * xs[k];
+          a = __fmaf_rn(-cw_[m], xs[k - 1], a);
+          a = __fmaf_rn(-ce[m], xs[k + 1], a);
+          a = __fmaf_rn(-cs[m], xs[k - L.P], a);
+          a = __fmaf_rn(-cn[m], xs[k + L.P], a);
+          v = xs[k] + (cb[m] - a) * cq[m];
+        }
+        if (k == pin) v = 0.0f;
+        xd[k] = v;
+      }
+    }
+  }
   // the tail levels, block 0 alone out of shared memory: b_tail in from
   // global memory, the tail's correction back out
   __device__ void tail_cycle() const {
@@ -1471,7 +1567,9 @@ struct MgInner {
     }
     // the coarsest level: a small one runs in the first warp alone, so its
     // many sweeps synchronise with __syncwarp instead of block barriers
-    if ((long long)H.lv[L - 1].nx * H.lv[L - 1].ny <= kMgWarpCoarse) {
+    if ((long long)H.lv[L - 1].nx * H.lv[L - 1].ny <= 64) {
+      if (threadIdx.x < 32) coarsest_warp(L - 1);
+    } else if ((long long)H.lv[L - 1].nx * H.lv[L - 1].ny <= kMgWarpCoarse) {
       if (threadIdx.x < 32) {
         for (int s = 0; s < H.nuc; ++s) {
           if (s > 0) __syncwarp();
