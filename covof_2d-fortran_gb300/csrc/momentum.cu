@@ -796,6 +796,9 @@ __device__ void krylov_finish(const MomArgs& a, const Team& tm, int iters, int s
 }
 
 // src/module_linear_solvers.f90:584-730 solve_bicgstab (left Jacobi).
+// Every division and square root of the recurrences runs once per block, in
+// thread 0, inside the reductions (GridReducer::sum_map), and is broadcast:
+// FP64 issue is the scarce resource of a GB300 SM.
 __device__ void bicgstab_case(const MomArgs& a, const Team& tm, GridReducer& R) {
   DofWalker W(a.D, tm, a.mono);
   double *x = a.x, *bh = a.v0, *r = a.v1, *rt = a.v2, *p = a.v3, *v = a.v4, *s = a.v5, *t = a.v6;
@@ -810,15 +813,16 @@ __device__ void bicgstab_case(const MomArgs& a, const Team& tm, GridReducer& R) 
     r[k] = rr; rt[k] = rr;
     acc[0] += rr * rr;
   }
-  bool ok = R.sum(acc);
-  const double rsq0 = acc[0];
-  const double r0 = sqrt(rsq0);
+  double o0[2];
+  bool ok = R.sum_map<1, 2>(acc, o0, [&](const double* w, double* o) { o[0] = w[0]; o[1] = sqrt(w[0]); });
+  const double rsq0 = o0[0];
+  const double r0 = o0[1];
   if (!ok || r0 < 1.0e-12) { krylov_finish(a, tm, 0, COVOF_OK, ok); return; }
-  double rho_old = 1.0, alpha = 1.0, omega = 1.0, rho = rsq0;
+  double rho_old = 1.0, alpha = 1.0, omega = 1.0, rho = rsq0, beta = 0.0;
   int iters = max_iter, status = COVOF_MAXITER;
   for (int it = 1; it <= max_iter && ok; ++it) {
     if (fabs(rho) < 1.0e-30) { status = COVOF_BREAKDOWN; break; }
-    const double beta = (rho / rho_old) * (alpha / omega);
+    // beta = (rho / rho_old) (alpha / omega), formed in the previous reduction
     FOR_DOFS(a, W, part, i, j, k) {
       p[k] = (it == 1) ? r[k] : r[k] + beta * (p[k] - omega * v[k]);
     }
@@ -830,21 +834,30 @@ __device__ void bicgstab_case(const MomArgs& a, const Team& tm, GridReducer& R) 
       v[k] = vv;
       a1[0] += rt[k] * vv;
     }
-    ok = R.sum(a1);
+    double o1[2];
+    ok = R.sum_map<1, 2>(a1, o1, [&](const double* w, double* o) {
+      o[0] = w[0];
+      o[1] = fabs(w[0]) < 1.0e-30 ? 0.0 : rho / w[0];
+    });
     if (!ok) break;
-    if (fabs(a1[0]) < 1.0e-30) { status = COVOF_BREAKDOWN; break; }
-    alpha = rho / a1[0];
+    if (fabs(o1[0]) < 1.0e-30) { status = COVOF_BREAKDOWN; break; }
+    alpha = o1[1];
     double a2[1] = {0.0};
     FOR_DOFS(a, W, part, i, j, k) {
       const double sv = r[k] - alpha * v[k];
       s[k] = sv;
       a2[0] += sv * sv;
     }
-    ok = R.sum(a2);
+    double o2[2];
+    ok = R.sum_map<1, 2>(a2, o2, [&](const double* w, double* o) {
+      const double sn = sqrt(w[0]);
+      o[0] = sn;
+      o[1] = sn / r0;
+    });
     if (!ok) break;
-    const double sn = sqrt(a2[0]);
+    const double sn = o2[0];
     if (sn != sn || sn > 1.0e30) { status = COVOF_NAN; break; }
-    if (sn / r0 < tol || sn < 1.0e-12) {
+    if (o2[1] < tol || sn < 1.0e-12) {
       FOR_DOFS(a, W, part, i, j, k) x[k] = x[k] + alpha * p[k];
       iters = it; status = COVOF_OK;
       break;
@@ -856,9 +869,10 @@ __device__ void bicgstab_case(const MomArgs& a, const Team& tm, GridReducer& R) 
       a3[0] += tt * tt;
       a3[1] += tt * s[k];
     }
-    ok = R.sum(a3);
+    double o3[1];
+    ok = R.sum_map<2, 1>(a3, o3, [&](const double* w, double* o) { o[0] = w[0] > 1.0e-30 ? w[1] / w[0] : 0.0; });
     if (!ok) break;
-    omega = a3[0] > 1.0e-30 ? a3[1] / a3[0] : 0.0;
+    omega = o3[0];
     double a4[2] = {0.0, 0.0};
     FOR_DOFS(a, W, part, i, j, k) {
       x[k] = x[k] + alpha * p[k] + omega * s[k];
@@ -867,15 +881,25 @@ __device__ void bicgstab_case(const MomArgs& a, const Team& tm, GridReducer& R) 
       a4[0] += rr * rr;
       a4[1] += rt[k] * rr;  // next iteration's rho = <r~, r>
     }
-    ok = R.sum(a4);
+    double o4[4];
+    ok = R.sum_map<2, 4>(a4, o4, [&](const double* w, double* o) {
+      const double rn = sqrt(w[0]);
+      o[0] = rn;
+      o[1] = rn / r0;
+      // the next iteration's beta (rho_old is this iteration's rho)
+      o[2] = (w[1] / rho) * (alpha / omega);
+      o[3] = w[1];
+    });
     if (!ok) break;
     rho_old = rho;
-    rho = a4[1];
-    const double rn = sqrt(a4[0]);
+    rho = o4[3];
+    beta = o4[2];
+    const double rn = o4[0];
     if (rn != rn || rn > 1.0e30) { status = COVOF_NAN; break; }
-    if (rn / r0 < tol || rn < 1.0e-12) { iters = it; status = COVOF_OK; break; }
+    if (o4[1] < tol || rn < 1.0e-12) { iters = it; status = COVOF_OK; break; }
     if (fabs(omega) < 1.0e-30) { status = COVOF_BREAKDOWN; break; }
   }
+  (void)rho_old;
   krylov_finish(a, tm, iters, status, ok);
 }
 
@@ -901,10 +925,11 @@ __device__ void cg_case(const MomArgs& a, const Team& tm, GridReducer& R) {
     acc[0] += rr * rr;
     acc[1] += rr * z;
   }
-  bool ok = R.sum(acc);
-  const double r0 = sqrt(acc[0]);
+  double o0[2];
+  bool ok = R.sum_map<2, 2>(acc, o0, [&](const double* w, double* o) { o[0] = sqrt(w[0]); o[1] = w[1]; });
+  const double r0 = o0[0];
   if (!ok || r0 < 1.0e-12) { krylov_finish(a, tm, 0, COVOF_OK, ok); return; }
-  double rz_old = acc[1];
+  double rz_old = o0[1];
   int iters = max_iter, status = COVOF_MAXITER;
   for (int it = 1; it <= max_iter && ok; ++it) {
     double a1[1] = {0.0};
@@ -913,10 +938,14 @@ __device__ void cg_case(const MomArgs& a, const Team& tm, GridReducer& R) {
       Ap[k] = y;
       a1[0] += p[k] * y;
     }
-    ok = R.sum(a1);
+    double o1[2];
+    ok = R.sum_map<1, 2>(a1, o1, [&](const double* w, double* o) {
+      o[0] = w[0];
+      o[1] = fabs(w[0]) < 1.0e-30 ? 0.0 : rz_old / w[0];
+    });
     if (!ok) break;
-    if (fabs(a1[0]) < 1.0e-30) { status = COVOF_BREAKDOWN; break; }
-    const double alpha = rz_old / a1[0];
+    if (fabs(o1[0]) < 1.0e-30) { status = COVOF_BREAKDOWN; break; }
+    const double alpha = o1[1];
     double a2[2] = {0.0, 0.0};
     FOR_DOFS(a, W, part, i, j, k) {
       x[k] = x[k] + alpha * p[k];
@@ -925,12 +954,19 @@ __device__ void cg_case(const MomArgs& a, const Team& tm, GridReducer& R) {
       a2[0] += rr * rr;
       a2[1] += rr * prec(a, k, rr);
     }
-    ok = R.sum(a2);
+    double o2[4];
+    ok = R.sum_map<2, 4>(a2, o2, [&](const double* w, double* o) {
+      const double rn = sqrt(w[0]);
+      o[0] = rn;
+      o[1] = rn / r0;
+      o[2] = w[1] / rz_old;  // beta
+      o[3] = w[1];
+    });
     if (!ok) break;
-    const double rn = sqrt(a2[0]);
-    if (rn / r0 < tol || rn < 1.0e-13) { iters = it; status = COVOF_OK; break; }
-    const double beta = a2[1] / rz_old;
-    rz_old = a2[1];
+    const double rn = o2[0];
+    if (o2[1] < tol || rn < 1.0e-13) { iters = it; status = COVOF_OK; break; }
+    const double beta = o2[2];
+    rz_old = o2[3];
     FOR_DOFS(a, W, part, i, j, k) p[k] = prec(a, k, r[k]) + beta * p[k];
     ok = R.gs.sync();
   }
@@ -944,6 +980,8 @@ __global__ void __launch_bounds__(512) k_cg(MomArgs a) {
 }
 
 // src/module_linear_solvers.f90:361-579 solve_bicgstab2 (left Jacobi).
+// Divisions and square roots run once per block inside the reductions, as
+// in bicgstab_case; each reduction also forms the next step's coefficients.
 __device__ void bicgstab2_case(const MomArgs& a, const Team& tm, GridReducer& R) {
   DofWalker W(a.D, tm, a.mono);
   double *x = a.x, *rt = a.v0, *r0 = a.v1, *r1 = a.v2, *r2 = a.v3, *u0 = a.v4, *u1 = a.v5, *u2 = a.v6;
@@ -957,21 +995,30 @@ __device__ void bicgstab2_case(const MomArgs& a, const Team& tm, GridReducer& R)
     u0[k] = 0.0; u1[k] = 0.0; u2[k] = 0.0; r1[k] = 0.0; r2[k] = 0.0;
     acc[0] += rr * rr;
   }
-  bool ok = R.sum(acc);
-  const double r0n = sqrt(acc[0]);
-  if (!ok || r0n < 1.0e-12) { krylov_finish(a, tm, 0, COVOF_OK, ok); return; }
   double rho0 = 1.0, alpha = 0.0, omega = 1.0;
+  // the loop head's rho0 = -omega rho0 and beta = alpha (rho1 / rho0), with
+  // rho1 = <r~, r0>, formed in the reduction before it
+  auto head = [&](double rho1, double* o) {
+    const double rn0 = -omega * rho0;
+    o[0] = rn0;
+    o[1] = alpha * (rho1 / rn0);
+    o[2] = rho1;
+  };
+  double i0[4];
+  bool ok = R.sum_map<1, 4>(acc, i0, [&](const double* w, double* o) {
+    head(w[0], o);
+    o[3] = sqrt(w[0]);
+  });
+  const double r0n = i0[3];
+  if (!ok || r0n < 1.0e-12) { krylov_finish(a, tm, 0, COVOF_OK, ok); return; }
+  double hd[3] = {i0[0], i0[1], i0[2]};
   int iter = 0, status = COVOF_MAXITER;
-  bool have_rho1 = true;
-  double rho1_next = acc[0];  // <r~, r0> with r~ = r0
   while (iter < max_iter && ok) {
     iter += 2;
-    rho0 = -omega * rho0;
-    double rho1 = rho1_next;
-    (void)have_rho1;
+    rho0 = hd[0];
     if (fabs(rho0) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
-    double beta = alpha * (rho1 / rho0);
-    rho0 = rho1;
+    double beta = hd[1];
+    rho0 = hd[2];
     FOR_DOFS(a, W, part, i, j, k) u0[k] = r0[k] - beta * u0[k];
     ok = R.gs.sync();
     if (!ok) break;
@@ -981,10 +1028,14 @@ __device__ void bicgstab2_case(const MomArgs& a, const Team& tm, GridReducer& R)
       u1[k] = y;
       g1[0] += rt[k] * y;
     }
-    ok = R.sum(g1);
+    double o1[2];
+    ok = R.sum_map<1, 2>(g1, o1, [&](const double* w, double* o) {
+      o[0] = w[0];
+      o[1] = fabs(w[0]) < 1.0e-300 ? 0.0 : rho0 / w[0];
+    });
     if (!ok) break;
-    if (fabs(g1[0]) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
-    alpha = rho0 / g1[0];
+    if (fabs(o1[0]) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
+    alpha = o1[1];
     FOR_DOFS(a, W, part, i, j, k) {
       r0[k] = r0[k] - alpha * u1[k];
       x[k] = x[k] + alpha * u0[k];
@@ -997,12 +1048,15 @@ __device__ void bicgstab2_case(const MomArgs& a, const Team& tm, GridReducer& R)
       r1[k] = y;
       g2[0] += rt[k] * y;
     }
-    ok = R.sum(g2);
+    double o2[2];
+    ok = R.sum_map<1, 2>(g2, o2, [&](const double* w, double* o) {
+      o[0] = w[0];
+      o[1] = alpha * (w[0] / rho0);
+    });
     if (!ok) break;
-    rho1 = g2[0];
     if (fabs(rho0) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
-    beta = alpha * (rho1 / rho0);
-    rho0 = rho1;
+    beta = o2[1];
+    rho0 = o2[0];
     FOR_DOFS(a, W, part, i, j, k) {
       u0[k] = r0[k] - beta * u0[k];
       u1[k] = r1[k] - beta * u1[k];
@@ -1015,10 +1069,14 @@ __device__ void bicgstab2_case(const MomArgs& a, const Team& tm, GridReducer& R)
       u2[k] = y;
       g3[0] += rt[k] * y;
     }
-    ok = R.sum(g3);
+    double o3[2];
+    ok = R.sum_map<1, 2>(g3, o3, [&](const double* w, double* o) {
+      o[0] = w[0];
+      o[1] = fabs(w[0]) < 1.0e-300 ? 0.0 : rho0 / w[0];
+    });
     if (!ok) break;
-    if (fabs(g3[0]) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
-    alpha = rho0 / g3[0];
+    if (fabs(o3[0]) < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
+    alpha = o3[1];
     FOR_DOFS(a, W, part, i, j, k) {
       x[k] = x[k] + alpha * u0[k];
       r0[k] = r0[k] - alpha * u1[k];
@@ -1036,21 +1094,29 @@ __device__ void bicgstab2_case(const MomArgs& a, const Team& tm, GridReducer& R)
       sg[3] += r0[k] * r1[k];
       sg[4] += r0[k] * y;
     }
-    ok = R.sum(sg);
+    // the minimal-residual pair (gamma1, gamma2); o[0] = 1: breakdown
+    double gm[3];
+    ok = R.sum_map<5, 3>(sg, gm, [&](const double* w, double* o) {
+      const double s11 = w[0], s12 = w[1], s22 = w[2], rhs1 = w[3], rhs2 = w[4];
+      const double rn1 = sqrt(s11), rn2 = sqrt(s22);
+      double gm1 = 0.0, gm2 = 0.0;
+      o[0] = 0.0;
+      if (rn1 < 1.0e-300) { o[0] = 1.0; }
+      else if (rn2 < 1.0e-300) { gm2 = 0.0; gm1 = rhs1 / s11; }
+      else {
+        const double i1 = 1.0 / rn1, i2 = 1.0 / rn2;
+        const double c12 = s12 * i1 * i2;
+        const double b1 = rhs1 * i1, b2 = rhs2 * i2;
+        const double det = 1.0 - c12 * c12;
+        if (fabs(det) < 1.0e-14) { gm2 = 0.0; gm1 = b1 * i1; }
+        else { gm1 = (b1 - c12 * b2) / (det * rn1); gm2 = (b2 - c12 * b1) / (det * rn2); }
+      }
+      o[1] = gm1;
+      o[2] = gm2;
+    });
     if (!ok) break;
-    const double s11 = sg[0], s12 = sg[1], s22 = sg[2], rhs1 = sg[3], rhs2 = sg[4];
-    const double rn1 = sqrt(s11), rn2 = sqrt(s22);
-    double gm1, gm2;
-    if (rn1 < 1.0e-300) { status = COVOF_BREAKDOWN; break; }
-    else if (rn2 < 1.0e-300) { gm2 = 0.0; gm1 = rhs1 / s11; }
-    else {
-      const double i1 = 1.0 / rn1, i2 = 1.0 / rn2;
-      const double c12 = s12 * i1 * i2;
-      const double b1 = rhs1 * i1, b2 = rhs2 * i2;
-      const double det = 1.0 - c12 * c12;
-      if (fabs(det) < 1.0e-14) { gm2 = 0.0; gm1 = b1 * i1; }
-      else { gm1 = (b1 - c12 * b2) / (det * rn1); gm2 = (b2 - c12 * b1) / (det * rn2); }
-    }
+    if (gm[0] != 0.0) { status = COVOF_BREAKDOWN; break; }
+    const double gm1 = gm[1], gm2 = gm[2];
     double fin[2] = {0.0, 0.0};
     FOR_DOFS(a, W, part, i, j, k) {
       x[k] = x[k] + gm1 * r0[k] + gm2 * r1[k];
@@ -1060,15 +1126,21 @@ __device__ void bicgstab2_case(const MomArgs& a, const Team& tm, GridReducer& R)
       fin[0] += rr * rr;
       fin[1] += rt[k] * rr;  // rho1 of the next sweep
     }
-    ok = R.sum(fin);
-    if (!ok) break;
-    rho1_next = fin[1];
     if (gm2 != 0.0) omega = gm2;
     else if (fabs(gm1) > 1.0e-300) omega = gm1;
     else omega = 1.0;
-    const double rn = sqrt(fin[0]);
+    double of[5];
+    ok = R.sum_map<2, 5>(fin, of, [&](const double* w, double* o) {
+      head(w[1], o);
+      const double rn = sqrt(w[0]);
+      o[3] = rn;
+      o[4] = rn / r0n;
+    });
+    if (!ok) break;
+    hd[0] = of[0]; hd[1] = of[1]; hd[2] = of[2];
+    const double rn = of[3];
     if (rn != rn || rn > 1.0e30) { status = COVOF_NAN; break; }
-    if (rn / r0n < tol || rn < 1.0e-12) { status = COVOF_OK; break; }
+    if (of[4] < tol || rn < 1.0e-12) { status = COVOF_OK; break; }
   }
   krylov_finish(a, tm, iter, status, ok);
 }
