@@ -60,7 +60,7 @@ def make_params(nx: int, ny: int, lx: float, ly: float) -> Params:
     p.recon = capi.RECON_PLIC
     p.p_inner_kind = capi.INNER_MG
     p.p_cheb_lo = 1.0e-3
-    p.p_mg_nu = 3
+    p.p_mg_nu = 2
     p.p_mg_cw = 2.0
     p.p_mg_tail = 2048
     p.time_scheme = capi.TIME_EULER

@@ -1199,7 +1199,7 @@ void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly)
   p->recon = COVOF_RECON_PLIC;
   p->p_inner_kind = COVOF_INNER_MG;
   p->p_cheb_lo = 1.0e-3;
-  p->p_mg_nu = 3;
+  p->p_mg_nu = 2;
   p->p_mg_cw = 2.0;
   p->p_mg_tail = 2048;
   p->time_scheme = COVOF_TIME_EULER;
