@@ -462,8 +462,9 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
     size_t bytes = 0;
     for (covof_handle* h : b->h) bytes = std::max(bytes, (size_t)h->mg.tail_smem);
     b->pplan.smem = bytes;
-    if (bytes > 48 * 1024 &&
-        cudaFuncSetAttribute(b->pfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+    // opt in whatever the size: the kernel's static shared memory counts
+    // against the 48 KB a launch gets without it
+    if (cudaFuncSetAttribute(b->pfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
       return fail(COVOF_CUDA_ERROR);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->pfn, 1024, bytes) != cudaSuccess || per_sm < 1)

@@ -286,8 +286,9 @@ int poisson_plan(covof_handle* h) {
     long long units = h->sm_count;
     if (L.p_blocks > 0 && L.p_blocks < units) units = L.p_blocks;
     const size_t tail = (size_t)h->mg.tail_smem;
-    if (tail > 48 * 1024 &&
-        cudaFuncSetAttribute(mfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail) != cudaSuccess)
+    // opt in whatever the size: the kernel's static shared memory counts
+    // against the 48 KB a launch gets without it
+    if (cudaFuncSetAttribute(mfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail) != cudaSuccess)
       return COVOF_CUDA_ERROR;
     const int nb = coop_blocks(h, mfn, kPoissonThreads, units, tail);
     if (nb < 1) return COVOF_CUDA_ERROR;

@@ -1339,9 +1339,12 @@ struct MgInner {
   float *x0a, *x0b, *b0;   // level 0 solution buffers and right-hand side
   const float *ax0, *ay0, *dg0;  // level 0: FP32 copy of A (faces, diagonal)
   float* sm;               // block 0: tail levels (7 fields each), H.tail_smem bytes
+  MgLv* tab;               // this block's shared table of the level views, built in setup
   // level l in global memory (S = false) or, for tail levels, in block 0's
-  // shared memory (S = true)
-  __device__ MgLv lv(int l, bool S = false) const {
+  // shared memory (S = true): one read of the block's table (the views are
+  // formed once per solve; the hierarchy itself lives in local memory)
+  __device__ __forceinline__ MgLv lv(int l, bool S = false) const { return tab[2 * l + (S ? 1 : 0)]; }
+  __device__ MgLv lv_make(int l, bool S) const {
     MgLv L;
     L.nx = H.lv[l].nx; L.ny = H.lv[l].ny; L.P = L.nx + 2;
     const size_t g = (size_t)(L.nx + 2) * (size_t)(L.ny + 2);
@@ -1455,6 +1458,9 @@ struct MgInner {
   // coarse operators of levels 1 .. nl-1 from the fine ones, then the tail
   // levels' coefficients into block 0's shared memory (once per solve)
   __device__ bool setup(GridReducer& R) const {
+    __syncthreads();  // a previous case of this block is done with the table
+    for (int q = threadIdx.x; q < 2 * H.nl; q += blockDim.x) tab[q] = lv_make(q >> 1, (q & 1) != 0);
+    __syncthreads();
     for (int l = 1; l < H.nl; ++l) {
       const MgLv F = lv(l - 1), Cc = lv(l);
       float* cax = const_cast<float*>(Cc.ax);
@@ -1645,7 +1651,7 @@ struct MgInner {
 
 // One mixed solve of case a by team tm with the multigrid inner iteration
 // (tail: the team's block 0 shared memory, at least a.mg.tail_smem bytes).
-__device__ void mixed_mg_case(const PoissonArgs& a, const Team& tm, GridReducer& R, float* tail) {
+__device__ void mixed_mg_case(const PoissonArgs& a, const Team& tm, GridReducer& R, float* tail, MgLv* tab) {
   const Dims D = a.D;
   // a launch without room for the tail is refused, not run (every block of
   // the team takes the same branch, so no barrier is left waiting)
@@ -1665,6 +1671,7 @@ __device__ void mixed_mg_case(const PoissonArgs& a, const Team& tm, GridReducer&
   in.H = a.mg;
   in.x0a = a.e32; in.x0b = a.d32; in.b0 = a.r32; in.ax0 = a.ax32; in.ay0 = a.ay32; in.dg0 = a.aP32;
   in.sm = tail;
+  in.tab = tab;
   if (!in.setup(R)) {
     if (tm.rank == 0 && threadIdx.x == 0) {
       a.res->iters = 0; a.res->relres = 1.0; a.res->status = COVOF_TIMEOUT; a.res->outer = 0;
@@ -1676,9 +1683,10 @@ __device__ void mixed_mg_case(const PoissonArgs& a, const Team& tm, GridReducer&
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg(PoissonArgs a) {
   extern __shared__ float mg_tail[];
+  __shared__ MgLv mg_tab[2 * kMgMaxLevels];
   const Team tm = grid_team();
   GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
-  mixed_mg_case(a, tm, R, mg_tail);
+  mixed_mg_case(a, tm, R, mg_tail, mg_tab);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_stream(PoissonArgs a) {
@@ -1798,11 +1806,12 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_smem_batch(const PoissonA
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg_batch(const PoissonArgs* __restrict__ cases,
                                                                 BatchTeams bt) {
   extern __shared__ float mg_tail[];
+  __shared__ MgLv mg_tab[2 * kMgMaxLevels];
   int4 T;
   const Team tm = batch_team(bt, T);
   const int t = bt.block_team[blockIdx.x];
   GridReducer R{bt.part + (size_t)16 * T.x, GridSync{bt.bar + 32 * t, bt.err + t, (unsigned)T.y, 0u}, 0, tm.rank};
-  for (int q = T.z; q < T.w; ++q) mixed_mg_case(cases[bt.case_list[q]], tm, R, mg_tail);
+  for (int q = T.z; q < T.w; ++q) mixed_mg_case(cases[bt.case_list[q]], tm, R, mg_tail, mg_tab);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt) {
