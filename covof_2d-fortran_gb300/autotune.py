@@ -75,7 +75,7 @@ def candidates(p: Params, sm_count: int) -> list[tuple[dict, dict]]:
         # coarsest level's sweeps)
         mg_blocks = sorted({sm_count, max(1, sm_count // 2)}, reverse=True)
         for nb in mg_blocks:
-            for nuc in (64, 32, 128):
+            for nuc in (-1, 64, 32):
                 for nu in (3, 2, 4):
                     for cw in (2.0, 1.9, 1.8):
                         out.append(({"p_threads": 0, "p_blocks": nb, "p_inner_form": 0},

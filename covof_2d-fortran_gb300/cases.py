@@ -79,7 +79,7 @@ def make_params(nx: int, ny: int, lx: float, ly: float) -> Params:
     p.ic_radius = 0.25
     p.uzawa_iter = 1
     p.uzawa_tol = 1.0e-12
-    p.p_mg_nuc = 64
+    p.p_mg_nuc = -1
     return p
 
 

@@ -113,8 +113,19 @@ int ensure_poisson(covof_handle* h) {
   H.nu = h->prm.p_mg_nu < 1 ? 1 : (h->prm.p_mg_nu > 8 ? 8 : h->prm.p_mg_nu);
   H.cw = (float)(h->prm.p_mg_cw > 0.0 && h->prm.p_mg_cw <= 4.0 ? h->prm.p_mg_cw : 1.0);
   // an even count leaves the coarsest correction in its first buffer
-  const int nuc = h->prm.p_mg_nuc > 0 ? (h->prm.p_mg_nuc > 1024 ? 1024 : h->prm.p_mg_nuc) : 8;
+  const int nuc = h->prm.p_mg_nuc > 0 ? (h->prm.p_mg_nuc > 1024 ? 1024 : h->prm.p_mg_nuc) : 64;
   H.nuc = (nuc + 1) & ~1;
+  // p_mg_nuc < 0: the coarsest level solved exactly (a dense inverse in the
+  // tail's shared memory) when it is in the tail and has at most 64 cells
+  H.exact = 0;
+  H.inv_off = 0;
+  const long long ncoarse = (long long)H.lv[H.nl - 1].nx * H.lv[H.nl - 1].ny;
+  if (h->prm.p_mg_nuc < 0 && H.tail < H.nl && ncoarse <= 64 && H.tail_smem + 64 * 64 * 4 <= kMgTailSmem) {
+    H.exact = 1;
+    H.inv_off = H.tail_smem / 4;
+    H.tail_smem += 64 * 64 * 4;
+    H.nuc = 0;
+  }
   if (pool > 0) CS(dalloc(&H.pool, (size_t)pool));
   h->have_poisson = true;
   return COVOF_OK;
@@ -1219,7 +1230,7 @@ void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly)
   p->ic_radius = 0.25;
   p->uzawa_iter = 1;
   p->uzawa_tol = 1.0e-12;
-  p->p_mg_nuc = 64;
+  p->p_mg_nuc = -1;
 }
 
 int covof_abi_version(void) { return COVOF_ABI_VERSION; }

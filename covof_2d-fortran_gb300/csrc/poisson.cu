@@ -1481,6 +1481,17 @@ struct MgInner {
           float internal = 0.0f;
           if (i0 + 1 <= F.nx) internal += axf(i0 + 1, j0) + axf(i0 + 1, j0 + 1);
           if (j0 + 1 <= F.ny) internal += ayf(i0, j0 + 1) + ayf(i0 + 1, j0 + 1);
+          if (l == 1 && pk >= 0 && I == 1 && J == 1) {
+            // pinned gauge: the fine operator is A without cell (1,1) (held
+            // at zero), so the aggregate holding it sums the other three
+            // cells only and its couplings to the pinned cell are not
+            // internal -- they stay on those cells' diagonals as a Dirichlet
+            // anchor.  The coarse operators are then nonsingular like the
+            // pinned system, instead of near-singular along the constant.
+            d = dgf(i0 + 1, j0) + dgf(i0, j0 + 1) + dgf(i0 + 1, j0 + 1);
+            internal = 0.0f;
+            if (i0 + 1 <= F.nx && j0 + 1 <= F.ny) internal = axf(i0 + 1, j0 + 1) + ayf(i0 + 1, j0 + 1);
+          }
           cdg[k] = d - 2.0f * internal;
         }
       });
@@ -1500,8 +1511,73 @@ struct MgInner {
         }
       }
       __syncthreads();
+      if (H.exact) coarse_inverse();
     }
     return true;
+  }
+  // Block 0: the inverse of the coarsest operator M + c 1 1' (c 64 = the mean
+  // diagonal: the near-null constant mode gets a moderate eigenvalue), by
+  // Gauss-Jordan elimination in place in FP32 (M is symmetric positive
+  // definite plus that rank-one term; no pivoting), then symmetrised.  The
+  // V-cycle applies P B P, P the projection off the constant: a symmetric
+  // operator, the pseudo-inverse of M on the mean-free vectors.
+  __device__ void coarse_inverse() const {
+    const int l = H.nl - 1;
+    const MgLv L = lv(l, true);
+    const int n = L.nx * L.ny;
+    float* B = sm + H.inv_off;      // 64 x 64, row r at B + 64 r
+    float* col = L.xb;              // scratch: the pivot column (the level's second buffer)
+    __shared__ float s_c;
+    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) B[e] = 0.0f;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float tr = 0.0f;
+      for (int c = 0; c < n; ++c) {
+        const int j = c / L.nx, i = c - j * L.nx;
+        tr += L.dg[L.id(i + 1, j + 1)];
+      }
+      // pinned gauge: the coarse operators carry the pin's Dirichlet anchor
+      // and are nonsingular; no rank-one term
+      s_c = pk >= 0 ? 0.0f : tr / ((float)n * (float)n);
+    }
+    __syncthreads();
+    const float cs = s_c;
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+      const int j = c / L.nx, i = c - j * L.nx;
+      const int k = L.id(i + 1, j + 1);
+      float* row = B + 64 * c;
+      for (int q = 0; q < n; ++q) row[q] = cs;
+      row[c] += L.dg[k];
+      if (i > 0) row[c - 1] -= L.ax[k];
+      if (i < L.nx - 1) row[c + 1] -= L.ax[k + 1];
+      if (j > 0) row[c - L.nx] -= L.ay[k];
+      if (j < L.ny - 1) row[c + L.nx] -= L.ay[k + L.P];
+    }
+    __syncthreads();
+    for (int p = 0; p < n; ++p) {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = B[64 * i + p];
+      __syncthreads();
+      const float ip = 1.0f / col[p];
+      for (int q = threadIdx.x; q < n; q += blockDim.x) B[64 * p + q] = (q == p ? 1.0f : B[64 * p + q]) * ip;
+      __syncthreads();
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int i = e / n, q = e - i * n;
+        if (i == p) continue;
+        const float f = col[i];
+        B[64 * i + q] = (q == p ? 0.0f : B[64 * i + q]) - f * B[64 * p + q];
+      }
+      __syncthreads();
+    }
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int i = e / n, q = e - i * n;
+      if (q > i) {
+        const float m = 0.5f * (B[64 * i + q] + B[64 * q + i]);
+        B[64 * i + q] = m;
+        B[64 * q + i] = m;
+      }
+    }
+    for (int e = threadIdx.x; e < L.P * (L.ny + 2); e += blockDim.x) col[e] = 0.0f;
+    __syncthreads();
   }
   __device__ __forceinline__ void set_rhs(int k, int, float v) { b0[k] = v; }
   __device__ __forceinline__ float y(int k, int) const { return k == pk ? 0.0f : __ldcg(x0a + k); }
@@ -1552,6 +1628,52 @@ struct MgInner {
       }
     }
   }
+  // The coarsest level solved by the first warp: x = P B P b (B the dense
+  // inverse of coarse_inverse, P the projection off the constant), into xa.
+  __device__ void coarsest_exact(int l) const {
+    const MgLv L = lv(l, true);
+    const int n = L.nx * L.ny, lane = threadIdx.x & 31;
+    const float* B = sm + H.inv_off;
+    float* v = L.xb;  // the mean-free right-hand side, compact
+    int kk[2];
+    float bb[2];
+    float sum = 0.0f;
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+      const int c = lane + 32 * m;
+      kk[m] = -1;
+      bb[m] = 0.0f;
+      if (c < n) {
+        const int j = c / L.nx, i = c - j * L.nx;
+        kk[m] = L.id(i + 1, j + 1);
+        bb[m] = L.b[kk[m]];
+        sum += bb[m];
+      }
+    }
+    // reference gauge: P B P with P the projection off the constant; the
+    // pinned gauge's coarse operator is nonsingular (plain B)
+    const bool proj = pk < 0;
+    const float mb = proj ? warp_sum(sum) / (float)n : 0.0f;
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+      if (kk[m] >= 0) v[lane + 32 * m] = bb[m] - mb;
+    __syncwarp();
+    float x[2] = {0.0f, 0.0f};
+    for (int c = 0; c < n; ++c) {
+      const float vc = v[c];
+      x[0] = __fmaf_rn(B[64 * c + lane], vc, x[0]);
+      x[1] = __fmaf_rn(B[64 * c + lane + 32], vc, x[1]);
+    }
+    float sx = 0.0f;
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+      if (kk[m] >= 0) sx += x[m];
+    const float mx = proj ? warp_sum(sx) / (float)n : 0.0f;
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+      if (kk[m] >= 0) L.xa[kk[m]] = x[m] - mx;
+    __syncwarp();
+  }
   // the tail levels, block 0 alone out of shared memory: b_tail in from
   // global memory, the tail's correction back out
   __device__ void tail_cycle() const {
@@ -1573,7 +1695,9 @@ struct MgInner {
     }
     // the coarsest level: a small one runs in the first warp alone, so its
     // many sweeps synchronise with __syncwarp instead of block barriers
-    if ((long long)H.lv[L - 1].nx * H.lv[L - 1].ny <= 64) {
+    if (H.exact) {
+      if (threadIdx.x < 32) coarsest_exact(L - 1);
+    } else if ((long long)H.lv[L - 1].nx * H.lv[L - 1].ny <= 64) {
       if (threadIdx.x < 32) coarsest_warp(L - 1);
     } else if ((long long)H.lv[L - 1].nx * H.lv[L - 1].ny <= kMgWarpCoarse) {
       if (threadIdx.x < 32) {

@@ -32,6 +32,10 @@ struct MgHier {
   float cw;    // coarse-correction weight
   int nu, nuc; // sweeps before / after each coarse correction; sweeps on the coarsest level
   int tail_smem;     // bytes of block 0's shared memory holding the tail levels
+  // exact != 0: the coarsest level (at most 64 cells, in the tail) is solved
+  // by a dense inverse formed once per solve, 64 x 64 floats at float offset
+  // inv_off of the tail's shared memory, instead of nuc sweeps
+  int exact, inv_off;
 };
 
 struct PoissonArgs {

@@ -173,7 +173,10 @@ typedef struct covof_params {
   double ic_radius;      /* two-phase length scale 2 ic_radius when l0_ref = 0 (0.25) */
   int uzawa_iter;        /* Uzawa iterations per step (1) */
   double uzawa_tol;      /* stop when max |div u| <= uzawa_tol (1e-12; with uzawa_iter > 1) */
-  int p_mg_nuc;          /* COVOF_INNER_MG: Jacobi sweeps on the coarsest level (0: 8; default 64) */
+  int p_mg_nuc;          /* COVOF_INNER_MG: Jacobi sweeps on the coarsest level; < 0 (default):
+                            solved exactly by a dense inverse formed once per solve when that
+                            level has at most 64 cells and sits in block 0's shared memory
+                            (else 64 sweeps); 0: 64 sweeps */
 } covof_params;
 enum { COVOF_INNER_CHEBYSHEV = 0, COVOF_INNER_CG = 1, COVOF_INNER_CHEBYSHEV_STREAM = 2, COVOF_INNER_MG = 3 };
 

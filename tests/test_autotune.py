@@ -30,7 +30,7 @@ def test_candidates_cover_shapes(pkg, at):
     assert {o["p_mg_nu"] for _, o in cg} == {2, 3, 4}
     assert {o["p_mg_cw"] for _, o in cg} == {1.8, 1.9, 2.0}
     assert {d["p_blocks"] for d, _ in cg} == {152, 76}
-    assert {o["p_mg_nuc"] for _, o in cg} == {32, 64, 128}
+    assert {o["p_mg_nuc"] for _, o in cg} == {-1, 32, 64}
     assert at.tuned_fields(p) == ("p_mg_nu", "p_mg_cw", "p_mg_nuc")
 
 
