@@ -849,7 +849,29 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     __syncthreads();
     int budget = a.max_iter - total_inner;
     if (budget > a.inner_max_iter) budget = a.inner_max_iter;
-    PcgOut o = inner.solve(R, a.inner_tol, budget);
+    double zs[3] = {0.0, 0.0, 0.0};
+    bool zdone = false;
+    PcgOut o{0, COVOF_OK, 0.0, 1.0, true};
+    if constexpr (!Inner::kScaled) {
+      // multigrid: z and its sums formed in the V-cycle's last sweep, which
+      // writes y anyway (one pass over the fine grid fewer)
+      if (budget >= 1 && inner.fused_ok()) {
+        const bool use_q = !fresh;
+        const double rn = r_norm;
+        o = inner.solve_fused(R, budget, [&](int k, float yk) {
+          const double zk = rn * (double)yk;
+          z[k] = zk;
+          zs[0] = fma(1.0, zk, zs[0]);
+          if (use_q) {
+            const double qk = qv[k];
+            zs[1] = fma(zk, qk, zs[1]);
+            zs[2] += qk;
+          }
+        });
+        zdone = true;
+      }
+    }
+    if (!zdone) o = inner.solve(R, a.inner_tol, budget);
     total_inner += o.iters;
     outer++;
     if (!o.ok) { ok = false; break; }
@@ -862,17 +884,18 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     // coefficients), so no extra grid barrier is needed.
     // One reduction gives gam and the orthogonalisation against the previous
     // direction: beta = <z, q_old> / <p_old, q_old>.
-    double zs[3] = {0.0, 0.0, 0.0};
-    own.each([&](int k, int c) {
-      const double zk = (r_norm * scl(k)) * (double)inner.y(k, c);
-      z[k] = zk;
-      zs[0] = fma(wgt(k), zk, zs[0]);
-      if (!fresh) {
-        const double qk = qv[k];
-        zs[1] = fma(zk, qk, zs[1]);
-        zs[2] += qk;
-      }
-    });
+    if (!zdone) {
+      own.each([&](int k, int c) {
+        const double zk = (r_norm * scl(k)) * (double)inner.y(k, c);
+        z[k] = zk;
+        zs[0] = fma(wgt(k), zk, zs[0]);
+        if (!fresh) {
+          const double qk = qv[k];
+          zs[1] = fma(zk, qk, zs[1]);
+          zs[2] += qk;
+        }
+      });
+    }
     // Reference gauge: the projection removes gam (aP-weighted mean of z);
     // the constant mode itself is then solved exactly, a coarse correction
     // z += (1'r / 1'A1) 1 -- without it the iterate would stay on the
@@ -1394,9 +1417,13 @@ struct MgInner {
     v = __fmaf_rn(-L.ay[k + L.P], ld<S>(x + k + L.P), v);
     return v;
   }
-  // one damped Jacobi sweep from buffer cur into the other (first: x = 0)
-  template <bool S, bool W = false>
-  __device__ void sweep(int l, bool first, int cur) const {
+  struct NoEpi {
+    __device__ __forceinline__ void operator()(int, float) const {}
+  };
+  // one damped Jacobi sweep from buffer cur into the other (first: x = 0);
+  // epi(k, v) sees every value written
+  template <bool S, bool W = false, class Epi = NoEpi>
+  __device__ void sweep(int l, bool first, int cur, Epi epi = Epi()) const {
     const MgLv L = lv(l, S);
     const float* xs = cur ? L.xb : L.xa;
     float* xd = cur ? L.xa : L.xb;
@@ -1418,6 +1445,7 @@ struct MgInner {
       }
       if (k == pin) v = 0.0f;
       xd[k] = v;
+      epi(k, v);
     });
   }
   // b_{l+1} = restriction of the residual of level l (buffer cur)
@@ -1730,7 +1758,10 @@ struct MgInner {
   }
   // One V-cycle on b0 into x0a.  b0 is complete on entry (a grid barrier
   // since its last write) and x0a on return.
-  __device__ bool vcycle(GridReducer& R) const {
+  // kEpi: the last level-0 sweep hands every value to epi and the cycle
+  // returns without its closing barrier (the caller's reduction is one)
+  template <bool kEpi = false, class Epi = NoEpi>
+  __device__ bool vcycle(GridReducer& R, Epi epi = Epi()) const {
     const int L = H.nl, nu = H.nu, t = H.tail;
     bool ok = true;
     for (int l = 0; ok && l < t && l < L - 1; ++l) {
@@ -1757,11 +1788,27 @@ struct MgInner {
       prolong<false>(l, nu & 1, out_buf(l + 1));
       for (int s = 0; ok && s < nu; ++s) {
         ok = R.gs.sync();
-        if (ok) sweep<false>(l, false, (nu + s) & 1);
+        if (!ok) break;
+        if (kEpi && l == 0 && s == nu - 1) sweep<false, false, Epi>(l, false, (nu + s) & 1, epi);
+        else sweep<false>(l, false, (nu + s) & 1);
       }
+      if (kEpi && l == 0) return ok;
       ok = ok && R.gs.sync();
     }
     return ok;
+  }
+  // the epilogue form needs level 0 among the grid-wide levels of the cycle
+  __device__ __forceinline__ bool fused_ok() const { return H.nl >= 2; }
+  // One V-cycle whose last level-0 sweep hands each value y(k) to epi; no
+  // closing barrier (the caller reduces what epi accumulated)
+  template <class Epi>
+  __device__ PcgOut solve_fused(GridReducer& R, int budget, Epi epi) {
+    PcgOut o{0, COVOF_OK, 0.0, 1.0, true};
+    if (budget < 1) return o;
+    const bool ok = R.gs.sync() && vcycle<true, Epi>(R, epi);
+    o.iters = 1;
+    if (!ok) { o.ok = false; o.status = COVOF_TIMEOUT; }
+    return o;
   }
   __device__ PcgOut solve(GridReducer& R, double, int budget) {
     PcgOut o{0, COVOF_OK, 0.0, 1.0, true};
