@@ -71,6 +71,11 @@ __device__ bool ssor_band(const SsorArgs& A, const SsorJob& J, int s, int b) {
 #pragma unroll
   for (int q = 0; q < kSsorAhead; ++q) fetch(q, ring[q]);
   double prev = 0.0;
+  // the neighbouring band's edge row for lane 0, one chunk at a time: lane q
+  // holds column t0 + q, loaded together right after the chunk's wait, so
+  // lane 0's step reads a register (a shuffle) instead of waiting on L2
+  double edge = 0.0;
+  const int j0 = fwd ? 32 * b + 1 : 32 * b + 32;  // lane 0's row
   const int T = ni + 31;
   for (int tt = 0; tt < T; tt += kSsorAhead) {
 #pragma unroll
@@ -79,7 +84,14 @@ __device__ bool ssor_band(const SsorArgs& A, const SsorJob& J, int s, int b) {
       if (t >= T) break;  // uniform across the warp
       if ((t & 31) == 0 && t < ni && has_dep) {
         if (!warp_wait_ge(J.prog + 32 * dep, base + (unsigned int)(t >> 5) + 1u, A.err)) return false;
+        const int cq = t + lane;
+        edge = 0.0;
+        if (cq < ni) {
+          const int iq = fwd ? cq + 1 : ni - cq;
+          edge = __ldcg(J.r + D.id(iq, j0) - ahead_row);
+        }
       }
+      const double edge0 = __shfl_sync(0xffffffffu, edge, t & 31);
       const double across = __shfl_up_sync(0xffffffffu, prev, 1);
       const int c = t - lane;
       if (valid && c >= 0 && c < ni) {
@@ -89,7 +101,7 @@ __device__ bool ssor_band(const SsorArgs& A, const SsorJob& J, int s, int b) {
         const bool edge_back = fwd ? (i == 1) : (i == ni);
         // across a domain edge the neighbour is a ghost entry, zero
         const double back = edge_back ? 0.0 : prev;
-        const double back_row = edge_back_row ? 0.0 : (lane == 0 ? __ldcg(J.r + k - ahead_row) : across);
+        const double back_row = edge_back_row ? 0.0 : (lane == 0 ? edge0 : across);
         double vW, vE, vS, vN;
         if (fwd) { vW = back; vE = o.e; vS = back_row; vN = o.n; }
         else     { vE = back; vW = o.e; vN = back_row; vS = o.n; }

@@ -82,6 +82,11 @@ __device__ bool svof_band(const SvofArgs& a, int s, int b) {
 #pragma unroll
   for (int q = 0; q < kSvofAhead; ++q) fetch(q, rc[q], ra[q], rr[q]);
   double prev = 0.0;  // this lane's value of the previous step
+  // the neighbouring band's edge row for lane 0, one chunk at a time: lane q
+  // holds column t0 + q, loaded together right after the chunk's wait, so
+  // lane 0's step reads a register (a shuffle) instead of waiting on L2
+  double edge = 0.0;
+  const int j0 = fwd ? 32 * b + 1 : 32 * b + 32;  // lane 0's row
   const int T = nx + 31;
   for (int tt = 0; tt < T; tt += kSvofAhead) {
 #pragma unroll
@@ -92,7 +97,14 @@ __device__ bool svof_band(const SvofArgs& a, int s, int b) {
       // chunk is left to wait for)
       if ((t & 31) == 0 && t < nx && has_dep) {
         if (!warp_wait_ge(a.prog + 32 * dep, base + (unsigned int)(t >> 5) + 1u, a.err)) return false;
+        const int cq = t + lane;
+        edge = 0.0;
+        if (cq < nx) {
+          const int iq = fwd ? cq + 1 : nx - cq;
+          edge = __ldcg(a.Cs + D.id(iq, j0) - ahead_row);
+        }
       }
+      const double edge0 = __shfl_sync(0xffffffffu, edge, t & 31);
       // lane r-1's previous value: the new neighbour across the band's rows
       const double across = __shfl_up_sync(0xffffffffu, prev, 1);
       const int c = t - lane;
@@ -110,8 +122,7 @@ __device__ bool svof_band(const SvofArgs& a, int s, int b) {
         // neighbours across a wall enter with a zero coefficient; they are
         // read as 0 (the reference multiplies its Neumann ghost copy by 0)
         const double back = edge_back ? 0.0 : prev;  // new, this lane's previous step
-        const double back_row = edge_back_row ? 0.0
-                              : (lane == 0 ? __ldcg(a.Cs + k - ahead_row) : across);  // new
+        const double back_row = edge_back_row ? 0.0 : (lane == 0 ? edge0 : across);  // new
         double vE, vW, vN, vS;
         if (fwd) { vE = ra[q]; vW = back; vN = rr[q]; vS = back_row; }
         else     { vW = ra[q]; vE = back; vS = rr[q]; vN = back_row; }
