@@ -375,6 +375,57 @@ def mono_steps(pkg, orc, n, nsteps, cpu_steps):
     return out
 
 
+def vof_steps(pkg, orc, reps):
+    """The VOF path on its own: ELVIRA reconstruction and whole Weymouth-Yue
+    steps (two direction passes) on device fields for the C1 bubble
+    (128x256, 16x16 sub-samples) and the same bubble at 1024x2048.  The
+    reconstruction is FP64 polygon clipping: its FP64 rate is estimated from
+    the interface cells (371 cut-box evaluations of ~60 flops per interface
+    cell) and set against the FP64 rate this GPU sustains on independent
+    FMA chains (covof_fp64_peak)."""
+    import ctypes
+    import torch
+    cap = pkg.capi
+    out = {"model": "FP64 work = interface cells x 371 cut_box_area x 60 flops per reconstruction"}
+    for nx, ny, nsub in ((128, 256, 16), (1024, 2048, 4)):
+        p, C0, dt = pkg.cases.bubble_case(nx=nx, ny=ny, nsub=nsub)
+        f = pkg.Fields.allocate(p)
+        f.C[...] = C0
+        orc.apply_vof_bc(p, f.C)
+        f.u[...], f.v[...] = pkg.cases.random_velocity(p, 0.05, 7)
+        orc.apply_velocity_bc(p, f.u, f.v, False)
+        inner = f.C[1:-1, 1:-1]
+        mixed = int(((inner > 0.0) & (inner < 1.0)).sum())
+        T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+        tC, tu, tv = T(f.C), T(f.u), T(f.v)
+        seg = torch.zeros(3 * tC.numel(), dtype=torch.float64, device=tC.device)
+        with pkg.Solver(p) as s:
+            peak = s.fp64_peak()
+            stream = torch.cuda.ExternalStream(s.stream_ptr)
+            rec, wy = [], []
+            for r in range(reps + 1):
+                e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+                torch.cuda.synchronize()
+                e0.record(stream)
+                st = s.lib.covof_vof_reconstruct_dev(s.h, ctypes.c_void_p(tC.data_ptr()),
+                                                     ctypes.c_void_p(seg.data_ptr()))
+                e1.record(stream)
+                st2 = s.lib.covof_vof_wy_step_dev(s.h, 1e-4, r % 2, ctypes.c_void_p(tu.data_ptr()),
+                                                  ctypes.c_void_p(tv.data_ptr()), ctypes.c_void_p(tC.data_ptr()))
+                e2.record(stream)
+                e2.synchronize()
+                assert st == cap.OK and st2 == cap.OK, (st, st2)
+                if r > 0:
+                    rec.append(e0.elapsed_time(e1))
+                    wy.append(e1.elapsed_time(e2))
+        rms = statistics.mean(rec)
+        gf = mixed * 371.0 * 60.0 / (rms * 1e-3) / 1e9
+        out[f"{nx}x{ny}"] = {"interface_cells": mixed, "reconstruct_ms": rms, "wy_step_ms": statistics.mean(wy),
+                             "reconstruct_fp64_gflops_est": gf, "fp64_peak_gflops_measured": peak,
+                             "frac": gf / peak}
+    return out
+
+
 def run_reference(args, world, rank):
     """--impl reference: the reference path's CPU implementation (the FP64
     C++ restatement; the Fortran reference cannot be built on these
@@ -558,6 +609,7 @@ def run_ours(args, world, rank, local):
         adjoint = None if args.skip_steps else adjoint_steps(pkg, 512, 3)
         rt = None if (args.skip_steps or args.skip_rt) else rt_steps(pkg, orc, 3)
         mono = None if args.skip_steps else mono_steps(pkg, orc, 256, 5, 0 if args.skip_cpu else 2)
+        vof = None if args.skip_steps else vof_steps(pkg, orc, 5)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
@@ -597,6 +649,7 @@ def run_ours(args, world, rank, local):
             "adjoint": adjoint,
             "rayleigh_taylor": rt,
             "monolithic": mono,
+            "vof": vof,
         }
     for r in results.values():
         r["solver"].close()

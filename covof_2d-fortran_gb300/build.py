@@ -22,7 +22,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_build"
 LIB = OUT_DIR / "libcovof_gpu.so"
-SOURCES = ["poisson.cu", "momentum.cu", "vof.cu", "svof.cu", "adjoint.cu", "capi.cu", "batch.cu", "static_scratch.cu", "output.cu", "precond.cu"]
+SOURCES = ["poisson.cu", "momentum.cu", "vof.cu", "svof.cu", "adjoint.cu", "capi.cu", "batch.cu", "static_scratch.cu", "output.cu", "precond.cu", "peak.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [

@@ -152,6 +152,7 @@ _SIGS = {
     "covof_al_step": [_VP, C.c_double] + [_VP] * 12 + [_IP, _IP],
     "covof_monolithic_step": [_VP, C.c_double] + [_VP] * 11 + [_IP],
     "covof_precond_apply": [_VP, C.c_double] + [_VP] * 13,
+    "covof_fp64_peak": [_VP, C.POINTER(C.c_double)],
     "covof_vtk_write_async": [_VP, C.c_char_p, C.c_char_p, C.c_int],
     "covof_vtk_wait": [_VP],
     "covof_history_open": [_VP, C.c_char_p, C.c_char_p],

@@ -312,6 +312,12 @@ class Solver:
                                                _dptr(gbv), C.byref(it), C.byref(rr))
         return it.value, rr.value, self._check(st, "covof_projection_vjp_dev")
 
+    def fp64_peak(self) -> float:
+        """GFLOP/s of independent FP64 FMA chains on this GPU."""
+        g = C.c_double()
+        self._check(self.lib.covof_fp64_peak(self.h, C.byref(g)), "covof_fp64_peak")
+        return g.value
+
     # -- geometric VOF ----------------------------------------------------------
     def reconstruct_interface(self, Cf: np.ndarray) -> np.ndarray:
         seg = np.zeros(Cf.shape + (3,), dtype=np.float64)

@@ -395,6 +395,11 @@ int covof_monolithic_step(covof_handle* h, double dt, double* u, double* v, doub
                           const double* rho_v, const double* mu, const double* mu_node, const double* fx_sigma,
                           const double* fy_sigma, const double* u_old, const double* v_old, int* iters);
 
+/* The FP64 rate this GPU sustains on independent FMA chains (GFLOP/s, two
+ * flops per FMA), measured on the handle's stream: the denominator of the
+ * interface reconstruction's FP64 rate. */
+int covof_fp64_peak(covof_handle* h, double* gflops);
+
 /* ---- device-resident time stepping ------------------------------------ */
 
 /* The members of flow_fields_t (src/module_fields.f90:27-92) that the hot
