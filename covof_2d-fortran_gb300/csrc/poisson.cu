@@ -1855,6 +1855,7 @@ __device__ void mixed_mg_case(const PoissonArgs& a, const Team& tm, GridReducer&
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg(PoissonArgs a) {
   extern __shared__ float mg_tail[];
   __shared__ MgLv mg_tab[2 * kMgMaxLevels];
+  if (a.redo && *a.redo == 0) return;  // the pinned fallback, not needed (every block agrees)
   const Team tm = grid_team();
   GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   mixed_mg_case(a, tm, R, mg_tail, mg_tab);
@@ -2038,6 +2039,84 @@ __global__ void k_poisson_apply(Dims D, const double* __restrict__ x, double* __
   if (i > D.nx || j > D.ny) return;
   int k = D.id(i, j);
   y[k] = stencil_exact(D, k, x, ax, ay, aP);
+}
+
+
+// ---------------------------------------------------------------------------
+// Pinned gauge through the reference gauge (see poisson.cuh).  Cell (1,1) is
+// k = D.P + 1; the pinned system's right-hand side holds 0 there.
+__global__ void __launch_bounds__(256) k_pin_sum(Dims D, const double* __restrict__ b, double* __restrict__ part) {
+  double acc[1] = {0.0};
+  const int n = D.nx * D.ny;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const int j = c / D.nx, i = c - j * D.nx;
+    acc[0] += b[D.id(i + 1, j + 1)];
+  }
+  block_sum<double, 1>(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
+}
+
+__global__ void __launch_bounds__(256) k_pin_rhs(Dims D, double* __restrict__ b, const double* __restrict__ part) {
+  double acc[1] = {0.0};
+  for (int q = threadIdx.x; q < kPinBlocks; q += blockDim.x) acc[0] += part[q];
+  block_sum<double, 1>(acc);
+  // b(1,1) is 0 in the pinned right-hand side, so the sum is the others'
+  if (threadIdx.x == 0) b[D.P + 1] = -acc[0];
+}
+
+__global__ void k_pin_level(Dims D, const double* __restrict__ x, double* __restrict__ s) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) s[0] = x[D.P + 1];
+}
+
+__global__ void k_pin_shift(Dims D, double* __restrict__ x, const double* __restrict__ s) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > D.nx || j > D.ny) return;
+  const int k = D.id(i, j);
+  x[k] = x[k] - s[0];
+}
+
+__global__ void __launch_bounds__(256) k_pin_resid(Dims D, const double* __restrict__ b,
+                                                   const double* __restrict__ x,
+                                                   const double* __restrict__ ax,
+                                                   const double* __restrict__ ay,
+                                                   const double* __restrict__ aP, double* __restrict__ part) {
+  double acc[2] = {0.0, 0.0};
+  const int n = D.nx * D.ny, pin = D.P + 1;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const int j = c / D.nx, i = c - j * D.nx;
+    const int k = D.id(i + 1, j + 1);
+    if (k == pin) continue;  // the pinned row: x(1,1) = 0 holds exactly
+    const double bk = b[k];
+    const double r = bk - stencil_exact(D, k, x, ax, ay, aP);
+    acc[0] = fma(r, r, acc[0]);
+    acc[1] = fma(bk, bk, acc[1]);
+  }
+  block_sum<double, 2>(acc);
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = acc[0]; part[2 * blockIdx.x + 1] = acc[1]; }
+}
+
+__global__ void __launch_bounds__(256) k_pin_final(Dims D, double* __restrict__ b, const double* __restrict__ part,
+                                                   double tol, PcgResult* res, int* redo) {
+  double acc[2] = {0.0, 0.0};
+  for (int q = threadIdx.x; q < kPinBlocks; q += blockDim.x) {
+    acc[0] += part[2 * q];
+    acc[1] += part[2 * q + 1];
+  }
+  block_sum<double, 2>(acc);
+  if (threadIdx.x == 0) {
+    double bn = sqrt(acc[1]);
+    if (bn < 1.0e-30) bn = 1.0;
+    const double rel = sqrt(acc[0]) / bn;
+    b[D.P + 1] = 0.0;  // the pinned right-hand side again
+    res->relres = rel;
+    const int bad = !(rel <= tol);
+    *redo = bad;
+    // the pinned residual decides: a reference-gauge run that stopped on its
+    // own limit but left the pinned system solved is a converged solve
+    if (!bad && res->status == COVOF_MAXITER) res->status = COVOF_OK;
+    if (bad && res->status == COVOF_OK) res->status = COVOF_MAXITER;
+  }
 }
 
 }  // namespace covof

@@ -55,6 +55,7 @@ struct PoissonArgs {
   // control
   unsigned int* bar; int* err; double* part;  // part: 16 * nblocks doubles
   PcgResult* res;
+  const int* redo;  // non-null: the launch runs only if *redo != 0 (the pinned fallback)
   double tol, inner_tol;
   int max_iter, inner_max_iter, max_refine, pinned;
 };
@@ -78,6 +79,20 @@ struct Tiles {
 };
 __host__ __device__ Tiles make_tiles(const Dims& D, int threads = 1024);
 __global__ void k_pcg_fp64(PoissonArgs a);
+// The pinned gauge through the reference gauge (mixed multigrid): b(1,1) :=
+// -sum of the other cells' b makes the Neumann system consistent, its
+// solution shifted by -x(1,1) solves the pinned one; the pinned residual is
+// then checked and the pinned solve rerun from it if the check fails.
+constexpr int kPinBlocks = 256;
+__global__ void k_pin_sum(Dims D, const double* __restrict__ b, double* __restrict__ part);
+__global__ void k_pin_rhs(Dims D, double* __restrict__ b, const double* __restrict__ part);
+__global__ void k_pin_level(Dims D, const double* __restrict__ x, double* __restrict__ s);
+__global__ void k_pin_shift(Dims D, double* __restrict__ x, const double* __restrict__ s);
+__global__ void k_pin_resid(Dims D, const double* __restrict__ b, const double* __restrict__ x,
+                            const double* __restrict__ ax, const double* __restrict__ ay,
+                            const double* __restrict__ aP, double* __restrict__ part);
+__global__ void k_pin_final(Dims D, double* __restrict__ b, const double* __restrict__ part, double tol,
+                            PcgResult* res, int* redo);
 __global__ void k_pcg_mixed(PoissonArgs a);
 __global__ void k_pcg_mixed_smem(PoissonArgs a);
 __global__ void k_pcg_mixed_cheb(PoissonArgs a);
