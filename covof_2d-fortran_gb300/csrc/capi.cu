@@ -80,7 +80,8 @@ int ensure_poisson(covof_handle* h) {
   CS(dalloc(&h->pxb, (size_t)8 * h->sm_count * (size_t)(h->D.nx + 2)));
   CS(dalloc(&h->e32, g)); CS(dalloc(&h->r32b, g)); CS(dalloc(&h->r32, g)); CS(dalloc(&h->d32, g));
   CS(dalloc(&h->Ad32, g)); CS(dalloc(&h->ax32, g)); CS(dalloc(&h->ay32, g)); CS(dalloc(&h->aP32, g));
-  CS(dalloc(&h->pin_part, (size_t)2 * kPinBlocks + 2)); CS(dalloc(&h->pin_redo, 1));
+  CS(dalloc(&h->pin_part, (size_t)4 * kPinBlocks + 4)); CS(dalloc(&h->pin_ctl, 4));
+  CS(dalloc(&h->pin_b, g));
   // multigrid levels: halve each dimension down to about 64 cells
   MgHier& H = h->mg;
   H.nl = 1;
@@ -422,6 +423,7 @@ int pois_pre(covof_handle* h, double dt, const double* u, const double* v, const
   a.tol = P.p_tol; a.inner_tol = P.p_inner_tol;
   a.max_iter = P.p_max_iter; a.inner_max_iter = P.p_inner_max_iter;
   a.max_refine = P.p_max_refine; a.pinned = pinned;
+  a.bskip = -1;
   a.mg = h->mg;
   return COVOF_OK;
 }
@@ -443,29 +445,34 @@ int poisson_enqueue(covof_handle* h, double dt, const double* u, const double* v
   const covof_params& P = h->prm;
   if (P.p_precision == COVOF_PREC_MIXED && P.p_inner_kind == COVOF_INNER_MG && a.pinned &&
       h->p_fn == (const void*)k_pcg_mixed_mg) {
-    // The pinned system solved as the consistent Neumann one: the reference
-    // gauge's deflation handles the constant mode exactly (29 against 41
-    // outer iterations at 1024^2), then x -= x(1,1), the pinned residual
-    // checked, and the pinned solve run from there only if that check fails.
+    // The pinned system solved through the reference gauge, whose
+    // deflation handles the constant mode exactly (35 against 41 outer
+    // iterations at 1024^2); the pinned residual is checked after the shift
+    // and the pinned solve rerun only if the check fails (see poisson.cuh).
     const Dims& D = h->D;
     double* part = h->pin_part;
-    double* lvl = h->pin_part + 2 * kPinBlocks;
+    double* lvl = h->pin_part + 4 * kPinBlocks;
+    int* ctl = h->pin_ctl;
     const dim3 blk(32, 8), grd = grid2(P.nx, P.ny, blk);
     if (timed) CK(cudaEventRecord(h->ev0, h->stream));
-    k_pin_sum<<<kPinBlocks, 256, 0, h->stream>>>(D, h->pb, part);
-    k_pin_rhs<<<1, 256, 0, h->stream>>>(D, h->pb, part);
+    k_pin_sum<<<kPinBlocks, 256, 0, h->stream>>>(D, h->pb, h->px, h->pax, h->pay, h->paP, part, ctl);
+    k_pin_rhs<<<1, 256, 0, h->stream>>>(D, part, lvl, ctl);
+    k_pin_form<<<grd, blk, 0, h->stream>>>(D, h->pb, h->pax, h->pay, h->paP, h->pin_b, lvl, ctl);
     CK(cudaGetLastError());
     PoissonArgs ar = a;
     ar.pinned = 0;
+    ar.b = h->pin_b;
+    ar.bskip = D.P + 1;
+    ar.redo = ctl + 2;
     void* args_r[] = {&ar};
     CS(launch_coop(h, h->p_fn, h->p_nb, h->p_threads, args_r, false, h->p_smem));
-    k_pin_level<<<1, 32, 0, h->stream>>>(D, h->px, lvl);
-    k_pin_shift<<<grd, blk, 0, h->stream>>>(D, h->px, lvl);
-    k_pin_resid<<<kPinBlocks, 256, 0, h->stream>>>(D, h->pb, h->px, h->pax, h->pay, h->paP, part);
-    k_pin_final<<<1, 256, 0, h->stream>>>(D, h->pb, part, P.p_tol, h->d_pres, h->pin_redo);
+    k_pin_level<<<1, 32, 0, h->stream>>>(D, h->px, lvl, ctl);
+    k_pin_shift<<<grd, blk, 0, h->stream>>>(D, h->px, lvl, ctl);
+    k_pin_resid<<<kPinBlocks, 256, 0, h->stream>>>(D, h->pb, h->px, h->pax, h->pay, h->paP, part, ctl);
+    k_pin_final<<<1, 256, 0, h->stream>>>(D, part, P.p_tol, h->d_pres, ctl);
     CK(cudaGetLastError());
     PoissonArgs af = a;
-    af.redo = h->pin_redo;
+    af.redo = ctl;
     void* args_f[] = {&af};
     CS(launch_coop(h, h->p_fn, h->p_nb, h->p_threads, args_f, false, h->p_smem));
     if (timed) CK(cudaEventRecord(h->ev1, h->stream));
@@ -1336,7 +1343,7 @@ int covof_destroy(covof_handle* h) {
   for (float** q : ff) dfree(*q);
   drop_graphs(h);
   dfree(h->bar); dfree(h->err); dfree(h->d_pres); dfree(h->d_kres); dfree(h->d_run);
-  dfree(h->vlist); dfree(h->vcount); dfree(h->mg.pool); dfree(h->pin_part); dfree(h->pin_redo);
+  dfree(h->vlist); dfree(h->vcount); dfree(h->mg.pool); dfree(h->pin_part); dfree(h->pin_ctl); dfree(h->pin_b);
   if (h->h_pres) cudaFreeHost(h->h_pres);
   if (h->h_kres) cudaFreeHost(h->h_kres);
   if (h->h_run) cudaFreeHost(h->h_run);

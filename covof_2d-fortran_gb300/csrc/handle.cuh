@@ -101,8 +101,11 @@ struct covof_handle {
   float *e32 = nullptr, *r32b = nullptr, *r32 = nullptr, *d32 = nullptr, *d32b = nullptr, *Ad32 = nullptr,
         *ax32 = nullptr, *ay32 = nullptr, *aP32 = nullptr;
   covof::MgHier mg{};  // multigrid hierarchy of the FP32 inner operator (pool: levels >= 1)
-  double* pin_part = nullptr;  // pinned gauge through the reference gauge: partial sums, level
-  int* pin_redo = nullptr;     // ... and the fallback flag
+  // pinned gauge through the reference gauge: partial sums and levels, the
+  // control ints, the consistent right-hand side
+  double* pin_part = nullptr;
+  int* pin_ctl = nullptr;
+  double* pin_b = nullptr;
   // momentum scratch (each 2g)
   bool have_mom = false;
   double *mx = nullptr, *mrhs = nullptr, *mdiag = nullptr, *mv[7] = {};

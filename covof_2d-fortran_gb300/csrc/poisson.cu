@@ -812,7 +812,7 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     own.each([&](int k, int c) {
       const double rr = (k == pk) ? 0.0 : a.b[k] - own.stencil(k, c, x, a.ax, a.ay, a.aP);
       r[k] = rr;
-      acc[0] = fma(a.b[k], a.b[k], acc[0]);
+      if (k != a.bskip) acc[0] = fma(a.b[k], a.b[k], acc[0]);
       acc[1] = fma(rr, rr, acc[1]);
       acc[2] += rr;
       acc[3] += wgt(k);
@@ -2044,43 +2044,88 @@ __global__ void k_poisson_apply(Dims D, const double* __restrict__ x, double* __
 
 // ---------------------------------------------------------------------------
 // Pinned gauge through the reference gauge (see poisson.cuh).  Cell (1,1) is
-// k = D.P + 1; the pinned system's right-hand side holds 0 there.
-__global__ void __launch_bounds__(256) k_pin_sum(Dims D, const double* __restrict__ b, double* __restrict__ part) {
-  double acc[1] = {0.0};
-  const int n = D.nx * D.ny;
+// k = D.P + 1.  e_k = aP_k - (its four face coefficients) = (A 1)_k.
+__device__ __forceinline__ double pin_ones_image(const Dims& D, int k, const double* ax, const double* ay,
+                                                 const double* aP) {
+  return aP[k] - ax[k] - ax[k + 1] - ay[k] - ay[k + D.P];
+}
+
+__global__ void __launch_bounds__(256) k_pin_sum(Dims D, const double* __restrict__ b, const double* __restrict__ x,
+                                                 const double* __restrict__ ax, const double* __restrict__ ay,
+                                                 const double* __restrict__ aP, double* __restrict__ part,
+                                                 const int* __restrict__ ctl) {
+  if (ctl[1] > 0) return;
+  double acc[3] = {0.0, 0.0, 0.0};  // sum b, sum x0, sum e (b and e without the pinned cell)
+  const int n = D.nx * D.ny, pin = D.P + 1;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
     const int j = c / D.nx, i = c - j * D.nx;
-    acc[0] += b[D.id(i + 1, j + 1)];
+    const int k = D.id(i + 1, j + 1);
+    acc[1] += x[k];
+    if (k == pin) continue;
+    acc[0] += b[k];
+    acc[2] += pin_ones_image(D, k, ax, ay, aP);
   }
-  block_sum<double, 1>(acc);
-  if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
+  block_sum<double, 3>(acc);
+  if (threadIdx.x == 0) {
+    part[3 * blockIdx.x] = acc[0];
+    part[3 * blockIdx.x + 1] = acc[1];
+    part[3 * blockIdx.x + 2] = acc[2];
+  }
 }
 
-__global__ void __launch_bounds__(256) k_pin_rhs(Dims D, double* __restrict__ b, const double* __restrict__ part) {
-  double acc[1] = {0.0};
-  for (int q = threadIdx.x; q < kPinBlocks; q += blockDim.x) acc[0] += part[q];
-  block_sum<double, 1>(acc);
-  // b(1,1) is 0 in the pinned right-hand side, so the sum is the others'
-  if (threadIdx.x == 0) b[D.P + 1] = -acc[0];
+__global__ void __launch_bounds__(256) k_pin_rhs(Dims D, const double* __restrict__ part, double* __restrict__ lvl,
+                                                 int* __restrict__ ctl) {
+  const int active = ctl[1] == 0;
+  __syncthreads();
+  if (threadIdx.x == 0) ctl[2] = active;
+  if (!active) return;
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int q = threadIdx.x; q < kPinBlocks; q += blockDim.x) {
+    acc[0] += part[3 * q];
+    acc[1] += part[3 * q + 1];
+    acc[2] += part[3 * q + 2];
+  }
+  block_sum<double, 3>(acc);
+  if (threadIdx.x == 0) {
+    const double kappa = -acc[1] / (double)((long long)D.nx * D.ny);
+    lvl[1] = kappa;
+    lvl[2] = -fma(kappa, acc[2], acc[0]);
+  }
 }
 
-__global__ void k_pin_level(Dims D, const double* __restrict__ x, double* __restrict__ s) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) s[0] = x[D.P + 1];
-}
-
-__global__ void k_pin_shift(Dims D, double* __restrict__ x, const double* __restrict__ s) {
+__global__ void k_pin_form(Dims D, const double* __restrict__ b, const double* __restrict__ ax,
+                           const double* __restrict__ ay, const double* __restrict__ aP, double* __restrict__ F,
+                           const double* __restrict__ lvl, const int* __restrict__ ctl) {
+  if (!ctl[2]) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (i > D.nx || j > D.ny) return;
   const int k = D.id(i, j);
-  x[k] = x[k] - s[0];
+  F[k] = (k == D.P + 1) ? lvl[2] : fma(lvl[1], pin_ones_image(D, k, ax, ay, aP), b[k]);
+}
+
+__global__ void k_pin_level(Dims D, const double* __restrict__ x, double* __restrict__ lvl,
+                            const int* __restrict__ ctl) {
+  if (threadIdx.x == 0 && blockIdx.x == 0 && ctl[2]) lvl[0] = x[D.P + 1];
+}
+
+__global__ void k_pin_shift(Dims D, double* __restrict__ x, const double* __restrict__ lvl,
+                            const int* __restrict__ ctl) {
+  if (!ctl[2]) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > D.nx || j > D.ny) return;
+  const int k = D.id(i, j);
+  x[k] = x[k] - lvl[0];
 }
 
 __global__ void __launch_bounds__(256) k_pin_resid(Dims D, const double* __restrict__ b,
                                                    const double* __restrict__ x,
                                                    const double* __restrict__ ax,
                                                    const double* __restrict__ ay,
-                                                   const double* __restrict__ aP, double* __restrict__ part) {
+                                                   const double* __restrict__ aP, double* __restrict__ part,
+                                                   const int* __restrict__ ctl) {
+  if (!ctl[2]) return;
   double acc[2] = {0.0, 0.0};
   const int n = D.nx * D.ny, pin = D.P + 1;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
@@ -2096,8 +2141,18 @@ __global__ void __launch_bounds__(256) k_pin_resid(Dims D, const double* __restr
   if (threadIdx.x == 0) { part[2 * blockIdx.x] = acc[0]; part[2 * blockIdx.x + 1] = acc[1]; }
 }
 
-__global__ void __launch_bounds__(256) k_pin_final(Dims D, double* __restrict__ b, const double* __restrict__ part,
-                                                   double tol, PcgResult* res, int* redo) {
+__global__ void __launch_bounds__(256) k_pin_final(Dims D, const double* __restrict__ part, double tol,
+                                                   PcgResult* res, int* ctl) {
+  const int active = ctl[2];
+  __syncthreads();
+  if (!active) {
+    // the pinned solve runs directly; count the direct solves down
+    if (threadIdx.x == 0) {
+      ctl[0] = 1;
+      if (ctl[1] > 0) ctl[1] = ctl[1] - 1;
+    }
+    return;
+  }
   double acc[2] = {0.0, 0.0};
   for (int q = threadIdx.x; q < kPinBlocks; q += blockDim.x) {
     acc[0] += part[2 * q];
@@ -2108,10 +2163,10 @@ __global__ void __launch_bounds__(256) k_pin_final(Dims D, double* __restrict__ 
     double bn = sqrt(acc[1]);
     if (bn < 1.0e-30) bn = 1.0;
     const double rel = sqrt(acc[0]) / bn;
-    b[D.P + 1] = 0.0;  // the pinned right-hand side again
     res->relres = rel;
     const int bad = !(rel <= tol);
-    *redo = bad;
+    ctl[0] = bad;
+    if (bad) ctl[1] = kPinRetry;
     // the pinned residual decides: a reference-gauge run that stopped on its
     // own limit but left the pinned system solved is a converged solve
     if (!bad && res->status == COVOF_MAXITER) res->status = COVOF_OK;

@@ -56,6 +56,7 @@ struct PoissonArgs {
   unsigned int* bar; int* err; double* part;  // part: 16 * nblocks doubles
   PcgResult* res;
   const int* redo;  // non-null: the launch runs only if *redo != 0 (the pinned fallback)
+  int bskip;        // cell left out of ||b|| (the pinned cell on the reference-gauge route), else -1
   double tol, inner_tol;
   int max_iter, inner_max_iter, max_refine, pinned;
 };
@@ -79,20 +80,34 @@ struct Tiles {
 };
 __host__ __device__ Tiles make_tiles(const Dims& D, int threads = 1024);
 __global__ void k_pcg_fp64(PoissonArgs a);
-// The pinned gauge through the reference gauge (mixed multigrid): b(1,1) :=
-// -sum of the other cells' b makes the Neumann system consistent, its
-// solution shifted by -x(1,1) solves the pinned one; the pinned residual is
-// then checked and the pinned solve rerun from it if the check fails.
+// The pinned gauge through the reference gauge (mixed multigrid).  The
+// pinned system (rows k != (1,1), x(1,1) = 0) and the reference-gauge one
+// share the operator A, whose rows sum to e = A 1 (the 1e-12 dvol shift).
+// With kappa = -mean(x0) of the initial guess, the right-hand side
+// F_k = b_k + kappa e_k (k != (1,1)), F(1,1) = -sum of the others, is
+// consistent, and if x0 solves the pinned system, x0 + kappa 1 solves this
+// one; a reference-gauge solution x of F, shifted by -x(1,1), leaves the
+// pinned residual (x(1,1) - kappa) e + (its own residual).  That residual is
+// checked and the pinned solve rerun from the shifted x if the check fails;
+// after a failure the next kPinRetry solves go to the pinned solve directly.
+// ctl (ints): [0] rerun the pinned solve, [1] direct solves left, [2] the
+// reference-gauge route runs in this solve.  lvl (doubles): [0] x(1,1),
+// [1] kappa, [2] F(1,1).
 constexpr int kPinBlocks = 256;
-__global__ void k_pin_sum(Dims D, const double* __restrict__ b, double* __restrict__ part);
-__global__ void k_pin_rhs(Dims D, double* __restrict__ b, const double* __restrict__ part);
-__global__ void k_pin_level(Dims D, const double* __restrict__ x, double* __restrict__ s);
-__global__ void k_pin_shift(Dims D, double* __restrict__ x, const double* __restrict__ s);
+constexpr int kPinRetry = 8;
+__global__ void k_pin_sum(Dims D, const double* __restrict__ b, const double* __restrict__ x,
+                          const double* __restrict__ ax, const double* __restrict__ ay,
+                          const double* __restrict__ aP, double* __restrict__ part, const int* __restrict__ ctl);
+__global__ void k_pin_rhs(Dims D, const double* __restrict__ part, double* __restrict__ lvl, int* __restrict__ ctl);
+__global__ void k_pin_form(Dims D, const double* __restrict__ b, const double* __restrict__ ax,
+                           const double* __restrict__ ay, const double* __restrict__ aP, double* __restrict__ F,
+                           const double* __restrict__ lvl, const int* __restrict__ ctl);
+__global__ void k_pin_level(Dims D, const double* __restrict__ x, double* __restrict__ lvl, const int* __restrict__ ctl);
+__global__ void k_pin_shift(Dims D, double* __restrict__ x, const double* __restrict__ lvl, const int* __restrict__ ctl);
 __global__ void k_pin_resid(Dims D, const double* __restrict__ b, const double* __restrict__ x,
                             const double* __restrict__ ax, const double* __restrict__ ay,
-                            const double* __restrict__ aP, double* __restrict__ part);
-__global__ void k_pin_final(Dims D, double* __restrict__ b, const double* __restrict__ part, double tol,
-                            PcgResult* res, int* redo);
+                            const double* __restrict__ aP, double* __restrict__ part, const int* __restrict__ ctl);
+__global__ void k_pin_final(Dims D, const double* __restrict__ part, double tol, PcgResult* res, int* ctl);
 __global__ void k_pcg_mixed(PoissonArgs a);
 __global__ void k_pcg_mixed_smem(PoissonArgs a);
 __global__ void k_pcg_mixed_cheb(PoissonArgs a);

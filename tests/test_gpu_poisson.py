@@ -152,3 +152,43 @@ def test_full_size_1024_converges_fp64_and_mixed(gpu_pkg, orc):
     for key, x in sols.items():
         d = np.linalg.norm(x - ref) / np.linalg.norm(ref)
         assert d < 1e-7, (key, d)
+
+
+def test_pinned_mixed_mg_route_with_large_level(gpu_pkg, orc):
+    """Pinned gauge, mixed multigrid: a pressure with a large level against
+    its right-hand side (a hydrostatic-like ramp, dt 1e-8) makes the
+    reference-gauge route miss the pinned tolerance, so the pinned solve
+    reruns and the next solves go to it directly before the route is tried
+    again.  Every one of eleven solves on the same handle, cold and warm
+    started, matches the oracle's pinned solution."""
+    pkg = gpu_pkg
+    cap = pkg.capi
+    p, _, ru, rv, _ = _inclusions(pkg, 128, 12)
+    dt = 1.0e-8
+    p.p_gauge = cap.GAUGE_PINNED
+    p.p_tol = 1e-12
+    ny = p.ny
+    ramp = np.zeros((ny + 2, p.nx + 2))
+    ramp[1:-1, 1:-1] = (np.arange(ny, dtype=np.float64) + 0.5)[:, None] * 10.0
+    b0 = orc.poisson_matvec(p, dt, ru, rv, ramp)
+    rng = np.random.default_rng(11)
+    q = p.copy()
+    q.p_precision = cap.PREC_MIXED
+    q.p_inner_kind = cap.INNER_MG
+    x = np.zeros_like(b0)
+    with pkg.Solver(q) as s:
+        for k in range(11):
+            b = b0.copy()
+            b[1:-1, 1:-1] *= 1.0 + 1e-3 * k
+            b[1:-1, 1:-1] += 1e-3 * np.abs(b0).max() * rng.standard_normal((ny, p.nx))
+            ref = np.zeros_like(b)
+            _, _, st_o = orc.poisson_solve_rhs(p, dt, b, ru, rv, ref)
+            assert st_o == 0
+            if k % 2 == 0:
+                x[...] = 0.0  # cold start; odd solves start from the last solution
+            it, rr, st = s.poisson_solve_rhs(dt, b, ru, rv, x)
+            assert st == cap.OK, (k, st, it, rr)
+            assert rr <= 1e-12, (k, rr)
+            assert x[1, 1] == 0.0
+            err = np.linalg.norm(x[1:-1, 1:-1] - ref[1:-1, 1:-1]) / np.linalg.norm(ref[1:-1, 1:-1])
+            assert err < 1e-10, (k, err)
