@@ -642,7 +642,12 @@ def run_ours(args, world, rank, local):
             "cpu_baseline": cpu,
             "e2e": {"value": world * 1000.0 / e2e_step, "unit": UNIT, "h2d_bytes_per_step": gbytes,
                     "d2h_bytes_per_step": b.nbytes},
-            "gpu_launches": 5 * args.steps,
+            # per solve: k_poisson_assemble, k_poisson_scale32, 2 x k_copy_interior,
+            # and the pinned route's k_pin_sum, k_pin_rhs, k_pin_form,
+            # k_pcg_mixed_mg, k_pin_level, k_pin_shift, k_pin_resid,
+            # k_pin_final and the fallback k_pcg_mixed_mg (returns at once
+            # when the pinned check passed)
+            "gpu_launches": 13 * args.steps,
             "clocks": mixed["clocks"],
             "sp_steps": steps,
             "batch": batch,
