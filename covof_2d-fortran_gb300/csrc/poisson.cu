@@ -1448,12 +1448,16 @@ struct MgInner {
       epi(k, v);
     });
   }
-  // b_{l+1} = restriction of the residual of level l (buffer cur)
+  // b_{l+1} = restriction of the residual of level l (buffer cur).
+  // first_next (grid levels): also the first sweep of level l+1 from x = 0,
+  // w b / dg into xb, bit for bit what sweep<false>(l + 1, true, 0) writes
+  // -- one grid-wide phase and barrier fewer per coarse level
   template <bool S>
-  __device__ void restrict_(int l, int cur) const {
+  __device__ void restrict_(int l, int cur, bool first_next = false) const {
     const MgLv F = lv(l, S), Cc = lv(l + 1, S);
     const float* x = cur ? F.xb : F.xa;
     const int pin = l == 0 ? pk : -1;
+    const float w = H.omega;
     cells<S>(Cc.nx, Cc.ny, [&](int I, int J) {
       float s = 0.0f;
       for (int dj = 0; dj < 2; ++dj)
@@ -1464,7 +1468,9 @@ struct MgInner {
           if (k == pin) continue;
           s += ld<S>(F.b + k) - apply<S>(F, x, k);
         }
-      Cc.b[Cc.id(I, J)] = s;
+      const int kc = Cc.id(I, J);
+      Cc.b[kc] = s;
+      if (first_next) Cc.xb[kc] = w * s / Cc.dg[kc];
     });
   }
   // x_l (buffer cl) += cw * x_{l+1} (buffer cc) at the parent cell
@@ -1607,7 +1613,12 @@ struct MgInner {
     for (int e = threadIdx.x; e < L.P * (L.ny + 2); e += blockDim.x) col[e] = 0.0f;
     __syncthreads();
   }
-  __device__ __forceinline__ void set_rhs(int k, int, float v) { b0[k] = v; }
+  // the right-hand side, and with it the first level-0 sweep from x = 0
+  // (w b / dg into x0b, bit for bit what sweep<false>(0, true, 0) writes)
+  __device__ __forceinline__ void set_rhs(int k, int, float v) {
+    b0[k] = v;
+    x0b[k] = k == pk ? 0.0f : H.omega * v / dg0[k];
+  }
   __device__ __forceinline__ float y(int k, int) const { return k == pk ? 0.0f : __ldcg(x0a + k); }
   // The nuc sweeps of a coarsest level of at most 64 cells in the first
   // warp: each lane's (at most two) cells keep their coefficients and
@@ -1765,12 +1776,14 @@ struct MgInner {
     const int L = H.nl, nu = H.nu, t = H.tail;
     bool ok = true;
     for (int l = 0; ok && l < t && l < L - 1; ++l) {
-      for (int s = 0; ok && s < nu; ++s) {
-        if (s > 0) ok = R.gs.sync();
-        if (ok) sweep<false>(l, s == 0, s & 1);
+      // the first sweep (from x = 0) of level 0 came with the right-hand
+      // side, that of a coarse grid level with its restriction
+      for (int s = 1; ok && s < nu; ++s) {
+        if (s > 1) ok = R.gs.sync();
+        if (ok) sweep<false>(l, false, s & 1);
       }
-      ok = ok && R.gs.sync();
-      if (ok) restrict_<false>(l, nu & 1);
+      if (nu > 1) ok = ok && R.gs.sync();
+      if (ok) restrict_<false>(l, nu & 1, l + 1 < t && l + 1 < L - 1);
       ok = ok && R.gs.sync();
     }
     if (!ok) return false;
