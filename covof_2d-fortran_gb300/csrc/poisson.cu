@@ -816,7 +816,9 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       acc[1] = fma(rr, rr, acc[1]);
       acc[2] += rr;
       acc[3] += wgt(k);
-      acc[4] += ones_image(k);
+      const double ek = ones_image(k);
+      acc[4] += ek;
+      if (!pinned) a.w[k] = ek;  // e = A 1, read by every direction update
     });
     double t[8];
     if (!R.sum_map<5, 8>(acc, t, [&](const double* w, double* o) {
@@ -918,7 +920,9 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     const bool was_fresh = fresh;
     own.each([&](int k, int c) {
       double wk = (k == pk) ? 0.0 : own.stencil(k, c, z, a.ax, a.ay, a.aP);
-      if (shift != 0.0) wk -= shift * ones_image(k);
+      // A (z - shift 1) = A z - shift e, e from its buffer: four FP64
+      // subtractions a cell fewer on the pass the FP64 pipe bounds
+      if (shift != 0.0) wk = fma(-shift, a.w[k], wk);
       const double zk = z[k] - shift;
       const double pk_ = was_fresh ? zk : fma(-beta, pv[k], zk);
       const double qk_ = was_fresh ? wk : fma(-beta, qv[k], wk);
