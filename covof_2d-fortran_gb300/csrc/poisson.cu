@@ -785,7 +785,10 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
   // reductions (GridReducer::sum_map), and is broadcast: FP64 issue is the
   // scarce resource of a GB300 SM, and one division evaluated by all 32
   // warps of a block costs microseconds.
-  double b_norm = 1.0, r_norm = 0.0, aP_sum = 1.0, e_sum = 1.0, r_sum = 0.0, sigma_old = 1.0;
+  // reciprocals formed once (FP64 divisions are slow on this part):
+  // 1 / sum of the deflation weights, 1 / sum(A 1), 1 / the previous <p,q>;
+  // rse = sum(r) / sum(A 1)
+  double b_norm = 1.0, r_norm = 0.0, inv_apsum = 1.0, inv_esum = 1.0, rse = 0.0, inv_sigma_old = 1.0;
   double rel = 0.0, cdef = 0.0, inv_r = 0.0;  // r_norm / b_norm, deflation, 1 / r_norm
   bool fresh = true;
   // e = A 1 (interior ones, zero ghosts): the 1e-12*dvol shift of aP, the
@@ -797,14 +800,14 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
   // whose near-null vector is the constant (weights 1, no scaling).
   auto wgt = [&](int k) -> double { return Inner::kScaled ? a.aP[k] : 1.0; };
   auto scl = [&](int k) -> double { return Inner::kScaled ? a.isd[k] : 1.0; };
-  // from ||r||^2 and sum(r): ||r||, ||r|| / ||b||, the deflation r_sum /
-  // aP_sum and 1 / ||r|| (thread 0 only)
-  auto residual_scalars = [&](double rr, double rsum, double bn, double apsum, double* o) {
+  // from ||r||^2 and sum(r): ||r||, sum(r) / sum(A 1), ||r|| / ||b||, the
+  // deflation sum(r) / (sum of the weights) and 1 / ||r|| (thread 0 only)
+  auto residual_scalars = [&](double rr, double rsum, double bn, double* o) {
     const double rn = sqrt(rr);
     o[0] = rn;
-    o[1] = rsum;
+    o[1] = pinned ? 0.0 : rsum * inv_esum;
     o[2] = rn / bn;
-    o[3] = pinned ? 0.0 : rsum / apsum;
+    o[3] = pinned ? 0.0 : rsum * inv_apsum;
     o[4] = 1.0 / rn;
   };
   auto true_residual = [&]() -> bool {
@@ -824,12 +827,14 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     if (!R.sum_map<5, 8>(acc, t, [&](const double* w, double* o) {
           double bn = sqrt(w[0]);
           if (bn < 1.0e-30) bn = 1.0;
-          residual_scalars(w[1], w[2], bn, w[3], o);
-          o[5] = bn; o[6] = w[3]; o[7] = w[4];
+          inv_apsum = 1.0 / w[3];
+          inv_esum = 1.0 / w[4];
+          residual_scalars(w[1], w[2], bn, o);
+          o[5] = bn; o[6] = inv_apsum; o[7] = inv_esum;
         }))
       return false;
-    r_norm = t[0]; r_sum = t[1]; rel = t[2]; cdef = t[3]; inv_r = t[4];
-    b_norm = t[5]; aP_sum = t[6]; e_sum = t[7];
+    r_norm = t[0]; rse = t[1]; rel = t[2]; cdef = t[3]; inv_r = t[4];
+    b_norm = t[5]; inv_apsum = t[6]; inv_esum = t[7];
     return true;
   };
   if (!true_residual()) ok = false;
@@ -905,9 +910,9 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     // eps * mean(p) (about 1e-6 relative for a hydrostatic pressure).
     double sb[2];
     if (!R.sum_map<3, 2>(zs, sb, [&](const double* w, double* o) {
-          const double sh = pinned ? 0.0 : w[0] / aP_sum - r_sum / e_sum;
+          const double sh = pinned ? 0.0 : w[0] * inv_apsum - rse;
           o[0] = sh;
-          o[1] = fresh ? 0.0 : (w[1] - sh * w[2]) / sigma_old;
+          o[1] = fresh ? 0.0 : (w[1] - sh * w[2]) * inv_sigma_old;
         })) {
       ok = false;
       break;
@@ -931,10 +936,11 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       acc[0] = fma(pk_, qk_, acc[0]);
       acc[1] = fma(pk_, r[k], acc[1]);
     });
-    double sa[2];
-    if (!R.sum_map<2, 2>(acc, sa, [&](const double* w, double* o) {
+    double sa[3];
+    if (!R.sum_map<2, 3>(acc, sa, [&](const double* w, double* o) {
           o[0] = w[0];
           o[1] = w[0] > 0.0 ? w[1] / w[0] : 0.0;
+          o[2] = w[0] > 0.0 ? 1.0 / w[0] : 0.0;
         })) {
       ok = false;
       break;
@@ -952,13 +958,13 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     });
     double t2[5];
     if (!R.sum_map<2, 5>(acc2, t2, [&](const double* w, double* o) {
-          residual_scalars(w[0], w[1], b_norm, aP_sum, o);
+          residual_scalars(w[0], w[1], b_norm, o);
         })) {
       ok = false;
       break;
     }
-    r_norm = t2[0]; r_sum = t2[1]; rel = t2[2]; cdef = t2[3]; inv_r = t2[4];
-    sigma_old = sigma;
+    r_norm = t2[0]; rse = t2[1]; rel = t2[2]; cdef = t2[3]; inv_r = t2[4];
+    inv_sigma_old = sa[2];
     fresh = false;
   }
   // mean removal (reference gauge)
