@@ -68,7 +68,7 @@ def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
     assert st == cap.OK
     assert rr <= 1e-12
     err = np.linalg.norm(x[1:-1, 1:-1] - ref[1:-1, 1:-1]) / np.linalg.norm(ref[1:-1, 1:-1])
-    # the spec bar for p is 1e-10 relative L2
+    # the parity bar for p is 1e-10 relative L2
     assert err < 1e-10, err
     if prec == "fp64":
         assert abs(it - it_o) <= max(3, it_o // 50), (it, it_o)
