@@ -1,17 +1,24 @@
 #!/usr/bin/env python
-"""Benchmark: standalone variable-density pressure Poisson, 1024^2 cells,
-200 circular heavy inclusions (rho 1000 / 1), zero-mean Gaussian RHS,
-homogeneous Neumann walls with a pinned reference cell, Jacobi-PCG to
-||r||/||b|| <= 1e-10.  Headline = the mixed path (flexible CG in FP64,
-preconditioned by one FP32 geometric-multigrid V-cycle per iteration); the
-plain FP64 Jacobi-PCG path (the reference's algorithm) and the mixed path
-with the FP32 Chebyshev inner iteration are timed beside it.
+"""Benchmark: the standalone variable-density pressure Poisson on 1024^2
+cells, 200 circular heavy inclusions (rho 1000 / 1), zero-mean Gaussian RHS,
+homogeneous Neumann walls with a pinned reference cell, solved to
+||r||/||b|| <= 1e-10.  Headline = the mixed path: FP64 flexible CG (true FP64
+residual as the exit test) preconditioned by one FP32 geometric-multigrid
+V-cycle per iteration.  Beside it, on the same system and each with its
+error against an oracle solve converged to 1e-13:
+  * plain FP64 Jacobi-PCG (the reference's algorithm for this workload);
+  * the same flexible CG and multigrid kernel with the V-cycle in FP64, so
+    that mixed / FP64-multigrid isolates what the FP32 arithmetic buys;
+  * the mixed path with an FP32 Jacobi-CG inner solve inside the FP64
+    iteration (the workload's literal mixed configuration);
+  * the mixed path with the FP32 Chebyshev inner iteration.
 
-Beside it ("sp_steps"): whole time steps (VOF + STANDARD_PROJECTION) of the
-rising-bubble case, 128x256, device-resident and replayed as CUDA graphs,
-plain FP64 vs mixed Poisson (steps/s); and ("batch") 256 independent
-droplet / bubble cases of uneven sizes stepped together by the batch engine
-(steps/s of the whole batch, mixed vs plain FP64).
+Further legs: whole time steps (VOF + STANDARD_PROJECTION) of the rising
+bubble, 128x256, device-resident and replayed as CUDA graphs; 256
+independent droplet / bubble cases of uneven sizes stepped together by the
+batch engine for 50 steps; the projection and its adjoint at 512^2; the
+Rayleigh-Taylor case at 4096^2 with tuned multigrid settings; the MONOLITHIC
+coupling on a lid-driven cavity; the VOF step on its own.
 
 Before timing, the autotuner (autotune.py) picks the mixed solve's launch
 shape and multigrid smoothing / coarse-correction weight on the same system
@@ -22,6 +29,9 @@ is measured with CUDA events on the library's own stream; a 512 MiB buffer is
 written between steps (outside the timed events) so every step starts with a
 cold L2.  e2e = the same solve through the host C ABI (pinned host arrays,
 H2D of the inputs and D2H of the pressure inside the timed region).
+cpu_baseline and --impl reference time whole FP64 Jacobi-PCG solves of the
+same system to 1e-10 on the host cores (the C++ restatement of the
+reference's solver, OpenMP over every core).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -42,9 +52,18 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "Poisson solves/s at rel-res 1e-10 (1024^2 variable-density, CG+Jacobi; mixed FP32/FP64-refine vs plain FP64)"
+METRIC = ("Poisson solves/s at rel-res 1e-10 (1024^2 variable-density; mixed = FP64 flexible CG + FP32 "
+          "multigrid V-cycle, vs plain FP64 Jacobi-PCG and the FP64 multigrid twin)")
 UNIT = "solves/s"
-WORKLOAD = "variable-density pressure Poisson 1024x1024, 200 inclusions rho 1000/1, Neumann + pinned cell, Jacobi-PCG to rel-res 1e-10"
+WORKLOAD = ("variable-density pressure Poisson 1024x1024, 200 inclusions rho 1000/1, Neumann walls + pinned cell, "
+            "zero-mean Gaussian RHS, solved to rel-res 1e-10 from a zero initial guess")
+
+
+def bench_config(n: int, world: int) -> dict:
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": WORKLOAD.replace("1024x1024", f"{n}x{n}"), "n": n, "inclusions": 200 if n >= 512 else 20, "tol": 1e-10,
+            "gauge": "pinned cell (1,1)", "l2": "flushed between steps (512 MiB write)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 # Algorithmic bytes per cell (per-unit model).
 # Plain FP64 Jacobi-PCG iteration: SpMV (4 words) + x, r update with
 #   <r,z>, <r,r> (7) + direction update (4) = 15 words = 120 B.
@@ -165,29 +184,27 @@ def barrier(world: int):
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(pkg, orc, p, b, ru, rv, dt, iters_full, nthreads, budget_s):
-    """Time Jacobi-PCG iterations of the oracle on the full 1024^2 system for
-    about budget_s seconds and scale to one whole solve."""
-    x = np.zeros_like(b)
+def cpu_solve(orc, p, b, ru, rv, dt, nthreads, tol=1e-10):
+    """One whole FP64 Jacobi-PCG solve of A x = b from a zero guess on
+    nthreads host threads (the oracle's restatement of the reference's
+    solver): (seconds, iterations, relres, solution)."""
     q = p.copy()
     q.p_precision = 0
-    n = 20
+    q.p_precond = 1  # Jacobi
+    q.p_tol = tol
+    q.p_max_iter = 10_000_000
+    x = np.zeros_like(b)
     t0 = time.perf_counter()
-    orc.poisson_fixed_iters(q, dt, b, ru, rv, x, n, nthreads)
-    t1 = time.perf_counter()
-    per_it = (t1 - t0) / n
-    n2 = max(20, min(int(budget_s / max(per_it, 1e-9)), 100000))
-    x[...] = 0.0
-    t0 = time.perf_counter()
-    orc.poisson_fixed_iters(q, dt, b, ru, rv, x, n2, nthreads)
-    t1 = time.perf_counter()
-    per_it = (t1 - t0) / n2
-    solve_s = per_it * iters_full
-    return {"value": 1.0 / solve_s, "unit": UNIT, "cores": nthreads,
-            "kind": "port",
-            "sample": f"{n2} Jacobi-PCG iterations of the FP64 C++ restatement on the full 1024^2 system "
-                      f"({t1 - t0:.1f} s, {per_it * 1e3:.2f} ms/iteration), scaled to the {iters_full} "
-                      f"iterations of one solve to 1e-10"}
+    it, rr, st = orc.poisson_solve_rhs(q, dt, b, ru, rv, x, nthreads)
+    el = time.perf_counter() - t0
+    assert st == 0 and rr <= tol, (st, it, rr)
+    return el, it, rr, x
+
+
+def rel_err(x, ref) -> float:
+    """Relative L2 error of the interior of x against ref."""
+    a, r = x[1:-1, 1:-1], ref[1:-1, 1:-1]
+    return float(np.linalg.norm(a - r) / np.linalg.norm(r))
 
 
 def bubble_state(pkg, orc, prec):
@@ -211,9 +228,10 @@ def sp_steps(pkg, orc, nsteps, cpu_steps):
     steps of the same loop on one host thread."""
     cap = pkg.capi
     out = {"workload": "rising bubble 128x256, ELVIRA + Weymouth-Yue, BiCGSTAB+Jacobi predictor, "
-                       "Jacobi-PCG Poisson to rel-res 1e-10, dt 1e-4, CUDA-graph step replay",
+                       "Poisson to rel-res 1e-10 (fp64: Jacobi-PCG; fp64_mg: FP64 flexible CG + FP64 V-cycle; "
+                       "mixed: the same with the FP32 V-cycle), dt 1e-4, CUDA-graph step replay",
            "steps": nsteps}
-    for name, prec in (("fp64", cap.PREC_FP64), ("mixed", cap.PREC_MIXED)):
+    for name, prec in (("fp64", cap.PREC_FP64), ("fp64_mg", cap.PREC_FP64_MG), ("mixed", cap.PREC_MIXED)):
         p, f, dt = bubble_state(pkg, orc, prec)
         with pkg.Solver(p) as s:
             s.state_set(f)
@@ -224,9 +242,10 @@ def sp_steps(pkg, orc, nsteps, cpu_steps):
                      "poisson_iters_per_step": r["poisson_iters"] / r["steps"],
                      "predictor_iters_per_step": r["mom_iters"] / r["steps"],
                      "max_relres": r["max_relres"]}
-        if name == "mixed":
+        if name != "fp64":
             out[name]["outer_per_step"] = r["refine_steps"] / r["steps"]
     out["speedup_mixed_vs_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    out["speedup_mixed_vs_fp64_mg"] = out["mixed"]["steps_per_s"] / out["fp64_mg"]["steps_per_s"]
     if cpu_steps > 0:
         p, f, dt = bubble_state(pkg, orc, cap.PREC_FP64)
         t0 = time.perf_counter()
@@ -243,12 +262,17 @@ def batch_steps(pkg, orc, ncases, nsteps):
     """Many independent droplet / bubble cases (sizes 64..512 per direction,
     density ratio 10..1000) stepped together by the batch engine, each batch
     step one CUDA-graph launch with the predictor and Poisson solves of all
-    cases in one persistent launch each: mixed vs plain FP64 Poisson."""
+    cases in one persistent launch each: the mixed multigrid Poisson, its
+    FP64 multigrid twin and plain FP64 Jacobi-PCG, nsteps steps each after
+    two warm-up steps."""
+    cap = pkg.capi
     out = {"workload": f"{ncases} droplet/bubble cases, nx, ny in {{64,128,256,512}}, density ratio "
                        "log-uniform 10..1000, viscosity ratio 1..100, sigma 0.01..25, Poisson to rel-res 1e-10, "
                        "CUDA-graph batch step", "cases": ncases, "steps": nsteps}
-    for name, mixed in (("mixed", True), ("fp64", False)):
-        cases = pkg.cases.droplet_batch(n_cases=ncases, mixed=mixed)
+    for name, prec in (("mixed", cap.PREC_MIXED), ("fp64_mg", cap.PREC_FP64_MG), ("fp64", cap.PREC_FP64)):
+        cases = pkg.cases.droplet_batch(n_cases=ncases, mixed=True)
+        for c in cases:
+            c[0].p_precision = prec
         with pkg.Batch([c[0] for c in cases]) as b:
             for i, (p, C0, dt) in enumerate(cases):
                 f = pkg.Fields.allocate(p)
@@ -261,12 +285,13 @@ def batch_steps(pkg, orc, ncases, nsteps):
             st, _, _ = b.run_steps(dts, 2, graph=True)
             st, stats, ms = b.run_steps(dts, nsteps, graph=True)
             info = b.info()
-        assert st == pkg.capi.OK, (name, st)
+        assert st == cap.OK, (name, st)
         out["cells"] = sum(c[0].nx * c[0].ny for c in cases)
         out[name] = {"steps_per_s": 1000.0 * nsteps / ms, "ms_per_step": ms / nsteps,
                      "poisson_iters_per_step": sum(x["poisson_iters"] for x in stats) / nsteps,
                      "max_relres": max(x["max_relres"] for x in stats), **info}
     out["speedup_mixed_vs_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    out["speedup_mixed_vs_fp64_mg"] = out["mixed"]["steps_per_s"] / out["fp64_mg"]["steps_per_s"]
     return out
 
 
@@ -313,31 +338,65 @@ def adjoint_steps(pkg, n, reps):
     return out
 
 
-def rt_steps(pkg, orc, nsteps):
+def rt_steps(pkg, orc, nsteps, args):
     """C5: Rayleigh-Taylor 4096 x 4096 (4:1 domain), whole time steps on the
-    resident fields with the mixed multigrid Poisson; a bounded sample of the
-    200-step run (steps are alike), plus the volume change over the sample."""
+    resident fields with the mixed multigrid Poisson.  The autotuner first
+    picks the multigrid settings and launch shape on the case's own Poisson
+    operator (initial density, a seeded zero-mean right-hand side); then a
+    sample of nsteps steps of the 200-step run (steps are alike) with those
+    settings, the volume change over the sample, and two steps of the FP64
+    multigrid twin with the same settings."""
+    import ctypes
+    import torch
+    cap = pkg.capi
     p, C0, dt = pkg.cases.rt_case(nx=4096, ny=4096, mixed=True)
+    p.p_inner_kind = cap.INNER_MG
     f = pkg.Fields.allocate(p)
     f.C[...] = C0
     orc.apply_vof_bc(p, f.C)
     orc.update_physical_properties(p, f)
     orc.compute_curvature_and_csf(p, f)
+    tuned = None
+    if not args.no_tune:
+        import importlib
+        at = importlib.import_module(pkg.__name__ + ".autotune")
+        rng = np.random.default_rng(pkg.cases.SEED + 6)
+        bt = np.zeros_like(f.C)
+        bt[1:-1, 1:-1] = rng.standard_normal((p.ny, p.nx)) * 1e-6
+        bt[1:-1, 1:-1] -= bt[1:-1, 1:-1].mean()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        tbt, tru, trv = (torch.from_numpy(a).to(dev) for a in (bt, f.rho_u, f.rho_v))
+        tuned = at.tune(p, dt, tbt, tru, trv, repeats=1, cache_path=None, budget_s=args.tune_budget)
+        del tbt, tru, trv
+        for k, v in tuned["params"].items():
+            setattr(p, k, v)
     v0 = float(f.C[1:-1, 1:-1].sum())
-    with pkg.Solver(p) as s:
-        s.state_set(f)
-        st, _ = s.run_steps(dt, 1, graph=False)
-        st, r = s.run_steps(dt, nsteps, graph=False)
-        s.state_get(f)
-    assert st == pkg.capi.OK, st
-    v1 = float(f.C[1:-1, 1:-1].sum())
-    return {"workload": "Rayleigh-Taylor 4096x4096 on [0,1]x[0,4], rho 3/1, ELVIRA + Weymouth-Yue, "
-                        "BiCGSTAB+Jacobi predictor, mixed multigrid Poisson to rel-res 1e-10, dt 2e-5",
-            "steps": nsteps, "ms_per_step": r["ms"] / r["steps"], "steps_per_s": 1000.0 * r["steps"] / r["ms"],
-            "poisson_vcycles_per_step": r["poisson_iters"] / r["steps"],
-            "predictor_iters_per_step": r["mom_iters"] / r["steps"], "max_relres": r["max_relres"],
-            "volume_change_rel": (v1 - v0) / v0,
-            "plain_fp64_ms_per_step_measured_separately": 37000.0}
+    out = {"workload": "Rayleigh-Taylor 4096x4096 on [0,1]x[0,4], rho 3/1, ELVIRA + Weymouth-Yue, "
+                       "BiCGSTAB+Jacobi predictor, mixed multigrid Poisson to rel-res 1e-10, dt 2e-5",
+           "autotune": None if tuned is None else {"launch": tuned["launch"], "params": tuned["params"],
+                                                   "tuned_ms": tuned["ms"], "rule_ms": tuned["rule_ms"],
+                                                   "system": "initial density, seeded zero-mean RHS"}}
+    for name, prec, k in (("mixed", cap.PREC_MIXED, nsteps), ("fp64_mg", cap.PREC_FP64_MG, 2)):
+        q = p.copy()
+        q.p_precision = prec
+        g = f.copy()
+        with pkg.Solver(q) as s:
+            if tuned is not None:
+                launch = cap.Launch(**tuned["launch"])
+                assert s.lib.covof_set_launch(s.h, ctypes.byref(launch)) == cap.OK
+            s.state_set(g)
+            st, _ = s.run_steps(dt, 1, graph=False)
+            st, r = s.run_steps(dt, k, graph=False)
+            s.state_get(g)
+        assert st == cap.OK, (name, st)
+        rec = {"steps": k, "ms_per_step": r["ms"] / r["steps"], "steps_per_s": 1000.0 * r["steps"] / r["ms"],
+               "poisson_vcycles_per_step": r["poisson_iters"] / r["steps"],
+               "predictor_iters_per_step": r["mom_iters"] / r["steps"], "max_relres": r["max_relres"]}
+        if name == "mixed":
+            rec["volume_change_rel"] = (float(g.C[1:-1, 1:-1].sum()) - v0) / v0
+        out[name] = rec
+    out["speedup_mixed_vs_fp64_mg"] = out["fp64_mg"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    return out
 
 
 def mono_steps(pkg, orc, n, nsteps, cpu_steps):
@@ -430,42 +489,77 @@ def vof_steps(pkg, orc, reps):
 
 
 def run_reference(args, world, rank):
-    """--impl reference: the reference path's CPU implementation (the FP64
-    C++ restatement; the Fortran reference cannot be built on these
-    machines), all host threads, bounded sample per step."""
+    """--impl reference: the reference path's CPU solver (the FP64 C++
+    restatement of its Jacobi-PCG; the Fortran reference cannot be built on
+    these machines) on every host core, one whole solve to 1e-10 per step."""
     if rank != 0:
         return
     import __graft_entry__ as ge
     pkg = ge.load_package()
     orc = ge._load_oracle()
-    p, b, ru, rv, dt = pkg.cases.poisson_inclusions(n=1024, n_incl=200)
+    n = args.size
+    p, b, ru, rv, dt = pkg.cases.poisson_inclusions(n=n, n_incl=200 if n >= 512 else 20)
     nth = os.cpu_count() or 1
-    # Iteration count of one full FP64 Jacobi-PCG solve of this system (the
-    # GPU FP64 path runs the same algorithm; measured count, see DESIGN.md).
-    iters_full = int(os.environ.get("COVOF_BENCH_FP64_ITERS", "0")) or 12402
-    x = np.zeros_like(b)
     for _ in range(args.warmup):
-        orc.poisson_fixed_iters(p, dt, b, ru, rv, x, 5, nth)
-    per = []
-    n_it = 50
+        cpu_solve(orc, p, b, ru, rv, dt, nth)
+    secs, its = [], []
     for _ in range(args.steps):
-        x[...] = 0.0
-        t0 = time.perf_counter()
-        orc.poisson_fixed_iters(p, dt, b, ru, rv, x, n_it, nth)
-        per.append((time.perf_counter() - t0) / n_it)
-    per_it = statistics.median(per)
-    val = 1.0 / (per_it * iters_full)
+        el, it, rr, _ = cpu_solve(orc, p, b, ru, rv, dt, nth)
+        secs.append(el)
+        its.append(it)
+    ms = 1e3 * statistics.mean(secs)
+    val = 1000.0 / ms
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_it * iters_full * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "n": 1024, "inclusions": 200},
+        "data": "synthetic", "config": bench_config(n, world),
+        "iters_per_solve": int(statistics.median(its)),
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": nth, "kind": "port",
-                         "sample": f"each step: {n_it} Jacobi-PCG iterations (OpenMP, {nth} threads) of the FP64 "
-                                   f"C++ restatement on the full system, scaled to {iters_full} iterations per solve"},
+                         "sample": f"each step one whole Jacobi-PCG solve of the same system to rel-res 1e-10 "
+                                   f"({int(statistics.median(its))} iterations) by the FP64 C++ restatement of "
+                                   f"the reference's solver, OpenMP on {nth} threads"},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def time_solves(pkg, s, q, dt, tb, tru, trv, tp, flush, steps, warmup, world, clocks=None):
+    """warmup + steps solves from a zero guess on the handle's stream, the L2
+    flushed before each; CUDA events around each solve."""
+    import torch
+    cap = pkg.capi
+    stream = torch.cuda.ExternalStream(s.stream_ptr, device=tb.device)
+    for _ in range(warmup):
+        tp.zero_()
+        it, rr, st = s.poisson_solve_rhs_dev(dt, tb, tru, trv, tp)
+        assert st == cap.OK, (cap.STATUS_NAMES.get(st), it, rr, s.last_refine_steps())
+    barrier(world)
+    if clocks:
+        clocks.start()
+    step_ms, kern_ms, iters, outer = [], [], [], []
+    t_wall0 = time.perf_counter()
+    for _ in range(steps):
+        flush.fill_(1.0)          # cold L2 (512 MiB > 129 MB)
+        tp.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        it, rr, st = s.poisson_solve_rhs_dev(dt, tb, tru, trv, tp)
+        e1.record(stream)
+        e1.synchronize()
+        assert st == cap.OK and rr <= q.p_tol, (st, rr)
+        step_ms.append(e0.elapsed_time(e1))
+        kern_ms.append(s.last_solve_ms())
+        iters.append(it)
+        outer.append(s.last_refine_steps())
+    barrier(world)
+    wall = time.perf_counter() - t_wall0
+    clk = clocks.stop() if clocks else None
+    return {"ms_per_step": statistics.mean(step_ms), "kernel_ms": statistics.mean(kern_ms),
+            "iters": int(statistics.median(iters)), "outer": int(statistics.median(outer)),
+            "wall_s": wall, "clocks": clk, "x": tp.cpu().numpy().copy()}
 
 
 def run_ours(args, world, rank, local):
@@ -488,8 +582,8 @@ def run_ours(args, world, rank, local):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     # autotune the mixed solve on this system (launch shape, multigrid
-    # smoothing and coarse weight; the stopping test stays the true FP64
-    # residual at 1e-10)
+    # smoothing, coarse weight and coarsest-level handling; the stopping test
+    # stays the true FP64 residual at 1e-10)
     tuned = None
     if not args.no_tune:
         import importlib
@@ -499,57 +593,40 @@ def run_ours(args, world, rank, local):
         q0.p_inner_kind = cap.INNER_MG
         tuned = at.tune(q0, dt, tb, tru, trv, repeats=1, cache_path=None, budget_s=args.tune_budget)
 
+    # the arms: (name, arithmetic, inner kind, tuned multigrid settings and launch)
+    arms = (("fp64_jacobi", cap.PREC_FP64, cap.INNER_MG, False),
+            ("fp64_mg", cap.PREC_FP64_MG, cap.INNER_MG, True),
+            ("mixed_mg", cap.PREC_MIXED, cap.INNER_MG, True),
+            ("mixed_jacobi_cg", cap.PREC_MIXED, cap.INNER_CG, False),
+            ("mixed_chebyshev", cap.PREC_MIXED, cap.INNER_CHEBYSHEV, False))
     results = {}
-    arms = (("fp64", cap.PREC_FP64, cap.INNER_MG), ("mixed", cap.PREC_MIXED, cap.INNER_MG),
-            ("mixed_chebyshev", cap.PREC_MIXED, cap.INNER_CHEBYSHEV))
-    for name, prec, kind in arms:
+    solvers = {}
+    for name, prec, kind, use_tuned in arms:
         q = p.copy()
         q.p_precision = prec
         q.p_inner_kind = kind
-        if name == "mixed" and tuned is not None:
+        q.p_max_iter = 10_000_000
+        if use_tuned and tuned is not None:
+            # the FP64 multigrid twin runs the mixed arm's tuned settings, so
+            # the two differ in the V-cycle's arithmetic only
             for k, v in tuned["params"].items():
                 setattr(q, k, v)
         s = pkg.Solver(q)
-        if name == "mixed" and tuned is not None:
+        if use_tuned and tuned is not None:
             import ctypes
             launch = cap.Launch(**tuned["launch"])
             assert s.lib.covof_set_launch(s.h, ctypes.byref(launch)) == cap.OK
-        stream = torch.cuda.ExternalStream(s.stream_ptr, device=dev)
-        for _ in range(args.warmup):
-            tp.zero_()
-            it, rr, st = s.poisson_solve_rhs_dev(dt, tb, tru, trv, tp)
-            assert st == cap.OK, (name, cap.STATUS_NAMES.get(st), it, rr, s.last_refine_steps())
-        barrier(world)
-        clocks = ClockSampler(local) if (name == "mixed" and rank == 0) else None
-        if clocks:
-            clocks.start()
-        step_ms, kern_ms, iters, outer = [], [], [], []
-        t_wall0 = time.perf_counter()
-        for _ in range(args.steps):
-            flush.fill_(1.0)          # cold L2 (512 MiB > 129 MB)
-            tp.zero_()
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            it, rr, st = s.poisson_solve_rhs_dev(dt, tb, tru, trv, tp)
-            e1.record(stream)
-            e1.synchronize()
-            assert st == cap.OK and rr <= q.p_tol, (name, st, rr)
-            step_ms.append(e0.elapsed_time(e1))
-            kern_ms.append(s.last_solve_ms())
-            iters.append(it)
-            outer.append(s.last_refine_steps())
-        barrier(world)
-        wall = time.perf_counter() - t_wall0
-        clk = clocks.stop() if clocks else None
-        results[name] = {"ms_per_step": statistics.mean(step_ms), "kernel_ms": statistics.mean(kern_ms),
-                         "iters": int(statistics.median(iters)), "outer": int(statistics.median(outer)),
-                         "wall_s": wall, "clocks": clk, "solver": s, "nu": q.p_mg_nu, "cw": q.p_mg_cw}
+        clocks = ClockSampler(local) if (name == "mixed_mg" and rank == 0) else None
+        r = time_solves(pkg, s, q, dt, tb, tru, trv, tp, flush, args.steps, args.warmup, world, clocks)
+        r.update(nu=q.p_mg_nu, cw=q.p_mg_cw, nuc=q.p_mg_nuc)
+        results[name] = r
+        solvers[name] = s
+    for k in results:
+        results[k]["ms_max"] = max_over_ranks(results[k]["ms_per_step"], world)
 
     # e2e through the host C ABI: pinned host arrays, copies inside the region
-    mixed = results["mixed"]
-    s = mixed["solver"]
+    mixed = results["mixed_mg"]
+    s = solvers["mixed_mg"]
 
     def pinned(a):
         t = torch.from_numpy(a).pin_memory()
@@ -573,25 +650,25 @@ def run_ours(args, world, rank, local):
         assert st == cap.OK
     e2e_step = max_over_ranks(statistics.mean(e2e_ms), world)
     gbytes = 4 * b.nbytes
+    for sv in solvers.values():
+        sv.close()
 
-    ms_mixed = max_over_ranks(mixed["ms_per_step"], world)
-    ms_fp64 = max_over_ranks(results["fp64"]["ms_per_step"], world)
+    ms_mixed = mixed["ms_max"]
     value = world * 1000.0 / ms_mixed
 
     # roofline of the dominant kernel (the persistent mixed-path kernel:
     # one V-cycle and one FP64 flexible-CG iteration per outer step)
     cells = n * n
-    it_m, out_m = mixed["iters"], max(mixed["outer"], 1)
+    out_m = max(mixed["outer"], 1)
     w_outer = w_vcycle_fp32(mixed["nu"]) + W_OUTER_FP64
     alg_bytes = out_m * cells * w_outer
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / (mixed["kernel_ms"] * 1e-3) / 1e9
-    it_f = results["fp64"]["iters"]
-    achieved64 = it_f * cells * W_ITER_FP64 / (results["fp64"]["kernel_ms"] * 1e-3) / 1e9
-    cheb = results["mixed_chebyshev"]
+    fj = results["fp64_jacobi"]
+    achieved64 = fj["iters"] * cells * W_ITER_FP64 / (fj["kernel_ms"] * 1e-3) / 1e9
     # measured DRAM bytes of one launch: the ncu capture's bytes per outer
-    # iteration (rule settings) x this launch's outer iterations, scaled by
-    # the model's bytes-per-iteration ratio when the tuned sweep count differs
+    # iteration x this launch's outer iterations, scaled by the model's
+    # bytes-per-iteration ratio when the tuned sweep count differs
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():
@@ -606,39 +683,64 @@ def run_ours(args, world, rank, local):
     line = None
     if rank == 0:
         orc = ge._load_oracle()
-        cpu = None if args.skip_cpu else cpu_sample(pkg, orc, p, b, ru, rv, dt, it_f, 1, args.cpu_budget)
+        nth = os.cpu_count() or 1
+        # the oracle's converged solution (the error of every arm is stated
+        # against it) and the CPU baseline: whole solves on every host core
+        t_ref, it_ref, rr_ref, x_ref = cpu_solve(orc, p, b, ru, rv, dt, nth, tol=1e-13)
+        cpu = None
+        if not args.skip_cpu:
+            el, it_c, rr_c, x_c = cpu_solve(orc, p, b, ru, rv, dt, nth)
+            cpu = {"value": 1.0 / el, "unit": UNIT, "cores": nth, "kind": "port",
+                   "sample": f"one whole Jacobi-PCG solve of the same system to rel-res 1e-10 ({it_c} iterations, "
+                             f"{el:.1f} s) by the FP64 C++ restatement of the reference's solver, OpenMP on "
+                             f"{nth} threads; its error against the converged oracle {rel_err(x_c, x_ref):.2e}"}
+        arms_out = {}
+        for name, r in results.items():
+            arms_out[name] = {"ms_per_step": r["ms_max"], "solves_per_s": world * 1000.0 / r["ms_max"],
+                              "kernel_ms": r["kernel_ms"], "iters": r["iters"], "outer_iters": r["outer"],
+                              "err_vs_oracle": rel_err(r["x"], x_ref)}
+            if name in ("fp64_mg", "mixed_mg"):
+                arms_out[name].update(mg_nu=r["nu"], mg_cw=r["cw"], mg_nuc=r["nuc"])
+        arms_out["fp64_jacobi"]["achieved_gbs"] = achieved64
+        arms_out["fp64_jacobi"]["algorithm"] = "FP64 Jacobi-PCG (the reference's algorithm), iters = PCG iterations"
+        arms_out["fp64_mg"]["algorithm"] = ("FP64 flexible CG + FP64 multigrid V-cycle (the mixed kernel in FP64), "
+                                            "iters = V-cycles")
+        arms_out["mixed_mg"]["algorithm"] = "FP64 flexible CG + FP32 multigrid V-cycle, iters = V-cycles"
+        arms_out["mixed_jacobi_cg"]["algorithm"] = ("FP64 flexible CG + FP32 Jacobi-CG inner solve (<= 32 "
+                                                    "steps), iters = FP32 inner steps")
+        arms_out["mixed_chebyshev"]["algorithm"] = ("FP64 flexible CG + FP32 Chebyshev inner iteration, "
+                                                    "iters = FP32 inner steps")
+        arms_out["oracle"] = {"iters": it_ref, "relres": rr_ref, "seconds": t_ref, "threads": nth,
+                              "what": "FP64 Jacobi-PCG of the C++ restatement converged to rel-res 1e-13"}
         steps = None if args.skip_steps else sp_steps(pkg, orc, 100, 0 if args.skip_cpu else 3)
-        batch = None if args.skip_steps else batch_steps(pkg, orc, 256, 5)
+        batch = None if args.skip_steps else batch_steps(pkg, orc, 256, args.batch_steps)
         adjoint = None if args.skip_steps else adjoint_steps(pkg, 512, 3)
-        rt = None if (args.skip_steps or args.skip_rt) else rt_steps(pkg, orc, 3)
+        rt = None if (args.skip_steps or args.skip_rt) else rt_steps(pkg, orc, args.rt_steps, args)
         mono = None if args.skip_steps else mono_steps(pkg, orc, 256, 5, 0 if args.skip_cpu else 2)
         vof = None if args.skip_steps else vof_steps(pkg, orc, 5)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n": n, "inclusions": 200 if n >= 512 else 20, "tol": 1e-10,
-                       "gauge": "pinned cell (1,1)", "l2": "flushed between steps (512 MiB write)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
-            "plain_fp64": {"ms_per_step": ms_fp64, "solves_per_s": world * 1000.0 / ms_fp64,
-                           "iters": it_f, "kernel_ms": results["fp64"]["kernel_ms"],
-                           "achieved_gbs": achieved64},
-            "mixed": {"inner": "multigrid V-cycle", "vcycles": it_m, "outer_fcg_iters": mixed["outer"],
-                      "kernel_ms": mixed["kernel_ms"], "mg_nu": mixed["nu"], "mg_cw": mixed["cw"]},
-            "mixed_chebyshev": {"ms_per_step": cheb["ms_per_step"], "solves_per_s": world * 1000.0 / cheb["ms_per_step"],
-                                "inner_steps_fp32": cheb["iters"], "outer_fcg_iters": cheb["outer"],
-                                "kernel_ms": cheb["kernel_ms"]},
+            "config": bench_config(n, world),
+            "err_vs_oracle": arms_out["mixed_mg"]["err_vs_oracle"],
+            "arms": arms_out,
+            "speedup": {
+                "mixed_mg_vs_fp64_mg": results["fp64_mg"]["ms_max"] / ms_mixed,
+                "mixed_mg_vs_fp64_jacobi": results["fp64_jacobi"]["ms_max"] / ms_mixed,
+                "mixed_jacobi_cg_vs_fp64_jacobi": results["fp64_jacobi"]["ms_max"] / results["mixed_jacobi_cg"]["ms_max"],
+                "note": "mixed_mg / fp64_mg isolates the FP32 inner arithmetic (same kernel, settings and "
+                        "launch); mixed_mg / fp64_jacobi also changes the algorithm"},
             "autotune": None if tuned is None else {
                 "launch": tuned["launch"], "params": tuned["params"], "candidates": tuned["candidates"],
                 "tuned_ms": tuned["ms"], "rule_ms": tuned["rule_ms"]},
-            "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "k_pcg_mixed_mg", "peak_source": peak_kind,
                          "bytes_per_cell_per_outer": w_outer,
                          "note": "achieved = algorithmic bytes (one FP32 V-cycle, (12 nu + 4.5) words/cell on "
                                  "each level, x 4/3 over the levels, + 21 FP64 words/cell per outer FCG "
-                                 "iteration) / CUDA-event kernel time, an effective rate; traffic = DRAM bytes per "
+                                 "iteration) / CUDA-event kernel time, of measured peak; traffic = DRAM bytes per "
                                  "launch from the ncu capture (bytes per outer iteration x this launch's "
                                  "outer iterations): much of the level data stays in L2, and the kernel is "
                                  "bound by grid-barrier latency and FP64 issue, not HBM"},
@@ -659,8 +761,6 @@ def run_ours(args, world, rank, local):
             "monolithic": mono,
             "vof": vof,
         }
-    for r in results.values():
-        r["solver"].close()
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -672,7 +772,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=1024)
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--batch-steps", type=int, default=50, help="time steps of the 256-case batch leg")
+    ap.add_argument("--rt-steps", type=int, default=10, help="time steps of the 4096^2 Rayleigh-Taylor sample")
     ap.add_argument("--skip-cpu", action="store_true", help="profiling runs: no CPU baseline")
     ap.add_argument("--skip-e2e", action="store_true", help="profiling runs: no host-API leg")
     ap.add_argument("--skip-steps", action="store_true", help="profiling runs: no rising-bubble time steps")

@@ -68,7 +68,7 @@ def candidates(p: Params, sm_count: int) -> list[tuple[dict, dict]]:
     # strips on every SM, then higher degrees and narrower intervals, which
     # trade FP64 outer iterations for cheap FP32 inner steps
     blocks = sorted({min(sm_count, p.ny), max(1, min(sm_count, p.ny) // 2)}, reverse=True)
-    if p.p_inner_kind == capi.INNER_MG:
+    if p.p_inner_kind == capi.INNER_MG or p.p_precision == capi.PREC_FP64_MG:
         # the over-correction weight matters most (aggregation coarse
         # operators are about twice too stiff), then the smoothing sweeps
         # (a coarse solve that leaves less error behind also counts: the
@@ -173,7 +173,7 @@ def tuned_fields(p: Params) -> tuple[str, ...]:
     """The parameters the tuner varies for p's arithmetic and inner kind."""
     if p.p_precision == capi.PREC_FP64:
         return ()
-    if p.p_inner_kind == capi.INNER_MG:
+    if p.p_inner_kind == capi.INNER_MG or p.p_precision == capi.PREC_FP64_MG:
         return ("p_mg_nu", "p_mg_cw", "p_mg_nuc")
     return ("p_inner_max_iter", "p_cheb_lo")
 

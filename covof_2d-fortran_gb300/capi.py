@@ -28,7 +28,7 @@ ADVECT_WEYMOUTH_YUE, ADVECT_CIAM, ADVECT_TVD = 0, 1, 2
 SOLVER_AUGMENTED_LAGRANGIAN, SOLVER_MONOLITHIC, SOLVER_STANDARD_PROJECTION, SOLVER_AAL, SOLVER_CAAL = 1, 2, 3, 4, 5
 LIMITER_SUPERBEE, LIMITER_VAN_LEER, LIMITER_MUSCL, LIMITER_HRIC = 0, 1, 2, 3
 GAUGE_REFERENCE, GAUGE_PINNED = 0, 1
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_FP64_MG = 0, 1, 2
 INNER_CHEBYSHEV, INNER_CG, INNER_CHEBYSHEV_STREAM, INNER_MG = 0, 1, 2, 3
 # resident fields (COVOF_FIELD_*), in header order; names follow the Fields dataclass
 FIELD_NAMES = ("u", "v", "p", "C", "rho", "rho_u", "rho_v", "mu", "mu_node", "fx_sigma",

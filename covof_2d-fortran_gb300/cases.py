@@ -233,7 +233,7 @@ def random_velocity(p: Params, scale: float, seed: int):
 
 
 def droplet_batch(n_cases: int = 256, seed: int = SEED + 4, sizes=(64, 128, 256, 512), nsub: int = 4,
-                  mixed: bool = True):
+                  mixed: bool = True, shapes=None):
     """Independent droplet / bubble cases: nx, ny drawn from sizes, square
     cells, short side of the domain 1 (dx = dy = 1/min(nx, ny)); 1-3 circles
     with radii 0.1-0.3 of the short side (fluid 1 inside for a droplet,
@@ -242,11 +242,16 @@ def droplet_batch(n_cases: int = 256, seed: int = SEED + 4, sizes=(64, 128, 256,
     log-uniform in [1, 100] (mu1 = 1e-2), sigma uniform in [0.01, 25],
     g = (0, -0.98); ELVIRA + Weymouth-Yue, BiCGSTAB + Jacobi predictor and the
     Poisson to 1e-10.  dt = min(1e-4, half the capillary limit
-    sqrt((rho1 + rho2) h^3 / (4 pi sigma))).  Returns [(params, C, dt)]."""
+    sqrt((rho1 + rho2) h^3 / (4 pi sigma))).  shapes: a list of (nx, ny) in
+    place of the drawn sizes (one case each; the rest is drawn as usual).
+    Returns [(params, C, dt)]."""
     rng = np.random.default_rng(seed)
     out = []
-    for _ in range(n_cases):
-        nx, ny = (int(v) for v in rng.choice(sizes, 2))
+    for c in range(n_cases if shapes is None else len(shapes)):
+        if shapes is None:
+            nx, ny = (int(v) for v in rng.choice(sizes, 2))
+        else:
+            nx, ny = (int(v) for v in shapes[c])
         m = min(nx, ny)
         lx, ly = nx / m, ny / m
         p = make_params(nx, ny, lx, ly)
@@ -260,7 +265,7 @@ def droplet_batch(n_cases: int = 256, seed: int = SEED + 4, sizes=(64, 128, 256,
             circles.append((cx, cy, r))
         droplet = bool(rng.integers(0, 2))
 
-        def inside(X, Y):
+        def inside(X, Y, circles=circles, droplet=droplet):
             m = np.zeros(np.broadcast(X, Y).shape, dtype=bool)
             for cx, cy, r in circles:
                 m |= np.hypot(X - cx, Y - cy) < r

@@ -10,7 +10,8 @@
 //   3. per case: unpack + velocity BC; Poisson assembly;
 //   4. ONE persistent cooperative launch: the Poisson solves of all cases
 //      (k_pcg_mixed_mg_batch / k_pcg_mixed_smem_batch / k_pcg_mixed_batch,
-//      or k_pcg_fp64_batch for FP64 batches);
+//      k_pcg_fp64_mg_batch for the FP64 multigrid form, or k_pcg_fp64_batch
+//      for plain FP64 batches);
 //   5. per case: copy-back, velocity correction, velocity BC, status log.
 // The grid of a batched solve is cut into teams (contiguous block ranges,
 // common.cuh: BatchTeams); a team solves its cases one after another with
@@ -381,11 +382,11 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
   auto fail = [&](int code) { covof_batch_destroy(b); return code; };
   b->ncases = ncases;
   b->mixed = cases[0].p_precision == COVOF_PREC_MIXED;
-  const bool mg = b->mixed && cases[0].p_inner_kind == COVOF_INNER_MG;
+  const bool mg = mg_path(cases[0]);
   for (int c = 0; c < ncases; ++c) {
     // one arithmetic per batch; a mixed batch runs either the multigrid inner
     // iteration for every case or Chebyshev for every case
-    if ((cases[c].p_precision == COVOF_PREC_MIXED) != b->mixed) return fail(COVOF_INVALID);
+    if (cases[c].p_precision != cases[0].p_precision) return fail(COVOF_INVALID);
     if (b->mixed && (cases[c].p_inner_kind == COVOF_INNER_MG) != mg) return fail(COVOF_UNSUPPORTED);
     if (b->mixed && cases[c].p_inner_kind == COVOF_INNER_CG) return fail(COVOF_UNSUPPORTED);
     if (cases[c].p_precond == COVOF_PRECOND_SSOR) return fail(COVOF_UNSUPPORTED);
@@ -428,7 +429,9 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
   bool smem_form = false;
   bool want_stream = false;
   for (int c = 0; c < ncases; ++c) want_stream |= cases[c].p_inner_kind == COVOF_INNER_CHEBYSHEV_STREAM;
-  if (mg) b->pfn = (const void*)k_pcg_mixed_mg_batch;
+  if (mg)
+    b->pfn = cases[0].p_precision == COVOF_PREC_FP64_MG ? (const void*)k_pcg_fp64_mg_batch
+                                                        : (const void*)k_pcg_mixed_mg_batch;
   if (b->mixed && !want_stream && !mg) {
     int optin = 0;
     cudaFuncAttributes fa;

@@ -44,8 +44,16 @@ int check_params(const covof_params* p) {
     if (t != COVOF_BC_DIRICHLET && t != COVOF_BC_FREESLIP) return COVOF_INVALID;
   }
   if (p->advection_method < COVOF_ADVECT_WEYMOUTH_YUE || p->advection_method > COVOF_ADVECT_TVD) return COVOF_INVALID;
+  if (p->p_precision < COVOF_PREC_FP64 || p->p_precision > COVOF_PREC_FP64_MG) return COVOF_INVALID;
   if (p->tvd_limiter < COVOF_LIMITER_SUPERBEE || p->tvd_limiter > COVOF_LIMITER_HRIC) return COVOF_INVALID;
   return COVOF_OK;
+}
+
+// The flexible CG with the multigrid V-cycle: MIXED with COVOF_INNER_MG (FP32
+// V-cycle) or FP64_MG (FP64 V-cycle).
+bool mg_path(const covof_params& p) {
+  return (p.p_precision == COVOF_PREC_MIXED && p.p_inner_kind == COVOF_INNER_MG) ||
+         p.p_precision == COVOF_PREC_FP64_MG;
 }
 
 int4 wall_flags(const covof_params& p) {
@@ -82,7 +90,9 @@ int ensure_poisson(covof_handle* h) {
   CS(dalloc(&h->Ad32, g)); CS(dalloc(&h->ax32, g)); CS(dalloc(&h->ay32, g)); CS(dalloc(&h->aP32, g));
   CS(dalloc(&h->pin_part, (size_t)4 * kPinBlocks + 4)); CS(dalloc(&h->pin_ctl, 4));
   CS(dalloc(&h->pin_b, g));
-  // multigrid levels: halve each dimension down to about 64 cells
+  // multigrid levels: halve each dimension down to about 64 cells; es =
+  // bytes per element of the V-cycle's arithmetic
+  const long long es = h->prm.p_precision == COVOF_PREC_FP64_MG ? 8 : 4;
   MgHier& H = h->mg;
   H.nl = 1;
   H.lv[0].nx = h->D.nx; H.lv[0].ny = h->D.ny; H.lv[0].off = 0;
@@ -97,14 +107,14 @@ int ensure_poisson(covof_handle* h) {
     H.nl += 1;
   }
   // the tail: from the first level of at most p_mg_tail cells whose levels
-  // down to the coarsest (seven FP32 fields each) fit in kMgTailSmem bytes of
+  // down to the coarsest (seven fields each) fit in kMgTailSmem bytes of
   // shared memory
   const long long tail_cells = h->prm.p_mg_tail > 0 ? h->prm.p_mg_tail : 2048;
   H.tail = H.nl;
   H.tail_smem = 0;
   for (int l = 1; l < H.nl; ++l) {
     long long bytes = 0;
-    for (int q = l; q < H.nl; ++q) bytes += 28LL * (H.lv[q].nx + 2) * (H.lv[q].ny + 2);
+    for (int q = l; q < H.nl; ++q) bytes += 7LL * es * (H.lv[q].nx + 2) * (H.lv[q].ny + 2);
     if ((long long)H.lv[l].nx * H.lv[l].ny <= tail_cells && bytes <= kMgTailSmem) {
       H.tail = l;
       H.tail_smem = (int)bytes;
@@ -122,13 +132,17 @@ int ensure_poisson(covof_handle* h) {
   H.exact = 0;
   H.inv_off = 0;
   const long long ncoarse = (long long)H.lv[H.nl - 1].nx * H.lv[H.nl - 1].ny;
-  if (h->prm.p_mg_nuc < 0 && H.tail < H.nl && ncoarse <= 64 && H.tail_smem + 64 * 64 * 4 <= kMgTailSmem) {
+  if (h->prm.p_mg_nuc < 0 && H.tail < H.nl && ncoarse <= 64 && H.tail_smem + 64 * 64 * es <= kMgTailSmem) {
     H.exact = 1;
-    H.inv_off = H.tail_smem / 4;
-    H.tail_smem += 64 * 64 * 4;
+    H.inv_off = (int)(H.tail_smem / es);
+    H.tail_smem += (int)(64 * 64 * es);
     H.nuc = 0;
   }
-  if (pool > 0) CS(dalloc(&H.pool, (size_t)pool));
+  if (pool > 0) {
+    unsigned char* raw = nullptr;
+    CS(dalloc(&raw, (size_t)(pool * es)));
+    H.pool = raw;
+  }
   h->have_poisson = true;
   return COVOF_OK;
 }
@@ -293,9 +307,9 @@ int poisson_plan(covof_handle* h) {
   long long units = (long long)make_tiles(h->D, threads).ntiles;
   size_t smem = 0;
   h->p_cluster = false;
-  if (mixed && P.p_inner_kind == COVOF_INNER_MG) {
+  if (mg_path(P)) {
     // multigrid inner: one persistent block per SM, tile-owned outer
-    const void* mfn = (const void*)k_pcg_mixed_mg;
+    const void* mfn = P.p_precision == COVOF_PREC_FP64_MG ? (const void*)k_pcg_fp64_mg : (const void*)k_pcg_mixed_mg;
     long long units = h->sm_count;
     if (L.p_blocks > 0 && L.p_blocks < units) units = L.p_blocks;
     const size_t tail = (size_t)h->mg.tail_smem;
@@ -396,15 +410,16 @@ int pois_pre(covof_handle* h, double dt, const double* u, const double* v, const
   const covof_params& P = h->prm;
   if (!rho_u || !rho_v || !p || (!b && (!u || !v))) return COVOF_INVALID;
   const bool mixed = P.p_precision == COVOF_PREC_MIXED;
-  // the symmetric Gauss-Seidel preconditioner belongs to the FP64 PCG
-  if (P.p_precond == COVOF_PRECOND_SSOR && mixed) return COVOF_UNSUPPORTED;
+  // the symmetric Gauss-Seidel preconditioner belongs to the plain FP64 PCG
+  if (P.p_precond == COVOF_PRECOND_SSOR && P.p_precision != COVOF_PREC_FP64) return COVOF_UNSUPPORTED;
   CS(ensure_poisson(h));
   CS(poisson_plan(h));
   const int pinned = P.p_gauge == COVOF_GAUGE_PINNED;
   const dim3 blk(32, 8), grd = grid2(P.nx, P.ny, blk);
   k_poisson_assemble<<<grd, blk, 0, h->stream>>>(h->D, dt, P.dx, P.dy, wall_flags(P), rho_u, rho_v, u, v,
                                                   b, pinned, h->pax, h->pay, h->paP, h->pb,
-                                                  mixed ? h->pisd : nullptr, mixed ? nullptr : h->pinvD);
+                                                  mixed ? h->pisd : nullptr,
+                                                  P.p_precision == COVOF_PREC_FP64 ? h->pinvD : nullptr);
   if (mixed)
     k_poisson_scale32<<<grid2(P.nx + 1, P.ny + 1, blk), blk, 0, h->stream>>>(
         h->D, h->pax, h->pay, h->pisd, h->ax32, h->ay32, h->aP32, h->paP, P.p_inner_kind == COVOF_INNER_MG ? 1 : 0);
@@ -443,8 +458,8 @@ int poisson_enqueue(covof_handle* h, double dt, const double* u, const double* v
   PoissonArgs a;
   CS(pois_pre(h, dt, u, v, b, rho_u, rho_v, p, &a));
   const covof_params& P = h->prm;
-  if (P.p_precision == COVOF_PREC_MIXED && P.p_inner_kind == COVOF_INNER_MG && a.pinned &&
-      h->p_fn == (const void*)k_pcg_mixed_mg) {
+  if (mg_path(P) && a.pinned &&
+      (h->p_fn == (const void*)k_pcg_mixed_mg || h->p_fn == (const void*)k_pcg_fp64_mg)) {
     // The pinned system solved through the reference gauge, whose
     // deflation handles the constant mode exactly (35 against 41 outer
     // iterations at 1024^2); the pinned residual is checked after the shift
@@ -1142,7 +1157,7 @@ int capture_steps(covof_handle* h, double dt) {
 int run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run_stats* out) {
   if (nsteps < 0 || !(dt > 0.0)) return COVOF_INVALID;
   const covof_params& P = h->prm;
-  if (P.p_precond == COVOF_PRECOND_SSOR && P.p_precision == COVOF_PREC_MIXED) return COVOF_UNSUPPORTED;
+  if (P.p_precond == COVOF_PRECOND_SSOR && P.p_precision != COVOF_PREC_FP64) return COVOF_UNSUPPORTED;
   CS(check_mom_params(P));
   CS(check_coupling(P));
   // the Uzawa exit test reads a scalar back per iteration: eager steps

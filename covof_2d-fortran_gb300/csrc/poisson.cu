@@ -476,6 +476,7 @@ struct StripOwn {
 // FP32 vectors.
 struct TiledInner {
   static constexpr bool kScaled = true;
+  using Scalar = float;
   Dims D; Tiles tl; Team tm; Sys<float> S; float* sd; int pinned;
   float* rhs;
   __device__ __forceinline__ void set_rhs(int k, int, float v) { S.x[k] = 0.0f; rhs[k] = v; }
@@ -493,6 +494,7 @@ struct TiledInner {
 // by iteration parity), plus the reduction partials.
 struct SmemInner {
   static constexpr bool kScaled = true;
+  using Scalar = float;
   Dims D; int r0, R, W, b, G, pinned_c;
   float *ys, *r, *Ad, *d, *ax, *ay, *hr, *hd;
   float* xb;  // [2][G][2 sides][2 (r,d)][W]
@@ -632,6 +634,7 @@ constexpr int kChebTab = 128;  // precomputed Chebyshev step coefficients
 
 struct SmemCheby {
   static constexpr bool kScaled = true;
+  using Scalar = float;
   Dims D; int r0, R, W, b, G, pinned_c, m;
   double lo;
   float2* tab;            // [kChebTab] (c1, c2) of step k, in shared memory
@@ -774,6 +777,7 @@ struct SmemCheby {
 // FCG outer loop (see k_pcg_mixed).
 template <class Own, class Inner>
 __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, GridReducer& R) {
+  using IS = typename Inner::Scalar;  // arithmetic of the inner iteration
   const Dims D = a.D;
   const int pk = a.pinned ? D.P + 1 : -1;
   const bool pinned = a.pinned != 0;
@@ -851,7 +855,7 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     if (outer >= a.max_refine || total_inner >= a.max_iter) { status = COVOF_MAXITER; break; }
     // cdef: aP_sum is the sum of the deflation weights
     own.each([&](int k, int c) {
-      inner.set_rhs(k, c, (k == pk) ? 0.0f : (float)((r[k] - cdef * wgt(k)) * scl(k) * inv_r));
+      inner.set_rhs(k, c, (k == pk) ? IS(0) : (IS)((r[k] - cdef * wgt(k)) * scl(k) * inv_r));
     });
     __syncthreads();
     int budget = a.max_iter - total_inner;
@@ -865,7 +869,7 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       if (budget >= 1 && inner.fused_ok()) {
         const bool use_q = !fresh;
         const double rn = r_norm;
-        o = inner.solve_fused(R, budget, [&](int k, float yk) {
+        o = inner.solve_fused(R, budget, [&](int k, IS yk) {
           const double zk = rn * (double)yk;
           z[k] = zk;
           zs[0] = fma(1.0, zk, zs[0]);
@@ -1015,6 +1019,7 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
 // finished reading it.  Rows of other blocks are read through L2 (__ldcg).
 struct StreamCheby {
   static constexpr bool kScaled = true;
+  using Scalar = float;
   Dims D; int r0, R, b, G, pk, m;
   double lo;
   float2* tab;              // [kChebTab] (c1, c2) of step k, in shared memory
@@ -1184,6 +1189,7 @@ __device__ __forceinline__ unsigned ld_cluster_acquire_u32(unsigned addr) {
 // [(Rmax+2)*W] (halo rows 0 and R+1); ax [Rmax*W]; ay [(Rmax+1)*W].
 struct ClusterCheby {
   static constexpr bool kScaled = true;
+  using Scalar = float;
   Dims D; int r0, R, Rs, W, b, G, pinned_c, m;  // Rs: rows of the south neighbour
   double lo;
   float2* tab;
@@ -1356,29 +1362,32 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cluster(PoissonArgs a) {
 // chosen on the host by cell count and shared-memory size) run in block 0
 // alone out of its shared memory, with __syncthreads instead of grid
 // barriers; their coefficients are loaded once per solve.
-struct MgLv {
+template <typename T>
+struct MgLvT {
   int nx, ny, P;
-  float *xa, *xb, *b;
-  const float *ax, *ay, *dg;
-  const float* wd;  // tail levels: omega / dg (the sweeps multiply instead of dividing)
+  T *xa, *xb, *b;
+  const T *ax, *ay, *dg;
+  const T* wd;  // tail levels: omega / dg (the sweeps multiply instead of dividing)
   __device__ __forceinline__ int id(int i, int j) const { return j * P + i; }
 };
 
-struct MgInner {
+template <typename T>
+struct MgInnerT {
+  using Scalar = T;
   static constexpr bool kScaled = false;
   Team tm;
   int pk;                  // pinned cell (level 0) or -1
   MgHier H;
-  float *x0a, *x0b, *b0;   // level 0 solution buffers and right-hand side
-  const float *ax0, *ay0, *dg0;  // level 0: FP32 copy of A (faces, diagonal)
-  float* sm;               // block 0: tail levels (7 fields each), H.tail_smem bytes
-  MgLv* tab;               // this block's shared table of the level views, built in setup
+  T *x0a, *x0b, *b0;   // level 0 solution buffers and right-hand side
+  const T *ax0, *ay0, *dg0;  // level 0: FP32 copy of A (faces, diagonal)
+  T* sm;               // block 0: tail levels (7 fields each), H.tail_smem bytes
+  MgLvT<T>* tab;               // this block's shared table of the level views, built in setup
   // level l in global memory (S = false) or, for tail levels, in block 0's
   // shared memory (S = true): one read of the block's table (the views are
   // formed once per solve; the hierarchy itself lives in local memory)
-  __device__ __forceinline__ MgLv lv(int l, bool S = false) const { return tab[2 * l + (S ? 1 : 0)]; }
-  __device__ MgLv lv_make(int l, bool S) const {
-    MgLv L;
+  __device__ __forceinline__ MgLvT<T> lv(int l, bool S = false) const { return tab[2 * l + (S ? 1 : 0)]; }
+  __device__ MgLvT<T> lv_make(int l, bool S) const {
+    MgLvT<T> L;
     L.nx = H.lv[l].nx; L.ny = H.lv[l].ny; L.P = L.nx + 2;
     const size_t g = (size_t)(L.nx + 2) * (size_t)(L.ny + 2);
     L.wd = nullptr;
@@ -1386,14 +1395,14 @@ struct MgInner {
       L.xa = x0a; L.xb = x0b; L.b = b0; L.ax = ax0; L.ay = ay0; L.dg = dg0;
       return L;
     }
-    float* base;
+    T* base;
     if (S) {
       // shared-memory levels hold a seventh field, omega / dg
       base = sm;
       for (int q = H.tail; q < l; ++q) base += 7 * (size_t)(H.lv[q].nx + 2) * (size_t)(H.lv[q].ny + 2);
       L.wd = base + 6 * g;
     } else {
-      base = H.pool + H.lv[l].off;
+      base = static_cast<T*>(H.pool) + H.lv[l].off;
     }
     L.xa = base; L.xb = base + g; L.b = base + 2 * g;
     L.ax = base + 3 * g; L.ay = base + 4 * g; L.dg = base + 5 * g;
@@ -1402,7 +1411,7 @@ struct MgInner {
   // shared-memory views read with plain loads; global ones through L2 (other
   // blocks wrote them since this block last looked)
   template <bool S>
-  __device__ __forceinline__ static float ld(const float* p) {
+  __device__ __forceinline__ static T ld(const T* p) {
     if constexpr (S) return *p;
     else return __ldcg(p);
   }
@@ -1419,41 +1428,41 @@ struct MgInner {
     }
   }
   template <bool S>
-  __device__ __forceinline__ static float apply(const MgLv& L, const float* x, int k) {
-    float v = L.dg[k] * ld<S>(x + k);
-    v = __fmaf_rn(-L.ax[k], ld<S>(x + k - 1), v);
-    v = __fmaf_rn(-L.ax[k + 1], ld<S>(x + k + 1), v);
-    v = __fmaf_rn(-L.ay[k], ld<S>(x + k - L.P), v);
-    v = __fmaf_rn(-L.ay[k + L.P], ld<S>(x + k + L.P), v);
+  __device__ __forceinline__ static T apply(const MgLvT<T>& L, const T* x, int k) {
+    T v = L.dg[k] * ld<S>(x + k);
+    v = fmad_(-L.ax[k], ld<S>(x + k - 1), v);
+    v = fmad_(-L.ax[k + 1], ld<S>(x + k + 1), v);
+    v = fmad_(-L.ay[k], ld<S>(x + k - L.P), v);
+    v = fmad_(-L.ay[k + L.P], ld<S>(x + k + L.P), v);
     return v;
   }
   struct NoEpi {
-    __device__ __forceinline__ void operator()(int, float) const {}
+    __device__ __forceinline__ void operator()(int, T) const {}
   };
   // one damped Jacobi sweep from buffer cur into the other (first: x = 0);
   // epi(k, v) sees every value written
   template <bool S, bool W = false, class Epi = NoEpi>
   __device__ void sweep(int l, bool first, int cur, Epi epi = Epi()) const {
-    const MgLv L = lv(l, S);
-    const float* xs = cur ? L.xb : L.xa;
-    float* xd = cur ? L.xa : L.xb;
-    const float w = H.omega;
+    const MgLvT<T> L = lv(l, S);
+    const T* xs = cur ? L.xb : L.xa;
+    T* xd = cur ? L.xa : L.xb;
+    const T w = H.omega;
     const int pin = l == 0 ? pk : -1;
     cells<S, W>(L.nx, L.ny, [&](int i, int j) {
       const int k = L.id(i, j);
-      float v;
+      T v;
       if constexpr (S) {
         // shared-memory levels: a multiply by omega / dg (block 0's
         // sequential tail is bound by the dependent chain, not by memory)
-        const float q = L.wd[k];
+        const T q = L.wd[k];
         if (first) v = ld<S>(L.b + k) * q;
         else v = ld<S>(xs + k) + (ld<S>(L.b + k) - apply<S>(L, xs, k)) * q;
       } else {
-        const float d = L.dg[k];
+        const T d = L.dg[k];
         if (first) v = w * ld<S>(L.b + k) / d;
         else v = ld<S>(xs + k) + w * (ld<S>(L.b + k) - apply<S>(L, xs, k)) / d;
       }
-      if (k == pin) v = 0.0f;
+      if (k == pin) v = T(0);
       xd[k] = v;
       epi(k, v);
     });
@@ -1464,12 +1473,12 @@ struct MgInner {
   // -- one grid-wide phase and barrier fewer per coarse level
   template <bool S>
   __device__ void restrict_(int l, int cur, bool first_next = false) const {
-    const MgLv F = lv(l, S), Cc = lv(l + 1, S);
-    const float* x = cur ? F.xb : F.xa;
+    const MgLvT<T> F = lv(l, S), Cc = lv(l + 1, S);
+    const T* x = cur ? F.xb : F.xa;
     const int pin = l == 0 ? pk : -1;
-    const float w = H.omega;
+    const T w = H.omega;
     cells<S>(Cc.nx, Cc.ny, [&](int I, int J) {
-      float s = 0.0f;
+      T s = T(0);
       for (int dj = 0; dj < 2; ++dj)
         for (int di = 0; di < 2; ++di) {
           const int i = 2 * I - 1 + di, j = 2 * J - 1 + dj;
@@ -1486,10 +1495,10 @@ struct MgInner {
   // x_l (buffer cl) += cw * x_{l+1} (buffer cc) at the parent cell
   template <bool S>
   __device__ void prolong(int l, int cl, int cc) const {
-    const MgLv F = lv(l, S), Cc = lv(l + 1, S);
-    float* x = cl ? F.xb : F.xa;
-    const float* xc = cc ? Cc.xb : Cc.xa;
-    const float cw = H.cw;
+    const MgLvT<T> F = lv(l, S), Cc = lv(l + 1, S);
+    T* x = cl ? F.xb : F.xa;
+    const T* xc = cc ? Cc.xb : Cc.xa;
+    const T cw = H.cw;
     const int pin = l == 0 ? pk : -1;
     cells<S>(F.nx, F.ny, [&](int i, int j) {
       const int k = F.id(i, j);
@@ -1506,13 +1515,13 @@ struct MgInner {
     for (int q = threadIdx.x; q < 2 * H.nl; q += blockDim.x) tab[q] = lv_make(q >> 1, (q & 1) != 0);
     __syncthreads();
     for (int l = 1; l < H.nl; ++l) {
-      const MgLv F = lv(l - 1), Cc = lv(l);
-      float* cax = const_cast<float*>(Cc.ax);
-      float* cay = const_cast<float*>(Cc.ay);
-      float* cdg = const_cast<float*>(Cc.dg);
-      auto axf = [&](int i, int j) -> float { return (i <= F.nx + 1 && j <= F.ny) ? F.ax[F.id(i, j)] : 0.0f; };
-      auto ayf = [&](int i, int j) -> float { return (i <= F.nx && j <= F.ny + 1) ? F.ay[F.id(i, j)] : 0.0f; };
-      auto dgf = [&](int i, int j) -> float { return (i <= F.nx && j <= F.ny) ? F.dg[F.id(i, j)] : 0.0f; };
+      const MgLvT<T> F = lv(l - 1), Cc = lv(l);
+      T* cax = const_cast<T*>(Cc.ax);
+      T* cay = const_cast<T*>(Cc.ay);
+      T* cdg = const_cast<T*>(Cc.dg);
+      auto axf = [&](int i, int j) -> T { return (i <= F.nx + 1 && j <= F.ny) ? F.ax[F.id(i, j)] : T(0); };
+      auto ayf = [&](int i, int j) -> T { return (i <= F.nx && j <= F.ny + 1) ? F.ay[F.id(i, j)] : T(0); };
+      auto dgf = [&](int i, int j) -> T { return (i <= F.nx && j <= F.ny) ? F.dg[F.id(i, j)] : T(0); };
       cells<false>(Cc.nx + 1, Cc.ny + 1, [&](int I, int J) {
         const int k = Cc.id(I, J);
         if (J <= Cc.ny) cax[k] = axf(2 * I - 1, 2 * J - 1) + axf(2 * I - 1, 2 * J);
@@ -1521,8 +1530,8 @@ struct MgInner {
           // Galerkin: sum of the aggregate's diagonals minus twice its
           // internal couplings (= its external faces plus its diagonal shifts)
           const int i0 = 2 * I - 1, j0 = 2 * J - 1;
-          float d = dgf(i0, j0) + dgf(i0 + 1, j0) + dgf(i0, j0 + 1) + dgf(i0 + 1, j0 + 1);
-          float internal = 0.0f;
+          T d = dgf(i0, j0) + dgf(i0 + 1, j0) + dgf(i0, j0 + 1) + dgf(i0 + 1, j0 + 1);
+          T internal = T(0);
           if (i0 + 1 <= F.nx) internal += axf(i0 + 1, j0) + axf(i0 + 1, j0 + 1);
           if (j0 + 1 <= F.ny) internal += ayf(i0, j0 + 1) + ayf(i0 + 1, j0 + 1);
           if (l == 1 && pk >= 0 && I == 1 && J == 1) {
@@ -1533,25 +1542,25 @@ struct MgInner {
             // anchor.  The coarse operators are then nonsingular like the
             // pinned system, instead of near-singular along the constant.
             d = dgf(i0 + 1, j0) + dgf(i0, j0 + 1) + dgf(i0 + 1, j0 + 1);
-            internal = 0.0f;
+            internal = T(0);
             if (i0 + 1 <= F.nx && j0 + 1 <= F.ny) internal = axf(i0 + 1, j0 + 1) + ayf(i0 + 1, j0 + 1);
           }
-          cdg[k] = d - 2.0f * internal;
+          cdg[k] = d - T(2) * internal;
         }
       });
       if (!R.gs.sync()) return false;
     }
     if (tm.rank == 0 && H.tail < H.nl) {
       for (int l = H.tail; l < H.nl; ++l) {
-        const MgLv G = lv(l), Sm = lv(l, true);
+        const MgLvT<T> G = lv(l), Sm = lv(l, true);
         const int g = Sm.P * (Sm.ny + 2);
         for (int k = threadIdx.x; k < g; k += blockDim.x) {
-          Sm.xa[k] = 0.0f; Sm.xb[k] = 0.0f; Sm.b[k] = 0.0f;
-          const_cast<float*>(Sm.ax)[k] = __ldcg(G.ax + k);
-          const_cast<float*>(Sm.ay)[k] = __ldcg(G.ay + k);
-          const float dk = __ldcg(G.dg + k);
-          const_cast<float*>(Sm.dg)[k] = dk;
-          const_cast<float*>(Sm.wd)[k] = dk != 0.0f ? H.omega / dk : 0.0f;
+          Sm.xa[k] = T(0); Sm.xb[k] = T(0); Sm.b[k] = T(0);
+          const_cast<T*>(Sm.ax)[k] = __ldcg(G.ax + k);
+          const_cast<T*>(Sm.ay)[k] = __ldcg(G.ay + k);
+          const T dk = __ldcg(G.dg + k);
+          const_cast<T*>(Sm.dg)[k] = dk;
+          const_cast<T*>(Sm.wd)[k] = dk != T(0) ? H.omega / dk : T(0);
         }
       }
       __syncthreads();
@@ -1567,29 +1576,29 @@ struct MgInner {
   // operator, the pseudo-inverse of M on the mean-free vectors.
   __device__ void coarse_inverse() const {
     const int l = H.nl - 1;
-    const MgLv L = lv(l, true);
+    const MgLvT<T> L = lv(l, true);
     const int n = L.nx * L.ny;
-    float* B = sm + H.inv_off;      // 64 x 64, row r at B + 64 r
-    float* col = L.xb;              // scratch: the pivot column (the level's second buffer)
-    __shared__ float s_c;
-    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) B[e] = 0.0f;
+    T* B = sm + H.inv_off;      // 64 x 64, row r at B + 64 r
+    T* col = L.xb;              // scratch: the pivot column (the level's second buffer)
+    __shared__ T s_c;
+    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) B[e] = T(0);
     __syncthreads();
     if (threadIdx.x == 0) {
-      float tr = 0.0f;
+      T tr = T(0);
       for (int c = 0; c < n; ++c) {
         const int j = c / L.nx, i = c - j * L.nx;
         tr += L.dg[L.id(i + 1, j + 1)];
       }
       // pinned gauge: the coarse operators carry the pin's Dirichlet anchor
       // and are nonsingular; no rank-one term
-      s_c = pk >= 0 ? 0.0f : tr / ((float)n * (float)n);
+      s_c = pk >= 0 ? T(0) : tr / ((T)n * (T)n);
     }
     __syncthreads();
-    const float cs = s_c;
+    const T cs = s_c;
     for (int c = threadIdx.x; c < n; c += blockDim.x) {
       const int j = c / L.nx, i = c - j * L.nx;
       const int k = L.id(i + 1, j + 1);
-      float* row = B + 64 * c;
+      T* row = B + 64 * c;
       for (int q = 0; q < n; ++q) row[q] = cs;
       row[c] += L.dg[k];
       if (i > 0) row[c - 1] -= L.ax[k];
@@ -1601,46 +1610,46 @@ struct MgInner {
     for (int p = 0; p < n; ++p) {
       for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = B[64 * i + p];
       __syncthreads();
-      const float ip = 1.0f / col[p];
-      for (int q = threadIdx.x; q < n; q += blockDim.x) B[64 * p + q] = (q == p ? 1.0f : B[64 * p + q]) * ip;
+      const T ip = T(1) / col[p];
+      for (int q = threadIdx.x; q < n; q += blockDim.x) B[64 * p + q] = (q == p ? T(1) : B[64 * p + q]) * ip;
       __syncthreads();
       for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
         const int i = e / n, q = e - i * n;
         if (i == p) continue;
-        const float f = col[i];
-        B[64 * i + q] = (q == p ? 0.0f : B[64 * i + q]) - f * B[64 * p + q];
+        const T f = col[i];
+        B[64 * i + q] = (q == p ? T(0) : B[64 * i + q]) - f * B[64 * p + q];
       }
       __syncthreads();
     }
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
       const int i = e / n, q = e - i * n;
       if (q > i) {
-        const float m = 0.5f * (B[64 * i + q] + B[64 * q + i]);
+        const T m = T(0.5) * (B[64 * i + q] + B[64 * q + i]);
         B[64 * i + q] = m;
         B[64 * q + i] = m;
       }
     }
-    for (int e = threadIdx.x; e < L.P * (L.ny + 2); e += blockDim.x) col[e] = 0.0f;
+    for (int e = threadIdx.x; e < L.P * (L.ny + 2); e += blockDim.x) col[e] = T(0);
     __syncthreads();
   }
   // the right-hand side, and with it the first level-0 sweep from x = 0
   // (w b / dg into x0b, bit for bit what sweep<false>(0, true, 0) writes)
-  __device__ __forceinline__ void set_rhs(int k, int, float v) {
+  __device__ __forceinline__ void set_rhs(int k, int, T v) {
     b0[k] = v;
-    x0b[k] = k == pk ? 0.0f : H.omega * v / dg0[k];
+    x0b[k] = k == pk ? T(0) : H.omega * v / dg0[k];
   }
-  __device__ __forceinline__ float y(int k, int) const { return k == pk ? 0.0f : __ldcg(x0a + k); }
+  __device__ __forceinline__ T y(int k, int) const { return k == pk ? T(0) : __ldcg(x0a + k); }
   // The nuc sweeps of a coarsest level of at most 64 cells in the first
   // warp: each lane's (at most two) cells keep their coefficients and
   // right-hand side in registers across the sweeps, so a sweep is five
   // shared-memory reads and a few FMAs per cell (the same arithmetic as
   // sweep<true>, bit for bit).
   __device__ void coarsest_warp(int l) const {
-    const MgLv L = lv(l, true);
+    const MgLvT<T> L = lv(l, true);
     const int n = L.nx * L.ny, lane = threadIdx.x & 31;
     const int pin = l == 0 ? pk : -1;
     int kk[2];
-    float cb[2], cq[2], cd[2], cw_[2], ce[2], cs[2], cn[2];
+    T cb[2], cq[2], cd[2], cw_[2], ce[2], cs[2], cn[2];
 #pragma unroll
     for (int m = 0; m < 2; ++m) {
       const int c = lane + 32 * m;
@@ -1655,24 +1664,24 @@ struct MgInner {
     }
     for (int s = 0; s < H.nuc; ++s) {
       if (s > 0) __syncwarp();
-      const float* xs = (s & 1) ? L.xb : L.xa;
-      float* xd = (s & 1) ? L.xa : L.xb;
+      const T* xs = (s & 1) ? L.xb : L.xa;
+      T* xd = (s & 1) ? L.xa : L.xb;
 #pragma unroll
       for (int m = 0; m < 2; ++m) {
         const int k = kk[m];
         if (k < 0) continue;
-        float v;
+        T v;
         if (s == 0) {
           v = cb[m] * cq[m];
         } else {
-          float a = cd[m] * xs[k];
-          a = __fmaf_rn(-cw_[m], xs[k - 1], a);
-          a = __fmaf_rn(-ce[m], xs[k + 1], a);
-          a = __fmaf_rn(-cs[m], xs[k - L.P], a);
-          a = __fmaf_rn(-cn[m], xs[k + L.P], a);
+          T a = cd[m] * xs[k];
+          a = fmad_(-cw_[m], xs[k - 1], a);
+          a = fmad_(-ce[m], xs[k + 1], a);
+          a = fmad_(-cs[m], xs[k - L.P], a);
+          a = fmad_(-cn[m], xs[k + L.P], a);
           v = xs[k] + (cb[m] - a) * cq[m];
         }
-        if (k == pin) v = 0.0f;
+        if (k == pin) v = T(0);
         xd[k] = v;
       }
     }
@@ -1680,18 +1689,18 @@ struct MgInner {
   // The coarsest level solved by the first warp: x = P B P b (B the dense
   // inverse of coarse_inverse, P the projection off the constant), into xa.
   __device__ void coarsest_exact(int l) const {
-    const MgLv L = lv(l, true);
+    const MgLvT<T> L = lv(l, true);
     const int n = L.nx * L.ny, lane = threadIdx.x & 31;
-    const float* B = sm + H.inv_off;
-    float* v = L.xb;  // the mean-free right-hand side, compact
+    const T* B = sm + H.inv_off;
+    T* v = L.xb;  // the mean-free right-hand side, compact
     int kk[2];
-    float bb[2];
-    float sum = 0.0f;
+    T bb[2];
+    T sum = T(0);
 #pragma unroll
     for (int m = 0; m < 2; ++m) {
       const int c = lane + 32 * m;
       kk[m] = -1;
-      bb[m] = 0.0f;
+      bb[m] = T(0);
       if (c < n) {
         const int j = c / L.nx, i = c - j * L.nx;
         kk[m] = L.id(i + 1, j + 1);
@@ -1702,22 +1711,22 @@ struct MgInner {
     // reference gauge: P B P with P the projection off the constant; the
     // pinned gauge's coarse operator is nonsingular (plain B)
     const bool proj = pk < 0;
-    const float mb = proj ? warp_sum(sum) / (float)n : 0.0f;
+    const T mb = proj ? warp_sum(sum) / (T)n : T(0);
 #pragma unroll
     for (int m = 0; m < 2; ++m)
       if (kk[m] >= 0) v[lane + 32 * m] = bb[m] - mb;
     __syncwarp();
-    float x[2] = {0.0f, 0.0f};
+    T x[2] = {T(0), T(0)};
     for (int c = 0; c < n; ++c) {
-      const float vc = v[c];
-      x[0] = __fmaf_rn(B[64 * c + lane], vc, x[0]);
-      x[1] = __fmaf_rn(B[64 * c + lane + 32], vc, x[1]);
+      const T vc = v[c];
+      x[0] = fmad_(B[64 * c + lane], vc, x[0]);
+      x[1] = fmad_(B[64 * c + lane + 32], vc, x[1]);
     }
-    float sx = 0.0f;
+    T sx = T(0);
 #pragma unroll
     for (int m = 0; m < 2; ++m)
       if (kk[m] >= 0) sx += x[m];
-    const float mx = proj ? warp_sum(sx) / (float)n : 0.0f;
+    const T mx = proj ? warp_sum(sx) / (T)n : T(0);
 #pragma unroll
     for (int m = 0; m < 2; ++m)
       if (kk[m] >= 0) L.xa[kk[m]] = x[m] - mx;
@@ -1728,7 +1737,7 @@ struct MgInner {
   __device__ void tail_cycle() const {
     const int L = H.nl, nu = H.nu, t = H.tail;
     {
-      const MgLv G = lv(t), Sm = lv(t, true);
+      const MgLvT<T> G = lv(t), Sm = lv(t, true);
       const int g = Sm.P * (Sm.ny + 2);
       for (int k = threadIdx.x; k < g; k += blockDim.x) Sm.b[k] = __ldcg(G.b + k);
     }
@@ -1771,9 +1780,9 @@ struct MgInner {
     }
     __syncthreads();
     const int pb = out_buf(t);
-    const MgLv G = lv(t), Sm = lv(t, true);
-    const float* src = pb ? Sm.xb : Sm.xa;
-    float* dst = pb ? G.xb : G.xa;
+    const MgLvT<T> G = lv(t), Sm = lv(t, true);
+    const T* src = pb ? Sm.xb : Sm.xa;
+    T* dst = pb ? G.xb : G.xa;
     const int g = Sm.P * (Sm.ny + 2);
     for (int k = threadIdx.x; k < g; k += blockDim.x) dst[k] = src[k];
   }
@@ -1843,9 +1852,14 @@ struct MgInner {
   }
 };
 
-// One mixed solve of case a by team tm with the multigrid inner iteration
-// (tail: the team's block 0 shared memory, at least a.mg.tail_smem bytes).
-__device__ void mixed_mg_case(const PoissonArgs& a, const Team& tm, GridReducer& R, float* tail, MgLv* tab) {
+// One solve of case a by team tm with the multigrid inner iteration in
+// arithmetic T (tail: the team's block 0 shared memory, at least
+// a.mg.tail_smem bytes).  T = float: the mixed path, level 0 is the FP32
+// copy of A; T = double: the same flexible CG and V-cycle with every level in
+// FP64, level 0 being A itself and its vectors the plain PCG's d, d2, Ad
+// (unused by the flexible CG).
+template <typename T>
+__device__ void mg_case(const PoissonArgs& a, const Team& tm, GridReducer& R, T* tail, MgLvT<T>* tab) {
   const Dims D = a.D;
   // a launch without room for the tail is refused, not run (every block of
   // the team takes the same branch, so no barrier is left waiting)
@@ -1859,11 +1873,15 @@ __device__ void mixed_mg_case(const PoissonArgs& a, const Team& tm, GridReducer&
   }
   const Tiles tl = make_tiles(D, blockDim.x);
   TileOwn own{D, tl, tm};
-  MgInner in;
+  MgInnerT<T> in;
   in.tm = tm;
   in.pk = a.pinned ? D.P + 1 : -1;
   in.H = a.mg;
-  in.x0a = a.e32; in.x0b = a.d32; in.b0 = a.r32; in.ax0 = a.ax32; in.ay0 = a.ay32; in.dg0 = a.aP32;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    in.x0a = a.e32; in.x0b = a.d32; in.b0 = a.r32; in.ax0 = a.ax32; in.ay0 = a.ay32; in.dg0 = a.aP32;
+  } else {
+    in.x0a = a.d; in.x0b = a.d2; in.b0 = a.Ad; in.ax0 = a.ax; in.ay0 = a.ay; in.dg0 = a.aP;
+  }
   in.sm = tail;
   in.tab = tab;
   if (!in.setup(R)) {
@@ -1875,13 +1893,25 @@ __device__ void mixed_mg_case(const PoissonArgs& a, const Team& tm, GridReducer&
   fcg_mixed(a, own, in, R);
 }
 
+// The multigrid tail's dynamic shared memory (both arithmetics).
+extern __shared__ __align__(16) unsigned char mg_dyn[];
+
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg(PoissonArgs a) {
-  extern __shared__ float mg_tail[];
-  __shared__ MgLv mg_tab[2 * kMgMaxLevels];
+  __shared__ MgLvT<float> mg_tab[2 * kMgMaxLevels];
   if (a.redo && *a.redo == 0) return;  // the pinned fallback, not needed (every block agrees)
   const Team tm = grid_team();
   GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
-  mixed_mg_case(a, tm, R, mg_tail, mg_tab);
+  mg_case<float>(a, tm, R, reinterpret_cast<float*>(mg_dyn), mg_tab);
+}
+
+// The FP64 multigrid form (COVOF_PREC_FP64_MG): the kernel above with the
+// V-cycle in FP64.
+__global__ void __launch_bounds__(1024, 1) k_pcg_fp64_mg(PoissonArgs a) {
+  __shared__ MgLvT<double> mg_tab[2 * kMgMaxLevels];
+  if (a.redo && *a.redo == 0) return;
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  mg_case<double>(a, tm, R, reinterpret_cast<double*>(mg_dyn), mg_tab);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_stream(PoissonArgs a) {
@@ -1998,15 +2028,26 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_smem_batch(const PoissonA
 
 // Multigrid inner form: each case's hierarchy is its own; the launch's
 // dynamic shared memory holds the largest tail of the batch.
+template <typename T>
+__device__ __forceinline__ void mg_batch(const PoissonArgs* __restrict__ cases, const BatchTeams& bt, T* tail,
+                                         MgLvT<T>* tab) {
+  int4 T4;
+  const Team tm = batch_team(bt, T4);
+  const int t = bt.block_team[blockIdx.x];
+  GridReducer R{bt.part + (size_t)16 * T4.x, GridSync{bt.bar + 32 * t, bt.err + t, (unsigned)T4.y, 0u}, 0, tm.rank};
+  for (int q = T4.z; q < T4.w; ++q) mg_case<T>(cases[bt.case_list[q]], tm, R, tail, tab);
+}
+
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg_batch(const PoissonArgs* __restrict__ cases,
                                                                 BatchTeams bt) {
-  extern __shared__ float mg_tail[];
-  __shared__ MgLv mg_tab[2 * kMgMaxLevels];
-  int4 T;
-  const Team tm = batch_team(bt, T);
-  const int t = bt.block_team[blockIdx.x];
-  GridReducer R{bt.part + (size_t)16 * T.x, GridSync{bt.bar + 32 * t, bt.err + t, (unsigned)T.y, 0u}, 0, tm.rank};
-  for (int q = T.z; q < T.w; ++q) mixed_mg_case(cases[bt.case_list[q]], tm, R, mg_tail, mg_tab);
+  __shared__ MgLvT<float> mg_tab[2 * kMgMaxLevels];
+  mg_batch<float>(cases, bt, reinterpret_cast<float*>(mg_dyn), mg_tab);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_pcg_fp64_mg_batch(const PoissonArgs* __restrict__ cases,
+                                                               BatchTeams bt) {
+  __shared__ MgLvT<double> mg_tab[2 * kMgMaxLevels];
+  mg_batch<double>(cases, bt, reinterpret_cast<double*>(mg_dyn), mg_tab);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt) {

@@ -12,10 +12,11 @@ struct PcgResult {
   double relres;  // ||r||/||b|| at exit (mixed: true FP64 residual)
 };
 
-// Geometric multigrid hierarchy of the mixed path's FP32 inner operator
-// (levels 1 .. nl-1; level 0 is the scaled fine operator itself).  Level l
-// owns 7 arrays of (nx+2)*(ny+2) floats at pool + off: two solution buffers,
-// right-hand side, west / south face coefficients, diagonal, scratch.
+// Geometric multigrid hierarchy of the flexible CG's inner V-cycle (levels
+// 1 .. nl-1; level 0 is the fine operator itself).  Level l owns 6 arrays of
+// (nx+2)*(ny+2) elements at pool + off (elements of the V-cycle's arithmetic:
+// float on the mixed path, double for COVOF_PREC_FP64_MG): two solution
+// buffers, right-hand side, west / south face coefficients, diagonal.
 constexpr int kMgMaxLevels = 16;
 constexpr long long kMgTailSmem = 200 * 1024;  // cap on the shared-memory tail (plus ~6 KB static)
 constexpr long long kMgWarpCoarse = 256;        // coarsest levels this small run in one warp
@@ -27,14 +28,14 @@ struct MgHier {
   MgLevel lv[kMgMaxLevels];
   int nl;      // levels including level 0
   int tail;    // first level run by block 0 alone out of shared memory, nl if none
-  float* pool;
+  void* pool;  // float or double elements, by the V-cycle's arithmetic
   float omega; // Jacobi weight
   float cw;    // coarse-correction weight
   int nu, nuc; // sweeps before / after each coarse correction; sweeps on the coarsest level
   int tail_smem;     // bytes of block 0's shared memory holding the tail levels
   // exact != 0: the coarsest level (at most 64 cells, in the tail) is solved
-  // by a dense inverse formed once per solve, 64 x 64 floats at float offset
-  // inv_off of the tail's shared memory, instead of nuc sweeps
+  // by a dense inverse formed once per solve, 64 x 64 elements at element
+  // offset inv_off of the tail's shared memory, instead of nuc sweeps
   int exact, inv_off;
 };
 
@@ -114,8 +115,10 @@ __global__ void k_pcg_mixed_cheb(PoissonArgs a);
 __global__ void k_pcg_mixed_stream(PoissonArgs a);
 __global__ void k_pcg_mixed_cluster(PoissonArgs a);
 __global__ void k_pcg_mixed_mg(PoissonArgs a);
+__global__ void k_pcg_fp64_mg(PoissonArgs a);
 __global__ void k_pcg_fp64_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_mg_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
+__global__ void k_pcg_fp64_mg_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_smem_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 // Shared-memory bytes of k_pcg_mixed_cheb for a strip of R rows of nx cells.

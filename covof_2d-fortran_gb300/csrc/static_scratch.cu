@@ -31,19 +31,15 @@ constexpr size_t kScratchBytes =
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-void* g_scratch_addr[kMaxDevices] = {};  // device address per device, set on first use
-
-// Once per device, with that device current: the host-side name g_scratch is
-// only a stand-in; the kernels need its device address.
-int scratch_base(int device, unsigned char** base) {
-  if (device < 0 || device >= kMaxDevices) return COVOF_UNSUPPORTED;
-  if (!g_scratch_addr[device]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return COVOF_CUDA_ERROR;
-    g_scratch_addr[device] = p;
-  }
-  *base = static_cast<unsigned char*>(g_scratch_addr[device]);
+// The device address of g_scratch on the current device.  The host-side
+// name g_scratch is only a stand-in; the kernels need the address, which is
+// looked up on every call (cheap once the module is loaded; a first call on
+// a device loads it, and a cudaDeviceReset can move the array, so no
+// address is kept between calls).
+int scratch_base(unsigned char** base) {
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return COVOF_CUDA_ERROR;
+  *base = static_cast<unsigned char*>(p);
   return COVOF_OK;
 }
 
@@ -60,18 +56,23 @@ extern "C" int covof_poisson_solve_rhs_static_dev(const covof_params* prm, doubl
   if (!prm || !b || !rho_u || !rho_v || !p) return COVOF_INVALID;
   const covof_params& P = *prm;
   if (P.nx < 2 || P.ny < 2 || !(P.dx > 0.0) || !(P.dy > 0.0)) return COVOF_INVALID;
+  // this entry runs the plain FP64 Jacobi-PCG only
+  if (P.p_precision != COVOF_PREC_FP64 || P.p_precond == COVOF_PRECOND_SSOR) return COVOF_UNSUPPORTED;
   for (int s = 0; s < 4; ++s)
     if (P.bc_type[s] != COVOF_BC_DIRICHLET && P.bc_type[s] != COVOF_BC_FREESLIP) return COVOF_UNSUPPORTED;
   const size_t g = (size_t)(P.nx + 2) * (size_t)(P.ny + 2);
   if (g > kMaxGhosted) return COVOF_TOO_LARGE;
 
+  // an error left by the caller's earlier asynchronous work is reported as
+  // such before the shared array is touched, not taken for this call's
+  if (cudaGetLastError() != cudaSuccess) return COVOF_CUDA_ERROR;
   int dev = 0, sms = 0, coop = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return COVOF_CUDA_ERROR;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return COVOF_CUDA_ERROR;
   if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
     return COVOF_UNSUPPORTED;
   unsigned char* base = nullptr;
-  int st = scratch_base(dev, &base);
+  int st = scratch_base(&base);
   if (st != COVOF_OK) return st;
 
   // carve the array (every vector keeps a zero ghost ring)

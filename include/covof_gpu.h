@@ -93,9 +93,13 @@ enum { COVOF_LIMITER_SUPERBEE = 0, COVOF_LIMITER_VAN_LEER = 1, COVOF_LIMITER_MUS
  * (src/module_simulation.f90:2531,2579-2582).  PINNED: same operator with
  * cell (1,1) held at p = 0 (no mean removal). */
 enum { COVOF_GAUGE_REFERENCE = 0, COVOF_GAUGE_PINNED = 1 };
-/* Poisson arithmetic.  FP64: plain FP64 PCG.  MIXED: FP32 PCG inner solves
- * inside FP64 iterative refinement (FP64 residual, FP64 solution). */
-enum { COVOF_PREC_FP64 = 0, COVOF_PREC_MIXED = 1 };
+/* Poisson arithmetic.  FP64: plain FP64 PCG (the reference's algorithm).
+ * MIXED: FP64 flexible CG on the true FP64 residual, preconditioned by an
+ * FP32 inner iteration (p_inner_kind; FP64 solution).  FP64_MG: the MIXED
+ * path with COVOF_INNER_MG and the V-cycle in FP64 (same kernels, same
+ * p_mg_* settings, same gauge handling): beside MIXED it isolates what the
+ * FP32 arithmetic of the inner iteration buys.  No reference counterpart. */
+enum { COVOF_PREC_FP64 = 0, COVOF_PREC_MIXED = 1, COVOF_PREC_FP64_MG = 2 };
 
 /* Plain-old-data parameter block (the subset of config_t,
  * src/module_config.f90:31-184, that the hot path reads). */
@@ -285,15 +289,19 @@ int covof_last_refine_steps(const covof_handle* h, int* steps);
  * the call: a host code whose pool allocator reserved the whole GPU at
  * start-up, or a time loop that must not pay cudaMalloc's device-wide
  * synchronisation.  Same operator, solver and results as
- * covof_poisson_solve_rhs_dev with prm->p_precision = FP64, but no handle:
- * inputs and outputs are the caller's device pointers, the scratch is a
- * fixed static device array (about 5.4 MB, held by every GPU that loads the
- * library until exit) and nothing is allocated.  Limit: (nx+2)*(ny+2) <=
- * 258*258 (256 x 256 cells); larger meshes return COVOF_TOO_LARGE.  The
- * first call on a device looks up the array's device address, so make it
- * before any stream capture.  Runs on the legacy default stream and is
- * synchronous.  All calls share the array: calls that overlap on the GPU
- * (from several host threads or streams) race. */
+ * covof_poisson_solve_rhs_dev with prm->p_precision = FP64 and the Jacobi
+ * preconditioner (other p_precision values and p_precond = SSOR return
+ * COVOF_UNSUPPORTED), but no handle: inputs and outputs are the caller's
+ * device pointers, the scratch is a fixed static device array (about 5.4 MB,
+ * held by every GPU that loads the library until exit) and nothing is
+ * allocated.  Limit: (nx+2)*(ny+2) <= 258*258 (256 x 256 cells); larger
+ * meshes return COVOF_TOO_LARGE.  Every call looks up the array's device
+ * address on the current device; the first call on a device also loads the
+ * library's device code there, so make it before any stream capture.  An
+ * error pending from the caller's earlier work is returned as
+ * COVOF_CUDA_ERROR before anything is launched.  Runs on the legacy default
+ * stream and is synchronous.  All calls share the array: calls that overlap
+ * on the GPU (from several host threads or streams) race. */
 int covof_poisson_solve_rhs_static_dev(const covof_params* prm, double dt, const double* b,
                                        const double* rho_u, const double* rho_v, double* p,
                                        int* iters, double* relres);

@@ -371,12 +371,145 @@ double dot_omp(const double* x, const double* y, size_t n) {
   return s;
 }
 
+// The Jacobi-PCG of poisson_pcg on nthreads host threads: the same
+// recurrences (z = r / a_P, alpha = <r,z>/<d,Ad>, beta = <r,z>_new/<r,z>_old,
+// exit on ||r||/||b||), with every vector pass inside one parallel region.
+// Rows are split statically among the threads; each thread writes its
+// partial sums to its own slot, and every thread combines the slots in
+// thread order, so all threads hold the same scalars and the result is
+// reproducible for a given thread count (it differs from the serial loop's
+// only in the association of the sums).  Three barriers per iteration:
+// after A d and <d,Ad>, after the x, r updates and their sums, after the
+// direction update (the next product reads the neighbours' rows).
+int poisson_pcg_par(const covof_params* prm, Poisson& P, std::vector<double>& x, int* iters_out,
+                    double* relres_out, int nthreads, int fixed_iters) {
+  const int nx = P.nx, ny = P.ny;
+  const size_t n = (size_t)nx * ny;
+  const bool pinned = prm->p_gauge == COVOF_GAUGE_PINNED;
+  const double tol = prm->p_tol;
+  const int max_iter = fixed_iters > 0 ? fixed_iters : prm->p_max_iter;
+  if (pinned) { P.b[0] = 0.0; x[0] = 0.0; }
+  std::vector<double> r(n), d(n), Ad(n);
+  constexpr int kPad = 8;  // one 64-byte line per thread and buffer
+  std::vector<double> part(2 * (size_t)nthreads * kPad, 0.0);
+  const double* aP = P.aP.data(); const double* aW = P.aW.data(); const double* aE = P.aE.data();
+  const double* aS = P.aS.data(); const double* aN = P.aN.data();
+  double* xp = x.data(); double* rp = r.data(); double* dp = d.data(); double* Adp = Ad.data();
+  const double* bp = P.b.data();
+  int iters = 0, status = COVOF_OK;
+  double r_norm = 0.0, b_norm = 1.0;
+  auto Arow = [&](const double* v, double* y, int j) {
+    for (int i = 1; i <= nx; ++i) {
+      const size_t q = P.k(i, j);
+      double val = aP[q] * v[q];
+      if (i > 1) val = val - aW[q] * v[q - 1];
+      if (i < nx) val = val - aE[q] * v[q + 1];
+      if (j > 1) val = val - aS[q] * v[q - nx];
+      if (j < ny) val = val - aN[q] * v[q + nx];
+      y[q] = val;
+    }
+    if (pinned && j == 1) y[0] = 0.0;
+  };
+  auto zval = [&](size_t q) { return (pinned && q == 0) ? 0.0 : rp[q] / aP[q]; };
+#pragma omp parallel num_threads(nthreads)
+  {
+    const int T = omp_get_num_threads(), t = omp_get_thread_num();
+    const int j0 = 1 + (int)((long long)ny * t / T), j1 = (int)((long long)ny * (t + 1) / T);
+    int buf = 0;
+    // combine NV partial sums of every thread, in thread order
+    auto reduce = [&](const double* mine, int nv, double* out) {
+      double* slot = part.data() + ((size_t)buf * T + t) * kPad;
+      for (int q = 0; q < nv; ++q) slot[q] = mine[q];
+#pragma omp barrier
+      for (int q = 0; q < nv; ++q) out[q] = 0.0;
+      for (int s = 0; s < T; ++s) {
+        const double* o = part.data() + ((size_t)buf * T + s) * kPad;
+        for (int q = 0; q < nv; ++q) out[q] += o[q];
+      }
+      buf ^= 1;  // the next reduction writes the other buffer: no second barrier
+    };
+    // r = b - A x; ||b||, ||r||, <r,z>; d = z
+    for (int j = j0; j <= j1; ++j) Arow(xp, Adp, j);
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int j = j0; j <= j1; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        const size_t q = P.k(i, j);
+        rp[q] = bp[q] - Adp[q];
+        const double z = zval(q);
+        dp[q] = z;
+        acc[0] += bp[q] * bp[q];
+        acc[1] += rp[q] * rp[q];
+        acc[2] += rp[q] * z;
+      }
+    double s3[3];
+    reduce(acc, 3, s3);
+    double bn = std::sqrt(s3[0]);
+    if (bn < 1.0e-30) bn = 1.0;
+    double rn = std::sqrt(s3[1]), rz_old = s3[2];
+    int it_local = 0, st_local = COVOF_OK;
+    bool converged = false;
+    if (fixed_iters > 0 || rn / bn > tol) {
+#pragma omp barrier
+      for (int it = 1; it <= max_iter; ++it) {
+        it_local = it;
+        double a1 = 0.0;
+        for (int j = j0; j <= j1; ++j) {
+          Arow(dp, Adp, j);
+          for (int i = 1; i <= nx; ++i) { const size_t q = P.k(i, j); a1 += dp[q] * Adp[q]; }
+        }
+        double dAd;
+        reduce(&a1, 1, &dAd);
+        if (std::fabs(dAd) < 1.0e-35) { st_local = COVOF_BREAKDOWN; break; }
+        const double alpha = rz_old / dAd;
+        double a2[2] = {0.0, 0.0};
+        for (int j = j0; j <= j1; ++j)
+          for (int i = 1; i <= nx; ++i) {
+            const size_t q = P.k(i, j);
+            xp[q] = xp[q] + alpha * dp[q];
+            rp[q] = rp[q] - alpha * Adp[q];
+            a2[0] += rp[q] * rp[q];
+            a2[1] += rp[q] * zval(q);
+          }
+        double s2[2];
+        reduce(a2, 2, s2);
+        rn = std::sqrt(s2[0]);
+        if (std::isnan(rn)) { st_local = COVOF_NAN; break; }
+        if (fixed_iters == 0 && rn / bn <= tol) { converged = true; break; }
+        if (std::fabs(rz_old) < 1.0e-35) { st_local = COVOF_BREAKDOWN; break; }
+        const double beta = s2[1] / rz_old;
+        rz_old = s2[1];
+        for (int j = j0; j <= j1; ++j)
+          for (int i = 1; i <= nx; ++i) { const size_t q = P.k(i, j); dp[q] = zval(q) + beta * dp[q]; }
+#pragma omp barrier
+      }
+      if (st_local == COVOF_OK && !converged && fixed_iters == 0) st_local = COVOF_MAXITER;
+    }
+    if (!pinned) {
+      // src/module_simulation.f90:2579-2582
+#pragma omp barrier
+      double s = 0.0;
+      for (int j = j0; j <= j1; ++j)
+        for (int i = 1; i <= nx; ++i) s += xp[P.k(i, j)];
+      double tot;
+      reduce(&s, 1, &tot);
+      const double mean = tot / (double)((long long)nx * ny);
+      for (int j = j0; j <= j1; ++j)
+        for (int i = 1; i <= nx; ++i) { const size_t q = P.k(i, j); xp[q] = xp[q] - mean; }
+    }
+    if (t == 0) { iters = it_local; status = st_local; r_norm = rn; b_norm = bn; }
+  }
+  if (iters_out) *iters_out = iters;
+  if (relres_out) *relres_out = r_norm / b_norm;
+  return status;
+}
+
 // src/module_simulation.f90:2535-2584  PCG + gauge.  x: (nx,ny) warm start / result.
 int poisson_pcg(const covof_params* prm, Poisson& P, std::vector<double>& x, int* iters_out,
                 double* relres_out, int nthreads, int fixed_iters) {
   const size_t n = (size_t)P.nx * P.ny;
   const bool pinned = prm->p_gauge == COVOF_GAUGE_PINNED;
   const bool sgs = prm->p_precond == COVOF_PRECOND_SSOR;
+  if (nthreads > 1 && !sgs) return poisson_pcg_par(prm, P, x, iters_out, relres_out, nthreads, fixed_iters);
   const bool par = nthreads > 1;
   const double tol = prm->p_tol;
   const int max_iter = fixed_iters > 0 ? fixed_iters : prm->p_max_iter;
@@ -2351,6 +2484,15 @@ int orc_mono_step(const covof_params* prm, double dt, double* u, double* v, doub
                    hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1), iters);
 }
 
+// Host threads of the Poisson solve inside orc_sp_step (and so of the time
+// loop): 1 by default, the reference's serial per-rank loop.
+static int g_step_threads = 1;
+int orc_set_step_threads(int n) {
+  if (n < 1) return COVOF_INVALID;
+  g_step_threads = n;
+  return COVOF_OK;
+}
+
 // src/module_simulation.f90:2424-2666 sim_solve_standard_projection
 int orc_sp_step(const covof_params* prm, double dt, double* u, double* v, double* p,
                 const double* rho_u, const double* rho_v, const double* mu,
@@ -2364,7 +2506,7 @@ int orc_sp_step(const covof_params* prm, double dt, double* u, double* v, double
   int s1 = predictor(prm, dt, u, v, rho_u, rho_v, mu, mu_node, fx_sigma, fy_sigma, u_old, v_old,
                      hist_of(u_old, v_old, u_nm1, v_nm1, has_nm1), &iu);
   if (s1 == COVOF_NAN) return s1;
-  int s2 = poisson_driver(prm, dt, u, v, nullptr, rho_u, rho_v, p, &ip, relres, 1, 0);
+  int s2 = poisson_driver(prm, dt, u, v, nullptr, rho_u, rho_v, p, &ip, relres, g_step_threads, 0);
   Mesh m = mesh_of(prm);
   project_correct(prm, m, dt, u, v, p, rho_u, rho_v);
   velocity_bc(prm, m, u, v, false);

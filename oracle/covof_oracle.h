@@ -102,6 +102,9 @@ int orc_predictor(const covof_params* prm, double dt, double* u, double* v, cons
                   const double* fx_sigma, const double* fy_sigma, const double* u_old,
                   const double* v_old, const double* u_nm1, const double* v_nm1, int has_nm1,
                   int* iters);
+/* host threads of the Poisson solve inside orc_sp_step (default 1; the
+ * Jacobi-PCG then runs the fused parallel loop, SGS stays serial) */
+int orc_set_step_threads(int n);
 int orc_sp_step(const covof_params* prm, double dt, double* u, double* v, double* p,
                 const double* rho_u, const double* rho_v, const double* mu,
                 const double* mu_node, const double* fx_sigma, const double* fy_sigma,

@@ -47,6 +47,7 @@ def lib():
             "orc_momentum_rhs": (i, [v, d] + [v] * 11 + [v, v, i]),
             "orc_predictor": (i, [v, d] + [v] * 10 + [v, v, i] + [v]),
             "orc_sp_step": (i, [v, d] + [v] * 11 + [v, v, i] + [v, v, v]),
+            "orc_set_step_threads": (i, [i]),
             "orc_reconstruct": (i, [v, v, v]),
             "orc_wy_step": (i, [v, d, i, v, v, v]),
             "orc_update_physical_properties": (i, [v] * 8),
@@ -128,6 +129,13 @@ def poisson_fixed_iters(prm, dt, b, rho_u, rho_v, p, n_iter, nthreads=1):
     st = lib().orc_poisson_fixed_iters(_params(prm), dt, _p(b), _p(rho_u), _p(rho_v), _p(p),
                                        int(n_iter), int(nthreads), C.byref(rr))
     return rr.value, st
+
+
+def set_step_threads(n):
+    """Host threads of the Poisson solve inside sp_step / time_step (1 by
+    default, the reference's serial loop)."""
+    st = lib().orc_set_step_threads(int(n))
+    assert st == 0, st
 
 
 def project_correct(prm, dt, u, v, p, rho_u, rho_v):

@@ -21,11 +21,14 @@ def _cases(pkg, orc, mixed, n=6, sizes=(32, 48, 64), seed=7):
     return out
 
 
-@pytest.mark.parametrize("mode", ["fp64", "mixed", "mixed_stream", "mixed_mg"])
+@pytest.mark.parametrize("mode", ["fp64", "mixed", "mixed_stream", "mixed_mg", "fp64_mg"])
 def test_batch_matches_oracle_per_case(gpu_pkg, orc, mode):
     pkg = gpu_pkg
-    mixed = mode != "fp64"
+    mixed = mode not in ("fp64", "fp64_mg")
     cases = _cases(pkg, orc, mixed)
+    if mode == "fp64_mg":
+        for p, f, dt in cases:
+            p.p_precision = pkg.capi.PREC_FP64_MG
     kind = {"mixed": pkg.capi.INNER_CHEBYSHEV, "mixed_stream": pkg.capi.INNER_CHEBYSHEV_STREAM,
             "mixed_mg": pkg.capi.INNER_MG}.get(mode)
     if kind is not None:

@@ -23,7 +23,7 @@ def test_operator_is_bit_identical(gpu_pkg, orc):
 
 @pytest.mark.parametrize("gauge", ["pinned", "reference"])
 @pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_strips", "mixed_cluster16", "mixed_cluster4", "mixed_stream", "mixed_cg", "mixed_mg",
-                                  "mixed_mg_plain", "mixed_mg_gridtail"])
+                                  "mixed_mg_plain", "mixed_mg_gridtail", "fp64_mg", "fp64_mg_gridtail"])
 @pytest.mark.parametrize("n", [64, 128])
 def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
     pkg = gpu_pkg
@@ -37,6 +37,12 @@ def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
     q = p.copy()
     q.p_precision = cap.PREC_FP64 if prec == "fp64" else cap.PREC_MIXED
     q.p_inner_kind = cap.INNER_CHEBYSHEV
+    if prec.startswith("fp64_mg"):
+        # the multigrid flexible CG with the V-cycle in FP64
+        q.p_precision = cap.PREC_FP64_MG
+        q.p_inner_kind = cap.INNER_MG
+        if prec == "fp64_mg_gridtail":
+            q.p_mg_tail = 1
     if prec == "mixed_stream":
         q.p_inner_kind = cap.INNER_CHEBYSHEV_STREAM
     elif prec == "mixed_cg":
