@@ -207,17 +207,29 @@ def rel_err(x, ref) -> float:
     return float(np.linalg.norm(a - r) / np.linalg.norm(r))
 
 
-def bubble_state(pkg, orc, prec):
+def initial_fields(pkg, p, C0=None, props=True):
+    """Fields at t = 0 through the GPU library: C's ghosts (apply_vof_bc),
+    the velocity ghosts (apply_velocity_bc), and with props the physical
+    properties and the surface-tension force of C (two-phase cases; single
+    phase: the constant properties)."""
+    f = pkg.Fields.allocate(p)
+    if C0 is not None:
+        f.C[...] = C0
+    with pkg.Solver(p) as s:
+        s.apply_vof_bc(f)
+        s.apply_velocity_bc(f)
+        if props:
+            s.update_physical_properties(f)
+            s.compute_curvature_and_csf(f)
+    return f
+
+
+def bubble_state(pkg, prec):
     """Rising-bubble case (128x256 on [0,1]x[0,2], ELVIRA + Weymouth-Yue,
     BiCGSTAB + Jacobi predictor, Poisson to 1e-10, dt 1e-4) at t = 0."""
     p, C0, dt = pkg.cases.bubble_case()
     p.p_precision = prec
-    f = pkg.Fields.allocate(p)
-    f.C[...] = C0
-    orc.apply_vof_bc(p, f.C)
-    orc.update_physical_properties(p, f)
-    orc.compute_curvature_and_csf(p, f)
-    return p, f, dt
+    return p, initial_fields(pkg, p, C0), dt
 
 
 def sp_steps(pkg, orc, nsteps, cpu_steps):
@@ -232,7 +244,7 @@ def sp_steps(pkg, orc, nsteps, cpu_steps):
                        "mixed: the same with the FP32 V-cycle), dt 1e-4, CUDA-graph step replay",
            "steps": nsteps}
     for name, prec in (("fp64", cap.PREC_FP64), ("fp64_mg", cap.PREC_FP64_MG), ("mixed", cap.PREC_MIXED)):
-        p, f, dt = bubble_state(pkg, orc, prec)
+        p, f, dt = bubble_state(pkg, prec)
         with pkg.Solver(p) as s:
             s.state_set(f)
             st, _ = s.run_steps(dt, 3, graph=True)
@@ -247,7 +259,7 @@ def sp_steps(pkg, orc, nsteps, cpu_steps):
     out["speedup_mixed_vs_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
     out["speedup_mixed_vs_fp64_mg"] = out["mixed"]["steps_per_s"] / out["fp64_mg"]["steps_per_s"]
     if cpu_steps > 0:
-        p, f, dt = bubble_state(pkg, orc, cap.PREC_FP64)
+        p, f, dt = bubble_state(pkg, cap.PREC_FP64)
         t0 = time.perf_counter()
         for k in range(cpu_steps):
             orc.time_step(p, dt, k, f)
@@ -258,38 +270,46 @@ def sp_steps(pkg, orc, nsteps, cpu_steps):
     return out
 
 
-def batch_steps(pkg, orc, ncases, nsteps):
+def batch_steps(pkg, ncases, nsteps, rank=0, world=1):
     """Many independent droplet / bubble cases (sizes 64..512 per direction,
     density ratio 10..1000) stepped together by the batch engine, each batch
     step one CUDA-graph launch with the predictor and Poisson solves of all
     cases in one persistent launch each: the mixed multigrid Poisson, its
     FP64 multigrid twin and plain FP64 Jacobi-PCG, nsteps steps each after
-    two warm-up steps."""
+    two warm-up steps.  With several ranks the cases are split across them
+    (shard.plan: cost-balanced, no collective on the data path); the time is
+    the slowest rank's, the statistics are gathered on the host."""
+    import importlib
+    shard = importlib.import_module(pkg.__name__ + ".shard")
     cap = pkg.capi
     out = {"workload": f"{ncases} droplet/bubble cases, nx, ny in {{64,128,256,512}}, density ratio "
                        "log-uniform 10..1000, viscosity ratio 1..100, sigma 0.01..25, Poisson to rel-res 1e-10, "
-                       "CUDA-graph batch step", "cases": ncases, "steps": nsteps}
+                       "CUDA-graph batch step", "cases": ncases, "steps": nsteps, "ranks": world,
+           "split": "cases split across ranks by cost (cells x longer side, longest first)" if world > 1
+           else "one batch"}
     for name, prec in (("mixed", cap.PREC_MIXED), ("fp64_mg", cap.PREC_FP64_MG), ("fp64", cap.PREC_FP64)):
         cases = pkg.cases.droplet_batch(n_cases=ncases, mixed=True)
         for c in cases:
             c[0].p_precision = prec
-        with pkg.Batch([c[0] for c in cases]) as b:
-            for i, (p, C0, dt) in enumerate(cases):
-                f = pkg.Fields.allocate(p)
-                f.C[...] = C0
-                orc.apply_vof_bc(p, f.C)
-                orc.update_physical_properties(p, f)
-                orc.compute_curvature_and_csf(p, f)
-                b.state_set(i, f)
-            dts = [c[2] for c in cases]
+        mine = shard.plan_params([c[0] for c in cases], world)[rank]
+        sub = [cases[c] for c in mine]
+        with pkg.Batch([c[0] for c in sub]) as b:
+            for i, (p, C0, dt) in enumerate(sub):
+                b.state_set(i, initial_fields(pkg, p, C0))
+            dts = [c[2] for c in sub]
             st, _, _ = b.run_steps(dts, 2, graph=True)
+            barrier(world)
             st, stats, ms = b.run_steps(dts, nsteps, graph=True)
             info = b.info()
         assert st == cap.OK, (name, st)
+        ms = max_over_ranks(ms, world)
+        recs = shard.gather({c: {"poisson_iters": s_["poisson_iters"], "max_relres": s_["max_relres"]}
+                             for c, s_ in zip(mine, stats)}, world)
+        assert sorted(recs) == list(range(ncases))
         out["cells"] = sum(c[0].nx * c[0].ny for c in cases)
         out[name] = {"steps_per_s": 1000.0 * nsteps / ms, "ms_per_step": ms / nsteps,
-                     "poisson_iters_per_step": sum(x["poisson_iters"] for x in stats) / nsteps,
-                     "max_relres": max(x["max_relres"] for x in stats), **info}
+                     "poisson_iters_per_step": sum(x["poisson_iters"] for x in recs.values()) / nsteps,
+                     "max_relres": max(x["max_relres"] for x in recs.values()), **info}
     out["speedup_mixed_vs_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
     out["speedup_mixed_vs_fp64_mg"] = out["mixed"]["steps_per_s"] / out["fp64_mg"]["steps_per_s"]
     return out
@@ -351,11 +371,7 @@ def rt_steps(pkg, orc, nsteps, args):
     cap = pkg.capi
     p, C0, dt = pkg.cases.rt_case(nx=4096, ny=4096, mixed=True)
     p.p_inner_kind = cap.INNER_MG
-    f = pkg.Fields.allocate(p)
-    f.C[...] = C0
-    orc.apply_vof_bc(p, f.C)
-    orc.update_physical_properties(p, f)
-    orc.compute_curvature_and_csf(p, f)
+    f = initial_fields(pkg, p, C0)
     tuned = None
     if not args.no_tune:
         import importlib
@@ -412,10 +428,7 @@ def mono_steps(pkg, orc, n, nsteps, cpu_steps):
     for name, prec in (("block_triangular", cap.PRECOND_BLOCK_TRIANGULAR), ("jacobi", cap.PRECOND_JACOBI)):
         p, dt = pkg.cases.cavity_case(n)
         p.precond = prec
-        f = pkg.Fields.allocate(p)
-        orc.apply_vof_bc(p, f.C)
-        orc.update_physical_properties(p, f)
-        orc.apply_velocity_bc(p, f.u, f.v, False)
+        f = initial_fields(pkg, p, props=True)
         g = f.copy()
         with pkg.Solver(p) as s:
             s.state_set(f)
@@ -453,9 +466,10 @@ def vof_steps(pkg, orc, reps):
         p, C0, dt = pkg.cases.bubble_case(nx=nx, ny=ny, nsub=nsub)
         f = pkg.Fields.allocate(p)
         f.C[...] = C0
-        orc.apply_vof_bc(p, f.C)
         f.u[...], f.v[...] = pkg.cases.random_velocity(p, 0.05, 7)
-        orc.apply_velocity_bc(p, f.u, f.v, False)
+        with pkg.Solver(p) as s0:
+            s0.apply_vof_bc(f)
+            s0.apply_velocity_bc(f)
         inner = f.C[1:-1, 1:-1]
         mixed = int(((inner > 0.0) & (inner < 1.0)).sum())
         T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
@@ -680,6 +694,9 @@ def run_ours(args, world, rank, local):
         except Exception:
             traffic = None
 
+    # the batch leg on every rank (cases split across ranks when N > 1)
+    batch = None if args.skip_steps else batch_steps(pkg, 256, args.batch_steps, rank, world)
+
     line = None
     if rank == 0:
         orc = ge._load_oracle()
@@ -713,7 +730,6 @@ def run_ours(args, world, rank, local):
         arms_out["oracle"] = {"iters": it_ref, "relres": rr_ref, "seconds": t_ref, "threads": nth,
                               "what": "FP64 Jacobi-PCG of the C++ restatement converged to rel-res 1e-13"}
         steps = None if args.skip_steps else sp_steps(pkg, orc, 100, 0 if args.skip_cpu else 3)
-        batch = None if args.skip_steps else batch_steps(pkg, orc, 256, args.batch_steps)
         adjoint = None if args.skip_steps else adjoint_steps(pkg, 512, 3)
         rt = None if (args.skip_steps or args.skip_rt) else rt_steps(pkg, orc, args.rt_steps, args)
         mono = None if args.skip_steps else mono_steps(pkg, orc, 256, 5, 0 if args.skip_cpu else 2)

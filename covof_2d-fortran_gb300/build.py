@@ -48,19 +48,27 @@ def _stale(target: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile (if needed) and return the path of libcovof_gpu.so."""
+CHECKED_DIR = PKG / "_build_checked"
+
+
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> Path:
+    """Compile (if needed) and return the path of libcovof_gpu.so.
+    checked: the bounds-check build (-DCOVOF_CHECKED) into _build_checked/,
+    for tests that run the parity cases with every stencil index checked."""
     nvcc = _nvcc()
-    OUT_DIR.mkdir(exist_ok=True)
+    out_dir = CHECKED_DIR if checked else OUT_DIR
+    lib = out_dir / "libcovof_gpu.so"
+    flags = NVCC_FLAGS + (["-DCOVOF_CHECKED"] if checked else [])
+    out_dir.mkdir(exist_ok=True)
     headers = sorted(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "covof_gpu.h"]
     objs = []
     jobs = []
     for src in SOURCES:
         s = CSRC / src
-        o = OUT_DIR / (s.stem + ".o")
+        o = out_dir / (s.stem + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc] + NVCC_FLAGS + ["-c", str(s), "-o", str(o)])
+            jobs.append([nvcc] + flags + ["-c", str(s), "-o", str(o)])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -72,10 +80,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(run, jobs))
-    if force or jobs or _stale(LIB, objs):
-        run([nvcc] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs] + ["-lcudart"])
-    return LIB
+    if force or jobs or _stale(lib, objs):
+        run([nvcc] + ARCH + ["-shared", "-o", str(lib)] + [str(o) for o in objs] + ["-lcudart"])
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, checked="--checked" in sys.argv))

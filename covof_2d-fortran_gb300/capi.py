@@ -11,6 +11,8 @@ from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "_build" / "libcovof_gpu.so"
+# the bounds-check build (build.py: checked=True) for runs that ask for it
+CHECKED_LIB_PATH = PKG / "_build_checked" / "libcovof_gpu.so"
 
 # status codes (include/covof_gpu.h)
 OK, MAXITER, BREAKDOWN, NAN, TIMEOUT, UNSUPPORTED, CUDA_ERROR, INVALID, TOO_LARGE = range(9)
@@ -114,6 +116,8 @@ _SIGS = {
     "covof_create": [C.POINTER(Params), C.POINTER(C.c_void_p)],
     "covof_destroy": [_VP],
     "covof_abi_version": [],
+    "covof_set_wait_budget": [C.c_longlong],
+    "covof_bounds_check": [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
     "covof_device_info": [_VP, _IP, _IP],
     "covof_get_stream": [_VP, C.POINTER(C.c_void_p)],
     "covof_last_solve_ms": [_VP, _DP],
@@ -130,6 +134,7 @@ _SIGS = {
     "covof_poisson_solve_rhs": [_VP, C.c_double] + [_VP] * 4 + [_IP, _DP],
     "covof_poisson_solve_rhs_dev": [_VP, C.c_double] + [_VP] * 4 + [_IP, _DP],
     "covof_poisson_apply": [_VP, C.c_double] + [_VP] * 4,
+    "covof_poisson_apply_dev": [_VP, C.c_double] + [_VP] * 4,
     "covof_project_correct": [_VP, C.c_double] + [_VP] * 5,
     "covof_vof_reconstruct": [_VP, _VP, _VP],
     "covof_vof_reconstruct_dev": [_VP, _VP, _VP],
@@ -144,6 +149,8 @@ _SIGS = {
     "covof_poisson_solve_rhs_static_dev": [C.POINTER(Params), C.c_double] + [_VP] * 4 + [_IP, _DP],
     "covof_update_physical_properties": [_VP] + [_VP] * 6,
     "covof_compute_curvature_and_csf": [_VP] + [_VP] * 4,
+    "covof_apply_velocity_bc": [_VP, _VP, _VP],
+    "covof_apply_vof_bc": [_VP, _VP],
     "covof_state_set": [_VP, C.c_int, _VP],
     "covof_state_get": [_VP, C.c_int, _VP],
     "covof_state_field_dev": [_VP, C.c_int, C.POINTER(C.c_void_p)],
@@ -177,6 +184,8 @@ def load_library(path: Path | str | None = None):
     global _lib
     if _lib is not None:
         return _lib
+    if path is None and os.environ.get("COVOF_GPU_CHECKED") == "1":
+        path = CHECKED_LIB_PATH
     p = Path(path) if path else LIB_PATH
     if not p.exists():
         raise ImportError(

@@ -96,3 +96,5 @@ __global__ void k_sum_final(const double* __restrict__ part, int n, double* __re
 }
 
 }  // namespace covof
+
+COVOF_UNIT_HOOKS(adjoint)

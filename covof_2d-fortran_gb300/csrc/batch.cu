@@ -604,3 +604,5 @@ int covof_batch_run_steps(covof_batch* b, const double* dt, int nsteps, int flag
 }
 
 }  // extern "C"
+
+COVOF_UNIT_HOOKS(batch)

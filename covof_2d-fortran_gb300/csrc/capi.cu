@@ -1289,6 +1289,35 @@ void covof_params_default(covof_params* p, int nx, int ny, double lx, double ly)
 
 int covof_abi_version(void) { return COVOF_ABI_VERSION; }
 
+int covof_bounds_check(long long* bad, long long* first) {
+  if (!bad || !first) return COVOF_INVALID;
+  int (*const get[])(unsigned long long*, unsigned long long*) = {
+      bounds_check_poisson, bounds_check_momentum, bounds_check_vof, bounds_check_svof,
+      bounds_check_adjoint, bounds_check_output, bounds_check_precond, bounds_check_peak,
+      bounds_check_batch, bounds_check_capi, bounds_check_static_scratch};
+  *bad = 0;
+  *first = 0;
+  for (auto f : get) {
+    unsigned long long c = 0, w = 0;
+    const int st = f(&c, &w);
+    if (st != COVOF_OK) return st;  // COVOF_UNSUPPORTED: not a checked build
+    if (c && !*first) *first = (long long)w;
+    *bad += (long long)c;
+  }
+  return COVOF_OK;
+}
+
+int covof_set_wait_budget(long long polls) {
+  if (polls < 0) return COVOF_INVALID;
+  const long long v = polls == 0 ? kSpinLimit : polls;
+  int (*const set[])(long long) = {set_wait_budget_poisson, set_wait_budget_momentum, set_wait_budget_vof,
+                                    set_wait_budget_svof, set_wait_budget_adjoint, set_wait_budget_output,
+                                    set_wait_budget_precond, set_wait_budget_peak, set_wait_budget_batch,
+                                    set_wait_budget_capi, set_wait_budget_static_scratch};
+  for (auto f : set) CS(f(v));
+  return COVOF_OK;
+}
+
 const char* covof_strerror(int s) {
   switch (s) {
     case COVOF_OK: return "ok";
@@ -1449,27 +1478,43 @@ int covof_poisson_solve_rhs(covof_handle* h, double dt, const double* b, const d
   return st;
 }
 
+// y = A x on device arrays: assembly from rho_u, rho_v, the operand's
+// interior into a solver vector with a zero ghost ring (as inside the
+// solvers), then the stencil; y's interior written.
+int poisson_apply_enqueue(covof_handle* h, double dt, const double* rho_u, const double* rho_v, const double* x,
+                          double* y) {
+  CS(ensure_poisson(h));
+  const covof_params& P = h->prm;
+  const size_t g = h->g;
+  const dim3 blk(32, 8), grd = grid2(P.nx, P.ny, blk);
+  // only the coefficients are used: the right-hand side slot reads y
+  k_poisson_assemble<<<grd, blk, 0, h->stream>>>(h->D, dt, P.dx, P.dy, wall_flags(P), rho_u, rho_v,
+                                                  nullptr, nullptr, y, 0, h->pax, h->pay, h->paP,
+                                                  h->pb, nullptr, nullptr);
+  CK(cudaMemsetAsync(h->px, 0, g * sizeof(double), h->stream));
+  k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, x, h->px, 0);
+  k_poisson_apply<<<grd, blk, 0, h->stream>>>(h->D, h->px, y, h->pax, h->pay, h->paP);
+  CK(cudaGetLastError());
+  return COVOF_OK;
+}
+
 int covof_poisson_apply(covof_handle* h, double dt, const double* rho_u, const double* rho_v,
                         const double* x, double* y) {
   if (!h || !rho_u || !rho_v || !x || !y) return COVOF_INVALID;
   CS(ensure_fields(h));
-  CS(ensure_poisson(h));
-  const covof_params& P = h->prm;
   const size_t g = h->g;
   CS(h2d(h, h->f_rho_u, rho_u, g)); CS(h2d(h, h->f_rho_v, rho_v, g));
   CS(h2d(h, h->f_p, x, g)); CS(h2d(h, h->f_b, y, g));
-  const dim3 blk(32, 8), grd = grid2(P.nx, P.ny, blk);
-  // b is irrelevant here: assemble from a zero velocity (u = v = rho arrays
-  // would do as well; only the coefficients are used).
-  k_poisson_assemble<<<grd, blk, 0, h->stream>>>(h->D, dt, P.dx, P.dy, wall_flags(P), h->f_rho_u, h->f_rho_v,
-                                                  nullptr, nullptr, h->f_b, 0, h->pax, h->pay, h->paP,
-                                                  h->pb, nullptr, nullptr);
-  // operand with a zero ghost ring, as inside the solver
-  CK(cudaMemsetAsync(h->px, 0, g * sizeof(double), h->stream));
-  k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, h->f_p, h->px, 0);
-  k_poisson_apply<<<grd, blk, 0, h->stream>>>(h->D, h->px, h->f_b, h->pax, h->pay, h->paP);
-  CK(cudaGetLastError());
+  CS(poisson_apply_enqueue(h, dt, h->f_rho_u, h->f_rho_v, h->f_p, h->f_b));
   CS(d2h(h, y, h->f_b, g));
+  CS(sync(h));
+  return COVOF_OK;
+}
+
+int covof_poisson_apply_dev(covof_handle* h, double dt, const double* rho_u, const double* rho_v,
+                            const double* x, double* y) {
+  if (!h || !rho_u || !rho_v || !x || !y) return COVOF_INVALID;
+  CS(poisson_apply_enqueue(h, dt, rho_u, rho_v, x, y));
   CS(sync(h));
   return COVOF_OK;
 }
@@ -1825,6 +1870,27 @@ int covof_update_physical_properties(covof_handle* h, double* C, double* rho, do
   return sync(h);
 }
 
+int covof_apply_velocity_bc(covof_handle* h, double* u, double* v) {
+  if (!h || !u || !v) return COVOF_INVALID;
+  CS(ensure_fields(h));
+  const size_t g = h->g;
+  CS(h2d(h, h->f_u, u, g)); CS(h2d(h, h->f_v, v, g));
+  CS(velocity_bc_dev(h, h->f_u, h->f_v));
+  CS(d2h(h, u, h->f_u, g)); CS(d2h(h, v, h->f_v, g));
+  return sync(h);
+}
+
+int covof_apply_vof_bc(covof_handle* h, double* C) {
+  if (!h || !C) return COVOF_INVALID;
+  CS(ensure_fields(h));
+  const size_t g = h->g;
+  CS(h2d(h, h->f_C, C, g));
+  k_vof_bc<<<(h->D.nx + h->D.ny + 127) / 128, 128, 0, h->stream>>>(h->D, h->f_C);
+  CK(cudaGetLastError());
+  CS(d2h(h, C, h->f_C, g));
+  return sync(h);
+}
+
 int covof_compute_curvature_and_csf(covof_handle* h, const double* C, double* fx_sigma,
                                     double* fy_sigma, double* curvature) {
   if (!h) return COVOF_INVALID;
@@ -1922,3 +1988,5 @@ int covof_run_steps(covof_handle* h, double dt, int nsteps, int flags, covof_run
 }
 
 }  // extern "C"
+
+COVOF_UNIT_HOOKS(capi)

@@ -16,9 +16,48 @@ namespace covof {
 // COVOF_TIMEOUT; the first writer wins.
 __device__ __forceinline__ void set_error(int* err, int code) { atomicCAS(err, 0, code); }
 
+// ---------------------------------------------------------------------------
+// Bounds-check build (-DCOVOF_CHECKED): every cell index formed on the device
+// through Dims::id and every stencil centre of the operators is checked
+// against the (nx+2) x (ny+2) ghosted extents.  A bad index is counted, the
+// first one recorded (site << 40 | index + 2^39), and the access redirected to
+// a valid element instead of leaving the array; covof_bounds_check reads and
+// clears the record.  One record per translation unit (no relocatable device
+// code); COVOF_UNIT_HOOKS gives each unit its reader.  The normal build
+// compiles every check away.
+#ifdef COVOF_CHECKED
+static __device__ unsigned long long g_oob_count = 0;
+static __device__ unsigned long long g_oob_first = 0;
+static __device__ __noinline__ void oob_record(int site, long long index) {
+  if (atomicAdd(&g_oob_count, 1ULL) == 0ULL)
+    g_oob_first = ((unsigned long long)site << 40) | (unsigned long long)(index + (1LL << 39));
+}
+#endif
+
 struct Dims {
   int nx, ny, P;  // P = nx + 2
-  __host__ __device__ __forceinline__ int id(int i, int j) const { return j * P + i; }
+  __host__ __device__ __forceinline__ int id(int i, int j) const {
+#if defined(COVOF_CHECKED) && defined(__CUDA_ARCH__)
+    if (i < 0 || i > nx + 1 || j < 0 || j > ny + 1) {
+      oob_record(1, (long long)j * P + i);
+      return 0;
+    }
+#endif
+    return j * P + i;
+  }
+  // the 3 x 3 neighbourhood of cell k lies inside the ghosted array (checked
+  // builds: else recorded under site and an interior cell returned)
+  __device__ __forceinline__ int nbhd(int k, int site) const {
+#ifdef COVOF_CHECKED
+    if (k - P - 1 < 0 || (long long)k + P + 1 >= (long long)P * (ny + 2)) {
+      oob_record(site, k);
+      return P + 1;
+    }
+#else
+    (void)site;
+#endif
+    return k;
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -27,11 +66,43 @@ struct Dims {
 // thread 0 of every block adds 1 with release semantics to one counter and
 // polls it with acquire loads until it reaches (epoch+1) * nblocks; no reset
 // and no second word, so the critical path is one atomic and one poll.
-// Every spin is bounded: after kSpinLimit polls (~1-2 s) the block records
-// COVOF_TIMEOUT and returns false, and every caller leaves its loop; a block
-// that left never arrives again, so every other block times out at its next
-// barrier and no block can wait forever.  The counter must be zero at launch.
+// Every spin is bounded: after g_spin_limit polls (kSpinLimit, ~1-2 s,
+// unless covof_set_wait_budget lowered it) the block records COVOF_TIMEOUT and
+// returns false, and every caller leaves its loop; a block that left never
+// arrives again, so every other block times out at its next barrier and no
+// block can wait forever.  The counter must be zero at launch.
 constexpr long long kSpinLimit = 1LL << 21;
+// One copy per translation unit (the library is built without relocatable
+// device code); COVOF_UNIT_HOOKS gives each unit its setter, and
+// covof_set_wait_budget calls them all.
+static __device__ long long g_spin_limit = kSpinLimit;
+#ifdef COVOF_CHECKED
+#define COVOF_BOUNDS_READER(unit)                                                                   \
+  int bounds_check_##unit(unsigned long long* count, unsigned long long* first) {                   \
+    const unsigned long long zero = 0;                                                             \
+    if (cudaMemcpyFromSymbol(count, g_oob_count, sizeof(*count)) != cudaSuccess ||                 \
+        cudaMemcpyFromSymbol(first, g_oob_first, sizeof(*first)) != cudaSuccess ||                 \
+        cudaMemcpyToSymbol(g_oob_count, &zero, sizeof(zero)) != cudaSuccess ||                     \
+        cudaMemcpyToSymbol(g_oob_first, &zero, sizeof(zero)) != cudaSuccess)                       \
+      return 6;                                                                                    \
+    return 0;                                                                                      \
+  }
+#else
+#define COVOF_BOUNDS_READER(unit)                                                      \
+  int bounds_check_##unit(unsigned long long* count, unsigned long long* first) {      \
+    *count = 0;                                                                       \
+    *first = 0;                                                                       \
+    return 5;                                                                         \
+  }
+#endif
+// Per-unit hooks: the wait budget setter and the bounds record reader.
+#define COVOF_UNIT_HOOKS(unit)                                                            \
+  namespace covof {                                                                      \
+  int set_wait_budget_##unit(long long polls) {                                          \
+    return cudaMemcpyToSymbol(g_spin_limit, &polls, sizeof(polls)) == cudaSuccess ? 0 : 6; \
+  }                                                                                      \
+  COVOF_BOUNDS_READER(unit)                                                              \
+  }
 
 __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
   unsigned int v;
@@ -51,7 +122,7 @@ __device__ __forceinline__ bool warp_wait_ge(const unsigned int* p, unsigned int
   if ((threadIdx.x & 31) == 0) {
     long long spins = 0;
     while ((int)(ld_acquire_u32(p) - need) < 0) {
-      if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+      if (++spins > g_spin_limit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
     }
   }
   return __shfl_sync(0xffffffffu, ok, 0) != 0;
@@ -83,7 +154,7 @@ struct GridSync {
       const unsigned int target = (epoch + 1u) * nblocks;
       long long spins = 0;
       while ((int)(ld_acquire_u32(count) - target) < 0) {
-        if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+        if (++spins > g_spin_limit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
       }
       s_ok = ok;
     }

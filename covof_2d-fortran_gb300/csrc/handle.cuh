@@ -11,6 +11,31 @@
 #include "adjoint.cuh"
 
 namespace covof {
+// the bounded waits' poll budget of each translation unit (common.cuh)
+int set_wait_budget_poisson(long long);
+int set_wait_budget_momentum(long long);
+int set_wait_budget_vof(long long);
+int set_wait_budget_svof(long long);
+int set_wait_budget_adjoint(long long);
+int set_wait_budget_output(long long);
+int set_wait_budget_precond(long long);
+int set_wait_budget_peak(long long);
+int set_wait_budget_batch(long long);
+int set_wait_budget_capi(long long);
+int set_wait_budget_static_scratch(long long);
+// the bounds-check record of each translation unit (common.cuh)
+int bounds_check_poisson(unsigned long long*, unsigned long long*);
+int bounds_check_momentum(unsigned long long*, unsigned long long*);
+int bounds_check_vof(unsigned long long*, unsigned long long*);
+int bounds_check_svof(unsigned long long*, unsigned long long*);
+int bounds_check_adjoint(unsigned long long*, unsigned long long*);
+int bounds_check_output(unsigned long long*, unsigned long long*);
+int bounds_check_precond(unsigned long long*, unsigned long long*);
+int bounds_check_peak(unsigned long long*, unsigned long long*);
+int bounds_check_batch(unsigned long long*, unsigned long long*);
+int bounds_check_capi(unsigned long long*, unsigned long long*);
+int bounds_check_static_scratch(unsigned long long*, unsigned long long*);
+
 namespace host {
 
 constexpr int kPoissonThreads = 1024;  // one cell per thread per 1024-cell tile

@@ -747,6 +747,8 @@ __device__ __forceinline__ double pa_at(const MomArgs& a, const DofWalker& W, in
   double y = cf[k] * __ldcg(x + k);
   const bool wall_row = part == 0 ? (i == 1 || i == D.nx + 1)
                                   : ((j == 1 && is_wall(a, SB)) || (j == D.ny + 1 && is_wall(a, ST)));
+  // checked builds: a row that reads neighbours has its neighbourhood in its block
+  if (!wall_row && D.nbhd(k - part * W.g, 7) != k - part * W.g) return 0.0;
   if (!wall_row) {
     const int P = D.P;
     const int o = part == 0 ? W.g : -W.g;  // offset of the other component's block
@@ -1342,3 +1344,5 @@ __global__ void k_al_divmax(AlArgs a) {
 }
 
 }  // namespace covof
+
+COVOF_UNIT_HOOKS(momentum)

@@ -332,3 +332,5 @@ int covof_history_write_async(covof_handle* h, const char* dir, const char* case
 }
 
 }  // extern "C"
+
+COVOF_UNIT_HOOKS(output)

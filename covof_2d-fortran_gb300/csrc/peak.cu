@@ -50,3 +50,5 @@ int covof_fp64_peak(covof_handle* h, double* gflops) {
   *gflops = flops / (ms * 1.0e-3) / 1.0e9;
   return COVOF_OK;
 }
+
+COVOF_UNIT_HOOKS(peak)

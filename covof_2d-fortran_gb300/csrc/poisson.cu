@@ -118,6 +118,7 @@ __device__ __forceinline__ double stencil_exact(const Dims& D, int k, const doub
                                                 const double* __restrict__ ax,
                                                 const double* __restrict__ ay,
                                                 const double* __restrict__ aP) {
+  k = D.nbhd(k, 2);
   double val = __dmul_rn(aP[k], x[k]);
   val = __dsub_rn(val, __dmul_rn(ax[k], x[k - 1]));
   val = __dsub_rn(val, __dmul_rn(ax[k + 1], x[k + 1]));
@@ -207,7 +208,7 @@ __device__ __forceinline__ T phase_stencil(const Dims& D, const Tiles& tl, int t
   const int i = tx0 + lx + 1, j = ty0 + ly + 1;
   T contrib = T(0);
   if (i <= D.nx && j <= D.ny) {
-    const int k = D.id(i, j);
+    const int k = D.nbhd(D.id(i, j), 6);
     const int c = (ly + 1) * HX + (lx + 1);
     const T dc = sd[c];
     T v = UNIT ? dc : S.aP[k] * dc;
@@ -244,7 +245,7 @@ __device__ PcgOut pcg_tiled(const Dims& D, const Tiles& tl, const Team& tm, Grid
     const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
     const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
     if (i <= D.nx && j <= D.ny) {
-      const int k = D.id(i, j);
+      const int k = D.nbhd(D.id(i, j), 5);
       T rv = S.b[k];
       if (!x_zero) {
         const T xc = __ldcg(S.x + k);
@@ -275,13 +276,16 @@ __device__ PcgOut pcg_tiled(const Dims& D, const Tiles& tl, const Team& tm, Grid
       rz_old = t[2];
       out[0] = b_norm;
       out[1] = rn;
-      out[2] = (rn / b_norm > rel) ? 0.0 : 1.0;
+      // 2: a NaN in b or x (the reference's loop test is false for NaN and
+      // it returns silently; here the status says so)
+      out[2] = isnan(rn) ? 2.0 : ((rn / b_norm > rel) ? 0.0 : 1.0);
     });
   }
   o.b_norm = sc[0];
   o.r_norm = sc[1];
   if (!o.ok || sc[2] != 0.0) {
     if (!o.ok) o.status = COVOF_TIMEOUT;
+    else if (sc[2] == 2.0) o.status = COVOF_NAN;
     return o;
   }
   double beta = 0.0;
@@ -413,6 +417,7 @@ __device__ __forceinline__ double stencil64(const Dims& D, int k, const double* 
                                             const double* __restrict__ ax,
                                             const double* __restrict__ ay,
                                             const double* __restrict__ aP) {
+  k = D.nbhd(k, 3);
   double v = aP[k] * __ldcg(x + k);
   v = fma(-ax[k], __ldcg(x + k - 1), v);
   v = fma(-ax[k + 1], __ldcg(x + k + 1), v);
@@ -460,6 +465,7 @@ struct StripOwn {
                                             const double* __restrict__ ax, const double* __restrict__ ay,
                                             const double* __restrict__ aP) const {
     const int P = D.P;
+    k = D.nbhd(k, 4);
     const double xs = c < D.nx ? __ldcg(x + k - P) : x[k - P];
     const double xn = c >= (R - 1) * D.nx ? __ldcg(x + k + P) : x[k + P];
     double v = aP[k] * x[k];
@@ -706,10 +712,10 @@ struct SmemCheby {
       long long spins = 0;
       if (b > 0)
         while ((int)(ld_acquire_u32(flags + b - 1) - want) < 0)
-          if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+          if (++spins > g_spin_limit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
       if (ok && b < G - 1)
         while ((int)(ld_acquire_u32(flags + b + 1) - want) < 0)
-          if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+          if (++spins > g_spin_limit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
       s_ok = ok;
     }
     __syncthreads();
@@ -1057,10 +1063,10 @@ struct StreamCheby {
       long long spins = 0;
       if (b > 0)
         while ((int)(ld_acquire_u32(flags + b - 1) - want) < 0)
-          if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+          if (++spins > g_spin_limit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
       if (ok && b < G - 1)
         while ((int)(ld_acquire_u32(flags + b + 1) - want) < 0)
-          if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+          if (++spins > g_spin_limit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
       s_ok = ok;
     }
     __syncthreads();
@@ -1239,7 +1245,7 @@ struct ClusterCheby {
       const unsigned target = (epoch + 1u) * (unsigned)G;
       long long spins = 0;
       while ((int)(ld_cluster_acquire_u32(bar0) - target) < 0)
-        if (++spins > kSpinLimit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
+        if (++spins > g_spin_limit) { set_error(err, COVOF_TIMEOUT); ok = 0; break; }
       s_ok = ok;
     }
     ++epoch;
@@ -1429,6 +1435,7 @@ struct MgInnerT {
   }
   template <bool S>
   __device__ __forceinline__ static T apply(const MgLvT<T>& L, const T* x, int k) {
+    k = Dims{L.nx, L.ny, L.P}.nbhd(k, 8);
     T v = L.dg[k] * ld<S>(x + k);
     v = fmad_(-L.ax[k], ld<S>(x + k - 1), v);
     v = fmad_(-L.ax[k + 1], ld<S>(x + k + 1), v);
@@ -2239,3 +2246,5 @@ __global__ void __launch_bounds__(256) k_pin_final(Dims D, const double* __restr
 }
 
 }  // namespace covof
+
+COVOF_UNIT_HOOKS(poisson)

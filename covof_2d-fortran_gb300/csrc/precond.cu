@@ -724,7 +724,9 @@ int pcg_sgs(covof_handle* h, const PoissonArgs& a) {
   double r_norm = sqrt(t[1]);
   int iters = 0, status = COVOF_OK;
   bool converged = false;
-  if (r_norm / b_norm > a.tol) {
+  if (r_norm != r_norm) {
+    status = COVOF_NAN;  // a NaN in b or x
+  } else if (r_norm / b_norm > a.tol) {
     CS(launch_ssor(h, &J, 1));
     vop(kCopy, d, z, nullptr, 0.0);
     CS(read_dots(h, g, {{r, z}}, t));
@@ -763,3 +765,5 @@ int pcg_sgs(covof_handle* h, const PoissonArgs& a) {
 
 }  // namespace host
 }  // namespace covof
+
+COVOF_UNIT_HOOKS(precond)

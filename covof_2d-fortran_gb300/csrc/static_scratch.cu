@@ -125,3 +125,5 @@ extern "C" int covof_poisson_solve_rhs_static_dev(const covof_params* prm, doubl
   if (relres) *relres = h.relres;
   return h.status;
 }
+
+COVOF_UNIT_HOOKS(static_scratch)

@@ -214,3 +214,5 @@ __global__ void k_diffusion_ghosts(Dims D, double* __restrict__ Ct) {
 }
 
 }  // namespace covof
+
+COVOF_UNIT_HOOKS(svof)

@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(128) k_vof_mixed(VofArgs a, const int* __restr
   const double* __restrict__ C = a.C;
   const double dx = a.dx, dy = a.dy;
   for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += nwarps) {
-    const int k = list[e];
+    const int k = a.D.nbhd(list[e], 22);  // checked builds: a listed cell outside the interior
     const int j = k / a.D.P, i = k - j * a.D.P;
     const double c = C[k];
     const double xmin = m.xf(i), xmax = m.xf(i + 1), ymin = m.yf(j), ymax = m.yf(j + 1);
@@ -332,6 +332,7 @@ __global__ void k_vof_pass(VofArgs a, int dir, int clamp, const double* __restri
   if (i > nx + 1 || j > ny + 1) return;
   const int k = a.D.id(i, j);
   if (i < 1 || i > nx || j < 1 || j > ny) { Cout[k] = Cin[k]; return; }
+  if (a.D.nbhd(k, 20) != k) return;  // checked builds: a neighbourhood outside the array
   const double area = a.dx * a.dy;
   const double cd = a.Cn[k] >= 0.5 ? 1.0 : 0.0;
   double c;
@@ -360,6 +361,7 @@ __global__ void k_ciam_pass(VofArgs a, int dir, const double* __restrict__ Cin, 
   if (i > nx + 1 || j > ny + 1) return;
   const int k = a.D.id(i, j);
   if (i < 1 || i > nx || j < 1 || j > ny) { Cout[k] = Cin[k]; return; }
+  if (a.D.nbhd(k, 20) != k) return;  // checked builds: a neighbourhood outside the array
   double c;
   if (dir == 0) {
     const double fw = x_flux(m, a.seg, a.u, a.dt, i, j);
@@ -431,6 +433,7 @@ __global__ void k_tvd_advect(VofArgs a, int lim, const double* __restrict__ Cin,
   if (i > nx + 1 || j > ny + 1) return;
   const int k = a.D.id(i, j);
   if (i < 1 || i > nx || j < 1 || j > ny) { Cout[k] = Cin[k]; return; }
+  if (a.D.nbhd(k, 20) != k) return;  // checked builds: a neighbourhood outside the array
   const double fw = tvd_face_flux(lim, a.u[k], a.dt, a.dx, Cin, k, 1, i, nx + 1);
   const double fe = tvd_face_flux(lim, a.u[k + 1], a.dt, a.dx, Cin, k + 1, 1, i + 1, nx + 1);
   const double fs = tvd_face_flux(lim, a.v[k], a.dt, a.dy, Cin, k, P, j, ny + 1);
@@ -513,6 +516,7 @@ __global__ void k_csf_normals(CsfArgs a) {
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (i > a.D.nx || j > a.D.ny) return;
   const int k = a.D.id(i, j);
+  if (a.D.nbhd(k, 21) != k) return;  // checked builds
   const double dcx = (a.N[k + 1] - a.N[k - 1]) / (2.0 * a.dx);
   const double dcy = (a.N[k + a.D.P] - a.N[k - a.D.P]) / (2.0 * a.dy);
   const double gm = sqrt(dcx * dcx + dcy * dcy);
@@ -527,6 +531,7 @@ __global__ void k_csf_kappa(CsfArgs a) {
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (i > a.D.nx || j > a.D.ny) return;
   const int k = a.D.id(i, j);
+  if (a.D.nbhd(k, 21) != k) return;  // checked builds
   double kap = 0.0;
   if (a.nxv[k] != 0.0 || a.nyv[k] != 0.0)
     kap = -((a.nxv[k + 1] - a.nxv[k - 1]) / (2.0 * a.dx) + (a.nyv[k + a.D.P] - a.nyv[k - a.D.P]) / (2.0 * a.dy));
@@ -554,3 +559,5 @@ __global__ void k_csf_force(CsfArgs a) {
 }
 
 }  // namespace covof
+
+COVOF_UNIT_HOOKS(vof)

@@ -355,6 +355,14 @@ class Solver:
         self._check(self.lib.covof_diffusion_smooth(self.h, _ptr(f.C), _ptr(f.C_tilde)),
                     "covof_diffusion_smooth")
 
+    def apply_velocity_bc(self, f: Fields):
+        """apply_velocity_bc (src/module_mpi_comm.f90:290-537): ghosts of f.u, f.v."""
+        self._check(self.lib.covof_apply_velocity_bc(self.h, _ptr(f.u), _ptr(f.v)), "covof_apply_velocity_bc")
+
+    def apply_vof_bc(self, f: Fields):
+        """apply_vof_bc (src/module_mpi_comm.f90:636-683): ghosts of f.C."""
+        self._check(self.lib.covof_apply_vof_bc(self.h, _ptr(f.C)), "covof_apply_vof_bc")
+
     def update_physical_properties(self, f: Fields):
         self._smoothed(f, upload=True)
         st = self.lib.covof_update_physical_properties(self.h, _ptr(f.C), _ptr(f.rho), _ptr(f.rho_u),

@@ -195,6 +195,22 @@ int covof_create(const covof_params* params, covof_handle** out);
 int covof_destroy(covof_handle* h);
 const char* covof_strerror(int status);
 int covof_abi_version(void);
+/* Failure-detection hook (no reference counterpart): the number of polls
+ * every bounded device-side wait (grid and team barriers, neighbour
+ * counters, wavefront progress) makes before it gives up, records
+ * COVOF_TIMEOUT and returns; 0 restores the default of 2^21 polls (about a
+ * second).  A test lowers it to make waits run out -- the solve returns
+ * COVOF_TIMEOUT, no GPU fault -- and restores it; the handle stays usable.
+ * Applies to the current device; set it while no kernel of this library runs. */
+int covof_set_wait_budget(long long polls);
+/* Bounds-check build (no reference counterpart): in a library compiled with
+ * -DCOVOF_CHECKED every cell index formed on the device and every stencil
+ * centre of the operators is checked against the (nx+2) x (ny+2) ghosted
+ * extents; a bad index is counted, the first recorded, and the access
+ * redirected inside the array.  Returns the count since the last call (bad)
+ * and the first record (first: site << 40 | index + 2^39), then clears them.
+ * The normal build returns COVOF_UNSUPPORTED. */
+int covof_bounds_check(long long* bad, long long* first);
 /* Device the handle was created on and the number of SMs it uses. */
 int covof_device_info(const covof_handle* h, int* device, int* sm_count);
 
@@ -275,6 +291,8 @@ int covof_project_correct(covof_handle* h, double dt, double* u, double* v, cons
  * operator (src/module_simulation.f90:2668-2707). */
 int covof_poisson_apply(covof_handle* h, double dt, const double* rho_u, const double* rho_v,
                         const double* x, double* y);
+int covof_poisson_apply_dev(covof_handle* h, double dt, const double* rho_u, const double* rho_v,
+                            const double* x, double* y);
 
 /* The handle's CUDA stream (a blocking stream: it orders after work on the
  * legacy default stream) and the device time of the last Poisson solve
@@ -369,6 +387,13 @@ int covof_diffusion_smooth(covof_handle* h, const double* C, double* C_tilde);
  * properties and mu_node follow the resident C_s. */
 int covof_update_physical_properties(covof_handle* h, double* C, double* rho, double* rho_u,
                                      double* rho_v, double* mu, double* mu_node);
+/* apply_velocity_bc (src/module_mpi_comm.f90:290-537, one rank, constant
+ * wall values bc_u / bc_v): the ghost values of u and v for the boundary
+ * types of the parameter block; interior faces untouched. */
+int covof_apply_velocity_bc(covof_handle* h, double* u, double* v);
+/* apply_vof_bc (src/module_mpi_comm.f90:636-683, one rank): the ghost values
+ * of C (zero gradient at walls). */
+int covof_apply_vof_bc(covof_handle* h, double* C);
 /* compute_curvature_and_csf (src/module_interface_vof.f90:627-789); the
  * normals come from the resident C_tilde (diffusion smoothing) or C_s (SVOF)
  * when those are enabled. */

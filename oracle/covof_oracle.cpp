@@ -448,7 +448,8 @@ int poisson_pcg_par(const covof_params* prm, Poisson& P, std::vector<double>& x,
     double rn = std::sqrt(s3[1]), rz_old = s3[2];
     int it_local = 0, st_local = COVOF_OK;
     bool converged = false;
-    if (fixed_iters > 0 || rn / bn > tol) {
+    if (std::isnan(rn)) st_local = COVOF_NAN;
+    else if (fixed_iters > 0 || rn / bn > tol) {
 #pragma omp barrier
       for (int it = 1; it <= max_iter; ++it) {
         it_local = it;
@@ -533,7 +534,10 @@ int poisson_pcg(const covof_params* prm, Poisson& P, std::vector<double>& x, int
   double r_norm = std::sqrt(DOT(r.data(), r.data()));
   int iters = 0, status = COVOF_OK;
   bool converged = false;
-  if (fixed_iters > 0 || r_norm / b_norm > tol) {
+  // a NaN in b or x: the reference's loop test (r_norm / b_norm > tol) is
+  // false and it returns silently; the status says so here
+  if (std::isnan(r_norm)) status = COVOF_NAN;
+  else if (fixed_iters > 0 || r_norm / b_norm > tol) {
     PREC(r.data(), z.data());
     d = z;
     double rz_old = DOT(r.data(), z.data());

@@ -15,6 +15,23 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built library")
 
 
+def pytest_sessionfinish(session, exitstatus):
+    """A run under the bounds-check build (COVOF_GPU_CHECKED=1) writes the
+    library's out-of-range record to COVOF_CHECKED_REPORT at the end."""
+    import os
+    out = os.environ.get("COVOF_CHECKED_REPORT")
+    if not out:
+        return
+    import ctypes
+    import json
+    import __graft_entry__ as ge
+    lib = ge.load_package().capi.load_library()
+    bad, first = ctypes.c_longlong(), ctypes.c_longlong()
+    st = lib.covof_bounds_check(ctypes.byref(bad), ctypes.byref(first))
+    Path(out).write_text(json.dumps({"status": st, "bad": bad.value, "first": first.value,
+                                     "exitstatus": int(exitstatus)}))
+
+
 @pytest.fixture(scope="session")
 def pkg():
     import __graft_entry__ as ge

@@ -107,3 +107,47 @@ def test_batch_rejects_mixed_inner_kinds(gpu_pkg, orc):
     ps[1].p_inner_kind = pkg.capi.INNER_CHEBYSHEV
     with pytest.raises(pkg.CovofError):
         pkg.Batch(ps)
+
+
+def test_sharded_sub_batches_match_the_whole_batch(gpu_pkg, orc):
+    """The multi-GPU split (shard.plan) run as its two sub-batches one after
+    the other on this GPU: every case is stepped exactly once, and each
+    case's fields match those of the single batch holding all cases within
+    the Krylov bars (the sub-batches' team sizes differ from the whole
+    batch's, so their reductions associate differently)."""
+    import importlib
+    pkg = gpu_pkg
+    shard = importlib.import_module(pkg.__name__ + ".shard")
+    cases = _cases(pkg, orc, True, n=7, seed=13)
+    for p, f, dt in cases:
+        p.p_inner_kind = pkg.capi.INNER_MG
+    nsteps = 2
+
+    def run(idx):
+        out = {}
+        with pkg.Batch([cases[c][0] for c in idx]) as b:
+            for i, c in enumerate(idx):
+                b.state_set(i, cases[c][1])
+            st, stats, _ = b.run_steps([cases[c][2] for c in idx], nsteps, graph=True)
+            assert st == 0, stats
+            for i, c in enumerate(idx):
+                g = cases[c][1].copy()
+                b.state_get(i, g)
+                out[c] = (g, stats[i])
+        return out
+
+    whole = run(list(range(len(cases))))
+    parts = shard.plan_params([c[0] for c in cases], 2)
+    assert all(len(x) > 0 for x in parts)
+    merged = {}
+    for part in parts:
+        merged.update(run(part))
+    assert sorted(merged) == list(range(len(cases)))
+    for c, (g, st) in merged.items():
+        assert st["steps"] == nsteps and st["first_bad_step"] == -1
+        r = whole[c][0]
+        for name in ("u", "v", "p"):
+            a, e = getattr(g, name), getattr(r, name)
+            tol = 1e-8 if name == "p" else 1e-9
+            assert np.linalg.norm(a - e) / np.linalg.norm(e) < tol, (c, name)
+        assert np.abs(g.C - r.C).max() <= 1e-12, c

@@ -121,3 +121,29 @@ def test_vortex_period_parity_and_conservation(gpu_pkg, orc):
             k += 1
     assert np.array_equal(g.C, f.C)
     assert worst < 1e-12
+
+
+@pytest.mark.parametrize("walls", ["noslip", "lid_freeslip"])
+def test_boundary_condition_entries_bit_exact(gpu_pkg, orc, walls):
+    """covof_apply_velocity_bc / covof_apply_vof_bc against the oracle's
+    apply_velocity_bc / apply_vof_bc on random interior values."""
+    pkg = gpu_pkg
+    cap = pkg.capi
+    p = pkg.cases.make_params(37, 29, 1.0, 0.8)
+    if walls == "lid_freeslip":
+        p.bc_type[0] = cap.BC_FREESLIP
+        p.bc_u[3] = 1.0
+        p.bc_v[1] = -0.25
+    rng = np.random.default_rng(9)
+    f = pkg.Fields.allocate(p)
+    f.u[...] = rng.standard_normal(f.u.shape)
+    f.v[...] = rng.standard_normal(f.v.shape)
+    f.C[...] = rng.random(f.C.shape)
+    g = f.copy()
+    orc.apply_velocity_bc(p, f.u, f.v, False)
+    orc.apply_vof_bc(p, f.C)
+    with pkg.Solver(p) as s:
+        s.apply_velocity_bc(g)
+        s.apply_vof_bc(g)
+    assert np.array_equal(g.u, f.u) and np.array_equal(g.v, f.v)
+    assert np.array_equal(g.C, f.C)
