@@ -66,10 +66,15 @@ def test_resident_steps_report_timeout_then_continue(gpu_pkg, orc, wait_budget):
     orc.apply_vof_bc(p, f.C)
     orc.update_physical_properties(p, f)
     orc.compute_curvature_and_csf(p, f)
+    import ctypes
     with pkg.Solver(p) as s:
         s.state_set(f)
         assert wait_budget(1) == cap.OK
-        st, stats = s.run_steps(dt, 2, graph=False)
+        raw = cap.RunStats()
+        st = s.lib.covof_run_steps(s.h, dt, 2, 0, ctypes.byref(raw))
+        stats = raw.as_dict()
+        # the call returns the first failing step's status, and both steps ran
+        assert st == cap.TIMEOUT and stats["steps"] == 2, (st, stats)
         assert stats["first_bad_step"] == 0 and stats["first_bad_status"] == cap.TIMEOUT, stats
         assert wait_budget(0) == cap.OK
         s.state_set(f)
