@@ -426,13 +426,6 @@ __device__ __forceinline__ double stencil64(const Dims& D, int k, const double* 
   return v;
 }
 
-// tiles per batch of TileOwn::each_batched (FP64 values: registers are the
-// limit at 1024 threads per SM)
-#ifndef COVOF_OWN_BATCH
-#define COVOF_OWN_BATCH 2
-#endif
-constexpr int kOwnBatch = COVOF_OWN_BATCH;
-
 struct TileOwn {
   Dims D; Tiles tl; Team tm;
   template <typename F>
@@ -446,35 +439,6 @@ struct TileOwn {
   __device__ __forceinline__ double stencil(int k, int, const double* __restrict__ x, const double* __restrict__ ax,
                                             const double* __restrict__ ay, const double* __restrict__ aP) const {
     return stencil64(D, k, x, ax, ay, aP);
-  }
-  // each() in batches of kOwnBatch tiles per thread: value(k, c) for every
-  // cell of a batch, then put(k, c, v) for each (see MgInnerT::cells_batched:
-  // the loads of several cells are in flight together instead of one L2
-  // round trip per cell).
-  template <class V, class Put>
-  __device__ __forceinline__ void each_batched(V value, Put put) const {
-    using R = decltype(value(0, 0));
-    constexpr int U = kOwnBatch;
-    for (int t0 = tm.rank; t0 < tl.ntiles; t0 += U * tm.size) {
-      R v[U];
-      int kk[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int tile = t0 + u * tm.size;
-        kk[u] = -1;
-        if (tile < tl.ntiles) {
-          const int i = (tile % tl.ntx) * tl.TX + (int)(threadIdx.x % tl.TX) + 1;
-          const int j = (tile / tl.ntx) * tl.TY + (int)(threadIdx.x / tl.TX) + 1;
-          if (i <= D.nx && j <= D.ny) {
-            kk[u] = D.id(i, j);
-            v[u] = value(kk[u], 0);
-          }
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u)
-        if (kk[u] >= 0) put(kk[u], 0, v[u]);
-    }
   }
 };
 
@@ -510,10 +474,6 @@ struct StripOwn {
     v = fma(-ay[k], xs, v);
     v = fma(-ay[k + P], xn, v);
     return v;
-  }
-  template <class V, class Put>
-  __device__ __forceinline__ void each_batched(V value, Put put) const {
-    each([&](int k, int c) { put(k, c, value(k, c)); });
   }
 };
 
@@ -900,8 +860,9 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     }
     if (outer >= a.max_refine || total_inner >= a.max_iter) { status = COVOF_MAXITER; break; }
     // cdef: aP_sum is the sum of the deflation weights
-    own.each_batched([&](int k, int) -> IS { return (k == pk) ? IS(0) : (IS)((r[k] - cdef * wgt(k)) * scl(k) * inv_r); },
-                     [&](int k, int c, IS v) { inner.set_rhs(k, c, v); });
+    own.each([&](int k, int c) {
+      inner.set_rhs(k, c, (k == pk) ? IS(0) : (IS)((r[k] - cdef * wgt(k)) * scl(k) * inv_r));
+    });
     __syncthreads();
     int budget = a.max_iter - total_inner;
     if (budget > a.inner_max_iter) budget = a.inner_max_iter;
@@ -972,7 +933,7 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     // consecutive directions are dominated by the same smooth mode.
     double acc[2] = {0.0, 0.0};
     const bool was_fresh = fresh;
-    own.each_batched([&](int k, int c) -> double3 {
+    own.each([&](int k, int c) {
       double wk = (k == pk) ? 0.0 : own.stencil(k, c, z, a.ax, a.ay, a.aP);
       // A (z - shift 1) = A z - shift e, e from its buffer: four FP64
       // subtractions a cell fewer on the pass the FP64 pipe bounds
@@ -980,12 +941,10 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       const double zk = z[k] - shift;
       const double pk_ = was_fresh ? zk : fma(-beta, pv[k], zk);
       const double qk_ = was_fresh ? wk : fma(-beta, qv[k], wk);
-      return make_double3(pk_, qk_, r[k]);
-    }, [&](int k, int, double3 v) {
-      pv[k] = v.x;
-      qv[k] = v.y;
-      acc[0] = fma(v.x, v.y, acc[0]);
-      acc[1] = fma(v.x, v.z, acc[1]);
+      pv[k] = pk_;
+      qv[k] = qk_;
+      acc[0] = fma(pk_, qk_, acc[0]);
+      acc[1] = fma(pk_, r[k], acc[1]);
     });
     double sa[3];
     if (!R.sum_map<2, 3>(acc, sa, [&](const double* w, double* o) {
@@ -1000,13 +959,12 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     if (!(sigma > 0.0)) { status = COVOF_BREAKDOWN; break; }
     const double alpha = sa[1];
     double acc2[2] = {0.0, 0.0};
-    own.each_batched([&](int k, int) -> double2 {
-      return make_double2(fma(alpha, pv[k], x[k]), fma(-alpha, qv[k], r[k]));
-    }, [&](int k, int, double2 v) {
-      x[k] = v.x;
-      r[k] = v.y;
-      acc2[0] = fma(v.y, v.y, acc2[0]);
-      acc2[1] += v.y;
+    own.each([&](int k, int) {
+      x[k] = fma(alpha, pv[k], x[k]);
+      const double rk = fma(-alpha, qv[k], r[k]);
+      r[k] = rk;
+      acc2[0] = fma(rk, rk, acc2[0]);
+      acc2[1] += rk;
     });
     double t2[5];
     if (!R.sum_map<2, 5>(acc2, t2, [&](const double* w, double* o) {
@@ -1475,41 +1433,6 @@ struct MgInnerT {
       f(i + 1, j + 1);
     }
   }
-  // The grid-level loop in batches of kBatch cells per thread: the loads of
-  // every cell of a batch are issued before any of its stores.  Written as
-  // one loop, a cell's store could alias the next cell's loads for the
-  // compiler, which then waits one L2 round trip per cell (about seven
-  // cells per thread at 1024^2: the phase is bound by that latency, not by
-  // bandwidth).  value(i, j) computes a cell, put(i, j, v) writes it.
-#ifndef COVOF_MG_BATCH
-#define COVOF_MG_BATCH 4
-#endif
-  static constexpr int kBatch = COVOF_MG_BATCH;
-  template <class V, class Put>
-  __device__ __forceinline__ void cells_batched(int ni, int nj, V value, Put put) const {
-    const int n = ni * nj;
-    const int t0 = tm.rank * (int)blockDim.x + (int)threadIdx.x;
-    const int st = tm.size * (int)blockDim.x;
-    for (int c0 = t0; c0 < n; c0 += kBatch * st) {
-      T v[kBatch];
-#pragma unroll
-      for (int u = 0; u < kBatch; ++u) {
-        const int c = c0 + u * st;
-        if (c < n) {
-          const int j = c / ni, i = c - j * ni;
-          v[u] = value(i + 1, j + 1);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < kBatch; ++u) {
-        const int c = c0 + u * st;
-        if (c < n) {
-          const int j = c / ni, i = c - j * ni;
-          put(i + 1, j + 1, v[u]);
-        }
-      }
-    }
-  }
   template <bool S>
   __device__ __forceinline__ static T apply(const MgLvT<T>& L, const T* x, int k) {
     k = Dims{L.nx, L.ny, L.P}.nbhd(k, 8);
@@ -1532,22 +1455,6 @@ struct MgInnerT {
     T* xd = cur ? L.xa : L.xb;
     const T w = H.omega;
     const int pin = l == 0 ? pk : -1;
-    if constexpr (!S && !W) {
-      // grid levels: batched (loads of several cells in flight per thread)
-      cells_batched(L.nx, L.ny, [&](int i, int j) -> T {
-        const int k = L.id(i, j);
-        const T d = L.dg[k];
-        T v;
-        if (first) v = w * ld<S>(L.b + k) / d;
-        else v = ld<S>(xs + k) + w * (ld<S>(L.b + k) - apply<S>(L, xs, k)) / d;
-        return k == pin ? T(0) : v;
-      }, [&](int i, int j, T v) {
-        const int k = L.id(i, j);
-        xd[k] = v;
-        epi(k, v);
-      });
-      return;
-    }
     cells<S, W>(L.nx, L.ny, [&](int i, int j) {
       const int k = L.id(i, j);
       T v;
@@ -1600,16 +1507,6 @@ struct MgInnerT {
     const T* xc = cc ? Cc.xb : Cc.xa;
     const T cw = H.cw;
     const int pin = l == 0 ? pk : -1;
-    if constexpr (!S) {
-      cells_batched(F.nx, F.ny, [&](int i, int j) -> T {
-        const int k = F.id(i, j);
-        return ld<S>(x + k) + cw * ld<S>(xc + Cc.id((i + 1) / 2, (j + 1) / 2));
-      }, [&](int i, int j, T v) {
-        const int k = F.id(i, j);
-        if (k != pin) x[k] = v;
-      });
-      return;
-    }
     cells<S>(F.nx, F.ny, [&](int i, int j) {
       const int k = F.id(i, j);
       if (k == pin) return;

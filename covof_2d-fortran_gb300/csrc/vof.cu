@@ -177,11 +177,14 @@ __global__ void __launch_bounds__(128) k_vof_mixed(VofArgs a, const int* __restr
   const double* __restrict__ C = a.C;
   const double dx = a.dx, dy = a.dy;
   for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += nwarps) {
-    const int k = a.D.nbhd(list[e], 22);  // checked builds: a listed cell outside the interior
+    const int k = list[e];
     const int j = k / a.D.P, i = k - j * a.D.P;
     const double c = C[k];
     const double xmin = m.xf(i), xmax = m.xf(i + 1), ymin = m.yf(j), ymax = m.yf(j + 1);
     const bool inner = (i >= 1 && i <= nx && j >= 1 && j <= ny);
+    // checked builds: an inner cell reads its 3 x 3 neighbourhood (ghost
+    // cells of the list read only themselves)
+    if (inner && a.D.nbhd(k, 22) != k) continue;
     auto Cq = [&](int p, int q) { return C[a.D.id(p, q)]; };
     if (a.method != COVOF_RECON_ELVIRA || !inner) {
       double pnx = 1.0, pny = 0.0;
