@@ -43,11 +43,35 @@ inline bool is_wall(const covof_params* p, int side) {
   return p->bc_type[side] == COVOF_BC_DIRICHLET || p->bc_type[side] == COVOF_BC_FREESLIP;
 }
 
-int check_params(const covof_params* p, bool allow_neumann) {
+// Periodic directions at np = 1: the reference makes a direction periodic
+// when either side names BC_PERIODIC (src/module_simulation.f90:116-118) but
+// then tests one side or the other (bc_left in apply_vof_bc, bc_right in
+// poisson_matvec's east term); this restatement takes a pair only.
+inline bool per_x(const covof_params* p) { return p->bc_type[L] == COVOF_BC_PERIODIC; }
+inline bool per_y(const covof_params* p) { return p->bc_type[B] == COVOF_BC_PERIODIC; }
+// the periodic VOF branches restated here are Weymouth-Yue's (CIAM's, TVD's
+// and the smoothing filters' are not)
+inline int check_periodic_vof(const covof_params* p) {
+  if (!(per_x(p) || per_y(p))) return COVOF_OK;
+  if (p->advection_method != COVOF_ADVECT_WEYMOUTH_YUE || p->enable_svof_smoothing ||
+      p->enable_diffusion_smoothing)
+    return COVOF_UNSUPPORTED;
+  return COVOF_OK;
+}
+
+// allow_periodic: the routine follows the reference's periodic branches
+// (Poisson, projection correction, VOF); the momentum path does not (its
+// velocity DOF count changes with periodicity) and refuses them.
+int check_params(const covof_params* p, bool allow_neumann, bool allow_periodic = false) {
   if (!p || p->nx < 2 || p->ny < 2 || !(p->dx > 0) || !(p->dy > 0)) return COVOF_INVALID;
   for (int s = 0; s < 4; ++s) {
     int t = p->bc_type[s];
-    if (t == COVOF_BC_PERIODIC) return COVOF_UNSUPPORTED;
+    if (t == COVOF_BC_PERIODIC) {
+      const int other = s ^ 1;  // L<->R, B<->T
+      if (p->bc_type[other] != COVOF_BC_PERIODIC) return COVOF_INVALID;
+      if (!allow_periodic) return COVOF_UNSUPPORTED;
+      continue;
+    }
     if (t == COVOF_BC_NEUMANN && !allow_neumann) return COVOF_UNSUPPORTED;
     if (t != COVOF_BC_DIRICHLET && t != COVOF_BC_FREESLIP && t != COVOF_BC_NEUMANN)
       return COVOF_INVALID;
@@ -152,6 +176,25 @@ void velocity_bc(const covof_params* prm, const Mesh& m, double* u, double* v, b
   double ur = homog ? 0.0 : prm->bc_u[R], vr = homog ? 0.0 : prm->bc_v[R];
   double ub = homog ? 0.0 : prm->bc_u[B], vb = homog ? 0.0 : prm->bc_v[B];
   double ut = homog ? 0.0 : prm->bc_u[T], vt = homog ? 0.0 : prm->bc_v[T];
+  // periodic directions at np = 1 (:332-351); the wall branches below then
+  // skip those sides (their types are PERIODIC)
+  if (per_x(prm))
+    for (int j = 1; j <= ny; ++j) {
+      u[m.id(0, j)] = u[m.id(nx, j)];
+      u[m.id(nx + 1, j)] = u[m.id(1, j)];
+      v[m.id(0, j)] = v[m.id(nx, j)];
+      v[m.id(nx + 1, j)] = v[m.id(1, j)];
+    }
+  if (per_y(prm)) {
+    for (int i = 1; i <= nx; ++i) {
+      v[m.id(i, 0)] = v[m.id(i, ny)];
+      v[m.id(i, ny + 1)] = v[m.id(i, 1)];
+    }
+    for (int i = 0; i <= nx + 1; ++i) {
+      u[m.id(i, 0)] = u[m.id(i, ny)];
+      u[m.id(i, ny + 1)] = u[m.id(i, 1)];
+    }
+  }
   // west (:339-373)
   for (int j = 1; j <= ny; ++j) {
     int t = prm->bc_type[L];
@@ -218,8 +261,8 @@ void velocity_bc(const covof_params* prm, const Mesh& m, double* u, double* v, b
       if (!homog) v[m.id(i, ny + 1)] = v[m.id(i, ny)];
     }
   }
-  // physical corners, non-homogeneous only (:484-500)
-  if (!homog) {
+  // physical corners, non-homogeneous only (:512-526; none on a periodic side)
+  if (!homog && !per_x(prm) && !per_y(prm)) {
     u[m.id(nx + 1, 0)] = u[m.id(nx + 1, 1)];
     v[m.id(nx + 1, 0)] = v[m.id(nx, 0)];
     u[m.id(nx + 1, ny + 1)] = u[m.id(nx + 1, ny)];
@@ -228,21 +271,55 @@ void velocity_bc(const covof_params* prm, const Mesh& m, double* u, double* v, b
   }
 }
 
-// src/module_mpi_comm.f90:636-683 apply_vof_bc (np=1, no JET_INLET)
-void vof_bc(const Mesh& m, double* C) {
+// src/module_mpi_comm.f90:25-56 exchange_halos_scalar at np = 1: the
+// periodic wrap of the ghost ring (x first, rows 0..ny+1, then y, columns
+// 0..nx+1, so the corners take the doubly wrapped values); nothing on a
+// non-periodic domain.
+void halo_scalar(const covof_params* prm, const Mesh& m, double* f) {
   const int nx = m.nx, ny = m.ny;
-  for (int j = 1; j <= ny; ++j) {
-    C[m.id(0, j)] = C[m.id(1, j)];
-    C[m.id(nx + 1, j)] = C[m.id(nx, j)];
+  if (per_x(prm))
+    for (int j = 0; j <= ny + 1; ++j) {
+      f[m.id(0, j)] = f[m.id(nx, j)];
+      f[m.id(nx + 1, j)] = f[m.id(1, j)];
+    }
+  if (per_y(prm))
+    for (int i = 0; i <= nx + 1; ++i) {
+      f[m.id(i, 0)] = f[m.id(i, ny)];
+      f[m.id(i, ny + 1)] = f[m.id(i, 1)];
+    }
+}
+
+// src/module_mpi_comm.f90:636-683 apply_vof_bc (np=1, no JET_INLET):
+// periodic wrap (rows / columns 1..n) or zero gradient per direction.
+void vof_bc(const covof_params* prm, const Mesh& m, double* C) {
+  const int nx = m.nx, ny = m.ny;
+  if (per_x(prm)) {
+    for (int j = 1; j <= ny; ++j) {
+      C[m.id(0, j)] = C[m.id(nx, j)];
+      C[m.id(nx + 1, j)] = C[m.id(1, j)];
+    }
+  } else {
+    for (int j = 1; j <= ny; ++j) {
+      C[m.id(0, j)] = C[m.id(1, j)];
+      C[m.id(nx + 1, j)] = C[m.id(nx, j)];
+    }
   }
-  for (int i = 1; i <= nx; ++i) C[m.id(i, 0)] = C[m.id(i, 1)];
-  for (int i = 1; i <= nx; ++i) C[m.id(i, ny + 1)] = C[m.id(i, ny)];
+  if (per_y(prm)) {
+    for (int i = 1; i <= nx; ++i) {
+      C[m.id(i, 0)] = C[m.id(i, ny)];
+      C[m.id(i, ny + 1)] = C[m.id(i, 1)];
+    }
+  } else {
+    for (int i = 1; i <= nx; ++i) C[m.id(i, 0)] = C[m.id(i, 1)];
+    for (int i = 1; i <= nx; ++i) C[m.id(i, ny + 1)] = C[m.id(i, ny)];
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Pressure Poisson.  Coefficient arrays are (nx, ny), index (i-1)+nx*(j-1).
 struct Poisson {
   int nx, ny;
+  bool perx = false, pery = false;  // periodic wrap of the stencil (np = 1)
   std::vector<double> aW, aE, aS, aN, aP, b;
   inline size_t k(int i, int j) const { return (size_t)(i - 1) + (size_t)nx * (size_t)(j - 1); }
 };
@@ -253,6 +330,7 @@ void poisson_assemble(const covof_params* prm, const Mesh& m, double dt, const d
   const int nx = m.nx, ny = m.ny;
   const double dx = m.dx, dy = m.dy, dvol = dx * dy;
   P.nx = nx; P.ny = ny;
+  P.perx = per_x(prm); P.pery = per_y(prm);
   size_t n = (size_t)nx * ny;
   P.aW.assign(n, 0.0); P.aE.assign(n, 0.0); P.aS.assign(n, 0.0); P.aN.assign(n, 0.0);
   P.aP.assign(n, 0.0); P.b.assign(n, 0.0);
@@ -296,34 +374,33 @@ void poisson_rhs_from_velocity(const Mesh& m, const double* u, const double* v, 
     }
 }
 
-// src/module_simulation.f90:2668-2707 poisson_matvec (non-periodic)
-void poisson_matvec(const Poisson& P, const double* x, double* y) {
+// src/module_simulation.f90:2668-2707 poisson_matvec, one row: the
+// neighbours across a periodic boundary wrap (x(nx,j) west of cell 1,
+// x(1,j) east of cell nx; likewise in y).
+inline double poisson_row(const Poisson& P, const double* x, int i, int j) {
   const int nx = P.nx, ny = P.ny;
-  for (int j = 1; j <= ny; ++j)
-    for (int i = 1; i <= nx; ++i) {
-      size_t q = P.k(i, j);
-      double val = P.aP[q] * x[q];
-      if (i > 1) val = val - P.aW[q] * x[q - 1];
-      if (i < nx) val = val - P.aE[q] * x[q + 1];
-      if (j > 1) val = val - P.aS[q] * x[q - nx];
-      if (j < ny) val = val - P.aN[q] * x[q + nx];
-      y[q] = val;
-    }
+  const size_t q = P.k(i, j);
+  double val = P.aP[q] * x[q];
+  if (i > 1) val = val - P.aW[q] * x[q - 1];
+  else if (P.perx) val = val - P.aW[q] * x[P.k(nx, j)];
+  if (i < nx) val = val - P.aE[q] * x[q + 1];
+  else if (P.perx) val = val - P.aE[q] * x[P.k(1, j)];
+  if (j > 1) val = val - P.aS[q] * x[q - nx];
+  else if (P.pery) val = val - P.aS[q] * x[P.k(i, ny)];
+  if (j < ny) val = val - P.aN[q] * x[q + nx];
+  else if (P.pery) val = val - P.aN[q] * x[P.k(i, 1)];
+  return val;
+}
+
+void poisson_matvec(const Poisson& P, const double* x, double* y) {
+  for (int j = 1; j <= P.ny; ++j)
+    for (int i = 1; i <= P.nx; ++i) y[P.k(i, j)] = poisson_row(P, x, i, j);
 }
 
 void poisson_matvec_omp(const Poisson& P, const double* x, double* y) {
-  const int nx = P.nx, ny = P.ny;
 #pragma omp parallel for schedule(static)
-  for (int j = 1; j <= ny; ++j)
-    for (int i = 1; i <= nx; ++i) {
-      size_t q = P.k(i, j);
-      double val = P.aP[q] * x[q];
-      if (i > 1) val = val - P.aW[q] * x[q - 1];
-      if (i < nx) val = val - P.aE[q] * x[q + 1];
-      if (j > 1) val = val - P.aS[q] * x[q - nx];
-      if (j < ny) val = val - P.aN[q] * x[q + nx];
-      y[q] = val;
-    }
+  for (int j = 1; j <= P.ny; ++j)
+    for (int i = 1; i <= P.nx; ++i) y[P.k(i, j)] = poisson_row(P, x, i, j);
 }
 
 // src/module_simulation.f90:2709-2758 poisson_ssor (SGS, omega = 1).
@@ -336,7 +413,9 @@ void poisson_sgs(const Poisson& P, const double* r, double* z, bool pinned) {
       size_t q = P.k(i, j);
       double val = r[q];
       if (i > 1) val = val + P.aW[q] * z[q - 1];
+      else if (P.perx) val = val + P.aW[q] * z[P.k(nx, j)];
       if (j > 1) val = val + P.aS[q] * z[q - nx];
+      else if (P.pery) val = val + P.aS[q] * z[P.k(i, ny)];
       z[q] = val / P.aP[q];
       if (pinned && i == 1 && j == 1) z[q] = 0.0;
     }
@@ -345,7 +424,9 @@ void poisson_sgs(const Poisson& P, const double* r, double* z, bool pinned) {
       size_t q = P.k(i, j);
       double val = P.aP[q] * z[q];
       if (i < nx) val = val + P.aE[q] * z[q + 1];
+      else if (P.perx) val = val + P.aE[q] * z[P.k(1, j)];
       if (j < ny) val = val + P.aN[q] * z[q + nx];
+      else if (P.pery) val = val + P.aN[q] * z[P.k(i, 1)];
       z[q] = val / P.aP[q];
       if (pinned && i == 1 && j == 1) z[q] = 0.0;
     }
@@ -399,14 +480,18 @@ int poisson_pcg_par(const covof_params* prm, Poisson& P, std::vector<double>& x,
   int iters = 0, status = COVOF_OK;
   double r_norm = 0.0, b_norm = 1.0;
   auto Arow = [&](const double* v, double* y, int j) {
-    for (int i = 1; i <= nx; ++i) {
-      const size_t q = P.k(i, j);
-      double val = aP[q] * v[q];
-      if (i > 1) val = val - aW[q] * v[q - 1];
-      if (i < nx) val = val - aE[q] * v[q + 1];
-      if (j > 1) val = val - aS[q] * v[q - nx];
-      if (j < ny) val = val - aN[q] * v[q + nx];
-      y[q] = val;
+    if (P.perx || P.pery) {
+      for (int i = 1; i <= nx; ++i) y[P.k(i, j)] = poisson_row(P, v, i, j);
+    } else {
+      for (int i = 1; i <= nx; ++i) {
+        const size_t q = P.k(i, j);
+        double val = aP[q] * v[q];
+        if (i > 1) val = val - aW[q] * v[q - 1];
+        if (i < nx) val = val - aE[q] * v[q + 1];
+        if (j > 1) val = val - aS[q] * v[q - nx];
+        if (j < ny) val = val - aN[q] * v[q + nx];
+        y[q] = val;
+      }
     }
     if (pinned && j == 1) y[0] = 0.0;
   };
@@ -594,19 +679,22 @@ int poisson_driver(const covof_params* prm, double dt, const double* u_star, con
   return st;
 }
 
-// src/module_simulation.f90:2586-2654 projection correction (non-periodic)
+// src/module_simulation.f90:2586-2654 projection correction.  With a
+// periodic direction the last face is the first one's image and is not
+// corrected (u_nx = nx, :2446-2449); the west / south neighbour of the first
+// face wraps.
 void project_correct(const covof_params* prm, const Mesh& m, double dt, double* u, double* v,
                      const double* p, const double* rho_u, const double* rho_v) {
   const int nx = m.nx, ny = m.ny;
-  const int u_nx = nx + 1, v_ny = ny + 1;
+  const int u_nx = per_x(prm) ? nx : nx + 1, v_ny = per_y(prm) ? ny : ny + 1;
   for (int j = 1; j <= ny; ++j)
     for (int i = 1; i <= u_nx; ++i) {
       bool wall = (i == 1 && is_wall(prm, L)) || (i == u_nx && is_wall(prm, R));
       if (wall) continue;
       double r = rho_u[m.id(i, j)];
       if (r < 1.0e-12) r = 1.0;
-      double pw = (i > 1) ? p[m.id(i - 1, j)] : p[m.id(1, j)];
-      double pe = (i <= nx) ? p[m.id(i, j)] : p[m.id(nx, j)];
+      double pw = (i > 1) ? p[m.id(i - 1, j)] : (per_x(prm) ? p[m.id(nx, j)] : p[m.id(1, j)]);
+      double pe = (i <= nx) ? p[m.id(i, j)] : (per_x(prm) ? p[m.id(1, j)] : p[m.id(nx, j)]);
       double g = (pe - pw) / m.dx;
       u[m.id(i, j)] = u[m.id(i, j)] - (dt / r) * g;
     }
@@ -616,8 +704,8 @@ void project_correct(const covof_params* prm, const Mesh& m, double dt, double* 
       if (wall) continue;
       double r = rho_v[m.id(i, j)];
       if (r < 1.0e-12) r = 1.0;
-      double ps = (j > 1) ? p[m.id(i, j - 1)] : p[m.id(i, 1)];
-      double pn = (j <= ny) ? p[m.id(i, j)] : p[m.id(i, ny)];
+      double ps = (j > 1) ? p[m.id(i, j - 1)] : (per_y(prm) ? p[m.id(i, ny)] : p[m.id(i, 1)]);
+      double pn = (j <= ny) ? p[m.id(i, j)] : (per_y(prm) ? p[m.id(i, 1)] : p[m.id(i, ny)]);
       double g = (pn - ps) / m.dy;
       v[m.id(i, j)] = v[m.id(i, j)] - (dt / r) * g;
     }
@@ -1765,7 +1853,7 @@ void reconstruct_elvira(const Mesh& m, const double* C, Seg* s) {
     }
 }
 
-// src/module_interface_reconstruction.f90:580-683 reconstruct_interface (np=1, walls)
+// src/module_interface_reconstruction.f90:580-683 reconstruct_interface (np=1)
 void reconstruct_interface(const covof_params* prm, const Mesh& m, const double* C, Seg* s) {
   const int nx = m.nx, ny = m.ny;
   if (prm->recon == COVOF_RECON_ELVIRA) reconstruct_elvira(m, C, s);
@@ -1774,14 +1862,20 @@ void reconstruct_interface(const covof_params* prm, const Mesh& m, const double*
   std::vector<double> snx(g, 0.0), sny(g, 0.0);
   for (int j = 1; j <= ny; ++j)
     for (int i = 1; i <= nx; ++i) { snx[m.id(i, j)] = s[m.id(i, j)].nx; sny[m.id(i, j)] = s[m.id(i, j)].ny; }
-  for (int j = 1; j <= ny; ++j) {
-    snx[m.id(0, j)] = snx[m.id(1, j)]; sny[m.id(0, j)] = sny[m.id(1, j)];
-    snx[m.id(nx + 1, j)] = snx[m.id(nx, j)]; sny[m.id(nx + 1, j)] = sny[m.id(nx, j)];
-  }
-  for (int i = 0; i <= nx + 1; ++i) {
-    snx[m.id(i, 0)] = snx[m.id(i, 1)]; sny[m.id(i, 0)] = sny[m.id(i, 1)];
-    snx[m.id(i, ny + 1)] = snx[m.id(i, ny)]; sny[m.id(i, ny + 1)] = sny[m.id(i, ny)];
-  }
+  // :606-627: the normals' halo exchange (the periodic wrap), then the
+  // first interior ring copied out on the non-periodic sides
+  halo_scalar(prm, m, snx.data());
+  halo_scalar(prm, m, sny.data());
+  if (!per_x(prm))
+    for (int j = 1; j <= ny; ++j) {
+      snx[m.id(0, j)] = snx[m.id(1, j)]; sny[m.id(0, j)] = sny[m.id(1, j)];
+      snx[m.id(nx + 1, j)] = snx[m.id(nx, j)]; sny[m.id(nx + 1, j)] = sny[m.id(nx, j)];
+    }
+  if (!per_y(prm))
+    for (int i = 0; i <= nx + 1; ++i) {
+      snx[m.id(i, 0)] = snx[m.id(i, 1)]; sny[m.id(i, 0)] = sny[m.id(i, 1)];
+      snx[m.id(i, ny + 1)] = snx[m.id(i, ny)]; sny[m.id(i, ny + 1)] = sny[m.id(i, ny)];
+    }
   auto ring = [&](int i, int j) {
     size_t k = m.id(i, j);
     double c = C[k];
@@ -1825,6 +1919,12 @@ void wy_pass(const covof_params* prm, const Mesh& m, double dt, int dir, const d
           flux[m.id(i, j)] = -cut_box_area(xp, xp + d, m.y_face(j), m.y_face(j + 1), s.nx, s.ny, s.alpha);
         }
       }
+    // :1223-1231: the two images of the periodic face carry the upwind one's flux
+    if (per_x(prm))
+      for (int j = 1; j <= ny; ++j) {
+        if (u[m.id(1, j)] >= 0.0) flux[m.id(1, j)] = flux[m.id(nx + 1, j)];
+        else flux[m.id(nx + 1, j)] = flux[m.id(1, j)];
+      }
     std::memcpy(Cout, Cin, g * sizeof(double));
     for (int j = 1; j <= ny; ++j)
       for (int i = 1; i <= nx; ++i) {
@@ -1847,6 +1947,12 @@ void wy_pass(const covof_params* prm, const Mesh& m, double dt, int dir, const d
           const Seg& s = seg[m.id(i, j)];
           flux[m.id(i, j)] = -cut_box_area(m.x_face(i), m.x_face(i + 1), yp, yp + d, s.nx, s.ny, s.alpha);
         }
+      }
+    // :1268-1276
+    if (per_y(prm))
+      for (int i = 1; i <= nx; ++i) {
+        if (v[m.id(i, 1)] >= 0.0) flux[m.id(i, 1)] = flux[m.id(i, ny + 1)];
+        else flux[m.id(i, ny + 1)] = flux[m.id(i, 1)];
       }
     std::memcpy(Cout, Cin, g * sizeof(double));
     for (int j = 1; j <= ny; ++j)
@@ -1925,7 +2031,7 @@ void ciam_step(const covof_params* prm, const Mesh& m, double dt, bool x_first, 
   std::vector<double> cs(g), cf(g);
   int d1 = x_first ? 0 : 1, d2 = x_first ? 1 : 0;
   ciam_pass(prm, m, dt, d1, u, v, C, cs.data());
-  vof_bc(m, cs.data());  // :1002-1004
+  vof_bc(prm, m, cs.data());  // :1002-1004
   ciam_pass(prm, m, dt, d2, u, v, cs.data(), cf.data());
   std::memcpy(C, cf.data(), g * sizeof(double));
 }
@@ -2021,7 +2127,8 @@ void wy_step(const covof_params* prm, const Mesh& m, double dt, bool x_first, co
   for (size_t k = 0; k < g; ++k) cd[k] = C[k] >= 0.5 ? 1.0 : 0.0;  // :1189-1197
   int d1 = x_first ? 0 : 1, d2 = x_first ? 1 : 0;
   wy_pass(prm, m, dt, d1, u, v, cd.data(), C, cs.data(), false);
-  vof_bc(m, cs.data());  // :1240-1243
+  halo_scalar(prm, m, cs.data());  // :1238-1242
+  vof_bc(prm, m, cs.data());
   wy_pass(prm, m, dt, d2, u, v, cd.data(), cs.data(), cf.data(), true);
   std::memcpy(C, cf.data(), g * sizeof(double));
 }
@@ -2118,10 +2225,13 @@ void update_props(const covof_params* prm, const Mesh& m, double* C, double* rho
     }
     return;
   }
-  C[m.id(0, 0)] = C[m.id(1, 1)];
-  C[m.id(nx + 1, 0)] = C[m.id(nx, 1)];
-  C[m.id(0, ny + 1)] = C[m.id(1, ny)];
-  C[m.id(nx + 1, ny + 1)] = C[m.id(nx, ny)];
+  // physical corners only (:532-535): a periodic side has no boundary
+  if (!per_x(prm) && !per_y(prm)) {
+    C[m.id(0, 0)] = C[m.id(1, 1)];
+    C[m.id(nx + 1, 0)] = C[m.id(nx, 1)];
+    C[m.id(0, ny + 1)] = C[m.id(1, ny)];
+    C[m.id(nx + 1, ny + 1)] = C[m.id(nx, ny)];
+  }
   const bool svof = prm->enable_svof_smoothing && Cs;
   for (int j = 0; j <= ny + 1; ++j)
     for (int i = 0; i <= nx + 1; ++i) {
@@ -2212,22 +2322,22 @@ double orc_compute_alpha(double a, double b, double c, double d, double nx, doub
 }
 
 int orc_apply_velocity_bc(const covof_params* prm, double* u, double* v, int homogeneous) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
   velocity_bc(prm, mesh_of(prm), u, v, homogeneous != 0);
   return COVOF_OK;
 }
 int orc_apply_vof_bc(const covof_params* prm, double* C) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
-  vof_bc(mesh_of(prm), C);
+  vof_bc(prm, mesh_of(prm), C);
   return COVOF_OK;
 }
 
 int orc_poisson_assemble(const covof_params* prm, double dt, const double* u_star,
                          const double* v_star, const double* rho_u, const double* rho_v,
                          double* aW, double* aE, double* aS, double* aN, double* aP, double* b) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
   Mesh m = mesh_of(prm);
   Poisson P;
@@ -2242,7 +2352,7 @@ int orc_poisson_assemble(const covof_params* prm, double dt, const double* u_sta
 
 int orc_poisson_matvec(const covof_params* prm, double dt, const double* rho_u,
                        const double* rho_v, const double* x, double* y) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
   Mesh m = mesh_of(prm);
   Poisson P;
@@ -2257,7 +2367,7 @@ int orc_poisson_matvec(const covof_params* prm, double dt, const double* rho_u,
 int orc_poisson_solve(const covof_params* prm, double dt, const double* u_star,
                       const double* v_star, const double* rho_u, const double* rho_v, double* p,
                       int* iters, double* relres, int nthreads) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
   return poisson_driver(prm, dt, u_star, v_star, nullptr, rho_u, rho_v, p, iters, relres, nthreads, 0);
 }
@@ -2265,7 +2375,7 @@ int orc_poisson_solve(const covof_params* prm, double dt, const double* u_star,
 int orc_poisson_solve_rhs(const covof_params* prm, double dt, const double* b,
                           const double* rho_u, const double* rho_v, double* p, int* iters,
                           double* relres, int nthreads) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
   return poisson_driver(prm, dt, nullptr, nullptr, b, rho_u, rho_v, p, iters, relres, nthreads, 0);
 }
@@ -2273,7 +2383,7 @@ int orc_poisson_solve_rhs(const covof_params* prm, double dt, const double* b,
 int orc_poisson_fixed_iters(const covof_params* prm, double dt, const double* b,
                             const double* rho_u, const double* rho_v, double* p, int n_iter,
                             int nthreads, double* relres) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
   if (n_iter < 1) return COVOF_INVALID;
   int it = 0;
@@ -2282,7 +2392,7 @@ int orc_poisson_fixed_iters(const covof_params* prm, double dt, const double* b,
 
 int orc_project_correct(const covof_params* prm, double dt, double* u, double* v, const double* p,
                         const double* rho_u, const double* rho_v) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
   project_correct(prm, mesh_of(prm), dt, u, v, p, rho_u, rho_v);
   return COVOF_OK;
@@ -2520,7 +2630,7 @@ int orc_sp_step(const covof_params* prm, double dt, double* u, double* v, double
 }
 
 int orc_reconstruct(const covof_params* prm, const double* C, double* seg) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
   Mesh m = mesh_of(prm);
   size_t g = (size_t)(m.nx + 2) * (m.ny + 2);
@@ -2532,8 +2642,9 @@ int orc_reconstruct(const covof_params* prm, const double* C, double* seg) {
 
 int orc_wy_step(const covof_params* prm, double dt, int x_first, const double* u, const double* v,
                 double* C) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
+  if ((st = check_periodic_vof(prm))) return st;
   wy_step(prm, mesh_of(prm), dt, x_first != 0, u, v, C);
   return COVOF_OK;
 }
@@ -2541,8 +2652,9 @@ int orc_wy_step(const covof_params* prm, double dt, int x_first, const double* u
 // the configured transport alone (Weymouth-Yue, CIAM or TVD)
 int orc_vof_transport(const covof_params* prm, double dt, int x_first, const double* u,
                       const double* v, double* C) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
+  if ((st = check_periodic_vof(prm))) return st;
   if (prm->advection_method < 0 || prm->advection_method > COVOF_ADVECT_TVD) return COVOF_INVALID;
   vof_transport(prm, mesh_of(prm), dt, x_first != 0, u, v, C);
   return COVOF_OK;
@@ -2565,7 +2677,7 @@ int orc_diffusion_smooth(const covof_params* prm, const double* C, double* C_til
 int orc_update_physical_properties(const covof_params* prm, double* C, double* rho,
                                    double* rho_u, double* rho_v, double* mu, double* mu_node,
                                    const double* C_s) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
   update_props(prm, mesh_of(prm), C, rho, rho_u, rho_v, mu, mu_node, C_s);
   return COVOF_OK;
@@ -2574,7 +2686,7 @@ int orc_update_physical_properties(const covof_params* prm, double* C, double* r
 int orc_compute_curvature_and_csf(const covof_params* prm, const double* C, double* fx_sigma,
                                   double* fy_sigma, double* curvature, const double* C_s,
                                   const double* C_tilde) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
   csf(prm, mesh_of(prm), C, fx_sigma, fy_sigma, curvature, C_s, C_tilde);
   return COVOF_OK;
@@ -2586,11 +2698,13 @@ int orc_vof_advect(const covof_params* prm, double dt, int step_count, const dou
                    const double* v, double* C, double* rho, double* rho_u, double* rho_v,
                    double* mu, double* mu_node, double* fx_sigma, double* fy_sigma,
                    double* curvature, double* C_s, double* C_tilde) {
-  int st = check_params(prm, true);
+  int st = check_params(prm, true, true);
   if (st) return st;
+  if ((st = check_periodic_vof(prm))) return st;
   Mesh m = mesh_of(prm);
   vof_transport(prm, m, dt, (step_count % 2) == 0, u, v, C);
-  vof_bc(m, C);
+  halo_scalar(prm, m, C);  // src/module_interface_vof.f90:809-810
+  vof_bc(prm, m, C);
   if (prm->enable_svof_smoothing && C_s) svof_smooth(prm, m, C, C_s);
   update_props(prm, m, C, rho, rho_u, rho_v, mu, mu_node, C_s);
   if (prm->enable_diffusion_smoothing && C_tilde) diffusion_smooth(prm, m, C, C_tilde);
