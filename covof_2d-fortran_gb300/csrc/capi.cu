@@ -40,12 +40,35 @@ int check_params(const covof_params* p) {
   if ((long long)(p->nx + 2) * (p->ny + 2) > (1LL << 30)) return COVOF_INVALID;
   for (int s = 0; s < 4; ++s) {
     const int t = p->bc_type[s];
-    if (t == COVOF_BC_PERIODIC || t == COVOF_BC_NEUMANN) return COVOF_UNSUPPORTED;
+    if (t == COVOF_BC_NEUMANN) return COVOF_UNSUPPORTED;
+    // a periodic direction names both of its sides (left / right, bottom / top)
+    if (t == COVOF_BC_PERIODIC) {
+      if (p->bc_type[s ^ 1] != COVOF_BC_PERIODIC) return COVOF_INVALID;
+      continue;
+    }
     if (t != COVOF_BC_DIRICHLET && t != COVOF_BC_FREESLIP) return COVOF_INVALID;
   }
   if (p->advection_method < COVOF_ADVECT_WEYMOUTH_YUE || p->advection_method > COVOF_ADVECT_TVD) return COVOF_INVALID;
   if (p->p_precision < COVOF_PREC_FP64 || p->p_precision > COVOF_PREC_FP64_MG) return COVOF_INVALID;
   if (p->tvd_limiter < COVOF_LIMITER_SUPERBEE || p->tvd_limiter > COVOF_LIMITER_HRIC) return COVOF_INVALID;
+  return COVOF_OK;
+}
+
+bool periodic(const covof_params& p) {
+  return p.bc_type[0] == COVOF_BC_PERIODIC || p.bc_type[2] == COVOF_BC_PERIODIC;
+}
+
+// The periodic branches on the GPU: the Poisson operator in the plain FP64
+// Jacobi-PCG, the projection correction, the velocity and VOF ghosts and the
+// Weymouth-Yue step (src/module_simulation.f90:2679-2701, 2602-2654;
+// src/module_mpi_comm.f90:25-56, 332-351, 636-683; src/module_interface_vof.f90:
+// 1223-1231, 1268-1276).  The momentum predictor (its velocity DOFs change
+// with periodicity), the multigrid and sweep Poisson solvers, CIAM / TVD and
+// the smoothing filters refuse periodic boundaries.
+int check_periodic_vof(const covof_params& p) {
+  if (!periodic(p)) return COVOF_OK;
+  if (p.advection_method != COVOF_ADVECT_WEYMOUTH_YUE || p.enable_svof_smoothing || p.enable_diffusion_smoothing)
+    return COVOF_UNSUPPORTED;
   return COVOF_OK;
 }
 
@@ -412,6 +435,9 @@ int pois_pre(covof_handle* h, double dt, const double* u, const double* v, const
   const bool mixed = P.p_precision == COVOF_PREC_MIXED;
   // the symmetric Gauss-Seidel preconditioner belongs to the plain FP64 PCG
   if (P.p_precond == COVOF_PRECOND_SSOR && P.p_precision != COVOF_PREC_FP64) return COVOF_UNSUPPORTED;
+  // periodic boundaries: the plain FP64 Jacobi-PCG
+  if (periodic(P) && (P.p_precision != COVOF_PREC_FP64 || P.p_precond == COVOF_PRECOND_SSOR))
+    return COVOF_UNSUPPORTED;
   CS(ensure_poisson(h));
   CS(poisson_plan(h));
   const int pinned = P.p_gauge == COVOF_GAUGE_PINNED;
@@ -424,6 +450,9 @@ int pois_pre(covof_handle* h, double dt, const double* u, const double* v, const
     k_poisson_scale32<<<grid2(P.nx + 1, P.ny + 1, blk), blk, 0, h->stream>>>(
         h->D, h->pax, h->pay, h->pisd, h->ax32, h->ay32, h->aP32, h->paP, P.p_inner_kind == COVOF_INNER_MG ? 1 : 0);
   k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, p, h->px, pinned);
+  // periodic: the initial guess's ghost ring carries the wrapped interior
+  // (the first residual's stencil reads it)
+  if (periodic(P)) k_wrap_ghosts<<<1, 1024, 0, h->stream>>>(h->D, h->px);
   CK(cudaGetLastError());
   PoissonArgs& a = *out;
   std::memset(&a, 0, sizeof(a));
@@ -543,6 +572,7 @@ BcArgs bc_args(const covof_handle* h) {
 
 int velocity_bc_dev(covof_handle* h, double* u, double* v) {
   const BcArgs b = bc_args(h);
+  if (periodic(h->prm)) k_vbc_periodic<<<1, 1024, 0, h->stream>>>(b, u, v);
   k_vbc_we<<<(h->D.ny + 127) / 128, 128, 0, h->stream>>>(b, u, v);
   k_vbc_sn<<<(h->D.nx + 127) / 128, 128, 0, h->stream>>>(b, u, v);
   k_vbc_corners<<<1, 32, 0, h->stream>>>(b, u, v);
@@ -569,6 +599,7 @@ int vjp_dev(covof_handle* h, double dt, const double* rho_u, const double* rho_v
             double* grad_bu, double* grad_bv, int* iters, double* relres) {
   const covof_params& P = h->prm;
   if (!rho_u || !rho_v || !p || !gu || !gv || !grad_u || !grad_v || !grad_bu || !grad_bv) return COVOF_INVALID;
+  if (periodic(P)) return COVOF_UNSUPPORTED;  // the adjoint's face kernels assume walls
   CS(ensure_adj(h));
   double gp_mean = 0.0;
   if (gp && P.p_gauge == COVOF_GAUGE_REFERENCE) {
@@ -629,6 +660,7 @@ MomArgs mom_args(covof_handle* h, double dt, const double* u_n, const double* v_
 }
 
 int check_mom_params(const covof_params& P) {
+  if (periodic(P)) return COVOF_UNSUPPORTED;
   if (P.convective_scheme != COVOF_CONV_UPWIND && P.convective_scheme != COVOF_CONV_CENTERED &&
       P.convective_scheme != COVOF_CONV_TVD_SUPERBEE)
     return COVOF_UNSUPPORTED;
@@ -879,6 +911,7 @@ VofArgs vof_args(covof_handle* h, double dt, const double* C, const double* Cn, 
 // Pure cells directly, interface cells one warp each (list built on the
 // device, so nothing here waits for the host), then the ghost ring.
 int reconstruct_dev(covof_handle* h, const double* C, double* seg_out) {
+  CS(check_periodic_vof(h->prm));
   CS(ensure_vof(h));
   VofArgs a = vof_args(h, 0.0, C, C, nullptr, nullptr);
   if (seg_out) a.seg = seg_out;
@@ -892,8 +925,11 @@ int reconstruct_dev(covof_handle* h, const double* C, double* seg_out) {
   return COVOF_OK;
 }
 
+// exchange_halos_scalar + apply_vof_bc (src/module_interface_vof.f90:809-810,
+// 1238-1242): the exchange is the periodic wrap, nothing on a closed domain
 int vof_bc_dev(covof_handle* h, double* C) {
-  k_vof_bc<<<(h->D.nx + h->D.ny + 127) / 128, 128, 0, h->stream>>>(h->D, C);
+  if (periodic(h->prm)) k_vof_halo_bc<<<1, 1024, 0, h->stream>>>(h->D, C, 1);
+  else k_vof_bc<<<(h->D.nx + h->D.ny + 127) / 128, 128, 0, h->stream>>>(h->D, C);
   CK(cudaGetLastError());
   return COVOF_OK;
 }
@@ -903,6 +939,7 @@ int vof_bc_dev(covof_handle* h, double* C) {
 // geometric schemes reconstruct, pass, apply the VOF BC, reconstruct, pass;
 // TVD is one explicit update.
 int wy_step_dev(covof_handle* h, double dt, int x_first, const double* u, const double* v, double* C) {
+  CS(check_periodic_vof(h->prm));
   CS(ensure_vof(h));
   const dim3 blk(32, 4), grd = grid2(h->D.nx + 2, h->D.ny + 2, blk);
   const int method = h->prm.advection_method;
@@ -970,6 +1007,7 @@ int csf_dev(covof_handle* h, const double* C, double* fx, double* fy, double* cu
 // src/module_interface_vof.f90:387-476 smooth_svof_helmholtz: C_s = C, the
 // wavefront Gauss-Seidel sweeps (svof.cu), then the clamp and ghost ring.
 int svof_dev(covof_handle* h, const double* C, double* Cs) {
+  if (periodic(h->prm)) return COVOF_UNSUPPORTED;
   CS(ensure_vof(h));
   const covof_params& P = h->prm;
   double kw = P.svof_filter_width;
@@ -997,6 +1035,7 @@ int svof_dev(covof_handle* h, const double* C, double* Cs) {
 
 // src/module_interface_vof.f90:1416-1461 vof_smooth_diffusion: C -> C_tilde
 int diffusion_dev(covof_handle* h, const double* C, double* Ct) {
+  if (periodic(h->prm)) return COVOF_UNSUPPORTED;
   CS(ensure_vof(h));
   const covof_params& P = h->prm;
   int steps = P.diffusion_smoothing_steps;
@@ -1342,6 +1381,8 @@ int covof_create(const covof_params* params, covof_handle** out) {
   if (!h) return COVOF_INVALID;
   h->prm = *params;
   h->D = Dims{params->nx, params->ny, params->nx + 2};
+  h->D.perx = params->bc_type[0] == COVOF_BC_PERIODIC ? 1 : 0;
+  h->D.pery = params->bc_type[2] == COVOF_BC_PERIODIC ? 1 : 0;
   h->g = (size_t)(params->nx + 2) * (size_t)(params->ny + 2);
   auto fail = [&](int code) { covof_destroy(h); return code; };
   if (cudaGetDevice(&h->device) != cudaSuccess) return fail(COVOF_CUDA_ERROR);
@@ -1493,6 +1534,7 @@ int poisson_apply_enqueue(covof_handle* h, double dt, const double* rho_u, const
                                                   h->pb, nullptr, nullptr);
   CK(cudaMemsetAsync(h->px, 0, g * sizeof(double), h->stream));
   k_copy_interior<<<grd, blk, 0, h->stream>>>(h->D, x, h->px, 0);
+  if (periodic(P)) k_wrap_ghosts<<<1, 1024, 0, h->stream>>>(h->D, h->px);
   k_poisson_apply<<<grd, blk, 0, h->stream>>>(h->D, h->px, y, h->pax, h->pay, h->paP);
   CK(cudaGetLastError());
   return COVOF_OK;
@@ -1885,7 +1927,8 @@ int covof_apply_vof_bc(covof_handle* h, double* C) {
   CS(ensure_fields(h));
   const size_t g = h->g;
   CS(h2d(h, h->f_C, C, g));
-  k_vof_bc<<<(h->D.nx + h->D.ny + 127) / 128, 128, 0, h->stream>>>(h->D, h->f_C);
+  if (periodic(h->prm)) k_vof_halo_bc<<<1, 1024, 0, h->stream>>>(h->D, h->f_C, 0);
+  else k_vof_bc<<<(h->D.nx + h->D.ny + 127) / 128, 128, 0, h->stream>>>(h->D, h->f_C);
   CK(cudaGetLastError());
   CS(d2h(h, C, h->f_C, g));
   return sync(h);

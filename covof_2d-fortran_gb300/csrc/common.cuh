@@ -36,6 +36,13 @@ static __device__ __noinline__ void oob_record(int site, long long index) {
 
 struct Dims {
   int nx, ny, P;  // P = nx + 2
+  // periodic directions (one rank: the ghost ring holds the wrapped
+  // interior, src/module_mpi_comm.f90:46-56)
+  int perx = 0, pery = 0;
+  // the interior cell whose value a ghost cell (i, j) carries in a periodic
+  // direction (i, j themselves otherwise)
+  __host__ __device__ __forceinline__ int wrap_i(int i) const { return perx ? (i == 0 ? nx : (i == nx + 1 ? 1 : i)) : i; }
+  __host__ __device__ __forceinline__ int wrap_j(int j) const { return pery ? (j == 0 ? ny : (j == ny + 1 ? 1 : j)) : j; }
   __host__ __device__ __forceinline__ int id(int i, int j) const {
 #if defined(COVOF_CHECKED) && defined(__CUDA_ARCH__)
     if (i < 0 || i > nx + 1 || j < 0 || j > ny + 1) {

@@ -191,6 +191,8 @@ int poisson_plan(covof_handle* h);
 int predictor_plan(covof_handle* h);
 int4 wall_flags(const covof_params& p);
 bool mg_path(const covof_params& p);
+bool periodic(const covof_params& p);
+int check_periodic_vof(const covof_params& p);
 dim3 grid2(int ni, int nj, dim3 b);
 int sync(covof_handle* h);
 int pois_pre(covof_handle* h, double dt, const double* u, const double* v, const double* b,

@@ -1226,10 +1226,37 @@ __global__ void k_vbc_sn(BcArgs b, double* u, double* v) {
     u[D.id(i, ny + 1)] = u[D.id(i, ny)];
   }
 }
+// The periodic directions of apply_velocity_bc at np = 1
+// (src/module_mpi_comm.f90:332-351), before the wall sides: x first (rows
+// 1..ny of u and v), then y (v columns 1..nx, u columns 0..nx+1); one block.
+__global__ void k_vbc_periodic(BcArgs b, double* u, double* v) {
+  const Dims& D = b.D;
+  const int nx = D.nx, ny = D.ny;
+  if (D.perx)
+    for (int j = 1 + (int)threadIdx.x; j <= ny; j += blockDim.x) {
+      u[D.id(0, j)] = u[D.id(nx, j)];
+      u[D.id(nx + 1, j)] = u[D.id(1, j)];
+      v[D.id(0, j)] = v[D.id(nx, j)];
+      v[D.id(nx + 1, j)] = v[D.id(1, j)];
+    }
+  __syncthreads();
+  if (D.pery) {
+    for (int i = 1 + (int)threadIdx.x; i <= nx; i += blockDim.x) {
+      v[D.id(i, 0)] = v[D.id(i, ny)];
+      v[D.id(i, ny + 1)] = v[D.id(i, 1)];
+    }
+    for (int i = (int)threadIdx.x; i <= nx + 1; i += blockDim.x) {
+      u[D.id(i, 0)] = u[D.id(i, ny)];
+      u[D.id(i, ny + 1)] = u[D.id(i, 1)];
+    }
+  }
+}
+// physical corners (:512-526): none when a direction is periodic
 __global__ void k_vbc_corners(BcArgs b, double* u, double* v) {
   const Dims& D = b.D;
   const int nx = D.nx, ny = D.ny;
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  if (D.perx || D.pery) return;
   u[D.id(nx + 1, 0)] = u[D.id(nx + 1, 1)];
   v[D.id(nx + 1, 0)] = v[D.id(nx, 0)];
   u[D.id(nx + 1, ny + 1)] = u[D.id(nx + 1, ny)];

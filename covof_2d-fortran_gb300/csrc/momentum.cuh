@@ -101,6 +101,7 @@ __global__ void k_mom_unpack(MomArgs a, double* u, double* v);
 __global__ void k_mom_pack(MomArgs a, const double* u, const double* v);
 __global__ void k_vbc_we(BcArgs b, double* u, double* v);
 __global__ void k_vbc_sn(BcArgs b, double* u, double* v);
+__global__ void k_vbc_periodic(BcArgs b, double* u, double* v);
 __global__ void k_vbc_corners(BcArgs b, double* u, double* v);
 
 }  // namespace covof

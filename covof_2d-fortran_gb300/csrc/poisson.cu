@@ -101,6 +101,22 @@ __global__ void k_poisson_scale32(Dims D, const double* __restrict__ ax, const d
   if (i <= D.nx && j <= D.ny) aP32[k] = 1.0f;
 }
 
+// The periodic wrap of a vector's ghost ring (one block): x first, rows
+// 1..ny, then y, columns 0..nx+1 (src/module_mpi_comm.f90:46-56).
+__global__ void k_wrap_ghosts(Dims D, double* __restrict__ x) {
+  if (D.perx)
+    for (int j = 1 + (int)threadIdx.x; j <= D.ny; j += blockDim.x) {
+      x[D.id(0, j)] = x[D.id(D.nx, j)];
+      x[D.id(D.nx + 1, j)] = x[D.id(1, j)];
+    }
+  __syncthreads();
+  if (D.pery)
+    for (int i = (int)threadIdx.x; i <= D.nx + 1; i += blockDim.x) {
+      x[D.id(i, 0)] = x[D.id(i, D.ny)];
+      x[D.id(i, D.ny + 1)] = x[D.id(i, 1)];
+    }
+}
+
 // Interior copy between a caller field and a solver vector (ghosts of dst untouched).
 __global__ void k_copy_interior(Dims D, const double* __restrict__ src, double* __restrict__ dst,
                                 int zero_pin) {
@@ -194,8 +210,11 @@ __device__ __forceinline__ T phase_stencil(const Dims& D, const Tiles& tl, int t
     const int i = tx0 + lx, j = ty0 + ly;  // global index incl. ghost (i = 0 .. nx+1)
     T v = T(0);
     if (i <= D.nx + 1 && j <= D.ny + 1) {
-      const int k = D.id(i, j);
-      const bool interior = i >= 1 && i <= D.nx && j >= 1 && j <= D.ny;
+      // a ghost cell in a periodic direction carries its wrapped interior
+      // cell's direction (src/module_simulation.f90:2679-2701)
+      const int si = D.wrap_i(i), sj = D.wrap_j(j);
+      const int k = D.id(si, sj);
+      const bool interior = si >= 1 && si <= D.nx && sj >= 1 && sj <= D.ny;
       if (interior && k != pinned_k) {
         const T z = precond<T, UNIT>(S, k, __ldcg(S.r + k));
         v = first ? z : fmad_(beta, __ldcg(dold + k), z);
@@ -2077,23 +2096,27 @@ __global__ void k_project_correct(Dims D, double dt, double dx, double dy, int4 
   int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int nx = D.nx, ny = D.ny;
-  if (i <= nx + 1 && j <= ny) {
+  // a periodic direction: the last face is the first one's image and is not
+  // corrected here (u_nx = nx, src/module_simulation.f90:2446-2449); the
+  // first face's upwind cell wraps (:2602-2616)
+  const int u_nx = D.perx ? nx : nx + 1, v_ny = D.pery ? ny : ny + 1;
+  if (i <= u_nx && j <= ny) {
     bool w = (i == 1 && wall.x) || (i == nx + 1 && wall.y);
     if (!w) {
       int k = D.id(i, j);
       double r = rho_u[k]; if (r < 1.0e-12) r = 1.0;
-      double pw = (i > 1) ? p[k - 1] : p[D.id(1, j)];
+      double pw = (i > 1) ? p[k - 1] : p[D.id(D.perx ? nx : 1, j)];
       double pe = (i <= nx) ? p[k] : p[D.id(nx, j)];
       double g = __ddiv_rn(__dsub_rn(pe, pw), dx);
       u[k] = __dsub_rn(u[k], __dmul_rn(__ddiv_rn(dt, r), g));
     }
   }
-  if (i <= nx && j <= ny + 1) {
+  if (i <= nx && j <= v_ny) {
     bool w = (j == 1 && wall.z) || (j == ny + 1 && wall.w);
     if (!w) {
       int k = D.id(i, j);
       double r = rho_v[k]; if (r < 1.0e-12) r = 1.0;
-      double ps = (j > 1) ? p[k - D.P] : p[D.id(i, 1)];
+      double ps = (j > 1) ? p[k - D.P] : p[D.id(i, D.pery ? ny : 1)];
       double pn = (j <= ny) ? p[k] : p[D.id(i, ny)];
       double g = __ddiv_rn(__dsub_rn(pn, ps), dy);
       v[k] = __dsub_rn(v[k], __dmul_rn(__ddiv_rn(dt, r), g));

@@ -76,6 +76,7 @@ __global__ void k_poisson_scale32(Dims D, const double* __restrict__ ax, const d
                                   const double* __restrict__ aP, int unscaled);
 __global__ void k_copy_interior(Dims D, const double* __restrict__ src, double* __restrict__ dst,
                                 int zero_pin);
+__global__ void k_wrap_ghosts(Dims D, double* __restrict__ x);
 struct Tiles {
   int TX, TY, ntx, nty, ntiles;
 };

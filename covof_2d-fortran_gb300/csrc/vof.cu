@@ -282,8 +282,14 @@ __global__ void __launch_bounds__(128) k_vof_ring_warp(VofArgs a) {
     const int k = a.D.id(i, j);
     const double c = a.C[k];
     if (!(c > 1.0e-6 && c < 1.0 - 1.0e-6)) continue;
-    const int si = i < 1 ? 1 : (i > nx ? nx : i);
-    const int sj = j < 1 ? 1 : (j > ny ? ny : j);
+    // the normal of the nearest interior cell, or of the wrapped one in a
+    // periodic direction (:606-627: the normals' halo exchange, then the
+    // copies on the non-periodic sides).  With x closed and y periodic the
+    // y wrap of the corners happens before the x copies fill column 0 / nx+1,
+    // so the reference's corner normal is zero and no segment is formed.
+    if (!a.D.perx && a.D.pery && (i == 0 || i == nx + 1) && (j == 0 || j == ny + 1)) continue;
+    const int si = a.D.perx ? a.D.wrap_i(i) : (i < 1 ? 1 : (i > nx ? nx : i));
+    const int sj = a.D.pery ? a.D.wrap_j(j) : (j < 1 ? 1 : (j > ny ? ny : j));
     const int ks = a.D.id(si, sj);
     double snx = a.seg[3 * ks], sny = a.seg[3 * ks + 1];
     const double nr = fhypot(snx, sny);
@@ -323,6 +329,23 @@ __device__ __forceinline__ double y_flux(const VMesh& m, const double* __restric
   return -cut_box_area(m.xf(i), m.xf(i + 1), yp, yp + d, seg[3 * ks], seg[3 * ks + 1], seg[3 * ks + 2]);
 }
 
+// The flux of face i (x) / j (y) with the periodic sync of
+// src/module_interface_vof.f90:1223-1231, 1268-1276: the two images of the
+// periodic face (1 and nx+1) carry the flux computed at the one the velocity
+// of face 1 comes from.
+__device__ __forceinline__ double x_flux_p(const VMesh& m, const double* __restrict__ seg,
+                                           const double* __restrict__ u, double dt, int i, int j) {
+  if (m.D.perx && (i == 1 || i == m.D.nx + 1))
+    return x_flux(m, seg, u, dt, u[m.D.id(1, j)] >= 0.0 ? m.D.nx + 1 : 1, j);
+  return x_flux(m, seg, u, dt, i, j);
+}
+__device__ __forceinline__ double y_flux_p(const VMesh& m, const double* __restrict__ seg,
+                                           const double* __restrict__ v, double dt, int i, int j) {
+  if (m.D.pery && (j == 1 || j == m.D.ny + 1))
+    return y_flux(m, seg, v, dt, i, v[m.D.id(i, 1)] >= 0.0 ? m.D.ny + 1 : 1);
+  return y_flux(m, seg, v, dt, i, j);
+}
+
 // One Weymouth-Yue direction pass (src/module_interface_vof.f90:1199-1285):
 // interior cells get C - div(flux)/dV + c_d dt/dh du; ghost cells copy Cin.
 // c_d = [C^n >= 0.5] is read from Cn (frozen at time n, :1189-1197).
@@ -340,12 +363,12 @@ __global__ void k_vof_pass(VofArgs a, int dir, int clamp, const double* __restri
   const double cd = a.Cn[k] >= 0.5 ? 1.0 : 0.0;
   double c;
   if (dir == 0) {
-    const double fw = x_flux(m, a.seg, a.u, a.dt, i, j);
-    const double fe = x_flux(m, a.seg, a.u, a.dt, i + 1, j);
+    const double fw = x_flux_p(m, a.seg, a.u, a.dt, i, j);
+    const double fe = x_flux_p(m, a.seg, a.u, a.dt, i + 1, j);
     c = Cin[k] - (fe - fw) / area + cd * (a.dt / a.dx) * (a.u[k + 1] - a.u[k]);
   } else {
-    const double fs = y_flux(m, a.seg, a.v, a.dt, i, j);
-    const double fn = y_flux(m, a.seg, a.v, a.dt, i, j + 1);
+    const double fs = y_flux_p(m, a.seg, a.v, a.dt, i, j);
+    const double fn = y_flux_p(m, a.seg, a.v, a.dt, i, j + 1);
     c = Cin[k] - (fn - fs) / area + cd * (a.dt / a.dy) * (a.v[k + a.D.P] - a.v[k]);
   }
   if (clamp) c = fmax(0.0, fmin(1.0, c));
@@ -445,6 +468,35 @@ __global__ void k_tvd_advect(VofArgs a, int lim, const double* __restrict__ Cin,
   Cout[k] = fmax(0.0, fmin(1.0, c));
 }
 
+// exchange_halos_scalar then apply_vof_bc on a periodic domain (np = 1,
+// src/module_mpi_comm.f90:25-56, 636-683), one block: the wrap in x (rows
+// 0..ny+1), then in y (columns 0..nx+1), then the apply_vof_bc edges
+// (periodic rows / columns 1..n again, zero gradient on the other
+// direction's sides).  halo = 0: apply_vof_bc alone.
+__global__ void k_vof_halo_bc(Dims D, double* __restrict__ C, int halo) {
+  const int nx = D.nx, ny = D.ny;
+  if (halo && D.perx)
+    for (int j = (int)threadIdx.x; j <= ny + 1; j += blockDim.x) {
+      C[D.id(0, j)] = C[D.id(nx, j)];
+      C[D.id(nx + 1, j)] = C[D.id(1, j)];
+    }
+  __syncthreads();
+  if (halo && D.pery)
+    for (int i = (int)threadIdx.x; i <= nx + 1; i += blockDim.x) {
+      C[D.id(i, 0)] = C[D.id(i, ny)];
+      C[D.id(i, ny + 1)] = C[D.id(i, 1)];
+    }
+  __syncthreads();
+  for (int j = 1 + (int)threadIdx.x; j <= ny; j += blockDim.x) {
+    C[D.id(0, j)] = C[D.id(D.perx ? nx : 1, j)];
+    C[D.id(nx + 1, j)] = C[D.id(D.perx ? 1 : nx, j)];
+  }
+  for (int i = 1 + (int)threadIdx.x; i <= nx; i += blockDim.x) {
+    C[D.id(i, 0)] = C[D.id(i, D.pery ? ny : 1)];
+    C[D.id(i, ny + 1)] = C[D.id(i, D.pery ? 1 : ny)];
+  }
+}
+
 // src/module_mpi_comm.f90:636-683 apply_vof_bc (np = 1): zero-gradient
 // edge ghosts, corners untouched.
 __global__ void k_vof_bc(Dims D, double* __restrict__ C) {
@@ -475,18 +527,22 @@ __global__ void k_props_cells(PropsArgs a) {
     return;
   }
   const bool corner = (i == 0 || i == nx + 1) && (j == 0 || j == ny + 1);
-  double cv;
+  // C's corners are rewritten at physical corners only (:532-535); mu's
+  // corners always equal the interior corner's (:553-556)
+  double cv = a.C[k], cm = cv;
   if (corner) {
     const int ki = a.D.id(i == 0 ? 1 : nx, j == 0 ? 1 : ny);
-    cv = a.C[ki];
-    a.C[k] = cv;
-  } else {
-    cv = a.C[k];
+    cm = a.C[ki];
+    if (!a.D.perx && !a.D.pery) {
+      cv = cm;
+      a.C[k] = cv;
+    }
   }
   // SVOF: the properties follow the smoothed indicator (:541-545)
   const double c = fmax(0.0, fmin(1.0, a.Cs ? a.Cs[k] : cv));
+  const double c_mu = fmax(0.0, fmin(1.0, a.Cs ? a.Cs[k] : cm));
   a.rho[k] = c * a.rho1 + (1.0 - c) * a.rho2;
-  a.mu[k] = c * a.mu1 + (1.0 - c) * a.mu2;
+  a.mu[k] = c_mu * a.mu1 + (1.0 - c_mu) * a.mu2;
 }
 
 // src/module_interface_vof.f90:575-615: face densities (arithmetic) and node

@@ -40,6 +40,7 @@ __global__ void k_vof_pass(VofArgs a, int dir, int clamp, const double* __restri
 __global__ void k_ciam_pass(VofArgs a, int dir, const double* __restrict__ Cin, double* __restrict__ Cout);
 __global__ void k_tvd_advect(VofArgs a, int lim, const double* __restrict__ Cin, double* __restrict__ Cout);
 __global__ void k_vof_bc(Dims D, double* __restrict__ C);
+__global__ void k_vof_halo_bc(Dims D, double* __restrict__ C, int halo);
 __global__ void k_props_cells(PropsArgs a);
 __global__ void k_props_faces(PropsArgs a);
 __global__ void k_csf_normals(CsfArgs a);
