@@ -6,7 +6,8 @@
 //   1. per case, in parallel branches: u_old = u, v_old = v; the VOF step
 //      (two-phase cases) and the velocity BC; predictor assembly;
 //   2. ONE persistent cooperative launch: the predictor Krylov solves of all
-//      cases (k_mom_krylov_batch);
+//      cases (k_mom_krylov_batch, or k_mom_bicgstab_batch / k_mom_cg_batch
+//      when every case uses that method);
 //   3. per case: unpack + velocity BC; Poisson assembly;
 //   4. ONE persistent cooperative launch: the Poisson solves of all cases
 //      (k_pcg_mixed_mg_batch / k_pcg_mixed_smem_batch / k_pcg_mixed_batch,
@@ -69,6 +70,7 @@ struct covof_batch {
   PoissonArgs* d_pargs = nullptr;
   MomArgs* d_margs = nullptr;
   const void* pfn = nullptr;  // the batched Poisson kernel
+  const void* mfn = nullptr;  // the batched momentum Krylov kernel
   cudaGraphExec_t graph[2] = {};
   std::vector<double> graph_dt;
   bool graph_refused = false;
@@ -298,7 +300,7 @@ int enqueue_batch_step(covof_batch* b, const double* dt, bool x_first) {
                    h->f_fy, h->f_u_old, h->f_v_old, &b->h_margs[c]);
   }));
   CK(cudaMemcpyAsync(b->d_margs, b->h_margs, sizeof(MomArgs) * b->ncases, cudaMemcpyHostToDevice, b->stream));
-  CS(launch_batch(b, b->mplan, (const void*)k_mom_krylov_batch, b->d_margs));
+  CS(launch_batch(b, b->mplan, b->mfn, b->d_margs));
   CS(per_case(b, [&](int c, covof_handle* h) -> int {
     CS(mom_post(h, b->h_margs[c], h->f_u, h->f_v));
     return pois_pre(h, dt[c], h->f_u, h->f_v, nullptr, h->f_rho_u, h->f_rho_v, h->f_p, &b->h_pargs[c]);
@@ -476,7 +478,16 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
   } else {
     pmax = max_coresident(b, b->pfn, 1024);
   }
-  const int mmax = max_coresident(b, (const void*)k_mom_krylov_batch, 512);
+  // one method across the batch: its own kernel (two blocks per SM)
+  b->mfn = (const void*)k_mom_krylov_batch;
+  {
+    bool same = true;
+    for (covof_handle* h : b->h) same = same && h->prm.linear_solver == b->h[0]->prm.linear_solver;
+    const int m = b->h[0]->prm.linear_solver;
+    if (same && m == COVOF_LINEAR_BICGSTAB) b->mfn = (const void*)k_mom_bicgstab_batch;
+    if (same && m == COVOF_LINEAR_CG) b->mfn = (const void*)k_mom_cg_batch;
+  }
+  const int mmax = max_coresident(b, b->mfn, 512);
   if (pmax < 1 || mmax < 1) return fail(COVOF_CUDA_ERROR);
   int s = make_plan(b->pplan, b->h, pmax, 1024, smem_form ? &tmin : nullptr);
   if (s != COVOF_OK) return fail(s);

@@ -219,16 +219,19 @@ int ensure_adj_host(covof_handle* h) {
   return COVOF_OK;
 }
 
-// Block count of a persistent cooperative kernel: at most one block per SM
-// (fewer arrivals per grid barrier; the 1024-thread Poisson blocks fill an
-// SM anyway), never more than the work units, never more than co-resident.
-int coop_blocks(covof_handle* h, const void* fn, int threads, long long units, size_t smem = 0) {
+// Block count of a persistent cooperative kernel: per_sm_max blocks on
+// every SM (one by default: fewer arrivals per grid barrier, and the
+// 1024-thread Poisson blocks fill an SM anyway), fewer when the kernel's
+// registers or shared memory allow fewer co-resident blocks or there are
+// fewer work units, never more than the partials array's slots.
+int coop_blocks(covof_handle* h, const void* fn, int threads, long long units, size_t smem = 0,
+                int per_sm_max = 1) {
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess || per_sm < 1)
     return -1;
-  long long nb = h->sm_count;
+  if (per_sm > per_sm_max) per_sm = per_sm_max;
+  long long nb = (long long)per_sm * h->sm_count;
   if (units < nb) nb = units < 1 ? 1 : units;
-  if (nb > (long long)per_sm * h->sm_count) nb = (long long)per_sm * h->sm_count;
   if (nb > h->part_blocks) nb = h->part_blocks;
   return (int)nb;
 }
@@ -687,7 +690,11 @@ int predictor_plan(covof_handle* h) {
                  : (const void*)k_bicgstab2;
   long long nseg = (long long)((P.nx + 1 + 31) / 32) * P.ny + (long long)((P.nx + 31) / 32) * (P.ny + 1);
   if (P.solver_type == COVOF_SOLVER_MONOLITHIC) nseg += (long long)((P.nx + 31) / 32) * P.ny;
-  const int nb = coop_blocks(h, fn, kKrylovThreads, (nseg + kKrylovThreads / 32 - 1) / (kKrylovThreads / 32));
+  // two 512-thread blocks per SM where the registers allow: the Krylov
+  // loops stream their vectors and coefficients from HBM, and a second
+  // block doubles the loads in flight
+  const int nb = coop_blocks(h, fn, kKrylovThreads, (nseg + kKrylovThreads / 32 - 1) / (kKrylovThreads / 32), 0,
+                             kKrylovBlocksPerSm);
   if (nb < 1) return COVOF_CUDA_ERROR;
   h->m_fn = fn;
   h->m_nb = nb;
@@ -1397,7 +1404,7 @@ int covof_create(const covof_params* params, covof_handle** out) {
   if (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess ||
       cudaEventCreate(&h->ev2) != cudaSuccess || cudaEventCreate(&h->ev3) != cudaSuccess)
     return fail(COVOF_CUDA_ERROR);
-  h->part_blocks = h->sm_count;  // persistent kernels run at most one block per SM
+  h->part_blocks = kKrylovBlocksPerSm * h->sm_count;  // most blocks of a persistent launch
   if (dalloc(&h->bar, (size_t)64 + h->sm_count) || dalloc(&h->err, 1) ||
       dalloc(&h->part, (size_t)kMaxPartRegions * h->part_blocks) ||
       dalloc(&h->d_pres, 1) || dalloc(&h->d_kres, 1) || dalloc(&h->d_run, 1))

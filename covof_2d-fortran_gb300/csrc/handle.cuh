@@ -39,7 +39,8 @@ int bounds_check_static_scratch(unsigned long long*, unsigned long long*);
 namespace host {
 
 constexpr int kPoissonThreads = 1024;  // one cell per thread per 1024-cell tile
-constexpr int kKrylovThreads = 512;    // momentum Krylov kernels (80 registers)
+constexpr int kKrylovThreads = 512;    // momentum Krylov kernels (64 registers)
+constexpr int kKrylovBlocksPerSm = 2;  // co-resident momentum Krylov blocks per SM
 constexpr int kMaxPartRegions = 16;  // doubles per block in the partials array
 
 template <typename T>

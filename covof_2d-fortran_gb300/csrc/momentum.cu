@@ -1266,17 +1266,33 @@ __global__ void k_vbc_corners(BcArgs b, double* u, double* v) {
 
 // Predictor Krylov solves of many cases in one persistent launch (teams,
 // see BatchTeams); each case's method is its own linear_solver.
-__global__ void __launch_bounds__(512) k_mom_krylov_batch(const MomArgs* __restrict__ cases, BatchTeams bt) {
+__device__ __forceinline__ void mom_krylov_batch(const MomArgs* __restrict__ cases, const BatchTeams& bt,
+                                                 int method) {
   int4 T;
   const Team tm = batch_team(bt, T);
   const int t = bt.block_team[blockIdx.x];
   GridReducer R{bt.part + (size_t)16 * T.x, GridSync{bt.bar + 32 * t, bt.err + t, (unsigned)T.y, 0u}, 0, tm.rank};
   for (int q = T.z; q < T.w; ++q) {
     const MomArgs& a = cases[bt.case_list[q]];
-    if (a.method == COVOF_LINEAR_BICGSTAB) bicgstab_case(a, tm, R);
-    else if (a.method == COVOF_LINEAR_CG) cg_case(a, tm, R);
+    const int m = method >= 0 ? method : a.method;
+    if (m == COVOF_LINEAR_BICGSTAB) bicgstab_case(a, tm, R);
+    else if (m == COVOF_LINEAR_CG) cg_case(a, tm, R);
     else bicgstab2_case(a, tm, R);
   }
+}
+
+__global__ void __launch_bounds__(512) k_mom_krylov_batch(const MomArgs* __restrict__ cases, BatchTeams bt) {
+  mom_krylov_batch(cases, bt, -1);
+}
+
+// Every case with the same method: that method alone, in 64 registers, so
+// two 512-thread blocks share an SM (twice the loads in flight for these
+// HBM-streaming loops; the mixed-method kernel above needs 128 registers).
+__global__ void __launch_bounds__(512, 2) k_mom_bicgstab_batch(const MomArgs* __restrict__ cases, BatchTeams bt) {
+  mom_krylov_batch(cases, bt, COVOF_LINEAR_BICGSTAB);
+}
+__global__ void __launch_bounds__(512, 2) k_mom_cg_batch(const MomArgs* __restrict__ cases, BatchTeams bt) {
+  mom_krylov_batch(cases, bt, COVOF_LINEAR_CG);
 }
 
 // ---------------------------------------------------------------------------

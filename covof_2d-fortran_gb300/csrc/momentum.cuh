@@ -97,6 +97,8 @@ __global__ void k_bicgstab(MomArgs a);
 __global__ void k_bicgstab2(MomArgs a);
 __global__ void k_cg(MomArgs a);
 __global__ void k_mom_krylov_batch(const MomArgs* __restrict__ cases, BatchTeams bt);
+__global__ void k_mom_bicgstab_batch(const MomArgs* __restrict__ cases, BatchTeams bt);
+__global__ void k_mom_cg_batch(const MomArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_mom_unpack(MomArgs a, double* u, double* v);
 __global__ void k_mom_pack(MomArgs a, const double* u, const double* v);
 __global__ void k_vbc_we(BcArgs b, double* u, double* v);
