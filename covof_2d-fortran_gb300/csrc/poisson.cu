@@ -799,6 +799,54 @@ struct SmemCheby {
   }
 };
 
+// Conversions between the FP64 outer vectors and the FP32 V-cycle with a
+// power-of-two scale 2^e, in integer arithmetic: on this part the F2F
+// conversions and FP64 multiplies issue on the FP64 pipe (about 1.7
+// instructions per SM per clock, 1/64 of the FP32 rate), while these run on
+// the integer pipe.
+// f32_scaled: v 2^e rounded to FP32 (round half away from zero on the
+// magnitude, deterministic; below FP32's normal range: signed zero; from
+// 2^127 up: +-FLT_MAX; NaN and infinities saturate too -- a NaN residual is
+// caught by its FP64 norm before the inner iteration runs).
+__device__ __forceinline__ float f32_scaled(double v, int e) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const unsigned int hi = (unsigned int)(u >> 32), lo = (unsigned int)u;
+  const unsigned int sign = hi & 0x80000000u;
+  const int ex = (int)((hi >> 20) & 0x7ffu) - 896 + e;  // FP32 biased exponent
+  unsigned int f = sign | ((unsigned int)ex << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  f += (lo >> 28) & 1u;
+  if (ex < 1) f = sign;
+  if (ex > 253) f = sign | 0x7f7fffffu;
+  return __uint_as_float(f);
+}
+// f64_scaled: y 2^e exactly (FP32 subnormals as zero; infinities and NaN
+// kept, so a failed inner iteration still shows in the outer sums).
+__device__ __forceinline__ double f64_scaled(float y, int e) {
+  const unsigned int f = __float_as_uint(y);
+  const unsigned int e8 = (f >> 23) & 0xffu;
+  const unsigned int ed = e8 == 0xffu ? 0x7ffu : e8 + 896u + (unsigned int)e;
+  const unsigned int hi = (f & 0x80000000u) | (ed << 20) | ((f & 0x7fffffu) >> 3);
+  const unsigned int lo = f << 29;
+  return e8 == 0u ? 0.0 : __hiloint2double((int)hi, (int)lo);
+}
+// The multigrid inner's right-hand side (r - c) 2^e: FP32 by the integer
+// conversion of r 2^e less cs = (c 2^e in FP32); FP64 by the expression
+// itself (cs = c, s2 = 2^e).
+__device__ __forceinline__ float mg_rhs(double r, float cs, double, int e) {
+  return __fsub_rn(f32_scaled(r, e), cs);
+}
+__device__ __forceinline__ double mg_rhs(double r, double cs, double s2, int) { return (r - cs) * s2; }
+__device__ __forceinline__ float mg_rhs_const(double c, int e, float) { return f32_scaled(c, e); }
+__device__ __forceinline__ double mg_rhs_const(double c, int, double) { return c; }
+// the V-cycle's output back in FP64: y 2^-e (s2i = 2^-e)
+__device__ __forceinline__ double mg_out(float y, int e, double) { return f64_scaled(y, -e); }
+__device__ __forceinline__ double mg_out(double y, int, double s2i) { return y * s2i; }
+// e with 2^e rn in [1, 2) (0 for a zero or subnormal rn)
+__device__ __forceinline__ int pow2_exp(double rn) {
+  const int ex = (int)(((unsigned long long)__double_as_longlong(rn) >> 52) & 0x7ffu);
+  return ex == 0 ? 0 : 1023 - ex;
+}
+
 // FCG outer loop (see k_pcg_mixed).
 template <class Own, class Inner>
 __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, GridReducer& R) {
@@ -820,6 +868,20 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
   double b_norm = 1.0, r_norm = 0.0, inv_apsum = 1.0, inv_esum = 1.0, rse = 0.0, inv_sigma_old = 1.0;
   double rel = 0.0, cdef = 0.0, inv_r = 0.0;  // r_norm / b_norm, deflation, 1 / r_norm
   bool fresh = true;
+  // Multigrid inner: the x, r update pass also writes the next V-cycle's
+  // right-hand side (and with it the first level-0 sweep), so the cycle
+  // starts on that pass's reduction barrier -- one pass over the fine grid
+  // and one grid barrier fewer per outer iteration.  The V-cycle is linear,
+  // so the scale may come from the previous residual norm (multiplied back
+  // in the epilogue), and the deflation constant of the new residual is
+  // known before its reduction: sum(r - alpha q) = sum(r) - alpha sum(q),
+  // with sum(q) from the direction pass's reduction.
+  // The multigrid inner's right-hand side is scaled by 2^e_rhs (a power of
+  // two near 1 / ||r||: exact scalings, done in the conversions).
+  constexpr bool kCarry = !Inner::kScaled;
+  bool carried = false;  // the inner right-hand side holds the current r
+  int e_rhs = 0;
+  double qsum = 0.0;     // sum(q) of the last direction pass (reference gauge)
   // e = A 1 (interior ones, zero ghosts): the 1e-12*dvol shift of aP, the
   // eigenvalue of the constant vector in the reference gauge.
   auto ones_image = [&](int k) { return a.aP[k] - a.ax[k] - a.ax[k + 1] - a.ay[k] - a.ay[k + D.P]; };
@@ -864,6 +926,7 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       return false;
     r_norm = t[0]; rse = t[1]; rel = t[2]; cdef = t[3]; inv_r = t[4];
     b_norm = t[5]; inv_apsum = t[6]; inv_esum = t[7];
+    carried = false;
     return true;
   };
   if (!true_residual()) ok = false;
@@ -879,10 +942,20 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     }
     if (outer >= a.max_refine || total_inner >= a.max_iter) { status = COVOF_MAXITER; break; }
     // cdef: aP_sum is the sum of the deflation weights
-    own.each([&](int k, int c) {
-      inner.set_rhs(k, c, (k == pk) ? IS(0) : (IS)((r[k] - cdef * wgt(k)) * scl(k) * inv_r));
-    });
-    __syncthreads();
+    const bool rhs_ready = carried;
+    if (!rhs_ready) {
+      if constexpr (kCarry) {
+        e_rhs = pow2_exp(r_norm);
+        const double s2 = ldexp(1.0, e_rhs);
+        const IS cs = mg_rhs_const(cdef, e_rhs, IS(0));
+        own.each([&](int k, int c) { inner.set_rhs(k, c, (k == pk) ? IS(0) : mg_rhs(r[k], cs, s2, e_rhs)); });
+      } else {
+        own.each([&](int k, int c) {
+          inner.set_rhs(k, c, (k == pk) ? IS(0) : (IS)((r[k] - cdef * wgt(k)) * scl(k) * inv_r));
+        });
+      }
+      __syncthreads();
+    }
     int budget = a.max_iter - total_inner;
     if (budget > a.inner_max_iter) budget = a.inner_max_iter;
     double zs[3] = {0.0, 0.0, 0.0};
@@ -892,18 +965,21 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       // multigrid: z and its sums formed in the V-cycle's last sweep, which
       // writes y anyway (one pass over the fine grid fewer)
       if (budget >= 1 && inner.fused_ok()) {
+        // z = 2^-e y; sum(z) from the FP32 sum of y (reference gauge: the
+        // projection's mean), <z, q_old> in FP64; sum(q_old) is the last
+        // direction pass's (qsum)
         const bool use_q = !fresh;
-        const double rn = r_norm;
-        o = inner.solve_fused(R, budget, [&](int k, IS yk) {
-          const double zk = rn * (double)yk;
+        const int e = e_rhs;
+        const double s2i = ldexp(1.0, -e);
+        IS ysum = IS(0);
+        o = inner.solve_fused(R, budget, rhs_ready, [&](int k, IS yk) {
+          const double zk = mg_out(yk, e, s2i);
           z[k] = zk;
-          zs[0] = fma(1.0, zk, zs[0]);
-          if (use_q) {
-            const double qk = qv[k];
-            zs[1] = fma(zk, qk, zs[1]);
-            zs[2] += qk;
-          }
+          if (!pinned) ysum += yk;
+          if (use_q) zs[1] = fma(zk, qv[k], zs[1]);
         });
+        zs[0] = (double)ysum * s2i;
+        zs[2] = 0.0;
         zdone = true;
       }
     }
@@ -940,8 +1016,9 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     double sb[2];
     if (!R.sum_map<3, 2>(zs, sb, [&](const double* w, double* o) {
           const double sh = pinned ? 0.0 : w[0] * inv_apsum - rse;
+          const double qs = zdone ? qsum : w[2];  // sum(q_old)
           o[0] = sh;
-          o[1] = fresh ? 0.0 : (w[1] - sh * w[2]) * inv_sigma_old;
+          o[1] = fresh ? 0.0 : (w[1] - sh * qs) * inv_sigma_old;
         })) {
       ok = false;
       break;
@@ -950,7 +1027,10 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     // p = z - beta p_old, q = A z - beta q_old, and <p,q>, <p,r> from the
     // formed vectors: the algebraic expansion of <p,q> cancels badly when
     // consecutive directions are dominated by the same smooth mode.
-    double acc[2] = {0.0, 0.0};
+    bool carry = false;
+    if constexpr (kCarry) carry = inner.fused_ok();
+    const bool want_qsum = carry && !pinned;
+    double acc[3] = {0.0, 0.0, 0.0};
     const bool was_fresh = fresh;
     own.each([&](int k, int c) {
       double wk = (k == pk) ? 0.0 : own.stencil(k, c, z, a.ax, a.ay, a.aP);
@@ -964,27 +1044,38 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
       qv[k] = qk_;
       acc[0] = fma(pk_, qk_, acc[0]);
       acc[1] = fma(pk_, r[k], acc[1]);
+      if (want_qsum) acc[2] += qk_;
     });
-    double sa[3];
-    if (!R.sum_map<2, 3>(acc, sa, [&](const double* w, double* o) {
+    double sa[4];
+    if (!R.sum_map<3, 4>(acc, sa, [&](const double* w, double* o) {
           o[0] = w[0];
           o[1] = w[0] > 0.0 ? w[1] / w[0] : 0.0;
           o[2] = w[0] > 0.0 ? 1.0 / w[0] : 0.0;
+          o[3] = w[2];
         })) {
       ok = false;
       break;
     }
+    qsum = sa[3];
     const double sigma = sa[0];
     if (!(sigma > 0.0)) { status = COVOF_BREAKDOWN; break; }
     const double alpha = sa[1];
+    // the next inner right-hand side (multigrid): (r_new - c_new) 2^e with
+    // 2^e ||r_old|| in [1, 2)
+    const double cnext = pinned ? 0.0 : fma(-alpha * qsum, inv_apsum, cdef);
+    const int e_next = pow2_exp(r_norm);
+    const double s2n = ldexp(1.0, e_next);
+    const IS csn = mg_rhs_const(cnext, e_next, IS(0));
     double acc2[2] = {0.0, 0.0};
-    own.each([&](int k, int) {
+    own.each([&](int k, int c) {
       x[k] = fma(alpha, pv[k], x[k]);
       const double rk = fma(-alpha, qv[k], r[k]);
       r[k] = rk;
       acc2[0] = fma(rk, rk, acc2[0]);
       acc2[1] += rk;
+      if (carry) inner.set_rhs(k, c, (k == pk) ? IS(0) : mg_rhs(rk, csn, s2n, e_next));
     });
+    if (carry) e_rhs = e_next;
     double t2[5];
     if (!R.sum_map<2, 5>(acc2, t2, [&](const double* w, double* o) {
           residual_scalars(w[0], w[1], b_norm, o);
@@ -995,6 +1086,7 @@ __device__ void fcg_mixed(const PoissonArgs& a, const Own& own, Inner& inner, Gr
     r_norm = t2[0]; rse = t2[1]; rel = t2[2]; cdef = t2[3]; inv_r = t2[4];
     inv_sigma_old = sa[2];
     fresh = false;
+    carried = carry;
   }
   // mean removal (reference gauge)
   if (ok && !a.pinned) {
@@ -1859,11 +1951,12 @@ struct MgInnerT {
   __device__ __forceinline__ bool fused_ok() const { return H.nl >= 2; }
   // One V-cycle whose last level-0 sweep hands each value y(k) to epi; no
   // closing barrier (the caller reduces what epi accumulated)
+  // (rhs_synced: a grid barrier already followed the right-hand side's writes)
   template <class Epi>
-  __device__ PcgOut solve_fused(GridReducer& R, int budget, Epi epi) {
+  __device__ PcgOut solve_fused(GridReducer& R, int budget, bool rhs_synced, Epi epi) {
     PcgOut o{0, COVOF_OK, 0.0, 1.0, true};
     if (budget < 1) return o;
-    const bool ok = R.gs.sync() && vcycle<true, Epi>(R, epi);
+    const bool ok = (rhs_synced || R.gs.sync()) && vcycle<true, Epi>(R, epi);
     o.iters = 1;
     if (!ok) { o.ok = false; o.status = COVOF_TIMEOUT; }
     return o;
