@@ -126,9 +126,11 @@ int ensure_poisson(covof_handle* h) {
     c.nx = (H.lv[H.nl - 1].nx + 1) / 2;
     c.ny = (H.lv[H.nl - 1].ny + 1) / 2;
     c.off = pool;
-    pool += 6LL * (c.nx + 2) * (c.ny + 2);
+    pool += 7LL * (c.nx + 2) * (c.ny + 2);
     H.nl += 1;
   }
+  H.wd0_off = pool;
+  pool += (long long)g;
   // the tail: from the first level of at most p_mg_tail cells whose levels
   // down to the coarsest (seven fields each) fit in kMgTailSmem bytes of
   // shared memory

@@ -1484,7 +1484,7 @@ struct MgLvT {
   int nx, ny, P;
   T *xa, *xb, *b;
   const T *ax, *ay, *dg;
-  const T* wd;  // tail levels: omega / dg (the sweeps multiply instead of dividing)
+  const T* wd;  // omega / dg (the sweeps multiply instead of dividing)
   __device__ __forceinline__ int id(int i, int j) const { return j * P + i; }
 };
 
@@ -1497,6 +1497,7 @@ struct MgInnerT {
   MgHier H;
   T *x0a, *x0b, *b0;   // level 0 solution buffers and right-hand side
   const T *ax0, *ay0, *dg0;  // level 0: FP32 copy of A (faces, diagonal)
+  T* wd0;              // level 0: omega / dg0 (formed in setup)
   T* sm;               // block 0: tail levels (7 fields each), H.tail_smem bytes
   MgLvT<T>* tab;               // this block's shared table of the level views, built in setup
   // level l in global memory (S = false) or, for tail levels, in block 0's
@@ -1509,7 +1510,7 @@ struct MgInnerT {
     const size_t g = (size_t)(L.nx + 2) * (size_t)(L.ny + 2);
     L.wd = nullptr;
     if (l == 0) {
-      L.xa = x0a; L.xb = x0b; L.b = b0; L.ax = ax0; L.ay = ay0; L.dg = dg0;
+      L.xa = x0a; L.xb = x0b; L.b = b0; L.ax = ax0; L.ay = ay0; L.dg = dg0; L.wd = wd0;
       return L;
     }
     T* base;
@@ -1520,6 +1521,7 @@ struct MgInnerT {
       L.wd = base + 6 * g;
     } else {
       base = static_cast<T*>(H.pool) + H.lv[l].off;
+      L.wd = base + 6 * g;
     }
     L.xa = base; L.xb = base + g; L.b = base + 2 * g;
     L.ax = base + 3 * g; L.ay = base + 4 * g; L.dg = base + 5 * g;
@@ -1564,23 +1566,13 @@ struct MgInnerT {
     const MgLvT<T> L = lv(l, S);
     const T* xs = cur ? L.xb : L.xa;
     T* xd = cur ? L.xa : L.xb;
-    const T w = H.omega;
     const int pin = l == 0 ? pk : -1;
     cells<S, W>(L.nx, L.ny, [&](int i, int j) {
       const int k = L.id(i, j);
-      T v;
-      if constexpr (S) {
-        // shared-memory levels: a multiply by omega / dg (block 0's
-        // sequential tail is bound by the dependent chain, not by memory)
-        const T q = L.wd[k];
-        if (first) v = ld<S>(L.b + k) * q;
-        else v = ld<S>(xs + k) + (ld<S>(L.b + k) - apply<S>(L, xs, k)) * q;
-      } else {
-        const T d = L.dg[k];
-        if (first) v = w * ld<S>(L.b + k) / d;
-        else v = ld<S>(xs + k) + w * (ld<S>(L.b + k) - apply<S>(L, xs, k)) / d;
-      }
-      if (k == pin) v = T(0);
+      // a multiply by omega / dg, formed once per solve in setup
+      const T q = L.wd[k];
+      const T v0 = first ? ld<S>(L.b + k) * q : ld<S>(xs + k) + (ld<S>(L.b + k) - apply<S>(L, xs, k)) * q;
+      const T v = k == pin ? T(0) : v0;
       xd[k] = v;
       epi(k, v);
     });
@@ -1594,7 +1586,6 @@ struct MgInnerT {
     const MgLvT<T> F = lv(l, S), Cc = lv(l + 1, S);
     const T* x = cur ? F.xb : F.xa;
     const int pin = l == 0 ? pk : -1;
-    const T w = H.omega;
     cells<S>(Cc.nx, Cc.ny, [&](int I, int J) {
       T s = T(0);
       for (int dj = 0; dj < 2; ++dj)
@@ -1607,7 +1598,7 @@ struct MgInnerT {
         }
       const int kc = Cc.id(I, J);
       Cc.b[kc] = s;
-      if (first_next) Cc.xb[kc] = w * s / Cc.dg[kc];
+      if (first_next) Cc.xb[kc] = s * Cc.wd[kc];
     });
   }
   // x_l (buffer cl) += cw * x_{l+1} (buffer cc) at the parent cell
@@ -1632,6 +1623,15 @@ struct MgInnerT {
     __syncthreads();  // a previous case of this block is done with the table
     for (int q = threadIdx.x; q < 2 * H.nl; q += blockDim.x) tab[q] = lv_make(q >> 1, (q & 1) != 0);
     __syncthreads();
+    {
+      const MgLvT<T> F = lv(0);
+      cells<false>(F.nx, F.ny, [&](int i, int j) {
+        const int k = F.id(i, j);
+        const T d = F.dg[k];
+        wd0[k] = d != T(0) ? T(H.omega) / d : T(0);
+      });
+      if (H.nl == 1 && !R.gs.sync()) return false;
+    }
     for (int l = 1; l < H.nl; ++l) {
       const MgLvT<T> F = lv(l - 1), Cc = lv(l);
       T* cax = const_cast<T*>(Cc.ax);
@@ -1663,7 +1663,9 @@ struct MgInnerT {
             internal = T(0);
             if (i0 + 1 <= F.nx && j0 + 1 <= F.ny) internal = axf(i0 + 1, j0 + 1) + ayf(i0 + 1, j0 + 1);
           }
-          cdg[k] = d - T(2) * internal;
+          const T dc = d - T(2) * internal;
+          cdg[k] = dc;
+          const_cast<T*>(Cc.wd)[k] = dc != T(0) ? T(H.omega) / dc : T(0);
         }
       });
       if (!R.gs.sync()) return false;
@@ -1751,10 +1753,10 @@ struct MgInnerT {
     __syncthreads();
   }
   // the right-hand side, and with it the first level-0 sweep from x = 0
-  // (w b / dg into x0b, bit for bit what sweep<false>(0, true, 0) writes)
+  // (b w / dg into x0b, bit for bit what sweep<false>(0, true, 0) writes)
   __device__ __forceinline__ void set_rhs(int k, int, T v) {
     b0[k] = v;
-    x0b[k] = k == pk ? T(0) : H.omega * v / dg0[k];
+    x0b[k] = k == pk ? T(0) : v * wd0[k];
   }
   __device__ __forceinline__ T y(int k, int) const { return k == pk ? T(0) : __ldcg(x0a + k); }
   // The nuc sweeps of a coarsest level of at most 64 cells in the first
@@ -2001,6 +2003,7 @@ __device__ void mg_case(const PoissonArgs& a, const Team& tm, GridReducer& R, T*
   } else {
     in.x0a = a.d; in.x0b = a.d2; in.b0 = a.Ad; in.ax0 = a.ax; in.ay0 = a.ay; in.dg0 = a.aP;
   }
+  in.wd0 = static_cast<T*>(a.mg.pool) + a.mg.wd0_off;
   in.sm = tail;
   in.tab = tab;
   if (!in.setup(R)) {

@@ -13,10 +13,12 @@ struct PcgResult {
 };
 
 // Geometric multigrid hierarchy of the flexible CG's inner V-cycle (levels
-// 1 .. nl-1; level 0 is the fine operator itself).  Level l owns 6 arrays of
+// 1 .. nl-1; level 0 is the fine operator itself).  Level l owns 7 arrays of
 // (nx+2)*(ny+2) elements at pool + off (elements of the V-cycle's arithmetic:
 // float on the mixed path, double for COVOF_PREC_FP64_MG): two solution
-// buffers, right-hand side, west / south face coefficients, diagonal.
+// buffers, right-hand side, west / south face coefficients, diagonal, and
+// omega / diagonal (the sweeps multiply instead of dividing); level 0's
+// omega / diagonal is at pool + wd0_off.
 constexpr int kMgMaxLevels = 16;
 constexpr long long kMgTailSmem = 200 * 1024;  // cap on the shared-memory tail (plus ~6 KB static)
 constexpr long long kMgWarpCoarse = 256;        // coarsest levels this small run in one warp
@@ -29,6 +31,7 @@ struct MgHier {
   int nl;      // levels including level 0
   int tail;    // first level run by block 0 alone out of shared memory, nl if none
   void* pool;  // float or double elements, by the V-cycle's arithmetic
+  long long wd0_off;  // level 0's omega / diagonal, (nx+2)*(ny+2) elements
   float omega; // Jacobi weight
   float cw;    // coarse-correction weight
   int nu, nuc; // sweeps before / after each coarse correction; sweeps on the coarsest level
