@@ -453,7 +453,8 @@ def mono_steps(pkg, orc, n, nsteps, cpu_steps):
 def vof_steps(pkg, orc, reps):
     """The VOF path on its own: ELVIRA reconstruction and whole Weymouth-Yue
     steps (two direction passes) on device fields for the C1 bubble
-    (128x256, 16x16 sub-samples) and the same bubble at 1024x2048.  The
+    (128x256, 16x16 sub-samples), the same bubble at 1024x2048, and a 64 x 64
+    array of droplets at 4096^2 (about 0.5 M interface cells).  The
     reconstruction is FP64 polygon clipping: its FP64 rate is estimated from
     the interface cells (371 cut-box evaluations of ~60 flops per interface
     cell) and set against the FP64 rate this GPU sustains on independent
@@ -462,8 +463,15 @@ def vof_steps(pkg, orc, reps):
     import torch
     cap = pkg.capi
     out = {"model": "FP64 work = interface cells x 371 cut_box_area x 60 flops per reconstruction"}
-    for nx, ny, nsub in ((128, 256, 16), (1024, 2048, 4)):
-        p, C0, dt = pkg.cases.bubble_case(nx=nx, ny=ny, nsub=nsub)
+    def bubble(nx, ny, nsub):
+        p, C0, _ = pkg.cases.bubble_case(nx=nx, ny=ny, nsub=nsub)
+        return p, C0
+
+    legs = [("128x256", lambda: bubble(128, 256, 16)), ("1024x2048", lambda: bubble(1024, 2048, 4)),
+            ("4096x4096_droplets", lambda: pkg.cases.droplet_array(4096, 64, 20.0))]
+    for label, make in legs:
+        p, C0 = make()
+        nx, ny = p.nx, p.ny
         f = pkg.Fields.allocate(p)
         f.C[...] = C0
         f.u[...], f.v[...] = pkg.cases.random_velocity(p, 0.05, 7)
@@ -496,7 +504,7 @@ def vof_steps(pkg, orc, reps):
                     wy.append(e1.elapsed_time(e2))
         rms = statistics.mean(rec)
         gf = mixed * 371.0 * 60.0 / (rms * 1e-3) / 1e9
-        out[f"{nx}x{ny}"] = {"interface_cells": mixed, "reconstruct_ms": rms, "wy_step_ms": statistics.mean(wy),
+        out[label] = {"interface_cells": mixed, "reconstruct_ms": rms, "wy_step_ms": statistics.mean(wy),
                              "reconstruct_fp64_gflops_est": gf, "fp64_peak_gflops_measured": peak,
                              "frac": gf / peak}
     return out

@@ -94,7 +94,8 @@ class RunStats(C.Structure):
 
 class Launch(C.Structure):
     """covof_launch (include/covof_gpu.h)."""
-    _fields_ = [("p_threads", C.c_int), ("p_blocks", C.c_int), ("p_inner_form", C.c_int)]
+    _fields_ = [("p_threads", C.c_int), ("p_blocks", C.c_int), ("p_inner_form", C.c_int),
+                ("vof_cell_min", C.c_int)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

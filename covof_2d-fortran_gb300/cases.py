@@ -232,6 +232,30 @@ def random_velocity(p: Params, scale: float, seed: int):
     return u, v
 
 
+def droplet_array(n: int = 4096, k: int = 64, r_cells: float = 20.0, seed: int = SEED + 6):
+    """A k x k array of gas droplets in liquid on the unit square at n x n
+    cells, one per (n/k)^2 block with a seeded centre jitter, radius r_cells
+    cells: about 2 pi r_cells k^2 interface cells (650k at the defaults), the
+    regime where the reconstruction's throughput, not one cell's latency,
+    sets its time.  C (liquid fraction) is the signed distance to the
+    block's droplet across one cell, clipped to [0, 1] (values strictly
+    between 0 and 1 only in the interface band).  Returns (params, C)."""
+    p = make_params(n, n, 1.0, 1.0)
+    rng = np.random.default_rng(seed)
+    b = n // k
+    jit = rng.uniform(-0.15, 0.15, size=(k, k, 2)) * b
+    C = np.ones((n + 2, n + 2), dtype=np.float64)
+    ci = np.arange(n) + 0.5
+    blk = np.minimum(np.arange(n) // b, k - 1)
+    cx = (blk[None, :] + 0.5) * b + jit[blk[:, None], blk[None, :], 0]
+    cy = (blk[:, None] + 0.5) * b + jit[blk[:, None], blk[None, :], 1]
+    d = np.hypot(ci[None, :] - cx, ci[:, None] - cy)
+    C[1:-1, 1:-1] = np.clip(d - r_cells + 0.5, 0.0, 1.0)
+    p.enable_two_phase = 1
+    p.recon = capi.RECON_ELVIRA
+    return p, C
+
+
 def droplet_batch(n_cases: int = 256, seed: int = SEED + 4, sizes=(64, 128, 256, 512), nsub: int = 4,
                   mixed: bool = True, shapes=None):
     """Independent droplet / bubble cases: nx, ny drawn from sizes, square

@@ -186,6 +186,11 @@ int ensure_mom(covof_handle* h) {
   return COVOF_OK;
 }
 
+// interface cells from which the reconstruction runs one thread per cell
+int vof_cell_min(const covof_handle* h) {
+  return h->launch.vof_cell_min > 0 ? h->launch.vof_cell_min : kVofCellMin;
+}
+
 int ensure_vof(covof_handle* h) {
   if (h->have_vof) return COVOF_OK;
   const size_t g = h->g;
@@ -201,6 +206,9 @@ int ensure_vof(covof_handle* h) {
   const int cap = per_sm * h->sm_count;
   if (cap < 1) return COVOF_CUDA_ERROR;
   h->svof_nb = nb < cap ? nb : cap;
+  // the thread-per-cell reconstruction: every block resident, grid-stride
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_vof_mixed_cell, 128, 0));
+  h->vof_cell_nb = (per_sm < 1 ? 1 : per_sm) * h->sm_count;
   h->have_vof = true;
   return COVOF_OK;
 }
@@ -917,8 +925,11 @@ VofArgs vof_args(covof_handle* h, double dt, const double* C, const double* Cn, 
   return a;
 }
 
-// Pure cells directly, interface cells one warp each (list built on the
-// device, so nothing here waits for the host), then the ghost ring.
+// Pure cells directly, interface cells one warp each -- or, from
+// vof_cell_min(h) interface cells on, one thread each: both kernels are
+// launched and the one that does not match the device-side count returns at
+// once (the list is built on the device, so nothing here waits for the
+// host) -- then the ghost ring.
 int reconstruct_dev(covof_handle* h, const double* C, double* seg_out) {
   CS(check_periodic_vof(h->prm));
   CS(ensure_vof(h));
@@ -927,7 +938,9 @@ int reconstruct_dev(covof_handle* h, const double* C, double* seg_out) {
   const dim3 blk(32, 4), grd = grid2(h->D.nx + 2, h->D.ny + 2, blk);
   CK(cudaMemsetAsync(h->vcount, 0, sizeof(int), h->stream));
   k_vof_classify<<<grd, blk, 0, h->stream>>>(a, h->vlist, h->vcount);
-  k_vof_mixed<<<4 * h->sm_count, 128, 0, h->stream>>>(a, h->vlist, h->vcount);
+  const int cmin = vof_cell_min(h);
+  k_vof_mixed<<<4 * h->sm_count, 128, 0, h->stream>>>(a, h->vlist, h->vcount, cmin);
+  k_vof_mixed_cell<<<h->vof_cell_nb, 128, 0, h->stream>>>(a, h->vlist, h->vcount, cmin);
   const int nring = 2 * h->D.ny + 2 * (h->D.nx + 2);
   k_vof_ring_warp<<<(nring + 3) / 4, 128, 0, h->stream>>>(a);
   CK(cudaGetLastError());
@@ -1963,7 +1976,7 @@ int covof_set_launch(covof_handle* h, const covof_launch* launch) {
   if (L.p_threads != 0 && L.p_threads != 128 && L.p_threads != 256 && L.p_threads != 512 && L.p_threads != 1024)
     return COVOF_INVALID;
   if (L.p_blocks < 0 || L.p_blocks > h->sm_count || L.p_inner_form < 0 || L.p_inner_form > 3 ||
-      (L.p_inner_form == 3 && L.p_blocks > 16))
+      (L.p_inner_form == 3 && L.p_blocks > 16) || L.vof_cell_min < 0)
     return COVOF_INVALID;
   if (h->stream) cudaStreamSynchronize(h->stream);
   const covof_launch keep = h->launch;
@@ -1987,6 +2000,7 @@ int covof_get_launch(covof_handle* h, covof_launch* launch) {
   launch->p_inner_form = h->p_fn == (const void*)k_pcg_mixed_cheb ? 1
                        : h->p_fn == (const void*)k_pcg_mixed_stream ? 2
                        : h->p_fn == (const void*)k_pcg_mixed_cluster ? 3 : 0;
+  launch->vof_cell_min = vof_cell_min(h);
   return COVOF_OK;
 }
 

@@ -41,6 +41,7 @@ namespace host {
 constexpr int kPoissonThreads = 1024;  // one cell per thread per 1024-cell tile
 constexpr int kKrylovThreads = 512;    // momentum Krylov kernels (64 registers)
 constexpr int kKrylovBlocksPerSm = 2;  // co-resident momentum Krylov blocks per SM
+constexpr int kVofCellMin = 16384;   // interface cells from which reconstruction runs a thread per cell
 constexpr int kMaxPartRegions = 16;  // doubles per block in the partials array
 
 template <typename T>
@@ -110,6 +111,7 @@ struct covof_handle {
   void* writer = nullptr;               // snapshot output state (output.cu)
   unsigned int* svof_prog = nullptr;  // SVOF band progress (32 words per band)
   int svof_nb = 0;                    // blocks of the SVOF launch (planned by ensure_vof)
+  int vof_cell_nb = 0;                // blocks of the thread-per-cell reconstruction (ensure_vof)
   // caller-field mirrors (host-pointer entry points)
   bool have_fields = false;
   double *f_u = nullptr, *f_v = nullptr, *f_p = nullptr, *f_rho_u = nullptr, *f_rho_v = nullptr,

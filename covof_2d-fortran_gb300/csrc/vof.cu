@@ -162,17 +162,20 @@ __global__ void k_vof_classify(VofArgs a, int* __restrict__ list, int* __restric
   if (mixed) list[base + __popc(bal & ((1u << lane) - 1u))] = k;
 }
 
-// One warp per listed cell.  ELVIRA (inner cells): candidate q on lanes
-// 4q .. 4q+3 (lanes 28-31 repeat candidate 6 and are ignored); its
-// bisection runs 2 levels per round, its 8 neighbour clips 2 per lane, and
-// the error is summed and the candidate chosen in the reference order.
-// PLIC, and ELVIRA on ghost cells: one normal, 5 levels per round.
+// One warp per listed cell, for lists shorter than max_count (the
+// thread-per-cell form below takes the longer ones).  ELVIRA (inner cells):
+// candidate q on lanes 4q .. 4q+3 (lanes 28-31 repeat candidate 6 and are
+// ignored); its bisection runs 2 levels per round, its 8 neighbour clips 2
+// per lane, and the error is summed and the candidate chosen in the
+// reference order.  PLIC, and ELVIRA on ghost cells: one normal, 5 levels
+// per round.
 __global__ void __launch_bounds__(128) k_vof_mixed(VofArgs a, const int* __restrict__ list,
-                                                    const int* __restrict__ count) {
+                                                    const int* __restrict__ count, int max_count) {
   const VMesh m{a.D, a.dx, a.dy};
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int n = *count;
+  if (n >= max_count) return;
   const int nx = a.D.nx, ny = a.D.ny;
   const double* __restrict__ C = a.C;
   const double dx = a.dx, dy = a.dy;
@@ -262,6 +265,114 @@ __global__ void __launch_bounds__(128) k_vof_mixed(VofArgs a, const int* __restr
       if (vq && eq < best_err) { best_err = eq; bnx = xq; bny = yq; ba = aq; }
     }
     if (lane == 0) put_seg(a.seg, k, bnx, bny, ba);
+  }
+}
+
+// compute_alpha (src/module_interface_reconstruction.f90:105-147) as the
+// serial 45-step bisection, one thread.
+__device__ double serial_alpha(double xmin, double xmax, double ymin, double ymax, double nx, double ny,
+                               double c_target) {
+  const double total = (xmax - xmin) * (ymax - ymin);
+  if (c_target <= 1.0e-7) return 1.0e9;
+  if (c_target >= 1.0 - 1.0e-7) return -1.0e9;
+  const double target = fmax(0.0, fmin(1.0, c_target)) * total;
+  const double v1 = nx * xmin + ny * ymin;
+  const double v2 = nx * xmax + ny * ymin;
+  const double v3 = nx * xmax + ny * ymax;
+  const double v4 = nx * xmin + ny * ymax;
+  const double mn = fmin(v1, fmin(v2, fmin(v3, v4)));
+  const double mx = fmax(v1, fmax(v2, fmax(v3, v4)));
+  double lo = -mx - 1.0e-12;
+  double hi = -mn + 1.0e-12;
+  for (int it = 0; it < 45; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (cut_box_area(xmin, xmax, ymin, ymax, nx, ny, mid) < target) hi = mid;
+    else lo = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+// One thread per listed cell, for lists of at least min_count cells.  A
+// warp instruction on the FP64 pipe costs the same whatever its active
+// lanes, and the warp form spends lanes on idle tree nodes and on 1.5
+// clips per bisection level; once the interface cells fill every warp slot
+// of the GPU, the serial form (32 cells per warp, one clip per level) does
+// the same work in fewer FP64 warp instructions.  Same arithmetic, same
+// order: bit-identical to the warp form and to the serial reference.
+__global__ void __launch_bounds__(128) k_vof_mixed_cell(VofArgs a, const int* __restrict__ list,
+                                                        const int* __restrict__ count, int min_count) {
+  const VMesh m{a.D, a.dx, a.dy};
+  const int n = *count;
+  if (n < min_count) return;
+  const int nx = a.D.nx, ny = a.D.ny;
+  const double* __restrict__ C = a.C;
+  const double dx = a.dx, dy = a.dy;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int k = list[e];
+    const int j = k / a.D.P, i = k - j * a.D.P;
+    const double c = C[k];
+    const double xmin = m.xf(i), xmax = m.xf(i + 1), ymin = m.yf(j), ymax = m.yf(j + 1);
+    const bool inner = (i >= 1 && i <= nx && j >= 1 && j <= ny);
+    if (inner && a.D.nbhd(k, 23) != k) continue;
+    auto Cq = [&](int p, int q) { return C[a.D.id(p, q)]; };
+    if (a.method != COVOF_RECON_ELVIRA || !inner) {
+      double pnx = 1.0, pny = 0.0;
+      if (a.method != COVOF_RECON_ELVIRA && inner) {
+        const double cmm = Cq(i - 1, j - 1), c0m = Cq(i, j - 1), cpm = Cq(i + 1, j - 1);
+        const double cm0 = Cq(i - 1, j), cp0 = Cq(i + 1, j);
+        const double cmp = Cq(i - 1, j + 1), c0p = Cq(i, j + 1), cpp = Cq(i + 1, j + 1);
+        const double mxv = -((cpp + 2.0 * cp0 + cpm) - (cmp + 2.0 * cm0 + cmm)) / (8.0 * dx);
+        const double myv = -((cpp + 2.0 * c0p + cmp) - (cpm + 2.0 * c0m + cmm)) / (8.0 * dy);
+        const double nrm = fhypot(mxv, myv);
+        if (nrm > 1.0e-12) { pnx = mxv / nrm; pny = myv / nrm; }
+      } else if (a.method != COVOF_RECON_ELVIRA) {
+        const double nrm = fhypot(1.0, 0.0);
+        pnx = 1.0 / nrm; pny = 0.0 / nrm;
+      }
+      put_seg(a.seg, k, pnx, pny, serial_alpha(xmin, xmax, ymin, ymax, pnx, pny, c));
+      continue;
+    }
+    const double Hm1 = (Cq(i - 1, j - 1) + Cq(i - 1, j) + Cq(i - 1, j + 1)) * dy;
+    const double H0 = (Cq(i, j - 1) + Cq(i, j) + Cq(i, j + 1)) * dy;
+    const double Hp1 = (Cq(i + 1, j - 1) + Cq(i + 1, j) + Cq(i + 1, j + 1)) * dy;
+    const double Wm1 = (Cq(i - 1, j - 1) + Cq(i, j - 1) + Cq(i + 1, j - 1)) * dx;
+    const double W0 = (Cq(i - 1, j) + Cq(i, j) + Cq(i + 1, j)) * dx;
+    const double Wp1 = (Cq(i - 1, j + 1) + Cq(i, j + 1) + Cq(i + 1, j + 1)) * dx;
+    const double sgy = (Cq(i, j + 1) < Cq(i, j - 1)) ? 1.0 : -1.0;
+    const double sgx = (Cq(i + 1, j) < Cq(i - 1, j)) ? 1.0 : -1.0;
+    double best_err = 1.0e30, bnx = 1.0, bny = 0.0, ba = 0.0;
+    for (int q = 0; q < 7; ++q) {
+      double cnx, cny;
+      switch (q) {
+        case 0: cnx = -sgy * (Hp1 - Hm1) / (2.0 * dx); cny = sgy * 1.0; break;
+        case 1: cnx = -sgy * (Hp1 - H0) / (dx); cny = sgy * 1.0; break;
+        case 2: cnx = -sgy * (H0 - Hm1) / (dx); cny = sgy * 1.0; break;
+        case 3: cnx = sgx * 1.0; cny = -sgx * (Wp1 - Wm1) / (2.0 * dy); break;
+        case 4: cnx = sgx * 1.0; cny = -sgx * (Wp1 - W0) / (dy); break;
+        case 5: cnx = sgx * 1.0; cny = -sgx * (W0 - Wm1) / (dy); break;
+        default:
+          cnx = -((Cq(i + 1, j + 1) + 2.0 * Cq(i + 1, j) + Cq(i + 1, j - 1)) -
+                  (Cq(i - 1, j + 1) + 2.0 * Cq(i - 1, j) + Cq(i - 1, j - 1))) / (8.0 * dx);
+          cny = -((Cq(i + 1, j + 1) + 2.0 * Cq(i, j + 1) + Cq(i - 1, j + 1)) -
+                  (Cq(i + 1, j - 1) + 2.0 * Cq(i, j - 1) + Cq(i - 1, j - 1))) / (8.0 * dy);
+          break;
+      }
+      const double cn = fhypot(cnx, cny);
+      if (cn < 1.0e-12) continue;
+      const double ux = cnx / cn, uy = cny / cn;
+      const double ca = serial_alpha(xmin, xmax, ymin, ymax, ux, uy, c);
+      double err = 0.0;
+      for (int dj = -1; dj <= 1; ++dj)
+        for (int di = -1; di <= 1; ++di) {
+          if (di == 0 && dj == 0) continue;
+          const double vt = Cq(i + di, j + dj) * dx * dy;
+          const double vr = cut_box_area(m.xf(i + di), m.xf(i + di + 1), m.yf(j + dj), m.yf(j + dj + 1), ux, uy, ca);
+          const double df = vr - vt;
+          err = err + df * df;
+        }
+      if (err < best_err) { best_err = err; bnx = ux; bny = uy; ba = ca; }
+    }
+    put_seg(a.seg, k, bnx, bny, ba);
   }
 }
 

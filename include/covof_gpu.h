@@ -526,6 +526,9 @@ typedef struct covof_launch {
   int p_inner_form;  /* mixed Chebyshev inner state: 1 shared-memory strips on every SM,
                       * 2 streamed through L2 / HBM, 3 one thread-block cluster of p_blocks
                       * (<= 16) CTAs exchanging rows through distributed shared memory */
+  int vof_cell_min;  /* interface reconstruction: from this many interface cells on, one
+                      * thread per cell instead of one warp per cell (same results bit for
+                      * bit); 0 = the built-in 16384 */
 } covof_launch;
 /* Set the overrides (validated: COVOF_INVALID for out-of-range values,
  * COVOF_UNSUPPORTED for shared-memory strips that do not fit); drops the

@@ -45,6 +45,31 @@ def test_reconstruct_bit_exact(gpu_pkg, orc, recon):
 
 
 @pytest.mark.parametrize("recon", ["PLIC", "ELVIRA"])
+def test_reconstruct_thread_per_cell_form_bit_exact(gpu_pkg, orc, recon):
+    """The thread-per-cell reconstruction (long interface lists) forced on
+    small cases through covof_launch.vof_cell_min = 1: bit-identical to the
+    oracle, bubble and ragged random fields (ghost-ring cells in the list);
+    the handle reports the threshold it uses, the built-in 16384 by default."""
+    import ctypes
+    pkg = gpu_pkg
+    cap = pkg.capi
+    p, f, _ = _bubble(pkg, orc)
+    p.recon = getattr(cap, "RECON_" + recon)
+    q = pkg.cases.make_params(37, 37, 1.0, 1.0)
+    q.recon = p.recon
+    for prm, Cf in ((p, f.C), (q, _random_C(37, 2)), (q, _random_C(37, 5))):
+        with pkg.Solver(prm) as s:
+            G = cap.Launch()
+            assert s.lib.covof_get_launch(s.h, ctypes.byref(G)) == cap.OK and G.vof_cell_min == 16384
+            L = cap.Launch(p_threads=0, p_blocks=0, p_inner_form=0, vof_cell_min=1)
+            assert s.lib.covof_set_launch(s.h, ctypes.byref(L)) == cap.OK
+            assert np.array_equal(s.reconstruct_interface(Cf), orc.reconstruct(prm, Cf))
+    with pkg.Solver(q) as s:
+        bad = cap.Launch(p_threads=0, p_blocks=0, p_inner_form=0, vof_cell_min=-1)
+        assert s.lib.covof_set_launch(s.h, ctypes.byref(bad)) == cap.INVALID
+
+
+@pytest.mark.parametrize("recon", ["PLIC", "ELVIRA"])
 @pytest.mark.parametrize("x_first", [True, False])
 def test_wy_step_bit_exact(gpu_pkg, orc, recon, x_first):
     pkg = gpu_pkg
