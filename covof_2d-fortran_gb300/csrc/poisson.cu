@@ -1485,6 +1485,7 @@ struct MgLvT {
   T *xa, *xb, *b;
   const T *ax, *ay, *dg;
   const T* wd;  // omega / dg (the sweeps multiply instead of dividing)
+  T* xs;        // tail levels: a W-cycle's first coarse correction, kept over its second visit
   __device__ __forceinline__ int id(int i, int j) const { return j * P + i; }
 };
 
@@ -1498,7 +1499,7 @@ struct MgInnerT {
   T *x0a, *x0b, *b0;   // level 0 solution buffers and right-hand side
   const T *ax0, *ay0, *dg0;  // level 0: FP32 copy of A (faces, diagonal)
   T* wd0;              // level 0: omega / dg0 (formed in setup)
-  T* sm;               // block 0: tail levels (7 fields each), H.tail_smem bytes
+  T* sm;               // block 0: tail levels (8 fields each), H.tail_smem bytes
   MgLvT<T>* tab;               // this block's shared table of the level views, built in setup
   // level l in global memory (S = false) or, for tail levels, in block 0's
   // shared memory (S = true): one read of the block's table (the views are
@@ -1509,16 +1510,19 @@ struct MgInnerT {
     L.nx = H.lv[l].nx; L.ny = H.lv[l].ny; L.P = L.nx + 2;
     const size_t g = (size_t)(L.nx + 2) * (size_t)(L.ny + 2);
     L.wd = nullptr;
+    L.xs = nullptr;
     if (l == 0) {
       L.xa = x0a; L.xb = x0b; L.b = b0; L.ax = ax0; L.ay = ay0; L.dg = dg0; L.wd = wd0;
       return L;
     }
     T* base;
     if (S) {
-      // shared-memory levels hold a seventh field, omega / dg
+      // shared-memory levels hold 8 fields: the grid levels' 7 and the
+      // W-cycle's saved correction
       base = sm;
-      for (int q = H.tail; q < l; ++q) base += 7 * (size_t)(H.lv[q].nx + 2) * (size_t)(H.lv[q].ny + 2);
+      for (int q = H.tail; q < l; ++q) base += 8 * (size_t)(H.lv[q].nx + 2) * (size_t)(H.lv[q].ny + 2);
       L.wd = base + 6 * g;
+      L.xs = base + 7 * g;
     } else {
       base = static_cast<T*>(H.pool) + H.lv[l].off;
       L.wd = base + 6 * g;
@@ -1852,27 +1856,12 @@ struct MgInnerT {
       if (kk[m] >= 0) L.xa[kk[m]] = x[m] - mx;
     __syncwarp();
   }
-  // the tail levels, block 0 alone out of shared memory: b_tail in from
-  // global memory, the tail's correction back out
-  __device__ void tail_cycle() const {
-    const int L = H.nl, nu = H.nu, t = H.tail;
-    {
-      const MgLvT<T> G = lv(t), Sm = lv(t, true);
-      const int g = Sm.P * (Sm.ny + 2);
-      for (int k = threadIdx.x; k < g; k += blockDim.x) Sm.b[k] = __ldcg(G.b + k);
-    }
-    __syncthreads();
-    for (int l = t; l < L - 1; ++l) {
-      for (int s = 0; s < nu; ++s) {
-        if (s > 0) __syncthreads();
-        sweep<true>(l, s == 0, s & 1);
-      }
-      __syncthreads();
-      restrict_<true>(l, nu & 1);
-      __syncthreads();
-    }
-    // the coarsest level: a small one runs in the first warp alone, so its
-    // many sweeps synchronise with __syncwarp instead of block barriers
+  // The coarsest level in block 0 (right-hand side in b, result in buffer
+  // out_buf): a small one runs in the first warp alone, so its many sweeps
+  // synchronise with __syncwarp instead of block barriers.  Ends with a
+  // block barrier.
+  __device__ void tail_coarsest() const {
+    const int L = H.nl;
     if (H.exact) {
       if (threadIdx.x < 32) coarsest_exact(L - 1);
     } else if ((long long)H.lv[L - 1].nx * H.lv[L - 1].ny <= 64) {
@@ -1890,15 +1879,94 @@ struct MgInnerT {
         sweep<true>(L - 1, s == 0, s & 1);
       }
     }
-    for (int l = L - 2; l >= t; --l) {
+    __syncthreads();
+  }
+  // A W-cycle's second visit to level l: its residual b <- b - A x and the
+  // first correction kept (x in xa); then, after the visit, x = xs + x.
+  __device__ void tail_resid_save(int l) const {
+    const MgLvT<T> L = lv(l, true);
+    cells<true>(L.nx, L.ny, [&](int i, int j) {
+      const int k = L.id(i, j);
+      const T r = L.b[k] - apply<true>(L, L.xa, k);
+      L.xs[k] = L.xa[k];
+      L.b[k] = r;
+    });
+  }
+  __device__ void tail_add_saved(int l) const {
+    const MgLvT<T> L = lv(l, true);
+    cells<true>(L.nx, L.ny, [&](int i, int j) {
+      const int k = L.id(i, j);
+      L.xa[k] = L.xs[k] + L.xa[k];
+    });
+  }
+  // Tail levels from l down as a V-cycle (block 0; b_l in, x_l out in
+  // buffer out_buf(l)).  Ends with a block barrier.
+  __device__ void tail_solve_v(int t) const {
+    const int L = H.nl, nu = H.nu;
+    for (int l = t; l < L - 1; ++l) {
+      for (int s = 0; s < nu; ++s) {
+        if (s > 0) __syncthreads();
+        sweep<true>(l, s == 0, s & 1);
+      }
       __syncthreads();
+      restrict_<true>(l, nu & 1);
+      __syncthreads();
+    }
+    tail_coarsest();
+    for (int l = L - 2; l >= t; --l) {
       prolong<true>(l, nu & 1, out_buf(l + 1));
       for (int s = 0; s < nu; ++s) {
         __syncthreads();
         sweep<true>(l, false, (nu + s) & 1);
       }
+      __syncthreads();
+    }
+  }
+  // Level l of the tail with H.gamma coarse corrections per level (2: a
+  // W-cycle, which a block-local tail affords: its extra visits cost block
+  // barriers, not grid barriers); D bounds the recursion at compile time,
+  // below it the levels run as a V-cycle.  b_l in, x_l out in buffer
+  // out_buf(l); ends with a block barrier.
+  template <int D>
+  __device__ __noinline__ void tail_solve(int l) const {
+    const int L = H.nl, nu = H.nu;
+    if (l == L - 1) { tail_coarsest(); return; }
+    for (int s = 0; s < nu; ++s) {
+      if (s > 0) __syncthreads();
+      sweep<true>(l, s == 0, s & 1);
     }
     __syncthreads();
+    restrict_<true>(l, nu & 1);
+    __syncthreads();
+    if constexpr (D > 0) tail_solve<D - 1>(l + 1);
+    else tail_solve_v(l + 1);
+    // an exact coarsest solve leaves nothing for a second visit
+    if (H.gamma > 1 && !(l + 1 == L - 1 && H.exact)) {
+      tail_resid_save(l + 1);
+      __syncthreads();
+      if constexpr (D > 0) tail_solve<D - 1>(l + 1);
+      else tail_solve_v(l + 1);
+      tail_add_saved(l + 1);
+      __syncthreads();
+    }
+    prolong<true>(l, nu & 1, out_buf(l + 1));
+    for (int s = 0; s < nu; ++s) {
+      __syncthreads();
+      sweep<true>(l, false, (nu + s) & 1);
+    }
+    __syncthreads();
+  }
+  // the tail levels, block 0 alone out of shared memory: b_tail in from
+  // global memory, the tail's correction back out
+  __device__ void tail_cycle() const {
+    const int t = H.tail;
+    {
+      const MgLvT<T> G = lv(t), Sm = lv(t, true);
+      const int g = Sm.P * (Sm.ny + 2);
+      for (int k = threadIdx.x; k < g; k += blockDim.x) Sm.b[k] = __ldcg(G.b + k);
+    }
+    __syncthreads();
+    tail_solve<kMgTailDepth>(t);
     const int pb = out_buf(t);
     const MgLvT<T> G = lv(t), Sm = lv(t, true);
     const T* src = pb ? Sm.xb : Sm.xa;

@@ -22,6 +22,7 @@ struct PcgResult {
 constexpr int kMgMaxLevels = 16;
 constexpr long long kMgTailSmem = 200 * 1024;  // cap on the shared-memory tail (plus ~6 KB static)
 constexpr long long kMgWarpCoarse = 256;        // coarsest levels this small run in one warp
+constexpr int kMgTailDepth = 6;                 // tail levels cycled with gamma > 1 (deeper ones: V)
 struct MgLevel {
   int nx, ny;
   long long off;
@@ -35,6 +36,7 @@ struct MgHier {
   float omega; // Jacobi weight
   float cw;    // coarse-correction weight
   int nu, nuc; // sweeps before / after each coarse correction; sweeps on the coarsest level
+  int gamma;   // coarse corrections per tail level (1: V-cycle, 2: W-cycle)
   int tail_smem;     // bytes of block 0's shared memory holding the tail levels
   // exact != 0: the coarsest level (at most 64 cells, in the tail) is solved
   // by a dense inverse formed once per solve, 64 x 64 elements at element
