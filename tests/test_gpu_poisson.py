@@ -23,7 +23,7 @@ def test_operator_is_bit_identical(gpu_pkg, orc):
 
 @pytest.mark.parametrize("gauge", ["pinned", "reference"])
 @pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_strips", "mixed_cluster16", "mixed_cluster4", "mixed_stream", "mixed_cg", "mixed_mg",
-                                  "mixed_mg_plain", "mixed_mg_gridtail", "fp64_mg", "fp64_mg_gridtail"])
+                                  "mixed_mg_plain", "mixed_mg_gridtail", "mixed_mg_nuc32", "fp64_mg", "fp64_mg_gridtail"])
 @pytest.mark.parametrize("n", [64, 128])
 def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
     pkg = gpu_pkg
@@ -58,6 +58,11 @@ def test_solve_matches_oracle(gpu_pkg, orc, n, prec, gauge):
         # no shared-memory tail: every level over the grid
         q.p_inner_kind = cap.INNER_MG
         q.p_mg_tail = 1
+    elif prec == "mixed_mg_nuc32":
+        # the coarsest level by 32 sweeps instead of its exact inverse: the
+        # tail's W-cycle visits it twice
+        q.p_inner_kind = cap.INNER_MG
+        q.p_mg_nuc = 32
     x = np.zeros_like(b)
     with pkg.Solver(q) as s:
         # "mixed" on these meshes is the strip form on every SM; the strip form
