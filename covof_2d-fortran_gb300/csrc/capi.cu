@@ -148,9 +148,10 @@ int ensure_poisson(covof_handle* h) {
   }
   H.omega = 0.8f;
   // the block-local tail levels run a W-cycle (two coarse corrections per
-  // level): at 1024^2 it cuts the outer iterations by a sixth for a few us
-  // more tail work
-  H.gamma = 2;
+  // level) on meshes of at least kMgWCells cells: at 1024^2 it cuts the outer
+  // iterations by a tenth for a few us more tail work; on small meshes the
+  // tail is most of the cycle and a W-cycle there costs more than it saves
+  H.gamma = (long long)h->D.nx * h->D.ny >= kMgWCells ? 2 : 1;
   H.nu = h->prm.p_mg_nu < 1 ? 1 : (h->prm.p_mg_nu > 8 ? 8 : h->prm.p_mg_nu);
   H.cw = (float)(h->prm.p_mg_cw > 0.0 && h->prm.p_mg_cw <= 4.0 ? h->prm.p_mg_cw : 1.0);
   // an even count leaves the coarsest correction in its first buffer

@@ -23,6 +23,7 @@ constexpr int kMgMaxLevels = 16;
 constexpr long long kMgTailSmem = 200 * 1024;  // cap on the shared-memory tail (plus ~6 KB static)
 constexpr long long kMgWarpCoarse = 256;        // coarsest levels this small run in one warp
 constexpr int kMgTailDepth = 6;                 // tail levels cycled with gamma > 1 (deeper ones: V)
+constexpr long long kMgWCells = 512LL * 512;    // meshes from this size on run the tail as a W-cycle
 struct MgLevel {
   int nx, ny;
   long long off;
