@@ -930,11 +930,12 @@ VofArgs vof_args(covof_handle* h, double dt, const double* C, const double* Cn, 
   return a;
 }
 
-// Pure cells directly, interface cells one warp each -- or, from
-// vof_cell_min(h) interface cells on, one thread each: both kernels are
-// launched and the one that does not match the device-side count returns at
-// once (the list is built on the device, so nothing here waits for the
-// host) -- then the ghost ring.
+// Pure cells directly, interface cells by one of three forms chosen on the
+// device-side count (the list is built on the device, so nothing here
+// waits for the host; the forms that do not match return at once): ELVIRA
+// lists of at most one wave of 128-thread blocks, one block per cell (the
+// latency form); one warp per cell; from vof_cell_min(h) cells on, one
+// thread per cell.  Then the ghost ring.
 int reconstruct_dev(covof_handle* h, const double* C, double* seg_out) {
   CS(check_periodic_vof(h->prm));
   CS(ensure_vof(h));
@@ -944,7 +945,9 @@ int reconstruct_dev(covof_handle* h, const double* C, double* seg_out) {
   CK(cudaMemsetAsync(h->vcount, 0, sizeof(int), h->stream));
   k_vof_classify<<<grd, blk, 0, h->stream>>>(a, h->vlist, h->vcount);
   const int cmin = vof_cell_min(h);
-  k_vof_mixed<<<4 * h->sm_count, 128, 0, h->stream>>>(a, h->vlist, h->vcount, cmin);
+  const int bmax = h->prm.recon == COVOF_RECON_ELVIRA ? (cmin < 4 * h->sm_count ? cmin : 4 * h->sm_count) : 0;
+  if (bmax > 0) k_vof_elvira_block<<<4 * h->sm_count, 128, 0, h->stream>>>(a, h->vlist, h->vcount, bmax);
+  k_vof_mixed<<<4 * h->sm_count, 128, 0, h->stream>>>(a, h->vlist, h->vcount, bmax, cmin);
   k_vof_mixed_cell<<<h->vof_cell_nb, 128, 0, h->stream>>>(a, h->vlist, h->vcount, cmin);
   const int nring = 2 * h->D.ny + 2 * (h->D.nx + 2);
   k_vof_ring_warp<<<(nring + 3) / 4, 128, 0, h->stream>>>(a);

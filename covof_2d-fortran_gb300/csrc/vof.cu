@@ -162,20 +162,21 @@ __global__ void k_vof_classify(VofArgs a, int* __restrict__ list, int* __restric
   if (mixed) list[base + __popc(bal & ((1u << lane) - 1u))] = k;
 }
 
-// One warp per listed cell, for lists shorter than max_count (the
-// thread-per-cell form below takes the longer ones).  ELVIRA (inner cells):
+// One warp per listed cell, for lists of min_count .. max_count - 1 cells
+// (the block and thread forms below take the shorter and the longer ones).
+// ELVIRA (inner cells):
 // candidate q on lanes 4q .. 4q+3 (lanes 28-31 repeat candidate 6 and are
 // ignored); its bisection runs 2 levels per round, its 8 neighbour clips 2
 // per lane, and the error is summed and the candidate chosen in the
 // reference order.  PLIC, and ELVIRA on ghost cells: one normal, 5 levels
 // per round.
 __global__ void __launch_bounds__(128) k_vof_mixed(VofArgs a, const int* __restrict__ list,
-                                                    const int* __restrict__ count, int max_count) {
+                                                    const int* __restrict__ count, int min_count, int max_count) {
   const VMesh m{a.D, a.dx, a.dy};
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int n = *count;
-  if (n >= max_count) return;
+  if (n < min_count || n >= max_count) return;
   const int nx = a.D.nx, ny = a.D.ny;
   const double* __restrict__ C = a.C;
   const double dx = a.dx, dy = a.dy;
@@ -265,6 +266,97 @@ __global__ void __launch_bounds__(128) k_vof_mixed(VofArgs a, const int* __restr
       if (vq && eq < best_err) { best_err = eq; bnx = xq; bny = yq; ba = aq; }
     }
     if (lane == 0) put_seg(a.seg, k, bnx, bny, ba);
+  }
+}
+
+// ELVIRA with one 128-thread block per listed cell, for lists shorter than
+// max_count (about one wave of blocks): the latency form.  Candidate q on
+// the 16 lanes 16q .. 16q+15 (lanes 112-127 repeat candidate 6 and are
+// ignored), so its bisection runs 4 levels per round (12 rounds against the
+// warp form's 23) and its 8 neighbour clips one per lane; the candidates
+// meet in shared memory and thread 0 chooses in the reference order.  Ghost
+// cells of the list (one normal) go to the first warp, 5 levels per round.
+// Bit-identical to the warp and thread forms.
+__global__ void __launch_bounds__(128) k_vof_elvira_block(VofArgs a, const int* __restrict__ list,
+                                                          const int* __restrict__ count, int max_count) {
+  __shared__ double s_err[7], s_ux[7], s_uy[7], s_ca[7];
+  __shared__ int s_valid[7];
+  const VMesh m{a.D, a.dx, a.dy};
+  const int n = *count;
+  if (n >= max_count) return;
+  const int lane = threadIdx.x & 31;
+  const int q = (threadIdx.x >> 4) < 7 ? (int)(threadIdx.x >> 4) : 6;
+  const int sub = lane & 15, gbase = lane & 16;
+  const int nx = a.D.nx, ny = a.D.ny;
+  const double* __restrict__ C = a.C;
+  const double dx = a.dx, dy = a.dy;
+  for (int e = blockIdx.x; e < n; e += gridDim.x) {
+    const int k = list[e];
+    const int j = k / a.D.P, i = k - j * a.D.P;
+    const double c = C[k];
+    const double xmin = m.xf(i), xmax = m.xf(i + 1), ymin = m.yf(j), ymax = m.yf(j + 1);
+    const bool inner = (i >= 1 && i <= nx && j >= 1 && j <= ny);
+    if (inner && a.D.nbhd(k, 24) != k) continue;
+    auto Cq = [&](int p, int qq) { return C[a.D.id(p, qq)]; };
+    if (!inner) {
+      // a ghost cell: the (1, 0) normal and a fresh line constant
+      if (threadIdx.x < 32) {
+        const double al = tree_alpha<5>(lane, 0, xmin, xmax, ymin, ymax, 1.0, 0.0, c);
+        if (lane == 0) put_seg(a.seg, k, 1.0, 0.0, al);
+      }
+      continue;
+    }
+    const double Hm1 = (Cq(i - 1, j - 1) + Cq(i - 1, j) + Cq(i - 1, j + 1)) * dy;
+    const double H0 = (Cq(i, j - 1) + Cq(i, j) + Cq(i, j + 1)) * dy;
+    const double Hp1 = (Cq(i + 1, j - 1) + Cq(i + 1, j) + Cq(i + 1, j + 1)) * dy;
+    const double Wm1 = (Cq(i - 1, j - 1) + Cq(i, j - 1) + Cq(i + 1, j - 1)) * dx;
+    const double W0 = (Cq(i - 1, j) + Cq(i, j) + Cq(i + 1, j)) * dx;
+    const double Wp1 = (Cq(i - 1, j + 1) + Cq(i, j + 1) + Cq(i + 1, j + 1)) * dx;
+    const double sgy = (Cq(i, j + 1) < Cq(i, j - 1)) ? 1.0 : -1.0;
+    const double sgx = (Cq(i + 1, j) < Cq(i - 1, j)) ? 1.0 : -1.0;
+    double cnx, cny;
+    switch (q) {
+      case 0: cnx = -sgy * (Hp1 - Hm1) / (2.0 * dx); cny = sgy * 1.0; break;
+      case 1: cnx = -sgy * (Hp1 - H0) / (dx); cny = sgy * 1.0; break;
+      case 2: cnx = -sgy * (H0 - Hm1) / (dx); cny = sgy * 1.0; break;
+      case 3: cnx = sgx * 1.0; cny = -sgx * (Wp1 - Wm1) / (2.0 * dy); break;
+      case 4: cnx = sgx * 1.0; cny = -sgx * (Wp1 - W0) / (dy); break;
+      case 5: cnx = sgx * 1.0; cny = -sgx * (W0 - Wm1) / (dy); break;
+      default:
+        cnx = -((Cq(i + 1, j + 1) + 2.0 * Cq(i + 1, j) + Cq(i + 1, j - 1)) -
+                (Cq(i - 1, j + 1) + 2.0 * Cq(i - 1, j) + Cq(i - 1, j - 1))) / (8.0 * dx);
+        cny = -((Cq(i + 1, j + 1) + 2.0 * Cq(i, j + 1) + Cq(i - 1, j + 1)) -
+                (Cq(i + 1, j - 1) + 2.0 * Cq(i, j - 1) + Cq(i - 1, j - 1))) / (8.0 * dy);
+        break;
+    }
+    const double cn = fhypot(cnx, cny);
+    const bool valid = !(cn < 1.0e-12);
+    const double ux = valid ? cnx / cn : 1.0, uy = valid ? cny / cn : 0.0;
+    const double ca = tree_alpha<4>(sub, gbase, xmin, xmax, ymin, ymax, ux, uy, c);
+    // neighbour s (reference order: dj = -1..1, di = -1..1, centre skipped) on lane sub = s
+    double sq = 0.0;
+    if (sub < 8) {
+      const int t = sub < 4 ? sub : sub + 1;
+      const int di = t % 3 - 1, dj = t / 3 - 1;
+      const double vt = Cq(i + di, j + dj) * dx * dy;
+      const double vr = cut_box_area(m.xf(i + di), m.xf(i + di + 1), m.yf(j + dj), m.yf(j + dj + 1), ux, uy, ca);
+      const double df = vr - vt;
+      sq = df * df;
+    }
+    double err = 0.0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) err = err + __shfl_sync(0xffffffffu, sq, gbase + s);
+    if (sub == 0 && (threadIdx.x >> 4) < 7) {
+      s_err[q] = err; s_valid[q] = valid ? 1 : 0; s_ux[q] = ux; s_uy[q] = uy; s_ca[q] = ca;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double best_err = 1.0e30, bnx = 1.0, bny = 0.0, ba = 0.0;
+      for (int qq = 0; qq < 7; ++qq)
+        if (s_valid[qq] && s_err[qq] < best_err) { best_err = s_err[qq]; bnx = s_ux[qq]; bny = s_uy[qq]; ba = s_ca[qq]; }
+      put_seg(a.seg, k, bnx, bny, ba);
+    }
+    __syncthreads();
   }
 }
 

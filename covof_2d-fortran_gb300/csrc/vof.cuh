@@ -33,7 +33,10 @@ struct CsfArgs {
 };
 
 __global__ void k_vof_classify(VofArgs a, int* __restrict__ list, int* __restrict__ count);
-__global__ void k_vof_mixed(VofArgs a, const int* __restrict__ list, const int* __restrict__ count, int max_count);
+__global__ void k_vof_mixed(VofArgs a, const int* __restrict__ list, const int* __restrict__ count, int min_count,
+                            int max_count);
+__global__ void k_vof_elvira_block(VofArgs a, const int* __restrict__ list, const int* __restrict__ count,
+                                   int max_count);
 __global__ void k_vof_mixed_cell(VofArgs a, const int* __restrict__ list, const int* __restrict__ count,
                                  int min_count);
 __global__ void k_vof_ring_warp(VofArgs a);

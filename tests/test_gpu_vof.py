@@ -36,12 +36,15 @@ def test_reconstruct_bit_exact(gpu_pkg, orc, recon):
         with pkg.Solver(p) as s:
             s_g = s.reconstruct_interface(Cf)
         assert np.array_equal(s_g, s_o)
-    # ragged random field (many pure/mixed transitions, ghost-ring cases)
-    q = pkg.cases.make_params(37, 37, 1.0, 1.0)
-    q.recon = p.recon
-    Cr = _random_C(37, 2)
-    with pkg.Solver(q) as s:
-        assert np.array_equal(s.reconstruct_interface(Cr), orc.reconstruct(q, Cr))
+    # ragged random fields (many pure/mixed transitions, ghost-ring cases):
+    # 37^2 (about 500 interface cells: ELVIRA's block-per-cell form on a
+    # 152-SM part) and 80^2 (about 2500: the warp-per-cell form)
+    for nr in (37, 80):
+        q = pkg.cases.make_params(nr, nr, 1.0, 1.0)
+        q.recon = p.recon
+        Cr = _random_C(nr, 2)
+        with pkg.Solver(q) as s:
+            assert np.array_equal(s.reconstruct_interface(Cr), orc.reconstruct(q, Cr))
 
 
 @pytest.mark.parametrize("recon", ["PLIC", "ELVIRA"])
