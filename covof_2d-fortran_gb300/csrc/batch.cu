@@ -406,6 +406,7 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
     const int s = covof_create(&cases[c], &b->h[c]);
     if (s != COVOF_OK) return fail(s);
     covof_handle* h = b->h[c];
+    h->vof_block_form = false;  // the cases' VOF stages run side by side
     if (ensure_fields(h) || ensure_poisson(h) || ensure_mom(h) || ensure_vof(h) || poisson_plan(h) ||
         predictor_plan(h))
       return fail(COVOF_CUDA_ERROR);

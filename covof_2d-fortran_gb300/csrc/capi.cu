@@ -945,7 +945,8 @@ int reconstruct_dev(covof_handle* h, const double* C, double* seg_out) {
   CK(cudaMemsetAsync(h->vcount, 0, sizeof(int), h->stream));
   k_vof_classify<<<grd, blk, 0, h->stream>>>(a, h->vlist, h->vcount);
   const int cmin = vof_cell_min(h);
-  const int bmax = h->prm.recon == COVOF_RECON_ELVIRA ? (cmin < 4 * h->sm_count ? cmin : 4 * h->sm_count) : 0;
+  const int bmax = h->prm.recon == COVOF_RECON_ELVIRA && h->vof_block_form
+                       ? (cmin < 4 * h->sm_count ? cmin : 4 * h->sm_count) : 0;
   if (bmax > 0) k_vof_elvira_block<<<4 * h->sm_count, 128, 0, h->stream>>>(a, h->vlist, h->vcount, bmax);
   k_vof_mixed<<<4 * h->sm_count, 128, 0, h->stream>>>(a, h->vlist, h->vcount, bmax, cmin);
   k_vof_mixed_cell<<<h->vof_cell_nb, 128, 0, h->stream>>>(a, h->vlist, h->vcount, cmin);

@@ -112,6 +112,10 @@ struct covof_handle {
   unsigned int* svof_prog = nullptr;  // SVOF band progress (32 words per band)
   int svof_nb = 0;                    // blocks of the SVOF launch (planned by ensure_vof)
   int vof_cell_nb = 0;                // blocks of the thread-per-cell reconstruction (ensure_vof)
+  // ELVIRA's block-per-cell latency form for short interface lists: on for
+  // a case that has the GPU to itself, off in a batch (many cases at once:
+  // there throughput counts, and the block form does 2.5x the clips per cell)
+  bool vof_block_form = true;
   // caller-field mirrors (host-pointer entry points)
   bool have_fields = false;
   double *f_u = nullptr, *f_v = nullptr, *f_p = nullptr, *f_rho_u = nullptr, *f_rho_v = nullptr,
