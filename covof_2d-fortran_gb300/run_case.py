@@ -4,6 +4,7 @@
     python covof_2d-fortran_gb300/run_case.py apply --n 4096 --reps 5
     python covof_2d-fortran_gb300/run_case.py bubble --nx 128 --ny 256 --steps 4
     python covof_2d-fortran_gb300/run_case.py batch --ncases 64 --steps 2
+    python covof_2d-fortran_gb300/run_case.py droplets --n 4096 --reps 3
 
 Each case runs `reps` (or `steps`) calls of the library on device-resident
 seeded inputs (cases.py) and prints one JSON line with the CUDA-event time of
@@ -23,7 +24,10 @@ kernel's launches in these calls; the launch count per call is fixed, so
   k_vof_ring_warp, k_vof_pass, k_props_*, k_csf_*, k_mom_*, k_bicgstab,
   the Poisson kernel).
 * batch: batch steps of droplet / bubble cases of uneven sizes
-  (k_mom_krylov_batch, k_pcg_mixed_mg_batch).
+  (k_mom_bicgstab_batch, k_pcg_mixed_mg_batch).
+* droplets: ELVIRA reconstructions of an array of 64 x 64 droplets on n^2
+  cells (0.5 M interface cells at 4096^2: k_vof_classify, k_vof_mixed_cell,
+  k_vof_ring_warp).
 """
 from __future__ import annotations
 
@@ -148,9 +152,34 @@ def run_batch(args):
     return out
 
 
+def run_droplets(args):
+    import torch
+    pkg, _ = _pkg()
+    cap = pkg.capi
+    p, C0 = pkg.cases.droplet_array(args.n, 64, 20.0 * args.n / 4096)
+    f = pkg.Fields.allocate(p)
+    f.C[...] = C0
+    with pkg.Solver(p) as s0:
+        s0.apply_vof_bc(f)
+    tC = torch.from_numpy(f.C).cuda()
+    seg = torch.zeros(3 * tC.numel(), dtype=torch.float64, device=tC.device)
+    out = []
+    with pkg.Solver(p) as s:
+        stream = torch.cuda.ExternalStream(s.stream_ptr, device=tC.device)
+        for _ in range(args.reps):
+            torch.cuda.synchronize()
+            e0, e1 = _events(torch, stream)
+            st = s.lib.covof_vof_reconstruct_dev(s.h, ctypes.c_void_p(tC.data_ptr()), ctypes.c_void_p(seg.data_ptr()))
+            e1.record(stream)
+            e1.synchronize()
+            assert st == cap.OK, st
+            out.append({"ms": e0.elapsed_time(e1)})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["poisson", "apply", "bubble", "batch"])
+    ap.add_argument("case", choices=["poisson", "apply", "bubble", "batch", "droplets"])
     ap.add_argument("--n", type=int, default=1024)
     ap.add_argument("--nx", type=int, default=128)
     ap.add_argument("--ny", type=int, default=256)
@@ -161,7 +190,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--ncases", type=int, default=64)
     args = ap.parse_args()
-    fn = {"poisson": run_poisson, "apply": run_apply, "bubble": run_bubble, "batch": run_batch}[args.case]
+    fn = {"poisson": run_poisson, "apply": run_apply, "bubble": run_bubble, "batch": run_batch,
+          "droplets": run_droplets}[args.case]
     print(json.dumps({"case": args.case, "args": vars(args), "calls": fn(args)}), flush=True)
 
 
