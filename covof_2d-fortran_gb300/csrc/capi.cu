@@ -119,12 +119,28 @@ int ensure_poisson(covof_handle* h) {
   MgHier& H = h->mg;
   H.nl = 1;
   H.lv[0].nx = h->D.nx; H.lv[0].ny = h->D.ny; H.lv[0].off = 0;
+  H.lv[0].fx = H.lv[0].fy = 1;
   long long pool = 0;
+  // cell sides of the level being coarsened: on anisotropic cells the
+  // couplings across the short side are the strong ones, and only that
+  // direction is halved (semi-coarsening) until the cells are within a
+  // factor 2 of square; aggregation across the weak direction leaves the
+  // smooth error of the strong one to a point smoother that cannot reduce it
+  double hx = h->prm.dx, hy = h->prm.dy;
   while (H.nl < kMgMaxLevels && (long long)H.lv[H.nl - 1].nx * H.lv[H.nl - 1].ny > 64 &&
          (H.lv[H.nl - 1].nx > 1 || H.lv[H.nl - 1].ny > 1)) {
+    const MgLevel& f = H.lv[H.nl - 1];
+    int fx = 2, fy = 2;
+    if (hy >= 2.0 * hx) fy = 1;
+    else if (hx >= 2.0 * hy) fx = 1;
+    // a direction already one cell wide: the other one only
+    if (f.nx < 2) { fx = 1; fy = 2; }
+    if (f.ny < 2) { fy = 1; fx = 2; }
     MgLevel& c = H.lv[H.nl];
-    c.nx = (H.lv[H.nl - 1].nx + 1) / 2;
-    c.ny = (H.lv[H.nl - 1].ny + 1) / 2;
+    c.fx = fx; c.fy = fy;
+    c.nx = (f.nx + fx - 1) / fx;
+    c.ny = (f.ny + fy - 1) / fy;
+    hx *= fx; hy *= fy;
     c.off = pool;
     pool += 7LL * (c.nx + 2) * (c.ny + 2);
     H.nl += 1;

@@ -1482,6 +1482,7 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cluster(PoissonArgs a) {
 template <typename T>
 struct MgLvT {
   int nx, ny, P;
+  int fx, fy;   // coarsening factors from the next finer level (1 or 2 per direction)
   T *xa, *xb, *b;
   const T *ax, *ay, *dg;
   const T* wd;  // omega / dg (the sweeps multiply instead of dividing)
@@ -1508,6 +1509,7 @@ struct MgInnerT {
   __device__ MgLvT<T> lv_make(int l, bool S) const {
     MgLvT<T> L;
     L.nx = H.lv[l].nx; L.ny = H.lv[l].ny; L.P = L.nx + 2;
+    L.fx = H.lv[l].fx; L.fy = H.lv[l].fy;
     const size_t g = (size_t)(L.nx + 2) * (size_t)(L.ny + 2);
     L.wd = nullptr;
     L.xs = nullptr;
@@ -1590,11 +1592,12 @@ struct MgInnerT {
     const MgLvT<T> F = lv(l, S), Cc = lv(l + 1, S);
     const T* x = cur ? F.xb : F.xa;
     const int pin = l == 0 ? pk : -1;
+    const int fx = Cc.fx, fy = Cc.fy;
     cells<S>(Cc.nx, Cc.ny, [&](int I, int J) {
       T s = T(0);
-      for (int dj = 0; dj < 2; ++dj)
-        for (int di = 0; di < 2; ++di) {
-          const int i = 2 * I - 1 + di, j = 2 * J - 1 + dj;
+      for (int dj = 0; dj < fy; ++dj)
+        for (int di = 0; di < fx; ++di) {
+          const int i = fx * (I - 1) + 1 + di, j = fy * (J - 1) + 1 + dj;
           if (i > F.nx || j > F.ny) continue;
           const int k = F.id(i, j);
           if (k == pin) continue;
@@ -1616,7 +1619,7 @@ struct MgInnerT {
     cells<S>(F.nx, F.ny, [&](int i, int j) {
       const int k = F.id(i, j);
       if (k == pin) return;
-      x[k] = ld<S>(x + k) + cw * ld<S>(xc + Cc.id((i + 1) / 2, (j + 1) / 2));
+      x[k] = ld<S>(x + k) + cw * ld<S>(xc + Cc.id((i - 1) / Cc.fx + 1, (j - 1) / Cc.fy + 1));
     });
   }
   // parity of the buffer holding level l's correction after its last sweep
@@ -1644,28 +1647,41 @@ struct MgInnerT {
       auto axf = [&](int i, int j) -> T { return (i <= F.nx + 1 && j <= F.ny) ? F.ax[F.id(i, j)] : T(0); };
       auto ayf = [&](int i, int j) -> T { return (i <= F.nx && j <= F.ny + 1) ? F.ay[F.id(i, j)] : T(0); };
       auto dgf = [&](int i, int j) -> T { return (i <= F.nx && j <= F.ny) ? F.dg[F.id(i, j)] : T(0); };
+      // aggregates of fx x fy fine cells: 2 x 2, or 2 x 1 / 1 x 2 on
+      // anisotropic cells (semi-coarsening)
+      const int fx = Cc.fx, fy = Cc.fy;
       cells<false>(Cc.nx + 1, Cc.ny + 1, [&](int I, int J) {
         const int k = Cc.id(I, J);
-        if (J <= Cc.ny) cax[k] = axf(2 * I - 1, 2 * J - 1) + axf(2 * I - 1, 2 * J);
-        if (I <= Cc.nx) cay[k] = ayf(2 * I - 1, 2 * J - 1) + ayf(2 * I, 2 * J - 1);
+        const int i0 = fx * (I - 1) + 1, j0 = fy * (J - 1) + 1;
+        if (J <= Cc.ny) cax[k] = fy == 2 ? axf(i0, j0) + axf(i0, j0 + 1) : axf(i0, j0);
+        if (I <= Cc.nx) cay[k] = fx == 2 ? ayf(i0, j0) + ayf(i0 + 1, j0) : ayf(i0, j0);
         if (I <= Cc.nx && J <= Cc.ny) {
           // Galerkin: sum of the aggregate's diagonals minus twice its
           // internal couplings (= its external faces plus its diagonal shifts)
-          const int i0 = 2 * I - 1, j0 = 2 * J - 1;
-          T d = dgf(i0, j0) + dgf(i0 + 1, j0) + dgf(i0, j0 + 1) + dgf(i0 + 1, j0 + 1);
+          T d;
+          if (fx == 2 && fy == 2) d = dgf(i0, j0) + dgf(i0 + 1, j0) + dgf(i0, j0 + 1) + dgf(i0 + 1, j0 + 1);
+          else if (fx == 2) d = dgf(i0, j0) + dgf(i0 + 1, j0);
+          else if (fy == 2) d = dgf(i0, j0) + dgf(i0, j0 + 1);
+          else d = dgf(i0, j0);
           T internal = T(0);
-          if (i0 + 1 <= F.nx) internal += axf(i0 + 1, j0) + axf(i0 + 1, j0 + 1);
-          if (j0 + 1 <= F.ny) internal += ayf(i0, j0 + 1) + ayf(i0 + 1, j0 + 1);
+          if (fx == 2 && i0 + 1 <= F.nx) internal += fy == 2 ? axf(i0 + 1, j0) + axf(i0 + 1, j0 + 1) : axf(i0 + 1, j0);
+          if (fy == 2 && j0 + 1 <= F.ny) internal += fx == 2 ? ayf(i0, j0 + 1) + ayf(i0 + 1, j0 + 1) : ayf(i0, j0 + 1);
           if (l == 1 && pk >= 0 && I == 1 && J == 1) {
             // pinned gauge: the fine operator is A without cell (1,1) (held
-            // at zero), so the aggregate holding it sums the other three
-            // cells only and its couplings to the pinned cell are not
-            // internal -- they stay on those cells' diagonals as a Dirichlet
-            // anchor.  The coarse operators are then nonsingular like the
-            // pinned system, instead of near-singular along the constant.
-            d = dgf(i0 + 1, j0) + dgf(i0, j0 + 1) + dgf(i0 + 1, j0 + 1);
+            // at zero), so the aggregate holding it sums its other cells
+            // only and its couplings to the pinned cell are not internal --
+            // they stay on those cells' diagonals as a Dirichlet anchor.  The
+            // coarse operators are then nonsingular like the pinned system,
+            // instead of near-singular along the constant.
             internal = T(0);
-            if (i0 + 1 <= F.nx && j0 + 1 <= F.ny) internal = axf(i0 + 1, j0 + 1) + ayf(i0 + 1, j0 + 1);
+            if (fx == 2 && fy == 2) {
+              d = dgf(i0 + 1, j0) + dgf(i0, j0 + 1) + dgf(i0 + 1, j0 + 1);
+              if (i0 + 1 <= F.nx && j0 + 1 <= F.ny) internal = axf(i0 + 1, j0 + 1) + ayf(i0 + 1, j0 + 1);
+            } else if (fx == 2) {
+              d = dgf(i0 + 1, j0);
+            } else if (fy == 2) {
+              d = dgf(i0, j0 + 1);
+            }
           }
           const T dc = d - T(2) * internal;
           cdg[k] = dc;

@@ -26,6 +26,7 @@ constexpr int kMgTailDepth = 6;                 // tail levels cycled with gamma
 constexpr long long kMgWCells = 512LL * 512;    // meshes from this size on run the tail as a W-cycle
 struct MgLevel {
   int nx, ny;
+  int fx, fy;  // coarsening factors from the next finer level (level 0: 1, 1)
   long long off;
 };
 struct MgHier {

@@ -203,3 +203,79 @@ def test_pinned_mixed_mg_route_with_large_level(gpu_pkg, orc):
             assert x[1, 1] == 0.0
             err = np.linalg.norm(x[1:-1, 1:-1] - ref[1:-1, 1:-1]) / np.linalg.norm(ref[1:-1, 1:-1])
             assert err < 1e-10, (k, err)
+
+
+@pytest.mark.parametrize("prec", ["mixed_mg", "fp64_mg"])
+@pytest.mark.parametrize("gauge", ["pinned", "reference"])
+@pytest.mark.parametrize("nx,ny,lx,ly", [(64, 256, 1.0, 1.0), (256, 48, 1.0, 1.0), (96, 96, 1.0, 4.0)])
+def test_multigrid_on_anisotropic_cells(gpu_pkg, orc, nx, ny, lx, ly, prec, gauge):
+    """Cells of aspect 4:1 to 1:5 (the hierarchy halves only the strongly
+    coupled direction until the cells are near square, 2 x 1 and 1 x 2
+    aggregates), log-normal random density: the solution matches the
+    oracle's converged Jacobi-PCG to 1e-10."""
+    pkg = gpu_pkg
+    cap = pkg.capi
+    p = pkg.cases.make_params(nx, ny, lx, ly)
+    rng = np.random.default_rng(nx + 7 * ny)
+    rho = np.exp(2.0 * rng.standard_normal((ny + 2, nx + 2)))
+    ru = np.ones_like(rho)
+    rv = np.ones_like(rho)
+    ru[1:-1, 1:] = 0.5 * (rho[1:-1, :-1] + rho[1:-1, 1:])
+    rv[1:, 1:-1] = 0.5 * (rho[:-1, 1:-1] + rho[1:, 1:-1])
+    b = np.zeros_like(rho)
+    b[1:-1, 1:-1] = rng.standard_normal((ny, nx))
+    b[1:-1, 1:-1] -= b[1:-1, 1:-1].mean()
+    p.p_gauge = cap.GAUGE_PINNED if gauge == "pinned" else cap.GAUGE_REFERENCE
+    p.p_tol = 1e-12
+    p.p_max_iter = 1000000
+    ref = np.zeros_like(b)
+    _, _, st_o = orc.poisson_solve_rhs(p, 1e-3, b, ru, rv, ref)
+    assert st_o == 0
+    q = p.copy()
+    q.p_precision = cap.PREC_MIXED if prec == "mixed_mg" else cap.PREC_FP64_MG
+    q.p_inner_kind = cap.INNER_MG
+    x = np.zeros_like(b)
+    with pkg.Solver(q) as s:
+        it, rr, st = s.poisson_solve_rhs(1e-3, b, ru, rv, x)
+        outer = s.last_refine_steps()
+    err = np.linalg.norm(x[1:-1, 1:-1] - ref[1:-1, 1:-1]) / np.linalg.norm(ref[1:-1, 1:-1])
+    print(f"anisotropic {nx}x{ny} on {lx}x{ly} {prec} {gauge}: {outer} V-cycles, err {err:.2e}")
+    assert st == cap.OK and rr <= 1e-12
+    assert err < 1e-10, err
+
+
+def test_semicoarsening_keeps_the_v_cycle_count(gpu_pkg):
+    """A two-layer density (3 over 1, the Rayleigh-Taylor set-up) on 256^2
+    cells of a [0,1] x [0,4] domain (cells 4:1): with the direction of the
+    strong couplings halved first, the flexible CG needs about as many
+    V-cycles as on square cells (full 2 x 2 aggregation needs several times
+    more on this mesh)."""
+    import math
+    pkg = gpu_pkg
+    cap = pkg.capi
+    n = 256
+    p = pkg.cases.make_params(n, n, 1.0, 4.0)
+    xc = (np.arange(n) + 0.5) * p.dx
+    yc = (np.arange(n) + 0.5) * p.dy
+    X, Y = np.meshgrid(xc, yc)
+    rho = np.ones((n + 2, n + 2))
+    rho[1:-1, 1:-1] = np.where(Y > 2.0 + 0.05 * np.cos(2 * math.pi * X), 3.0, 1.0)
+    rho[0, :], rho[-1, :], rho[:, 0], rho[:, -1] = rho[1, :], rho[-2, :], rho[:, 1], rho[:, -2]
+    ru = np.ones_like(rho)
+    rv = np.ones_like(rho)
+    ru[1:-1, 1:] = 0.5 * (rho[1:-1, :-1] + rho[1:-1, 1:])
+    rv[1:, 1:-1] = 0.5 * (rho[:-1, 1:-1] + rho[1:, 1:-1])
+    b = np.zeros_like(rho)
+    b[1:-1, 1:-1] = np.random.default_rng(4).standard_normal((n, n))
+    b[1:-1, 1:-1] -= b[1:-1, 1:-1].mean()
+    p.p_precision = cap.PREC_MIXED
+    p.p_inner_kind = cap.INNER_MG
+    p.p_tol = 1e-10
+    p.p_max_iter = 1000000
+    x = np.zeros_like(b)
+    with pkg.Solver(p) as s:
+        it, rr, st = s.poisson_solve_rhs(2e-5, b, ru, rv, x)
+        outer = s.last_refine_steps()
+    print(f"two-layer 256^2 on 1x4: {outer} V-cycles")
+    assert st == cap.OK and rr <= 1e-10
+    assert outer <= 60, outer
