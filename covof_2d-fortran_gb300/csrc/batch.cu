@@ -432,9 +432,15 @@ int covof_batch_create(const covof_params* cases, int ncases, covof_batch** out)
   bool smem_form = false;
   bool want_stream = false;
   for (int c = 0; c < ncases; ++c) want_stream |= cases[c].p_inner_kind == COVOF_INNER_CHEBYSHEV_STREAM;
-  if (mg)
-    b->pfn = cases[0].p_precision == COVOF_PREC_FP64_MG ? (const void*)k_pcg_fp64_mg_batch
-                                                        : (const void*)k_pcg_mixed_mg_batch;
+  if (mg) {
+    // the semi-coarsening kernel when some case has anisotropic cells
+    bool semi = false;
+    for (covof_handle* h : b->h) semi = semi || h->mg.semi != 0;
+    if (cases[0].p_precision == COVOF_PREC_FP64_MG)
+      b->pfn = semi ? (const void*)k_pcg_fp64_mg_batch_semi : (const void*)k_pcg_fp64_mg_batch;
+    else
+      b->pfn = semi ? (const void*)k_pcg_mixed_mg_batch_semi : (const void*)k_pcg_mixed_mg_batch;
+  }
   if (b->mixed && !want_stream && !mg) {
     int optin = 0;
     cudaFuncAttributes fa;

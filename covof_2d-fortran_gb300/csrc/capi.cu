@@ -120,6 +120,7 @@ int ensure_poisson(covof_handle* h) {
   H.nl = 1;
   H.lv[0].nx = h->D.nx; H.lv[0].ny = h->D.ny; H.lv[0].off = 0;
   H.lv[0].fx = H.lv[0].fy = 1;
+  H.semi = 0;
   long long pool = 0;
   // cell sides of the level being coarsened: on anisotropic cells the
   // couplings across the short side are the strong ones, and only that
@@ -141,6 +142,7 @@ int ensure_poisson(covof_handle* h) {
     c.nx = (f.nx + fx - 1) / fx;
     c.ny = (f.ny + fy - 1) / fy;
     hx *= fx; hy *= fy;
+    if (fx != 2 || fy != 2) H.semi = 1;
     c.off = pool;
     pool += 7LL * (c.nx + 2) * (c.ny + 2);
     H.nl += 1;
@@ -366,7 +368,10 @@ int poisson_plan(covof_handle* h) {
   h->p_cluster = false;
   if (mg_path(P)) {
     // multigrid inner: one persistent block per SM, tile-owned outer
-    const void* mfn = P.p_precision == COVOF_PREC_FP64_MG ? (const void*)k_pcg_fp64_mg : (const void*)k_pcg_mixed_mg;
+    const bool semi = h->mg.semi != 0;
+    const void* mfn = P.p_precision == COVOF_PREC_FP64_MG
+                          ? (semi ? (const void*)k_pcg_fp64_mg_semi : (const void*)k_pcg_fp64_mg)
+                          : (semi ? (const void*)k_pcg_mixed_mg_semi : (const void*)k_pcg_mixed_mg);
     long long units = h->sm_count;
     if (L.p_blocks > 0 && L.p_blocks < units) units = L.p_blocks;
     const size_t tail = (size_t)h->mg.tail_smem;
@@ -522,7 +527,8 @@ int poisson_enqueue(covof_handle* h, double dt, const double* u, const double* v
   CS(pois_pre(h, dt, u, v, b, rho_u, rho_v, p, &a));
   const covof_params& P = h->prm;
   if (mg_path(P) && a.pinned &&
-      (h->p_fn == (const void*)k_pcg_mixed_mg || h->p_fn == (const void*)k_pcg_fp64_mg)) {
+      (h->p_fn == (const void*)k_pcg_mixed_mg || h->p_fn == (const void*)k_pcg_fp64_mg ||
+       h->p_fn == (const void*)k_pcg_mixed_mg_semi || h->p_fn == (const void*)k_pcg_fp64_mg_semi)) {
     // The pinned system solved through the reference gauge, whose
     // deflation handles the constant mode exactly (35 against 41 outer
     // iterations at 1024^2); the pinned residual is checked after the shift

@@ -1482,7 +1482,6 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_cluster(PoissonArgs a) {
 template <typename T>
 struct MgLvT {
   int nx, ny, P;
-  int fx, fy;   // coarsening factors from the next finer level (1 or 2 per direction)
   T *xa, *xb, *b;
   const T *ax, *ay, *dg;
   const T* wd;  // omega / dg (the sweeps multiply instead of dividing)
@@ -1490,7 +1489,10 @@ struct MgLvT {
   __device__ __forceinline__ int id(int i, int j) const { return j * P + i; }
 };
 
-template <typename T>
+// kSemi: the hierarchy has semi-coarsened levels (2 x 1 / 1 x 2
+// aggregates); without it every level is 2 x 2 and the grid code keeps its
+// compile-time 2 x 2 loops
+template <typename T, bool kSemi = false>
 struct MgInnerT {
   using Scalar = T;
   static constexpr bool kScaled = false;
@@ -1509,7 +1511,6 @@ struct MgInnerT {
   __device__ MgLvT<T> lv_make(int l, bool S) const {
     MgLvT<T> L;
     L.nx = H.lv[l].nx; L.ny = H.lv[l].ny; L.P = L.nx + 2;
-    L.fx = H.lv[l].fx; L.fy = H.lv[l].fy;
     const size_t g = (size_t)(L.nx + 2) * (size_t)(L.ny + 2);
     L.wd = nullptr;
     L.xs = nullptr;
@@ -1592,21 +1593,39 @@ struct MgInnerT {
     const MgLvT<T> F = lv(l, S), Cc = lv(l + 1, S);
     const T* x = cur ? F.xb : F.xa;
     const int pin = l == 0 ? pk : -1;
-    const int fx = Cc.fx, fy = Cc.fy;
-    cells<S>(Cc.nx, Cc.ny, [&](int I, int J) {
-      T s = T(0);
-      for (int dj = 0; dj < fy; ++dj)
-        for (int di = 0; di < fx; ++di) {
-          const int i = fx * (I - 1) + 1 + di, j = fy * (J - 1) + 1 + dj;
-          if (i > F.nx || j > F.ny) continue;
-          const int k = F.id(i, j);
-          if (k == pin) continue;
-          s += ld<S>(F.b + k) - apply<S>(F, x, k);
-        }
-      const int kc = Cc.id(I, J);
-      Cc.b[kc] = s;
-      if (first_next) Cc.xb[kc] = s * Cc.wd[kc];
-    });
+    if constexpr (!kSemi) {
+      cells<S>(Cc.nx, Cc.ny, [&](int I, int J) {
+        T s = T(0);
+        for (int dj = 0; dj < 2; ++dj)
+          for (int di = 0; di < 2; ++di) {
+            const int i = 2 * I - 1 + di, j = 2 * J - 1 + dj;
+            if (i > F.nx || j > F.ny) continue;
+            const int k = F.id(i, j);
+            if (k == pin) continue;
+            s += ld<S>(F.b + k) - apply<S>(F, x, k);
+          }
+        const int kc = Cc.id(I, J);
+        Cc.b[kc] = s;
+        if (first_next) Cc.xb[kc] = s * Cc.wd[kc];
+      });
+    } else {
+      // fx x fy aggregates, the same sums in the same order
+      const int fx = H.lv[l + 1].fx, fy = H.lv[l + 1].fy;
+      cells<S>(Cc.nx, Cc.ny, [&](int I, int J) {
+        T s = T(0);
+        for (int dj = 0; dj < fy; ++dj)
+          for (int di = 0; di < fx; ++di) {
+            const int i = fx * (I - 1) + 1 + di, j = fy * (J - 1) + 1 + dj;
+            if (i > F.nx || j > F.ny) continue;
+            const int k = F.id(i, j);
+            if (k == pin) continue;
+            s += ld<S>(F.b + k) - apply<S>(F, x, k);
+          }
+        const int kc = Cc.id(I, J);
+        Cc.b[kc] = s;
+        if (first_next) Cc.xb[kc] = s * Cc.wd[kc];
+      });
+    }
   }
   // x_l (buffer cl) += cw * x_{l+1} (buffer cc) at the parent cell
   template <bool S>
@@ -1616,11 +1635,22 @@ struct MgInnerT {
     const T* xc = cc ? Cc.xb : Cc.xa;
     const T cw = H.cw;
     const int pin = l == 0 ? pk : -1;
-    cells<S>(F.nx, F.ny, [&](int i, int j) {
-      const int k = F.id(i, j);
-      if (k == pin) return;
-      x[k] = ld<S>(x + k) + cw * ld<S>(xc + Cc.id((i - 1) / Cc.fx + 1, (j - 1) / Cc.fy + 1));
-    });
+    if constexpr (!kSemi) {
+      cells<S>(F.nx, F.ny, [&](int i, int j) {
+        const int k = F.id(i, j);
+        if (k == pin) return;
+        x[k] = ld<S>(x + k) + cw * ld<S>(xc + Cc.id((i + 1) / 2, (j + 1) / 2));
+      });
+    } else {
+      const int fx = H.lv[l + 1].fx, fy = H.lv[l + 1].fy;
+      cells<S>(F.nx, F.ny, [&](int i, int j) {
+        const int k = F.id(i, j);
+        if (k == pin) return;
+        // the parent cell: (i + 1) / 2 across a halved direction, i across a kept one
+        const int I = fx == 2 ? (i + 1) >> 1 : i, J = fy == 2 ? (j + 1) >> 1 : j;
+        x[k] = ld<S>(x + k) + cw * ld<S>(xc + Cc.id(I, J));
+      });
+    }
   }
   // parity of the buffer holding level l's correction after its last sweep
   __device__ __forceinline__ int out_buf(int l) const { return l == H.nl - 1 ? (H.nuc & 1) : 0; }
@@ -1648,9 +1678,9 @@ struct MgInnerT {
       auto ayf = [&](int i, int j) -> T { return (i <= F.nx && j <= F.ny + 1) ? F.ay[F.id(i, j)] : T(0); };
       auto dgf = [&](int i, int j) -> T { return (i <= F.nx && j <= F.ny) ? F.dg[F.id(i, j)] : T(0); };
       // aggregates of fx x fy fine cells: 2 x 2, or 2 x 1 / 1 x 2 on
-      // anisotropic cells (semi-coarsening)
-      const int fx = Cc.fx, fy = Cc.fy;
-      cells<false>(Cc.nx + 1, Cc.ny + 1, [&](int I, int J) {
+      // anisotropic cells (semi-coarsening); compile-time factors
+      auto gal = [&](int I, int J, auto FX, auto FY) {
+        constexpr int fx = decltype(FX)::value, fy = decltype(FY)::value;
         const int k = Cc.id(I, J);
         const int i0 = fx * (I - 1) + 1, j0 = fy * (J - 1) + 1;
         if (J <= Cc.ny) cax[k] = fy == 2 ? axf(i0, j0) + axf(i0, j0 + 1) : axf(i0, j0);
@@ -1687,7 +1717,16 @@ struct MgInnerT {
           cdg[k] = dc;
           const_cast<T*>(Cc.wd)[k] = dc != T(0) ? T(H.omega) / dc : T(0);
         }
-      });
+      };
+      using two = std::integral_constant<int, 2>;
+      using one = std::integral_constant<int, 1>;
+      const int cfx = H.lv[l].fx, cfy = H.lv[l].fy;
+      if (!kSemi || (cfx == 2 && cfy == 2)) {
+        cells<false>(Cc.nx + 1, Cc.ny + 1, [&](int I, int J) { gal(I, J, two(), two()); });
+      } else if constexpr (kSemi) {
+        if (cfx == 2) cells<false>(Cc.nx + 1, Cc.ny + 1, [&](int I, int J) { gal(I, J, two(), one()); });
+        else cells<false>(Cc.nx + 1, Cc.ny + 1, [&](int I, int J) { gal(I, J, one(), two()); });
+      }
       if (!R.gs.sync()) return false;
     }
     if (tm.rank == 0 && H.tail < H.nl) {
@@ -2063,7 +2102,7 @@ struct MgInnerT {
 // copy of A; T = double: the same flexible CG and V-cycle with every level in
 // FP64, level 0 being A itself and its vectors the plain PCG's d, d2, Ad
 // (unused by the flexible CG).
-template <typename T>
+template <typename T, bool kSemi = false>
 __device__ void mg_case(const PoissonArgs& a, const Team& tm, GridReducer& R, T* tail, MgLvT<T>* tab) {
   const Dims D = a.D;
   // a launch without room for the tail is refused, not run (every block of
@@ -2078,7 +2117,7 @@ __device__ void mg_case(const PoissonArgs& a, const Team& tm, GridReducer& R, T*
   }
   const Tiles tl = make_tiles(D, blockDim.x);
   TileOwn own{D, tl, tm};
-  MgInnerT<T> in;
+  MgInnerT<T, kSemi> in;
   in.tm = tm;
   in.pk = a.pinned ? D.P + 1 : -1;
   in.H = a.mg;
@@ -2118,6 +2157,24 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_fp64_mg(PoissonArgs a) {
   const Team tm = grid_team();
   GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
   mg_case<double>(a, tm, R, reinterpret_cast<double*>(mg_dyn), mg_tab);
+}
+
+// The same two kernels for hierarchies with semi-coarsened levels
+// (anisotropic cells).
+__global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg_semi(PoissonArgs a) {
+  __shared__ MgLvT<float> mg_tab[2 * kMgMaxLevels];
+  if (a.redo && *a.redo == 0) return;
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  mg_case<float, true>(a, tm, R, reinterpret_cast<float*>(mg_dyn), mg_tab);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_pcg_fp64_mg_semi(PoissonArgs a) {
+  __shared__ MgLvT<double> mg_tab[2 * kMgMaxLevels];
+  if (a.redo && *a.redo == 0) return;
+  const Team tm = grid_team();
+  GridReducer R{a.part, GridSync{a.bar, a.err, (unsigned)tm.size, 0u}, 0, tm.rank};
+  mg_case<double, true>(a, tm, R, reinterpret_cast<double*>(mg_dyn), mg_tab);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_stream(PoissonArgs a) {
@@ -2234,14 +2291,14 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_smem_batch(const PoissonA
 
 // Multigrid inner form: each case's hierarchy is its own; the launch's
 // dynamic shared memory holds the largest tail of the batch.
-template <typename T>
+template <typename T, bool kSemi = false>
 __device__ __forceinline__ void mg_batch(const PoissonArgs* __restrict__ cases, const BatchTeams& bt, T* tail,
                                          MgLvT<T>* tab) {
   int4 T4;
   const Team tm = batch_team(bt, T4);
   const int t = bt.block_team[blockIdx.x];
   GridReducer R{bt.part + (size_t)16 * T4.x, GridSync{bt.bar + 32 * t, bt.err + t, (unsigned)T4.y, 0u}, 0, tm.rank};
-  for (int q = T4.z; q < T4.w; ++q) mg_case<T>(cases[bt.case_list[q]], tm, R, tail, tab);
+  for (int q = T4.z; q < T4.w; ++q) mg_case<T, kSemi>(cases[bt.case_list[q]], tm, R, tail, tab);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg_batch(const PoissonArgs* __restrict__ cases,
@@ -2254,6 +2311,19 @@ __global__ void __launch_bounds__(1024, 1) k_pcg_fp64_mg_batch(const PoissonArgs
                                                                BatchTeams bt) {
   __shared__ MgLvT<double> mg_tab[2 * kMgMaxLevels];
   mg_batch<double>(cases, bt, reinterpret_cast<double*>(mg_dyn), mg_tab);
+}
+
+// batches with an anisotropic case
+__global__ void __launch_bounds__(1024, 1) k_pcg_mixed_mg_batch_semi(const PoissonArgs* __restrict__ cases,
+                                                                     BatchTeams bt) {
+  __shared__ MgLvT<float> mg_tab[2 * kMgMaxLevels];
+  mg_batch<float, true>(cases, bt, reinterpret_cast<float*>(mg_dyn), mg_tab);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_pcg_fp64_mg_batch_semi(const PoissonArgs* __restrict__ cases,
+                                                                    BatchTeams bt) {
+  __shared__ MgLvT<double> mg_tab[2 * kMgMaxLevels];
+  mg_batch<double, true>(cases, bt, reinterpret_cast<double*>(mg_dyn), mg_tab);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_pcg_mixed_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt) {

@@ -39,6 +39,7 @@ struct MgHier {
   float cw;    // coarse-correction weight
   int nu, nuc; // sweeps before / after each coarse correction; sweeps on the coarsest level
   int gamma;   // coarse corrections per tail level (1: V-cycle, 2: W-cycle)
+  int semi;    // some level is semi-coarsened (2 x 1 or 1 x 2 aggregates)
   int tail_smem;     // bytes of block 0's shared memory holding the tail levels
   // exact != 0: the coarsest level (at most 64 cells, in the tail) is solved
   // by a dense inverse formed once per solve, 64 x 64 elements at element
@@ -124,9 +125,13 @@ __global__ void k_pcg_mixed_stream(PoissonArgs a);
 __global__ void k_pcg_mixed_cluster(PoissonArgs a);
 __global__ void k_pcg_mixed_mg(PoissonArgs a);
 __global__ void k_pcg_fp64_mg(PoissonArgs a);
+__global__ void k_pcg_mixed_mg_semi(PoissonArgs a);
+__global__ void k_pcg_fp64_mg_semi(PoissonArgs a);
 __global__ void k_pcg_fp64_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_mg_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_fp64_mg_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
+__global__ void k_pcg_mixed_mg_batch_semi(const PoissonArgs* __restrict__ cases, BatchTeams bt);
+__global__ void k_pcg_fp64_mg_batch_semi(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 __global__ void k_pcg_mixed_smem_batch(const PoissonArgs* __restrict__ cases, BatchTeams bt);
 // Shared-memory bytes of k_pcg_mixed_cheb for a strip of R rows of nx cells.
