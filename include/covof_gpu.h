@@ -521,7 +521,8 @@ int covof_history_write_async(covof_handle* h, const char* dir, const char* case
  * choice to the built-in rules; the autotuner (autotune.py) times candidates
  * and sets the fastest.  No reference counterpart. */
 typedef struct covof_launch {
-  int p_threads;     /* plain FP64 PCG: threads per block, 128, 256, 512 or 1024 */
+  int p_threads;     /* threads per block, 128, 256, 512 or 1024, of the plain FP64 PCG and of
+                      * the multigrid solve (0: the built-in choice by mesh size) */
   int p_blocks;      /* blocks of the persistent solve (mixed: row strips), at most one per SM */
   int p_inner_form;  /* mixed Chebyshev inner state: 1 shared-memory strips on every SM,
                       * 2 streamed through L2 / HBM, 3 one thread-block cluster of p_blocks
