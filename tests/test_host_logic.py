@@ -28,3 +28,21 @@ def test_vortex_velocity_is_discretely_solenoidal(pkg):
     u, v = pkg.cases.vortex_velocity(p, 0.3, dt, T)
     div = (u[1:-1, 2:] - u[1:-1, 1:-1]) / p.dx + (v[2:, 1:-1] - v[1:-1, 1:-1]) / p.dy
     assert np.abs(div).max() < 1e-12
+
+
+def test_droplet_array_interface_band(pkg):
+    """The reconstruction benchmark's droplet array: fractions in [0, 1],
+    seeded, and about 2 pi r k^2 x (band factor) interface cells (every
+    droplet's boundary crosses about 2 pi r cells, each crossing cell mixed)."""
+    import math
+    p, C = pkg.cases.droplet_array(512, 8, 20.0)
+    p2, C2 = pkg.cases.droplet_array(512, 8, 20.0)
+    assert np.array_equal(C, C2)
+    assert C.shape == (514, 514) and C.min() >= 0.0 and C.max() <= 1.0
+    inner = C[1:-1, 1:-1]
+    mixed = int(((inner > 0.0) & (inner < 1.0)).sum())
+    ring = 2.0 * math.pi * 20.0 * 8 * 8
+    assert 0.8 * ring < mixed < 1.6 * ring, (mixed, ring)
+    # gas inside the droplets: about k^2 pi r^2 cells of C = 0
+    gas = float((1.0 - inner).sum())
+    assert abs(gas - 64 * math.pi * 400.0) < 0.02 * 64 * math.pi * 400.0
